@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 unstructured finite-volume hot path.
+
+Workload (default, config C2): laminar Navier-Stokes around a cylinder on a
+~130k-cell mixed quad/triangle mesh (48 quad layers + seeded Delaunay fill to
+30 D), Re 40, Mach 0.2, Venkatakrishnan-limited second-order HLLC, implicit
+LU-SGS at CFL 50.  One step = one LU-SGS iteration (residual, local dt,
+diagonal, forward + backward level-scheduled sweeps, update) over the mesh.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--precision fp64|fp32]
+
+Prints ONE JSON line on rank 0.  value = cell-iterations per second of the
+whole job with the state resident in HBM (CUDA events on the solver's stream,
+L2 flushed between timed steps); e2e = the same metric through the C ABI with
+the step's input field copied from pinned host memory and its residual norm
+read back inside the timed region.  Multi-GPU runs are independent replicas
+(the reference's spatial decomposition is not needed on one GB300), so the
+scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-iters/s and time-to-1e-8 residual drop: FP32+learned vs FP64 plain"
+UNIT = "cell-iters/s"
+FLUSH_BYTES = 256 << 20  # > 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"], r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peak_gbs() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def alg_bytes(pass_name: str, nc: int, nf: int, viscous: bool, fp32: bool) -> int:
+    """Compulsory bytes of one launch: each array the kernel touches, once."""
+    s = 4 if fp32 else 8
+    v = 1 if viscous else 0
+    if pass_name == "face_state":
+        return nf * (8 + 4 * s + 4 * s + 2 * s + v * s) + nc * 4 * s
+    if pass_name == "cell_grad":
+        return nc * (16 + 4 * s + 4 * s + 8 * s + 4 * s + s + v * 4 * s) + nf * (8 + 4 * s + 4 * s + 4 * s + 2 * s)
+    if pass_name == "face_flux":
+        return nf * (8 + 4 * s + 4 * s + 4 * s + 4 * s + v * (4 * s + s + 4 * s)) + nc * (4 * s + 8 * s + 4 * s + v * 2 * s)
+    if pass_name == "cell_update":
+        return nc * (16 + 32 + s + v * s + 32 + 8 + 8) + nf * (4 * s + v * 4 * s)
+    if pass_name in ("sweep_fwd", "sweep_bwd"):
+        return nc * (4 + 16 + 32 + 8 + v * s + 32 + 32 + 32 + 32) + nf * (8 + 32 + v * 32)
+    if pass_name == "lusgs_update":
+        return nc * (32 + 64 + 32 + (16 if fp32 else 0))
+    raise KeyError(pass_name)
+
+
+def traffic_table() -> dict:
+    p = ROOT / "profiles" / "traffic.json"
+    try:
+        return json.loads(p.read_text())
+    except Exception:
+        return {}
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(grd_path: str, w, seconds: float) -> dict:
+    """C restatement of the reference's serial LU-SGS path on one host core."""
+    import oracle
+    from oracle import grd
+
+    t = grd.read_grd(grd_path, w.mesh.wall_tag, w.mesh.far_tag)
+    o = oracle.Oracle(t, w.mach, w.aoa, w.re, w.flow == "laminar")
+    o.lusgs_step(w.cfl) if w.advance == "lusgs" else o.rk_step()  # warm-up step
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        o.lusgs_step(w.cfl) if w.advance == "lusgs" else o.rk_step()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 2000:
+            break
+    return {"value": t.ncell * n / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} {w.advance} steps of the same {t.ncell}-cell workload, oracle/cfd_oracle.c -O2, "
+                      f"{el:.1f} s on 1 host core"}
+
+
+def _ref_worker(args):
+    grd_path, cfg_name, steps, warmup = args
+    sys.path.insert(0, str(ROOT))
+    from tmp_gb300 import configs
+    import oracle
+    from oracle import grd
+
+    w = configs.WORKLOADS[cfg_name]()
+    t = grd.read_grd(grd_path, w.mesh.wall_tag, w.mesh.far_tag)
+    o = oracle.Oracle(t, w.mach, w.aoa, w.re, w.flow == "laminar")
+    step = (lambda: o.lusgs_step(w.cfl)) if w.advance == "lusgs" else (lambda: o.rk_step())
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    return t.ncell * steps, time.perf_counter() - t0
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU algorithm (C restatement, bit-exact to
+    the reference's compiled serial path) on all host cores as independent
+    copies of the workload (the reference has no threading)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    import oracle
+    from tmp_gb300 import configs
+
+    oracle.build()
+    w = configs.WORKLOADS[args.config]()
+    path = str(configs.grd_path(w))
+    ncores = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 10))
+    warm = min(args.warmup, 1)
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(ncores) as pool:
+        res = pool.map(_ref_worker, [(path, args.config, steps, warm)] * ncores)
+    wall = time.perf_counter() - t0
+    cells = sum(r[0] for r in res)
+    slowest = max(r[1] for r in res)
+    value = cells / slowest
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": steps, "warmup": warm, "ms_per_step": 1e3 * slowest / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "ncell": w.mesh.ncell, "nedge": w.mesh.nedge, "mach": w.mach,
+                       "re": w.re, "cfl": w.cfl, "copies": ncores},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
+                             "sample": f"{ncores} independent copies x {steps} {w.advance} steps of the "
+                                       f"{w.mesh.ncell}-cell workload (oracle/cfd_oracle.c, bit-exact restatement "
+                                       f"of the reference's serial path), {wall:.1f} s wall"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from tmp_gb300 import abi, configs
+    from tmp_gb300.build import build_library
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    build_library()
+    w = configs.WORKLOADS[args.config]()
+    path = configs.grd_path(w)
+    mesh = abi.Mesh.load_grd(path, w.mesh.wall_tag, w.mesh.far_tag)
+    fp32 = args.precision == "fp32"
+    viscous = w.flow == "laminar"
+    stream = torch.cuda.current_stream()
+    case = abi.Case([mesh], [dict(mach=w.mach, aoa_deg=w.aoa, reynolds=w.re)],
+                    abi.FLOW_LAMINAR if viscous else abi.FLOW_EULER,
+                    abi.ADV_LUSGS if w.advance == "lusgs" else abi.ADV_RK5,
+                    abi.PREC_FP32 if fp32 else abi.PREC_FP64, cfl=w.cfl, stream=stream.cuda_stream)
+    case.init_freestream()
+    nc, nf = case.ncell, case.nedge
+    U0 = case.get("U").copy()
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    # warm-up (also builds the CUDA graph of one step)
+    case.step_graph(max(args.warmup, 3))
+    torch.cuda.synchronize()
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = case.launches()
+    for k in range(args.steps):
+        flush.zero_()  # evict L2 (129 MB) between timed steps, outside the events
+        evs[k][0].record(stream)
+        case.step_graph(1)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    launches = case.launches() - l0
+    ms = [a.elapsed_time(b) for a, b in evs]
+    t_local = sum(ms) / 1e3
+    t = torch.tensor([t_local], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    t_max = float(t.item())
+    value = nc * args.steps * world / t_max
+    case.sync()
+
+    # end to end through the C ABI: pinned host field in, norm out, per step
+    e2e = None
+    if not args.no_e2e:
+        host = torch.from_numpy(U0.reshape(-1)).pin_memory()
+        hv = host.numpy()
+        case.put("U", hv)
+        case.step_graph(1)
+        case.norm("DW_RHO2")
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            case.put("U", hv)
+            case.step_graph(1)
+            case.norm("DW_RHO2")  # device->host read of the step's residual norm (synchronises)
+        el = time.perf_counter() - t0
+        te = torch.tensor([el], dtype=torch.float64, device="cuda")
+        if dist:
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e = {"value": nc * args.steps * world / float(te.item()), "unit": UNIT,
+               "h2d_bytes_per_step": nc * 32, "d2h_bytes_per_step": 8}
+
+    # per-pass device times for the roofline (L2 flushed before each rep)
+    passes = ["face_state", "cell_grad", "face_flux", "cell_update"]
+    if w.advance == "lusgs":
+        passes += ["sweep_fwd", "sweep_bwd", "lusgs_update"]
+    per = {p: case.bench_pass(p, 5, FLUSH_BYTES) for p in passes}
+    per_step = dict(per)
+    if w.advance == "rk5":
+        per_step = {p: 5 * v for p, v in per.items()}
+    dominant = max(per_step, key=per_step.get)
+    nlev = mesh.levels()
+    launches_of = {"sweep_fwd": nlev[0], "sweep_bwd": nlev[1]}
+    peak, peak_kind = measured_peak_gbs()
+    rows = {}
+    for p, v in per.items():
+        b = alg_bytes(p, nc, nf, viscous, fp32)
+        rows[p] = {"ms": round(v, 5), "alg_bytes": b, "gbs": round(b / (v * 1e-3) / 1e9, 1),
+                   "launches": launches_of.get(p, 1)}
+    db = alg_bytes(dominant, nc, nf, viscous, fp32)
+    achieved = db / (per[dominant] * 1e-3) / 1e9
+    tr = traffic_table().get(f"{args.config}_{args.precision}_{dominant}")
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": tr, "alg_bytes_per_launch": db, "per_pass": rows}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if fp32 else "f64", "data": "synthetic",
+            "config": {"workload": w.name, "ncell": nc, "nedge": nf, "levels": list(nlev), "mach": w.mach,
+                       "re": w.re, "cfl": w.cfl, "precision": args.precision,
+                       "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
+            "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(str(path), w, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

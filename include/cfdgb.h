@@ -1,0 +1,174 @@
+/*
+ * cfdgb.h - C ABI of the GB300 (sm_103a) unstructured finite-volume hot path.
+ *
+ * The library replaces the per-iteration path of the reference solver
+ * (SenhuWong/tmp, src/UnstructSolver + the per-iteration part of src/UniTioga):
+ * residual evaluation, local time step, 5-stage Runge-Kutta and LU-SGS
+ * stepping, residual norms, and the overset fringe data update.  Every
+ * function returns an int status (CFD_OK == 0, negative on error) and leaves
+ * a message for cfd_last_error().  All device memory belongs to the handles.
+ * Calls on one case handle are issued on that case's stream and are not
+ * thread-safe for the same handle; different handles may be used from
+ * different threads.  No signature uses a framework type.
+ */
+#ifndef CFDGB_H
+#define CFDGB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define CFD_OK               0
+#define CFD_ERR_ARG         -1  /* bad argument (null pointer, size, enum)         */
+#define CFD_ERR_IO          -2  /* mesh file missing or unreadable                  */
+#define CFD_ERR_MESH        -3  /* topology the solver cannot use (bad BC tag ...)  */
+#define CFD_ERR_CUDA        -4  /* CUDA runtime failure; message has the CUDA text  */
+#define CFD_ERR_PSTAR       -5  /* HLLC |p*_L - p*_R| >= 1e-10 on some face         */
+#define CFD_ERR_NONPHYSICAL -6  /* NaN or non-positive density/pressure             */
+#define CFD_ERR_TIMEOUT     -7  /* a bounded device wait gave up                    */
+#define CFD_ERR_STATE       -8  /* call not valid in the handle's current state     */
+#define CFD_ERR_WALLTAN     -9  /* slip-wall tangential velocity check failed       */
+
+/* ---- boundary codes (the reference's edge3d<2>::BoundaryType) ------------ */
+#define CFD_BC_WALL     -2
+#define CFD_BC_FARFIELD -3
+
+/* ---- enums --------------------------------------------------------------- */
+#define CFD_FLOW_EULER    0   /* Euler2D                                   */
+#define CFD_FLOW_LAMINAR  1   /* ViscousFlow2D (laminar branch)            */
+#define CFD_ADV_RK5       0   /* RungeKuttaStrategy(5)                     */
+#define CFD_ADV_LUSGS     1   /* LUSGSIntegrator                           */
+#define CFD_PREC_FP64     0   /* plain: every kernel in binary64           */
+#define CFD_PREC_FP32     1   /* face states/gradients/limiter/fluxes in
+                                 binary32; residual sums, update, norms,
+                                 LU-SGS diagonal and sweeps in binary64    */
+
+/* Field selectors for cfd_get_field / cfd_put_field.  Cell fields use the
+ * reference's interleaved layout [NEQU*cell + eq]; face fields [4*face + eq]. */
+#define CFD_FIELD_U        0  /* primitive [rho, p, u, v], 4/cell (getU)            */
+#define CFD_FIELD_W        1  /* conservative [rho, rhoE, rhou, rhov], 4/cell       */
+#define CFD_FIELD_R        2  /* residual, 4/cell (getResidual)                     */
+#define CFD_FIELD_GRAD     3  /* Green-Gauss gradient of U, 8/cell [eq][x,y]        */
+#define CFD_FIELD_PHI      4  /* Venkatakrishnan limiter, 4/cell                    */
+#define CFD_FIELD_SPEC_C   5  /* convective spectral radius, 1/cell                 */
+#define CFD_FIELD_SPEC_V   6  /* viscous spectral radius, 1/cell                    */
+#define CFD_FIELD_DT       7  /* local time step, 1/cell (getStableTime)           */
+#define CFD_FIELD_DIAG     8  /* LU-SGS scalar diagonal, 1/cell                     */
+#define CFD_FIELD_DW1      9  /* LU-SGS forward-sweep increment, 4/cell             */
+#define CFD_FIELD_DW      10  /* LU-SGS backward-sweep increment, 4/cell            */
+#define CFD_FIELD_GRADT   11  /* gradient of T = p/rho, 2/cell                      */
+#define CFD_FIELD_MU      12  /* laminar viscosity per cell, 1/cell                 */
+#define CFD_FIELD_UEDGE   13  /* face state, 4/face (getUEdge)                      */
+#define CFD_FIELD_MUEDGE  14  /* laminar viscosity per face, 1/face                 */
+#define CFD_FIELD_VOL     15  /* cell area, 1/cell (read only)                      */
+#define CFD_FIELD_CENTER  16  /* cell centre, 2/cell (read only)                    */
+#define CFD_FIELD_NORMAL  17  /* unit face normal, 2/face (read only)               */
+#define CFD_FIELD_AREA    18  /* face length, 1/face (read only)                    */
+#define CFD_FIELD_ECENTER 19  /* face centre, 2/face (read only)                    */
+#define CFD_FIELD_WALLDIST 20 /* projected wall distance, 1/cell (read only)        */
+
+/* Residual-norm selectors for cfd_residual_norm. */
+#define CFD_NORM_DW_RHO2   0  /* sum dW_rho^2 (LUSGSIntegrator::postprocessUpdate) */
+#define CFD_NORM_RK_DRHO   1  /* sum |rho - rho0| (RungeKuttaStrategy::converged)  */
+#define CFD_NORM_L2_R_RHO  2  /* sqrt(sum R_rho^2 / ncell)                         */
+
+typedef struct cfd_mesh_s* cfd_mesh_t;
+typedef struct cfd_case_s* cfd_case_t;
+
+/* Per-mesh physical parameters; the first four mirror WrapSolver::setParams
+ * (UnstructSolver/SolverWrapper.h:27-56), which calls
+ * set_fs_variable2(Ma, AoA, 1.225, 101325, Re). */
+typedef struct {
+    double mach;
+    double aoa_deg;
+    double reynolds;
+    double density;   /* dimensional freestream density  (reference: 1.225)  */
+    double pressure;  /* dimensional freestream pressure (reference: 101325) */
+} cfd_freestream_t;
+
+typedef struct {
+    int flow;          /* CFD_FLOW_*                                              */
+    int advance;       /* CFD_ADV_*                                               */
+    int precision;     /* CFD_PREC_*                                              */
+    int first_order;   /* 1: limiter forced to 0 (piecewise-constant faces)       */
+    double cfl;        /* LU-SGS CFL (LUSGSIntegrator::d_CFL_number); RK uses 0.8 */
+    int sweep_mode;    /* 0: auto, 1: one launch per level, 2: persistent cluster */
+    int reserved[7];
+} cfd_params_t;
+
+/* ---- errors -------------------------------------------------------------- */
+/* Last error message of the calling thread ("" when none). */
+const char* cfd_last_error(void);
+/* ABI version: major*10000 + minor*100 + patch. */
+int cfd_version(void);
+
+/* ---- meshes (UnstructReader / UnstructTopologyHolder) -------------------- */
+/* Read a 2D .grd file (UnstructReader::readForUnstruct, reader/UnstructReader.h:124-272).
+ * wall_tag / far_tag are the file's negative right-cell codes that map to the
+ * wall and far-field boundary types (UnstructReader::setWallSign/setOverSign). */
+int cfd_mesh_load_grd(const char* path, int wall_tag, int far_tag, cfd_mesh_t* out);
+/* Same mesh from arrays in .grd order: xy[2*nnode]; edge_nodes[2*nedge] (1-based
+ * node ids); edge_cells[2*nedge] (1-based left/right cell ids, right may be a tag). */
+int cfd_mesh_from_arrays(int nnode, const double* xy, int nedge, const int* edge_nodes,
+                         const int* edge_cells, int ncell, int wall_tag, int far_tag,
+                         cfd_mesh_t* out);
+int cfd_mesh_info(cfd_mesh_t mesh, int* nnode, int* nedge, int* ncell);
+/* Topology as the reference builds it: lr[2*nedge] (0-based, or CFD_BC_*),
+ * cell_edges[4*ncell] and cell_verts[4*ncell] (0-based, -1 padded; cell3d
+ * edgeInd / pointInd order), cell_sizes[2*ncell] = {nverts, nedges}. Any
+ * output pointer may be NULL. */
+int cfd_mesh_topology(cfd_mesh_t mesh, int* lr, int* cell_edges, int* cell_verts, int* cell_sizes);
+/* LU-SGS level schedule of the reference's cell order: number of forward and
+ * backward levels (cells in one level have no dependency on each other). */
+int cfd_mesh_levels(cfd_mesh_t mesh, int* n_forward, int* n_backward);
+void cfd_mesh_free(cfd_mesh_t mesh);
+
+/* ---- cases (TopologyHolderStrategy + TimeIntegrator) --------------------- */
+/* One case = nmesh meshes packed into one set of device arrays (overset
+ * components or independent batched cases).  fs[nmesh] gives each mesh's
+ * freestream.  stream: a cudaStream_t to issue on, or NULL for the library's
+ * own non-blocking stream. */
+int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t* fs,
+                    const cfd_params_t* params, void* stream, cfd_case_t* out);
+void cfd_case_free(cfd_case_t c);
+int cfd_case_info(cfd_case_t c, int* nmesh, int* ncell_total, int* nedge_total);
+/* cudaStream_t the case issues on. */
+int cfd_case_stream(cfd_case_t c, void** stream);
+int cfd_set_cfl(cfd_case_t c, double cfl);
+/* Uniform freestream initial state (Euler2D/ViscousFlow2D::initializeData and
+ * the integrator's initializeData). */
+int cfd_init_freestream(cfd_case_t c);
+/* One residual evaluation from the current U (preprocessAdvanceSerial):
+ * face states, gradients, limiter, spectral radii, HLLC (+ laminar) fluxes. */
+int cfd_residual(cfd_case_t c, int stage);
+/* dt = CFL*vol/spec_c (SolveTime). */
+int cfd_local_dt(cfd_case_t c, double cfl);
+/* nsteps iterations of the case's integrator (singleStepSerial). */
+int cfd_step(cfd_case_t c, int nsteps);
+int cfd_rk_step(cfd_case_t c);
+int cfd_lusgs_step(cfd_case_t c);
+/* Capture one integrator step in a CUDA graph and replay it nsteps times. */
+int cfd_step_graph(cfd_case_t c, int nsteps);
+/* Norm of the last step for one mesh (synchronises; also reports device-side
+ * error flags as CFD_ERR_PSTAR / CFD_ERR_NONPHYSICAL / CFD_ERR_WALLTAN). */
+int cfd_residual_norm(cfd_case_t c, int mesh, int which, double* out);
+/* Copy a field of one mesh to / from host memory (layout above). */
+int cfd_get_field(cfd_case_t c, int mesh, int which, double* host);
+int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host);
+/* Wait for the case's stream and report any device-side error flag. */
+int cfd_sync(cfd_case_t c);
+/* Number of kernel launches the library issued on this case so far. */
+long long cfd_launch_count(cfd_case_t c);
+/* Measurement helper (no reference counterpart; the reference only has a
+ * scope timer, toolBox/Timer.h:5-20): run one pass reps times on the case's
+ * stream, each bracketed by CUDA events, writing flush_bytes to a scratch
+ * buffer before each rep to evict L2, and return the mean duration in ms.
+ * pass: 0 face_state, 1 cell_grad, 2 face_flux, 3 cell_update, 4 forward sweep
+ * (all levels), 5 backward sweep (all levels), 6 LU-SGS update, 7 whole step. */
+int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFDGB_H */

@@ -1,0 +1,108 @@
+"""Test oracle: a CPU restatement of the reference solver's per-iteration path.
+
+TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and bench.py's
+cpu_baseline leg may import this package, and only as the checker or as the
+reported CPU baseline; the product path (tmp_gb300) never uses it.
+
+Pinning: tests/test_oracle_golden.py checks the oracle against fixtures dumped
+by the reference's own compiled code (tests/golden/).
+
+  grd.read_grd      .grd reader + cell assembly restated in numpy/Python
+                    (reader/UnstructReader.h:124-272, UniTioga/CellBrick.cpp:13-136)
+  Oracle            ctypes wrapper of cfd_oracle.c (geometry, residual, RK5, LU-SGS)
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import grd  # noqa: F401
+from .build import LIB, build
+
+FIELD = dict(U=0, W=1, R=2, GRAD=3, PHI=4, SPEC_C=5, SPEC_V=6, DT=7, DIAG=8, DW1=9, DW=10, GRADT=11, MU=12,
+             UEDGE=13, MUEDGE=14, VOL=15, CENTER=16, NORMAL=17, AREA=18, ECENTER=19, WALLDIST=20, UL=21, UR=22,
+             WNOW=23)
+# values per element, per-face flag
+SHAPE = dict(U=(4, 0), W=(4, 0), R=(4, 0), GRAD=(8, 0), PHI=(4, 0), SPEC_C=(1, 0), SPEC_V=(1, 0), DT=(1, 0),
+             DIAG=(1, 0), DW1=(4, 0), DW=(4, 0), GRADT=(2, 0), MU=(1, 0), UEDGE=(4, 1), MUEDGE=(1, 1), VOL=(1, 0),
+             CENTER=(2, 0), NORMAL=(2, 1), AREA=(1, 1), ECENTER=(2, 1), WALLDIST=(1, 0), UL=(4, 1), UR=(4, 1),
+             WNOW=(4, 0))
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        ip, dp, vp = C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [C.c_int, dp, C.c_int, ip, ip, C.c_int, ip, ip, ip, ip]
+        L.orc_free.argtypes = [vp]
+        L.orc_geometry.argtypes = [vp]
+        L.orc_set_freestream.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+        L.orc_init_freestream.argtypes = [vp]
+        L.orc_cons_from_U.argtypes = [vp]
+        L.orc_residual.argtypes = [vp, C.c_int]
+        L.orc_residual.restype = C.c_int
+        L.orc_solve_time.argtypes = [vp, C.c_double]
+        L.orc_rk_step.argtypes = [vp, C.c_int]
+        L.orc_rk_step.restype = C.c_int
+        L.orc_lusgs_step.argtypes = [vp, C.c_double, C.c_int]
+        L.orc_lusgs_step.restype = C.c_int
+        L.orc_field.argtypes = [vp, C.c_int]
+        L.orc_field.restype = dp
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    """One mesh, one flow strategy; mirrors the reference's serial driver calls."""
+
+    def __init__(self, mesh: "grd.Topo", mach: float, aoa: float, re: float, viscous: bool,
+                 density: float = 1.225, pressure: float = 101325.0):
+        L = _load()
+        self.m = mesh
+        self._keep = [np.ascontiguousarray(a) for a in (mesh.xy, mesh.edge_nodes, mesh.lr, mesh.cell_verts,
+                                                         mesh.cell_nvert, mesh.cell_edges, mesh.cell_nedge)]
+        xy, en, lr, cv, cnv, ce, cne = self._keep
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+        self.h = L.orc_create(mesh.nnode, xy.ctypes.data_as(C.POINTER(C.c_double)), mesh.nedge, ip(en), ip(lr),
+                              mesh.ncell, ip(cv), ip(cnv), ip(ce), ip(cne))
+        L.orc_geometry(self.h)
+        L.orc_set_freestream(self.h, mach, aoa, re, density, pressure, int(viscous))
+        L.orc_init_freestream(self.h)
+        L.orc_cons_from_U(self.h)
+        self.viscous = viscous
+
+    def set_U(self, U: np.ndarray):
+        self.field("U")[:] = np.asarray(U, np.float64).reshape(self.field("U").shape)
+        _load().orc_cons_from_U(self.h)
+
+    def residual(self, first_order: bool = False) -> int:
+        return _load().orc_residual(self.h, int(first_order))
+
+    def solve_time(self, cfl: float):
+        _load().orc_solve_time(self.h, cfl)
+
+    def rk_step(self, first_order: bool = False) -> int:
+        return _load().orc_rk_step(self.h, int(first_order))
+
+    def lusgs_step(self, cfl: float, first_order: bool = False) -> int:
+        return _load().orc_lusgs_step(self.h, cfl, int(first_order))
+
+    def field(self, name: str) -> np.ndarray:
+        """A live numpy view of one oracle array."""
+        width, per_face = SHAPE[name]
+        n = (self.m.nedge if per_face else self.m.ncell) * width
+        p = _load().orc_field(self.h, FIELD[name])
+        a = np.ctypeslib.as_array(p, shape=(n,))
+        return a.reshape(-1, width) if width > 1 else a
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_free(self.h)
+            self.h = None

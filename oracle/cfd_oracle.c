@@ -1,0 +1,595 @@
+/*
+ * CPU restatement of the reference solver's per-iteration path, in plain C.
+ *
+ * TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline leg use this library as the checker and as the reported CPU
+ * baseline.  The product (tmp_gb300/libcfdgb.so) never links or calls it.
+ *
+ * Parity pin: tests/test_oracle_golden.py checks every array this oracle
+ * produces against fixtures dumped by the reference's own code
+ * (tests/golden/make_golden.py runs oracle/_ref/ref_driver, built from the
+ * reference sources by oracle/build_ref.sh).
+ *
+ * Each routine follows the cited reference function with the same operation
+ * order; compiled with -ffp-contract=off it reproduces the reference bit for
+ * bit on x86-64 and aarch64.  Arrays use the reference's interleaved layout
+ * [NEQU*cell + eq] with NEQU = 4, primitive [rho, p, u, v], conservative
+ * [rho, rhoE, rhou, rhov].
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define NEQU 4
+#define BC_WALL (-2)
+#define BC_FAR (-3)
+
+typedef struct {
+    int nnode, nedge, ncell;
+    const double* xy;   /* 2*nnode */
+    const int* en;      /* 2*nedge node ids (0-based, file order) */
+    const int* lr;      /* 2*nedge left, right|BC */
+    const int* cv;      /* 4*ncell vertex ids (-1 pad), cell3d order */
+    const int* cnv;     /* ncell */
+    const int* ce;      /* 4*ncell edge ids ascending (-1 pad) */
+    const int* cne;     /* ncell */
+    int viscous;
+    /* freestream (nondimensional) and Sutherland constants */
+    double rho_inf, p_inf, u_inf, v_inf, c_inf, mach, re, t_inf;
+    /* geometry */
+    double *vol, *cen, *nrm, *area, *ecen, *walld;
+    /* state and intermediates */
+    double *U, *Ue, *grad, *gradT, *specc, *specv, *R, *dt, *mu, *mue, *phi, *UL, *UR;
+    double *umax, *umin;
+    /* integrators */
+    double *W, *Wnow, *D, *dW1, *dW;
+} orc_t;
+
+static const double Gamma = 1.4;
+
+static double dot2(double a0, double a1, double b0, double b1) {
+    double r = 0;
+    r += a0 * b0;
+    r += a1 * b1;
+    return r;
+}
+static double dmax(double a, double b) { return (a < b) ? b : a; }
+static double dmin(double a, double b) { return (b < a) ? b : a; }
+
+orc_t* orc_create(int nnode, const double* xy, int nedge, const int* en, const int* lr, int ncell, const int* cv,
+                  const int* cnv, const int* ce, const int* cne) {
+    orc_t* o = (orc_t*)calloc(1, sizeof(orc_t));
+    o->nnode = nnode; o->nedge = nedge; o->ncell = ncell;
+    o->xy = xy; o->en = en; o->lr = lr; o->cv = cv; o->cnv = cnv; o->ce = ce; o->cne = cne;
+    size_t c = (size_t)ncell, e = (size_t)nedge;
+    o->vol = calloc(c, 8); o->cen = calloc(2 * c, 8); o->nrm = calloc(2 * e, 8); o->area = calloc(e, 8);
+    o->ecen = calloc(2 * e, 8); o->walld = calloc(c, 8);
+    o->U = calloc(4 * c, 8); o->Ue = calloc(4 * e, 8); o->grad = calloc(8 * c, 8); o->gradT = calloc(2 * c, 8);
+    o->specc = calloc(c, 8); o->specv = calloc(c, 8); o->R = calloc(4 * c, 8); o->dt = calloc(c, 8);
+    o->mu = calloc(c, 8); o->mue = calloc(e, 8); o->phi = calloc(4 * c, 8); o->UL = calloc(4 * e, 8);
+    o->UR = calloc(4 * e, 8); o->umax = calloc(4 * c, 8); o->umin = calloc(4 * c, 8);
+    o->W = calloc(4 * c, 8); o->Wnow = calloc(4 * c, 8); o->D = calloc(c, 8); o->dW1 = calloc(4 * c, 8);
+    o->dW = calloc(4 * c, 8);
+    return o;
+}
+
+void orc_free(orc_t* o) {
+    if (!o) return;
+    double* p[] = {o->vol, o->cen, o->nrm, o->area, o->ecen, o->walld, o->U, o->Ue, o->grad, o->gradT, o->specc,
+                   o->specv, o->R, o->dt, o->mu, o->mue, o->phi, o->UL, o->UR, o->umax, o->umin, o->W, o->Wnow,
+                   o->D, o->dW1, o->dW};
+    for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++) free(p[i]);
+    free(o);
+}
+
+/* triangle_area, mathTools/cellVolume.cpp:6-19 */
+static double tri_area(const double* p1, const double* p2, const double* p3) {
+    double a = 0.5 * ((p1[0] - p2[0]) * (p1[1] + p2[1]) + (p2[0] - p3[0]) * (p2[1] + p3[1]) +
+                      (p3[0] - p1[0]) * (p3[1] + p1[1]));
+    if (a < 0) a = -a;
+    return a;
+}
+
+/* edge3d::find_area/find_normal/find_center (toolBox/edge3d_int.h:93-230),
+ * computeCellVolume2D (mathTools/cellVolume.cpp:21-75), cell3d::find_center,
+ * UnstructBlock2D::ComputeWallCellDistance (UnstructBlock.h:265-298). */
+void orc_geometry(orc_t* o) {
+    for (int k = 0; k < o->nedge; k++) {
+        const double* p0 = o->xy + 2 * o->en[2 * k];
+        const double* p1 = o->xy + 2 * o->en[2 * k + 1];
+        double dx = p1[0] - p0[0], dy = p1[1] - p0[1];
+        double l2 = 0;
+        l2 += dx * dx;
+        l2 += dy * dy;
+        double A = sqrt(l2);
+        o->area[k] = A;
+        o->nrm[2 * k] = dy / A;
+        o->nrm[2 * k + 1] = -dx / A;
+        double cx = 0, cy = 0;
+        cx = cx + p0[0]; cy = cy + p0[1];
+        cx = cx + p1[0]; cy = cy + p1[1];
+        o->ecen[2 * k] = cx / 2.0;
+        o->ecen[2 * k + 1] = cy / 2.0;
+    }
+    for (int c = 0; c < o->ncell; c++) {
+        int n = o->cnv[c];
+        const double* p[4];
+        for (int i = 0; i < n; i++) p[i] = o->xy + 2 * o->cv[4 * c + i];
+        double area;
+        if (n == 3) {
+            area = tri_area(p[0], p[1], p[2]);
+        } else {
+            double abx = p[1][0] - p[0][0], aby = p[1][1] - p[0][1];
+            double acx = p[2][0] - p[0][0], acy = p[2][1] - p[0][1];
+            double adx = p[3][0] - p[0][0], ady = p[3][1] - p[0][1];
+            double abac = abx * acy - aby * acx, abad = abx * ady - aby * adx, acad = acx * ady - acy * adx;
+            area = 0;
+            if (abac * abad > 0) {
+                if (acad * abad > 0) { area += tri_area(p[0], p[2], p[1]); area += tri_area(p[0], p[2], p[3]); }
+                else { area += tri_area(p[0], p[3], p[1]); area += tri_area(p[0], p[3], p[2]); }
+            } else {
+                area += tri_area(p[0], p[1], p[2]);
+                area += tri_area(p[0], p[1], p[3]);
+            }
+        }
+        o->vol[c] = area;
+        double cx = 0, cy = 0;
+        for (int i = 0; i < n; i++) { cx = cx + p[i][0]; cy = cy + p[i][1]; }
+        o->cen[2 * c] = cx / (double)n;
+        o->cen[2 * c + 1] = cy / (double)n;
+    }
+    for (int c = 0; c < o->ncell; c++) {
+        double d = 100000000000.0;
+        for (int k = 0; k < o->nedge; k++) {
+            if (o->lr[2 * k + 1] != BC_WALL) continue;
+            double x = o->cen[2 * c] - o->ecen[2 * k], y = o->cen[2 * c + 1] - o->ecen[2 * k + 1];
+            d = dmin(d, fabs(dot2(x, y, o->nrm[2 * k], o->nrm[2 * k + 1])));
+        }
+        o->walld[c] = d;
+    }
+}
+
+/* TopologyHolderStrategy::set_fs_variable2 + update_nondim_variable
+ * (TopologyHolderStrategy.cpp:325-396). */
+void orc_set_freestream(orc_t* o, double Ma, double AOA, double Re, double density, double pressure, int viscous) {
+    const double R = 287.0, PI = 3.141593;
+    double aoa = PI * AOA / 180;
+    double c = sqrt(Gamma * pressure / density);
+    double T = pressure / (R * density);
+    double vm = c * Ma;
+    double u = vm * cos(aoa), v = vm * sin(aoa);
+    o->u_inf = u / (c / sqrt(Gamma));
+    o->v_inf = v / (c / sqrt(Gamma));
+    o->p_inf = pressure / pressure;
+    o->rho_inf = density / density;
+    o->c_inf = sqrt(Gamma);
+    o->mach = Ma;
+    o->re = Re;
+    o->t_inf = T;
+    o->viscous = viscous;
+}
+
+void orc_init_freestream(orc_t* o) {
+    for (int k = 0; k < o->ncell; k++) {
+        o->U[4 * k] = o->rho_inf; o->U[4 * k + 1] = o->p_inf;
+        o->U[4 * k + 2] = o->u_inf; o->U[4 * k + 3] = o->v_inf;
+    }
+}
+
+/* initializeConsData / initializePrimData / UpdatePrimitiveVariables
+ * (TopologyHolderStrategy.cpp:48-109) */
+static void cons_from_prim(const double* u, double* w) {
+    double vm = 0;
+    vm += u[2] * u[2]; w[2] = u[0] * u[2];
+    vm += u[3] * u[3]; w[3] = u[0] * u[3];
+    w[0] = u[0];
+    w[1] = u[1] / (Gamma - 1) + 0.5 * u[0] * vm;
+}
+static void prim_from_cons(const double* w, double* u) {
+    double vm = 0;
+    u[0] = w[0];
+    u[2] = w[2] / u[0]; vm += u[2] * u[2];
+    u[3] = w[3] / u[0]; vm += u[3] * u[3];
+    u[1] = (Gamma - 1) * (w[1] - 0.5 * u[0] * vm);
+}
+
+void orc_cons_from_U(orc_t* o) {
+    for (int k = 0; k < o->ncell; k++) cons_from_prim(o->U + 4 * k, o->W + 4 * k);
+}
+
+static double sutherland(const orc_t* o, double T) {
+    double cc = 110.5 / o->t_inf;
+    return (1.0 + cc) / (T + cc) * pow(T, 1.5) * sqrt(Gamma) * o->mach / o->re;
+}
+
+/* BoundaryStrategy::HandleInvicidBoundary / HandleViscousBoundary
+ * (BoundaryStrategy.h:73-335).  Returns 1 when the slip-wall check fails. */
+static int face_states(orc_t* o) {
+    int bad = 0;
+    for (int k = 0; k < o->nedge; k++) {
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        double* ue = o->Ue + 4 * k;
+        const double* ul = o->U + 4 * l;
+        double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1];
+        if (r >= 0) {
+            for (int j = 0; j < 4; j++) ue[j] = (ul[j] + o->U[4 * r + j]) / 2;
+        } else if (r == BC_WALL) {
+            if (o->viscous) {
+                ue[0] = ul[0]; ue[1] = ul[1]; ue[2] = 0; ue[3] = 0;
+            } else {
+                double vn = dot2(ul[2], ul[3], nx, ny);
+                double t0 = ul[2] - nx * vn, t1 = ul[3] - ny * vn;
+                if (dot2(t0, t1, nx, ny) > 1.0e-7) bad = 1;
+                ue[0] = ul[0]; ue[1] = ul[1]; ue[2] = t0; ue[3] = t1;
+            }
+        } else {
+            double vnl = dot2(ul[2], ul[3], nx, ny);
+            double tl0 = ul[2] - nx * vnl, tl1 = ul[3] - ny * vnl;
+            double vnr = dot2(o->u_inf, o->v_inf, nx, ny);
+            double tr0 = o->u_inf - nx * vnr, tr1 = o->v_inf - ny * vnr;
+            double rl = ul[0], pl = ul[1];
+            if (fabs(vnr) < o->c_inf) {
+                double cl = sqrt(Gamma * pl / rl);
+                double vnb = (vnl + vnr + 2 * (cl - o->c_inf) / (Gamma - 1)) / 2;
+                double cb = (vnl - vnr + 2 * (o->c_inf + cl) / (Gamma - 1)) * (Gamma - 1) / 4;
+                double sb, e0, e1;
+                if (vnr >= 0) { sb = (pl / pow(rl, Gamma)); e0 = tl0 + nx * vnb; e1 = tl1 + ny * vnb; }
+                else { sb = (o->p_inf / pow(o->rho_inf, Gamma)); e0 = tr0 + nx * vnb; e1 = tr1 + ny * vnb; }
+                ue[0] = pow((cb * cb / (Gamma * sb)), (1.0 / (Gamma - 1)));
+                ue[1] = ue[0] * cb * cb / Gamma;
+                ue[2] = e0; ue[3] = e1;
+            } else if (vnr >= 0) {
+                for (int j = 0; j < 4; j++) ue[j] = ul[j];
+            } else {
+                ue[0] = o->rho_inf; ue[1] = o->p_inf; ue[2] = o->u_inf; ue[3] = o->v_inf;
+            }
+        }
+    }
+    return bad;
+}
+
+/* HLLCFluxStrategy::computeFlux inner-face branch (HLLCFluxStrategy.cpp:40-133).
+ * Returns 1 when the p* consistency check fails. */
+static int hllc(const double* ql, const double* qr, double nx, double ny, double A, double* F) {
+    double dl = ql[0], pl = ql[1], ul = ql[2], vl = ql[3];
+    double vnl = dot2(ul, vl, nx, ny);
+    double cl = sqrt(Gamma * pl / dl);
+    double hl = pl * Gamma / ((Gamma - 1) * dl) + 0.5 * dot2(ul, vl, ul, vl);
+    double dr = qr[0], pr = qr[1], ur = qr[2], vr = qr[3];
+    double vnr = dot2(ur, vr, nx, ny);
+    double cr = sqrt(Gamma * pr / dr);
+    double hr = pr * Gamma / ((Gamma - 1) * dr) + 0.5 * dot2(ur, vr, ur, vr);
+    double el = sqrt(dl) / (sqrt(dl) + sqrt(dr));
+    double er = 1 - el;
+    double ht = el * hl + er * hr;
+    double vnt = el * vnl + er * vnr;
+    double ct = sqrt((Gamma - 1) * (ht - 0.5 * (vnt * vnt)));
+    double sl = dmin(vnl - cl, vnt - ct);
+    double sr = dmax(vnt + ct, vnr + cr);
+    double sm = (dr * vnr * (sr - vnr) - dl * vnl * (sl - vnl) + pl - pr) / (dr * (sr - vnr) - dl * (sl - vnl));
+    double ps = dl * (vnl - sl) * (vnl - sm) + pl;
+    double ps2 = dr * (vnr - sr) * (vnr - sm) + pr;
+    int bad = !(fabs(ps2 - ps) < 1e-10);
+    if (sl > 0.0) {
+        double re = pl / (Gamma - 1) + 0.5 * dl * dot2(ul, vl, ul, vl);
+        F[0] = vnl * dl * A; F[1] = vnl * (re + pl) * A;
+        F[2] = (vnl * dl * ul + pl * nx) * A; F[3] = (vnl * dl * vl + pl * ny) * A;
+    } else if (sr < 0.0) {
+        double re = pr / (Gamma - 1) + 0.5 * dr * dot2(ur, vr, ur, vr);
+        F[0] = vnr * dr * A; F[1] = vnr * (re + pr) * A;
+        F[2] = (vnr * dr * ur + pr * nx) * A; F[3] = (vnr * dr * vr + pr * ny) * A;
+    } else {
+        double s, vn, d, p, u, v;
+        if (sm < 0.0) { s = sr; vn = vnr; d = dr; p = pr; u = ur; v = vr; }
+        else { s = sl; vn = vnl; d = dl; p = pl; u = ul; v = vl; }
+        double re = p / (Gamma - 1) + 0.5 * d * dot2(u, v, u, v);
+        double f0 = (s - vn) * d / (s - sm);
+        double f1 = ((s - vn) * re - p * vn + ps * sm) / (s - sm);
+        double f2 = ((s - vn) * d * u + (ps - p) * nx) / (s - sm);
+        double f3 = ((s - vn) * d * v + (ps - p) * ny) / (s - sm);
+        F[0] = f0 * sm * A; F[1] = (f1 + ps) * sm * A;
+        F[2] = (f2 * sm + ps * nx) * A; F[3] = (f3 * sm + ps * ny) * A;
+    }
+    return bad;
+}
+
+static double venkat(double d2, double d1max, double d1min, double eps2) {
+    if (d2 > 0) return (d1max * d1max + eps2 + 2 * d2 * d1max) / (d1max * d1max + 2 * d2 * d2 + d1max * d2 + eps2);
+    if (d2 < 0) return (d1min * d1min + eps2 + 2 * d2 * d1min) / (d1min * d1min + 2 * d2 * d2 + d1min * d2 + eps2);
+    return 1;
+}
+
+/* One residual evaluation, preprocessAdvanceSerial of Euler2D (Euler2D.h:133-140)
+ * or ViscousFlow2D (ViscousFlow2D.h:192-212), with the reference's own face-loop
+ * scatter order.  Returns a bit mask: 1 = p* check failed, 4 = wall check failed. */
+int orc_residual(orc_t* o, int first_order) {
+    int nc = o->ncell, ne = o->nedge, err = 0;
+    memset(o->grad, 0, 8 * 8 * (size_t)nc);
+    memset(o->gradT, 0, 2 * 8 * (size_t)nc);
+    memset(o->specc, 0, 8 * (size_t)nc);
+    memset(o->specv, 0, 8 * (size_t)nc);
+    memset(o->R, 0, 4 * 8 * (size_t)nc);
+    if (face_states(o)) err |= 4;
+    /* solveGradient */
+    for (int k = 0; k < ne; k++) {
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1], A = o->area[k];
+        const double* ue = o->Ue + 4 * k;
+        if (o->viscous) {
+            double et = ue[1] / ue[0];
+            o->gradT[2 * l] = o->gradT[2 * l] + nx * (A * et);
+            o->gradT[2 * l + 1] = o->gradT[2 * l + 1] + ny * (A * et);
+        }
+        for (int j = 0; j < 4; j++) {
+            o->grad[8 * l + 2 * j] = o->grad[8 * l + 2 * j] + nx * (A * ue[j]);
+            o->grad[8 * l + 2 * j + 1] = o->grad[8 * l + 2 * j + 1] + ny * (A * ue[j]);
+        }
+        if (r >= 0) {
+            if (o->viscous) {
+                double et = ue[1] / ue[0];
+                o->gradT[2 * r] = o->gradT[2 * r] - nx * (A * et);
+                o->gradT[2 * r + 1] = o->gradT[2 * r + 1] - ny * (A * et);
+            }
+            for (int j = 0; j < 4; j++) {
+                o->grad[8 * r + 2 * j] = o->grad[8 * r + 2 * j] - nx * (A * ue[j]);
+                o->grad[8 * r + 2 * j + 1] = o->grad[8 * r + 2 * j + 1] - ny * (A * ue[j]);
+            }
+        }
+    }
+    for (int c = 0; c < nc; c++) {
+        for (int j = 0; j < 8; j++) o->grad[8 * c + j] = o->grad[8 * c + j] / o->vol[c];
+        if (o->viscous) { o->gradT[2 * c] = o->gradT[2 * c] / o->vol[c]; o->gradT[2 * c + 1] = o->gradT[2 * c + 1] / o->vol[c]; }
+    }
+    /* LaminarFluxStrategy::computeMu (LaminarFluxStrategy.h:76-96) */
+    if (o->viscous) {
+        for (int c = 0; c < nc; c++) o->mu[c] = sutherland(o, o->U[4 * c + 1] / o->U[4 * c]);
+        for (int k = 0; k < ne; k++) o->mue[k] = sutherland(o, o->Ue[4 * k + 1] / o->Ue[4 * k]);
+    }
+    /* solveSpectralRadius */
+    for (int k = 0; k < ne; k++) {
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        const double* ue = o->Ue + 4 * k;
+        double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1], A = o->area[k];
+        double c = sqrt(Gamma * ue[1] / ue[0]);
+        double vn = dot2(ue[2], ue[3], nx, ny);
+        double s = (fabs(vn) + c) * A;
+        o->specc[l] += s;
+        if (r >= 0) o->specc[r] += s;
+        if (o->viscous) {
+            s = dmax(4 / (3.0 * ue[0]), Gamma / ue[0]) * (o->mue[k] / 0.72) * A * A;
+            o->specv[l] += s / o->vol[l];
+            if (r >= 0) o->specv[r] += s / o->vol[r];
+        }
+    }
+    /* Vankatakrishnan_Limiter::init + computeLimiter (Vankatakrishnan_Limiter.hpp:69-177,186-200) */
+    for (int i = 0; i < 4 * nc; i++) { o->umax[i] = o->U[i]; o->umin[i] = o->U[i]; o->phi[i] = 1.0; }
+    for (int k = 0; k < ne; k++) {
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        if (r < 0) continue;
+        for (int j = 0; j < 4; j++) {
+            o->umax[4 * l + j] = dmax(o->umax[4 * l + j], o->U[4 * r + j]);
+            o->umin[4 * l + j] = dmin(o->umin[4 * l + j], o->U[4 * r + j]);
+            o->umax[4 * r + j] = dmax(o->umax[4 * r + j], o->U[4 * l + j]);
+            o->umin[4 * r + j] = dmin(o->umin[4 * r + j], o->U[4 * l + j]);
+        }
+    }
+    for (int i = 0; i < 4 * nc; i++) { o->umax[i] = o->umax[i] - o->U[i]; o->umin[i] = o->umin[i] - o->U[i]; }
+    for (int k = 0; k < ne; k++) {
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        double eps2 = pow(5, 3) * pow(o->vol[l], 1);
+        for (int side = 0; side < 2; side++) {
+            int c = side ? r : l;
+            if (c < 0) continue;
+            double vx = o->ecen[2 * k] - o->cen[2 * c], vy = o->ecen[2 * k + 1] - o->cen[2 * c + 1];
+            double* dst = side ? o->UR : o->UL;
+            for (int j = 0; j < 4; j++) {
+                double d2 = dot2(o->grad[8 * c + 2 * j], o->grad[8 * c + 2 * j + 1], vx, vy);
+                dst[4 * k + j] = d2;
+                double lim = venkat(d2, o->umax[4 * c + j], o->umin[4 * c + j], eps2);
+                o->phi[4 * c + j] = dmin(o->phi[4 * c + j], lim);
+            }
+        }
+    }
+    if (first_order)
+        for (int i = 0; i < 4 * nc; i++) o->phi[i] = 0.0;
+    /* updateLeftRight + flux loop (HLLCFluxStrategy.h:35-100, HLLCFluxStrategy.cpp:4-170) */
+    for (int k = 0; k < ne; k++) {
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1], A = o->area[k];
+        double* ql = o->UL + 4 * k;
+        double* qr = o->UR + 4 * k;
+        double F[4];
+        if (r >= 0) {
+            for (int j = 0; j < 4; j++) {
+                if (first_order) { ql[j] = 0; qr[j] = 0; }
+                ql[j] = ql[j] * o->phi[4 * l + j] + o->U[4 * l + j];
+                qr[j] = qr[j] * o->phi[4 * r + j] + o->U[4 * r + j];
+            }
+            if (hllc(ql, qr, nx, ny, A, F)) err |= 1;
+        } else {
+            for (int j = 0; j < 4; j++) ql[j] = qr[j] = o->Ue[4 * k + j];
+            if (r == BC_WALL) {
+                F[0] = 0 * A; F[1] = 0 * A; F[2] = ql[1] * nx * A; F[3] = ql[1] * ny * A;
+            } else {
+                double d = ql[0], p = ql[1], u = ql[2], v = ql[3];
+                double re = p / (Gamma - 1) + 0.5 * d * dot2(u, v, u, v);
+                double vn = dot2(u, v, nx, ny);
+                F[0] = vn * d * A; F[1] = vn * (re + p) * A;
+                F[2] = (vn * d * u + p * nx) * A; F[3] = (vn * d * v + p * ny) * A;
+            }
+        }
+        for (int j = 0; j < 4; j++) o->R[4 * l + j] += F[j];
+        if (r >= 0)
+            for (int j = 0; j < 4; j++) o->R[4 * r + j] -= F[j];
+    }
+    /* LaminarFluxStrategy::computeFlux(int) (LaminarFluxStrategy.h:110-216) */
+    if (o->viscous) {
+        for (int k = 0; k < ne; k++) {
+            int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+            double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1], A = o->area[k];
+            double mu = o->mue[k], eff = 2.0 / 3.0 * mu;
+            double g[3][2];
+            if (r >= 0) {
+                double lx = o->cen[2 * r] - o->cen[2 * l], ly = o->cen[2 * r + 1] - o->cen[2 * l + 1];
+                double l2 = dot2(lx, ly, lx, ly);
+                for (int j = 0; j < 2; j++) {
+                    double ax = (o->grad[8 * l + 2 * (2 + j)] + o->grad[8 * r + 2 * (2 + j)]) * 0.5;
+                    double ay = (o->grad[8 * l + 2 * (2 + j) + 1] + o->grad[8 * r + 2 * (2 + j) + 1]) * 0.5;
+                    double kk = (o->U[4 * r + 2 + j] - o->U[4 * l + 2 + j] - dot2(ax, ay, lx, ly)) / l2;
+                    g[j][0] = ax + lx * kk; g[j][1] = ay + ly * kk;
+                }
+                double ax = (o->gradT[2 * l] + o->gradT[2 * r]) * 0.5, ay = (o->gradT[2 * l + 1] + o->gradT[2 * r + 1]) * 0.5;
+                double rt = o->U[4 * r + 1] / o->U[4 * r], lt = o->U[4 * l + 1] / o->U[4 * l];
+                double kk = (rt - lt - dot2(ax, ay, lx, ly)) / l2;
+                g[2][0] = ax + lx * kk; g[2][1] = ay + ly * kk;
+            } else {
+                for (int j = 0; j < 2; j++) { g[j][0] = o->grad[8 * l + 2 * (2 + j)]; g[j][1] = o->grad[8 * l + 2 * (2 + j) + 1]; }
+                if (r == BC_WALL) { g[2][0] = 0; g[2][1] = 0; }
+                else { g[2][0] = o->gradT[2 * l]; g[2][1] = o->gradT[2 * l + 1]; }
+            }
+            double ve0 = o->Ue[4 * k + 2], ve1 = o->Ue[4 * k + 3];
+            double txx = eff * (2.0 * g[0][0] - g[1][1]);
+            double tyy = eff * (2.0 * g[1][1] - g[0][0]);
+            double txy = mu * (g[0][1] + g[1][0]);
+            double qx = -Gamma / (Gamma - 1) * (mu / 0.72) * g[2][0];
+            double qy = -Gamma / (Gamma - 1) * (mu / 0.72) * g[2][1];
+            double Fv[4];
+            Fv[0] = 0.0;
+            Fv[1] = ((ve0 * txx + ve1 * txy - qx) * nx + (ve0 * txy + ve1 * tyy - qy) * ny) * A;
+            Fv[2] = (txx * nx + txy * ny) * A;
+            Fv[3] = (txy * nx + tyy * ny) * A;
+            for (int j = 0; j < 4; j++) o->R[4 * l + j] -= Fv[j];
+            if (r >= 0)
+                for (int j = 0; j < 4; j++) o->R[4 * r + j] += Fv[j];
+        }
+    }
+    return err;
+}
+
+/* Euler2D/ViscousFlow2D::SolveTime, laminar branch (Euler2D.h:67-77, ViscousFlow2D.h:223-242) */
+void orc_solve_time(orc_t* o, double cfl) {
+    for (int c = 0; c < o->ncell; c++) o->dt[c] = cfl * o->vol[c] / o->specc[c];
+}
+
+/* RungeKuttaStrategy::singleStepSerial (RungeKuttaStrategy.h:74-86,39-72). */
+int orc_rk_step(orc_t* o, int first_order) {
+    static const double a[5] = {1.0 / 4, 1.0 / 6, 3.0 / 8, 1.0 / 2, 1.0};
+    int err = 0;
+    orc_cons_from_U(o);
+    for (int s = 0; s < 5; s++) {
+        err |= orc_residual(o, first_order);
+        if (s == 0) orc_solve_time(o, 0.8);
+        for (int k = 0; k < o->ncell; k++) {
+            for (int j = 0; j < 4; j++)
+                o->Wnow[4 * k + j] = o->W[4 * k + j] + a[s] * o->dt[k] * (-o->R[4 * k + j]) / o->vol[k];
+            prim_from_cons(o->Wnow + 4 * k, o->U + 4 * k);
+        }
+    }
+    return err;
+}
+
+/* ConservativeParam2ConvectiveFlux (TopologyHolderStrategy.cpp:129-141) */
+static void conv_flux(const double* w, double nx, double ny, double* F) {
+    double u = w[2] / w[0], v = w[3] / w[0];
+    double vn = dot2(u, v, nx, ny);
+    double d = w[0];
+    double p = (Gamma - 1) * (w[1] - 0.5 * d * dot2(u, v, u, v));
+    F[0] = w[0] * vn; F[1] = (w[1] + p) * vn; F[2] = w[2] * vn + p * nx; F[3] = w[3] * vn + p * ny;
+}
+
+/* SolveDF + SolveViscousFlux (TopologyHolderStrategy.cpp:143-323) for cell i,
+ * face k, forward (fb = 1) or backward (fb = 0), increment array dWx. */
+static void solve_df(const orc_t* o, int i, int k, const double* dWx, int fb, double* DF) {
+    int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+    int j, left;
+    for (int m = 0; m < 4; m++) DF[m] = 0;
+    if (i == l) {
+        if (!(r >= 0 && (int)(r < l) == fb)) return;
+        j = r; left = 1;
+    } else {
+        if (!((int)(l < r) == fb)) return;
+        j = l; left = 0;
+    }
+    double w0[4], dw[4], wp[4], fc[4], fcp[4];
+    for (int m = 0; m < 4; m++) { w0[m] = o->W[4 * j + m]; dw[m] = dWx[4 * j + m]; wp[m] = w0[m] + dw[m]; }
+    double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1], A = o->area[k];
+    conv_flux(w0, nx, ny, fc);
+    conv_flux(wp, nx, ny, fcp);
+    const double* uj = o->U + 4 * j;
+    double lx = o->cen[2 * j] - o->cen[2 * i], ly = o->cen[2 * j + 1] - o->cen[2 * i + 1];
+    double vn = dot2(uj[2], uj[3], nx, ny);
+    double c = sqrt(Gamma * uj[1] / uj[0]);
+    double rA = 1.5 * (fabs(vn) + c);
+    if (o->viscous) rA += dmax(4 / (3 * uj[0]), Gamma / uj[0]) * (o->mu[i] / 0.72) / sqrt(dot2(lx, ly, lx, ly));
+    for (int m = 0; m < 4; m++) {
+        double fv = rA * dw[m];
+        double dfc = left ? (fcp[m] - fc[m]) : (fc[m] - fcp[m]);
+        DF[m] = 0.5 * (dfc - fv) * A;
+    }
+}
+
+/* LUSGSIntegrator::UpdateSerial (LUSGS_Integrator.cpp:228-240): residual,
+ * SolveTime, SolveDiag, serial forward and backward sweeps, W += dW. */
+int orc_lusgs_step(orc_t* o, double cfl, int first_order) {
+    int err = orc_residual(o, first_order);
+    orc_solve_time(o, cfl);
+    for (int c = 0; c < o->ncell; c++) {
+        double OMEGAN = 1.5;
+        double d = o->vol[c] / o->dt[c] + 0.5 * OMEGAN * o->specc[c];
+        if (o->viscous) d += o->specv[c];
+        o->D[c] = d;
+    }
+    double DF[4];
+    for (int c = 0; c < o->ncell; c++) {
+        double s[4] = {0, 0, 0, 0};
+        for (int e = 0; e < o->cne[c]; e++) {
+            solve_df(o, c, o->ce[4 * c + e], o->dW1, 1, DF);
+            for (int m = 0; m < 4; m++) s[m] += DF[m];
+        }
+        for (int m = 0; m < 4; m++) o->dW1[4 * c + m] = (-o->R[4 * c + m] - s[m]) / o->D[c];
+    }
+    for (int c = o->ncell - 1; c >= 0; c--) {
+        double s[4] = {0, 0, 0, 0};
+        for (int e = 0; e < o->cne[c]; e++) {
+            solve_df(o, c, o->ce[4 * c + e], o->dW, 0, DF);
+            for (int m = 0; m < 4; m++) s[m] += DF[m];
+        }
+        for (int m = 0; m < 4; m++) o->dW[4 * c + m] = o->dW1[4 * c + m] - s[m] / o->D[c];
+    }
+    for (int c = 0; c < o->ncell; c++) {
+        for (int m = 0; m < 4; m++) o->W[4 * c + m] = o->W[4 * c + m] + o->dW[4 * c + m];
+        prim_from_cons(o->W + 4 * c, o->U + 4 * c);
+    }
+    return err;
+}
+
+/* Field access by name id (same ids as CFD_FIELD_* in include/cfdgb.h where shared). */
+double* orc_field(orc_t* o, int which) {
+    switch (which) {
+        case 0: return o->U;
+        case 1: return o->W;
+        case 2: return o->R;
+        case 3: return o->grad;
+        case 4: return o->phi;
+        case 5: return o->specc;
+        case 6: return o->specv;
+        case 7: return o->dt;
+        case 8: return o->D;
+        case 9: return o->dW1;
+        case 10: return o->dW;
+        case 11: return o->gradT;
+        case 12: return o->mu;
+        case 13: return o->Ue;
+        case 14: return o->mue;
+        case 15: return o->vol;
+        case 16: return o->cen;
+        case 17: return o->nrm;
+        case 18: return o->area;
+        case 19: return o->ecen;
+        case 20: return o->walld;
+        case 21: return o->UL;
+        case 22: return o->UR;
+        case 23: return o->Wnow;
+        default: return 0;
+    }
+}

@@ -1,0 +1,107 @@
+"""Host-side mesh handling through the C ABI (no GPU needed): .grd parsing,
+topology identical to the reference's, LU-SGS level schedule, error paths."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden, manifest
+
+
+@pytest.mark.parametrize("mesh_case", ["omesh_euler_rk5", "mixed_lam_lusgs"])
+def test_topology_matches_reference(built_lib, mesh_case):
+    from tmp_gb300 import abi
+
+    c = manifest()[mesh_case]
+    g = golden(mesh_case)
+    m = abi.Mesh.load_grd(GOLDEN / c["mesh"], c["wall_tag"], c["far_tag"])
+    t = m.topology()
+    np.testing.assert_array_equal(t["lr"].ravel(), g["topo_lr"])
+    np.testing.assert_array_equal(t["cell_edges"].ravel(), g["topo_cedges"])
+    np.testing.assert_array_equal(t["cell_verts"].ravel(), g["topo_cverts"])
+    np.testing.assert_array_equal(t["cell_sizes"].ravel(), g["topo_csize"])
+
+
+def test_from_arrays_equals_file(built_lib):
+    from tmp_gb300 import abi, meshgen
+
+    gm = meshgen.o_mesh(16, 6, r0=0.5, dr1=0.05, rout=3.0)
+    m = abi.Mesh.from_arrays(gm.xy, gm.edge_nodes, gm.edge_cells, gm.ncell, gm.wall_tag, gm.far_tag)
+    assert (m.nnode, m.nedge, m.ncell) == (gm.nnode, gm.nedge, gm.ncell)
+
+
+def _levels_py(topo):
+    lr = topo["lr"]
+    ce = topo["cell_edges"]
+    n = len(ce)
+    lf = np.zeros(n, int)
+    for c in range(n):
+        for e in ce[c]:
+            if e < 0:
+                continue
+            j = lr[e, 1] if lr[e, 0] == c else lr[e, 0]
+            if 0 <= j < c:
+                lf[c] = max(lf[c], lf[j] + 1)
+    lb = np.zeros(n, int)
+    for c in range(n - 1, -1, -1):
+        for e in ce[c]:
+            if e < 0:
+                continue
+            j = lr[e, 1] if lr[e, 0] == c else lr[e, 0]
+            if j > c:
+                lb[c] = max(lb[c], lb[j] + 1)
+    return lf.max() + 1, lb.max() + 1
+
+
+def test_level_schedule(built_lib):
+    """Level counts equal a direct longest-chain count over lower/upper neighbours;
+    a structured O-grid numbered circumferentially has ntheta + nr - 1 levels."""
+    from tmp_gb300 import abi, meshgen
+
+    c = manifest()["mixed_lam_lusgs"]
+    m = abi.Mesh.load_grd(GOLDEN / c["mesh"], c["wall_tag"], c["far_tag"])
+    assert m.levels() == _levels_py(m.topology())
+    gm = meshgen.o_mesh(12, 5, r0=0.5, dr1=0.05, rout=3.0)
+    mo = abi.Mesh.from_arrays(gm.xy, gm.edge_nodes, gm.edge_cells, gm.ncell, gm.wall_tag, gm.far_tag)
+    assert mo.levels() == _levels_py(mo.topology())
+
+
+def test_missing_file_is_io_error(built_lib, tmp_path):
+    from tmp_gb300 import abi
+
+    with pytest.raises(abi.CfdError) as ei:
+        abi.Mesh.load_grd(tmp_path / "nope.grd", -1, -2)
+    assert ei.value.code == -2
+
+
+def test_bad_boundary_tag_is_mesh_error(built_lib):
+    from tmp_gb300 import abi
+
+    c = manifest()["omesh_euler_rk5"]
+    with pytest.raises(abi.CfdError) as ei:
+        abi.Mesh.load_grd(GOLDEN / c["mesh"], -7, -8)  # file uses -1/-2
+    assert ei.value.code == -3
+    assert "boundary" in str(ei.value)
+
+
+def test_truncated_file_is_mesh_error(built_lib, tmp_path):
+    from tmp_gb300 import abi
+
+    src = (GOLDEN / "omesh.grd").read_text().splitlines()
+    p = tmp_path / "cut.grd"
+    p.write_text("\n".join(src[: len(src) // 2]) + "\n")
+    with pytest.raises(abi.CfdError) as ei:
+        abi.Mesh.load_grd(p, -1, -2)
+    assert ei.value.code == -3
+
+
+def test_reference_shipped_mesh_if_present(built_lib):
+    from pathlib import Path
+
+    from tmp_gb300 import abi
+
+    p = Path("/root/reference/mix_element_laminar.grd")
+    if not p.exists():
+        pytest.skip("reference meshes not present")
+    m = abi.Mesh.load_grd(p, -1, -2)
+    assert (m.nnode, m.nedge, m.ncell) == (40359, 80308, 39949)

@@ -1,0 +1,248 @@
+"""ctypes binding of the C ABI in include/cfdgb.h (libcfdgb.so).
+
+Loading fails loudly: there is no fallback path.  Every call checks the
+returned status and raises :class:`CfdError` with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libcfdgb.so"
+
+# status / enums (mirrors include/cfdgb.h)
+OK = 0
+ERR = {-1: "ARG", -2: "IO", -3: "MESH", -4: "CUDA", -5: "PSTAR", -6: "NONPHYSICAL", -7: "TIMEOUT",
+       -8: "STATE", -9: "WALLTAN"}
+BC_WALL, BC_FARFIELD = -2, -3
+FLOW_EULER, FLOW_LAMINAR = 0, 1
+ADV_RK5, ADV_LUSGS = 0, 1
+PREC_FP64, PREC_FP32 = 0, 1
+FIELD = dict(U=0, W=1, R=2, GRAD=3, PHI=4, SPEC_C=5, SPEC_V=6, DT=7, DIAG=8, DW1=9, DW=10, GRADT=11, MU=12,
+             UEDGE=13, MUEDGE=14, VOL=15, CENTER=16, NORMAL=17, AREA=18, ECENTER=19, WALLDIST=20)
+# values per element and whether the field lives on faces
+FIELD_SHAPE = dict(U=(4, 0), W=(4, 0), R=(4, 0), GRAD=(8, 0), PHI=(4, 0), SPEC_C=(1, 0), SPEC_V=(1, 0),
+                   DT=(1, 0), DIAG=(1, 0), DW1=(4, 0), DW=(4, 0), GRADT=(2, 0), MU=(1, 0), UEDGE=(4, 1),
+                   MUEDGE=(1, 1), VOL=(1, 0), CENTER=(2, 0), NORMAL=(2, 1), AREA=(1, 1), ECENTER=(2, 1),
+                   WALLDIST=(1, 0))
+NORM = dict(DW_RHO2=0, RK_DRHO=1, L2_R_RHO=2)
+
+
+class CfdError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERR.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Freestream(C.Structure):
+    _fields_ = [("mach", C.c_double), ("aoa_deg", C.c_double), ("reynolds", C.c_double),
+                ("density", C.c_double), ("pressure", C.c_double)]
+
+
+class Params(C.Structure):
+    _fields_ = [("flow", C.c_int), ("advance", C.c_int), ("precision", C.c_int), ("first_order", C.c_int),
+                ("cfl", C.c_double), ("sweep_mode", C.c_int), ("reserved", C.c_int * 7)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libcfdgb.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with tmp_gb300.build.build_library() "
+                           "(there is no CPU fallback)")
+    L = C.CDLL(str(LIB_PATH))
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    sig = {
+        "cfd_last_error": (C.c_char_p, []),
+        "cfd_version": (C.c_int, []),
+        "cfd_mesh_load_grd": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(vp)]),
+        "cfd_mesh_from_arrays": (C.c_int, [C.c_int, dp, C.c_int, ip, ip, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]),
+        "cfd_mesh_info": (C.c_int, [vp, ip, ip, ip]),
+        "cfd_mesh_topology": (C.c_int, [vp, ip, ip, ip, ip]),
+        "cfd_mesh_levels": (C.c_int, [vp, ip, ip]),
+        "cfd_mesh_free": (None, [vp]),
+        "cfd_case_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(Freestream), C.POINTER(Params), vp,
+                                      C.POINTER(vp)]),
+        "cfd_case_free": (None, [vp]),
+        "cfd_case_info": (C.c_int, [vp, ip, ip, ip]),
+        "cfd_case_stream": (C.c_int, [vp, C.POINTER(vp)]),
+        "cfd_set_cfl": (C.c_int, [vp, C.c_double]),
+        "cfd_init_freestream": (C.c_int, [vp]),
+        "cfd_residual": (C.c_int, [vp, C.c_int]),
+        "cfd_local_dt": (C.c_int, [vp, C.c_double]),
+        "cfd_step": (C.c_int, [vp, C.c_int]),
+        "cfd_rk_step": (C.c_int, [vp]),
+        "cfd_lusgs_step": (C.c_int, [vp]),
+        "cfd_step_graph": (C.c_int, [vp, C.c_int]),
+        "cfd_residual_norm": (C.c_int, [vp, C.c_int, C.c_int, dp]),
+        "cfd_get_field": (C.c_int, [vp, C.c_int, C.c_int, dp]),
+        "cfd_put_field": (C.c_int, [vp, C.c_int, C.c_int, dp]),
+        "cfd_sync": (C.c_int, [vp]),
+        "cfd_launch_count": (C.c_longlong, [vp]),
+        "cfd_bench_pass": (C.c_int, [vp, C.c_int, C.c_int, C.c_longlong, dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != OK:
+        raise CfdError(rc, lib().cfd_last_error().decode(errors="replace"))
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class Mesh:
+    """A 2D mesh in the reference's .grd topology (UnstructReader semantics)."""
+
+    def __init__(self, handle: int):
+        self.h = C.c_void_p(handle)
+        n = [C.c_int(), C.c_int(), C.c_int()]
+        check(lib().cfd_mesh_info(self.h, *[C.byref(x) for x in n]))
+        self.nnode, self.nedge, self.ncell = (x.value for x in n)
+
+    @classmethod
+    def load_grd(cls, path: str | os.PathLike, wall_tag: int, far_tag: int) -> "Mesh":
+        h = C.c_void_p()
+        check(lib().cfd_mesh_load_grd(str(path).encode(), int(wall_tag), int(far_tag), C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def from_arrays(cls, xy: np.ndarray, edge_nodes: np.ndarray, edge_cells: np.ndarray, ncell: int,
+                    wall_tag: int, far_tag: int) -> "Mesh":
+        xy = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
+        en = np.ascontiguousarray(edge_nodes, dtype=np.int32).reshape(-1)
+        ec = np.ascontiguousarray(edge_cells, dtype=np.int32).reshape(-1)
+        h = C.c_void_p()
+        check(lib().cfd_mesh_from_arrays(len(xy) // 2, _dptr(xy), len(en) // 2, _iptr(en), _iptr(ec), int(ncell),
+                                         int(wall_tag), int(far_tag), C.byref(h)))
+        return cls(h.value)
+
+    def topology(self):
+        lr = np.empty(2 * self.nedge, np.int32)
+        ce = np.empty(4 * self.ncell, np.int32)
+        cv = np.empty(4 * self.ncell, np.int32)
+        cs = np.empty(2 * self.ncell, np.int32)
+        check(lib().cfd_mesh_topology(self.h, _iptr(lr), _iptr(ce), _iptr(cv), _iptr(cs)))
+        return dict(lr=lr.reshape(-1, 2), cell_edges=ce.reshape(-1, 4), cell_verts=cv.reshape(-1, 4),
+                    cell_sizes=cs.reshape(-1, 2))
+
+    def levels(self):
+        a, b = C.c_int(), C.c_int()
+        check(lib().cfd_mesh_levels(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.cfd_mesh_free(self.h)
+            self.h = None
+
+
+class Case:
+    """Device-resident solver state for one or more packed meshes."""
+
+    def __init__(self, meshes: Sequence[Mesh], freestreams: Sequence[dict], flow: int, advance: int,
+                 precision: int = PREC_FP64, cfl: float = 1.0, first_order: bool = False, stream: int | None = None,
+                 sweep_mode: int = 0):
+        self.meshes = list(meshes)
+        arr = (C.c_void_p * len(meshes))(*[m.h.value for m in meshes])
+        fs = (Freestream * len(meshes))(*[Freestream(f["mach"], f.get("aoa_deg", 0.0), f.get("reynolds", 1.0),
+                                                     f.get("density", 1.225), f.get("pressure", 101325.0))
+                                          for f in freestreams])
+        p = Params(flow, advance, precision, int(first_order), float(cfl), int(sweep_mode))
+        h = C.c_void_p()
+        check(lib().cfd_case_create(arr, len(meshes), fs, C.byref(p), C.c_void_p(stream) if stream else None,
+                                    C.byref(h)))
+        self.h = h
+        self.flow, self.advance, self.precision = flow, advance, precision
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(lib().cfd_case_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        self.nmesh, self.ncell, self.nedge = a.value, b.value, c.value
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(lib().cfd_case_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def init_freestream(self):
+        check(lib().cfd_init_freestream(self.h))
+
+    def set_cfl(self, cfl: float):
+        check(lib().cfd_set_cfl(self.h, float(cfl)))
+
+    def residual(self, stage: int = 0):
+        check(lib().cfd_residual(self.h, int(stage)))
+
+    def local_dt(self, cfl: float):
+        check(lib().cfd_local_dt(self.h, float(cfl)))
+
+    def step(self, n: int = 1):
+        check(lib().cfd_step(self.h, int(n)))
+
+    def step_graph(self, n: int = 1):
+        check(lib().cfd_step_graph(self.h, int(n)))
+
+    def sync(self):
+        check(lib().cfd_sync(self.h))
+
+    def norm(self, which: str = "DW_RHO2", mesh: int = 0) -> float:
+        v = C.c_double()
+        check(lib().cfd_residual_norm(self.h, int(mesh), NORM[which], C.byref(v)))
+        return v.value
+
+    def launches(self) -> int:
+        return int(lib().cfd_launch_count(self.h))
+
+    PASSES = dict(face_state=0, cell_grad=1, face_flux=2, cell_update=3, sweep_fwd=4, sweep_bwd=5,
+                  lusgs_update=6, step=7)
+
+    def bench_pass(self, name: str, reps: int, flush_bytes: int = 0) -> float:
+        """Mean device time (ms) of one pass, CUDA events on the case's stream."""
+        v = C.c_double()
+        check(lib().cfd_bench_pass(self.h, self.PASSES[name], int(reps), int(flush_bytes), C.byref(v)))
+        return v.value
+
+    def _count(self, name: str, mesh: int) -> int:
+        width, per_face = FIELD_SHAPE[name]
+        m = self.meshes[mesh]
+        return width * (m.nedge if per_face else m.ncell)
+
+    def get(self, name: str, mesh: int = 0) -> np.ndarray:
+        width, _ = FIELD_SHAPE[name]
+        out = np.empty(self._count(name, mesh), np.float64)
+        check(lib().cfd_get_field(self.h, int(mesh), FIELD[name], _dptr(out)))
+        return out.reshape(-1, width) if width > 1 else out
+
+    def put(self, name: str, values: np.ndarray, mesh: int = 0):
+        a = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        if a.size != self._count(name, mesh):
+            raise ValueError(f"{name} needs {self._count(name, mesh)} values, got {a.size}")
+        check(lib().cfd_put_field(self.h, int(mesh), FIELD[name], _dptr(a)))
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.cfd_case_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

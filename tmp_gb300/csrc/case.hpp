@@ -1,0 +1,105 @@
+// Device-resident state of one case (one or more meshes packed together) and
+// the host-side launchers of the kernels that operate on it.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "fv_device.cuh"
+#include "mesh.hpp"
+
+namespace cfdgb {
+
+struct DevArrays {
+    int nc = 0, nf = 0, nn = 0, nmesh = 0;
+    // topology
+    int2* lr = nullptr;          // [nf]
+    int2* enodes = nullptr;      // [nf] global node ids
+    int* fmesh = nullptr;        // [nf]
+    int* cmesh = nullptr;        // [nc]
+    int4* cface = nullptr;       // [nc] signed face codes
+    int4* cverts = nullptr;      // [nc] global node ids, -1 padded
+    int* cnvert = nullptr;       // [nc]
+    d2* xy = nullptr;            // [nn]
+    MeshPrm* prm = nullptr;      // [nmesh]
+    // binary64 geometry
+    d4* fgeo = nullptr;          // [nf] (nx, ny, length, 0)
+    d2* fcen = nullptr;          // [nf] face centre
+    d4* cgeo = nullptr;          // [nc] (vol, xc, yc, 0)
+    d4* fg0 = nullptr;           // [nf] (nx, ny, length, 125*vol_left)
+    d4* fg1 = nullptr;           // [nf] (xf-xl, yf-yl, xf-xr, yf-yr)
+    d4* fvis = nullptr;          // [nf] (dx, dy, dx^2+dy^2, 0)
+    double* walld = nullptr;     // [nc]
+    // binary32 copies (fast form)
+    float4* fg0f = nullptr;
+    float4* fg1f = nullptr;
+    float4* fvisf = nullptr;
+    float4* cgeof = nullptr;
+    // state (binary64)
+    d4* U = nullptr;
+    d4* W = nullptr;
+    d4* W0 = nullptr;
+    d4* R = nullptr;
+    double* dt = nullptr;
+    double* diag = nullptr;
+    d4* dW1 = nullptr;
+    d4* dW = nullptr;
+    // residual intermediates, binary64 form
+    d4* grad = nullptr;          // [2*nc]
+    d4* phi = nullptr;
+    double* specc = nullptr;
+    double* specv = nullptr;
+    d2* gradT = nullptr;
+    double* mu = nullptr;
+    d4* Ue = nullptr;            // [nf]
+    d2* fspec = nullptr;         // [nf]
+    double* mue = nullptr;       // [nf]
+    d4* Fc = nullptr;            // [nf]
+    d4* Fv = nullptr;            // [nf]
+    // residual intermediates, binary32 form
+    float4* Uf = nullptr;
+    float4* gradf = nullptr;
+    float4* phif = nullptr;
+    float* speccf = nullptr;
+    float* specvf = nullptr;
+    float2* gradTf = nullptr;
+    float* muf = nullptr;
+    float4* Uef = nullptr;
+    float2* fspecf = nullptr;
+    float* muef = nullptr;
+    float4* Fcf = nullptr;
+    float4* Fvf = nullptr;
+    // LU-SGS level schedule (all meshes merged level by level)
+    int* fwd_order = nullptr;
+    int* bwd_order = nullptr;
+    std::vector<int> fwd_ptr, bwd_ptr;  // host copies, size nlev+1
+    // reductions
+    int nblk_norm = 0;
+    int4* norm_blocks = nullptr;  // (mesh, begin, end, 0) per block
+    double* norm_partial = nullptr;
+    double* norm_out = nullptr;   // [nmesh]
+    unsigned* err = nullptr;      // device error word
+};
+
+struct LaunchCfg {
+    cudaStream_t stream;
+    long long* counter;  // launches issued
+};
+
+// ---- k_fp64.cu (compiled with -fmad=false) ----
+void launch_geometry(const DevArrays& d, const LaunchCfg& L);
+// which: -1 = all three residual passes, 0 = face_state, 1 = cell_grad, 2 = face_flux
+void launch_residual_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
+void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);
+void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bool forward, int begin, int end, bool fp32);
+void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
+void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);
+void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, bool fp32);
+// ---- k_fp32.cu ----
+void launch_residual_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
+void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);
+// ---- k_misc.cu ----
+void launch_to_fp32(const DevArrays& d, const LaunchCfg& L, bool geometry);
+void launch_norm(const DevArrays& d, const LaunchCfg& L, int which);
+
+}  // namespace cfdgb

@@ -1,0 +1,717 @@
+// C ABI of the library (include/cfdgb.h): mesh and case handles, the
+// integrator drivers and field access.  Host code only; every numerical pass
+// is a CUDA kernel launched on the case's stream (see case.hpp launchers).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/cfdgb.h"
+#include "case.hpp"
+#include "mesh.hpp"
+
+using namespace cfdgb;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+void dalloc(T** p, size_t n) {
+    if (n == 0) n = 1;
+    ck(cudaMalloc((void**)p, n * sizeof(T)), "cudaMalloc");
+}
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+// Nondimensional freestream exactly as TopologyHolderStrategy::set_fs_variable2
+// followed by update_nondim_variable (TopologyHolderStrategy.cpp:325-396), with
+// the class constants R = 287.0, Gamma = 1.4 and PI = 3.141593
+// (TopologyHolderStrategy.h:23-25).
+MeshPrm make_prm(const cfd_freestream_t& fs, bool viscous) {
+    const double R = 287.0, Gamma = 1.4, PI = 3.141593;
+    double aoa = PI * fs.aoa_deg / 180;
+    double c = sqrt(Gamma * fs.pressure / fs.density);
+    double temp = fs.pressure / (R * fs.density);
+    double vmag = c * fs.mach;
+    double u = vmag * cos(aoa), v = vmag * sin(aoa);
+    MeshPrm m{};
+    m.rho_inf = fs.density / fs.density;
+    m.p_inf = fs.pressure / fs.pressure;
+    m.u_inf = u / (c / sqrt(Gamma));
+    m.v_inf = v / (c / sqrt(Gamma));
+    m.c_inf = sqrt(Gamma);
+    m.mach = fs.mach;
+    m.re = fs.reynolds;
+    m.cc = 110.5 / temp;
+    m.sqrt_gamma = sqrt(Gamma);
+    m.viscous = viscous ? 1 : 0;
+    return m;
+}
+
+}  // namespace
+
+struct cfd_mesh_s {
+    HostMesh m;
+};
+
+struct cfd_case_s {
+    int nmesh = 0;
+    cfd_params_t p{};
+    std::vector<int> coff, foff, noff;  // per-mesh offsets (size nmesh+1)
+    std::vector<MeshPrm> prm;
+    DevArrays d;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    long long launches = 0;
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    long long graph_nodes = 0;
+    bool viscous() const { return p.flow == CFD_FLOW_LAMINAR; }
+    bool fp32() const { return p.precision == CFD_PREC_FP32; }
+    LaunchCfg L() { return LaunchCfg{stream, &launches}; }
+    void drop_graph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        gexec = nullptr;
+        graph = nullptr;
+    }
+};
+
+namespace {
+
+void free_case(cfd_case_s* c) {
+    DevArrays& d = c->d;
+    c->drop_graph();
+    void* ptrs[] = {d.lr, d.enodes, d.fmesh, d.cmesh, d.cface, d.cverts, d.cnvert, d.xy, d.prm, d.fgeo, d.fcen,
+                    d.cgeo, d.fg0, d.fg1, d.fvis, d.walld, d.fg0f, d.fg1f, d.fvisf, d.cgeof, d.U, d.W, d.W0, d.R,
+                    d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
+                    d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
+                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
+                    d.norm_out, d.err};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+// Integrator steps -------------------------------------------------------------
+void residual_pass(cfd_case_s* c) {
+    auto L = c->L();
+    if (c->fp32()) launch_residual_fp32(c->d, L, c->viscous(), c->p.first_order);
+    else launch_residual_fp64(c->d, L, c->viscous(), c->p.first_order);
+}
+void launch_pass(const DevArrays& d, const LaunchCfg& L, bool visc, bool f32, int which, int first_order) {
+    if (f32) launch_residual_fp32(d, L, visc, first_order, which);
+    else launch_residual_fp64(d, L, visc, first_order, which);
+}
+void update_pass(cfd_case_s* c, int mode, double cfl, int stage, double alpha) {
+    auto L = c->L();
+    if (c->fp32()) launch_update_fp32(c->d, L, c->viscous(), mode, cfl, stage, alpha);
+    else launch_update_fp64(c->d, L, c->viscous(), mode, cfl, stage, alpha);
+}
+
+// RungeKuttaStrategy(5): CFL 0.8, alpha = 1/4, 1/6, 3/8, 1/2, 1
+// (RungeKuttaStrategy.h:124-131).
+void rk_step(cfd_case_s* c) {
+    static const double alpha[5] = {1.0 / 4, 1.0 / 6, 3.0 / 8, 1.0 / 2, 1.0};
+    for (int s = 0; s < 5; s++) {
+        residual_pass(c);
+        update_pass(c, 1 /*UPD_RK*/, 0.8, s, alpha[s]);
+    }
+}
+
+// LUSGSIntegrator::UpdateSerial (LUSGS_Integrator.cpp:228-240).
+void lusgs_step(cfd_case_s* c) {
+    residual_pass(c);
+    update_pass(c, 2 /*UPD_LUSGS*/, c->p.cfl, 0, 0.0);
+    auto L = c->L();
+    const DevArrays& d = c->d;
+    for (size_t k = 0; k + 1 < d.fwd_ptr.size(); k++)
+        launch_sweep_level(d, L, c->viscous(), true, d.fwd_ptr[k], d.fwd_ptr[k + 1], c->fp32());
+    for (size_t k = 0; k + 1 < d.bwd_ptr.size(); k++)
+        launch_sweep_level(d, L, c->viscous(), false, d.bwd_ptr[k], d.bwd_ptr[k + 1], c->fp32());
+    launch_lusgs_update(d, L, c->fp32());
+}
+
+void one_step(cfd_case_s* c) {
+    if (c->p.advance == CFD_ADV_RK5) rk_step(c);
+    else lusgs_step(c);
+}
+
+int check_errors(cfd_case_s* c) {
+    unsigned e = 0;
+    ck(cudaMemcpyAsync(&e, c->d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream), "cudaMemcpyAsync(err)");
+    ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (e) {
+        ck(cudaMemsetAsync(c->d.err, 0, sizeof(unsigned), c->stream), "cudaMemsetAsync(err)");
+        ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+        if (e & ERR_PSTAR) return fail(CFD_ERR_PSTAR, "SOmething wrong at p star: |p*_R - p*_L| >= 1e-10 on a face");
+        if (e & ERR_WALLTAN) return fail(CFD_ERR_WALLTAN, "Something wrong with Vector computation: wall tangential velocity not tangent");
+        if (e & ERR_NONPHYS) return fail(CFD_ERR_NONPHYSICAL, "non-physical state: NaN or non-positive density/pressure");
+        if (e & ERR_TIMEOUT) return fail(CFD_ERR_TIMEOUT, "a bounded device wait gave up");
+    }
+    return CFD_OK;
+}
+
+#define ABI_TRY try {
+#define ABI_CATCH                                                                 \
+    }                                                                             \
+    catch (const CudaError& ex) { return fail(CFD_ERR_CUDA, ex.what()); }         \
+    catch (const std::bad_alloc&) { return fail(CFD_ERR_CUDA, "host allocation failed"); } \
+    catch (const std::exception& ex) { return fail(CFD_ERR_MESH, ex.what()); }
+
+}  // namespace
+
+extern "C" {
+
+const char* cfd_last_error(void) { return g_err.c_str(); }
+int cfd_version(void) { return 10000; }
+
+int cfd_mesh_load_grd(const char* path, int wall_tag, int far_tag, cfd_mesh_t* out) {
+    if (!path || !out) return fail(CFD_ERR_ARG, "null argument");
+    *out = nullptr;
+    FILE* fp = fopen(path, "rb");
+    if (!fp) return fail(CFD_ERR_IO, std::string("Open file Failure: ") + path);
+    fclose(fp);
+    try {
+        auto* m = new cfd_mesh_s;
+        try {
+            m->m = load_grd(path, wall_tag, far_tag);
+        } catch (...) {
+            delete m;
+            throw;
+        }
+        *out = m;
+        return CFD_OK;
+    } catch (const std::exception& ex) {
+        return fail(CFD_ERR_MESH, ex.what());
+    }
+}
+
+int cfd_mesh_from_arrays(int nnode, const double* xy, int nedge, const int* edge_nodes, const int* edge_cells,
+                         int ncell, int wall_tag, int far_tag, cfd_mesh_t* out) {
+    if (!out || !xy || !edge_nodes || !edge_cells || nnode <= 0 || nedge <= 0 || ncell <= 0)
+        return fail(CFD_ERR_ARG, "null array or non-positive size");
+    *out = nullptr;
+    try {
+        auto* m = new cfd_mesh_s;
+        try {
+            m->m = mesh_from_arrays(nnode, xy, nedge, edge_nodes, edge_cells, ncell, wall_tag, far_tag);
+        } catch (...) {
+            delete m;
+            throw;
+        }
+        *out = m;
+        return CFD_OK;
+    } catch (const std::exception& ex) {
+        return fail(CFD_ERR_MESH, ex.what());
+    }
+}
+
+int cfd_mesh_info(cfd_mesh_t mesh, int* nnode, int* nedge, int* ncell) {
+    if (!mesh) return fail(CFD_ERR_ARG, "null mesh");
+    if (nnode) *nnode = mesh->m.nnode;
+    if (nedge) *nedge = mesh->m.nedge;
+    if (ncell) *ncell = mesh->m.ncell;
+    return CFD_OK;
+}
+
+int cfd_mesh_topology(cfd_mesh_t mesh, int* lr, int* cell_edges, int* cell_verts, int* cell_sizes) {
+    if (!mesh) return fail(CFD_ERR_ARG, "null mesh");
+    const HostMesh& m = mesh->m;
+    if (lr) memcpy(lr, m.lr.data(), m.lr.size() * sizeof(int));
+    if (cell_edges) memcpy(cell_edges, m.cell_edges.data(), m.cell_edges.size() * sizeof(int));
+    if (cell_verts) memcpy(cell_verts, m.cell_verts.data(), m.cell_verts.size() * sizeof(int));
+    if (cell_sizes)
+        for (int c = 0; c < m.ncell; c++) {
+            cell_sizes[2 * c] = m.cell_nvert[c];
+            cell_sizes[2 * c + 1] = m.cell_nedge[c];
+        }
+    return CFD_OK;
+}
+
+int cfd_mesh_levels(cfd_mesh_t mesh, int* n_forward, int* n_backward) {
+    if (!mesh) return fail(CFD_ERR_ARG, "null mesh");
+    if (n_forward) *n_forward = mesh->m.n_lev_fwd;
+    if (n_backward) *n_backward = mesh->m.n_lev_bwd;
+    return CFD_OK;
+}
+
+void cfd_mesh_free(cfd_mesh_t mesh) { delete mesh; }
+
+int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t* fs, const cfd_params_t* params,
+                    void* stream, cfd_case_t* out) {
+    if (!meshes || nmesh <= 0 || !fs || !params || !out) return fail(CFD_ERR_ARG, "null argument or nmesh <= 0");
+    *out = nullptr;
+    for (int i = 0; i < nmesh; i++)
+        if (!meshes[i]) return fail(CFD_ERR_ARG, "null mesh in list");
+    const cfd_params_t& P = *params;
+    if (P.flow != CFD_FLOW_EULER && P.flow != CFD_FLOW_LAMINAR) return fail(CFD_ERR_ARG, "Undefined Flow Type");
+    if (P.advance != CFD_ADV_RK5 && P.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_ARG, "Undefined Advance Type");
+    if (P.precision != CFD_PREC_FP64 && P.precision != CFD_PREC_FP32) return fail(CFD_ERR_ARG, "unknown precision");
+    for (int i = 0; i < nmesh; i++)
+        if (!(fs[i].density > 0) || !(fs[i].pressure > 0) || !(fs[i].mach > 0))
+            return fail(CFD_ERR_ARG, "freestream density, pressure and Mach must be positive");
+    cfd_case_s* c = new (std::nothrow) cfd_case_s;
+    if (!c) return fail(CFD_ERR_CUDA, "host allocation failed");
+    try {
+        c->nmesh = nmesh;
+        c->p = P;
+        bool visc = P.flow == CFD_FLOW_LAMINAR;
+        c->coff.assign(nmesh + 1, 0);
+        c->foff.assign(nmesh + 1, 0);
+        c->noff.assign(nmesh + 1, 0);
+        long long nc = 0, nf = 0, nn = 0;
+        for (int i = 0; i < nmesh; i++) {
+            const HostMesh& m = meshes[i]->m;
+            c->coff[i] = (int)nc;
+            c->foff[i] = (int)nf;
+            c->noff[i] = (int)nn;
+            nc += m.ncell;
+            nf += m.nedge;
+            nn += m.nnode;
+            c->prm.push_back(make_prm(fs[i], visc));
+        }
+        if (nc >= (1LL << 31) - 1 || nf >= (1LL << 31) - 1) throw std::runtime_error("case too large for 32-bit indices");
+        c->coff[nmesh] = (int)nc;
+        c->foff[nmesh] = (int)nf;
+        c->noff[nmesh] = (int)nn;
+        DevArrays& d = c->d;
+        d.nc = (int)nc;
+        d.nf = (int)nf;
+        d.nn = (int)nn;
+        d.nmesh = nmesh;
+        // host staging of packed topology
+        std::vector<int2> lr(nf), en(nf);
+        std::vector<int> fmesh(nf), cmesh(nc), cnv(nc);
+        std::vector<int4> cface(nc), cverts(nc);
+        std::vector<d2> xy(nn);
+        int maxf = 0, maxb = 0;
+        for (int i = 0; i < nmesh; i++) {
+            const HostMesh& m = meshes[i]->m;
+            int co = c->coff[i], fo = c->foff[i], no = c->noff[i];
+            for (int k = 0; k < m.nnode; k++) xy[no + k] = d2{m.xy[2 * k], m.xy[2 * k + 1]};
+            for (int k = 0; k < m.nedge; k++) {
+                int l = m.lr[2 * k], r = m.lr[2 * k + 1];
+                lr[fo + k] = make_int2(l + co, r >= 0 ? r + co : r);
+                en[fo + k] = make_int2(m.edge_nodes[2 * k] + no, m.edge_nodes[2 * k + 1] + no);
+                fmesh[fo + k] = i;
+            }
+            for (int k = 0; k < m.ncell; k++) {
+                int code[4] = {0, 0, 0, 0};
+                for (int s = 0; s < m.cell_nedge[k]; s++) {
+                    int e = m.cell_edges[4 * k + s];
+                    int gf = e + fo;
+                    code[s] = (m.lr[2 * e] == k) ? (gf + 1) : -(gf + 1);
+                }
+                cface[co + k] = make_int4(code[0], code[1], code[2], code[3]);
+                int v[4];
+                for (int s = 0; s < 4; s++) v[s] = m.cell_verts[4 * k + s] >= 0 ? m.cell_verts[4 * k + s] + no : -1;
+                cverts[co + k] = make_int4(v[0], v[1], v[2], v[3]);
+                cnv[co + k] = m.cell_nvert[k];
+                cmesh[co + k] = i;
+            }
+            maxf = std::max(maxf, m.n_lev_fwd);
+            maxb = std::max(maxb, m.n_lev_bwd);
+        }
+        // merged level schedule
+        std::vector<int> fo_(nc), bo_(nc);
+        {
+            std::vector<int> cntf(maxf + 1, 0), cntb(maxb + 1, 0);
+            for (int i = 0; i < nmesh; i++) {
+                const HostMesh& m = meshes[i]->m;
+                for (int k = 0; k < m.ncell; k++) {
+                    cntf[m.lev_fwd[k] + 1]++;
+                    cntb[m.lev_bwd[k] + 1]++;
+                }
+            }
+            for (int k = 0; k < maxf; k++) cntf[k + 1] += cntf[k];
+            for (int k = 0; k < maxb; k++) cntb[k + 1] += cntb[k];
+            d.fwd_ptr = cntf;
+            d.bwd_ptr = cntb;
+            std::vector<int> pf(cntf.begin(), cntf.end() - 1), pb(cntb.begin(), cntb.end() - 1);
+            for (int i = 0; i < nmesh; i++) {
+                const HostMesh& m = meshes[i]->m;
+                int co = c->coff[i];
+                for (int k = 0; k < m.ncell; k++) fo_[pf[m.lev_fwd[k]]++] = co + k;
+                for (int k = m.ncell - 1; k >= 0; k--) bo_[pb[m.lev_bwd[k]]++] = co + k;
+            }
+        }
+        // norm chunks
+        std::vector<int4> nb;
+        const int chunk = 8192;
+        for (int i = 0; i < nmesh; i++)
+            for (int b = c->coff[i]; b < c->coff[i + 1]; b += chunk)
+                nb.push_back(make_int4(i, b, std::min(b + chunk, c->coff[i + 1]), 0));
+        d.nblk_norm = (int)nb.size();
+
+        if (stream) {
+            c->stream = (cudaStream_t)stream;
+        } else {
+            ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            c->own_stream = true;
+        }
+        dalloc(&d.lr, nf); dalloc(&d.enodes, nf); dalloc(&d.fmesh, nf); dalloc(&d.cmesh, nc);
+        dalloc(&d.cface, nc); dalloc(&d.cverts, nc); dalloc(&d.cnvert, nc); dalloc(&d.xy, nn);
+        dalloc(&d.prm, nmesh);
+        dalloc(&d.fgeo, nf); dalloc(&d.fcen, nf); dalloc(&d.cgeo, nc); dalloc(&d.fg0, nf); dalloc(&d.fg1, nf);
+        dalloc(&d.fvis, nf);
+        dalloc(&d.U, nc); dalloc(&d.W, nc); dalloc(&d.W0, nc); dalloc(&d.R, nc); dalloc(&d.dt, nc);
+        dalloc(&d.diag, nc); dalloc(&d.dW1, nc); dalloc(&d.dW, nc);
+        if (c->fp32()) {
+            dalloc(&d.fg0f, nf); dalloc(&d.fg1f, nf); dalloc(&d.fvisf, nf); dalloc(&d.cgeof, nc);
+            dalloc(&d.Uf, nc); dalloc(&d.gradf, 2 * (size_t)nc); dalloc(&d.phif, nc); dalloc(&d.speccf, nc);
+            dalloc(&d.Uef, nf); dalloc(&d.fspecf, nf); dalloc(&d.Fcf, nf);
+            if (visc) { dalloc(&d.specvf, nc); dalloc(&d.gradTf, nc); dalloc(&d.muf, nc); dalloc(&d.muef, nf); dalloc(&d.Fvf, nf); }
+        } else {
+            dalloc(&d.grad, 2 * (size_t)nc); dalloc(&d.phi, nc); dalloc(&d.specc, nc);
+            dalloc(&d.Ue, nf); dalloc(&d.fspec, nf); dalloc(&d.Fc, nf);
+            if (visc) { dalloc(&d.specv, nc); dalloc(&d.gradT, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf); dalloc(&d.Fv, nf); }
+        }
+        dalloc(&d.fwd_order, nc); dalloc(&d.bwd_order, nc);
+        dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
+        dalloc(&d.err, 1);
+        cudaStream_t s = c->stream;
+        ck(cudaMemcpyAsync(d.lr, lr.data(), nf * sizeof(int2), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.enodes, en.data(), nf * sizeof(int2), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.fmesh, fmesh.data(), nf * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.cmesh, cmesh.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.cface, cface.data(), nc * sizeof(int4), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.cverts, cverts.data(), nc * sizeof(int4), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.cnvert, cnv.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.xy, xy.data(), nn * sizeof(d2), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.prm, c->prm.data(), nmesh * sizeof(MeshPrm), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.fwd_order, fo_.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.bwd_order, bo_.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemcpyAsync(d.norm_blocks, nb.data(), nb.size() * sizeof(int4), cudaMemcpyHostToDevice, s), "upload");
+        ck(cudaMemsetAsync(d.err, 0, sizeof(unsigned), s), "memset");
+        ck(cudaMemsetAsync(d.dW1, 0, nc * sizeof(d4), s), "memset");
+        ck(cudaMemsetAsync(d.dW, 0, nc * sizeof(d4), s), "memset");
+        ck(cudaMemsetAsync(d.W0, 0, nc * sizeof(d4), s), "memset");
+        auto L = c->L();
+        launch_geometry(d, L);
+        if (c->fp32()) launch_to_fp32(d, L, true);
+        ck(cudaGetLastError(), "geometry launch");
+        ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        *out = c;
+        return CFD_OK;
+    } catch (const CudaError& ex) {
+        free_case(c);
+        return fail(CFD_ERR_CUDA, ex.what());
+    } catch (const std::exception& ex) {
+        free_case(c);
+        return fail(CFD_ERR_MESH, ex.what());
+    }
+}
+
+void cfd_case_free(cfd_case_t c) {
+    if (c) free_case(c);
+}
+
+int cfd_case_info(cfd_case_t c, int* nmesh, int* ncell_total, int* nedge_total) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (nmesh) *nmesh = c->nmesh;
+    if (ncell_total) *ncell_total = c->d.nc;
+    if (nedge_total) *nedge_total = c->d.nf;
+    return CFD_OK;
+}
+
+int cfd_case_stream(cfd_case_t c, void** stream) {
+    if (!c || !stream) return fail(CFD_ERR_ARG, "null argument");
+    *stream = (void*)c->stream;
+    return CFD_OK;
+}
+
+int cfd_set_cfl(cfd_case_t c, double cfl) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (!(cfl > 0)) return fail(CFD_ERR_ARG, "CFL must be positive");
+    c->p.cfl = cfl;
+    c->drop_graph();
+    return CFD_OK;
+}
+
+int cfd_init_freestream(cfd_case_t c) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    ABI_TRY
+    std::vector<d4> u(c->d.nc);
+    for (int m = 0; m < c->nmesh; m++) {
+        const MeshPrm& p = c->prm[m];
+        for (int k = c->coff[m]; k < c->coff[m + 1]; k++) u[k] = d4{p.rho_inf, p.p_inf, p.u_inf, p.v_inf};
+    }
+    ck(cudaMemcpyAsync(c->d.U, u.data(), u.size() * sizeof(d4), cudaMemcpyHostToDevice, c->stream), "upload U");
+    auto L = c->L();
+    launch_cons_from_prim(c->d, L, 0, c->d.nc);
+    if (c->fp32()) launch_to_fp32(c->d, L, false);
+    ck(cudaGetLastError(), "launch");
+    ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_residual(cfd_case_t c, int stage) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    (void)stage;
+    ABI_TRY
+    residual_pass(c);
+    update_pass(c, 0 /*UPD_RESID*/, 0.0, 0, 0.0);
+    ck(cudaGetLastError(), "residual launch");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_local_dt(cfd_case_t c, double cfl) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    ABI_TRY
+    launch_local_dt(c->d, c->L(), cfl, c->fp32());
+    ck(cudaGetLastError(), "launch");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_step(cfd_case_t c, int nsteps) {
+    if (!c || nsteps < 0) return fail(CFD_ERR_ARG, "null case or negative step count");
+    ABI_TRY
+    for (int i = 0; i < nsteps; i++) one_step(c);
+    ck(cudaGetLastError(), "step launch");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_rk_step(cfd_case_t c) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (c->p.advance != CFD_ADV_RK5) return fail(CFD_ERR_STATE, "case was created for LU-SGS");
+    return cfd_step(c, 1);
+}
+
+int cfd_lusgs_step(cfd_case_t c) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (c->p.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_STATE, "case was created for Runge-Kutta");
+    return cfd_step(c, 1);
+}
+
+int cfd_step_graph(cfd_case_t c, int nsteps) {
+    if (!c || nsteps < 0) return fail(CFD_ERR_ARG, "null case or negative step count");
+    ABI_TRY
+    if (!c->gexec) {
+        ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        long long before = c->launches;
+        one_step(c);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        c->launches = before;  // captured, not issued
+        ck(e, "cudaStreamEndCapture");
+        c->graph = g;
+        ck(cudaGraphInstantiate(&c->gexec, g, 0), "cudaGraphInstantiate");
+        // count kernels per replay
+        size_t n = 0;
+        ck(cudaGraphGetNodes(g, nullptr, &n), "cudaGraphGetNodes");
+        c->graph_nodes = (long long)n;
+    }
+    for (int i = 0; i < nsteps; i++) {
+        ck(cudaGraphLaunch(c->gexec, c->stream), "cudaGraphLaunch");
+        c->launches += c->graph_nodes;
+    }
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_residual_norm(cfd_case_t c, int mesh, int which, double* out) {
+    if (!c || !out) return fail(CFD_ERR_ARG, "null argument");
+    if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
+    if (which < 0 || which > 2) return fail(CFD_ERR_ARG, "unknown norm");
+    ABI_TRY
+    launch_norm(c->d, c->L(), which);
+    ck(cudaGetLastError(), "norm launch");
+    double v = 0;
+    ck(cudaMemcpyAsync(&v, c->d.norm_out + mesh, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "norm readback");
+    int st = check_errors(c);
+    if (which == CFD_NORM_L2_R_RHO) v = sqrt(v / (double)(c->coff[mesh + 1] - c->coff[mesh]));
+    *out = v;
+    return st;
+    ABI_CATCH
+}
+
+int cfd_sync(cfd_case_t c) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    ABI_TRY
+    return check_errors(c);
+    ABI_CATCH
+}
+
+long long cfd_launch_count(cfd_case_t c) { return c ? c->launches : -1; }
+
+int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms) {
+    if (!c || !avg_ms || reps <= 0) return fail(CFD_ERR_ARG, "null argument or reps <= 0");
+    if (pass < 0 || pass > 7) return fail(CFD_ERR_ARG, "unknown pass");
+    ABI_TRY
+    DevArrays& d = c->d;
+    auto L = c->L();
+    void* flush = nullptr;
+    if (flush_bytes > 0) ck(cudaMalloc(&flush, (size_t)flush_bytes), "cudaMalloc(flush)");
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "cudaEventCreate");
+    ck(cudaEventCreate(&e1), "cudaEventCreate");
+    double total = 0;
+    bool visc = c->viscous(), f32 = c->fp32();
+    for (int r = 0; r < reps; r++) {
+        if (flush) ck(cudaMemsetAsync(flush, r & 0xff, (size_t)flush_bytes, c->stream), "flush");
+        ck(cudaEventRecord(e0, c->stream), "cudaEventRecord");
+        switch (pass) {
+            case 0: launch_pass(d, L, visc, f32, 0, c->p.first_order); break;  // face_state
+            case 1: launch_pass(d, L, visc, f32, 1, c->p.first_order); break;  // cell_grad
+            case 2: launch_pass(d, L, visc, f32, 2, c->p.first_order); break;  // face_flux
+            case 3: update_pass(c, c->p.advance == CFD_ADV_RK5 ? 0 : 2, c->p.cfl, 0, 0.0); break;
+            case 4:
+                for (size_t k = 0; k + 1 < d.fwd_ptr.size(); k++)
+                    launch_sweep_level(d, L, visc, true, d.fwd_ptr[k], d.fwd_ptr[k + 1], f32);
+                break;
+            case 5:
+                for (size_t k = 0; k + 1 < d.bwd_ptr.size(); k++)
+                    launch_sweep_level(d, L, visc, false, d.bwd_ptr[k], d.bwd_ptr[k + 1], f32);
+                break;
+            case 6: launch_lusgs_update(d, L, f32); break;
+            case 7: one_step(c); break;
+        }
+        ck(cudaEventRecord(e1, c->stream), "cudaEventRecord");
+        ck(cudaEventSynchronize(e1), "cudaEventSynchronize");
+        float ms = 0;
+        ck(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        total += ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (flush) cudaFree(flush);
+    *avg_ms = total / reps;
+    return CFD_OK;
+    ABI_CATCH
+}
+
+// Field access ------------------------------------------------------------------
+namespace {
+struct FieldRef {
+    const void* p64;     // binary64 array (or null)
+    const void* p32;     // binary32 array (fast form) or null
+    int width;           // values per element
+    bool per_face;
+    bool writable;
+};
+
+FieldRef field_ref(cfd_case_s* c, int which) {
+    DevArrays& d = c->d;
+    bool f = c->fp32();
+    switch (which) {
+        case CFD_FIELD_U: return {d.U, nullptr, 4, false, true};
+        case CFD_FIELD_W: return {d.W, nullptr, 4, false, true};
+        case CFD_FIELD_R: return {d.R, nullptr, 4, false, false};
+        case CFD_FIELD_GRAD: return {f ? nullptr : d.grad, f ? d.gradf : nullptr, 8, false, false};
+        case CFD_FIELD_PHI: return {f ? nullptr : d.phi, f ? d.phif : nullptr, 4, false, false};
+        case CFD_FIELD_SPEC_C: return {f ? nullptr : d.specc, f ? d.speccf : nullptr, 1, false, false};
+        case CFD_FIELD_SPEC_V: return {f ? nullptr : d.specv, f ? d.specvf : nullptr, 1, false, false};
+        case CFD_FIELD_DT: return {d.dt, nullptr, 1, false, false};
+        case CFD_FIELD_DIAG: return {d.diag, nullptr, 1, false, false};
+        case CFD_FIELD_DW1: return {d.dW1, nullptr, 4, false, false};
+        case CFD_FIELD_DW: return {d.dW, nullptr, 4, false, false};
+        case CFD_FIELD_GRADT: return {f ? nullptr : d.gradT, f ? d.gradTf : nullptr, 2, false, false};
+        case CFD_FIELD_MU: return {f ? nullptr : d.mu, f ? d.muf : nullptr, 1, false, false};
+        case CFD_FIELD_UEDGE: return {f ? nullptr : d.Ue, f ? d.Uef : nullptr, 4, true, false};
+        case CFD_FIELD_MUEDGE: return {f ? nullptr : d.mue, f ? d.muef : nullptr, 1, true, false};
+        default: return {nullptr, nullptr, 0, false, false};
+    }
+}
+
+// Geometry fields stored inside wider records.
+int get_geometry(cfd_case_s* c, int mesh, int which, double* host) {
+    DevArrays& d = c->d;
+    int nc = c->coff[mesh + 1] - c->coff[mesh], nf = c->foff[mesh + 1] - c->foff[mesh];
+    if (which == CFD_FIELD_VOL || which == CFD_FIELD_CENTER) {
+        std::vector<d4> g(nc);
+        ck(cudaMemcpyAsync(g.data(), d.cgeo + c->coff[mesh], nc * sizeof(d4), cudaMemcpyDeviceToHost, c->stream), "download");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+        for (int k = 0; k < nc; k++) {
+            if (which == CFD_FIELD_VOL) host[k] = g[k].x;
+            else { host[2 * k] = g[k].y; host[2 * k + 1] = g[k].z; }
+        }
+        return CFD_OK;
+    }
+    if (which == CFD_FIELD_NORMAL || which == CFD_FIELD_AREA) {
+        std::vector<d4> g(nf);
+        ck(cudaMemcpyAsync(g.data(), d.fgeo + c->foff[mesh], nf * sizeof(d4), cudaMemcpyDeviceToHost, c->stream), "download");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+        for (int k = 0; k < nf; k++) {
+            if (which == CFD_FIELD_AREA) host[k] = g[k].z;
+            else { host[2 * k] = g[k].x; host[2 * k + 1] = g[k].y; }
+        }
+        return CFD_OK;
+    }
+    if (which == CFD_FIELD_ECENTER) {
+        ck(cudaMemcpyAsync(host, d.fcen + c->foff[mesh], nf * sizeof(d2), cudaMemcpyDeviceToHost, c->stream), "download");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+        return CFD_OK;
+    }
+    return fail(CFD_ERR_ARG, "unknown field");
+}
+}  // namespace
+
+int cfd_get_field(cfd_case_t c, int mesh, int which, double* host) {
+    if (!c || !host) return fail(CFD_ERR_ARG, "null argument");
+    if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
+    ABI_TRY
+    if (which >= CFD_FIELD_VOL && which <= CFD_FIELD_ECENTER) return get_geometry(c, mesh, which, host);
+    FieldRef r = field_ref(c, which);
+    if (!r.p64 && !r.p32) return fail(CFD_ERR_ARG, "field not available for this case (flow type, precision or id)");
+    int off = r.per_face ? c->foff[mesh] : c->coff[mesh];
+    int n = r.per_face ? (c->foff[mesh + 1] - off) : (c->coff[mesh + 1] - off);
+    size_t cnt = (size_t)n * r.width;
+    if (r.p64) {
+        ck(cudaMemcpyAsync(host, (const double*)r.p64 + (size_t)off * r.width, cnt * 8, cudaMemcpyDeviceToHost, c->stream), "download");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+    } else {
+        std::vector<float> tmp(cnt);
+        ck(cudaMemcpyAsync(tmp.data(), (const float*)r.p32 + (size_t)off * r.width, cnt * 4, cudaMemcpyDeviceToHost, c->stream), "download");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+        for (size_t i = 0; i < cnt; i++) host[i] = tmp[i];
+    }
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host) {
+    if (!c || !host) return fail(CFD_ERR_ARG, "null argument");
+    if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
+    if (which != CFD_FIELD_U) return fail(CFD_ERR_ARG, "only the primitive field U can be written");
+    ABI_TRY
+    int off = c->coff[mesh], n = c->coff[mesh + 1] - off;
+    ck(cudaMemcpyAsync(c->d.U + off, host, (size_t)n * 32, cudaMemcpyHostToDevice, c->stream), "upload");
+    auto L = c->L();
+    launch_cons_from_prim(c->d, L, off, off + n);
+    if (c->fp32()) launch_to_fp32(c->d, L, false);
+    ck(cudaGetLastError(), "launch");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+}  // extern "C"

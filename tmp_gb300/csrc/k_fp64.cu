@@ -1,0 +1,309 @@
+// Binary64 kernels: geometry, the plain-form residual, RK/LU-SGS updates and the
+// level-scheduled LU-SGS sweeps.  This translation unit is compiled with
+// -fmad=false so that every a*b+c rounds twice, as in the reference's
+// compiled code; together with the reference's operation order that makes the
+// plain form reproduce the reference bit for bit (pow() aside).
+#include "case.hpp"
+#include "fv_kernels.cuh"
+
+namespace cfdgb {
+
+static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
+
+// ---------------------------------------------------------------------------
+// Geometry.  edge3d::find_area/find_normal/find_center (toolBox/edge3d_int.h:93-230)
+__global__ void k_geom_faces(int nf, const int2* __restrict__ en, const d2* __restrict__ xy, d4* __restrict__ fgeo,
+                             d2* __restrict__ fcen) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    int2 e = en[f];
+    d2 p0 = xy[e.x], p1 = xy[e.y];
+    double dx = p1.x - p0.x, dy = p1.y - p0.y;
+    double l2 = 0;
+    l2 += (dx * dx);
+    l2 += (dy * dy);
+    double A = sqrt(l2);
+    fgeo[f] = d4{dy / A, -dx / A, A, 0.0};
+    double cx = 0, cy = 0;
+    cx = cx + p0.x; cy = cy + p0.y;
+    cx = cx + p1.x; cy = cy + p1.y;
+    fcen[f] = d2{cx / 2.0, cy / 2.0};
+}
+
+// triangle_area (mathTools/cellVolume.cpp:6-19)
+__device__ __forceinline__ double tri_area(d2 p1, d2 p2, d2 p3) {
+    double a = 0.5 * ((p1.x - p2.x) * (p1.y + p2.y) + (p2.x - p3.x) * (p2.y + p3.y) + (p3.x - p1.x) * (p3.y + p1.y));
+    if (a < 0) a = -a;
+    return a;
+}
+
+// computeCellVolume2D (mathTools/cellVolume.cpp:21-75) and cell3d::find_center
+// (toolBox/cell3d_int.h:100-108).
+__global__ void k_geom_cells(int nc, const int4* __restrict__ cv, const int* __restrict__ cnv, const d2* __restrict__ xy,
+                             d4* __restrict__ cgeo) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    int4 v = cv[c];
+    int n = cnv[c];
+    d2 p[4];
+    p[0] = xy[v.x]; p[1] = xy[v.y]; p[2] = xy[v.z];
+    p[3] = n == 4 ? xy[v.w] : d2{0.0, 0.0};
+    double area;
+    if (n == 3) {
+        area = tri_area(p[0], p[1], p[2]);
+    } else {
+        double abx = p[1].x - p[0].x, aby = p[1].y - p[0].y;
+        double acx = p[2].x - p[0].x, acy = p[2].y - p[0].y;
+        double adx = p[3].x - p[0].x, ady = p[3].y - p[0].y;
+        // z components of AB x AC, AB x AD, AC x AD (the x,y components vanish in 2D)
+        double abac = abx * acy - aby * acx;
+        double abad = abx * ady - aby * adx;
+        double acad = acx * ady - acy * adx;
+        area = 0;
+        if (abac * abad > 0) {
+            if (acad * abad > 0) {
+                area += tri_area(p[0], p[2], p[1]);
+                area += tri_area(p[0], p[2], p[3]);
+            } else {
+                area += tri_area(p[0], p[3], p[1]);
+                area += tri_area(p[0], p[3], p[2]);
+            }
+        } else {
+            area += tri_area(p[0], p[1], p[2]);
+            area += tri_area(p[0], p[1], p[3]);
+        }
+    }
+    double cx = 0, cy = 0;
+    for (int i = 0; i < n; i++) { cx = cx + p[i].x; cy = cy + p[i].y; }
+    cgeo[c] = d4{area, cx / (double)n, cy / (double)n, 0.0};
+}
+
+// Per-face quantities the residual kernels read: 125*vol(left) for the limiter's
+// epsilon^2 = K^3 * vol^(3/ndim) with K = 5 and the integer 3/2 = 1
+// (Vankatakrishnan_Limiter.hpp:108,138 - both sides use the left cell's volume),
+// the centre offsets of Vankatakrishnan_Limiter.hpp:107,137, and the centre line
+// of LaminarFluxStrategy.h:136,149.
+__global__ void k_geom_derived(int nf, const int2* __restrict__ lr, const d4* __restrict__ fgeo,
+                               const d2* __restrict__ fcen, const d4* __restrict__ cgeo, d4* __restrict__ fg0,
+                               d4* __restrict__ fg1, d4* __restrict__ fvis) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    int2 e = lr[f];
+    d4 g = fgeo[f];
+    d2 xf = fcen[f];
+    d4 cl = cgeo[e.x];
+    fg0[f] = d4{g.x, g.y, g.z, 125.0 * cl.x};
+    double dlx = xf.x - cl.y, dly = xf.y - cl.z;
+    double drx = 0, dry = 0, lx, ly;
+    if (e.y >= 0) {
+        d4 cr = cgeo[e.y];
+        drx = xf.x - cr.y;
+        dry = xf.y - cr.z;
+        lx = cr.y - cl.y;
+        ly = cr.z - cl.z;
+    } else {
+        lx = dlx;
+        ly = dly;
+    }
+    fg1[f] = d4{dlx, dly, drx, dry};
+    double l2 = 0;
+    l2 += lx * lx;
+    l2 += ly * ly;
+    fvis[f] = d4{lx, ly, l2, 0.0};
+}
+
+void launch_geometry(const DevArrays& d, const LaunchCfg& L) {
+    k_geom_faces<<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.enodes, d.xy, d.fgeo, d.fcen);
+    k_geom_cells<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.cverts, d.cnvert, d.xy, d.cgeo);
+    k_geom_derived<<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fgeo, d.fcen, d.cgeo, d.fg0, d.fg1, d.fvis);
+    *L.counter += 3;
+}
+
+// ---------------------------------------------------------------------------
+// Residual, binary64.
+template <bool V>
+static void residual64(const DevArrays& d, const LaunchCfg& L, int first_order, int which) {
+    if (which < 0 || which == 0) {
+        k_face_state<double, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fmesh, d.prm, d.fg0, d.U, d.Ue,
+                                                                        d.fspec, d.mue, d.err);
+        *L.counter += 1;
+    }
+    if (which < 0 || which == 1) {
+        k_cell_grad<double, V><<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.cmesh, d.prm, d.cgeo,
+                                                                       d.fg0, d.fg1, d.U, d.Ue, d.fspec, first_order,
+                                                                       d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu);
+        *L.counter += 1;
+    }
+    if (which < 0 || which == 2) {
+        k_face_flux<double, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fg0, d.fg1, d.fvis, d.U, d.grad,
+                                                                       d.phi, d.Ue, d.mue, d.gradT, d.Fc, d.Fv, d.err);
+        *L.counter += 1;
+    }
+}
+void launch_residual_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which) {
+    if (viscous) residual64<true>(d, L, first_order, which);
+    else residual64<false>(d, L, first_order, which);
+}
+
+template <bool V, int M>
+static void update64(const DevArrays& d, const LaunchCfg& L, double cfl, int stage, double alpha) {
+    k_cell_update<double, V, M><<<nblk(d.nc, 256), 256, 0, L.stream>>>(
+        d.nc, d.cface, d.cgeo, d.Fc, d.Fv, d.specc, d.specv, cfl, stage, alpha, d.R, d.U, d.W, d.W0, d.dt, d.diag,
+        (d4*)nullptr);
+    *L.counter += 1;
+}
+void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage,
+                        double alpha) {
+    if (viscous) {
+        if (mode == UPD_RESID) update64<true, UPD_RESID>(d, L, cfl, stage, alpha);
+        else if (mode == UPD_RK) update64<true, UPD_RK>(d, L, cfl, stage, alpha);
+        else update64<true, UPD_LUSGS>(d, L, cfl, stage, alpha);
+    } else {
+        if (mode == UPD_RESID) update64<false, UPD_RESID>(d, L, cfl, stage, alpha);
+        else if (mode == UPD_RK) update64<false, UPD_RK>(d, L, cfl, stage, alpha);
+        else update64<false, UPD_LUSGS>(d, L, cfl, stage, alpha);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// LU-SGS sweeps.  For cell i of the current level, sum SolveDF over its faces in
+// ascending order (TopologyHolderStrategy.cpp:217-323) taking only neighbours
+// below i (forward) or above i (backward), then
+//   forward:  dW1_i = (-R_i - sum) / D_i          (LUSGS_Integrator.cpp:492-523)
+//   backward: dW_i  = dW1_i - sum / D_i           (LUSGS_Integrator.cpp:526-560)
+// Cells of one level have no face between them, so they run in parallel and
+// the result equals the reference's serial sweep.
+template <bool VISC, bool FWD, class MuT>
+__global__ void __launch_bounds__(128) k_sweep(int begin, int end, const int* __restrict__ order,
+                                               const int4* __restrict__ cface, const int2* __restrict__ lr,
+                                               const d4* __restrict__ fg0, const d4* __restrict__ fvis,
+                                               const d4* __restrict__ W, const d4* __restrict__ U,
+                                               const MuT* __restrict__ mu, const d4* __restrict__ R,
+                                               const double* __restrict__ D, d4* dW1, d4* dW) {
+    int idx = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= end) return;
+    const double G = 1.4;
+    int i = order[idx];
+    int4 cf = cface[i];
+    int codes[4] = {cf.x, cf.y, cf.z, cf.w};
+    double dF[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int s = 0; s < 4; s++) {
+        int code = codes[s];
+        if (code == 0) break;
+        int f = code_face(code);
+        bool left = code > 0;
+        int2 e = lr[f];
+        int j = left ? e.y : e.x;
+        bool use = FWD ? (j >= 0 && j < i) : (j > i);
+        double DF[4] = {0.0, 0.0, 0.0, 0.0};
+        if (use) {
+            double w0[4], dw[4], wp[4], fc[4], fcp[4], uj[4];
+            to_arr(ld4(W + j), w0);
+            to_arr(ld4((FWD ? dW1 : dW) + j), dw);
+#pragma unroll
+            for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
+            d4 g = fg0[f];
+            double nx = g.x, ny = g.y, A = g.z;
+            conv_flux_w<double>(w0, nx, ny, fc);
+            conv_flux_w<double>(wp, nx, ny, fcp);
+            to_arr(ld4(U + j), uj);
+            // SolveViscousFlux (TopologyHolderStrategy.cpp:143-188)
+            double vn = dot2(uj[2], uj[3], nx, ny);
+            double c = sqrt(G * uj[1] / uj[0]);
+            double rA = 1.5 * (fabs(vn) + c);
+            if (VISC) rA += smax(4 / (3 * uj[0]), G / uj[0]) * ((double)mu[i] / 0.72) / sqrt(fvis[f].z);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                double fv = rA * dw[k];
+                double dfc = left ? (fcp[k] - fc[k]) : (fc[k] - fcp[k]);
+                DF[k] = 0.5 * (dfc - fv) * A;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) dF[k] += DF[k];
+    }
+    double Di = D[i];
+    if (FWD) {
+        double r[4];
+        to_arr(ld4(R + i), r);
+        st4(dW1 + i, d4{(-r[0] - dF[0]) / Di, (-r[1] - dF[1]) / Di, (-r[2] - dF[2]) / Di, (-r[3] - dF[3]) / Di});
+    } else {
+        double a[4];
+        to_arr(ld4(dW1 + i), a);
+        st4(dW + i, d4{a[0] - dF[0] / Di, a[1] - dF[1] / Di, a[2] - dF[2] / Di, a[3] - dF[3] / Di});
+    }
+}
+
+template <class MuT>
+static void sweep_t(const DevArrays& d, const LaunchCfg& L, bool viscous, bool forward, int begin, int end,
+                    const MuT* mu) {
+    int n = end - begin;
+    const int* order = forward ? d.fwd_order : d.bwd_order;
+    dim3 grid(nblk(n, 128));
+    if (viscous) {
+        if (forward) k_sweep<true, true, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW);
+        else k_sweep<true, false, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW);
+    } else {
+        if (forward) k_sweep<false, true, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW);
+        else k_sweep<false, false, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW);
+    }
+    *L.counter += 1;
+}
+void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bool forward, int begin, int end,
+                        bool fp32) {
+    if (end - begin <= 0) return;
+    if (fp32) sweep_t<float>(d, L, viscous, forward, begin, end, d.muf);
+    else sweep_t<double>(d, L, viscous, forward, begin, end, d.mu);
+}
+
+// W += dW, U = prim(W)  (LUSGSIntegrator::UpdatePrimitiveVariable, LUSGS_Integrator.cpp:242-255)
+__global__ void k_lusgs_update(int nc, const d4* __restrict__ dW, d4* __restrict__ W, d4* __restrict__ U,
+                               float4* __restrict__ Uf, unsigned* __restrict__ err) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    double w[4], dw[4], u[4];
+    to_arr(ld4(W + c), w);
+    to_arr(ld4(dW + c), dw);
+#pragma unroll
+    for (int k = 0; k < 4; k++) w[k] = w[k] + dw[k];
+    prim_from_cons<double>(w, u);
+    st4(W + c, d4{w[0], w[1], w[2], w[3]});
+    st4(U + c, d4{u[0], u[1], u[2], u[3]});
+    if (Uf) Uf[c] = make_float4((float)u[0], (float)u[1], (float)u[2], (float)u[3]);
+    if (!(u[0] > 0.0) || !(u[1] > 0.0)) atomicOr(err, ERR_NONPHYS);
+}
+void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy) {
+    k_lusgs_update<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.dW, d.W, d.U, fp32_copy ? d.Uf : nullptr, d.err);
+    *L.counter += 1;
+}
+
+// W = cons(U) (TopologyHolderStrategy::initializeConsData, .cpp:48-66)
+__global__ void k_cons_from_prim(int begin, int end, const d4* __restrict__ U, d4* __restrict__ W) {
+    int c = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= end) return;
+    double u[4], w[4];
+    to_arr(ld4(U + c), u);
+    cons_from_prim<double>(u, w);
+    st4(W + c, d4{w[0], w[1], w[2], w[3]});
+}
+void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end) {
+    if (end <= begin) return;
+    k_cons_from_prim<<<nblk(end - begin, 256), 256, 0, L.stream>>>(begin, end, d.U, d.W);
+    *L.counter += 1;
+}
+
+// dt = CFL*vol/spec_c (Euler2D::SolveTime / ViscousFlow2D::SolveTime laminar branch)
+template <class T>
+__global__ void k_local_dt(int nc, const d4* __restrict__ cgeo, const T* __restrict__ specc, double cfl,
+                           double* __restrict__ dt) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    dt[c] = cfl * cgeo[c].x / (double)specc[c];
+}
+void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, bool fp32) {
+    if (fp32) k_local_dt<float><<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.cgeo, d.speccf, cfl, d.dt);
+    else k_local_dt<double><<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.cgeo, d.specc, cfl, d.dt);
+    *L.counter += 1;
+}
+
+}  // namespace cfdgb
