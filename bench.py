@@ -243,7 +243,8 @@ def run_ours(args):
     mesh = abi.Mesh.load_grd(path, w.mesh.wall_tag, w.mesh.far_tag)
     fp32 = args.precision == "fp32"
     viscous = w.flow == "laminar"
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # a real stream: graph capture is not allowed on the legacy default stream
+    torch.cuda.set_stream(stream)
     case = abi.Case([mesh], [dict(mach=w.mach, aoa_deg=w.aoa, reynolds=w.re)],
                     abi.FLOW_LAMINAR if viscous else abi.FLOW_EULER,
                     abi.ADV_LUSGS if w.advance == "lusgs" else abi.ADV_RK5,
