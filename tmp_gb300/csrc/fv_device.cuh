@@ -135,7 +135,9 @@ __device__ __forceinline__ unsigned boundary_state(int bc, bool viscous, const T
         } else {
             T vnl = dot2(ul[2], ul[3], nx, ny);
             T t0 = ul[2] - nx * vnl, t1 = ul[3] - ny * vnl;
-            if (dot2(t0, t1, nx, ny) > T(1.0e-7)) err |= ERR_WALLTAN;
+            // binary64: the reference's absolute bound; binary32: scaled to its rounding
+            T wtol = sizeof(T) == 8 ? T(1.0e-7) : T(1.0e-4) * (dabs(t0) + dabs(t1) + T(1));
+            if (dot2(t0, t1, nx, ny) > wtol) err |= ERR_WALLTAN;
             ue[0] = ul[0]; ue[1] = ul[1]; ue[2] = t0; ue[3] = t1;
         }
         return err;
