@@ -69,6 +69,9 @@ struct DevArrays {
     float* muef = nullptr;
     float4* Fcf = nullptr;
     float4* Fvf = nullptr;
+    // LU-SGS per-step constants of SolveDF for every (cell, face slot)
+    double* swfc = nullptr;      // [16*nc] F_c(W_j)[m] at (i*4+s)*4+m
+    double* swra = nullptr;      // [4*nc]  r_A at i*4+s
     // LU-SGS level schedule (all meshes merged level by level)
     int* fwd_order = nullptr;
     int* bwd_order = nullptr;
@@ -92,6 +95,8 @@ void launch_geometry(const DevArrays& d, const LaunchCfg& L);
 void launch_residual_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);
 void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bool forward, int begin, int end, bool fp32);
+void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32);
+void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, int begin, int end);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
 void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);
 void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, bool fp32);

@@ -110,7 +110,7 @@ void free_case(cfd_case_s* c) {
                     d.cgeo, d.fg0, d.fg1, d.fvis, d.walld, d.fg0f, d.fg1f, d.fvisf, d.cgeof, d.U, d.W, d.W0, d.R,
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
-                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
+                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -144,16 +144,30 @@ void rk_step(cfd_case_s* c) {
     }
 }
 
+// Forward or backward sweep over all levels.  sweep_mode 1 keeps one thread per
+// cell (the direct form); otherwise the per-step SolveDF constants are computed
+// once (before the forward sweep) and each level runs 16 lanes per cell.
+void sweeps(cfd_case_s* c, bool forward) {
+    auto L = c->L();
+    const DevArrays& d = c->d;
+    const std::vector<int>& ptr = forward ? d.fwd_ptr : d.bwd_ptr;
+    if (c->p.sweep_mode == 1) {
+        for (size_t k = 0; k + 1 < ptr.size(); k++)
+            launch_sweep_level(d, L, c->viscous(), forward, ptr[k], ptr[k + 1], c->fp32());
+        return;
+    }
+    if (forward) launch_sweep_prep(d, L, c->viscous(), c->fp32());
+    for (size_t k = 0; k + 1 < ptr.size(); k++) launch_sweep16_level(d, L, forward, ptr[k], ptr[k + 1]);
+}
+
 // LUSGSIntegrator::UpdateSerial (LUSGS_Integrator.cpp:228-240).
 void lusgs_step(cfd_case_s* c) {
     residual_pass(c);
     update_pass(c, 2 /*UPD_LUSGS*/, c->p.cfl, 0, 0.0);
     auto L = c->L();
     const DevArrays& d = c->d;
-    for (size_t k = 0; k + 1 < d.fwd_ptr.size(); k++)
-        launch_sweep_level(d, L, c->viscous(), true, d.fwd_ptr[k], d.fwd_ptr[k + 1], c->fp32());
-    for (size_t k = 0; k + 1 < d.bwd_ptr.size(); k++)
-        launch_sweep_level(d, L, c->viscous(), false, d.bwd_ptr[k], d.bwd_ptr[k + 1], c->fp32());
+    sweeps(c, true);
+    sweeps(c, false);
     launch_lusgs_update(d, L, c->fp32());
 }
 
@@ -393,6 +407,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             if (visc) { dalloc(&d.specv, nc); dalloc(&d.gradT, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf); dalloc(&d.Fv, nf); }
         }
         dalloc(&d.fwd_order, nc); dalloc(&d.bwd_order, nc);
+        if (P.advance == CFD_ADV_LUSGS) { dalloc(&d.swfc, 16 * (size_t)nc); dalloc(&d.swra, 4 * (size_t)nc); }
         dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
         dalloc(&d.err, 1);
         cudaStream_t s = c->stream;
@@ -585,14 +600,8 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
             case 1: launch_pass(d, L, visc, f32, 1, c->p.first_order); break;  // cell_grad
             case 2: launch_pass(d, L, visc, f32, 2, c->p.first_order); break;  // face_flux
             case 3: update_pass(c, c->p.advance == CFD_ADV_RK5 ? 0 : 2, c->p.cfl, 0, 0.0); break;
-            case 4:
-                for (size_t k = 0; k + 1 < d.fwd_ptr.size(); k++)
-                    launch_sweep_level(d, L, visc, true, d.fwd_ptr[k], d.fwd_ptr[k + 1], f32);
-                break;
-            case 5:
-                for (size_t k = 0; k + 1 < d.bwd_ptr.size(); k++)
-                    launch_sweep_level(d, L, visc, false, d.bwd_ptr[k], d.bwd_ptr[k + 1], f32);
-                break;
+            case 4: sweeps(c, true); break;   // includes the SolveDF constant pass
+            case 5: sweeps(c, false); break;
             case 6: launch_lusgs_update(d, L, f32); break;
             case 7: one_step(c); break;
         }

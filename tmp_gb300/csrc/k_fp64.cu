@@ -256,6 +256,132 @@ void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bo
     else sweep_t<double>(d, L, viscous, forward, begin, end, d.mu);
 }
 
+// ---------------------------------------------------------------------------
+// Fast sweeps.  Within one LU-SGS step W, U, mu and the geometry are fixed, so
+// the parts of SolveDF that do not depend on the neighbour's increment -
+// F_c(W_j) and r_A (SolveViscousFlux) - are computed for every (cell, face slot)
+// in one fully parallel pass.  The level kernel then only evaluates
+// F_c(W_j + dW_j) and the combination, with 16 lanes per cell (4 face slots x
+// 4 equations) so that a cell's dependent binary64 chain is one face long.
+// The four slot contributions are added in slot (= ascending face) order
+// starting from 0, exactly as the reference's loop, so results are unchanged.
+
+// swfc[(i*4+s)*4+m] = F_c(W_j)[m] (ConservativeParam2ConvectiveFlux), swra[i*4+s] = r_A
+template <bool VISC, class MuT>
+__global__ void __launch_bounds__(256) k_sweep_prep(int nc, const int4* __restrict__ cface, const int2* __restrict__ lr,
+                                                    const d4* __restrict__ fg0, const d4* __restrict__ fvis,
+                                                    const d4* __restrict__ W, const d4* __restrict__ U,
+                                                    const MuT* __restrict__ mu, double* __restrict__ swfc,
+                                                    double* __restrict__ swra) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * nc) return;
+    int i = t >> 2, s = t & 3;
+    const double G = 1.4;
+    int code = (&cface[i].x)[s];
+    double fc[4] = {0.0, 0.0, 0.0, 0.0}, rA = 0.0;
+    if (code != 0) {
+        int f = code_face(code);
+        int2 e = lr[f];
+        int j = code > 0 ? e.y : e.x;
+        if (j >= 0) {
+            double w0[4], uj[4];
+            to_arr(ld4(W + j), w0);
+            to_arr(ld4(U + j), uj);
+            d4 g = fg0[f];
+            conv_flux_w<double>(w0, g.x, g.y, fc);
+            double vn = dot2(uj[2], uj[3], g.x, g.y);
+            double c = sqrt(G * uj[1] / uj[0]);
+            rA = 1.5 * (fabs(vn) + c);
+            if (VISC) rA += smax(4 / (3 * uj[0]), G / uj[0]) * ((double)mu[i] / 0.72) / sqrt(fvis[f].z);
+        }
+    }
+    st4(reinterpret_cast<d4*>(swfc) + t, d4{fc[0], fc[1], fc[2], fc[3]});
+    swra[t] = rA;
+}
+
+template <bool FWD>
+__global__ void __launch_bounds__(64) k_sweep16(int begin, int end, const int* __restrict__ order,
+                                                const int4* __restrict__ cface, const int2* __restrict__ lr,
+                                                const d4* __restrict__ fg0, const d4* __restrict__ W,
+                                                const double* __restrict__ swfc, const double* __restrict__ swra,
+                                                const d4* __restrict__ R, const double* __restrict__ D, d4* dW1,
+                                                d4* dW) {
+    const double GM1 = 1.4 - 1.0;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane = threadIdx.x & 31;
+    int s = (lane >> 2) & 3, m = lane & 3;
+    int idx = begin + (t >> 4);
+    bool active = idx < end;
+    int i = active ? order[idx] : 0;
+    int4 cf = active ? cface[i] : make_int4(0, 0, 0, 0);
+    int code = s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w;
+    double DF = 0.0;
+    if (active && code != 0) {
+        int f = code_face(code);
+        bool left = code > 0;
+        int2 e = lr[f];
+        int j = left ? e.y : e.x;
+        bool use = FWD ? (j >= 0 && j < i) : (j > i);
+        if (use) {
+            double w0[4], dw[4], wp[4];
+            to_arr(ld4(W + j), w0);
+            to_arr(ld4((FWD ? dW1 : dW) + j), dw);
+#pragma unroll
+            for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
+            d4 g = fg0[f];
+            double u = wp[2] / wp[0], v = wp[3] / wp[0];
+            double vn = dot2(u, v, g.x, g.y);
+            double p = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
+            double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + p) * vn : m == 2 ? wp[2] * vn + p * g.x
+                                                                                   : wp[3] * vn + p * g.y;
+            double fc = swfc[(size_t)i * 16 + s * 4 + m];
+            double rA = swra[(size_t)i * 4 + s];
+            double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
+            double fv = rA * dwm;
+            double dfc = left ? (fcp - fc) : (fc - fcp);
+            DF = 0.5 * (dfc - fv) * g.z;
+        }
+    }
+    // ordered sum over the cell's face slots (lanes m, m+4, m+8, m+12 of its 16-lane group)
+    int base = lane & 16;
+    double v0 = __shfl_sync(0xffffffffu, DF, base + m);
+    double v1 = __shfl_sync(0xffffffffu, DF, base + 4 + m);
+    double v2 = __shfl_sync(0xffffffffu, DF, base + 8 + m);
+    double v3 = __shfl_sync(0xffffffffu, DF, base + 12 + m);
+    if (!active || s != 0) return;
+    double dF = 0.0;
+    if (cf.x != 0) dF += v0;
+    if (cf.y != 0) dF += v1;
+    if (cf.z != 0) dF += v2;
+    if (cf.w != 0) dF += v3;
+    double Di = D[i];
+    double* out = reinterpret_cast<double*>(FWD ? dW1 : dW) + (size_t)i * 4 + m;
+    if (FWD) *out = (-(&R[i].x)[m] - dF) / Di;
+    else *out = (&dW1[i].x)[m] - dF / Di;
+}
+
+void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32) {
+    int n = 4 * d.nc;
+    if (viscous) {
+        if (fp32) k_sweep_prep<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.muf, d.swfc, d.swra);
+        else k_sweep_prep<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.mu, d.swfc, d.swra);
+    } else {
+        k_sweep_prep<false, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, (const double*)nullptr, d.swfc, d.swra);
+    }
+    *L.counter += 1;
+}
+
+void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, int begin, int end) {
+    int n = end - begin;
+    if (n <= 0) return;
+    int threads = 16 * n;
+    if (forward)
+        k_sweep16<true><<<nblk(threads, 64), 64, 0, L.stream>>>(begin, end, d.fwd_order, d.cface, d.lr, d.fg0, d.W, d.swfc, d.swra, d.R, d.diag, d.dW1, d.dW);
+    else
+        k_sweep16<false><<<nblk(threads, 64), 64, 0, L.stream>>>(begin, end, d.bwd_order, d.cface, d.lr, d.fg0, d.W, d.swfc, d.swra, d.R, d.diag, d.dW1, d.dW);
+    *L.counter += 1;
+}
+
 // W += dW, U = prim(W)  (LUSGSIntegrator::UpdatePrimitiveVariable, LUSGS_Integrator.cpp:242-255)
 __global__ void k_lusgs_update(int nc, const d4* __restrict__ dW, d4* __restrict__ W, d4* __restrict__ U,
                                float4* __restrict__ Uf, unsigned* __restrict__ err) {
