@@ -168,6 +168,19 @@ long long cfd_launch_count(cfd_case_t c);
  * (all levels), 5 backward sweep (all levels), 6 LU-SGS update, 7 whole step. */
 int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms);
 
+/* Residual norm of a caller-owned device array that allocates nothing (no
+ * counterpart in the reference, which has no device code).  For callers that
+ * may not allocate device memory while they run: solvers that reserve all of
+ * it at start-up, hosts whose memory pool owns the device, or a time loop
+ * being captured into a CUDA graph.  d_records: n records of 4 doubles
+ * ([4*cell + eq], component 0 is reduced); which: CFD_NORM_DW_RHO2 (sum x^2) or
+ * CFD_NORM_L2_R_RHO (sqrt(sum x^2 / n)); the result is written to d_out[0] on
+ * the device, asynchronously on `stream`.  The scratch is a static 32 KiB
+ * device array shared by all calls: n is limited to 33,554,432 records
+ * (CFD_ERR_ARG beyond), overlapping calls race, and the first call on each
+ * device looks up the array's address (make it before any stream capture). */
+int cfd_residual_norm_noalloc(const double* d_records, int n, int which, double* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -74,6 +74,11 @@ MeshPrm make_prm(const cfd_freestream_t& fs, bool viscous) {
 
 }  // namespace
 
+namespace cfdgb {
+// Lets other translation units report through cfd_last_error().
+int set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace cfdgb
+
 struct cfd_mesh_s {
     HostMesh m;
 };
