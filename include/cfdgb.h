@@ -167,6 +167,11 @@ long long cfd_launch_count(cfd_case_t c);
  * pass: 0 face_state, 1 cell_grad, 2 face_flux, 3 cell_update, 4 forward sweep
  * (all levels), 5 backward sweep (all levels), 6 LU-SGS update, 7 whole step. */
 int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms);
+/* Failure-detection self-test (no reference counterpart): launch a kernel that
+ * waits, at most `polls` polls, on a device flag nothing sets, exactly as the
+ * dataflow LU-SGS sweep waits on its neighbours.  Returns CFD_ERR_TIMEOUT when
+ * the bounded wait gave up (the expected outcome) and leaves the case usable. */
+int cfd_selftest_bounded_wait(cfd_case_t c, long long polls);
 
 /* Residual norm of a caller-owned device array that allocates nothing (no
  * counterpart in the reference, which has no device code).  For callers that

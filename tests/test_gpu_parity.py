@@ -217,3 +217,64 @@ def test_nonphysical_state_is_reported():
     case.put("U", g["init_U"])
     case.step(1)
     case.norm("DW_RHO2")
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_sweep_schedules_agree_bitwise(mode):
+    """The dataflow sweep (default), per-level 16-lane and per-level direct sweeps
+    give identical bits: all three keep the reference's dependence exactly."""
+    from tmp_gb300 import abi
+
+    c, g = manifest()["mixed_lam_lusgs"], golden("mixed_lam_lusgs")
+    m = abi.Mesh.load_grd(GOLDEN / c["mesh"], c["wall_tag"], c["far_tag"])
+    out = []
+    for sm in (0, mode):
+        case = abi.Case([m], [dict(mach=c["mach"], aoa_deg=c["aoa"], reynolds=c["re"])], abi.FLOW_LAMINAR,
+                        abi.ADV_LUSGS, abi.PREC_FP64, cfl=c["cfl"], sweep_mode=sm)
+        case.put("U", g["init_U"])
+        case.step(3)
+        case.sync()
+        out.append((case.get("U"), case.get("DW1"), case.get("DW")))
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["mixed_lam_lusgs", "omesh_euler_lusgs"])
+def test_fp32_form_lusgs_steps(name):
+    """Fast form (binary32 fluxes and sweep combination, binary64 update): fields
+    after the fixture's steps within 1e-4 of the binary64 reference."""
+    from tmp_gb300 import abi
+
+    c, g = manifest()[name], golden(name)
+    _, case = make_case(c, precision=abi.PREC_FP32)
+    case.put("U", g["init_U"])
+    case.step(c["nsteps"])
+    case.sync()
+    assert rel(case.get("U"), g["end_U"]) <= 1e-4
+
+
+def test_bounded_wait_reports_timeout_and_context_survives():
+    """A device wait on a flag nothing sets gives up after its poll limit, the
+    host reads CFD_ERR_TIMEOUT, and the same case keeps working (no GPU fault)."""
+    from tmp_gb300 import abi
+
+    c, g = manifest()["omesh_euler_lusgs"], golden("omesh_euler_lusgs")
+    _, case = make_case(c)
+    rc = abi.lib().cfd_selftest_bounded_wait(case.h, 1 << 16)
+    assert rc == -7
+    case.put("U", g["init_U"])
+    case.step(1)
+    assert case.norm("DW_RHO2") > 0
+
+
+def test_graph_replay_dataflow_epochs():
+    """Graph replays of the dataflow sweep use fresh epochs each time (the epoch
+    lives in device memory): 5 replays equal 5 eager steps bit for bit."""
+    c, g = manifest()["omesh_euler_lusgs"], golden("omesh_euler_lusgs")
+    _, a = make_case(c)
+    _, b = make_case(c)
+    a.put("U", g["init_U"])
+    b.put("U", g["init_U"])
+    a.step(5)
+    b.step_graph(5)
+    np.testing.assert_array_equal(a.get("U"), b.get("U"))

@@ -89,6 +89,7 @@ def lib() -> C.CDLL:
         "cfd_sync": (C.c_int, [vp]),
         "cfd_launch_count": (C.c_longlong, [vp]),
         "cfd_bench_pass": (C.c_int, [vp, C.c_int, C.c_int, C.c_longlong, dp]),
+        "cfd_selftest_bounded_wait": (C.c_int, [vp, C.c_longlong]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

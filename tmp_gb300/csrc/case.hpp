@@ -72,6 +72,10 @@ struct DevArrays {
     // LU-SGS per-step constants of SolveDF for every (cell, face slot)
     double* swfc = nullptr;      // [16*nc] F_c(W_j)[m] at (i*4+s)*4+m
     double* swra = nullptr;      // [4*nc]  r_A at i*4+s
+    double* invD = nullptr;      // [nc] 1/D (fast form's sweep)
+    unsigned* ready = nullptr;   // [nc] dataflow sweep: epoch at which the cell's increment is final
+    unsigned* epoch = nullptr;   // [1]  bumped before every dataflow sweep
+    int flow_grid = 0;           // co-resident blocks of the dataflow sweep
     // LU-SGS level schedule (all meshes merged level by level)
     int* fwd_order = nullptr;
     int* bwd_order = nullptr;
@@ -81,7 +85,7 @@ struct DevArrays {
     int4* norm_blocks = nullptr;  // (mesh, begin, end, 0) per block
     double* norm_partial = nullptr;
     double* norm_out = nullptr;   // [nmesh]
-    unsigned* err = nullptr;      // device error word
+    unsigned* err = nullptr;      // [2] device error word; err[1] stays 0 (a flag nothing sets)
 };
 
 struct LaunchCfg {
@@ -97,6 +101,10 @@ void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, in
 void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bool forward, int begin, int end, bool fp32);
 void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32);
 void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, int begin, int end);
+cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid);
+int sweep_flow_max_grid(bool low);
+void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
+void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
 void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);
 void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, bool fp32);

@@ -115,7 +115,7 @@ void free_case(cfd_case_s* c) {
                     d.cgeo, d.fg0, d.fg1, d.fvis, d.walld, d.fg0f, d.fg1f, d.fvisf, d.cgeof, d.U, d.W, d.W0, d.R,
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
-                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
+                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.ready, d.epoch, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -162,7 +162,13 @@ void sweeps(cfd_case_s* c, bool forward) {
         return;
     }
     if (forward) launch_sweep_prep(d, L, c->viscous(), c->fp32());
-    for (size_t k = 0; k + 1 < ptr.size(); k++) launch_sweep16_level(d, L, forward, ptr[k], ptr[k + 1]);
+    if (c->p.sweep_mode == 2) {
+        for (size_t k = 0; k + 1 < ptr.size(); k++) launch_sweep16_level(d, L, forward, ptr[k], ptr[k + 1]);
+        return;
+    }
+    // default: one dataflow launch per direction (the fast form uses 1/D)
+    if (forward && c->fp32()) launch_inv_diag(d, L);
+    ck(launch_sweep_flow(d, L, forward, c->fp32(), d.flow_grid), "cooperative sweep launch");
 }
 
 // LUSGSIntegrator::UpdateSerial (LUSGS_Integrator.cpp:228-240).
@@ -412,9 +418,13 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             if (visc) { dalloc(&d.specv, nc); dalloc(&d.gradT, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf); dalloc(&d.Fv, nf); }
         }
         dalloc(&d.fwd_order, nc); dalloc(&d.bwd_order, nc);
-        if (P.advance == CFD_ADV_LUSGS) { dalloc(&d.swfc, 16 * (size_t)nc); dalloc(&d.swra, 4 * (size_t)nc); }
+        if (P.advance == CFD_ADV_LUSGS) {
+            dalloc(&d.swfc, 16 * (size_t)nc); dalloc(&d.swra, 4 * (size_t)nc); dalloc(&d.invD, nc);
+            dalloc(&d.ready, nc); dalloc(&d.epoch, 1);
+            d.flow_grid = sweep_flow_max_grid(P.precision == CFD_PREC_FP32);
+        }
         dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
-        dalloc(&d.err, 1);
+        dalloc(&d.err, 2);
         cudaStream_t s = c->stream;
         ck(cudaMemcpyAsync(d.lr, lr.data(), nf * sizeof(int2), cudaMemcpyHostToDevice, s), "upload");
         ck(cudaMemcpyAsync(d.enodes, en.data(), nf * sizeof(int2), cudaMemcpyHostToDevice, s), "upload");
@@ -428,10 +438,14 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         ck(cudaMemcpyAsync(d.fwd_order, fo_.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
         ck(cudaMemcpyAsync(d.bwd_order, bo_.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
         ck(cudaMemcpyAsync(d.norm_blocks, nb.data(), nb.size() * sizeof(int4), cudaMemcpyHostToDevice, s), "upload");
-        ck(cudaMemsetAsync(d.err, 0, sizeof(unsigned), s), "memset");
+        ck(cudaMemsetAsync(d.err, 0, 2 * sizeof(unsigned), s), "memset");
         ck(cudaMemsetAsync(d.dW1, 0, nc * sizeof(d4), s), "memset");
         ck(cudaMemsetAsync(d.dW, 0, nc * sizeof(d4), s), "memset");
         ck(cudaMemsetAsync(d.W0, 0, nc * sizeof(d4), s), "memset");
+        if (d.ready) {
+            ck(cudaMemsetAsync(d.ready, 0, nc * sizeof(unsigned), s), "memset");
+            ck(cudaMemsetAsync(d.epoch, 0, sizeof(unsigned), s), "memset");
+        }
         auto L = c->L();
         launch_geometry(d, L);
         if (c->fp32()) launch_to_fp32(d, L, true);
@@ -583,6 +597,15 @@ int cfd_sync(cfd_case_t c) {
 }
 
 long long cfd_launch_count(cfd_case_t c) { return c ? c->launches : -1; }
+
+int cfd_selftest_bounded_wait(cfd_case_t c, long long polls) {
+    if (!c || polls <= 0) return fail(CFD_ERR_ARG, "null case or non-positive poll count");
+    ABI_TRY
+    launch_wait_selftest(c->d, c->L(), polls);
+    ck(cudaGetLastError(), "self-test launch");
+    return check_errors(c);
+    ABI_CATCH
+}
 
 int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms) {
     if (!c || !avg_ms || reps <= 0) return fail(CFD_ERR_ARG, "null argument or reps <= 0");

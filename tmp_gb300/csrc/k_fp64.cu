@@ -382,6 +382,186 @@ void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, 
     *L.counter += 1;
 }
 
+// ---------------------------------------------------------------------------
+// Dataflow sweep: one persistent cooperative launch per sweep direction.
+// Cells are taken in level order (position p = g, g + G, ... for 16-lane group
+// g of G); a cell waits only for its own lower (forward) / upper (backward)
+// face neighbours, each of which publishes its finished increment with a
+// release store of the sweep's epoch into ready[j].  Every dependency sits at
+// an earlier position, all groups are resident (cooperative launch), and each
+// group finishes its positions in order, so the earliest unfinished cell can
+// always proceed.  Every wait is bounded: after kSpinLimit polls the kernel
+// raises ERR_TIMEOUT and goes on, so it always terminates.
+// The epoch lives in device memory and is bumped by a one-thread kernel before
+// each sweep, so graph replays use fresh epochs and the flags never need
+// clearing.  LOW selects the fast form: the SolveDF combination in binary32,
+// the sum widened, and dW = (-R - sum) * (1/D) with 1/D from binary64.
+constexpr long long kSpinLimit = 1LL << 22;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Spin until *flag == want, at most `limit` polls; on give-up raise ERR_TIMEOUT
+// and return false (the caller goes on, so the kernel always terminates).
+__device__ __forceinline__ bool bounded_wait(const unsigned* flag, unsigned want, long long limit, unsigned* err) {
+    long long it = 0;
+    while (ld_acquire_u32(flag) != want) {
+        if (++it > limit) {
+            atomicOr(err, ERR_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
+
+__global__ void k_bump_epoch(unsigned* epoch) { epoch[0] += 1u; }
+
+// Self-test of the bounded wait: waits on a flag nothing sets.
+__global__ void k_wait_selftest(const unsigned* flag, long long limit, unsigned* err) {
+    bounded_wait(flag, 0xffffffffu, limit, err);
+}
+void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit) {
+    k_wait_selftest<<<1, 32, 0, L.stream>>>(d.err + 1, limit, d.err);
+    *L.counter += 1;
+}
+
+template <bool FWD, bool LOW>
+__global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restrict__ order,
+                                                    const int4* __restrict__ cface, const int2* __restrict__ lr,
+                                                    const d4* __restrict__ fg0, const d4* __restrict__ W,
+                                                    const double* __restrict__ swfc, const double* __restrict__ swra,
+                                                    const d4* __restrict__ R, const double* __restrict__ D,
+                                                    const double* __restrict__ invD, d4* dW1, d4* dW,
+                                                    unsigned* ready, const unsigned* __restrict__ epoch,
+                                                    unsigned* err) {
+    const double GM1 = 1.4 - 1.0;
+    const int lane = threadIdx.x & 31;
+    const int half = lane & 16;
+    const unsigned hmask = 0xffffu << half;
+    const int s = (lane >> 2) & 3, m = lane & 3;
+    const int G = (gridDim.x * blockDim.x) >> 4;
+    const unsigned ep = epoch[0];
+    d4* dst = FWD ? dW1 : dW;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 4; p < nc; p += G) {
+        const int i = order[p];
+        const int4 cf = cface[i];
+        const int code = s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w;
+        double DF = 0.0;
+        if (code != 0) {
+            int f = code_face(code);
+            bool left = code > 0;
+            int2 e = lr[f];
+            int j = left ? e.y : e.x;
+            bool use = FWD ? (j >= 0 && j < i) : (j > i);
+            if (use) {
+                // independent of the neighbour's increment: load before waiting
+                double w0[4];
+                to_arr(ld4(W + j), w0);
+                d4 g = fg0[f];
+                double fc = swfc[(size_t)i * 16 + s * 4 + m];
+                double rA = swra[(size_t)i * 4 + s];
+                bounded_wait(ready + j, ep, kSpinLimit, err);
+                const double2* q = reinterpret_cast<const double2*>(dst + j);
+                double2 a = __ldcg(q), b = __ldcg(q + 1);
+                double dw[4] = {a.x, a.y, b.x, b.y};
+                double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
+                if (LOW) {
+                    float wp0 = (float)(w0[0] + dw[0]), wp1 = (float)(w0[1] + dw[1]);
+                    float wp2 = (float)(w0[2] + dw[2]), wp3 = (float)(w0[3] + dw[3]);
+                    float nx = (float)g.x, ny = (float)g.y;
+                    float u = wp2 / wp0, v = wp3 / wp0;
+                    float vn = u * nx + v * ny;
+                    float pr = (1.4f - 1.0f) * (wp1 - 0.5f * wp0 * (u * u + v * v));
+                    float fcp = m == 0 ? wp0 * vn : m == 1 ? (wp1 + pr) * vn : m == 2 ? wp2 * vn + pr * nx
+                                                                                      : wp3 * vn + pr * ny;
+                    float dfc = left ? (fcp - (float)fc) : ((float)fc - fcp);
+                    DF = (double)(0.5f * (dfc - (float)rA * (float)dwm) * (float)g.z);
+                } else {
+                    double wp[4];
+#pragma unroll
+                    for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
+                    double u = wp[2] / wp[0], v = wp[3] / wp[0];
+                    double vn = dot2(u, v, g.x, g.y);
+                    double pr = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
+                    double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + pr) * vn : m == 2 ? wp[2] * vn + pr * g.x
+                                                                                           : wp[3] * vn + pr * g.y;
+                    double dfc = left ? (fcp - fc) : (fc - fcp);
+                    DF = 0.5 * (dfc - rA * dwm) * g.z;
+                }
+            }
+        }
+        // ordered sum over the 4 face slots of this half-warp's cell
+        double v0 = __shfl_sync(hmask, DF, half + m);
+        double v1 = __shfl_sync(hmask, DF, half + 4 + m);
+        double v2 = __shfl_sync(hmask, DF, half + 8 + m);
+        double v3 = __shfl_sync(hmask, DF, half + 12 + m);
+        double dF = 0.0;
+        if (cf.x != 0) dF += v0;
+        if (cf.y != 0) dF += v1;
+        if (cf.z != 0) dF += v2;
+        if (cf.w != 0) dF += v3;
+        double res;
+        if (FWD) {
+            double r = (&R[i].x)[m];
+            res = LOW ? (-r - dF) * invD[i] : (-r - dF) / D[i];
+        } else {
+            double a1 = (&dW1[i].x)[m];
+            res = LOW ? a1 - dF * invD[i] : a1 - dF / D[i];
+        }
+        double r1 = __shfl_sync(hmask, res, half + 1);
+        double r2 = __shfl_sync(hmask, res, half + 2);
+        double r3 = __shfl_sync(hmask, res, half + 3);
+        if ((lane & 15) == 0) {
+            st4(dst + i, d4{res, r1, r2, r3});
+            st_release_u32(ready + i, ep);
+        }
+    }
+}
+
+cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid) {
+    k_bump_epoch<<<1, 1, 0, L.stream>>>(d.epoch);
+    int nc = d.nc;
+    const int* order = forward ? d.fwd_order : d.bwd_order;
+    void* args[] = {(void*)&nc, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0, (void*)&d.W,
+                    (void*)&d.swfc, (void*)&d.swra, (void*)&d.R, (void*)&d.diag, (void*)&d.invD, (void*)&d.dW1,
+                    (void*)&d.dW, (void*)&d.ready, (void*)&d.epoch, (void*)&d.err};
+    void* fn;
+    if (forward) fn = low ? (void*)k_sweep_flow<true, true> : (void*)k_sweep_flow<true, false>;
+    else fn = low ? (void*)k_sweep_flow<false, true> : (void*)k_sweep_flow<false, false>;
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
+    *L.counter += 2;
+    return e;
+}
+
+int sweep_flow_max_grid(bool low) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void* fn = low ? (void*)k_sweep_flow<true, true> : (void*)k_sweep_flow<true, false>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
+    int per2 = 0;
+    void* fn2 = low ? (void*)k_sweep_flow<false, true> : (void*)k_sweep_flow<false, false>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, fn2, 256, 0);
+    per = per < per2 ? per : per2;
+    return sms * (per > 0 ? per : 1);
+}
+
+// 1/D for the fast form's sweep (binary64)
+__global__ void k_inv_diag(int nc, const double* __restrict__ D, double* __restrict__ invD) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < nc) invD[c] = 1.0 / D[c];
+}
+void launch_inv_diag(const DevArrays& d, const LaunchCfg& L) {
+    k_inv_diag<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.diag, d.invD);
+    *L.counter += 1;
+}
+
 // W += dW, U = prim(W)  (LUSGSIntegrator::UpdatePrimitiveVariable, LUSGS_Integrator.cpp:242-255)
 __global__ void k_lusgs_update(int nc, const d4* __restrict__ dW, d4* __restrict__ W, d4* __restrict__ U,
                                float4* __restrict__ Uf, unsigned* __restrict__ err) {
