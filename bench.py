@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--sweep-mode", type=int, default=0, help="LU-SGS schedule (0 dataflow, 1/2 per level)")
+    ap.add_argument("--sweep-bpsm", type=int, default=0, help="dataflow sweep blocks per SM (0 = default)")
     return ap.parse_args()
 
 
@@ -248,7 +250,8 @@ def run_ours(args):
     case = abi.Case([mesh], [dict(mach=w.mach, aoa_deg=w.aoa, reynolds=w.re)],
                     abi.FLOW_LAMINAR if viscous else abi.FLOW_EULER,
                     abi.ADV_LUSGS if w.advance == "lusgs" else abi.ADV_RK5,
-                    abi.PREC_FP32 if fp32 else abi.PREC_FP64, cfl=w.cfl, stream=stream.cuda_stream)
+                    abi.PREC_FP32 if fp32 else abi.PREC_FP64, cfl=w.cfl, stream=stream.cuda_stream,
+                    sweep_mode=args.sweep_mode, sweep_blocks_per_sm=args.sweep_bpsm)
     case.init_freestream()
     nc, nf = case.ncell, case.nedge
     U0 = case.get("U").copy()

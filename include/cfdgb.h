@@ -93,8 +93,12 @@ typedef struct {
     int precision;     /* CFD_PREC_*                                              */
     int first_order;   /* 1: limiter forced to 0 (piecewise-constant faces)       */
     double cfl;        /* LU-SGS CFL (LUSGSIntegrator::d_CFL_number); RK uses 0.8 */
-    int sweep_mode;    /* 0: auto, 1: one launch per level, 2: persistent cluster */
-    int reserved[7];
+    int sweep_mode;    /* LU-SGS schedule: 0 dataflow (one cooperative launch per sweep),
+                          1 one launch per level, one thread per cell,
+                          2 one launch per level, 16 lanes per cell               */
+    int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
+                                the occupancy limit)                             */
+    int reserved[6];
 } cfd_params_t;
 
 /* ---- errors -------------------------------------------------------------- */

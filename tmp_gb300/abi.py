@@ -45,7 +45,8 @@ class Freestream(C.Structure):
 
 class Params(C.Structure):
     _fields_ = [("flow", C.c_int), ("advance", C.c_int), ("precision", C.c_int), ("first_order", C.c_int),
-                ("cfl", C.c_double), ("sweep_mode", C.c_int), ("reserved", C.c_int * 7)]
+                ("cfl", C.c_double), ("sweep_mode", C.c_int), ("sweep_blocks_per_sm", C.c_int),
+                ("reserved", C.c_int * 6)]
 
 
 _lib = None
@@ -163,13 +164,13 @@ class Case:
 
     def __init__(self, meshes: Sequence[Mesh], freestreams: Sequence[dict], flow: int, advance: int,
                  precision: int = PREC_FP64, cfl: float = 1.0, first_order: bool = False, stream: int | None = None,
-                 sweep_mode: int = 0):
+                 sweep_mode: int = 0, sweep_blocks_per_sm: int = 0):
         self.meshes = list(meshes)
         arr = (C.c_void_p * len(meshes))(*[m.h.value for m in meshes])
         fs = (Freestream * len(meshes))(*[Freestream(f["mach"], f.get("aoa_deg", 0.0), f.get("reynolds", 1.0),
                                                      f.get("density", 1.225), f.get("pressure", 101325.0))
                                           for f in freestreams])
-        p = Params(flow, advance, precision, int(first_order), float(cfl), int(sweep_mode))
+        p = Params(flow, advance, precision, int(first_order), float(cfl), int(sweep_mode), int(sweep_blocks_per_sm))
         h = C.c_void_p()
         check(lib().cfd_case_create(arr, len(meshes), fs, C.byref(p), C.c_void_p(stream) if stream else None,
                                     C.byref(h)))

@@ -102,7 +102,7 @@ void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bo
 void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32);
 void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, int begin, int end);
 cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid);
-int sweep_flow_max_grid(bool low);
+int sweep_flow_max_grid(bool low, int blocks_per_sm);
 void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
 void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);

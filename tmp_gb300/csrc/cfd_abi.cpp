@@ -421,7 +421,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         if (P.advance == CFD_ADV_LUSGS) {
             dalloc(&d.swfc, 16 * (size_t)nc); dalloc(&d.swra, 4 * (size_t)nc); dalloc(&d.invD, nc);
             dalloc(&d.ready, nc); dalloc(&d.epoch, 1);
-            d.flow_grid = sweep_flow_max_grid(P.precision == CFD_PREC_FP32);
+            d.flow_grid = sweep_flow_max_grid(P.precision == CFD_PREC_FP32, P.sweep_blocks_per_sm);
         }
         dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
         dalloc(&d.err, 2);

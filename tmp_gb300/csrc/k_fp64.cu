@@ -403,6 +403,12 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -440,84 +446,110 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
                                                     const double* __restrict__ invD, d4* dW1, d4* dW,
                                                     unsigned* ready, const unsigned* __restrict__ epoch,
                                                     unsigned* err) {
+    // One warp per cell.  Lanes 0..15: (face slot s, equation m); lanes 16..31
+    // mirror them and only help with the divide (v = w3/w0 beside u = w2/w0).
     const double GM1 = 1.4 - 1.0;
     const int lane = threadIdx.x & 31;
-    const int half = lane & 16;
-    const unsigned hmask = 0xffffu << half;
+    const int hv = lane >> 4;
     const int s = (lane >> 2) & 3, m = lane & 3;
-    const int G = (gridDim.x * blockDim.x) >> 4;
+    const int warp = threadIdx.x >> 5;
+    const int B = gridDim.x, NW = blockDim.x >> 5;
+    const long long G = (long long)B * NW;
     const unsigned ep = epoch[0];
     d4* dst = FWD ? dW1 : dW;
-    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 4; p < nc; p += G) {
+    // position p = k*G + warp*B + block: consecutive positions (one level's
+    // cells) go to consecutive blocks, i.e. to different SMs
+    for (long long p = (long long)warp * B + blockIdx.x; p < nc; p += G) {
         const int i = order[p];
         const int4 cf = cface[i];
         const int code = s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w;
-        double DF = 0.0;
+        bool use = false, left = false;
+        int f = 0, j = 0;
         if (code != 0) {
-            int f = code_face(code);
-            bool left = code > 0;
+            f = code_face(code);
+            left = code > 0;
             int2 e = lr[f];
-            int j = left ? e.y : e.x;
-            bool use = FWD ? (j >= 0 && j < i) : (j > i);
-            if (use) {
-                // independent of the neighbour's increment: load before waiting
-                double w0[4];
-                to_arr(ld4(W + j), w0);
-                d4 g = fg0[f];
-                double fc = swfc[(size_t)i * 16 + s * 4 + m];
-                double rA = swra[(size_t)i * 4 + s];
-                bounded_wait(ready + j, ep, kSpinLimit, err);
-                const double2* q = reinterpret_cast<const double2*>(dst + j);
-                double2 a = __ldcg(q), b = __ldcg(q + 1);
-                double dw[4] = {a.x, a.y, b.x, b.y};
-                double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
-                if (LOW) {
-                    float wp0 = (float)(w0[0] + dw[0]), wp1 = (float)(w0[1] + dw[1]);
-                    float wp2 = (float)(w0[2] + dw[2]), wp3 = (float)(w0[3] + dw[3]);
-                    float nx = (float)g.x, ny = (float)g.y;
-                    float u = wp2 / wp0, v = wp3 / wp0;
-                    float vn = u * nx + v * ny;
-                    float pr = (1.4f - 1.0f) * (wp1 - 0.5f * wp0 * (u * u + v * v));
-                    float fcp = m == 0 ? wp0 * vn : m == 1 ? (wp1 + pr) * vn : m == 2 ? wp2 * vn + pr * nx
-                                                                                      : wp3 * vn + pr * ny;
-                    float dfc = left ? (fcp - (float)fc) : ((float)fc - fcp);
-                    DF = (double)(0.5f * (dfc - (float)rA * (float)dwm) * (float)g.z);
-                } else {
-                    double wp[4];
-#pragma unroll
-                    for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
-                    double u = wp[2] / wp[0], v = wp[3] / wp[0];
-                    double vn = dot2(u, v, g.x, g.y);
-                    double pr = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
-                    double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + pr) * vn : m == 2 ? wp[2] * vn + pr * g.x
-                                                                                           : wp[3] * vn + pr * g.y;
-                    double dfc = left ? (fcp - fc) : (fc - fcp);
-                    DF = 0.5 * (dfc - rA * dwm) * g.z;
+            j = left ? e.y : e.x;
+            use = FWD ? (j >= 0 && j < i) : (j > i);
+        }
+        double w0[4] = {0.0, 0.0, 0.0, 0.0}, dw[4] = {0.0, 0.0, 0.0, 0.0};
+        d4 g = d4{0.0, 0.0, 0.0, 0.0};
+        double fc = 0.0, rA = 0.0;
+        if (use) {
+            // independent of the neighbour's increment: load before waiting
+            to_arr(ld4(W + j), w0);
+            g = fg0[f];
+            fc = swfc[(size_t)i * 16 + s * 4 + m];
+            rA = swra[(size_t)i * 4 + s];
+            long long it = 0;
+            while (ld_relaxed_u32(ready + j) != ep) {
+                if (++it > kSpinLimit) {
+                    atomicOr(err, ERR_TIMEOUT);
+                    break;
                 }
             }
+            fence_acq_rel_gpu();
+            const double2* q = reinterpret_cast<const double2*>(dst + j);
+            double2 a = __ldcg(q), b = __ldcg(q + 1);
+            dw[0] = a.x; dw[1] = a.y; dw[2] = b.x; dw[3] = b.y;
         }
-        // ordered sum over the 4 face slots of this half-warp's cell
-        double v0 = __shfl_sync(hmask, DF, half + m);
-        double v1 = __shfl_sync(hmask, DF, half + 4 + m);
-        double v2 = __shfl_sync(hmask, DF, half + 8 + m);
-        double v3 = __shfl_sync(hmask, DF, half + 12 + m);
+        double DF = 0.0;
+        if (LOW) {
+            float wp0 = (float)(w0[0] + dw[0]), wp1 = (float)(w0[1] + dw[1]);
+            float wp2 = (float)(w0[2] + dw[2]), wp3 = (float)(w0[3] + dw[3]);
+            if (use) {
+                float nx = (float)g.x, ny = (float)g.y;
+                float u = wp2 / wp0, v = wp3 / wp0;
+                float vn = u * nx + v * ny;
+                float pr = (1.4f - 1.0f) * (wp1 - 0.5f * wp0 * (u * u + v * v));
+                float fcp = m == 0 ? wp0 * vn : m == 1 ? (wp1 + pr) * vn : m == 2 ? wp2 * vn + pr * nx
+                                                                                  : wp3 * vn + pr * ny;
+                float dwm = (float)(m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3]);
+                float dfc = left ? (fcp - (float)fc) : ((float)fc - fcp);
+                DF = (double)(0.5f * (dfc - (float)rA * dwm) * (float)g.z);
+            }
+        } else {
+            double wp[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
+            // one divide per half-warp, exchanged
+            double q = use ? (hv ? wp[3] : wp[2]) / wp[0] : 0.0;
+            double u = __shfl_sync(0xffffffffu, q, lane & 15);
+            double v = __shfl_sync(0xffffffffu, q, (lane & 15) | 16);
+            if (use) {
+                double vn = dot2(u, v, g.x, g.y);
+                double pr = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
+                double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + pr) * vn : m == 2 ? wp[2] * vn + pr * g.x
+                                                                                       : wp[3] * vn + pr * g.y;
+                double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
+                double dfc = left ? (fcp - fc) : (fc - fcp);
+                DF = 0.5 * (dfc - rA * dwm) * g.z;
+            }
+        }
+        // ordered sum over the 4 face slots (lanes m, m+4, m+8, m+12)
+        double v0 = __shfl_sync(0xffffffffu, DF, m);
+        double v1 = __shfl_sync(0xffffffffu, DF, 4 + m);
+        double v2 = __shfl_sync(0xffffffffu, DF, 8 + m);
+        double v3 = __shfl_sync(0xffffffffu, DF, 12 + m);
         double dF = 0.0;
         if (cf.x != 0) dF += v0;
         if (cf.y != 0) dF += v1;
         if (cf.z != 0) dF += v2;
         if (cf.w != 0) dF += v3;
-        double res;
-        if (FWD) {
-            double r = (&R[i].x)[m];
-            res = LOW ? (-r - dF) * invD[i] : (-r - dF) / D[i];
-        } else {
-            double a1 = (&dW1[i].x)[m];
-            res = LOW ? a1 - dF * invD[i] : a1 - dF / D[i];
+        double res = 0.0;
+        if (lane < 4) {
+            if (FWD) {
+                double r = (&R[i].x)[m];
+                res = LOW ? (-r - dF) * invD[i] : (-r - dF) / D[i];
+            } else {
+                double a1 = (&dW1[i].x)[m];
+                res = LOW ? a1 - dF * invD[i] : a1 - dF / D[i];
+            }
         }
-        double r1 = __shfl_sync(hmask, res, half + 1);
-        double r2 = __shfl_sync(hmask, res, half + 2);
-        double r3 = __shfl_sync(hmask, res, half + 3);
-        if ((lane & 15) == 0) {
+        double r1 = __shfl_sync(0xffffffffu, res, 1);
+        double r2 = __shfl_sync(0xffffffffu, res, 2);
+        double r3 = __shfl_sync(0xffffffffu, res, 3);
+        if (lane == 0) {
             st4(dst + i, d4{res, r1, r2, r3});
             st_release_u32(ready + i, ep);
         }
@@ -539,17 +571,18 @@ cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forwa
     return e;
 }
 
-int sweep_flow_max_grid(bool low) {
-    int dev = 0, sms = 0, per = 0;
+int sweep_flow_max_grid(bool low, int blocks_per_sm) {
+    int dev = 0, sms = 0, per = 0, per2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     void* fn = low ? (void*)k_sweep_flow<true, true> : (void*)k_sweep_flow<true, false>;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
-    int per2 = 0;
     void* fn2 = low ? (void*)k_sweep_flow<false, true> : (void*)k_sweep_flow<false, false>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, fn2, 256, 0);
     per = per < per2 ? per : per2;
-    return sms * (per > 0 ? per : 1);
+    if (per < 1) per = 1;
+    int want = blocks_per_sm > 0 ? blocks_per_sm : 2;
+    return sms * (want < per ? want : per);
 }
 
 // 1/D for the fast form's sweep (binary64)
