@@ -73,8 +73,6 @@ struct DevArrays {
     double* swfc = nullptr;      // [16*nc] F_c(W_j)[m] at (i*4+s)*4+m
     double* swra = nullptr;      // [4*nc]  r_A at i*4+s
     double* invD = nullptr;      // [nc] 1/D (fast form's sweep)
-    unsigned* ready = nullptr;   // [nc] dataflow sweep: epoch at which the cell's increment is final
-    unsigned* epoch = nullptr;   // [1]  bumped before every dataflow sweep
     int flow_grid = 0;           // co-resident blocks of the dataflow sweep
     // LU-SGS level schedule (all meshes merged level by level)
     int* fwd_order = nullptr;
@@ -99,7 +97,7 @@ void launch_geometry(const DevArrays& d, const LaunchCfg& L);
 void launch_residual_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);
 void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bool forward, int begin, int end, bool fp32);
-void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32);
+void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32, bool reset);
 void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, int begin, int end);
 cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid);
 int sweep_flow_max_grid(bool low, int blocks_per_sm);

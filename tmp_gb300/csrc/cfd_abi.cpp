@@ -115,7 +115,7 @@ void free_case(cfd_case_s* c) {
                     d.cgeo, d.fg0, d.fg1, d.fvis, d.walld, d.fg0f, d.fg1f, d.fvisf, d.cgeof, d.U, d.W, d.W0, d.R,
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
-                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.ready, d.epoch, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
+                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -161,7 +161,7 @@ void sweeps(cfd_case_s* c, bool forward) {
             launch_sweep_level(d, L, c->viscous(), forward, ptr[k], ptr[k + 1], c->fp32());
         return;
     }
-    if (forward) launch_sweep_prep(d, L, c->viscous(), c->fp32());
+    if (forward) launch_sweep_prep(d, L, c->viscous(), c->fp32(), c->p.sweep_mode == 0);
     if (c->p.sweep_mode == 2) {
         for (size_t k = 0; k + 1 < ptr.size(); k++) launch_sweep16_level(d, L, forward, ptr[k], ptr[k + 1]);
         return;
@@ -420,7 +420,6 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         dalloc(&d.fwd_order, nc); dalloc(&d.bwd_order, nc);
         if (P.advance == CFD_ADV_LUSGS) {
             dalloc(&d.swfc, 16 * (size_t)nc); dalloc(&d.swra, 4 * (size_t)nc); dalloc(&d.invD, nc);
-            dalloc(&d.ready, nc); dalloc(&d.epoch, 1);
             d.flow_grid = sweep_flow_max_grid(P.precision == CFD_PREC_FP32, P.sweep_blocks_per_sm);
         }
         dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
@@ -442,10 +441,6 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         ck(cudaMemsetAsync(d.dW1, 0, nc * sizeof(d4), s), "memset");
         ck(cudaMemsetAsync(d.dW, 0, nc * sizeof(d4), s), "memset");
         ck(cudaMemsetAsync(d.W0, 0, nc * sizeof(d4), s), "memset");
-        if (d.ready) {
-            ck(cudaMemsetAsync(d.ready, 0, nc * sizeof(unsigned), s), "memset");
-            ck(cudaMemsetAsync(d.epoch, 0, sizeof(unsigned), s), "memset");
-        }
         auto L = c->L();
         launch_geometry(d, L);
         if (c->fp32()) launch_to_fp32(d, L, true);
@@ -621,6 +616,8 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
     double total = 0;
     bool visc = c->viscous(), f32 = c->fp32();
     for (int r = 0; r < reps; r++) {
+        // a lone backward sweep needs the "not yet computed" markers the forward pass sets
+        if (pass == 5 && c->p.sweep_mode == 0) launch_sweep_prep(d, L, visc, f32, true);
         if (flush) ck(cudaMemsetAsync(flush, r & 0xff, (size_t)flush_bytes, c->stream), "flush");
         ck(cudaEventRecord(e0, c->stream), "cudaEventRecord");
         switch (pass) {

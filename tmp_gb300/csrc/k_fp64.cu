@@ -10,6 +10,10 @@ namespace cfdgb {
 
 static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
 
+// "increment not yet computed" marker of the dataflow LU-SGS sweep: a
+// signalling NaN, a bit pattern arithmetic never produces
+constexpr unsigned long long kSentinel = 0x7ff4c0ffee5eed11ULL;
+
 // ---------------------------------------------------------------------------
 // Geometry.  edge3d::find_area/find_normal/find_center (toolBox/edge3d_int.h:93-230)
 __global__ void k_geom_faces(int nf, const int2* __restrict__ en, const d2* __restrict__ xy, d4* __restrict__ fgeo,
@@ -272,9 +276,14 @@ __global__ void __launch_bounds__(256) k_sweep_prep(int nc, const int4* __restri
                                                     const d4* __restrict__ fg0, const d4* __restrict__ fvis,
                                                     const d4* __restrict__ W, const d4* __restrict__ U,
                                                     const MuT* __restrict__ mu, double* __restrict__ swfc,
-                                                    double* __restrict__ swra) {
+                                                    double* __restrict__ swra, double* __restrict__ dW1,
+                                                    double* __restrict__ dW, int reset) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 4 * nc) return;
+    if (reset) {  // the dataflow sweep's "not yet computed" marker (see k_sweep_flow)
+        dW1[t] = __longlong_as_double((long long)kSentinel);
+        dW[t] = __longlong_as_double((long long)kSentinel);
+    }
     int i = t >> 2, s = t & 3;
     const double G = 1.4;
     int code = (&cface[i].x)[s];
@@ -360,13 +369,16 @@ __global__ void __launch_bounds__(64) k_sweep16(int begin, int end, const int* _
     else *out = (&dW1[i].x)[m] - dF / Di;
 }
 
-void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32) {
+void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32, bool reset) {
     int n = 4 * d.nc;
+    double* a = reinterpret_cast<double*>(d.dW1);
+    double* b = reinterpret_cast<double*>(d.dW);
+    int r = reset ? 1 : 0;
     if (viscous) {
-        if (fp32) k_sweep_prep<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.muf, d.swfc, d.swra);
-        else k_sweep_prep<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.mu, d.swfc, d.swra);
+        if (fp32) k_sweep_prep<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.muf, d.swfc, d.swra, a, b, r);
+        else k_sweep_prep<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.mu, d.swfc, d.swra, a, b, r);
     } else {
-        k_sweep_prep<false, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, (const double*)nullptr, d.swfc, d.swra);
+        k_sweep_prep<false, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, (const double*)nullptr, d.swfc, d.swra, a, b, r);
     }
     *L.counter += 1;
 }
@@ -384,19 +396,25 @@ void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, 
 
 // ---------------------------------------------------------------------------
 // Dataflow sweep: one persistent cooperative launch per sweep direction.
-// Cells are taken in level order (position p = g, g + G, ... for 16-lane group
-// g of G); a cell waits only for its own lower (forward) / upper (backward)
-// face neighbours, each of which publishes its finished increment with a
-// release store of the sweep's epoch into ready[j].  Every dependency sits at
-// an earlier position, all groups are resident (cooperative launch), and each
-// group finishes its positions in order, so the earliest unfinished cell can
-// always proceed.  Every wait is bounded: after kSpinLimit polls the kernel
-// raises ERR_TIMEOUT and goes on, so it always terminates.
-// The epoch lives in device memory and is bumped by a one-thread kernel before
-// each sweep, so graph replays use fresh epochs and the flags never need
-// clearing.  LOW selects the fast form: the SolveDF combination in binary32,
-// the sum widened, and dW = (-R - sum) * (1/D) with 1/D from binary64.
+// Cells are taken in level order, one warp per cell (positions p = k*G +
+// warp*B + block); a cell waits only for its own lower (forward) / upper
+// (backward) face neighbours.  The increments of a sweep are pre-filled with a
+// signalling-NaN sentinel (k_sweep_prep, every step), and a neighbour's
+// increment is final once none of its four 8-byte words - each written once,
+// single-copy atomic - still holds the sentinel, so the data itself is the
+// ready signal: no flags, fences or epochs.  Every dependency sits at an
+// earlier position, all warps are resident (cooperative launch), and each warp
+// finishes its positions in order, so the earliest unfinished cell can always
+// proceed.  Every wait is bounded: after kSpinLimit polls the kernel raises
+// ERR_TIMEOUT and goes on, so it always terminates.  Arithmetic never produces
+// the sentinel (NaN results are quiet NaNs), so a NaN state cannot stall it.
+// LOW selects the fast form: the SolveDF combination in binary32, the sum
+// widened, and dW = (-R - sum) * (1/D) with 1/D from binary64.
 constexpr long long kSpinLimit = 1LL << 22;
+
+__device__ __forceinline__ bool is_sentinel(double x) {
+    return (unsigned long long)__double_as_longlong(x) == kSentinel;
+}
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
     unsigned v;
@@ -426,8 +444,6 @@ __device__ __forceinline__ bool bounded_wait(const unsigned* flag, unsigned want
     return true;
 }
 
-__global__ void k_bump_epoch(unsigned* epoch) { epoch[0] += 1u; }
-
 // Self-test of the bounded wait: waits on a flag nothing sets.
 __global__ void k_wait_selftest(const unsigned* flag, long long limit, unsigned* err) {
     bounded_wait(flag, 0xffffffffu, limit, err);
@@ -444,7 +460,6 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
                                                     const double* __restrict__ swfc, const double* __restrict__ swra,
                                                     const d4* __restrict__ R, const double* __restrict__ D,
                                                     const double* __restrict__ invD, d4* dW1, d4* dW,
-                                                    unsigned* ready, const unsigned* __restrict__ epoch,
                                                     unsigned* err) {
     // One warp per cell.  Lanes 0..15: (face slot s, equation m); lanes 16..31
     // mirror them and only help with the divide (v = w3/w0 beside u = w2/w0).
@@ -455,7 +470,6 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
     const int warp = threadIdx.x >> 5;
     const int B = gridDim.x, NW = blockDim.x >> 5;
     const long long G = (long long)B * NW;
-    const unsigned ep = epoch[0];
     d4* dst = FWD ? dW1 : dW;
     // position p = k*G + warp*B + block: consecutive positions (one level's
     // cells) go to consecutive blocks, i.e. to different SMs
@@ -481,16 +495,20 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
             g = fg0[f];
             fc = swfc[(size_t)i * 16 + s * 4 + m];
             rA = swra[(size_t)i * 4 + s];
+            // the neighbour's increment is final once none of its four words is
+            // the sentinel (each aligned 8-byte word is written exactly once)
+            const double2* q = reinterpret_cast<const double2*>(dst + j);
+            double2 a, b;
             long long it = 0;
-            while (ld_relaxed_u32(ready + j) != ep) {
+            while (true) {
+                a = __ldcv(q);
+                b = __ldcv(q + 1);
+                if (!is_sentinel(a.x) && !is_sentinel(a.y) && !is_sentinel(b.x) && !is_sentinel(b.y)) break;
                 if (++it > kSpinLimit) {
                     atomicOr(err, ERR_TIMEOUT);
                     break;
                 }
             }
-            fence_acq_rel_gpu();
-            const double2* q = reinterpret_cast<const double2*>(dst + j);
-            double2 a = __ldcg(q), b = __ldcg(q + 1);
             dw[0] = a.x; dw[1] = a.y; dw[2] = b.x; dw[3] = b.y;
         }
         double DF = 0.0;
@@ -550,24 +568,24 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
         double r2 = __shfl_sync(0xffffffffu, res, 2);
         double r3 = __shfl_sync(0xffffffffu, res, 3);
         if (lane == 0) {
-            st4(dst + i, d4{res, r1, r2, r3});
-            st_release_u32(ready + i, ep);
+            double2* o = reinterpret_cast<double2*>(dst + i);
+            __stcg(o, make_double2(res, r1));
+            __stcg(o + 1, make_double2(r2, r3));
         }
     }
 }
 
 cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid) {
-    k_bump_epoch<<<1, 1, 0, L.stream>>>(d.epoch);
     int nc = d.nc;
     const int* order = forward ? d.fwd_order : d.bwd_order;
     void* args[] = {(void*)&nc, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0, (void*)&d.W,
                     (void*)&d.swfc, (void*)&d.swra, (void*)&d.R, (void*)&d.diag, (void*)&d.invD, (void*)&d.dW1,
-                    (void*)&d.dW, (void*)&d.ready, (void*)&d.epoch, (void*)&d.err};
+                    (void*)&d.dW, (void*)&d.err};
     void* fn;
     if (forward) fn = low ? (void*)k_sweep_flow<true, true> : (void*)k_sweep_flow<true, false>;
     else fn = low ? (void*)k_sweep_flow<false, true> : (void*)k_sweep_flow<false, false>;
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
-    *L.counter += 2;
+    *L.counter += 1;
     return e;
 }
 
