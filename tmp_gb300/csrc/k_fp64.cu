@@ -486,7 +486,16 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
             j = left ? e.y : e.x;
             use = FWD ? (j >= 0 && j < i) : (j > i);
         }
-        double w0[4] = {0.0, 0.0, 0.0, 0.0}, dw[4] = {0.0, 0.0, 0.0, 0.0};
+        // this cell's own inputs of the final update, loaded before any wait:
+        // R_i (forward) or dW1_i (backward), and D_i (plain) or 1/D_i (fast form)
+        double own = 0.0, dinv = 1.0;
+        if (lane < 4) {
+            own = FWD ? (&R[i].x)[m] : (&dW1[i].x)[m];
+            dinv = LOW ? invD[i] : D[i];
+        }
+        // lanes without a contributing neighbour compute on harmless values and
+        // are masked at the end, so the arithmetic below is issued once per warp
+        double w0[4] = {1.0, 1.0, 0.0, 0.0}, dw[4] = {0.0, 0.0, 0.0, 0.0};
         d4 g = d4{0.0, 0.0, 0.0, 0.0};
         double fc = 0.0, rA = 0.0;
         if (use) {
@@ -511,38 +520,36 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
             }
             dw[0] = a.x; dw[1] = a.y; dw[2] = b.x; dw[3] = b.y;
         }
-        double DF = 0.0;
+        __syncwarp();  // reconverge before the arithmetic
+        double DF;
         if (LOW) {
-            float wp0 = (float)(w0[0] + dw[0]), wp1 = (float)(w0[1] + dw[1]);
-            float wp2 = (float)(w0[2] + dw[2]), wp3 = (float)(w0[3] + dw[3]);
-            if (use) {
-                float nx = (float)g.x, ny = (float)g.y;
-                float u = wp2 / wp0, v = wp3 / wp0;
-                float vn = u * nx + v * ny;
-                float pr = (1.4f - 1.0f) * (wp1 - 0.5f * wp0 * (u * u + v * v));
-                float fcp = m == 0 ? wp0 * vn : m == 1 ? (wp1 + pr) * vn : m == 2 ? wp2 * vn + pr * nx
-                                                                                  : wp3 * vn + pr * ny;
-                float dwm = (float)(m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3]);
-                float dfc = left ? (fcp - (float)fc) : ((float)fc - fcp);
-                DF = (double)(0.5f * (dfc - (float)rA * dwm) * (float)g.z);
-            }
+            float wp0 = (float)w0[0] + (float)dw[0], wp1 = (float)w0[1] + (float)dw[1];
+            float wp2 = (float)w0[2] + (float)dw[2], wp3 = (float)w0[3] + (float)dw[3];
+            float nx = (float)g.x, ny = (float)g.y;
+            float u = wp2 / wp0, v = wp3 / wp0;
+            float vn = u * nx + v * ny;
+            float pr = (1.4f - 1.0f) * (wp1 - 0.5f * wp0 * (u * u + v * v));
+            float fcp = m == 0 ? wp0 * vn : m == 1 ? (wp1 + pr) * vn : m == 2 ? wp2 * vn + pr * nx : wp3 * vn + pr * ny;
+            float dwm = (float)(m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3]);
+            float dfc = left ? (fcp - (float)fc) : ((float)fc - fcp);
+            float df = 0.5f * (dfc - (float)rA * dwm) * (float)g.z;
+            DF = use ? (double)df : 0.0;
         } else {
             double wp[4];
 #pragma unroll
             for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
             // one divide per half-warp, exchanged
-            double q = use ? (hv ? wp[3] : wp[2]) / wp[0] : 0.0;
+            double q = (hv ? wp[3] : wp[2]) / wp[0];
             double u = __shfl_sync(0xffffffffu, q, lane & 15);
             double v = __shfl_sync(0xffffffffu, q, (lane & 15) | 16);
-            if (use) {
-                double vn = dot2(u, v, g.x, g.y);
-                double pr = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
-                double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + pr) * vn : m == 2 ? wp[2] * vn + pr * g.x
-                                                                                       : wp[3] * vn + pr * g.y;
-                double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
-                double dfc = left ? (fcp - fc) : (fc - fcp);
-                DF = 0.5 * (dfc - rA * dwm) * g.z;
-            }
+            double vn = dot2(u, v, g.x, g.y);
+            double pr = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
+            double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + pr) * vn : m == 2 ? wp[2] * vn + pr * g.x
+                                                                                   : wp[3] * vn + pr * g.y;
+            double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
+            double dfc = left ? (fcp - fc) : (fc - fcp);
+            double df = 0.5 * (dfc - rA * dwm) * g.z;
+            DF = use ? df : 0.0;
         }
         // ordered sum over the 4 face slots (lanes m, m+4, m+8, m+12)
         double v0 = __shfl_sync(0xffffffffu, DF, m);
@@ -556,13 +563,8 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
         if (cf.w != 0) dF += v3;
         double res = 0.0;
         if (lane < 4) {
-            if (FWD) {
-                double r = (&R[i].x)[m];
-                res = LOW ? (-r - dF) * invD[i] : (-r - dF) / D[i];
-            } else {
-                double a1 = (&dW1[i].x)[m];
-                res = LOW ? a1 - dF * invD[i] : a1 - dF / D[i];
-            }
+            if (FWD) res = LOW ? (-own - dF) * dinv : (-own - dF) / dinv;
+            else res = LOW ? own - dF * dinv : own - dF / dinv;
         }
         double r1 = __shfl_sync(0xffffffffu, res, 1);
         double r2 = __shfl_sync(0xffffffffu, res, 2);
