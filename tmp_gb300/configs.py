@@ -49,7 +49,14 @@ def c2() -> Workload:
     return Workload("C2 cylinder mixed quad/tri ~130k laminar LU-SGS", m, "laminar", "lusgs", 0.2, 0.0, 40.0, 50.0)
 
 
-WORKLOADS = {"c1": c1, "c2": c2}
+def c2big() -> Workload:
+    """The C2 recipe at ~1M cells (larger than L2, used for DRAM-level profiles)."""
+    m = meshgen.mixed_mesh(cylinder(720), nlayer=96, dr1=2.5e-3, growth=1.03, rfar=30.0, seed=2025, density=1.0,
+                           grade=0.79)
+    return Workload("C2big cylinder mixed quad/tri ~1M laminar LU-SGS", m, "laminar", "lusgs", 0.2, 0.0, 40.0, 50.0)
+
+
+WORKLOADS = {"c1": c1, "c2": c2, "c2big": c2big}
 
 
 def grd_path(w: Workload, cache_dir: str | os.PathLike | None = None) -> Path:
