@@ -469,11 +469,16 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
     const int s = (lane >> 2) & 3, m = lane & 3;
     const int warp = threadIdx.x >> 5;
     const int B = gridDim.x, NW = blockDim.x >> 5;
-    const long long G = (long long)B * NW;
     d4* dst = FWD ? dW1 : dW;
-    // position p = k*G + warp*B + block: consecutive positions (one level's
-    // cells) go to consecutive blocks, i.e. to different SMs
-    for (long long p = (long long)warp * B + blockIdx.x; p < nc; p += G) {
+    // Position p = block + B*q goes to block p % B and warp (q + block) % NW:
+    // consecutive positions (one level's cells) land on different SMs and, as
+    // the warp index rotates with the block, on different SM sub-partitions
+    // (whose FP64 pipes are separate).  Each warp visits its positions in
+    // increasing order: q = q0, q0 + NW, q0 + 2*NW, ...
+    const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
+    for (long long q = q0;; q += NW) {
+        const long long p = (long long)blockIdx.x + (long long)B * q;
+        if (p >= nc) break;
         const int i = order[p];
         const int4 cf = cface[i];
         const int code = s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w;
