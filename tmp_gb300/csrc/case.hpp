@@ -73,6 +73,15 @@ struct DevArrays {
     double* swfc = nullptr;      // [16*nc] F_c(W_j)[m] at (i*4+s)*4+m
     double* swra = nullptr;      // [4*nc]  r_A at i*4+s
     double* invD = nullptr;      // [nc] 1/D (fast form's sweep)
+    // fast-form sweep: binary32 copies and level-paired order
+    float* swfcf = nullptr;      // [16*nc]
+    float* swraf = nullptr;      // [4*nc]
+    float4* Wf = nullptr;        // [nc]
+    float4* dW1f = nullptr;      // [nc]
+    float4* dWf = nullptr;       // [nc]
+    int* fwd_order2 = nullptr;   // [npos2_fwd] cells of each level in pairs, odd levels padded with -1
+    int* bwd_order2 = nullptr;
+    int npos2_fwd = 0, npos2_bwd = 0;
     int flow_grid = 0;           // co-resident blocks of the dataflow sweep
     // LU-SGS level schedule (all meshes merged level by level)
     int* fwd_order = nullptr;
@@ -102,6 +111,8 @@ void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, 
 cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid);
 int sweep_flow_max_grid(bool low, int blocks_per_sm);
 void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
+void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous);
+cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
 void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
 void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);

@@ -115,7 +115,7 @@ void free_case(cfd_case_s* c) {
                     d.cgeo, d.fg0, d.fg1, d.fvis, d.walld, d.fg0f, d.fg1f, d.fvisf, d.cgeof, d.U, d.W, d.W0, d.R,
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
-                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
+                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.swfcf, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -161,14 +161,22 @@ void sweeps(cfd_case_s* c, bool forward) {
             launch_sweep_level(d, L, c->viscous(), forward, ptr[k], ptr[k + 1], c->fp32());
         return;
     }
-    if (forward) launch_sweep_prep(d, L, c->viscous(), c->fp32(), c->p.sweep_mode == 0);
+    if (forward && !(c->fp32() && c->p.sweep_mode == 0))
+        launch_sweep_prep(d, L, c->viscous(), c->fp32(), c->p.sweep_mode == 0);
     if (c->p.sweep_mode == 2) {
         for (size_t k = 0; k + 1 < ptr.size(); k++) launch_sweep16_level(d, L, forward, ptr[k], ptr[k + 1]);
         return;
     }
-    // default: one dataflow launch per direction (the fast form uses 1/D)
-    if (forward && c->fp32()) launch_inv_diag(d, L);
-    ck(launch_sweep_flow(d, L, forward, c->fp32(), d.flow_grid), "cooperative sweep launch");
+    // default: one dataflow launch per direction
+    if (c->fp32()) {
+        if (forward) {
+            launch_inv_diag(d, L);
+            launch_sweep_prep32(d, L, c->viscous());
+        }
+        ck(launch_sweep_flow32(d, L, forward, d.flow_grid), "cooperative sweep launch");
+    } else {
+        ck(launch_sweep_flow(d, L, forward, false, d.flow_grid), "cooperative sweep launch");
+    }
 }
 
 // LUSGSIntegrator::UpdateSerial (LUSGS_Integrator.cpp:228-240).
@@ -386,6 +394,18 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
                 for (int k = m.ncell - 1; k >= 0; k--) bo_[pb[m.lev_bwd[k]]++] = co + k;
             }
         }
+        // level-paired orders of the fast-form sweep (two cells of one level per warp)
+        auto pair_order = [](const std::vector<int>& order, const std::vector<int>& ptr) {
+            std::vector<int> o2;
+            for (size_t k = 0; k + 1 < ptr.size(); k++) {
+                for (int p = ptr[k]; p < ptr[k + 1]; p++) o2.push_back(order[p]);
+                if ((ptr[k + 1] - ptr[k]) & 1) o2.push_back(-1);
+            }
+            return o2;
+        };
+        std::vector<int> fo2 = pair_order(fo_, d.fwd_ptr), bo2 = pair_order(bo_, d.bwd_ptr);
+        d.npos2_fwd = (int)fo2.size();
+        d.npos2_bwd = (int)bo2.size();
         // norm chunks
         std::vector<int4> nb;
         const int chunk = 8192;
@@ -420,6 +440,11 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         dalloc(&d.fwd_order, nc); dalloc(&d.bwd_order, nc);
         if (P.advance == CFD_ADV_LUSGS) {
             dalloc(&d.swfc, 16 * (size_t)nc); dalloc(&d.swra, 4 * (size_t)nc); dalloc(&d.invD, nc);
+            if (P.precision == CFD_PREC_FP32) {
+                dalloc(&d.swfcf, 16 * (size_t)nc); dalloc(&d.swraf, 4 * (size_t)nc); dalloc(&d.Wf, nc);
+                dalloc(&d.dW1f, nc); dalloc(&d.dWf, nc);
+                dalloc(&d.fwd_order2, d.npos2_fwd); dalloc(&d.bwd_order2, d.npos2_bwd);
+            }
             d.flow_grid = sweep_flow_max_grid(P.precision == CFD_PREC_FP32, P.sweep_blocks_per_sm);
         }
         dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
@@ -436,6 +461,10 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         ck(cudaMemcpyAsync(d.prm, c->prm.data(), nmesh * sizeof(MeshPrm), cudaMemcpyHostToDevice, s), "upload");
         ck(cudaMemcpyAsync(d.fwd_order, fo_.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
         ck(cudaMemcpyAsync(d.bwd_order, bo_.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+        if (d.fwd_order2) {
+            ck(cudaMemcpyAsync(d.fwd_order2, fo2.data(), fo2.size() * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+            ck(cudaMemcpyAsync(d.bwd_order2, bo2.data(), bo2.size() * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+        }
         ck(cudaMemcpyAsync(d.norm_blocks, nb.data(), nb.size() * sizeof(int4), cudaMemcpyHostToDevice, s), "upload");
         ck(cudaMemsetAsync(d.err, 0, 2 * sizeof(unsigned), s), "memset");
         ck(cudaMemsetAsync(d.dW1, 0, nc * sizeof(d4), s), "memset");
@@ -617,7 +646,10 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
     bool visc = c->viscous(), f32 = c->fp32();
     for (int r = 0; r < reps; r++) {
         // a lone backward sweep needs the "not yet computed" markers the forward pass sets
-        if (pass == 5 && c->p.sweep_mode == 0) launch_sweep_prep(d, L, visc, f32, true);
+        if (pass == 5 && c->p.sweep_mode == 0) {
+            if (f32) launch_sweep_prep32(d, L, visc);
+            else launch_sweep_prep(d, L, visc, f32, true);
+        }
         if (flush) ck(cudaMemsetAsync(flush, r & 0xff, (size_t)flush_bytes, c->stream), "flush");
         ck(cudaEventRecord(e0, c->stream), "cudaEventRecord");
         switch (pass) {

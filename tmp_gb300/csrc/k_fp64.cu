@@ -596,12 +596,180 @@ cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forwa
     return e;
 }
 
+// ---------------------------------------------------------------------------
+// Fast-form dataflow sweep.  Same protocol as k_sweep_flow, but everything on
+// the dependence chain except the final update is binary32: float copies of
+// W (Wf), of the per-step SolveDF constants and of the increments (dW1f/dWf,
+// published beside the binary64 increments and polled instead of them), so
+// the binary64 pipe only sees the widening of the slot sum and
+// dW = (-R - sum) * (1/D).  Two cells per warp (16 lanes each): the cells of a
+// pair always come from the same level (order2 pads odd levels with -1), so
+// the two halves never depend on each other and may wait for each other.
+constexpr unsigned kSentinelF = 0x7fa0c0deu;  // a signalling binary32 NaN
+
+__device__ __forceinline__ bool is_sentinel_f(float x) { return __float_as_uint(x) == kSentinelF; }
+
+template <bool VISC, class MuT>
+__global__ void __launch_bounds__(256) k_sweep_prep32(int nc, const int4* __restrict__ cface, const int2* __restrict__ lr,
+                                                      const float4* __restrict__ fg0f, const float4* __restrict__ fvisf,
+                                                      const d4* __restrict__ W, const d4* __restrict__ U,
+                                                      const MuT* __restrict__ mu, float* __restrict__ swfcf,
+                                                      float* __restrict__ swraf, float4* __restrict__ Wf,
+                                                      float* __restrict__ dW1f, float* __restrict__ dWf) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * nc) return;
+    int i = t >> 2, s = t & 3;
+    const float G = 1.4f;
+    dW1f[t] = __uint_as_float(kSentinelF);
+    dWf[t] = __uint_as_float(kSentinelF);
+    if (s == 0) {
+        d4 w = ld4(W + i);
+        Wf[i] = make_float4((float)w.x, (float)w.y, (float)w.z, (float)w.w);
+    }
+    int code = (&cface[i].x)[s];
+    float fc[4] = {0.f, 0.f, 0.f, 0.f}, rA = 0.f;
+    if (code != 0) {
+        int f = code_face(code);
+        int2 e = lr[f];
+        int j = code > 0 ? e.y : e.x;
+        if (j >= 0) {
+            d4 wd = ld4(W + j), ud = ld4(U + j);
+            float w0[4] = {(float)wd.x, (float)wd.y, (float)wd.z, (float)wd.w};
+            float uj[4] = {(float)ud.x, (float)ud.y, (float)ud.z, (float)ud.w};
+            float4 g = fg0f[f];
+            conv_flux_w<float>(w0, g.x, g.y, fc);
+            float vn = uj[2] * g.x + uj[3] * g.y;
+            float c = sqrtf(G * uj[1] / uj[0]);
+            rA = 1.5f * (fabsf(vn) + c);
+            if (VISC) rA += fmaxf(4.f / (3.f * uj[0]), G / uj[0]) * ((float)mu[i] / 0.72f) / sqrtf(fvisf[f].z);
+        }
+    }
+    reinterpret_cast<float4*>(swfcf)[t] = make_float4(fc[0], fc[1], fc[2], fc[3]);
+    swraf[t] = rA;
+}
+
+void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous) {
+    int n = 4 * d.nc;
+    float* a = reinterpret_cast<float*>(d.dW1f);
+    float* b = reinterpret_cast<float*>(d.dWf);
+    if (viscous)
+        k_sweep_prep32<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muf, d.swfcf, d.swraf, d.Wf, a, b);
+    else
+        k_sweep_prep32<false, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, (const float*)nullptr, d.swfcf, d.swraf, d.Wf, a, b);
+    *L.counter += 1;
+}
+
+template <bool FWD>
+__global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __restrict__ order2,
+                                                      const int4* __restrict__ cface, const int2* __restrict__ lr,
+                                                      const float4* __restrict__ fg0f, const float4* __restrict__ Wf,
+                                                      const float* __restrict__ swfcf, const float* __restrict__ swraf,
+                                                      const d4* __restrict__ R, const double* __restrict__ invD,
+                                                      d4* dW1, d4* dW, float4* dW1f, float4* dWf, unsigned* err) {
+    const float GM1 = 1.4f - 1.0f;
+    const int lane = threadIdx.x & 31;
+    const int h = lane >> 4, base = lane & 16;
+    const int s = (lane >> 2) & 3, m = lane & 3;
+    const int warp = threadIdx.x >> 5;
+    const int B = gridDim.x, NW = blockDim.x >> 5;
+    d4* dst = FWD ? dW1 : dW;
+    float4* dstf = FWD ? dW1f : dWf;
+    const int npairs = npos >> 1;
+    const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
+    for (long long q = q0;; q += NW) {
+        const long long P = (long long)blockIdx.x + (long long)B * q;  // pair index, same mapping as k_sweep_flow
+        if (P >= npairs) break;
+        const int i = order2[2 * P + h];
+        const bool active = i >= 0;
+        const int4 cf = active ? cface[i] : make_int4(0, 0, 0, 0);
+        const int code = s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w;
+        bool use = false, left = false;
+        int f = 0, j = 0;
+        if (code != 0) {
+            f = code_face(code);
+            left = code > 0;
+            int2 e = lr[f];
+            j = left ? e.y : e.x;
+            use = FWD ? (j >= 0 && j < i) : (j > i);
+        }
+        double own = 0.0, dinv = 1.0;
+        if (active && s == 0) {
+            own = FWD ? (&R[i].x)[m] : (&dW1[i].x)[m];
+            dinv = invD[i];
+        }
+        float4 w0 = make_float4(1.f, 1.f, 0.f, 0.f), dw = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        float fc = 0.f, rA = 0.f;
+        if (use) {
+            w0 = Wf[j];
+            g = fg0f[f];
+            fc = swfcf[(size_t)i * 16 + s * 4 + m];
+            rA = swraf[(size_t)i * 4 + s];
+            const float4* qf = (FWD ? dW1f : dWf) + j;
+            long long it = 0;
+            while (true) {
+                dw = __ldcv(qf);
+                if (!is_sentinel_f(dw.x) && !is_sentinel_f(dw.y) && !is_sentinel_f(dw.z) && !is_sentinel_f(dw.w)) break;
+                if (++it > kSpinLimit) {
+                    atomicOr(err, ERR_TIMEOUT);
+                    break;
+                }
+            }
+        }
+        __syncwarp();
+        float wp0 = w0.x + dw.x, wp1 = w0.y + dw.y, wp2 = w0.z + dw.z, wp3 = w0.w + dw.w;
+        float u = wp2 / wp0, v = wp3 / wp0;
+        float vn = u * g.x + v * g.y;
+        float pr = GM1 * (wp1 - 0.5f * wp0 * (u * u + v * v));
+        float fcp = m == 0 ? wp0 * vn : m == 1 ? (wp1 + pr) * vn : m == 2 ? wp2 * vn + pr * g.x : wp3 * vn + pr * g.y;
+        float dwm = m == 0 ? dw.x : m == 1 ? dw.y : m == 2 ? dw.z : dw.w;
+        float dfc = left ? (fcp - fc) : (fc - fcp);
+        float DF = use ? 0.5f * (dfc - rA * dwm) * g.z : 0.f;
+        float v0 = __shfl_sync(0xffffffffu, DF, base + m);
+        float v1 = __shfl_sync(0xffffffffu, DF, base + 4 + m);
+        float v2 = __shfl_sync(0xffffffffu, DF, base + 8 + m);
+        float v3 = __shfl_sync(0xffffffffu, DF, base + 12 + m);
+        float dF = 0.f;
+        if (cf.x != 0) dF += v0;
+        if (cf.y != 0) dF += v1;
+        if (cf.z != 0) dF += v2;
+        if (cf.w != 0) dF += v3;
+        double res = 0.0;
+        if (s == 0) res = FWD ? (-own - (double)dF) * dinv : own - (double)dF * dinv;
+        float resf = (float)res;
+        double r1 = __shfl_sync(0xffffffffu, res, base + 1);
+        double r2 = __shfl_sync(0xffffffffu, res, base + 2);
+        double r3 = __shfl_sync(0xffffffffu, res, base + 3);
+        float f1 = __shfl_sync(0xffffffffu, resf, base + 1);
+        float f2 = __shfl_sync(0xffffffffu, resf, base + 2);
+        float f3 = __shfl_sync(0xffffffffu, resf, base + 3);
+        if (active && (lane & 15) == 0) {
+            double2* o = reinterpret_cast<double2*>(dst + i);
+            __stcg(o, make_double2(res, r1));
+            __stcg(o + 1, make_double2(r2, r3));
+            __stcg(dstf + i, make_float4(resf, f1, f2, f3));
+        }
+    }
+}
+
+cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid) {
+    int npos = forward ? d.npos2_fwd : d.npos2_bwd;
+    const int* order = forward ? d.fwd_order2 : d.bwd_order2;
+    void* args[] = {(void*)&npos, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0f, (void*)&d.Wf,
+                    (void*)&d.swfcf, (void*)&d.swraf, (void*)&d.R, (void*)&d.invD, (void*)&d.dW1, (void*)&d.dW,
+                    (void*)&d.dW1f, (void*)&d.dWf, (void*)&d.err};
+    void* fn = forward ? (void*)k_sweep_flow32<true> : (void*)k_sweep_flow32<false>;
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
+    *L.counter += 1;
+    return e;
+}
+
 int sweep_flow_max_grid(bool low, int blocks_per_sm) {
     int dev = 0, sms = 0, per = 0, per2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    void* fn = low ? (void*)k_sweep_flow<true, true> : (void*)k_sweep_flow<true, false>;
-    void* fn2 = low ? (void*)k_sweep_flow<false, true> : (void*)k_sweep_flow<false, false>;
+    void* fn = low ? (void*)k_sweep_flow32<true> : (void*)k_sweep_flow<true, false>;
+    void* fn2 = low ? (void*)k_sweep_flow32<false> : (void*)k_sweep_flow<false, false>;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, fn2, 256, 0);
     per = per < per2 ? per : per2;
