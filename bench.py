@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "mixed"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -243,14 +243,15 @@ def run_ours(args):
     w = configs.WORKLOADS[args.config]()
     path = configs.grd_path(w)
     mesh = abi.Mesh.load_grd(path, w.mesh.wall_tag, w.mesh.far_tag)
-    fp32 = args.precision == "fp32"
+    fp32 = args.precision != "fp64"
     viscous = w.flow == "laminar"
     stream = torch.cuda.Stream()  # a real stream: graph capture is not allowed on the legacy default stream
     torch.cuda.set_stream(stream)
     case = abi.Case([mesh], [dict(mach=w.mach, aoa_deg=w.aoa, reynolds=w.re)],
                     abi.FLOW_LAMINAR if viscous else abi.FLOW_EULER,
                     abi.ADV_LUSGS if w.advance == "lusgs" else abi.ADV_RK5,
-                    abi.PREC_FP32 if fp32 else abi.PREC_FP64, cfl=w.cfl, stream=stream.cuda_stream,
+                    dict(fp64=abi.PREC_FP64, fp32=abi.PREC_FP32, mixed=abi.PREC_MIXED)[args.precision], cfl=w.cfl,
+                    stream=stream.cuda_stream,
                     sweep_mode=args.sweep_mode, sweep_blocks_per_sm=args.sweep_bpsm)
     case.init_freestream()
     nc, nf = case.ncell, case.nedge

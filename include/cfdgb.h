@@ -40,9 +40,15 @@ extern "C" {
 #define CFD_ADV_RK5       0   /* RungeKuttaStrategy(5)                     */
 #define CFD_ADV_LUSGS     1   /* LUSGSIntegrator                           */
 #define CFD_PREC_FP64     0   /* plain: every kernel in binary64           */
-#define CFD_PREC_FP32     1   /* face states/gradients/limiter/fluxes in
-                                 binary32; residual sums, update, norms,
-                                 LU-SGS diagonal and sweeps in binary64    */
+#define CFD_PREC_FP32     1   /* fast form: face states, gradients, limiter,
+                                 fluxes and the LU-SGS sweep combination in
+                                 binary32; residual sums, update, norms and
+                                 the LU-SGS diagonal in binary64 (converges
+                                 to the binary32 discretisation, ~1e-4)   */
+#define CFD_PREC_MIXED    2   /* defect correction: binary64 residual (as
+                                 CFD_PREC_FP64) with the binary32 LU-SGS
+                                 sweep as the implicit operator; converges
+                                 to the binary64 solution                 */
 
 /* Field selectors for cfd_get_field / cfd_put_field.  Cell fields use the
  * reference's interleaved layout [NEQU*cell + eq]; face fields [4*face + eq]. */
@@ -160,6 +166,10 @@ int cfd_residual_norm(cfd_case_t c, int mesh, int which, double* out);
 /* Copy a field of one mesh to / from host memory (layout above). */
 int cfd_get_field(cfd_case_t c, int mesh, int which, double* host);
 int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host);
+/* Per-cell CFL multipliers of one mesh for LU-SGS (dt_i = CFL * mult_i * vol_i /
+ * spec_c,i).  The reference uses one constant CFL (LUSGS_Integrator.h:18); the
+ * multipliers are the hook of local-CFL controllers.  NULL removes them. */
+int cfd_set_cell_cfl(cfd_case_t c, int mesh, const double* mult);
 /* Wait for the case's stream and report any device-side error flag. */
 int cfd_sync(cfd_case_t c);
 /* Number of kernel launches the library issued on this case so far. */

@@ -21,7 +21,7 @@ ERR = {-1: "ARG", -2: "IO", -3: "MESH", -4: "CUDA", -5: "PSTAR", -6: "NONPHYSICA
 BC_WALL, BC_FARFIELD = -2, -3
 FLOW_EULER, FLOW_LAMINAR = 0, 1
 ADV_RK5, ADV_LUSGS = 0, 1
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
 FIELD = dict(U=0, W=1, R=2, GRAD=3, PHI=4, SPEC_C=5, SPEC_V=6, DT=7, DIAG=8, DW1=9, DW=10, GRADT=11, MU=12,
              UEDGE=13, MUEDGE=14, VOL=15, CENTER=16, NORMAL=17, AREA=18, ECENTER=19, WALLDIST=20)
 # values per element and whether the field lives on faces
@@ -91,6 +91,7 @@ def lib() -> C.CDLL:
         "cfd_launch_count": (C.c_longlong, [vp]),
         "cfd_bench_pass": (C.c_int, [vp, C.c_int, C.c_int, C.c_longlong, dp]),
         "cfd_selftest_bounded_wait": (C.c_int, [vp, C.c_longlong]),
+        "cfd_set_cell_cfl": (C.c_int, [vp, C.c_int, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -185,6 +186,14 @@ class Case:
         s = C.c_void_p()
         check(lib().cfd_case_stream(self.h, C.byref(s)))
         return s.value or 0
+
+    def set_cell_cfl(self, mult, mesh: int = 0):
+        """Per-cell CFL multipliers (None removes them)."""
+        if mult is None:
+            check(lib().cfd_set_cell_cfl(self.h, int(mesh), None))
+            return
+        a = np.ascontiguousarray(mult, dtype=np.float64).reshape(-1)
+        check(lib().cfd_set_cell_cfl(self.h, int(mesh), _dptr(a)))
 
     def init_freestream(self):
         check(lib().cfd_init_freestream(self.h))

@@ -42,6 +42,7 @@ struct DevArrays {
     d4* R = nullptr;
     double* dt = nullptr;
     double* diag = nullptr;
+    float* cflmul = nullptr;     // [nc] optional per-cell CFL multiplier (null = 1)
     d4* dW1 = nullptr;
     d4* dW = nullptr;
     // residual intermediates, binary64 form
@@ -111,7 +112,7 @@ void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, 
 cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid);
 int sweep_flow_max_grid(bool low, int blocks_per_sm);
 void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
-void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous);
+void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, bool mu64);
 cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
 void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);

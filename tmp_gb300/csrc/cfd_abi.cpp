@@ -97,6 +97,8 @@ struct cfd_case_s {
     long long graph_nodes = 0;
     bool viscous() const { return p.flow == CFD_FLOW_LAMINAR; }
     bool fp32() const { return p.precision == CFD_PREC_FP32; }
+    bool mixed() const { return p.precision == CFD_PREC_MIXED; }
+    bool fast_sweep() const { return p.precision != CFD_PREC_FP64 && p.advance == CFD_ADV_LUSGS; }
     LaunchCfg L() { return LaunchCfg{stream, &launches}; }
     void drop_graph() {
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -115,7 +117,7 @@ void free_case(cfd_case_s* c) {
                     d.cgeo, d.fg0, d.fg1, d.fvis, d.walld, d.fg0f, d.fg1f, d.fvisf, d.cgeof, d.U, d.W, d.W0, d.R,
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
-                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.swfcf, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
+                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.swfcf, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -161,17 +163,17 @@ void sweeps(cfd_case_s* c, bool forward) {
             launch_sweep_level(d, L, c->viscous(), forward, ptr[k], ptr[k + 1], c->fp32());
         return;
     }
-    if (forward && !(c->fp32() && c->p.sweep_mode == 0))
+    if (forward && !(c->fast_sweep() && c->p.sweep_mode == 0))
         launch_sweep_prep(d, L, c->viscous(), c->fp32(), c->p.sweep_mode == 0);
     if (c->p.sweep_mode == 2) {
         for (size_t k = 0; k + 1 < ptr.size(); k++) launch_sweep16_level(d, L, forward, ptr[k], ptr[k + 1]);
         return;
     }
     // default: one dataflow launch per direction
-    if (c->fp32()) {
+    if (c->fast_sweep()) {
         if (forward) {
             launch_inv_diag(d, L);
-            launch_sweep_prep32(d, L, c->viscous());
+            launch_sweep_prep32(d, L, c->viscous(), c->mixed());
         }
         ck(launch_sweep_flow32(d, L, forward, d.flow_grid), "cooperative sweep launch");
     } else {
@@ -305,7 +307,8 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
     const cfd_params_t& P = *params;
     if (P.flow != CFD_FLOW_EULER && P.flow != CFD_FLOW_LAMINAR) return fail(CFD_ERR_ARG, "Undefined Flow Type");
     if (P.advance != CFD_ADV_RK5 && P.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_ARG, "Undefined Advance Type");
-    if (P.precision != CFD_PREC_FP64 && P.precision != CFD_PREC_FP32) return fail(CFD_ERR_ARG, "unknown precision");
+    if (P.precision != CFD_PREC_FP64 && P.precision != CFD_PREC_FP32 && P.precision != CFD_PREC_MIXED)
+        return fail(CFD_ERR_ARG, "unknown precision");
     for (int i = 0; i < nmesh; i++)
         if (!(fs[i].density > 0) || !(fs[i].pressure > 0) || !(fs[i].mach > 0))
             return fail(CFD_ERR_ARG, "freestream density, pressure and Mach must be positive");
@@ -437,15 +440,18 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             dalloc(&d.Ue, nf); dalloc(&d.fspec, nf); dalloc(&d.Fc, nf);
             if (visc) { dalloc(&d.specv, nc); dalloc(&d.gradT, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf); dalloc(&d.Fv, nf); }
         }
+        if (c->mixed()) {  // binary32 geometry and state copy used by the binary32 sweep
+            dalloc(&d.fg0f, nf); dalloc(&d.fg1f, nf); dalloc(&d.fvisf, nf); dalloc(&d.cgeof, nc); dalloc(&d.Uf, nc);
+        }
         dalloc(&d.fwd_order, nc); dalloc(&d.bwd_order, nc);
         if (P.advance == CFD_ADV_LUSGS) {
             dalloc(&d.swfc, 16 * (size_t)nc); dalloc(&d.swra, 4 * (size_t)nc); dalloc(&d.invD, nc);
-            if (P.precision == CFD_PREC_FP32) {
+            if (P.precision != CFD_PREC_FP64) {
                 dalloc(&d.swfcf, 16 * (size_t)nc); dalloc(&d.swraf, 4 * (size_t)nc); dalloc(&d.Wf, nc);
                 dalloc(&d.dW1f, nc); dalloc(&d.dWf, nc);
                 dalloc(&d.fwd_order2, d.npos2_fwd); dalloc(&d.bwd_order2, d.npos2_bwd);
             }
-            d.flow_grid = sweep_flow_max_grid(P.precision == CFD_PREC_FP32, P.sweep_blocks_per_sm);
+            d.flow_grid = sweep_flow_max_grid(P.precision != CFD_PREC_FP64, P.sweep_blocks_per_sm);
         }
         dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
         dalloc(&d.err, 2);
@@ -473,6 +479,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         auto L = c->L();
         launch_geometry(d, L);
         if (c->fp32()) launch_to_fp32(d, L, true);
+        else if (c->mixed()) launch_to_fp32(d, L, true);  // binary32 geometry for the sweep
         ck(cudaGetLastError(), "geometry launch");
         ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
         *out = c;
@@ -622,6 +629,37 @@ int cfd_sync(cfd_case_t c) {
 
 long long cfd_launch_count(cfd_case_t c) { return c ? c->launches : -1; }
 
+int cfd_set_cell_cfl(cfd_case_t c, int mesh, const double* mult) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
+    ABI_TRY
+    DevArrays& d = c->d;
+    if (!mult) {
+        if (d.cflmul) {
+            cudaFree(d.cflmul);
+            d.cflmul = nullptr;
+            c->drop_graph();
+        }
+        return CFD_OK;
+    }
+    if (!d.cflmul) {
+        dalloc(&d.cflmul, d.nc);
+        std::vector<float> one(d.nc, 1.0f);
+        ck(cudaMemcpyAsync(d.cflmul, one.data(), one.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+        c->drop_graph();  // the captured step must see the new pointer
+    }
+    int off = c->coff[mesh], n = c->coff[mesh + 1] - off;
+    std::vector<float> m(n);
+    for (int k = 0; k < n; k++) {
+        if (!(mult[k] > 0)) return fail(CFD_ERR_ARG, "CFL multipliers must be positive");
+        m[k] = (float)mult[k];
+    }
+    ck(cudaMemcpyAsync(d.cflmul + off, m.data(), n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    return CFD_OK;
+    ABI_CATCH
+}
+
 int cfd_selftest_bounded_wait(cfd_case_t c, long long polls) {
     if (!c || polls <= 0) return fail(CFD_ERR_ARG, "null case or non-positive poll count");
     ABI_TRY
@@ -647,7 +685,7 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
     for (int r = 0; r < reps; r++) {
         // a lone backward sweep needs the "not yet computed" markers the forward pass sets
         if (pass == 5 && c->p.sweep_mode == 0) {
-            if (f32) launch_sweep_prep32(d, L, visc);
+            if (c->fast_sweep()) launch_sweep_prep32(d, L, visc, c->mixed());
             else launch_sweep_prep(d, L, visc, f32, true);
         }
         if (flush) ck(cudaMemsetAsync(flush, r & 0xff, (size_t)flush_bytes, c->stream), "flush");

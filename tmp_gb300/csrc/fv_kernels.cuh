@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(256) k_cell_update(
     int nc, const int4* __restrict__ cface, const d4* __restrict__ cgeo64, const v4<T>* __restrict__ Fc,
     const v4<T>* __restrict__ Fv, const T* __restrict__ specc, const T* __restrict__ specv, double cfl,
     int stage, double alpha, d4* __restrict__ R, d4* __restrict__ U64, d4* __restrict__ W, d4* __restrict__ W0,
-    double* __restrict__ dt, double* __restrict__ diag, v4<T>* __restrict__ Ulow) {
+    double* __restrict__ dt, double* __restrict__ diag, v4<T>* __restrict__ Ulow, const float* __restrict__ cflmul) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     int4 cf = cface[c];
@@ -345,8 +345,10 @@ __global__ void __launch_bounds__(256) k_cell_update(
             st4(Ulow + c, q);
         }
     } else {
-        // SolveTime + TopologyHolderStrategy::SolveDiag (TopologyHolderStrategy.cpp:190-215)
-        double dtc = cfl * vol / sc;
+        // SolveTime + TopologyHolderStrategy::SolveDiag (TopologyHolderStrategy.cpp:190-215);
+        // an optional per-cell CFL multiplier (local CFL controller) scales the CFL
+        double cl = cflmul ? cfl * (double)cflmul[c] : cfl;
+        double dtc = cl * vol / sc;
         dt[c] = dtc;
         double OMEGAN = 1.5;
         double d = vol / dtc + 0.5 * OMEGAN * sc;

@@ -39,7 +39,7 @@ template <bool V, int M>
 static void update32(const DevArrays& d, const LaunchCfg& L, double cfl, int stage, double alpha) {
     k_cell_update<float, V, M><<<nblk(d.nc, 256), 256, 0, L.stream>>>(
         d.nc, d.cface, d.cgeo, d.Fcf, d.Fvf, d.speccf, d.specvf, cfl, stage, alpha, d.R, d.U, d.W, d.W0, d.dt, d.diag,
-        d.Uf);
+        d.Uf, d.cflmul);
     *L.counter += 1;
 }
 void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage,

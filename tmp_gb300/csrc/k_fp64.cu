@@ -153,7 +153,7 @@ template <bool V, int M>
 static void update64(const DevArrays& d, const LaunchCfg& L, double cfl, int stage, double alpha) {
     k_cell_update<double, V, M><<<nblk(d.nc, 256), 256, 0, L.stream>>>(
         d.nc, d.cface, d.cgeo, d.Fc, d.Fv, d.specc, d.specv, cfl, stage, alpha, d.R, d.U, d.W, d.W0, d.dt, d.diag,
-        (d4*)nullptr);
+        (d4*)nullptr, d.cflmul);
     *L.counter += 1;
 }
 void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage,
@@ -648,11 +648,13 @@ __global__ void __launch_bounds__(256) k_sweep_prep32(int nc, const int4* __rest
     swraf[t] = rA;
 }
 
-void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous) {
+void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, bool mu64) {
     int n = 4 * d.nc;
     float* a = reinterpret_cast<float*>(d.dW1f);
     float* b = reinterpret_cast<float*>(d.dWf);
-    if (viscous)
+    if (viscous && mu64)
+        k_sweep_prep32<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.mu, d.swfcf, d.swraf, d.Wf, a, b);
+    else if (viscous)
         k_sweep_prep32<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muf, d.swfcf, d.swraf, d.Wf, a, b);
     else
         k_sweep_prep32<false, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, (const float*)nullptr, d.swfcf, d.swraf, d.Wf, a, b);
