@@ -166,6 +166,11 @@ int cfd_residual_norm(cfd_case_t c, int mesh, int which, double* out);
 /* Copy a field of one mesh to / from host memory (layout above). */
 int cfd_get_field(cfd_case_t c, int mesh, int which, double* host);
 int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host);
+/* Force on the walls of one mesh from the current state (evaluates the
+ * fluxes first): out4 = {Fx, Fy, CL, CD}, coefficients on 0.5*rho*V^2*ref_length
+ * in the freestream direction.  No reference counterpart: the reference
+ * integrates only Cp (Euler2D.cpp:392-618). */
+int cfd_wall_force(cfd_case_t c, int mesh, double ref_length, double* out4);
 /* Per-cell CFL multipliers of one mesh for LU-SGS (dt_i = CFL * mult_i * vol_i /
  * spec_c,i).  The reference uses one constant CFL (LUSGS_Integrator.h:18); the
  * multipliers are the hook of local-CFL controllers.  NULL removes them. */

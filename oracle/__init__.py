@@ -53,6 +53,7 @@ def _load():
         L.orc_rk_step.restype = C.c_int
         L.orc_lusgs_step.argtypes = [vp, C.c_double, C.c_int]
         L.orc_lusgs_step.restype = C.c_int
+        L.orc_wall_force.argtypes = [vp, dp]
         L.orc_field.argtypes = [vp, C.c_int]
         L.orc_field.restype = dp
         _lib = L
@@ -93,6 +94,12 @@ class Oracle:
 
     def lusgs_step(self, cfl: float, first_order: bool = False) -> int:
         return _load().orc_lusgs_step(self.h, cfl, int(first_order))
+
+    def wall_force(self) -> np.ndarray:
+        """(Fx, Fy) through the wall faces in the last residual evaluation."""
+        f = np.zeros(2)
+        _load().orc_wall_force(self.h, f.ctypes.data_as(C.POINTER(C.c_double)))
+        return f
 
     def field(self, name: str) -> np.ndarray:
         """A live numpy view of one oracle array."""

@@ -34,4 +34,7 @@ for u in "${UNITS[@]}"; do
 done
 for p in "${pids[@]}"; do wait "$p"; done
 "$CXX" "${FLAGS[@]}" "$HERE/ref_driver.cpp" "${OBJS[@]}" -o "$OUT/ref_driver"
-echo "built $OUT/ref_driver"
+# the overset interpolation weights (mathTools/math.cpp) in a second driver
+"$CXX" "${FLAGS[@]}" "$HERE/ref_weights.cpp" "$SRC/mathTools/math.cpp" "$OUT/obj/mathTools_vector3d.o" \
+  -o "$OUT/ref_weights"
+echo "built $OUT/ref_driver $OUT/ref_weights"

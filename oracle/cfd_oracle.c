@@ -43,6 +43,7 @@ typedef struct {
     double *umax, *umin;
     /* integrators */
     double *W, *Wnow, *D, *dW1, *dW;
+    double force[2]; /* momentum flux through wall faces of the last residual */
 } orc_t;
 
 static const double Gamma = 1.4;
@@ -310,6 +311,8 @@ int orc_residual(orc_t* o, int first_order) {
     memset(o->specv, 0, 8 * (size_t)nc);
     memset(o->R, 0, 4 * 8 * (size_t)nc);
     if (face_states(o)) err |= 4;
+    o->force[0] = 0;
+    o->force[1] = 0;
     /* solveGradient */
     for (int k = 0; k < ne; k++) {
         int l = o->lr[2 * k], r = o->lr[2 * k + 1];
@@ -421,6 +424,7 @@ int orc_residual(orc_t* o, int first_order) {
         for (int j = 0; j < 4; j++) o->R[4 * l + j] += F[j];
         if (r >= 0)
             for (int j = 0; j < 4; j++) o->R[4 * r + j] -= F[j];
+        if (r == BC_WALL) { o->force[0] += F[2]; o->force[1] += F[3]; }
     }
     /* LaminarFluxStrategy::computeFlux(int) (LaminarFluxStrategy.h:110-216) */
     if (o->viscous) {
@@ -461,6 +465,7 @@ int orc_residual(orc_t* o, int first_order) {
             for (int j = 0; j < 4; j++) o->R[4 * l + j] -= Fv[j];
             if (r >= 0)
                 for (int j = 0; j < 4; j++) o->R[4 * r + j] += Fv[j];
+            if (r == BC_WALL) { o->force[0] -= Fv[2]; o->force[1] -= Fv[3]; }
         }
     }
     return err;
@@ -561,6 +566,13 @@ int orc_lusgs_step(orc_t* o, double cfl, int first_order) {
         prim_from_cons(o->W + 4 * c, o->U + 4 * c);
     }
     return err;
+}
+
+/* Wall force of the last residual evaluation (Fx, Fy): not in the reference,
+ * which integrates Cp only (Euler2D.cpp:392-618). */
+void orc_wall_force(orc_t* o, double* f) {
+    f[0] = o->force[0];
+    f[1] = o->force[1];
 }
 
 /* Field access by name id (same ids as CFD_FIELD_* in include/cfdgb.h where shared). */

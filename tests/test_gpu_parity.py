@@ -278,3 +278,25 @@ def test_graph_replay_dataflow_epochs():
     a.step(5)
     b.step_graph(5)
     np.testing.assert_array_equal(a.get("U"), b.get("U"))
+
+
+@pytest.mark.parametrize("name", ["mixed_lam_lusgs", "omesh_euler_rk5", "mixed_euler_lusgs_sup"])
+def test_wall_force_and_distance(name, built_oracle):
+    """Wall force (CL/CD) against the oracle's wall-face flux sum; wall distance
+    bit-exact against the reference's ComputeWallCellDistance dump."""
+    import oracle
+    from oracle import grd
+
+    c, g = manifest()[name], golden(name)
+    _, case = make_case(c)
+    np.testing.assert_array_equal(case.get("WALLDIST"), g["geo_wall"])
+    case.put("U", g["init_U"])
+    f = case.wall_force()
+    t = grd.read_grd(GOLDEN / c["mesh"], c["wall_tag"], c["far_tag"])
+    o = oracle.Oracle(t, c["mach"], c["aoa"], c["re"], c["flow"] == "viscous")
+    o.set_U(g["init_U"])
+    o.residual(bool(c["first_order"]))
+    fo = o.wall_force()
+    scale = max(abs(fo[0]), abs(fo[1]))
+    assert abs(f["fx"] - fo[0]) <= 1e-12 * scale and abs(f["fy"] - fo[1]) <= 1e-12 * scale
+    assert np.isfinite(f["cl"]) and np.isfinite(f["cd"])

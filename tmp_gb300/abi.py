@@ -92,6 +92,7 @@ def lib() -> C.CDLL:
         "cfd_bench_pass": (C.c_int, [vp, C.c_int, C.c_int, C.c_longlong, dp]),
         "cfd_selftest_bounded_wait": (C.c_int, [vp, C.c_longlong]),
         "cfd_set_cell_cfl": (C.c_int, [vp, C.c_int, dp]),
+        "cfd_wall_force": (C.c_int, [vp, C.c_int, C.c_double, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -186,6 +187,12 @@ class Case:
         s = C.c_void_p()
         check(lib().cfd_case_stream(self.h, C.byref(s)))
         return s.value or 0
+
+    def wall_force(self, mesh: int = 0, ref_length: float = 1.0) -> dict:
+        """Wall force of the current state: Fx, Fy, CL, CD."""
+        out = np.zeros(4)
+        check(lib().cfd_wall_force(self.h, int(mesh), float(ref_length), _dptr(out)))
+        return dict(fx=out[0], fy=out[1], cl=out[2], cd=out[3])
 
     def set_cell_cfl(self, mult, mesh: int = 0):
         """Per-cell CFL multipliers (None removes them)."""

@@ -29,7 +29,13 @@ struct DevArrays {
     d4* fg0 = nullptr;           // [nf] (nx, ny, length, 125*vol_left)
     d4* fg1 = nullptr;           // [nf] (xf-xl, yf-yl, xf-xr, yf-yr)
     d4* fvis = nullptr;          // [nf] (dx, dy, dx^2+dy^2, 0)
-    double* walld = nullptr;     // [nc]
+    double* walld = nullptr;     // [nc] projected wall distance
+    int* wall_ptr = nullptr;     // [nmesh+1] per-mesh ranges of wall_faces
+    int* wall_faces = nullptr;   // global ids of wall faces, ascending within each mesh
+    int4* wblocks = nullptr;     // (mesh, begin, end) chunks of wall_faces for the force sum
+    int nwblk = 0;
+    double* wpartial = nullptr;  // [2*nwblk]
+    double* wforce = nullptr;    // [2*nmesh] (Fx, Fy)
     // binary32 copies (fast form)
     float4* fg0f = nullptr;
     float4* fg1f = nullptr;
@@ -118,6 +124,8 @@ void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limi
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
 void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);
 void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, bool fp32);
+void launch_wall_distance(const DevArrays& d, const LaunchCfg& L);
+void launch_wall_force(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32);
 // ---- k_fp32.cu ----
 void launch_residual_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);

@@ -117,7 +117,7 @@ void free_case(cfd_case_s* c) {
                     d.cgeo, d.fg0, d.fg1, d.fvis, d.walld, d.fg0f, d.fg1f, d.fvisf, d.cgeof, d.U, d.W, d.W0, d.R,
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
-                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.swfcf, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
+                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.wall_ptr, d.wall_faces, d.wblocks, d.wpartial, d.wforce, d.swfcf, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -416,6 +416,18 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             for (int b = c->coff[i]; b < c->coff[i + 1]; b += chunk)
                 nb.push_back(make_int4(i, b, std::min(b + chunk, c->coff[i + 1]), 0));
         d.nblk_norm = (int)nb.size();
+        // wall faces per mesh (ascending) and their 256-face chunks
+        std::vector<int> wptr(nmesh + 1, 0), wfaces;
+        std::vector<int4> wb;
+        for (int i = 0; i < nmesh; i++) {
+            wptr[i] = (int)wfaces.size();
+            for (int k = c->foff[i]; k < c->foff[i + 1]; k++)
+                if (lr[k].y == kWall) wfaces.push_back(k);
+            for (int b = wptr[i]; b < (int)wfaces.size(); b += 256)
+                wb.push_back(make_int4(i, b, std::min(b + 256, (int)wfaces.size()), 0));
+        }
+        wptr[nmesh] = (int)wfaces.size();
+        d.nwblk = (int)wb.size();
 
         if (stream) {
             c->stream = (cudaStream_t)stream;
@@ -455,6 +467,8 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         }
         dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
         dalloc(&d.err, 2);
+        dalloc(&d.walld, nc); dalloc(&d.wall_ptr, nmesh + 1); dalloc(&d.wall_faces, wfaces.size());
+        dalloc(&d.wblocks, wb.size()); dalloc(&d.wpartial, 2 * wb.size()); dalloc(&d.wforce, 2 * (size_t)nmesh);
         cudaStream_t s = c->stream;
         ck(cudaMemcpyAsync(d.lr, lr.data(), nf * sizeof(int2), cudaMemcpyHostToDevice, s), "upload");
         ck(cudaMemcpyAsync(d.enodes, en.data(), nf * sizeof(int2), cudaMemcpyHostToDevice, s), "upload");
@@ -476,8 +490,14 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         ck(cudaMemsetAsync(d.dW1, 0, nc * sizeof(d4), s), "memset");
         ck(cudaMemsetAsync(d.dW, 0, nc * sizeof(d4), s), "memset");
         ck(cudaMemsetAsync(d.W0, 0, nc * sizeof(d4), s), "memset");
+        ck(cudaMemcpyAsync(d.wall_ptr, wptr.data(), wptr.size() * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+        if (!wfaces.empty())
+            ck(cudaMemcpyAsync(d.wall_faces, wfaces.data(), wfaces.size() * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
+        if (!wb.empty())
+            ck(cudaMemcpyAsync(d.wblocks, wb.data(), wb.size() * sizeof(int4), cudaMemcpyHostToDevice, s), "upload");
         auto L = c->L();
         launch_geometry(d, L);
+        launch_wall_distance(d, L);
         if (c->fp32()) launch_to_fp32(d, L, true);
         else if (c->mixed()) launch_to_fp32(d, L, true);  // binary32 geometry for the sweep
         ck(cudaGetLastError(), "geometry launch");
@@ -628,6 +648,31 @@ int cfd_sync(cfd_case_t c) {
 }
 
 long long cfd_launch_count(cfd_case_t c) { return c ? c->launches : -1; }
+
+int cfd_wall_force(cfd_case_t c, int mesh, double ref_length, double* out4) {
+    if (!c || !out4) return fail(CFD_ERR_ARG, "null argument");
+    if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
+    if (!(ref_length > 0)) return fail(CFD_ERR_ARG, "reference length must be positive");
+    ABI_TRY
+    auto L = c->L();
+    residual_pass(c);  // fluxes of the current state
+    launch_wall_force(c->d, L, c->viscous(), c->fp32());
+    ck(cudaGetLastError(), "wall force launch");
+    double f[2];
+    ck(cudaMemcpyAsync(f, c->d.wforce + 2 * mesh, sizeof(f), cudaMemcpyDeviceToHost, c->stream), "download");
+    int st = check_errors(c);
+    // nondimensional freestream: rho = 1, |V| = M sqrt(gamma); alpha as in set_fs_variable2
+    const MeshPrm& p = c->prm[mesh];
+    double q = 0.5 * p.rho_inf * (p.u_inf * p.u_inf + p.v_inf * p.v_inf) * ref_length;
+    double vm = sqrt(p.u_inf * p.u_inf + p.v_inf * p.v_inf);
+    double ca = p.u_inf / vm, sa = p.v_inf / vm;
+    out4[0] = f[0];
+    out4[1] = f[1];
+    out4[2] = (-f[0] * sa + f[1] * ca) / q;  // lift coefficient
+    out4[3] = (f[0] * ca + f[1] * sa) / q;   // drag coefficient
+    return st;
+    ABI_CATCH
+}
 
 int cfd_set_cell_cfl(cfd_case_t c, int mesh, const double* mult) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
@@ -785,6 +830,12 @@ int cfd_get_field(cfd_case_t c, int mesh, int which, double* host) {
     if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
     ABI_TRY
     if (which >= CFD_FIELD_VOL && which <= CFD_FIELD_ECENTER) return get_geometry(c, mesh, which, host);
+    if (which == CFD_FIELD_WALLDIST) {
+        int off = c->coff[mesh], n = c->coff[mesh + 1] - off;
+        ck(cudaMemcpyAsync(host, c->d.walld + off, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream), "download");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+        return CFD_OK;
+    }
     FieldRef r = field_ref(c, which);
     if (!r.p64 && !r.p32) return fail(CFD_ERR_ARG, "field not available for this case (flow type, precision or id)");
     int off = r.per_face ? c->foff[mesh] : c->coff[mesh];

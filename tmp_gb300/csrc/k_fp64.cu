@@ -841,3 +841,129 @@ void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, bool fp
 }
 
 }  // namespace cfdgb
+
+namespace cfdgb {
+
+// ---------------------------------------------------------------------------
+// Projected wall distance, UnstructBlock2D::ComputeWallCellDistance
+// (UnstructBlock.h:265-298): min over the mesh's wall faces of
+// |(x_c - x_f) . n_f|, starting from 1e11.  A minimum is order-independent, so
+// the brute-force scan (wall faces staged in shared memory) is exact.
+__global__ void __launch_bounds__(256) k_wall_distance(int nc, const int* __restrict__ cmesh,
+                                                       const d4* __restrict__ cgeo, const int* __restrict__ wall_ptr,
+                                                       const int* __restrict__ wall_faces, const d4* __restrict__ fgeo,
+                                                       const d2* __restrict__ fcen, double* __restrict__ walld) {
+    __shared__ double sx[256], sy[256], snx[256], sny[256];
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int m = c < nc ? cmesh[c] : 0;
+    // all cells of a block belong to meshes in [m_lo, m_hi]; stage each mesh's wall list in turn
+    int m_lo = cmesh[min(blockIdx.x * blockDim.x, nc - 1)];
+    int m_hi = cmesh[min(blockIdx.x * blockDim.x + blockDim.x - 1, nc - 1)];
+    double xc = 0, yc = 0;
+    if (c < nc) {
+        d4 g = cgeo[c];
+        xc = g.y;
+        yc = g.z;
+    }
+    double d = 100000000000.0;
+    for (int mm = m_lo; mm <= m_hi; mm++) {
+        int b = wall_ptr[mm], e = wall_ptr[mm + 1];
+        for (int t0 = b; t0 < e; t0 += 256) {
+            int t = t0 + threadIdx.x;
+            __syncthreads();
+            if (t < e) {
+                int f = wall_faces[t];
+                d2 xf = fcen[f];
+                d4 g = fgeo[f];
+                sx[threadIdx.x] = xf.x; sy[threadIdx.x] = xf.y; snx[threadIdx.x] = g.x; sny[threadIdx.x] = g.y;
+            }
+            __syncthreads();
+            if (c < nc && m == mm) {
+                int n = min(256, e - t0);
+                for (int k = 0; k < n; k++) {
+                    double x = xc - sx[k], y = yc - sy[k];
+                    d = smin(d, fabs(dot2(x, y, snx[k], sny[k])));
+                }
+            }
+        }
+    }
+    if (c < nc) walld[c] = d;
+}
+
+void launch_wall_distance(const DevArrays& d, const LaunchCfg& L) {
+    k_wall_distance<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.cmesh, d.cgeo, d.wall_ptr, d.wall_faces, d.fgeo,
+                                                           d.fcen, d.walld);
+    *L.counter += 1;
+}
+
+// ---------------------------------------------------------------------------
+// Force on the walls of each mesh: sum over wall faces of the momentum flux the
+// fluid sends through the face (convective minus viscous, the same terms that
+// enter R[lC]); faces in ascending index within fixed 256-face chunks, chunks
+// added in order, so the result is deterministic.  The reference integrates Cp
+// only (Euler2D.cpp:392-618); lift and drag follow on the host.
+template <class T, bool VISC>
+__global__ void __launch_bounds__(256) k_wall_force(const int* __restrict__ wall_ptr, const int* __restrict__ wall_faces,
+                                                    const int4* __restrict__ wblocks, const v4<T>* __restrict__ Fc,
+                                                    const v4<T>* __restrict__ Fv, double* __restrict__ partial) {
+    __shared__ double sxs[256], sys_[256];
+    int4 b = wblocks[blockIdx.x];  // (mesh, begin, end) in wall_faces
+    double fx = 0.0, fy = 0.0;
+    int t = b.y + threadIdx.x;
+    if (t < b.z) {
+        int f = wall_faces[t];
+        v4<T> c = ld4(Fc + f);
+        fx = (double)c.z;
+        fy = (double)c.w;
+        if (VISC) {
+            v4<T> v = ld4(Fv + f);
+            fx = fx - (double)v.z;
+            fy = fy - (double)v.w;
+        }
+    }
+    sxs[threadIdx.x] = fx;
+    sys_[threadIdx.x] = fy;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sxs[threadIdx.x] += sxs[threadIdx.x + s];
+            sys_[threadIdx.x] += sys_[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = sxs[0];
+        partial[2 * blockIdx.x + 1] = sys_[0];
+    }
+}
+
+__global__ void k_wall_force_final(int nblk_total, const int4* __restrict__ wblocks, const double* __restrict__ partial,
+                                   int nmesh, double* __restrict__ out) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmesh) return;
+    double fx = 0.0, fy = 0.0;
+    for (int i = 0; i < nblk_total; i++)
+        if (wblocks[i].x == m) {
+            fx += partial[2 * i];
+            fy += partial[2 * i + 1];
+        }
+    out[2 * m] = fx;
+    out[2 * m + 1] = fy;
+}
+
+void launch_wall_force(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32) {
+    if (d.nwblk > 0) {
+        if (fp32) {
+            if (viscous) k_wall_force<float, true><<<d.nwblk, 256, 0, L.stream>>>(d.wall_ptr, d.wall_faces, d.wblocks, d.Fcf, d.Fvf, d.wpartial);
+            else k_wall_force<float, false><<<d.nwblk, 256, 0, L.stream>>>(d.wall_ptr, d.wall_faces, d.wblocks, d.Fcf, d.Fvf, d.wpartial);
+        } else {
+            if (viscous) k_wall_force<double, true><<<d.nwblk, 256, 0, L.stream>>>(d.wall_ptr, d.wall_faces, d.wblocks, d.Fc, d.Fv, d.wpartial);
+            else k_wall_force<double, false><<<d.nwblk, 256, 0, L.stream>>>(d.wall_ptr, d.wall_faces, d.wblocks, d.Fc, d.Fv, d.wpartial);
+        }
+        *L.counter += 1;
+    }
+    k_wall_force_final<<<nblk(d.nmesh, 128), 128, 0, L.stream>>>(d.nwblk, d.wblocks, d.wpartial, d.nmesh, d.wforce);
+    *L.counter += 1;
+}
+
+}  // namespace cfdgb
