@@ -192,6 +192,63 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
  * the bounded wait gave up (the expected outcome) and leaves the case usable. */
 int cfd_selftest_bounded_wait(cfd_case_t c, long long polls);
 
+/* ---- overset connectivity and fringe exchange (UniTioga MeshBlock) ------- */
+/* Layouts of a node array for the fringe update (dataUpdate.cpp:4-5). */
+#define CFD_LAYOUT_ROW     0  /* q[node*nvar + k]   */
+#define CFD_LAYOUT_COLUMN  1  /* q[k*nnodes + node] */
+
+typedef struct cfd_block_s* cfd_block_t;    /* one mesh on the device as a donor (MeshBlock) */
+typedef struct cfd_interp_s* cfd_interp_t;  /* an interpolation list (MeshBlock::interpList)  */
+
+/* Interpolation weights of n (cell, point) pairs, evaluated on the device:
+ * computeNodalWeight2D (mathTools/math.cpp:229-312) with solvec and
+ * newtonSolve2D.  nvert[i] is 3 or 4; xv[8*i ..] holds the cell's vertices
+ * (x0,y0,..,x3,y3); xp[2*i ..] the point; frac[4*i ..] receives the weights
+ * (vertex order of xv; 0 in the unused slot of a triangle).  A triangle whose
+ * 2x2 system is singular returns CFD_ERR_MESH (the reference throws).  All
+ * arrays are host memory. */
+int cfd_nodal_weights(long long n, const int* nvert, const double* xv, const double* xp, double* frac);
+/* Upload one mesh's nodes and cells and build its donor-search bins on the
+ * device (replaces the ADT of MeshBlock::search, search.cpp:81-270). */
+int cfd_block_create(cfd_mesh_t mesh, void* stream, cfd_block_t* out);
+void cfd_block_free(cfd_block_t b);
+/* Donor search for npts points (host xy[2*npts]): donor_cell[i] = the lowest-
+ * numbered cell whose bounding box holds the point within TOL = 1e-10 and whose
+ * weights all lie in [-TOL, 1+TOL] (checkContainment.cpp:4-64), else -1.
+ * donor_nodes[4*i] / weights[4*i] (may be NULL) get its vertices and weights
+ * (-1 / 0 when not found or in a triangle's unused slot). */
+int cfd_block_search(cfd_block_t b, long long npts, const double* xy, int* donor_cell, int* donor_nodes,
+                     double* weights);
+/* Cell values as the mean of their nodes' values (Orchestra.cpp:270-291), on
+ * device arrays in ROW layout: q_cell[c*nvar + k] = (sum_j q_node[v_j*nvar + k]) / nvert. */
+int cfd_block_node_to_cell(cfd_block_t b, const double* d_q_node, int nvar, double* d_q_cell, void* stream);
+/* Interpolation list for the receptor points xy[2*n] (host), found in the donor
+ * block: receptor i writes node recv_node[i] of the receiving array.  Points
+ * without a donor are left out of the list (n_found counts those kept). */
+int cfd_interp_create(cfd_block_t donor, long long n, const double* xy, const int* recv_node, cfd_interp_t* out);
+/* Interpolation list from explicit entries (as findInterpData fills interpList,
+ * bookkeeping.cpp:396-424): nweights[i] in {3,4}, inode[4*i], weights[4*i].
+ * A weight outside [-TOL, 1+TOL] returns CFD_ERR_MESH: getInterpolatedSolution
+ * throws "weights are not convex" (dataUpdate.cpp:52-55); the weights of a
+ * list never change, so the check is made once, here. */
+int cfd_interp_create_list(long long n, const int* recv_node, const int* nweights, const int* inode,
+                           const double* weights, void* stream, cfd_interp_t* out);
+int cfd_interp_info(cfd_interp_t it, long long* n_found, long long* n_requested);
+/* Host copies of the list: recv_node[n], donor_cell[n] (-1 for an explicit
+ * list), inode[4n], weights[4n]; any pointer may be NULL. */
+int cfd_interp_get(cfd_interp_t it, int* recv_node, int* donor_cell, int* inode, double* weights);
+/* Fringe exchange on device arrays: every receptor's value is interpolated
+ * from q_donor (getInterpolatedSolution, dataUpdate.cpp:6-111) and then written
+ * into q_recv (updateSolnData, dataUpdate.cpp:113-132), in `layout` with nvar
+ * values per node, asynchronously on `stream` (NULL: the list's stream).  All
+ * values are interpolated before any is written, so the two arrays may be the
+ * same; where several receptors name one node the last in the list wins, as
+ * in the reference's update loop.  Node indices are checked on the host
+ * against nnodes_donor / nnodes_recv (CFD_ERR_ARG). */
+int cfd_interp_update(cfd_interp_t it, const double* d_q_donor, long long nnodes_donor, double* d_q_recv,
+                      long long nnodes_recv, int nvar, int layout, void* stream);
+void cfd_interp_free(cfd_interp_t it);
+
 /* Residual norm of a caller-owned device array that allocates nothing (no
  * counterpart in the reference, which has no device code).  For callers that
  * may not allocate device memory while they run: solvers that reserve all of

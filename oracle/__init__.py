@@ -10,6 +10,9 @@ by the reference's own compiled code (tests/golden/).
   grd.read_grd      .grd reader + cell assembly restated in numpy/Python
                     (reader/UnstructReader.h:124-272, UniTioga/CellBrick.cpp:13-136)
   Oracle            ctypes wrapper of cfd_oracle.c (geometry, residual, RK5, LU-SGS)
+  nodal_weights, donor_search, interp_update
+                    overset weights / containment / fringe update restated in C
+                    (mathTools/math.cpp, UniTioga/checkContainment.cpp, dataUpdate.cpp)
 """
 from __future__ import annotations
 
@@ -56,6 +59,10 @@ def _load():
         L.orc_wall_force.argtypes = [vp, dp]
         L.orc_field.argtypes = [vp, C.c_int]
         L.orc_field.restype = dp
+        L.orc_nodal_weights.argtypes = [C.c_long, ip, dp, dp, dp]
+        L.orc_nodal_weights.restype = C.c_long
+        L.orc_donor_search.argtypes = [dp, C.c_int, ip, ip, C.c_long, dp, ip, ip, dp]
+        L.orc_interp_update.argtypes = [C.c_long, ip, ip, ip, dp, dp, C.c_long, dp, C.c_long, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -113,3 +120,48 @@ class Oracle:
         if getattr(self, "h", None) and _lib is not None:
             _lib.orc_free(self.h)
             self.h = None
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def nodal_weights(nvert, xv, xp):
+    """computeNodalWeight2D for n pairs: nvert[n], xv[n,4,2], xp[n,2] -> (frac[n,4], n_singular)."""
+    nv = np.ascontiguousarray(nvert, np.int32)
+    x = np.ascontiguousarray(xv, np.float64).reshape(-1)
+    p = np.ascontiguousarray(xp, np.float64).reshape(-1)
+    out = np.zeros(4 * nv.size)
+    bad = _load().orc_nodal_weights(nv.size, _ip(nv), _dp(x), _dp(p), _dp(out))
+    return out.reshape(-1, 4), int(bad)
+
+
+def donor_search(xy, cell_verts, cell_nvert, pts):
+    """Brute-force containment: (lowest containing cell, number of containing cells, its weights)."""
+    x = np.ascontiguousarray(xy, np.float64).reshape(-1)
+    cv = np.ascontiguousarray(cell_verts, np.int32).reshape(-1)
+    nv = np.ascontiguousarray(cell_nvert, np.int32)
+    p = np.ascontiguousarray(pts, np.float64).reshape(-1)
+    n = p.size // 2
+    donor = np.zeros(n, np.int32)
+    cnt = np.zeros(n, np.int32)
+    w = np.zeros(4 * n)
+    _load().orc_donor_search(_dp(x), nv.size, _ip(cv), _ip(nv), n, _dp(p), _ip(donor), _ip(cnt), _dp(w))
+    return donor, cnt, w.reshape(n, 4)
+
+
+def interp_update(recv, nw, inode, w, q, nnodes, qr, nnodes_recv, nvar, layout):
+    """getInterpolatedSolution + updateSolnData into qr (modified in place)."""
+    r = np.ascontiguousarray(recv, np.int32)
+    n_w = np.ascontiguousarray(nw, np.int32)
+    i4 = np.ascontiguousarray(inode, np.int32).reshape(-1)
+    w4 = np.ascontiguousarray(w, np.float64).reshape(-1)
+    qa = np.ascontiguousarray(q, np.float64).reshape(-1)
+    assert qr.dtype == np.float64 and qr.flags.c_contiguous
+    _load().orc_interp_update(r.size, _ip(r), _ip(n_w), _ip(i4), _dp(w4), _dp(qa), nnodes, _dp(qr), nnodes_recv,
+                              nvar, layout)
+    return qr

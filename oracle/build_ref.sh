@@ -34,7 +34,21 @@ for u in "${UNITS[@]}"; do
 done
 for p in "${pids[@]}"; do wait "$p"; done
 "$CXX" "${FLAGS[@]}" "$HERE/ref_driver.cpp" "${OBJS[@]}" -o "$OUT/ref_driver"
-# the overset interpolation weights (mathTools/math.cpp) in a second driver
-"$CXX" "${FLAGS[@]}" "$HERE/ref_weights.cpp" "$SRC/mathTools/math.cpp" "$OUT/obj/mathTools_vector3d.o" \
-  -o "$OUT/ref_weights"
-echo "built $OUT/ref_driver $OUT/ref_weights"
+# the overset search, weights and data update (UniTioga + mathTools) in a second driver
+# (MeshBlock.cpp reaches MPI types only through its HDF5 writer: the MPI stand-in is force-included)
+OVS=(UniTioga/search UniTioga/utils UniTioga/ADT UniTioga/recursiveADT UniTioga/checkContainment
+     UniTioga/dataUpdate UniTioga/MeshBlock UniTioga/write UniTioga/linkList
+     mathTools/math mathTools/median mathTools/kaiser)
+OOBJS=()
+pids=()
+for u in "${OVS[@]}"; do
+  o="$OUT/obj/$(echo "$u" | tr '/' '_').o"
+  OOBJS+=("$o")
+  if [ ! -f "$o" ] || [ "$SRC/$u.cpp" -nt "$o" ]; then
+    "$CXX" "${FLAGS[@]}" -include "$HERE/shims/mpi.h" -c "$SRC/$u.cpp" -o "$o" & pids+=($!)
+  fi
+done
+for p in "${pids[@]}"; do wait "$p"; done
+"$CXX" "${FLAGS[@]}" "$HERE/ref_overset.cpp" "${OOBJS[@]}" "$OUT/obj/mathTools_vector3d.o" \
+  "$OUT/obj/mathTools_cellVolume.o" -o "$OUT/ref_overset"
+echo "built $OUT/ref_driver $OUT/ref_overset"

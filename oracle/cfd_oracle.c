@@ -605,3 +605,175 @@ double* orc_field(orc_t* o, int which) {
         default: return 0;
     }
 }
+
+/* ------------------------------------------------------------------------
+ * Overset: interpolation weights, donor search, fringe data update.
+ * ------------------------------------------------------------------------ */
+#define OVS_TOL 1.0e-10 /* TOL, UniTioga/codetypes.h:54 */
+
+/* solvec for n = 2 (mathTools/math.cpp:4-60): elimination with a row exchange
+ * when the pivot is below 1e-8, then back substitution; 0 = singular. */
+static int ovs_solvec2(double* a00, double* a01, double* a10, double* a11, double* b0, double* b1) {
+    const double eps = 1e-8;
+    double fact, sum, t;
+    if (fabs(*a00) < eps) {
+        if (fabs(*a10) < eps) return 0;
+        t = *a00; *a00 = *a10; *a10 = t;
+        t = *a01; *a01 = *a11; *a11 = t;
+        t = *b0; *b0 = *b1; *b1 = t;
+    }
+    fact = -*a10 / *a00;
+    *a10 += fact * *a00;
+    *a11 += fact * *a01;
+    *b1 += fact * *b0;
+    if (fabs(*a11) < eps) return 0;
+    sum = 0;
+    *b1 = (*b1 - sum) / *a11;
+    sum = 0;
+    sum += *a01 * *b1;
+    *b0 = (*b0 - sum) / *a00;
+    return 1;
+}
+
+/* computeNodalWeight2D (math.cpp:229-312) with findClockWise (:190-227) and
+ * newtonSolve2D (:126-187).  x[8] = (x0,y0,..,x3,y3).  Returns 0 for a
+ * singular triangle (the reference throws). */
+static int ovs_weights(int nvert, const double* x, double px, double py, double* frac) {
+    int mp[4] = {0, 1, 2, 3};
+    double f[4][2], p[2], u, v, uv, r0, r1, l00, l01, l10, l11, norm;
+    int i, iter, ok = 1;
+    frac[0] = frac[1] = frac[2] = frac[3] = 0.0;
+    if (nvert == 3) {
+        double a00 = x[0] - x[4], a01 = x[2] - x[4], a10 = x[1] - x[5], a11 = x[3] - x[5];
+        double b0 = px - x[4], b1 = py - x[5];
+        if (!ovs_solvec2(&a00, &a01, &a10, &a11, &b0, &b1)) return 0;
+        frac[0] = b0;
+        frac[1] = b1;
+        frac[2] = 1. - frac[0] - frac[1];
+        return 1;
+    }
+    {
+        double abx = x[2] - x[0], aby = x[3] - x[1], acx = x[4] - x[0], acy = x[5] - x[1];
+        double adx = x[6] - x[0], ady = x[7] - x[1];
+        double zabac = abx * acy - aby * acx, zabad = abx * ady - aby * adx;
+        if (zabac * zabad > 0) {
+            double zacad = acx * ady - acy * adx;
+            if (!(zacad * zabad > 0)) { mp[2] = 3; mp[3] = 2; }
+        } else {
+            mp[1] = 2;
+            mp[2] = 1;
+        }
+    }
+    p[0] = px;
+    p[1] = py;
+    for (i = 0; i < 2; i++) {
+        f[0][i] = x[2 * mp[0] + i] - p[i];
+        f[1][i] = x[2 * mp[1] + i] - x[2 * mp[0] + i];
+        f[2][i] = x[2 * mp[3] + i] - x[2 * mp[0] + i];
+        f[3][i] = x[2 * mp[0] + i] - x[2 * mp[1] + i] + x[2 * mp[2] + i] - x[2 * mp[3] + i];
+    }
+    u = v = 0.5;
+    for (iter = 0; iter < 500; iter++) {
+        uv = u * v;
+        r0 = f[0][0] + f[1][0] * u + f[2][0] * v + f[3][0] * uv;
+        r1 = f[0][1] + f[1][1] * u + f[2][1] * v + f[3][1] * uv;
+        norm = r0 * r0 + r1 * r1;
+        if (sqrt(norm) <= 1e-14) break;
+        l00 = f[1][0] + f[3][0] * v;
+        l01 = f[2][0] + f[3][0] * u;
+        l10 = f[1][1] + f[3][1] * v;
+        l11 = f[2][1] + f[3][1] * u;
+        if (!ovs_solvec2(&l00, &l01, &l10, &l11, &r0, &r1)) { ok = 0; break; }
+        u -= r0 * 1.0;
+        v -= r1 * 1.0;
+    }
+    if (iter == 500 || !ok) { u = 2.0; v = 0.0; }
+    frac[mp[0]] = (1 - u) * (1 - v);
+    frac[mp[1]] = u * (1 - v);
+    frac[mp[2]] = u * v;
+    frac[mp[3]] = (1 - u) * v;
+    return 1;
+}
+
+/* Weights of n (cell, point) pairs; returns the number of singular triangles
+ * (their frac is -1e300). */
+long orc_nodal_weights(long n, const int* nvert, const double* xv, const double* xp, double* frac) {
+    long i, bad = 0;
+    for (i = 0; i < n; i++) {
+        if (!ovs_weights(nvert[i], xv + 8 * i, xp[2 * i], xp[2 * i + 1], frac + 4 * i)) {
+            frac[4 * i] = frac[4 * i + 1] = frac[4 * i + 2] = frac[4 * i + 3] = -1e300;
+            bad++;
+        }
+    }
+    return bad;
+}
+
+/* Containment of MeshBlock::search by brute force: for every point, every cell
+ * whose TOL-widened box holds it (recursiveADT.cpp:117-124) and whose weights
+ * lie in [-TOL, 1+TOL] (checkContainment.cpp:41-46) contains it.  donor[i] =
+ * the lowest such cell (-1 if none), ncontain[i] = how many there are,
+ * w[4*i] = the donor's weights.  cverts[4*c] are 0-based, -1 padded. */
+void orc_donor_search(const double* xy, int ncell, const int* cverts, const int* nvert, long npts,
+                      const double* pts, int* donor, int* ncontain, double* w) {
+    long i;
+    int c, m;
+    for (i = 0; i < npts; i++) {
+        double px = pts[2 * i], py = pts[2 * i + 1];
+        donor[i] = -1;
+        ncontain[i] = 0;
+        w[4 * i] = w[4 * i + 1] = w[4 * i + 2] = w[4 * i + 3] = 0.0;
+        for (c = 0; c < ncell; c++) {
+            double x[8], f[4], xmin = 1.0e15, ymin = 1.0e15, xmax = -1.0e15, ymax = -1.0e15;
+            int nv = nvert[c], inside = 1;
+            for (m = 0; m < 4; m++) {
+                int id = m < nv ? cverts[4 * c + m] : cverts[4 * c + 2];
+                x[2 * m] = xy[2 * id];
+                x[2 * m + 1] = xy[2 * id + 1];
+                if (m < nv) {
+                    xmin = xmin < x[2 * m] ? xmin : x[2 * m];
+                    ymin = ymin < x[2 * m + 1] ? ymin : x[2 * m + 1];
+                    xmax = xmax > x[2 * m] ? xmax : x[2 * m];
+                    ymax = ymax > x[2 * m + 1] ? ymax : x[2 * m + 1];
+                }
+            }
+            if (!(px >= xmin - OVS_TOL && py >= ymin - OVS_TOL && px <= xmax + OVS_TOL && py <= ymax + OVS_TOL))
+                continue;
+            if (!ovs_weights(nv, x, px, py, f)) continue;
+            for (m = 0; m < nv; m++)
+                if ((f[m] + OVS_TOL) * (f[m] - 1.0 - OVS_TOL) > 0) inside = 0;
+            if (!inside) continue;
+            if (donor[i] < 0) {
+                donor[i] = c;
+                for (m = 0; m < 4; m++) w[4 * i + m] = f[m];
+            }
+            ncontain[i]++;
+        }
+    }
+}
+
+/* getInterpolatedSolution + updateSolnData (UniTioga/dataUpdate.cpp:6-132):
+ * receptor i gets sum_m q[inode[4i+m]] * w[4i+m] (m < nw[i], from 0, in list
+ * order) and writes it to node recv[i] of qr, records in list order; layout 0
+ * = ROW q[node*nvar+k], 1 = COLUMN q[k*nnodes+node]. */
+void orc_interp_update(long n, const int* recv, const int* nw, const int* inode, const double* w,
+                       const double* q, long nnodes, double* qr, long nnodes_recv, int nvar, int layout) {
+    long i;
+    int k, m;
+    double* vals = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * (size_t)nvar);
+    for (i = 0; i < n; i++)
+        for (k = 0; k < nvar; k++) {
+            double qq = 0;
+            for (m = 0; m < nw[i]; m++) {
+                long node = inode[4 * i + m];
+                double qv = layout == 0 ? q[node * nvar + k] : q[(long)k * nnodes + node];
+                qq += qv * w[4 * i + m];
+            }
+            vals[i * nvar + k] = qq;
+        }
+    for (i = 0; i < n; i++)
+        for (k = 0; k < nvar; k++) {
+            if (layout == 0) qr[(long)recv[i] * nvar + k] = vals[i * nvar + k];
+            else qr[(long)k * nnodes_recv + recv[i]] = vals[i * nvar + k];
+        }
+    free(vals);
+}

@@ -1,0 +1,198 @@
+// Test-oracle driver around the reference's own overset code (UniTioga and
+// mathTools, compiled from their sources by oracle/build_ref.sh).  Test
+// infrastructure only.  Run it in a scratch directory: the reference's search
+// and data update write debug files into the working directory.
+//
+//   ref_overset weights IN OUT   computeNodalWeight2D (mathTools/math.cpp:229-312)
+//     IN:  int32 n, then n records {int32 nvert, double xv[4][2], double xp[2]}
+//     OUT: n records of double frac[4] (unused entries 0; -1e300 where it throws)
+//   ref_overset search MESH PTS OUT   MeshBlock::search (UniTioga/search.cpp:81-270)
+//     MESH: int32 nnode, ncell; double xy[2*nnode]; int32 nvert[ncell]; int32 verts[4*ncell] (0-based)
+//     PTS:  int32 n; double xy[2*n]
+//     OUT:  int32 donor[n] in the mesh's own cell numbering (-1: none)
+//   ref_overset interp LIST OUT   MeshBlock::getInterpolatedSolution + updateSolnData
+//     (UniTioga/dataUpdate.cpp:6-132), ROW then COLUMN
+//     LIST: int32 nnodes, nvar, ninterp, nrecv_nodes; double q[nnodes*nvar] (ROW);
+//           ninterp records {int32 recv, int32 nw, int32 inode[4], double w[4]}
+//     OUT:  for ROW then COLUMN: double recv_q[nrecv_nodes*nvar] in that layout,
+//           starting from zeros and updated by every record in order
+#include <cstdio>
+#include <cstdlib>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "MeshBlock.h"
+
+void computeNodalWeight2D(double xv[8][3], double* xp, double* frac, int nvert);
+
+template <class T>
+static bool rd(FILE* f, T* p, size_t n) {
+    return fread(p, sizeof(T), n, f) == n;
+}
+
+static int do_weights(const char* in, const char* out) {
+    FILE* fi = fopen(in, "rb");
+    if (!fi) return 3;
+    int n = 0;
+    if (!rd(fi, &n, 1)) return 3;
+    std::vector<double> res(4 * (size_t)n, 0.0);
+    for (int q = 0; q < n; q++) {
+        int nv;
+        double v[8], p[2];
+        if (!rd(fi, &nv, 1) || !rd(fi, v, 8) || !rd(fi, p, 2)) return 3;
+        double xv[8][3] = {{0}};
+        for (int i = 0; i < 4; i++) {
+            xv[i][0] = v[2 * i];
+            xv[i][1] = v[2 * i + 1];
+        }
+        double frac[8] = {0};
+        try {
+            computeNodalWeight2D(xv, p, frac, nv);
+        } catch (const std::exception&) {
+            frac[0] = frac[1] = frac[2] = frac[3] = -1e300;
+        }
+        for (int i = 0; i < 4; i++) res[4 * (size_t)q + i] = frac[i];
+    }
+    fclose(fi);
+    FILE* fo = fopen(out, "wb");
+    if (!fo) return 4;
+    fwrite(res.data(), 8, res.size(), fo);
+    fclose(fo);
+    return 0;
+}
+
+static int do_search(const char* meshf, const char* ptsf, const char* out) {
+    FILE* fm = fopen(meshf, "rb");
+    if (!fm) return 3;
+    int nnode, ncell;
+    if (!rd(fm, &nnode, 1) || !rd(fm, &ncell, 1)) return 3;
+    std::vector<double> xy(2 * (size_t)nnode);
+    std::vector<int> nvert(ncell), verts(4 * (size_t)ncell);
+    if (!rd(fm, xy.data(), xy.size()) || !rd(fm, nvert.data(), ncell) || !rd(fm, verts.data(), verts.size())) return 3;
+    fclose(fm);
+    FILE* fp = fopen(ptsf, "rb");
+    if (!fp) return 3;
+    int n;
+    if (!rd(fp, &n, 1)) return 3;
+    std::vector<double> pts(2 * (size_t)n);
+    if (!rd(fp, pts.data(), pts.size())) return 3;
+    fclose(fp);
+
+    // MeshBlock numbers cells type by type: triangles first, then quadrilaterals.
+    std::vector<int> order;
+    int ntri = 0;
+    for (int pass = 0; pass < 2; pass++)
+        for (int c = 0; c < ncell; c++)
+            if (nvert[c] == (pass == 0 ? 3 : 4)) order.push_back(c);
+    for (int c = 0; c < ncell; c++) ntri += nvert[c] == 3;
+    const int nquad = ncell - ntri;
+
+    MeshBlock* mb = new MeshBlock();
+    mb->d_dim = 2;
+    mb->nnodes = nnode;
+    mb->ncells = ncell;
+    mb->x = xy.data();
+    int types_nv[2], types_nc[2];
+    int* vconn[2] = {nullptr, nullptr};
+    int nt = 0;
+    std::vector<int> vtri, vquad;
+    for (int c : order) {
+        auto& dst = nvert[c] == 3 ? vtri : vquad;
+        for (int m = 0; m < nvert[c]; m++) dst.push_back(verts[4 * (size_t)c + m] + BASE);
+    }
+    if (ntri) { types_nv[nt] = 3; types_nc[nt] = ntri; vconn[nt] = vtri.data(); nt++; }
+    if (nquad) { types_nv[nt] = 4; types_nc[nt] = nquad; vconn[nt] = vquad.data(); nt++; }
+    mb->ntypes = nt;
+    mb->nv = types_nv;
+    mb->nc = types_nc;
+    mb->vconn = vconn;
+    std::vector<double> cellres(ncell, 1.0);
+    mb->cellRes = cellres.data();
+    mb->ihigh = 0;
+    mb->nsearch = n;
+    mb->xsearch = pts.data();
+    std::vector<int> tags(n, 1);
+    std::vector<double> res(n, 1.0);
+    mb->tagsearch = tags.data();
+    mb->res_search = res.data();
+    mb->search();
+    std::vector<int> donor(n, -1);
+    for (int i = 0; i < n; i++) donor[i] = mb->donorId[i] < 0 ? -1 : order[mb->donorId[i]];
+    FILE* fo = fopen(out, "wb");
+    if (!fo) return 4;
+    fwrite(donor.data(), 4, donor.size(), fo);
+    fclose(fo);
+    return 0;  // the block is left allocated: the driver exits next
+}
+
+static int do_interp(const char* listf, const char* out) {
+    FILE* fl = fopen(listf, "rb");
+    if (!fl) return 3;
+    int nnodes, nvar, ninterp, nrecv;
+    if (!rd(fl, &nnodes, 1) || !rd(fl, &nvar, 1) || !rd(fl, &ninterp, 1) || !rd(fl, &nrecv, 1)) return 3;
+    std::vector<double> qrow((size_t)nnodes * nvar);
+    if (!rd(fl, qrow.data(), qrow.size())) return 3;
+    std::vector<int> recv(ninterp), nw(ninterp), inode(4 * (size_t)ninterp);
+    std::vector<double> w(4 * (size_t)ninterp);
+    for (int i = 0; i < ninterp; i++)
+        if (!rd(fl, &recv[i], 1) || !rd(fl, &nw[i], 1) || !rd(fl, &inode[4 * (size_t)i], 4) ||
+            !rd(fl, &w[4 * (size_t)i], 4))
+            return 3;
+    fclose(fl);
+    std::vector<double> qcol((size_t)nnodes * nvar);
+    for (int i = 0; i < nnodes; i++)
+        for (int k = 0; k < nvar; k++) qcol[(size_t)k * nnodes + i] = qrow[(size_t)i * nvar + k];
+
+    MeshBlock* mb = new MeshBlock();
+    mb->d_dim = 2;
+    mb->nnodes = nnodes;
+    mb->ninterp = ninterp;
+    std::vector<double> xdummy(2 * (size_t)nnodes, 0.0);
+    mb->x = xdummy.data();
+    mb->interpList = new INTERPLIST[ninterp];
+    for (int i = 0; i < ninterp; i++) {
+        INTERPLIST& e = mb->interpList[i];
+        e.cancel = 0;
+        e.nweights = nw[i];
+        e.receptorInfo[0] = 0;
+        e.receptorInfo[1] = recv[i];
+        e.receptorInfo[2] = 0;
+        e.inode = new int[nw[i] + 1];
+        e.weights = new double[nw[i] + 1];
+        for (int m = 0; m < nw[i]; m++) {
+            e.inode[m] = inode[4 * (size_t)i + m];
+            e.weights[m] = w[4 * (size_t)i + m];
+        }
+    }
+    FILE* fo = fopen(out, "wb");
+    if (!fo) return 4;
+    for (int layout = 0; layout < 2; layout++) {
+        int nints = 0, nreals = 0;
+        int* idata = nullptr;
+        double* rdata = nullptr;
+        mb->getInterpolatedSolution(&nints, &nreals, &idata, &rdata, layout == 0 ? qrow.data() : qcol.data(),
+                                    nvar, layout);
+        std::vector<double> target((size_t)nrecv * nvar, 0.0);
+        const int save = mb->nnodes;
+        mb->nnodes = nrecv;  // updateSolnData's COLUMN stride is the receiving block's node count
+        for (int i = 0; i < nints; i++) mb->updateSolnData(idata[3 * i + 1], &rdata[(size_t)i * nvar], target.data(), nvar, layout);
+        mb->nnodes = save;
+        fwrite(target.data(), 8, target.size(), fo);
+    }
+    fclose(fo);
+    return 0;
+}
+
+int main(int argc, char** argv) {
+    if (argc < 2) {
+        fprintf(stderr, "usage: %s weights|search|interp ...\n", argv[0]);
+        return 2;
+    }
+    const std::string mode = argv[1];
+    if (mode == "weights" && argc == 4) return do_weights(argv[2], argv[3]);
+    if (mode == "search" && argc == 5) return do_search(argv[2], argv[3], argv[4]);
+    if (mode == "interp" && argc == 4) return do_interp(argv[2], argv[3]);
+    fprintf(stderr, "bad arguments\n");
+    return 2;
+}

@@ -1,0 +1,202 @@
+"""Overset kernels on the GPU against the oracle and the reference's fixtures.
+
+Weights and interpolated values are compared bit for bit.  Donor search is
+compared with the oracle's brute-force containment everywhere (both take the
+lowest-numbered containing cell) and with the reference's own search wherever
+exactly one cell contains the point.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+import oracle
+from oracle import grd
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ov():
+    return np.load(GOLDEN / "overset.npz")
+
+
+def _eq(a, b):
+    return np.array_equal(np.asarray(a, np.float64).view(np.int64), np.asarray(b, np.float64).view(np.int64))
+
+
+def _blocks(abi):
+    out = {}
+    for name, f in (("mx", "mixed.grd"), ("om", "omesh.grd")):
+        mesh = abi.Mesh.load_grd(GOLDEN / f, -1, -2)
+        out[name] = (mesh, abi.Block(mesh), grd.read_grd(GOLDEN / f, -1, -2))
+    return out
+
+
+def test_weights_match_reference(built_lib, ov):
+    from tmp_gb300 import abi
+
+    ok = ov["w_frac"][:, 0] != -1e300
+    f = abi.nodal_weights(ov["w_nvert"][ok], ov["w_xv"][ok], ov["w_xp"][ok])
+    assert _eq(f, ov["w_frac"][ok])
+    with pytest.raises(abi.CfdError) as e:
+        abi.nodal_weights(ov["w_nvert"][~ok][:3], ov["w_xv"][~ok][:3], ov["w_xp"][~ok][:3])
+    assert e.value.code == -3
+
+
+def test_weights_match_oracle_random(built_lib):
+    from tmp_gb300 import abi
+
+    rng = np.random.default_rng(7)
+    n = 200_000
+    nv = rng.choice([3, 4], n).astype(np.int32)
+    xv = rng.normal(0, 1, (n, 4, 2)) * 10.0 ** rng.integers(-6, 3, (n, 1, 1))
+    xp = xv[:, :3].mean(1) + rng.normal(0, 0.5, (n, 2)) * np.abs(xv).max((1, 2))[:, None]
+    ref, bad = oracle.nodal_weights(nv, xv, xp)
+    ok = ref[:, 0] != -1e300
+    assert _eq(abi.nodal_weights(nv[ok], xv[ok], xp[ok]), ref[ok])
+
+
+def test_search_matches_reference_and_oracle(built_lib, ov):
+    from tmp_gb300 import abi
+
+    for name, (mesh, blk, topo) in _blocks(abi).items():
+        pts, ref = ov[f"s_{name}_pts"], ov[f"s_{name}_donor"]
+        d, nodes, w = blk.search(pts)
+        od, cnt, ow = oracle.donor_search(topo.xy, topo.cell_verts, topo.cell_nvert, pts)
+        assert np.array_equal(d, od)
+        assert _eq(w, ow)
+        uniq = cnt <= 1
+        assert np.array_equal(d[uniq], ref[uniq])
+        cv = topo.cell_verts.reshape(-1, 4)
+        hit = d >= 0
+        assert np.array_equal(nodes[hit], cv[d[hit]])
+        assert np.all(nodes[~hit] == -1)
+
+
+def test_search_larger_mesh_random_points(built_lib):
+    from tmp_gb300 import abi, meshgen
+
+    m = meshgen.mixed_mesh(meshgen.naca_body(96), nlayer=12, dr1=2e-3, growth=1.25, rfar=8.0, seed=3,
+                           density=1.0, grade=1.0)
+    path = GOLDEN.parent / "_ovs_tmp.grd"
+    meshgen.write_grd(path, m)
+    try:
+        mesh = abi.Mesh.load_grd(path, -1, -2)
+        topo = grd.read_grd(path, -1, -2)
+    finally:
+        path.unlink()
+    blk = abi.Block(mesh)
+    rng = np.random.default_rng(11)
+    xy = topo.xy.reshape(-1, 2)
+    lo, hi = xy.min(0), xy.max(0)
+    pts = np.concatenate([lo + rng.uniform(-0.02, 1.02, (30000, 2)) * (hi - lo),
+                          xy[rng.choice(len(xy), 2000, replace=False)],
+                          rng.normal(0.5, 0.3, (8000, 2))])
+    d, _, w = blk.search(pts)
+    od, cnt, ow = oracle.donor_search(topo.xy, topo.cell_verts, topo.cell_nvert, pts)
+    assert np.array_equal(d, od) and _eq(w, ow)
+    assert (cnt > 1).sum() > 100 and (d >= 0).sum() > 20000
+
+
+@pytest.mark.parametrize("nvar", [4, 6])
+@pytest.mark.parametrize("layout", [0, 1])
+def test_interp_update_matches_reference(built_lib, ov, nvar, layout):
+    import torch
+
+    from tmp_gb300 import abi
+
+    nn, nr = (int(x) for x in ov[f"i{nvar}_dims"])
+    q = ov[f"i{nvar}_q"]
+    qin = q.reshape(-1) if layout == 0 else np.ascontiguousarray(q.T).reshape(-1)
+    it = abi.Interp.from_list(ov[f"i{nvar}_recv"], ov[f"i{nvar}_nw"], ov[f"i{nvar}_inode"], ov[f"i{nvar}_w"])
+    dq = torch.tensor(qin, dtype=torch.float64, device="cuda")
+    dr = torch.zeros(nr * nvar, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    it.update(dq.data_ptr(), nn, dr.data_ptr(), nr, nvar, layout)
+    torch.cuda.synchronize()
+    ref = ov[f"i{nvar}_row" if layout == 0 else f"i{nvar}_col"]
+    assert _eq(dr.cpu().numpy(), ref)
+
+
+def test_interp_in_place_and_edge_cases(built_lib):
+    import torch
+
+    from tmp_gb300 import abi
+
+    rng = np.random.default_rng(5)
+    nn, nvar, n = 500, 4, 300
+    q = rng.normal(0, 1, nn * nvar)
+    recv = rng.integers(0, nn, n).astype(np.int32)
+    nw = rng.choice([3, 4], n).astype(np.int32)
+    inode = rng.integers(0, nn, (n, 4)).astype(np.int32)
+    w = np.zeros((n, 4))
+    for i in range(n):
+        w[i, :nw[i]] = rng.dirichlet(np.ones(nw[i]))
+    expect = oracle.interp_update(recv, nw, inode, w, q, nn, q.copy(), nn, nvar, 0)
+    it = abi.Interp.from_list(recv, nw, inode, w)
+    dq = torch.tensor(q, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    it.update(dq.data_ptr(), nn, dq.data_ptr(), nn, nvar, abi.LAYOUT_ROW)
+    torch.cuda.synchronize()
+    assert _eq(dq.cpu().numpy(), expect)
+    # empty list, non-convex weights, out-of-range nodes
+    empty = abi.Interp.from_list(np.zeros(0), np.zeros(0), np.zeros((0, 4)), np.zeros((0, 4)))
+    assert empty.info() == (0, 0)
+    empty.update(dq.data_ptr(), nn, dq.data_ptr(), nn, nvar)
+    bad_w = w.copy()
+    bad_w[0, 0] = 1.5
+    with pytest.raises(abi.CfdError) as e:
+        abi.Interp.from_list(recv, nw, inode, bad_w)
+    assert e.value.code == -3
+    with pytest.raises(abi.CfdError):
+        it.update(dq.data_ptr(), 10, dq.data_ptr(), nn, nvar)
+
+
+def test_interp_from_search_and_node_to_cell(built_lib):
+    import torch
+
+    from tmp_gb300 import abi
+
+    blocks = _blocks(abi)
+    mesh_d, blk_d, topo_d = blocks["mx"]
+    _, _, topo_r = blocks["om"]
+    # receptors: the nodes of the other mesh, shifted into the donor's domain
+    pts = topo_r.xy.reshape(-1, 2) * 0.9 + np.array([0.31, -0.17])
+    recv = np.arange(len(pts), dtype=np.int32)
+    it = abi.Interp.search(blk_d, pts, recv)
+    nfound, nreq = it.info()
+    d, nodes, w = blk_d.search(pts)
+    assert nreq == len(pts) and nfound == (d >= 0).sum() > 0
+    r, dc, inode, wl = it.get()
+    hit = d >= 0
+    assert np.array_equal(r, recv[hit]) and np.array_equal(dc, d[hit]) and _eq(wl, w[hit])
+    nvar = 4
+    rng = np.random.default_rng(9)
+    qd = rng.normal(0, 1, topo_d.nnode * nvar)
+    qr = rng.normal(0, 1, topo_r.nnode * nvar)
+    nwl = np.where(inode[:, 3] < 0, 3, 4).astype(np.int32)
+    expect = oracle.interp_update(r, nwl, np.where(inode < 0, 0, inode), wl, qd, topo_d.nnode, qr.copy(),
+                                  topo_r.nnode, nvar, 0)
+    dqd = torch.tensor(qd, dtype=torch.float64, device="cuda")
+    dqr = torch.tensor(qr, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    it.update(dqd.data_ptr(), topo_d.nnode, dqr.data_ptr(), topo_r.nnode, nvar)
+    torch.cuda.synchronize()
+    assert _eq(dqr.cpu().numpy(), expect)
+    # node -> cell mean (Orchestra.cpp:270-291), summed in vertex order then divided
+    dc_out = torch.zeros(topo_d.ncell * nvar, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    blk_d.node_to_cell(dqd.data_ptr(), nvar, dc_out.data_ptr())
+    torch.cuda.synchronize()
+    cv = topo_d.cell_verts.reshape(-1, 4)
+    qn = qd.reshape(-1, nvar)
+    exp = np.zeros((topo_d.ncell, nvar))
+    for c in range(topo_d.ncell):
+        s = np.zeros(nvar)
+        for j in range(topo_d.cell_nvert[c]):
+            s = s + qn[cv[c, j]]
+        exp[c] = s / topo_d.cell_nvert[c]
+    assert _eq(dc_out.cpu().numpy(), exp.reshape(-1))

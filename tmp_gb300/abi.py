@@ -30,6 +30,7 @@ FIELD_SHAPE = dict(U=(4, 0), W=(4, 0), R=(4, 0), GRAD=(8, 0), PHI=(4, 0), SPEC_C
                    MUEDGE=(1, 1), VOL=(1, 0), CENTER=(2, 0), NORMAL=(2, 1), AREA=(1, 1), ECENTER=(2, 1),
                    WALLDIST=(1, 0))
 NORM = dict(DW_RHO2=0, RK_DRHO=1, L2_R_RHO=2)
+LAYOUT_ROW, LAYOUT_COLUMN = 0, 1
 
 
 class CfdError(RuntimeError):
@@ -93,6 +94,17 @@ def lib() -> C.CDLL:
         "cfd_selftest_bounded_wait": (C.c_int, [vp, C.c_longlong]),
         "cfd_set_cell_cfl": (C.c_int, [vp, C.c_int, dp]),
         "cfd_wall_force": (C.c_int, [vp, C.c_int, C.c_double, dp]),
+        "cfd_nodal_weights": (C.c_int, [C.c_longlong, ip, dp, dp, dp]),
+        "cfd_block_create": (C.c_int, [vp, vp, C.POINTER(vp)]),
+        "cfd_block_free": (None, [vp]),
+        "cfd_block_search": (C.c_int, [vp, C.c_longlong, dp, ip, ip, dp]),
+        "cfd_block_node_to_cell": (C.c_int, [vp, vp, C.c_int, vp, vp]),
+        "cfd_interp_create": (C.c_int, [vp, C.c_longlong, dp, ip, C.POINTER(vp)]),
+        "cfd_interp_create_list": (C.c_int, [C.c_longlong, ip, ip, ip, dp, vp, C.POINTER(vp)]),
+        "cfd_interp_info": (C.c_int, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+        "cfd_interp_get": (C.c_int, [vp, ip, ip, ip, dp]),
+        "cfd_interp_update": (C.c_int, [vp, vp, C.c_longlong, vp, C.c_longlong, C.c_int, C.c_int, vp]),
+        "cfd_interp_free": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -260,6 +272,111 @@ class Case:
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
             _lib.cfd_case_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+# ---- overset (UniTioga MeshBlock) -------------------------------------------
+
+def nodal_weights(nvert: np.ndarray, xv: np.ndarray, xp: np.ndarray) -> np.ndarray:
+    """computeNodalWeight2D on the device for n (cell, point) pairs.
+
+    nvert[n] in {3, 4}; xv[n, 4, 2] vertices; xp[n, 2] points -> frac[n, 4]."""
+    nv = np.ascontiguousarray(nvert, dtype=np.int32)
+    x = np.ascontiguousarray(xv, dtype=np.float64).reshape(-1)
+    p = np.ascontiguousarray(xp, dtype=np.float64).reshape(-1)
+    n = nv.size
+    if x.size != 8 * n or p.size != 2 * n:
+        raise ValueError("xv must be [n, 4, 2] and xp [n, 2]")
+    out = np.zeros(4 * n)
+    check(lib().cfd_nodal_weights(n, _iptr(nv), _dptr(x), _dptr(p), _dptr(out)))
+    return out.reshape(n, 4)
+
+
+class Block:
+    """One mesh on the device as an overset donor (MeshBlock)."""
+
+    def __init__(self, mesh: Mesh, stream: int | None = None):
+        self.h = C.c_void_p()
+        self.ncell = mesh.ncell
+        self.nnode = mesh.nnode
+        check(lib().cfd_block_create(mesh.h, C.c_void_p(stream) if stream else None, C.byref(self.h)))
+
+    def search(self, xy: np.ndarray):
+        """(donor_cell[n], donor_nodes[n, 4], weights[n, 4]) for points xy[n, 2]."""
+        p = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
+        n = p.size // 2
+        d = np.zeros(n, np.int32)
+        nodes = np.zeros(4 * n, np.int32)
+        w = np.zeros(4 * n)
+        check(lib().cfd_block_search(self.h, n, _dptr(p), _iptr(d), _iptr(nodes), _dptr(w)))
+        return d, nodes.reshape(n, 4), w.reshape(n, 4)
+
+    def node_to_cell(self, q_node_ptr: int, nvar: int, q_cell_ptr: int, stream: int | None = None):
+        """Device arrays (raw pointers) in ROW layout."""
+        check(lib().cfd_block_node_to_cell(self.h, C.c_void_p(q_node_ptr), int(nvar), C.c_void_p(q_cell_ptr),
+                                           C.c_void_p(stream) if stream else None))
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.cfd_block_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Interp:
+    """An interpolation list (MeshBlock::interpList) resident on the device."""
+
+    def __init__(self, handle: C.c_void_p):
+        self.h = handle
+
+    @classmethod
+    def search(cls, donor: Block, xy: np.ndarray, recv_node: np.ndarray) -> "Interp":
+        p = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
+        r = np.ascontiguousarray(recv_node, dtype=np.int32)
+        h = C.c_void_p()
+        check(lib().cfd_interp_create(donor.h, r.size, _dptr(p), _iptr(r), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_list(cls, recv_node, nweights, inode, weights, stream: int | None = None) -> "Interp":
+        r = np.ascontiguousarray(recv_node, dtype=np.int32)
+        nw = np.ascontiguousarray(nweights, dtype=np.int32)
+        i4 = np.ascontiguousarray(inode, dtype=np.int32).reshape(-1)
+        w4 = np.ascontiguousarray(weights, dtype=np.float64).reshape(-1)
+        h = C.c_void_p()
+        check(lib().cfd_interp_create_list(r.size, _iptr(r), _iptr(nw), _iptr(i4), _dptr(w4),
+                                           C.c_void_p(stream) if stream else None, C.byref(h)))
+        return cls(h)
+
+    def info(self):
+        a, b = C.c_longlong(), C.c_longlong()
+        check(lib().cfd_interp_info(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def get(self):
+        n, _ = self.info()
+        recv = np.zeros(n, np.int32)
+        donor = np.zeros(n, np.int32)
+        inode = np.zeros(4 * n, np.int32)
+        w = np.zeros(4 * n)
+        check(lib().cfd_interp_get(self.h, _iptr(recv), _iptr(donor), _iptr(inode), _dptr(w)))
+        return recv, donor, inode.reshape(n, 4), w.reshape(n, 4)
+
+    def update(self, q_donor_ptr: int, nnodes_donor: int, q_recv_ptr: int, nnodes_recv: int, nvar: int,
+               layout: int = LAYOUT_ROW, stream: int | None = None):
+        """Device arrays (raw pointers)."""
+        check(lib().cfd_interp_update(self.h, C.c_void_p(q_donor_ptr), int(nnodes_donor), C.c_void_p(q_recv_ptr),
+                                      int(nnodes_recv), int(nvar), int(layout),
+                                      C.c_void_p(stream) if stream else None))
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.cfd_interp_free(self.h)
             self.h = None
 
     def __del__(self):

@@ -31,6 +31,7 @@ UNITS = [
     ("k_fp64.cu", ["-fmad=false"]),
     ("k_fp32.cu", []),
     ("k_misc.cu", []),
+    ("k_overset.cu", ["-fmad=false"]),
     ("k_noalloc.cu", []),
 ]
 

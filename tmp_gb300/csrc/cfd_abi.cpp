@@ -79,10 +79,6 @@ namespace cfdgb {
 int set_last_error(int code, const std::string& msg) { return fail(code, msg); }
 }  // namespace cfdgb
 
-struct cfd_mesh_s {
-    HostMesh m;
-};
-
 struct cfd_case_s {
     int nmesh = 0;
     cfd_params_t p{};

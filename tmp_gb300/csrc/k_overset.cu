@@ -1,0 +1,841 @@
+// Overset connectivity and fringe exchange on the device: interpolation
+// weights, donor search and the fringe data update of UniTioga's MeshBlock
+// (mathTools/math.cpp, UniTioga/search.cpp, checkContainment.cpp,
+// dataUpdate.cpp), plus the node-to-cell mean of Orchestra.cpp, and the C ABI
+// entry points for them.
+//
+// This unit is compiled with -fmad=false: every a*b+c is rounded twice, as in
+// the reference's compiled code, so the weights are bit-identical to
+// computeNodalWeight2D's.
+//
+// Donor search.  The reference builds an alternating digital tree over the
+// bounding boxes of the cells near the query points and walks it per point.
+// Here the donor block keeps a uniform grid of bins over its bounding box;
+// each cell is listed, in ascending cell order, in every bin its
+// TOL-widened bounding box touches (a radix sort of (bin, cell) keys makes the
+// lists).  A query thread walks the candidate list of its bin and takes the
+// first cell that passes the reference's two tests: the point lies in the
+// cell's box widened by TOL (recursiveADT.cpp:117-124) and every weight lies in
+// [-TOL, 1 + TOL] (checkContainment.cpp:41-46).  Where exactly one cell passes
+// both tests the donor is the reference's; where several do (a point on a
+// shared edge, within 1e-10) the lowest-numbered one is taken, whereas the
+// reference takes the first in its tree order.
+#include <cuda_runtime.h>
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/cfdgb.h"
+#include "mesh.hpp"
+
+namespace {
+
+constexpr double kTol = 1.0e-10;  // TOL, UniTioga/codetypes.h:54
+constexpr int kNewtonMax = 500;   // newtonSolve2D itmax, math.cpp:131
+
+struct OversetError : std::runtime_error {
+    int code;
+    OversetError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw OversetError(CFD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+void dalloc(T** p, size_t n) {
+    ck(cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc");
+}
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// Weights (mathTools/math.cpp)
+// ---------------------------------------------------------------------------
+
+// solvec (math.cpp:4-60) for a 2x2 system: Gaussian elimination in which a
+// pivot below 1e-8 in magnitude is exchanged with the next row's, then back
+// substitution.  Returns false where the reference sets iflag = 0.
+__device__ __forceinline__ bool solvec2(double& a00, double& a01, double& a10, double& a11, double& b0,
+                                        double& b1) {
+    const double eps = 1e-8;
+    if (fabs(a00) < eps) {
+        if (fabs(a10) < eps) return false;
+        double t;
+        t = a10; a10 = a00; a00 = t;
+        t = a11; a11 = a01; a01 = t;
+        t = b1; b1 = b0; b0 = t;
+    }
+    const double fact = -a10 / a00;
+    a10 += fact * a00;
+    a11 += fact * a01;
+    b1 += fact * b0;
+    if (fabs(a11) < eps) return false;
+    double sum = 0;
+    b1 = (b1 - sum) / a11;
+    sum = 0;
+    sum += a01 * b1;
+    b0 = (b0 - sum) / a00;
+    return true;
+}
+
+// Bilinear parameters (u, v) of the point by Newton's method from (0.5, 0.5)
+// (newtonSolve2D, math.cpp:126-187).  f[term][coord] as in the reference:
+// f0 = v1 - p, f1 = v2 - v1, f2 = v4 - v1, f3 = v1 - v2 + v3 - v4.
+__device__ __forceinline__ void newton2(const double f[4][2], double& u_out, double& v_out) {
+    double u = 0.5, v = 0.5;
+    bool ok = true;
+    int iter;
+    for (iter = 0; iter < kNewtonMax; iter++) {
+        const double uv = u * v;
+        double r0 = f[0][0] + f[1][0] * u + f[2][0] * v + f[3][0] * uv;
+        double r1 = f[0][1] + f[1][1] * u + f[2][1] * v + f[3][1] * uv;
+        const double norm = r0 * r0 + r1 * r1;
+        if (sqrt(norm) <= 1e-14) break;
+        double l00 = f[1][0] + f[3][0] * v, l01 = f[2][0] + f[3][0] * u;
+        double l10 = f[1][1] + f[3][1] * v, l11 = f[2][1] + f[3][1] * u;
+        if (!solvec2(l00, l01, l10, l11, r0, r1)) {
+            ok = false;
+            break;
+        }
+        u -= r0 * 1.0;
+        v -= r1 * 1.0;
+    }
+    if (iter == kNewtonMax || !ok) {
+        u = 2.0;
+        v = 0.0;
+    }
+    u_out = u;
+    v_out = v;
+}
+
+// computeNodalWeight2D (math.cpp:229-312).  x[2*m], y = x[2*m+1] for the cell's
+// vertices in its own order; frac[m] receives the weights in that order.
+// Returns false for a triangle whose system is singular (the reference throws).
+__device__ bool nodal_weights(int nvert, const double x[8], double px, double py, double frac[4]) {
+    frac[0] = frac[1] = frac[2] = frac[3] = 0.0;
+    if (nvert == 3) {
+        double a00 = x[0] - x[4], a01 = x[2] - x[4];
+        double a10 = x[1] - x[5], a11 = x[3] - x[5];
+        double b0 = px - x[4], b1 = py - x[5];
+        if (!solvec2(a00, a01, a10, a11, b0, b1)) return false;
+        frac[0] = b0;
+        frac[1] = b1;
+        frac[2] = 1. - frac[0] - frac[1];
+        return true;
+    }
+    // findClockWise (math.cpp:190-227): which pair of vertices is the diagonal,
+    // from the signs of the z components of AB x AC, AB x AD and AC x AD.
+    const double abx = x[2] - x[0], aby = x[3] - x[1];
+    const double acx = x[4] - x[0], acy = x[5] - x[1];
+    const double adx = x[6] - x[0], ady = x[7] - x[1];
+    const double z_abac = abx * acy - aby * acx;
+    const double z_abad = abx * ady - aby * adx;
+    int m0 = 0, m1 = 1, m2 = 2, m3 = 3;
+    if (z_abac * z_abad > 0) {
+        const double z_acad = acx * ady - acy * adx;
+        if (!(z_acad * z_abad > 0)) {
+            m2 = 3;
+            m3 = 2;
+        }
+    } else {
+        m1 = 2;
+        m2 = 1;
+    }
+    double f[4][2];
+    const double p[2] = {px, py};
+    for (int i = 0; i < 2; i++) {
+        const double x0 = x[2 * m0 + i], x1 = x[2 * m1 + i], x2 = x[2 * m2 + i], x3 = x[2 * m3 + i];
+        f[0][i] = x0 - p[i];
+        f[1][i] = x1 - x0;
+        f[2][i] = x3 - x0;
+        f[3][i] = x0 - x1 + x2 - x3;
+    }
+    double u, v;
+    newton2(f, u, v);
+    const double w0 = (1 - u) * (1 - v), w1 = u * (1 - v), w2 = u * v, w3 = (1 - u) * v;
+    // scatter through the mapping without a dynamically indexed local array
+    frac[0] = m0 == 0 ? w0 : 0.0;  // m0 is always 0
+    frac[1] = m1 == 1 ? w1 : (m2 == 1 ? w2 : 0.0);
+    frac[2] = m2 == 2 ? w2 : (m1 == 2 ? w1 : (m3 == 2 ? w3 : 0.0));
+    frac[3] = m3 == 3 ? w3 : (m2 == 3 ? w2 : 0.0);
+    return true;
+}
+
+__device__ __forceinline__ bool inside_weights(int nvert, const double frac[4]) {
+    for (int m = 0; m < 4; m++) {
+        if (m < nvert && (frac[m] + kTol) * (frac[m] - 1.0 - kTol) > 0) return false;
+    }
+    return true;
+}
+
+__global__ void k_nodal_weights(long long n, const int* __restrict__ nvert, const double* __restrict__ xv,
+                                const double* __restrict__ xp, double* __restrict__ frac, int* err) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x[8];
+    for (int k = 0; k < 8; k++) x[k] = xv[8 * i + k];
+    double f[4];
+    const int nv = nvert[i];
+    if (nv != 3 && nv != 4) {
+        atomicOr(err, 2);
+        for (int k = 0; k < 4; k++) frac[4 * i + k] = 0.0;
+        return;
+    }
+    if (!nodal_weights(nv, x, xp[2 * i], xp[2 * i + 1], f)) atomicOr(err, 1);
+    for (int k = 0; k < 4; k++) frac[4 * i + k] = f[k];
+}
+
+// ---------------------------------------------------------------------------
+// Search bins
+// ---------------------------------------------------------------------------
+
+struct BinGrid {
+    double x0, y0, inv_hx, inv_hy;
+    int nbx, nby;
+};
+
+__device__ __forceinline__ int bin_coord(double x, double x0, double inv_h, int nb) {
+    double d = floor((x - x0) * inv_h);
+    if (!(d >= 0.0)) d = 0.0;
+    if (d > nb - 1) d = nb - 1;
+    return (int)d;
+}
+
+// Per cell: float prefilter box (the TOL-widened box rounded outwards), the
+// range of bins that box touches and their number.
+__global__ void k_cell_boxes(int ncell, const double* __restrict__ xy, const int4* __restrict__ cv, BinGrid g,
+                             float4* __restrict__ fbox, int4* __restrict__ brange, long long* __restrict__ count) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int4 v = cv[c];
+    const int nv = v.w < 0 ? 3 : 4;
+    const int id[4] = {v.x, v.y, v.z, v.w};
+    double xmin = 1.0e15, ymin = 1.0e15, xmax = -1.0e15, ymax = -1.0e15;  // BIGVALUE
+    for (int m = 0; m < 4; m++) {
+        if (m < nv) {
+            const double px = xy[2 * id[m]], py = xy[2 * id[m] + 1];
+            xmin = xmin < px ? xmin : px;
+            ymin = ymin < py ? ymin : py;
+            xmax = xmax > px ? xmax : px;
+            ymax = ymax > py ? ymax : py;
+        }
+    }
+    const double lx = xmin - kTol, ly = ymin - kTol, hx = xmax + kTol, hy = ymax + kTol;
+    fbox[c] = make_float4(__double2float_rd(lx), __double2float_rd(ly), __double2float_ru(hx),
+                          __double2float_ru(hy));
+    const int ix0 = bin_coord(lx, g.x0, g.inv_hx, g.nbx), ix1 = bin_coord(hx, g.x0, g.inv_hx, g.nbx);
+    const int iy0 = bin_coord(ly, g.y0, g.inv_hy, g.nby), iy1 = bin_coord(hy, g.y0, g.inv_hy, g.nby);
+    brange[c] = make_int4(ix0, iy0, ix1, iy1);
+    count[c] = (long long)(ix1 - ix0 + 1) * (iy1 - iy0 + 1);
+}
+
+__global__ void k_emit_keys(int ncell, const int4* __restrict__ brange, const long long* __restrict__ offs, int nbx,
+                            unsigned long long* __restrict__ keys) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int4 r = brange[c];
+    long long o = offs[c];
+    for (int iy = r.y; iy <= r.w; iy++)
+        for (int ix = r.x; ix <= r.z; ix++) {
+            const unsigned long long b = (unsigned long long)iy * nbx + ix;
+            keys[o++] = (b << 32) | (unsigned)c;
+        }
+}
+
+// binptr[b] = first entry of bin b (lower bound of b << 32 in the sorted keys);
+// also peels the cell number off every key.
+__global__ void k_bin_ptr(long long nbins, long long nent, const unsigned long long* __restrict__ keys,
+                          int* __restrict__ binptr, int* __restrict__ cells) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < nent) cells[t] = (int)(keys[t] & 0xffffffffull);
+    if (t > nbins) return;
+    const unsigned long long key = (unsigned long long)t << 32;
+    long long lo = 0, hi = nent;
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (keys[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    binptr[t] = (int)lo;
+}
+
+__global__ void k_donor_search(long long n, const double* __restrict__ pts, const double* __restrict__ xy,
+                               const int4* __restrict__ cv, const float4* __restrict__ fbox,
+                               const int* __restrict__ binptr, const int* __restrict__ cells, BinGrid g,
+                               int* __restrict__ donor, int* __restrict__ dnodes, double* __restrict__ w,
+                               int* err) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double px = pts[2 * i], py = pts[2 * i + 1];
+    const float pxu = __double2float_ru(px), pxd = __double2float_rd(px);
+    const float pyu = __double2float_ru(py), pyd = __double2float_rd(py);
+    const int b = bin_coord(py, g.y0, g.inv_hy, g.nby) * g.nbx + bin_coord(px, g.x0, g.inv_hx, g.nbx);
+    int found = -1;
+    int4 fv = make_int4(-1, -1, -1, -1);
+    double fw[4] = {0.0, 0.0, 0.0, 0.0};
+    const int e1 = binptr[b + 1];
+    for (int e = binptr[b]; e < e1; e++) {
+        const int c = cells[e];
+        const float4 fb = fbox[c];
+        if (pxu < fb.x || pyu < fb.y || pxd > fb.z || pyd > fb.w) continue;
+        const int4 v = cv[c];
+        const int nv = v.w < 0 ? 3 : 4;
+        double x[8];
+        x[0] = xy[2 * v.x]; x[1] = xy[2 * v.x + 1];
+        x[2] = xy[2 * v.y]; x[3] = xy[2 * v.y + 1];
+        x[4] = xy[2 * v.z]; x[5] = xy[2 * v.z + 1];
+        if (nv == 4) {
+            x[6] = xy[2 * v.w]; x[7] = xy[2 * v.w + 1];
+        } else {
+            x[6] = x[4]; x[7] = x[5];
+        }
+        double xmin = 1.0e15, ymin = 1.0e15, xmax = -1.0e15, ymax = -1.0e15;
+        for (int m = 0; m < 4; m++) {
+            if (m < nv) {
+                xmin = xmin < x[2 * m] ? xmin : x[2 * m];
+                ymin = ymin < x[2 * m + 1] ? ymin : x[2 * m + 1];
+                xmax = xmax > x[2 * m] ? xmax : x[2 * m];
+                ymax = ymax > x[2 * m + 1] ? ymax : x[2 * m + 1];
+            }
+        }
+        if (!(px >= xmin - kTol && py >= ymin - kTol && px <= xmax + kTol && py <= ymax + kTol)) continue;
+        double f[4];
+        if (!nodal_weights(nv, x, px, py, f)) {
+            atomicOr(err, 1);
+            continue;
+        }
+        if (!inside_weights(nv, f)) continue;
+        found = c;
+        fv = v;
+        for (int m = 0; m < 4; m++) fw[m] = f[m];
+        break;
+    }
+    donor[i] = found;
+    if (dnodes) {
+        dnodes[4 * i] = fv.x;
+        dnodes[4 * i + 1] = fv.y;
+        dnodes[4 * i + 2] = fv.z;
+        dnodes[4 * i + 3] = found >= 0 ? fv.w : -1;
+    }
+    if (w)
+        for (int m = 0; m < 4; m++) w[4 * i + m] = fw[m];
+}
+
+// ---------------------------------------------------------------------------
+// Fringe exchange (dataUpdate.cpp) and the node-to-cell mean (Orchestra.cpp)
+// ---------------------------------------------------------------------------
+
+// One thread per (receptor, variable): qq = sum over the donor's nodes, in list
+// order, of q[node] * weight, starting from 0 (getInterpolatedSolution).
+__global__ void k_interp_gather(long long n, int nvar, int layout, const int* __restrict__ nw,
+                                const int* __restrict__ inode, const double* __restrict__ w,
+                                const double* __restrict__ q, long long nnodes, double* __restrict__ vals) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n * nvar) return;
+    const long long i = t / nvar;
+    const int k = (int)(t - i * nvar);
+    const int nwi = nw[i];
+    double qq = 0;
+    for (int m = 0; m < 4; m++) {
+        if (m < nwi) {
+            const double weight = w[4 * i + m];
+            const long long node = inode[4 * i + m];
+            const double qv = layout == CFD_LAYOUT_ROW ? q[node * nvar + k] : q[(long long)k * nnodes + node];
+            qq += qv * weight;
+        }
+    }
+    vals[t] = qq;
+}
+
+// updateSolnData: receptor i's values into node recv[i] of the receiving array.
+__global__ void k_interp_scatter(long long n, int nvar, int layout, const int* __restrict__ recv,
+                                 const double* __restrict__ vals, double* __restrict__ q, long long nnodes) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n * nvar) return;
+    const long long i = t / nvar;
+    const int k = (int)(t - i * nvar);
+    const long long node = recv[i];
+    if (layout == CFD_LAYOUT_ROW) q[node * nvar + k] = vals[t];
+    else q[(long long)k * nnodes + node] = vals[t];
+}
+
+__global__ void k_node_to_cell(int ncell, int nvar, const int4* __restrict__ cv, const double* __restrict__ qn,
+                               double* __restrict__ qc) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)ncell * nvar) return;
+    const int c = (int)(t / nvar);
+    const int k = (int)(t - (long long)c * nvar);
+    const int4 v = cv[c];
+    const int nv = v.w < 0 ? 3 : 4;
+    double s = 0;
+    s += qn[(long long)v.x * nvar + k];
+    s += qn[(long long)v.y * nvar + k];
+    s += qn[(long long)v.z * nvar + k];
+    if (nv == 4) s += qn[(long long)v.w * nvar + k];
+    s /= nv;
+    qc[t] = s;
+}
+
+inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Handles
+// ---------------------------------------------------------------------------
+
+struct cfd_block_s {
+    int nnode = 0, ncell = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    double* xy = nullptr;  // 2*nnode
+    int4* cv = nullptr;    // ncell, w = -1 for a triangle
+    float4* fbox = nullptr;
+    BinGrid grid{};
+    long long nbins = 0, nent = 0;
+    int* binptr = nullptr;  // nbins + 1
+    int* cells = nullptr;   // nent
+    int* err = nullptr;
+    ~cfd_block_s() {
+        dfree(xy);
+        dfree(cv);
+        dfree(fbox);
+        dfree(binptr);
+        dfree(cells);
+        dfree(err);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct cfd_interp_s {
+    long long n = 0, requested = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<int> h_recv, h_donor, h_nw, h_inode;
+    std::vector<double> h_w;
+    int* recv = nullptr;
+    int* nw = nullptr;
+    int* inode = nullptr;
+    double* w = nullptr;
+    double* vals = nullptr;
+    long long vals_cap = 0;
+    ~cfd_interp_s() {
+        dfree(recv);
+        dfree(nw);
+        dfree(inode);
+        dfree(w);
+        dfree(vals);
+    }
+};
+
+namespace {
+
+int report(const OversetError& e) { return cfdgb::set_last_error(e.code, e.what()); }
+
+void read_err(int* d_err, cudaStream_t s, int* h) {
+    ck(cudaMemcpyAsync(h, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}
+
+// Search points (device) in block b; outputs are device arrays.
+void search_device(cfd_block_t b, long long n, const double* d_pts, int* d_donor, int* d_nodes, double* d_w) {
+    if (n == 0) return;
+    ck(cudaMemsetAsync(b->err, 0, sizeof(int), b->stream), "cudaMemsetAsync");
+    k_donor_search<<<blocks_for(n, 128), 128, 0, b->stream>>>(n, d_pts, b->xy, b->cv, b->fbox, b->binptr, b->cells,
+                                                               b->grid, d_donor, d_nodes, d_w, b->err);
+    ck(cudaGetLastError(), "k_donor_search");
+    int h = 0;
+    read_err(b->err, b->stream, &h);
+    if (h & 1) throw OversetError(CFD_ERR_MESH, "donor search: a triangle's weight system is singular (matrix degenerate)");
+}
+
+// Keep the last entry per receiving node (updateSolnData writes in list order,
+// so the last one wins) and upload the list.
+void finish_list(cfd_interp_s* it) {
+    const long long n0 = (long long)it->h_recv.size();
+    std::vector<char> keep(n0, 1);
+    {
+        std::vector<std::pair<int, long long>> order(n0);
+        for (long long i = 0; i < n0; i++) order[i] = {it->h_recv[i], i};
+        std::stable_sort(order.begin(), order.end(),
+                         [](const auto& a, const auto& b) { return a.first < b.first; });
+        for (long long j = 0; j + 1 < n0; j++)
+            if (order[j].first == order[j + 1].first) keep[order[j].second] = 0;
+    }
+    long long n = 0;
+    for (long long i = 0; i < n0; i++) {
+        if (!keep[i]) continue;
+        it->h_recv[n] = it->h_recv[i];
+        it->h_donor[n] = it->h_donor[i];
+        it->h_nw[n] = it->h_nw[i];
+        for (int m = 0; m < 4; m++) {
+            it->h_inode[4 * n + m] = it->h_inode[4 * i + m];
+            it->h_w[4 * n + m] = it->h_w[4 * i + m];
+        }
+        n++;
+    }
+    it->n = n;
+    it->h_recv.resize(n);
+    it->h_donor.resize(n);
+    it->h_nw.resize(n);
+    it->h_inode.resize(4 * n);
+    it->h_w.resize(4 * n);
+    dalloc(&it->recv, n);
+    dalloc(&it->nw, n);
+    dalloc(&it->inode, 4 * n);
+    dalloc(&it->w, 4 * n);
+    ck(cudaMemcpyAsync(it->recv, it->h_recv.data(), n * sizeof(int), cudaMemcpyHostToDevice, it->stream), "copy");
+    ck(cudaMemcpyAsync(it->nw, it->h_nw.data(), n * sizeof(int), cudaMemcpyHostToDevice, it->stream), "copy");
+    ck(cudaMemcpyAsync(it->inode, it->h_inode.data(), 4 * n * sizeof(int), cudaMemcpyHostToDevice, it->stream),
+       "copy");
+    ck(cudaMemcpyAsync(it->w, it->h_w.data(), 4 * n * sizeof(double), cudaMemcpyHostToDevice, it->stream), "copy");
+    ck(cudaStreamSynchronize(it->stream), "cudaStreamSynchronize");
+}
+
+}  // namespace
+
+extern "C" {
+
+int cfd_nodal_weights(long long n, const int* nvert, const double* xv, const double* xp, double* frac) {
+    if (n < 0 || (n > 0 && (!nvert || !xv || !xp || !frac))) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_nodal_weights: bad argument");
+    if (n == 0) return CFD_OK;
+    int *d_nv = nullptr, *d_err = nullptr;
+    double *d_xv = nullptr, *d_xp = nullptr, *d_f = nullptr;
+    int rc = CFD_OK;
+    try {
+        dalloc(&d_nv, n);
+        dalloc(&d_xv, 8 * n);
+        dalloc(&d_xp, 2 * n);
+        dalloc(&d_f, 4 * n);
+        dalloc(&d_err, 1);
+        ck(cudaMemcpy(d_nv, nvert, n * sizeof(int), cudaMemcpyHostToDevice), "copy");
+        ck(cudaMemcpy(d_xv, xv, 8 * n * sizeof(double), cudaMemcpyHostToDevice), "copy");
+        ck(cudaMemcpy(d_xp, xp, 2 * n * sizeof(double), cudaMemcpyHostToDevice), "copy");
+        ck(cudaMemset(d_err, 0, sizeof(int)), "cudaMemset");
+        k_nodal_weights<<<blocks_for(n, 128), 128>>>(n, d_nv, d_xv, d_xp, d_f, d_err);
+        ck(cudaGetLastError(), "k_nodal_weights");
+        ck(cudaMemcpy(frac, d_f, 4 * n * sizeof(double), cudaMemcpyDeviceToHost), "copy");
+        int h = 0;
+        ck(cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost), "copy");
+        if (h & 2) throw OversetError(CFD_ERR_ARG, "cfd_nodal_weights: nvert must be 3 or 4");
+        if (h & 1) throw OversetError(CFD_ERR_MESH, "cfd_nodal_weights: Error matrix degenerate (singular triangle)");
+    } catch (const OversetError& e) {
+        rc = report(e);
+    }
+    dfree(d_nv);
+    dfree(d_xv);
+    dfree(d_xp);
+    dfree(d_f);
+    dfree(d_err);
+    return rc;
+}
+
+int cfd_block_create(cfd_mesh_t mesh, void* stream, cfd_block_t* out) {
+    if (!mesh || !out) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_block_create: null argument");
+    *out = nullptr;
+    const cfdgb::HostMesh& m = mesh->m;
+    if (m.ncell <= 0 || m.nnode <= 0) return cfdgb::set_last_error(CFD_ERR_MESH, "cfd_block_create: empty mesh");
+    cfd_block_s* b = new (std::nothrow) cfd_block_s;
+    if (!b) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_block_create: out of host memory");
+    void* tmp = nullptr;
+    long long* d_count = nullptr;
+    long long* d_offs = nullptr;
+    int4* d_brange = nullptr;
+    unsigned long long *d_k0 = nullptr, *d_k1 = nullptr;
+    try {
+        b->nnode = m.nnode;
+        b->ncell = m.ncell;
+        if (stream) {
+            b->stream = (cudaStream_t)stream;
+        } else {
+            ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            b->own_stream = true;
+        }
+        cudaStream_t s = b->stream;
+        std::vector<int4> hcv(m.ncell);
+        for (int c = 0; c < m.ncell; c++) {
+            const int* v = &m.cell_verts[4 * c];
+            if (m.cell_nvert[c] != 3 && m.cell_nvert[c] != 4)
+                throw OversetError(CFD_ERR_MESH, "cfd_block_create: only triangles and quadrilaterals");
+            hcv[c] = make_int4(v[0], v[1], v[2], m.cell_nvert[c] == 4 ? v[3] : -1);
+        }
+        // Bins: a uniform grid over the nodes' box with about four bins per cell.
+        double x0 = 1e300, y0 = 1e300, x1 = -1e300, y1 = -1e300;
+        for (int i = 0; i < m.nnode; i++) {
+            x0 = std::min(x0, m.xy[2 * i]);
+            x1 = std::max(x1, m.xy[2 * i]);
+            y0 = std::min(y0, m.xy[2 * i + 1]);
+            y1 = std::max(y1, m.xy[2 * i + 1]);
+        }
+        const double ex = std::max(x1 - x0, 1e-300), ey = std::max(y1 - y0, 1e-300);
+        const double h = std::sqrt(ex * ey / (4.0 * m.ncell));
+        const int nbx = (int)std::min(16384.0, std::max(1.0, std::ceil(ex / h)));
+        const int nby = (int)std::min(16384.0, std::max(1.0, std::ceil(ey / h)));
+        b->grid = BinGrid{x0, y0, nbx / ex, nby / ey, nbx, nby};
+        b->nbins = (long long)nbx * nby;
+
+        dalloc(&b->xy, 2 * (size_t)m.nnode);
+        dalloc(&b->cv, m.ncell);
+        dalloc(&b->fbox, m.ncell);
+        dalloc(&b->err, 1);
+        dalloc(&d_count, m.ncell);
+        dalloc(&d_offs, m.ncell + 1);
+        dalloc(&d_brange, m.ncell);
+        ck(cudaMemcpyAsync(b->xy, m.xy.data(), 2 * (size_t)m.nnode * sizeof(double), cudaMemcpyHostToDevice, s),
+           "copy");
+        ck(cudaMemcpyAsync(b->cv, hcv.data(), m.ncell * sizeof(int4), cudaMemcpyHostToDevice, s), "copy");
+        k_cell_boxes<<<blocks_for(m.ncell, 256), 256, 0, s>>>(m.ncell, b->xy, b->cv, b->grid, b->fbox, d_brange,
+                                                             d_count);
+        ck(cudaGetLastError(), "k_cell_boxes");
+        size_t tb_scan = 0, tb_sort = 0;
+        ck(cub::DeviceScan::InclusiveSum(nullptr, tb_scan, d_count, d_offs + 1, m.ncell, s), "scan size");
+        ck(cudaMemsetAsync(d_offs, 0, sizeof(long long), s), "cudaMemsetAsync");
+        ck(cudaMalloc(&tmp, std::max<size_t>(tb_scan, 1)), "cudaMalloc");
+        ck(cub::DeviceScan::InclusiveSum(tmp, tb_scan, d_count, d_offs + 1, m.ncell, s), "scan");
+        long long nent = 0;
+        ck(cudaMemcpyAsync(&nent, d_offs + m.ncell, sizeof(long long), cudaMemcpyDeviceToHost, s), "copy");
+        ck(cudaStreamSynchronize(s), "sync");
+        if (nent >= (1ll << 31)) throw OversetError(CFD_ERR_MESH, "cfd_block_create: too many bin entries");
+        b->nent = nent;
+        dalloc(&d_k0, nent);
+        dalloc(&d_k1, nent);
+        k_emit_keys<<<blocks_for(m.ncell, 256), 256, 0, s>>>(m.ncell, d_brange, d_offs, nbx, d_k0);
+        ck(cudaGetLastError(), "k_emit_keys");
+        int bin_bits = 1;
+        while ((1ll << bin_bits) < b->nbins + 1) bin_bits++;
+        cub::DoubleBuffer<unsigned long long> keys(d_k0, d_k1);
+        ck(cub::DeviceRadixSort::SortKeys(nullptr, tb_sort, keys, (int)nent, 0, 32 + bin_bits, s), "sort size");
+        ck(cudaStreamSynchronize(s), "sync");
+        cudaFree(tmp);
+        tmp = nullptr;
+        ck(cudaMalloc(&tmp, std::max<size_t>(tb_sort, 1)), "cudaMalloc");
+        ck(cub::DeviceRadixSort::SortKeys(tmp, tb_sort, keys, (int)nent, 0, 32 + bin_bits, s), "sort");
+        dalloc(&b->binptr, b->nbins + 1);
+        dalloc(&b->cells, nent);
+        const long long nt = std::max(nent, b->nbins + 1);
+        k_bin_ptr<<<blocks_for(nt, 256), 256, 0, s>>>(b->nbins, nent, keys.Current(), b->binptr, b->cells);
+        ck(cudaGetLastError(), "k_bin_ptr");
+        ck(cudaStreamSynchronize(s), "sync");
+    } catch (const OversetError& e) {
+        if (tmp) cudaFree(tmp);
+        dfree(d_count);
+        dfree(d_offs);
+        dfree(d_brange);
+        dfree(d_k0);
+        dfree(d_k1);
+        delete b;
+        return report(e);
+    }
+    cudaFree(tmp);
+    dfree(d_count);
+    dfree(d_offs);
+    dfree(d_brange);
+    dfree(d_k0);
+    dfree(d_k1);
+    *out = b;
+    return CFD_OK;
+}
+
+void cfd_block_free(cfd_block_t b) { delete b; }
+
+int cfd_block_search(cfd_block_t b, long long npts, const double* xy, int* donor_cell, int* donor_nodes,
+                     double* weights) {
+    if (!b || npts < 0 || (npts > 0 && (!xy || !donor_cell)))
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_block_search: bad argument");
+    if (npts == 0) return CFD_OK;
+    double *d_pts = nullptr, *d_w = nullptr;
+    int *d_donor = nullptr, *d_nodes = nullptr;
+    int rc = CFD_OK;
+    try {
+        cudaStream_t s = b->stream;
+        dalloc(&d_pts, 2 * npts);
+        dalloc(&d_donor, npts);
+        if (donor_nodes) dalloc(&d_nodes, 4 * npts);
+        if (weights) dalloc(&d_w, 4 * npts);
+        ck(cudaMemcpyAsync(d_pts, xy, 2 * npts * sizeof(double), cudaMemcpyHostToDevice, s), "copy");
+        search_device(b, npts, d_pts, d_donor, d_nodes, d_w);
+        ck(cudaMemcpyAsync(donor_cell, d_donor, npts * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+        if (donor_nodes)
+            ck(cudaMemcpyAsync(donor_nodes, d_nodes, 4 * npts * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+        if (weights) ck(cudaMemcpyAsync(weights, d_w, 4 * npts * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
+        ck(cudaStreamSynchronize(s), "sync");
+    } catch (const OversetError& e) {
+        rc = report(e);
+    }
+    dfree(d_pts);
+    dfree(d_donor);
+    dfree(d_nodes);
+    dfree(d_w);
+    return rc;
+}
+
+int cfd_block_node_to_cell(cfd_block_t b, const double* d_q_node, int nvar, double* d_q_cell, void* stream) {
+    if (!b || !d_q_node || !d_q_cell || nvar <= 0)
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_block_node_to_cell: bad argument");
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    const long long n = (long long)b->ncell * nvar;
+    k_node_to_cell<<<blocks_for(n, 256), 256, 0, s>>>(b->ncell, nvar, b->cv, d_q_node, d_q_cell);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cfdgb::set_last_error(CFD_ERR_CUDA, std::string("k_node_to_cell: ") + cudaGetErrorString(e));
+    return CFD_OK;
+}
+
+int cfd_interp_create(cfd_block_t donor, long long n, const double* xy, const int* recv_node, cfd_interp_t* out) {
+    if (!donor || !out || n < 0 || (n > 0 && (!xy || !recv_node)))
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_create: bad argument");
+    *out = nullptr;
+    cfd_interp_s* it = new (std::nothrow) cfd_interp_s;
+    if (!it) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_create: out of host memory");
+    it->stream = donor->stream;
+    it->requested = n;
+    double *d_pts = nullptr, *d_w = nullptr;
+    int *d_donor = nullptr, *d_nodes = nullptr;
+    try {
+        std::vector<int> hd(n), hn(4 * n);
+        std::vector<double> hw(4 * n);
+        if (n > 0) {
+            cudaStream_t s = donor->stream;
+            dalloc(&d_pts, 2 * n);
+            dalloc(&d_donor, n);
+            dalloc(&d_nodes, 4 * n);
+            dalloc(&d_w, 4 * n);
+            ck(cudaMemcpyAsync(d_pts, xy, 2 * n * sizeof(double), cudaMemcpyHostToDevice, s), "copy");
+            search_device(donor, n, d_pts, d_donor, d_nodes, d_w);
+            ck(cudaMemcpyAsync(hd.data(), d_donor, n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+            ck(cudaMemcpyAsync(hn.data(), d_nodes, 4 * n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+            ck(cudaMemcpyAsync(hw.data(), d_w, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
+            ck(cudaStreamSynchronize(s), "sync");
+        }
+        for (long long i = 0; i < n; i++) {
+            if (hd[i] < 0) continue;
+            it->h_recv.push_back(recv_node[i]);
+            it->h_donor.push_back(hd[i]);
+            it->h_nw.push_back(hn[4 * i + 3] < 0 ? 3 : 4);
+            for (int m = 0; m < 4; m++) {
+                it->h_inode.push_back(hn[4 * i + m] < 0 ? 0 : hn[4 * i + m]);
+                it->h_w.push_back(hw[4 * i + m]);
+            }
+        }
+        finish_list(it);
+    } catch (const OversetError& e) {
+        dfree(d_pts);
+        dfree(d_donor);
+        dfree(d_nodes);
+        dfree(d_w);
+        delete it;
+        return report(e);
+    }
+    dfree(d_pts);
+    dfree(d_donor);
+    dfree(d_nodes);
+    dfree(d_w);
+    *out = it;
+    return CFD_OK;
+}
+
+int cfd_interp_create_list(long long n, const int* recv_node, const int* nweights, const int* inode,
+                           const double* weights, void* stream, cfd_interp_t* out) {
+    if (!out || n < 0 || (n > 0 && (!recv_node || !nweights || !inode || !weights)))
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_create_list: bad argument");
+    *out = nullptr;
+    for (long long i = 0; i < n; i++)
+        if ((nweights[i] != 3 && nweights[i] != 4) || recv_node[i] < 0)
+            return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_create_list: nweights must be 3 or 4 and recv_node >= 0");
+    for (long long i = 0; i < 4 * n; i++) {
+        if ((i % 4) >= nweights[i / 4]) continue;
+        if (inode[i] < 0) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_create_list: negative donor node");
+        // getInterpolatedSolution's convexity check (dataUpdate.cpp:52-55), made once here
+        if (weights[i] < -kTol || weights[i] > 1.0 + kTol)
+            return cfdgb::set_last_error(CFD_ERR_MESH, "cfd_interp_create_list: weights are not convex");
+    }
+    cfd_interp_s* it = new (std::nothrow) cfd_interp_s;
+    if (!it) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_create_list: out of host memory");
+    try {
+        if (stream) {
+            it->stream = (cudaStream_t)stream;
+        } else {
+            it->stream = cudaStreamPerThread;
+        }
+        it->requested = n;
+        it->h_recv.assign(recv_node, recv_node + n);
+        it->h_donor.assign(n, -1);
+        it->h_nw.assign(nweights, nweights + n);
+        it->h_inode.resize(4 * n);
+        it->h_w.resize(4 * n);
+        for (long long i = 0; i < 4 * n; i++) {
+            const bool used = (i % 4) < nweights[i / 4];
+            it->h_inode[i] = used ? inode[i] : 0;
+            it->h_w[i] = used ? weights[i] : 0.0;
+        }
+        finish_list(it);
+    } catch (const OversetError& e) {
+        delete it;
+        return report(e);
+    }
+    *out = it;
+    return CFD_OK;
+}
+
+int cfd_interp_info(cfd_interp_t it, long long* n_found, long long* n_requested) {
+    if (!it) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_info: null handle");
+    if (n_found) *n_found = it->n;
+    if (n_requested) *n_requested = it->requested;
+    return CFD_OK;
+}
+
+int cfd_interp_get(cfd_interp_t it, int* recv_node, int* donor_cell, int* inode, double* weights) {
+    if (!it) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_get: null handle");
+    if (recv_node) std::copy(it->h_recv.begin(), it->h_recv.end(), recv_node);
+    if (donor_cell) std::copy(it->h_donor.begin(), it->h_donor.end(), donor_cell);
+    if (inode)
+        for (long long i = 0; i < 4 * it->n; i++) inode[i] = (i % 4) < it->h_nw[i / 4] ? it->h_inode[i] : -1;
+    if (weights) std::copy(it->h_w.begin(), it->h_w.end(), weights);
+    return CFD_OK;
+}
+
+int cfd_interp_update(cfd_interp_t it, const double* d_q_donor, long long nnodes_donor, double* d_q_recv,
+                      long long nnodes_recv, int nvar, int layout, void* stream) {
+    if (!it || !d_q_donor || !d_q_recv || nvar <= 0 || (layout != CFD_LAYOUT_ROW && layout != CFD_LAYOUT_COLUMN))
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_update: bad argument");
+    if (it->n == 0) return CFD_OK;
+    for (long long i = 0; i < it->n; i++)
+        if (it->h_recv[i] >= nnodes_recv)
+            return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_update: a receptor node is beyond nnodes_recv");
+    for (long long i = 0; i < 4 * it->n; i++)
+        if ((i % 4) < it->h_nw[i / 4] && it->h_inode[i] >= nnodes_donor)
+            return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_interp_update: a donor node is beyond nnodes_donor");
+    cudaStream_t s = stream ? (cudaStream_t)stream : it->stream;
+    try {
+        const long long nv = it->n * nvar;
+        if (nv > it->vals_cap) {
+            dfree(it->vals);
+            dalloc(&it->vals, nv);
+            it->vals_cap = nv;
+        }
+        k_interp_gather<<<blocks_for(nv, 256), 256, 0, s>>>(it->n, nvar, layout, it->nw, it->inode, it->w, d_q_donor,
+                                                           nnodes_donor, it->vals);
+        ck(cudaGetLastError(), "k_interp_gather");
+        k_interp_scatter<<<blocks_for(nv, 256), 256, 0, s>>>(it->n, nvar, layout, it->recv, it->vals, d_q_recv,
+                                                            nnodes_recv);
+        ck(cudaGetLastError(), "k_interp_scatter");
+    } catch (const OversetError& e) {
+        return report(e);
+    }
+    return CFD_OK;
+}
+
+void cfd_interp_free(cfd_interp_t it) { delete it; }
+
+}  // extern "C"

@@ -34,4 +34,12 @@ HostMesh mesh_from_arrays(int nnode, const double* xy, int nedge, const int* edg
 // Compute lev_fwd / lev_bwd (called by the builders).
 void build_levels(HostMesh& m);
 
+// Lets translation units other than the ABI's report through cfd_last_error().
+int set_last_error(int code, const std::string& msg);
+
 }  // namespace cfdgb
+
+// The opaque cfd_mesh_t handle of the C ABI.
+struct cfd_mesh_s {
+    cfdgb::HostMesh m;
+};
