@@ -7,7 +7,16 @@ Workload (default, config C2): laminar Navier-Stokes around a cylinder on a
 LU-SGS at CFL 50.  One step = one LU-SGS iteration (residual, local dt,
 diagonal, forward + backward level-scheduled sweeps, update) over the mesh.
 
-  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--precision fp64|fp32]
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--precision fp64|fp32|mixed]
+
+Precision forms: fp64 = the plain path (every kernel in binary64, results
+equal to the reference's); fp32 = fluxes, gradients, limiter and the LU-SGS
+sweep in binary32 with the update, norms and diagonal in binary64; mixed =
+binary64 residual with the binary32 sweep (defect correction; converges to
+the binary64 solution).  `value` is the --precision form; "forms" adds the
+other two measured the same way in the same run, and "time_to_drop" the wall
+time each form takes from the freestream start to a --drop fall of the L2
+density residual (normalised by iteration 1), capped at --drop-seconds.
 
 Prints ONE JSON line on rank 0.  value = cell-iterations per second of the
 whole job with the state resident in HBM (CUDA events on the solver's stream,
@@ -51,6 +60,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--sweep-mode", type=int, default=0, help="LU-SGS schedule (0 dataflow, 1/2 per level)")
     ap.add_argument("--sweep-bpsm", type=int, default=0, help="dataflow sweep blocks per SM (0 = default)")
+    ap.add_argument("--forms", default="fp64,fp32,mixed", help="precision forms timed besides --precision ('' = none)")
+    ap.add_argument("--drop", type=float, default=1e-2, help="residual fall for time_to_drop (0 = skip)")
+    ap.add_argument("--drop-seconds", type=float, default=30.0, help="cap per form for time_to_drop")
     return ap.parse_args()
 
 
@@ -113,8 +125,13 @@ def measured_peak_gbs() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def alg_bytes(pass_name: str, nc: int, nf: int, viscous: bool, fp32: bool) -> int:
-    """Compulsory bytes of one launch: each array the kernel touches, once."""
+def alg_bytes(pass_name: str, nc: int, nf: int, viscous: bool, precision: str) -> int:
+    """Compulsory bytes of one launch: each array the kernel touches, once.
+
+    The residual passes run in binary32 only in the fp32 form; the LU-SGS
+    sweeps in both the fp32 and mixed forms."""
+    sweep = pass_name in ("sweep_fwd", "sweep_bwd", "lusgs_update")
+    fp32 = precision == "fp32" or (precision == "mixed" and sweep)
     s = 4 if fp32 else 8
     v = 1 if viscous else 0
     if pass_name == "face_state":
@@ -243,43 +260,54 @@ def run_ours(args):
     w = configs.WORKLOADS[args.config]()
     path = configs.grd_path(w)
     mesh = abi.Mesh.load_grd(path, w.mesh.wall_tag, w.mesh.far_tag)
-    fp32 = args.precision != "fp64"
     viscous = w.flow == "laminar"
     stream = torch.cuda.Stream()  # a real stream: graph capture is not allowed on the legacy default stream
     torch.cuda.set_stream(stream)
-    case = abi.Case([mesh], [dict(mach=w.mach, aoa_deg=w.aoa, reynolds=w.re)],
-                    abi.FLOW_LAMINAR if viscous else abi.FLOW_EULER,
-                    abi.ADV_LUSGS if w.advance == "lusgs" else abi.ADV_RK5,
-                    dict(fp64=abi.PREC_FP64, fp32=abi.PREC_FP32, mixed=abi.PREC_MIXED)[args.precision], cfl=w.cfl,
-                    stream=stream.cuda_stream,
-                    sweep_mode=args.sweep_mode, sweep_blocks_per_sm=args.sweep_bpsm)
-    case.init_freestream()
-    nc, nf = case.ncell, case.nedge
-    U0 = case.get("U").copy()
+    prec_code = dict(fp64=abi.PREC_FP64, fp32=abi.PREC_FP32, mixed=abi.PREC_MIXED)
+
+    def make_case(precision):
+        c = abi.Case([mesh], [dict(mach=w.mach, aoa_deg=w.aoa, reynolds=w.re)],
+                     abi.FLOW_LAMINAR if viscous else abi.FLOW_EULER,
+                     abi.ADV_LUSGS if w.advance == "lusgs" else abi.ADV_RK5,
+                     prec_code[precision], cfl=w.cfl, stream=stream.cuda_stream,
+                     sweep_mode=args.sweep_mode, sweep_blocks_per_sm=args.sweep_bpsm)
+        c.init_freestream()
+        return c
+
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
-    # warm-up (also builds the CUDA graph of one step)
-    case.step_graph(max(args.warmup, 3))
-    torch.cuda.synchronize()
+    def timed_steps(c, nsteps, before_timing=None):
+        """(per-step device ms, kernel launches) of graph-replayed steps, L2 flushed between them."""
+        c.step_graph(max(args.warmup, 3))  # warm-up; also captures the step's CUDA graph
+        torch.cuda.synchronize()
+        if before_timing:
+            before_timing()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+        l0 = c.launches()
+        for k in range(nsteps):
+            flush.zero_()  # evict L2 (129 MB) between timed steps, outside the events
+            evs[k][0].record(stream)
+            c.step_graph(1)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs], c.launches() - l0
 
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    case = make_case(args.precision)
+    nc, nf = case.ncell, case.nedge
+    U0 = case.get("U").copy()
+
     sampler = ClockSampler(local)
-    sampler.start()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    l0 = case.launches()
-    for k in range(args.steps):
-        flush.zero_()  # evict L2 (129 MB) between timed steps, outside the events
-        evs[k][0].record(stream)
-        case.step_graph(1)
-        evs[k][1].record(stream)
-    torch.cuda.synchronize()
+
+    def start_timing():
+        sampler.start()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    ms, launches = timed_steps(case, args.steps, start_timing)
     if dist:
         dist.barrier()
     clocks = sampler.stop()
-    launches = case.launches() - l0
-    ms = [a.elapsed_time(b) for a, b in evs]
     t_local = sum(ms) / 1e3
     t = torch.tensor([t_local], dtype=torch.float64, device="cuda")
     if dist:
@@ -311,6 +339,36 @@ def run_ours(args):
         e2e = {"value": nc * args.steps * world / float(te.item()), "unit": UNIT,
                "h2d_bytes_per_step": nc * 32, "d2h_bytes_per_step": 8}
 
+    # the other precision forms, timed the same way
+    forms = {}
+    for f in [x for x in args.forms.split(",") if x and x != args.precision]:
+        c2 = make_case(f)
+        fm, _ = timed_steps(c2, args.steps)
+        forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3)}
+        c2.close()
+    forms[args.precision] = {"ms_per_step": 1e3 * t_local / args.steps, "value": nc * args.steps / t_local}
+
+    # wall time from the freestream start to a residual fall of args.drop, per form
+    drop = None
+    if args.drop > 0 and rank == 0:
+        drop = {"target": args.drop, "norm": "L2 density residual / iteration 1", "cap_s": args.drop_seconds}
+        for f in forms:
+            c2 = make_case(f)
+            c2.step_graph(1)
+            r0 = c2.norm("L2_R_RHO")
+            chunk, it, r = 50, 1, 1.0
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < args.drop_seconds:
+                c2.step_graph(chunk)
+                it += chunk
+                r = c2.norm("L2_R_RHO") / r0
+                if not r < 1e3 or r <= args.drop:
+                    break
+            el = time.perf_counter() - t0
+            drop[f] = {"reached": bool(r <= args.drop), "seconds": round(el, 3), "iterations": it, "fall": r}
+            c2.close()
+
     # per-pass device times for the roofline (L2 flushed before each rep)
     passes = ["face_state", "cell_grad", "face_flux", "cell_update"]
     if w.advance == "lusgs":
@@ -325,10 +383,10 @@ def run_ours(args):
     peak, peak_kind = measured_peak_gbs()
     rows = {}
     for p, v in per.items():
-        b = alg_bytes(p, nc, nf, viscous, fp32)
+        b = alg_bytes(p, nc, nf, viscous, args.precision)
         rows[p] = {"ms": round(v, 5), "alg_bytes": b, "gbs": round(b / (v * 1e-3) / 1e9, 1),
                    "launches": launches_of.get(p, 1)}
-    db = alg_bytes(dominant, nc, nf, viscous, fp32)
+    db = alg_bytes(dominant, nc, nf, viscous, args.precision)
     achieved = db / (per[dominant] * 1e-3) / 1e9
     tr = traffic_table().get(f"{args.config}_{args.precision}_{dominant}")
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -337,11 +395,12 @@ def run_ours(args):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if fp32 else "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
             "config": {"workload": w.name, "ncell": nc, "nedge": nf, "levels": list(nlev), "mach": w.mach,
                        "re": w.re, "cfl": w.cfl, "precision": args.precision,
                        "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
-            "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline}
+            "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "forms": forms,
+            "time_to_drop": drop}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(str(path), w, args.cpu_seconds)
     if rank == 0:

@@ -249,6 +249,34 @@ int cfd_interp_update(cfd_interp_t it, const double* d_q_donor, long long nnodes
                       long long nnodes_recv, int nvar, int layout, void* stream);
 void cfd_interp_free(cfd_interp_t it);
 
+/* Hole cutting.  A hole map is the Cartesian map of one block's walls
+ * (tioga::getHoleMap, holeMap.cpp:7-180): the box of the wall nodes
+ * (MeshBlock::getWallBounds, MeshBlock.cpp:653-685), 192 map cells along its
+ * longer side plus 2 cells of padding, the cells touched by the boxes of
+ * wall-adjacent mesh cells marked (MeshBlock::markWallBoundary,
+ * MeshBlock.cpp:687-778), then a flood fill from the map's border
+ * (fillHoleMap2D, utils.cpp:782-860): map cells the fill cannot reach are
+ * inside the body.  isym: 3 = four neighbours (tioga's default), 1 = only
+ * the y neighbours, 2 = only the x neighbours.  The wall nodes are the ends
+ * of the block's wall faces.  A block without walls returns CFD_ERR_MESH. */
+typedef struct cfd_holemap_s* cfd_holemap_t;
+int cfd_holemap_create(cfd_block_t b, int isym, cfd_holemap_t* out);
+/* nx[2] map cells and extents[4] = {xmin, ymin, xmax, ymax}. */
+int cfd_holemap_info(cfd_holemap_t h, int* nx, double* extents);
+/* Host copy of the map, nx[0]*nx[1] ints (1 = inside), row y*nx[0] + x. */
+int cfd_holemap_get(cfd_holemap_t h, int* sam);
+/* checkHoleMap (utils.cpp:645-670) for n host points: inside[i] = 1 or 0. */
+int cfd_holemap_check(cfd_holemap_t h, long long n, const double* xy, int* inside);
+void cfd_holemap_free(cfd_holemap_t h);
+/* Node blanking of one block against others (MeshBlock::processDonors,
+ * bookkeeping.cpp:88-186): iblank[i] = 0 where some other block j that has a
+ * hole map (maps[j] != NULL) gives node i no donor cell and its map holds the
+ * node, else 1; mandatory[i] = 1 for an unblanked node within nfringe layers
+ * of cells of a blanked node (a mandatory receptor, nodeRes = BIGVALUE), else
+ * 0.  Host output arrays of the block's node count; mandatory may be NULL. */
+int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, const cfd_holemap_t* maps,
+                      int nfringe, int* iblank, int* mandatory);
+
 /* Residual norm of a caller-owned device array that allocates nothing (no
  * counterpart in the reference, which has no device code).  For callers that
  * may not allocate device memory while they run: solvers that reserve all of

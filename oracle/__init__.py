@@ -62,6 +62,9 @@ def _load():
         L.orc_nodal_weights.argtypes = [C.c_long, ip, dp, dp, dp]
         L.orc_nodal_weights.restype = C.c_long
         L.orc_donor_search.argtypes = [dp, C.c_int, ip, ip, C.c_long, dp, ip, ip, dp]
+        L.orc_holemap.argtypes = [dp, C.c_int, ip, ip, C.c_int, ip, C.c_int, ip, dp, ip, C.c_long]
+        L.orc_holemap.restype = C.c_int
+        L.orc_holemap_check.argtypes = [ip, dp, ip, C.c_long, dp, ip]
         L.orc_interp_update.argtypes = [C.c_long, ip, ip, ip, dp, dp, C.c_long, dp, C.c_long, C.c_int, C.c_int]
         _lib = L
     return _lib
@@ -165,3 +168,62 @@ def interp_update(recv, nw, inode, w, q, nnodes, qr, nnodes_recv, nvar, layout):
     _load().orc_interp_update(r.size, _ip(r), _ip(n_w), _ip(i4), _dp(w4), _dp(qa), nnodes, _dp(qr), nnodes_recv,
                               nvar, layout)
     return qr
+
+
+def holemap(xy, cell_verts, cell_nvert, wall_nodes, isym=3):
+    """Hole map of one block's walls: (nx[2], extents[4], sam[ny, nx])."""
+    x = np.ascontiguousarray(xy, np.float64).reshape(-1)
+    cv = np.ascontiguousarray(cell_verts, np.int32).reshape(-1)
+    nv = np.ascontiguousarray(cell_nvert, np.int32)
+    wn = np.ascontiguousarray(wall_nodes, np.int32)
+    nxy = np.zeros(2, np.int32)
+    geo = np.zeros(4)
+    sam = np.zeros(200_000, np.int32)
+    rc = _load().orc_holemap(_dp(x), nv.size, _ip(cv), _ip(nv), wn.size, _ip(wn), isym, _ip(nxy), _dp(geo), _ip(sam),
+                             sam.size)
+    if rc != 0:
+        raise ValueError("hole map larger than 200000 cells")
+    return nxy, geo, sam[:nxy[0] * nxy[1]].reshape(nxy[1], nxy[0]).copy()
+
+
+def holemap_check(nxy, geo, sam, pts):
+    p = np.ascontiguousarray(pts, np.float64).reshape(-1)
+    n = p.size // 2
+    out = np.zeros(n, np.int32)
+    nx = np.ascontiguousarray(nxy, np.int32)
+    g = np.ascontiguousarray(geo, np.float64)
+    s = np.ascontiguousarray(sam, np.int32).reshape(-1)
+    _load().orc_holemap_check(_ip(nx), _dp(g), _ip(s), n, _dp(p), _ip(out))
+    return out
+
+
+def blank(self_topo, others, nfringe=1):
+    """processDonors' hole test and mandatory fringes (bookkeeping.cpp:88-186).
+
+    others: list of (topo, wall_nodes or None, isym).  Returns (iblank, mandatory)."""
+    xy = self_topo.xy.reshape(-1, 2)
+    ib = np.ones(len(xy), np.int32)
+    for topo, wall, isym in others:
+        if wall is None:
+            continue
+        donor, _, _ = donor_search(topo.xy, topo.cell_verts, topo.cell_nvert, xy)
+        nxy, geo, sam = holemap(topo.xy, topo.cell_verts, topo.cell_nvert, wall, isym)
+        inside = holemap_check(nxy, geo, sam, xy)
+        ib[(donor < 0) & (inside == 1)] = 0
+    tag = (ib == 0).astype(np.int32)
+    cv = self_topo.cell_verts.reshape(-1, 4)
+    for _ in range(nfringe):
+        tag1 = tag.copy()
+        for c in range(self_topo.ncell):
+            vs = cv[c, :self_topo.cell_nvert[c]]
+            if np.any(tag[vs] == 1):
+                tag1[vs] = 1
+        tag = tag1
+    return ib, ((tag == 1) & (ib == 1)).astype(np.int32)
+
+
+def wall_nodes(topo):
+    """Ends of the wall faces (right side == wall code), ascending."""
+    lr = topo.lr.reshape(-1, 2)
+    en = topo.edge_nodes.reshape(-1, 2)
+    return np.unique(en[lr[:, 1] == -2].reshape(-1)).astype(np.int32)

@@ -777,3 +777,104 @@ void orc_interp_update(long n, const int* recv, const int* nw, const int* inode,
         }
     free(vals);
 }
+
+/* Hole map of one block's walls, 2D: tioga::getHoleMap (holeMap.cpp:7-180)
+ * for a single block, MeshBlock::getWallBounds (MeshBlock.cpp:653-685),
+ * markWallBoundary (:687-778) and fillHoleMap2D (utils.cpp:782-860).
+ * wall_nodes: 0-based ids.  geo[4] = {xmin, ymin, xmax, ymax} of the map,
+ * nxy[2] its size; sam (capacity cap) receives nx*ny ints.  Returns 0, or -1
+ * when sam is too small. */
+int orc_holemap(const double* xy, int ncell, const int* cverts, const int* nvert, int nwall, const int* wall_nodes,
+                int isym, int* nxy, double* geo, int* sam, long cap) {
+    double wb[4] = {1.0e15, 1.0e15, -1.0e15, -1.0e15}, ds[2], dsmax, dsbox;
+    int i, j, k, c, m, jj, nx[2];
+    unsigned char* isw;
+    long n, nnode_max = 0;
+    for (i = 0; i < nwall; i++) {
+        const double* p = xy + 2 * wall_nodes[i];
+        for (j = 0; j < 2; j++) {
+            wb[j] = wb[j] < p[j] ? wb[j] : p[j];
+            wb[2 + j] = wb[2 + j] > p[j] ? wb[2 + j] : p[j];
+        }
+        if (wall_nodes[i] + 1 > nnode_max) nnode_max = wall_nodes[i] + 1;
+    }
+    for (j = 0; j < 2; j++) ds[j] = wb[2 + j] - wb[j];
+    dsmax = ds[0] > ds[1] ? ds[0] : ds[1];
+    dsbox = dsmax / 192;
+    for (j = 0; j < 2; j++) {
+        double r;
+        wb[j] -= (2 * dsbox);
+        wb[2 + j] += (2 * dsbox);
+        r = (wb[2 + j] - wb[j]) / dsbox;
+        nx[j] = (int)floor(r > 1 ? r : 1);
+    }
+    nxy[0] = nx[0];
+    nxy[1] = nx[1];
+    for (j = 0; j < 4; j++) geo[j] = wb[j];
+    n = (long)nx[0] * nx[1];
+    if (n > cap) return -1;
+    for (i = 0; i < n; i++) sam[i] = 0;
+    for (c = 0; c < ncell; c++)
+        for (m = 0; m < nvert[c]; m++)
+            if (cverts[4 * c + m] + 1 > nnode_max) nnode_max = cverts[4 * c + m] + 1;
+    isw = (unsigned char*)calloc((size_t)nnode_max, 1);
+    for (i = 0; i < nwall; i++) isw[wall_nodes[i]] = 1;
+    for (k = 0; k < 2; k++) ds[k] = (wb[2 + k] - wb[k]) / nx[k];
+    for (c = 0; c < ncell; c++) {
+        int wall = 0, imin[2] = {2147483647, 2147483647}, imax[2] = {-2147483647, -2147483647}, ii;
+        for (m = 0; m < nvert[c]; m++)
+            if (isw[cverts[4 * c + m]]) { wall = 1; break; }
+        if (!wall) continue;
+        for (m = 0; m < nvert[c]; m++)
+            for (k = 0; k < 2; k++) {
+                int iv = (int)floor((xy[2 * cverts[4 * c + m] + k] - wb[k]) / ds[k]);
+                imin[k] = imin[k] < iv ? imin[k] : iv;
+                imax[k] = imax[k] > iv ? imax[k] : iv;
+            }
+        for (k = 0; k < 2; k++) {
+            imin[k] = imin[k] > 0 ? imin[k] : 0;
+            imax[k] = imax[k] < nx[k] - 1 ? imax[k] : nx[k] - 1;
+        }
+        for (jj = imin[1]; jj < imax[1] + 1; jj++)
+            for (ii = imin[0]; ii < imax[0] + 1; ii++) sam[jj * nx[0] + ii] = 2;
+    }
+    free(isw);
+    /* flood fill from the border, sweep by sweep in row order */
+    for (jj = 0; jj < nx[1]; jj += nx[1] - 1)
+        for (i = 0; i < nx[0]; i++) sam[jj * nx[0] + i] = 1;
+    for (jj = 0; jj < nx[1]; jj++)
+        for (i = 0; i < nx[0]; i += nx[0] - 1) sam[jj * nx[0] + i] = 1;
+    {
+        long npaint = 1;
+        while (npaint > 0) {
+            npaint = 0;
+            for (j = 1; j < nx[1] - 1; j++)
+                for (i = 1; i < nx[0] - 1; i++) {
+                    int mm = j * nx[0] + i, p;
+                    if (sam[mm] != 0) continue;
+                    if (isym == 1) p = sam[mm - nx[0]] == 1 || sam[mm + nx[0]] == 1;
+                    else if (isym == 2) p = sam[mm - 1] == 1 || sam[mm + 1] == 1;
+                    else p = sam[mm - nx[0]] == 1 || sam[mm + nx[0]] == 1 || sam[mm - 1] == 1 || sam[mm + 1] == 1;
+                    if (p) { sam[mm] = 1; npaint++; }
+                }
+        }
+    }
+    for (i = 0; i < n; i++) sam[i] = (sam[i] == 0 || sam[i] == 2);
+    return 0;
+}
+
+/* checkHoleMap (utils.cpp:645-670) for n points. */
+void orc_holemap_check(const int* nxy, const double* geo, const int* sam, long n, const double* pts, int* inside) {
+    long i;
+    int k;
+    double dx[2];
+    for (k = 0; k < 2; k++) dx[k] = (geo[2 + k] - geo[k]) / nxy[k];
+    for (i = 0; i < n; i++) {
+        int ix[2], out = 0;
+        for (k = 0; k < 2; k++) {
+            ix[k] = (int)((pts[2 * i + k] - geo[k]) / dx[k]);
+            if (ix[k] < 0 || ix[k] > nxy[k] - 1) out = 1;
+        }
+        inside[i] = out ? 0 : sam[ix[1] * nxy[0] + ix[0]];
+    }
+}

@@ -16,13 +16,20 @@
 //           ninterp records {int32 recv, int32 nw, int32 inode[4], double w[4]}
 //     OUT:  for ROW then COLUMN: double recv_q[nrecv_nodes*nvar] in that layout,
 //           starting from zeros and updated by every record in order
+//   ref_overset holemap MESH WALL PTS OUT   tioga::getHoleMap (UniTioga/holeMap.cpp:7-180)
+//     with MeshBlock::getWallBounds/markWallBoundary and fillHoleMap, then checkHoleMap
+//     (utils.cpp:645-670) of the points
+//     WALL: int32 isym, nwall; int32 wall_nodes[nwall] (0-based)
+//     OUT:  int32 nx[2]; double extents[4]; int32 sam[nx*ny]; int32 inside[n]
 #include <cstdio>
 #include <cstdlib>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
-#include "MeshBlock.h"
+#include "tioga.h"  // also brings MeshBlock.h, which has no include guard
+
+int checkHoleMap(int dim, double* x, int* nx, int* sam, double* extents);
 
 void computeNodalWeight2D(double xv[8][3], double* xp, double* frac, int nvert);
 
@@ -62,54 +69,78 @@ static int do_weights(const char* in, const char* out) {
     return 0;
 }
 
-static int do_search(const char* meshf, const char* ptsf, const char* out) {
-    FILE* fm = fopen(meshf, "rb");
-    if (!fm) return 3;
-    int nnode, ncell;
-    if (!rd(fm, &nnode, 1) || !rd(fm, &ncell, 1)) return 3;
-    std::vector<double> xy(2 * (size_t)nnode);
-    std::vector<int> nvert(ncell), verts(4 * (size_t)ncell);
-    if (!rd(fm, xy.data(), xy.size()) || !rd(fm, nvert.data(), ncell) || !rd(fm, verts.data(), verts.size())) return 3;
-    fclose(fm);
-    FILE* fp = fopen(ptsf, "rb");
-    if (!fp) return 3;
-    int n;
-    if (!rd(fp, &n, 1)) return 3;
-    std::vector<double> pts(2 * (size_t)n);
-    if (!rd(fp, pts.data(), pts.size())) return 3;
-    fclose(fp);
-
-    // MeshBlock numbers cells type by type: triangles first, then quadrilaterals.
-    std::vector<int> order;
-    int ntri = 0;
-    for (int pass = 0; pass < 2; pass++)
-        for (int c = 0; c < ncell; c++)
-            if (nvert[c] == (pass == 0 ? 3 : 4)) order.push_back(c);
-    for (int c = 0; c < ncell; c++) ntri += nvert[c] == 3;
-    const int nquad = ncell - ntri;
-
-    MeshBlock* mb = new MeshBlock();
-    mb->d_dim = 2;
-    mb->nnodes = nnode;
-    mb->ncells = ncell;
-    mb->x = xy.data();
+// A mesh as a MeshBlock (static storage: the driver makes one per run).
+struct BlockData {
+    int nnode = 0, ncell = 0;
+    std::vector<double> xy;
+    std::vector<int> nvert, verts, order, vtri, vquad;
+    std::vector<double> cellres;
     int types_nv[2], types_nc[2];
     int* vconn[2] = {nullptr, nullptr};
-    int nt = 0;
-    std::vector<int> vtri, vquad;
-    for (int c : order) {
-        auto& dst = nvert[c] == 3 ? vtri : vquad;
-        for (int m = 0; m < nvert[c]; m++) dst.push_back(verts[4 * (size_t)c + m] + BASE);
+};
+
+static bool read_block(const char* meshf, BlockData& d) {
+    FILE* fm = fopen(meshf, "rb");
+    if (!fm) return false;
+    if (!rd(fm, &d.nnode, 1) || !rd(fm, &d.ncell, 1)) return false;
+    d.xy.resize(2 * (size_t)d.nnode);
+    d.nvert.resize(d.ncell);
+    d.verts.resize(4 * (size_t)d.ncell);
+    if (!rd(fm, d.xy.data(), d.xy.size()) || !rd(fm, d.nvert.data(), d.ncell) || !rd(fm, d.verts.data(), d.verts.size()))
+        return false;
+    fclose(fm);
+    return true;
+}
+
+// MeshBlock numbers cells type by type: triangles first, then quadrilaterals.
+static MeshBlock* make_block(BlockData& d) {
+    int ntri = 0;
+    for (int pass = 0; pass < 2; pass++)
+        for (int c = 0; c < d.ncell; c++)
+            if (d.nvert[c] == (pass == 0 ? 3 : 4)) d.order.push_back(c);
+    for (int c = 0; c < d.ncell; c++) ntri += d.nvert[c] == 3;
+    const int nquad = d.ncell - ntri;
+    MeshBlock* mb = new MeshBlock();
+    mb->d_dim = 2;
+    mb->nnodes = d.nnode;
+    mb->ncells = d.ncell;
+    mb->x = d.xy.data();
+    for (int c : d.order) {
+        auto& dst = d.nvert[c] == 3 ? d.vtri : d.vquad;
+        for (int m = 0; m < d.nvert[c]; m++) dst.push_back(d.verts[4 * (size_t)c + m] + BASE);
     }
-    if (ntri) { types_nv[nt] = 3; types_nc[nt] = ntri; vconn[nt] = vtri.data(); nt++; }
-    if (nquad) { types_nv[nt] = 4; types_nc[nt] = nquad; vconn[nt] = vquad.data(); nt++; }
+    int nt = 0;
+    if (ntri) { d.types_nv[nt] = 3; d.types_nc[nt] = ntri; d.vconn[nt] = d.vtri.data(); nt++; }
+    if (nquad) { d.types_nv[nt] = 4; d.types_nc[nt] = nquad; d.vconn[nt] = d.vquad.data(); nt++; }
     mb->ntypes = nt;
-    mb->nv = types_nv;
-    mb->nc = types_nc;
-    mb->vconn = vconn;
-    std::vector<double> cellres(ncell, 1.0);
-    mb->cellRes = cellres.data();
+    mb->nv = d.types_nv;
+    mb->nc = d.types_nc;
+    mb->vconn = d.vconn;
+    d.cellres.assign(d.ncell, 1.0);
+    mb->cellRes = d.cellres.data();
     mb->ihigh = 0;
+    mb->meshtag = 1;
+    return mb;
+}
+
+static bool read_points(const char* ptsf, std::vector<double>& pts) {
+    FILE* fp = fopen(ptsf, "rb");
+    if (!fp) return false;
+    int n;
+    if (!rd(fp, &n, 1)) return false;
+    pts.resize(2 * (size_t)n);
+    if (!rd(fp, pts.data(), pts.size())) return false;
+    fclose(fp);
+    return true;
+}
+
+static int do_search(const char* meshf, const char* ptsf, const char* out) {
+    static BlockData d;
+    std::vector<double> pts;
+    if (!read_block(meshf, d) || !read_points(ptsf, pts)) return 3;
+    const int n = (int)(pts.size() / 2);
+    MeshBlock* mb = make_block(d);
+    const std::vector<int>& order = d.order;
     mb->nsearch = n;
     mb->xsearch = pts.data();
     std::vector<int> tags(n, 1);
@@ -124,6 +155,43 @@ static int do_search(const char* meshf, const char* ptsf, const char* out) {
     fwrite(donor.data(), 4, donor.size(), fo);
     fclose(fo);
     return 0;  // the block is left allocated: the driver exits next
+}
+
+static int do_holemap(const char* meshf, const char* wallf, const char* ptsf, const char* out) {
+    static BlockData d;
+    std::vector<double> pts;
+    if (!read_block(meshf, d) || !read_points(ptsf, pts)) return 3;
+    FILE* fw = fopen(wallf, "rb");
+    if (!fw) return 3;
+    int isym, nwall;
+    if (!rd(fw, &isym, 1) || !rd(fw, &nwall, 1)) return 3;
+    static std::vector<int> wall(nwall);
+    if (!rd(fw, wall.data(), nwall)) return 3;
+    fclose(fw);
+    for (int& w : wall) w += BASE;
+    MeshBlock* mb = make_block(d);
+    mb->nwbc = nwall;
+    mb->wbcnode = wall.data();
+    TIOGA::tioga* tg = new TIOGA::tioga();
+    tg->d_dim = 2;
+    tg->isym = isym;
+    tg->scomm = MPI_COMM_WORLD;
+    tg->nblocks = 1;
+    tg->mblocks.emplace_back(mb);
+    tg->mtags.push_back(1);
+    tg->getHoleMap();
+    HOLEMAP& h = tg->holeMap[0];
+    const int n = (int)(pts.size() / 2);
+    std::vector<int> inside(n);
+    for (int i = 0; i < n; i++) inside[i] = checkHoleMap(2, &pts[2 * (size_t)i], h.nx, h.sam, h.extents);
+    FILE* fo = fopen(out, "wb");
+    if (!fo) return 4;
+    fwrite(h.nx, 4, 2, fo);
+    fwrite(h.extents, 8, 4, fo);
+    fwrite(h.sam, 4, (size_t)h.nx[0] * h.nx[1], fo);
+    fwrite(inside.data(), 4, inside.size(), fo);
+    fclose(fo);
+    return 0;  // tg and the block are left allocated: the driver exits next
 }
 
 static int do_interp(const char* listf, const char* out) {
@@ -193,6 +261,7 @@ int main(int argc, char** argv) {
     if (mode == "weights" && argc == 4) return do_weights(argv[2], argv[3]);
     if (mode == "search" && argc == 5) return do_search(argv[2], argv[3], argv[4]);
     if (mode == "interp" && argc == 4) return do_interp(argv[2], argv[3]);
+    if (mode == "holemap" && argc == 6) return do_holemap(argv[2], argv[3], argv[4], argv[5]);
     fprintf(stderr, "bad arguments\n");
     return 2;
 }

@@ -26,3 +26,10 @@ static inline int MPI_Allgather(const void* s, int sc, MPI_Datatype st, void* r,
 static inline int MPI_Isend(const void*, int, MPI_Datatype, int, int, MPI_Comm, MPI_Request* q) { *q = 0; return 0; }
 static inline int MPI_Irecv(void*, int, MPI_Datatype, int, int, MPI_Comm, MPI_Request* q) { *q = 0; return 0; }
 static inline int MPI_Waitall(int, MPI_Request*, MPI_Status*) { return 0; }
+typedef int MPI_Op;
+#define MPI_MAX 1
+#define MPI_MIN 2
+#define MPI_SUM 3
+/* one rank: the reduction of one contribution is that contribution */
+static inline int MPI_Allreduce(const void* s, void* r, int n, MPI_Datatype t, MPI_Op, MPI_Comm) {
+  memcpy(r, s, (size_t)n * (size_t)t); return 0; }

@@ -13,6 +13,9 @@ mathTools sources by oracle/build_ref.sh) on seeded inputs:
             omesh.grd (quadrilaterals)
   interp    getInterpolatedSolution + updateSolnData, ROW and COLUMN, with
             repeated receivers, nvar = 4 and 6
+  holemap   tioga::getHoleMap (markWallBoundary + fillHoleMap) of each golden
+            mesh's walls for isym = 3, 1, 2, and checkHoleMap of random points
+            and of the other mesh's nodes
 
 usage: python tests/golden/make_golden_overset.py [REFERENCE_ROOT]
 """
@@ -29,6 +32,7 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 sys.path.insert(0, str(ROOT))
 
+import oracle  # noqa: E402
 from oracle import grd  # noqa: E402
 
 DRV = ROOT / "oracle" / "_ref" / "ref_overset"
@@ -176,6 +180,32 @@ def main():
             out.update({f"i{nvar}_q": q, f"i{nvar}_recv": recv, f"i{nvar}_nw": nw, f"i{nvar}_inode": inode,
                         f"i{nvar}_w": w, f"i{nvar}_row": res[0], f"i{nvar}_col": res[1],
                         f"i{nvar}_dims": np.array([nnodes, nrecv])})
+        for name, m, other in (("mx", mx, om), ("om", om, mx)):
+            wall = oracle.wall_nodes(m)
+            xy = m.xy.reshape(-1, 2)
+            wxy = xy[wall]
+            lo, hi = wxy.min(0), wxy.max(0)
+            span = hi - lo
+            pts = np.concatenate([lo - 0.1 * span + rng.uniform(0, 1.2, (4000, 2)) * span,
+                                  other.xy.reshape(-1, 2) * 0.5 + lo + 0.5 * span - 0.25])
+            write_mesh(td / "m.bin", m)
+            with open(td / "p.bin", "wb") as f:
+                np.array([len(pts)], np.int32).tofile(f)
+                pts.astype(np.float64).tofile(f)
+            for isym in (3, 1, 2):
+                with open(td / "wl.bin", "wb") as f:
+                    np.array([isym, wall.size], np.int32).tofile(f)
+                    wall.astype(np.int32).tofile(f)
+                _run("holemap", td / "m.bin", td / "wl.bin", td / "p.bin", td / "h.out", cwd=td)
+                raw = (td / "h.out").read_bytes()
+                nxy = np.frombuffer(raw[:8], np.int32)
+                geo = np.frombuffer(raw[8:40], np.float64)
+                nsam = int(nxy[0]) * int(nxy[1])
+                sam = np.frombuffer(raw[40:40 + 4 * nsam], np.int32).reshape(nxy[1], nxy[0])
+                inside = np.frombuffer(raw[40 + 4 * nsam:], np.int32)
+                out.update({f"h_{name}_{isym}_nx": nxy, f"h_{name}_{isym}_ext": geo,
+                            f"h_{name}_{isym}_sam": sam, f"h_{name}_{isym}_in": inside})
+            out[f"h_{name}_pts"] = pts
     np.savez_compressed(HERE / "overset.npz", **out)
     print(f"wrote {HERE / 'overset.npz'}: {nv.size} weight cases, "
           f"{sum(v.size for k, v in out.items() if k.endswith('_donor'))} search points")

@@ -200,3 +200,31 @@ def test_interp_from_search_and_node_to_cell(built_lib):
             s = s + qn[cv[c, j]]
         exp[c] = s / topo_d.cell_nvert[c]
     assert _eq(dc_out.cpu().numpy(), exp.reshape(-1))
+
+
+@pytest.mark.parametrize("isym", [3, 1, 2])
+def test_holemap_matches_reference(built_lib, ov, isym):
+    from tmp_gb300 import abi
+
+    for name, (mesh, blk, topo) in _blocks(abi).items():
+        hm = abi.HoleMap(blk, isym)
+        nx, ext = hm.info()
+        assert np.array_equal(nx, ov[f"h_{name}_{isym}_nx"]) and _eq(ext, ov[f"h_{name}_{isym}_ext"])
+        assert np.array_equal(hm.get(), ov[f"h_{name}_{isym}_sam"])
+        assert np.array_equal(hm.check(ov[f"h_{name}_pts"]), ov[f"h_{name}_{isym}_in"])
+
+
+def test_overset_blank_matches_oracle(built_lib):
+    from tmp_gb300 import abi
+
+    blocks = _blocks(abi)
+    _, blk_mx, topo_mx = blocks["mx"]
+    _, blk_om, topo_om = blocks["om"]
+    # mesh without walls of its own would not cut: both golden meshes have walls
+    for nfringe in (0, 1, 2):
+        ib, md = abi.overset_blank(blk_om, [blk_mx], [abi.HoleMap(blk_mx)], nfringe)
+        eib, emd = oracle.blank(topo_om, [(topo_mx, oracle.wall_nodes(topo_mx), 3)], nfringe)
+        assert np.array_equal(ib, eib) and np.array_equal(md, emd)
+        assert (ib == 0).sum() > 0 and (nfringe == 0 or md.sum() > 0)
+    ib, md = abi.overset_blank(blk_mx, [blk_om], [None], 1)
+    assert np.all(ib == 1) and np.all(md == 0)

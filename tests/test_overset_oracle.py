@@ -60,3 +60,15 @@ def test_interp_update_bitwise(ov, nvar, layout):
     ref = ov[f"i{nvar}_row" if layout == 0 else f"i{nvar}_col"]
     assert np.array_equal(qr.view(np.int64), ref.view(np.int64))
     assert len(np.unique(ov[f"i{nvar}_recv"])) < len(ov[f"i{nvar}_recv"])  # repeated receivers: last wins
+
+
+@pytest.mark.parametrize("isym", [3, 1, 2])
+def test_holemap_bitwise(ov, isym):
+    for name, m in _meshes().items():
+        nxy, geo, sam = oracle.holemap(m.xy, m.cell_verts, m.cell_nvert, oracle.wall_nodes(m), isym)
+        assert np.array_equal(nxy, ov[f"h_{name}_{isym}_nx"])
+        assert np.array_equal(geo.view(np.int64), ov[f"h_{name}_{isym}_ext"].view(np.int64))
+        assert np.array_equal(sam, ov[f"h_{name}_{isym}_sam"])
+        inside = oracle.holemap_check(nxy, geo, sam, ov[f"h_{name}_pts"])
+        assert np.array_equal(inside, ov[f"h_{name}_{isym}_in"])
+        assert 0 < inside.sum() < inside.size

@@ -105,6 +105,12 @@ def lib() -> C.CDLL:
         "cfd_interp_get": (C.c_int, [vp, ip, ip, ip, dp]),
         "cfd_interp_update": (C.c_int, [vp, vp, C.c_longlong, vp, C.c_longlong, C.c_int, C.c_int, vp]),
         "cfd_interp_free": (None, [vp]),
+        "cfd_holemap_create": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
+        "cfd_holemap_info": (C.c_int, [vp, ip, dp]),
+        "cfd_holemap_get": (C.c_int, [vp, ip]),
+        "cfd_holemap_check": (C.c_int, [vp, C.c_longlong, dp, ip]),
+        "cfd_holemap_free": (None, [vp]),
+        "cfd_overset_blank": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.POINTER(vp), C.c_int, ip, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -381,3 +387,48 @@ class Interp:
 
     def __del__(self):
         self.close()
+
+
+class HoleMap:
+    """Cartesian hole map of one block's walls (tioga::getHoleMap)."""
+
+    def __init__(self, block: Block, isym: int = 3):
+        self.h = C.c_void_p()
+        check(lib().cfd_holemap_create(block.h, int(isym), C.byref(self.h)))
+
+    def info(self):
+        nx = np.zeros(2, np.int32)
+        ext = np.zeros(4)
+        check(lib().cfd_holemap_info(self.h, _iptr(nx), _dptr(ext)))
+        return nx, ext
+
+    def get(self) -> np.ndarray:
+        nx, _ = self.info()
+        sam = np.zeros(int(nx[0]) * int(nx[1]), np.int32)
+        check(lib().cfd_holemap_get(self.h, _iptr(sam)))
+        return sam.reshape(nx[1], nx[0])
+
+    def check(self, xy: np.ndarray) -> np.ndarray:
+        p = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
+        out = np.zeros(p.size // 2, np.int32)
+        check(lib().cfd_holemap_check(self.h, out.size, _dptr(p), _iptr(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.cfd_holemap_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def overset_blank(block: Block, others: Sequence[Block], maps: Sequence[HoleMap | None], nfringe: int = 1):
+    """(iblank, mandatory) of the block's nodes against the other blocks (processDonors)."""
+    n = len(others)
+    ob = (C.c_void_p * max(n, 1))(*[o.h.value for o in others])
+    mp = (C.c_void_p * max(n, 1))(*[(m.h.value if m is not None else None) for m in maps])
+    ib = np.zeros(block.nnode, np.int32)
+    md = np.zeros(block.nnode, np.int32)
+    check(lib().cfd_overset_blank(block.h, n, ob, mp, int(nfringe), _iptr(ib), _iptr(md)))
+    return ib, md

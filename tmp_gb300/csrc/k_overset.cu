@@ -26,6 +26,7 @@
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <new>
@@ -389,6 +390,172 @@ __global__ void k_node_to_cell(int ncell, int nvar, const int4* __restrict__ cv,
     qc[t] = s;
 }
 
+
+// ---------------------------------------------------------------------------
+// Hole map (holeMap.cpp, MeshBlock.cpp:653-778, utils.cpp:645-860)
+// ---------------------------------------------------------------------------
+
+struct MapGeom {
+    double lo[2], hi[2], ds[2];
+    int nx, ny;
+};
+
+// Box of the wall nodes (getWallBounds): one block, exact min / max.
+__global__ void k_wall_box(int nwall, const int* __restrict__ wn, const double* __restrict__ xy, double* box) {
+    __shared__ double s[4][256];
+    double lo0 = 1.0e15, lo1 = 1.0e15, hi0 = -1.0e15, hi1 = -1.0e15;  // BIGVALUE
+    for (int i = threadIdx.x; i < nwall; i += blockDim.x) {
+        const double x = xy[2 * wn[i]], y = xy[2 * wn[i] + 1];
+        lo0 = lo0 < x ? lo0 : x;
+        lo1 = lo1 < y ? lo1 : y;
+        hi0 = hi0 > x ? hi0 : x;
+        hi1 = hi1 > y ? hi1 : y;
+    }
+    s[0][threadIdx.x] = lo0;
+    s[1][threadIdx.x] = lo1;
+    s[2][threadIdx.x] = hi0;
+    s[3][threadIdx.x] = hi1;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            const int o = threadIdx.x + h;
+            s[0][threadIdx.x] = s[0][threadIdx.x] < s[0][o] ? s[0][threadIdx.x] : s[0][o];
+            s[1][threadIdx.x] = s[1][threadIdx.x] < s[1][o] ? s[1][threadIdx.x] : s[1][o];
+            s[2][threadIdx.x] = s[2][threadIdx.x] > s[2][o] ? s[2][threadIdx.x] : s[2][o];
+            s[3][threadIdx.x] = s[3][threadIdx.x] > s[3][o] ? s[3][threadIdx.x] : s[3][o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) box[threadIdx.x] = s[threadIdx.x][0];
+}
+
+__device__ __forceinline__ int map_floor(double v) {
+    const double f = floor(v);
+    if (!(f > -2147483648.0)) return INT_MIN;
+    if (f > 2147483647.0) return INT_MAX;
+    return (int)f;
+}
+
+// markWallBoundary: every cell with a wall node marks the map cells its
+// vertices' box spans with 2.
+__global__ void k_mark_walls(int ncell, const int4* __restrict__ cv, const unsigned char* __restrict__ wflag,
+                             const double* __restrict__ xy, MapGeom g, int* __restrict__ sam) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int4 v = cv[c];
+    const int nv = v.w < 0 ? 3 : 4;
+    const int id[4] = {v.x, v.y, v.z, v.w};
+    bool wall = false;
+    for (int m = 0; m < 4; m++)
+        if (m < nv && wflag[id[m]]) wall = true;
+    if (!wall) return;
+    int imin[2] = {INT_MAX, INT_MAX}, imax[2] = {-INT_MAX, -INT_MAX};
+    for (int m = 0; m < 4; m++) {
+        if (m >= nv) continue;
+        for (int k = 0; k < 2; k++) {
+            const int iv = map_floor((xy[2 * id[m] + k] - g.lo[k]) / g.ds[k]);
+            imin[k] = imin[k] < iv ? imin[k] : iv;
+            imax[k] = imax[k] > iv ? imax[k] : iv;
+        }
+    }
+    const int nxk[2] = {g.nx, g.ny};
+    for (int k = 0; k < 2; k++) {
+        imin[k] = imin[k] > 0 ? imin[k] : 0;
+        imax[k] = imax[k] < nxk[k] - 1 ? imax[k] : nxk[k] - 1;
+    }
+    for (int jj = imin[1]; jj <= imax[1]; jj++)
+        for (int ii = imin[0]; ii <= imax[0]; ii++) sam[jj * g.nx + ii] = 2;
+}
+
+// fillHoleMap2D in one block, in shared memory: the border is set to 1, then
+// sweeps paint every 0 cell with a painted neighbour until a sweep paints
+// nothing (the painted set is the same whatever the sweep order); finally
+// sam = 1 for unpainted and wall cells.  A sweep that paints nothing ends the
+// loop, so at most nx*ny sweeps run.
+__global__ void k_fill_map(int nx, int ny, int isym, int* __restrict__ sam) {
+    extern __shared__ unsigned char hm[];
+    volatile unsigned char* h = hm;
+    const int n = nx * ny;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int x = i % nx, y = i / nx;
+        h[i] = (x == 0 || x == nx - 1 || y == 0 || y == ny - 1) ? 1 : (unsigned char)sam[i];
+    }
+    __syncthreads();
+    for (int sweep = 0; sweep < n; sweep++) {
+        int painted = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int x = i % nx, y = i / nx;
+            if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || h[i] != 0) continue;
+            bool p;
+            if (isym == 1) p = h[i - nx] == 1 || h[i + nx] == 1;
+            else if (isym == 2) p = h[i - 1] == 1 || h[i + 1] == 1;
+            else p = h[i - nx] == 1 || h[i + nx] == 1 || h[i - 1] == 1 || h[i + 1] == 1;
+            if (p) {
+                h[i] = 1;
+                painted = 1;
+            }
+        }
+        if (!__syncthreads_or(painted)) break;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sam[i] = (h[i] == 0 || h[i] == 2) ? 1 : 0;
+}
+
+// checkHoleMap: the map cell of the point by truncation; outside the map is 0.
+__device__ __forceinline__ int hole_at(double px, double py, const MapGeom& g, const int* __restrict__ sam) {
+    const double q[2] = {px, py};
+    const int nxk[2] = {g.nx, g.ny};
+    int ix[2];
+    for (int k = 0; k < 2; k++) {
+        const double t = (q[k] - g.lo[k]) / g.ds[k];
+        ix[k] = !(t > -2147483648.0) ? INT_MIN : (t > 2147483647.0 ? INT_MAX : (int)t);
+        if (ix[k] < 0 || ix[k] > nxk[k] - 1) return 0;
+    }
+    return sam[ix[1] * g.nx + ix[0]];
+}
+
+__global__ void k_hole_check(long long n, const double* __restrict__ pts, MapGeom g, const int* __restrict__ sam,
+                             int* __restrict__ inside) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    inside[i] = hole_at(pts[2 * i], pts[2 * i + 1], g, sam);
+}
+
+// processDonors' hole test for one other block: a node without a donor cell
+// in that block and inside its map is blanked.
+__global__ void k_blank_nodes(int n, const double* __restrict__ xy, const int* __restrict__ donor, MapGeom g,
+                              const int* __restrict__ sam, int* __restrict__ iblank) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (donor[i] < 0 && hole_at(xy[2 * i], xy[2 * i + 1], g, sam)) iblank[i] = 0;
+}
+
+// One layer of mandatory fringes: every cell with a tagged vertex tags all of
+// its vertices in the next generation.
+__global__ void k_fringe_layer(int ncell, const int4* __restrict__ cv, const int* __restrict__ tag,
+                               int* __restrict__ tag1) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int4 v = cv[c];
+    const bool quad = v.w >= 0;
+    if (tag[v.x] == 1 || tag[v.y] == 1 || tag[v.z] == 1 || (quad && tag[v.w] == 1)) {
+        tag1[v.x] = 1;
+        tag1[v.y] = 1;
+        tag1[v.z] = 1;
+        if (quad) tag1[v.w] = 1;
+    }
+}
+
+__global__ void k_tag_holes(int n, const int* __restrict__ iblank, int* __restrict__ tag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) tag[i] = iblank[i] == 0 ? 1 : 0;
+}
+
+__global__ void k_mandatory(int n, const int* __restrict__ iblank, const int* __restrict__ tag,
+                            int* __restrict__ mand) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) mand[i] = (tag[i] && iblank[i]) ? 1 : 0;
+}
+
 inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -409,7 +576,12 @@ struct cfd_block_s {
     int* binptr = nullptr;  // nbins + 1
     int* cells = nullptr;   // nent
     int* err = nullptr;
+    int nwall = 0;
+    int* wall_nodes = nullptr;           // ends of the wall faces, ascending
+    unsigned char* wall_flag = nullptr;  // per node: 1 on a wall face
     ~cfd_block_s() {
+        dfree(wall_nodes);
+        dfree(wall_flag);
         dfree(xy);
         dfree(cv);
         dfree(fbox);
@@ -438,6 +610,13 @@ struct cfd_interp_s {
         dfree(w);
         dfree(vals);
     }
+};
+
+struct cfd_holemap_s {
+    MapGeom g{};
+    cudaStream_t stream = nullptr;
+    int* sam = nullptr;  // nx*ny on the device
+    ~cfd_holemap_s() { dfree(sam); }
 };
 
 namespace {
@@ -596,6 +775,20 @@ int cfd_block_create(cfd_mesh_t mesh, void* stream, cfd_block_t* out) {
         ck(cudaMemcpyAsync(b->xy, m.xy.data(), 2 * (size_t)m.nnode * sizeof(double), cudaMemcpyHostToDevice, s),
            "copy");
         ck(cudaMemcpyAsync(b->cv, hcv.data(), m.ncell * sizeof(int4), cudaMemcpyHostToDevice, s), "copy");
+        {
+            std::vector<unsigned char> flag(m.nnode, 0);
+            for (int e = 0; e < m.nedge; e++)
+                if (m.lr[2 * e + 1] == cfdgb::kWall) flag[m.edge_nodes[2 * e]] = flag[m.edge_nodes[2 * e + 1]] = 1;
+            std::vector<int> wn;
+            for (int i = 0; i < m.nnode; i++)
+                if (flag[i]) wn.push_back(i);
+            b->nwall = (int)wn.size();
+            dalloc(&b->wall_nodes, wn.size());
+            dalloc(&b->wall_flag, m.nnode);
+            ck(cudaMemcpyAsync(b->wall_nodes, wn.data(), wn.size() * sizeof(int), cudaMemcpyHostToDevice, s), "copy");
+            ck(cudaMemcpyAsync(b->wall_flag, flag.data(), m.nnode, cudaMemcpyHostToDevice, s), "copy");
+            ck(cudaStreamSynchronize(s), "sync");
+        }
         k_cell_boxes<<<blocks_for(m.ncell, 256), 256, 0, s>>>(m.ncell, b->xy, b->cv, b->grid, b->fbox, d_brange,
                                                              d_count);
         ck(cudaGetLastError(), "k_cell_boxes");
@@ -837,5 +1030,167 @@ int cfd_interp_update(cfd_interp_t it, const double* d_q_donor, long long nnodes
 }
 
 void cfd_interp_free(cfd_interp_t it) { delete it; }
+
+constexpr int kHoleMapSize = 192;  // HOLEMAPSIZE, UniTioga/codetypes.h:55
+
+int cfd_holemap_create(cfd_block_t b, int isym, cfd_holemap_t* out) {
+    if (!b || !out || isym < 1 || isym > 3) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_holemap_create: bad argument");
+    *out = nullptr;
+    if (b->nwall == 0) return cfdgb::set_last_error(CFD_ERR_MESH, "cfd_holemap_create: the block has no wall faces");
+    cfd_holemap_s* h = new (std::nothrow) cfd_holemap_s;
+    if (!h) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_holemap_create: out of host memory");
+    double* d_box = nullptr;
+    try {
+        cudaStream_t s = b->stream;
+        h->stream = s;
+        dalloc(&d_box, 4);
+        k_wall_box<<<1, 256, 0, s>>>(b->nwall, b->wall_nodes, b->xy, d_box);
+        ck(cudaGetLastError(), "k_wall_box");
+        double box[4];
+        ck(cudaMemcpyAsync(box, d_box, sizeof(box), cudaMemcpyDeviceToHost, s), "copy");
+        ck(cudaStreamSynchronize(s), "sync");
+        // tioga::getHoleMap (holeMap.cpp:89-116) for one block in 2D.  The
+        // reference also folds an unset third extent into dsmax; it is taken as 0.
+        MapGeom& g = h->g;
+        double ds[2], dsmax, dsbox;
+        int nxk[2];
+        for (int j = 0; j < 2; j++) {
+            g.lo[j] = box[j];
+            g.hi[j] = box[2 + j];
+            ds[j] = g.hi[j] - g.lo[j];
+        }
+        dsmax = ds[0] > ds[1] ? ds[0] : ds[1];
+        dsbox = dsmax / kHoleMapSize;
+        for (int j = 0; j < 2; j++) {
+            g.lo[j] -= (2 * dsbox);
+            g.hi[j] += (2 * dsbox);
+            const double r = (g.hi[j] - g.lo[j]) / dsbox;
+            nxk[j] = (int)floor(r > 1 ? r : 1);
+        }
+        g.nx = nxk[0];
+        g.ny = nxk[1];
+        for (int k = 0; k < 2; k++) g.ds[k] = (g.hi[k] - g.lo[k]) / nxk[k];
+        const long long ncell_map = (long long)g.nx * g.ny;
+        if (!(dsbox > 0) || g.nx < 3 || g.ny < 3 || ncell_map > 200000)
+            throw OversetError(CFD_ERR_MESH, "cfd_holemap_create: degenerate wall box");
+        dalloc(&h->sam, ncell_map);
+        ck(cudaMemsetAsync(h->sam, 0, ncell_map * sizeof(int), s), "cudaMemsetAsync");
+        k_mark_walls<<<blocks_for(b->ncell, 256), 256, 0, s>>>(b->ncell, b->cv, b->wall_flag, b->xy, g, h->sam);
+        ck(cudaGetLastError(), "k_mark_walls");
+        ck(cudaFuncSetAttribute(k_fill_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ncell_map),
+           "cudaFuncSetAttribute");
+        k_fill_map<<<1, 1024, ncell_map, s>>>(g.nx, g.ny, isym, h->sam);
+        ck(cudaGetLastError(), "k_fill_map");
+        ck(cudaStreamSynchronize(s), "sync");
+    } catch (const OversetError& e) {
+        dfree(d_box);
+        delete h;
+        return report(e);
+    }
+    dfree(d_box);
+    *out = h;
+    return CFD_OK;
+}
+
+int cfd_holemap_info(cfd_holemap_t h, int* nx, double* extents) {
+    if (!h) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_holemap_info: null handle");
+    if (nx) {
+        nx[0] = h->g.nx;
+        nx[1] = h->g.ny;
+    }
+    if (extents) {
+        extents[0] = h->g.lo[0];
+        extents[1] = h->g.lo[1];
+        extents[2] = h->g.hi[0];
+        extents[3] = h->g.hi[1];
+    }
+    return CFD_OK;
+}
+
+int cfd_holemap_get(cfd_holemap_t h, int* sam) {
+    if (!h || !sam) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_holemap_get: null argument");
+    try {
+        ck(cudaMemcpyAsync(sam, h->sam, (size_t)h->g.nx * h->g.ny * sizeof(int), cudaMemcpyDeviceToHost, h->stream),
+           "copy");
+        ck(cudaStreamSynchronize(h->stream), "sync");
+    } catch (const OversetError& e) {
+        return report(e);
+    }
+    return CFD_OK;
+}
+
+int cfd_holemap_check(cfd_holemap_t h, long long n, const double* xy, int* inside) {
+    if (!h || n < 0 || (n > 0 && (!xy || !inside))) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_holemap_check: bad argument");
+    if (n == 0) return CFD_OK;
+    double* d_pts = nullptr;
+    int* d_in = nullptr;
+    int rc = CFD_OK;
+    try {
+        cudaStream_t s = h->stream;
+        dalloc(&d_pts, 2 * n);
+        dalloc(&d_in, n);
+        ck(cudaMemcpyAsync(d_pts, xy, 2 * n * sizeof(double), cudaMemcpyHostToDevice, s), "copy");
+        k_hole_check<<<blocks_for(n, 256), 256, 0, s>>>(n, d_pts, h->g, h->sam, d_in);
+        ck(cudaGetLastError(), "k_hole_check");
+        ck(cudaMemcpyAsync(inside, d_in, n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+        ck(cudaStreamSynchronize(s), "sync");
+    } catch (const OversetError& e) {
+        rc = report(e);
+    }
+    dfree(d_pts);
+    dfree(d_in);
+    return rc;
+}
+
+void cfd_holemap_free(cfd_holemap_t h) { delete h; }
+
+int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, const cfd_holemap_t* maps,
+                      int nfringe, int* iblank, int* mandatory) {
+    if (!self || nother < 0 || (nother > 0 && (!others || !maps)) || nfringe < 0 || !iblank)
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_blank: bad argument");
+    for (int j = 0; j < nother; j++)
+        if (!others[j] || others[j] == self) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_blank: bad other block");
+    const int n = self->nnode;
+    int *d_ib = nullptr, *d_donor = nullptr, *d_tag = nullptr, *d_tag1 = nullptr;
+    int rc = CFD_OK;
+    try {
+        cudaStream_t s = self->stream;
+        dalloc(&d_ib, n);
+        dalloc(&d_donor, n);
+        std::vector<int> ones(n, 1);
+        ck(cudaMemcpyAsync(d_ib, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice, s), "copy");
+        for (int j = 0; j < nother; j++) {
+            if (!maps[j]) continue;
+            ck(cudaStreamSynchronize(s), "sync");
+            search_device(others[j], n, self->xy, d_donor, nullptr, nullptr);  // on the other block's stream
+            ck(cudaStreamSynchronize(others[j]->stream), "sync");
+            k_blank_nodes<<<blocks_for(n, 256), 256, 0, s>>>(n, self->xy, d_donor, maps[j]->g, maps[j]->sam, d_ib);
+            ck(cudaGetLastError(), "k_blank_nodes");
+        }
+        ck(cudaMemcpyAsync(iblank, d_ib, n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+        if (mandatory) {
+            dalloc(&d_tag, n);
+            dalloc(&d_tag1, n);
+            k_tag_holes<<<blocks_for(n, 256), 256, 0, s>>>(n, d_ib, d_tag);
+            ck(cudaMemcpyAsync(d_tag1, d_tag, n * sizeof(int), cudaMemcpyDeviceToDevice, s), "copy");
+            for (int it = 0; it < nfringe; it++) {
+                k_fringe_layer<<<blocks_for(self->ncell, 256), 256, 0, s>>>(self->ncell, self->cv, d_tag, d_tag1);
+                ck(cudaGetLastError(), "k_fringe_layer");
+                ck(cudaMemcpyAsync(d_tag, d_tag1, n * sizeof(int), cudaMemcpyDeviceToDevice, s), "copy");
+            }
+            k_mandatory<<<blocks_for(n, 256), 256, 0, s>>>(n, d_ib, d_tag1, d_tag);
+            ck(cudaGetLastError(), "k_mandatory");
+            ck(cudaMemcpyAsync(mandatory, d_tag, n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+        }
+        ck(cudaStreamSynchronize(s), "sync");
+    } catch (const OversetError& e) {
+        rc = report(e);
+    }
+    dfree(d_ib);
+    dfree(d_donor);
+    dfree(d_tag);
+    dfree(d_tag1);
+    return rc;
+}
 
 }  // extern "C"
