@@ -157,6 +157,17 @@ def traffic_table() -> dict:
         return {}
 
 
+def traffic_bytes(pass_name: str, precision: str, nc: int):
+    """DRAM bytes of one launch from the committed ncu capture (per cell, scaled by the cell count)."""
+    sweep = pass_name in ("sweep_fwd", "sweep_bwd")
+    form = "fp32" if precision == "fp32" or (precision == "mixed" and sweep) else "fp64"
+    row = traffic_table().get(f"{form}_{'sweep_fwd' if sweep else pass_name}")
+    if not row:
+        return None
+    return {"bytes": round(row["bytes_per_cell"] * nc), "from": row["source"],
+            "note": "DRAM read+write of one launch on C2big (947,090 cells), scaled by the cell count"}
+
+
 # ---------------------------------------------------------------------------
 def cpu_baseline(grd_path: str, w, seconds: float) -> dict:
     """C restatement of the reference's serial LU-SGS path on one host core."""
@@ -379,19 +390,24 @@ def run_ours(args):
         per_step = {p: 5 * v for p, v in per.items()}
     dominant = max(per_step, key=per_step.get)
     nlev = mesh.levels()
-    launches_of = {"sweep_fwd": nlev[0], "sweep_bwd": nlev[1]}
+    per_level = args.sweep_mode != 0  # modes 1 and 2 launch once per level; the dataflow sweep once per direction
+    launches_of = {"sweep_fwd": nlev[0] if per_level else 1, "sweep_bwd": nlev[1] if per_level else 1}
     peak, peak_kind = measured_peak_gbs()
     rows = {}
     for p, v in per.items():
         b = alg_bytes(p, nc, nf, viscous, args.precision)
         rows[p] = {"ms": round(v, 5), "alg_bytes": b, "gbs": round(b / (v * 1e-3) / 1e9, 1),
-                   "launches": launches_of.get(p, 1)}
+                   "frac": round(b / (v * 1e-3) / 1e9 / peak, 4), "launches": launches_of.get(p, 1)}
+        t = traffic_bytes(p, args.precision, nc)
+        if t:
+            rows[p]["traffic"] = t["bytes"]
     db = alg_bytes(dominant, nc, nf, viscous, args.precision)
     achieved = db / (per[dominant] * 1e-3) / 1e9
-    tr = traffic_table().get(f"{args.config}_{args.precision}_{dominant}")
+    tr = traffic_bytes(dominant, args.precision, nc)
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": tr, "alg_bytes_per_launch": db, "per_pass": rows}
+                "traffic": tr["bytes"] if tr else None, "traffic_source": tr, "alg_bytes_per_launch": db,
+                "per_pass": rows}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
