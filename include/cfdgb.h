@@ -277,6 +277,51 @@ void cfd_holemap_free(cfd_holemap_t h);
 int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, const cfd_holemap_t* maps,
                       int nfringe, int* iblank, int* mandatory);
 
+/* ---- learned relaxation (no reference counterpart) ------------------------- */
+/* A 12-64-64-2 perceptron (relu, bf16 weights, fp32 arithmetic) that maps 12
+ * features of a cell after its LU-SGS sweeps to o = (o0, o1): the cell's update
+ * is W += omega * dW with omega = 1 + 2*sigmoid(o0), and, when enabled, its
+ * next time step is multiplied by 2^(2*tanh(o1)).  The reference uses one
+ * constant CFL and omega = 1 (LUSGS_Integrator.h:18, .cpp:242-255), which stay
+ * the fallback; neither output changes the fixed point (dW = 0 there).
+ * Parameters, fp32, in this order: W1[64][12], b1[64], W2[64][64], b2[64],
+ * W3[2][64], b3[2]; the input transform norm[24] = mean[12], scale[12]
+ * (x^ = (x - mean) * scale).  Features, per cell (dW scaled per equation by
+ * rho, |rhoE|, rho(|u|+c), rho(|u|+c)): 0 log10|dW|, 1 log10|dW_prev|,
+ * 2 (dW.dW_prev)/|dW_prev|^2 clipped to [-4, 4], 3 cos(dW, dW_prev),
+ * 4 log10(|R_rho| dt/(vol rho)), 5 log10(spec_v/spec_c + 1e-12), 6 Mach,
+ * 7 min limiter, 8 log10(D dt/vol), 9 log10(wall distance/sqrt(vol) + 1e-6),
+ * 10 rho - 1, 11 p - 1. */
+#define CFD_MLP_INPUTS  12
+#define CFD_MLP_OUTPUTS 2
+#define CFD_MLP_PARAMS  5122
+typedef struct cfd_mlp_s* cfd_mlp_t;
+/* He-uniform weights from a seed; b3[0] = -4 (omega ~ 1.04 untrained). */
+int cfd_mlp_create(unsigned long long seed, cfd_mlp_t* out);
+void cfd_mlp_free(cfd_mlp_t m);
+/* Host copies of the fp32 parameters and the input transform (either may be NULL). */
+int cfd_mlp_get_params(cfd_mlp_t m, float* params, float* norm);
+int cfd_mlp_set_params(cfd_mlp_t m, const float* params, const float* norm);
+/* Raw outputs y[2n] for inputs x[12n] (device arrays). */
+int cfd_mlp_forward(cfd_mlp_t m, const float* d_x, long long n, float* d_y, void* stream);
+/* Loss (1/n) sum_i sum_o m_io (y_io - t_io)^2 over all n <= 2^20 rows and its
+ * gradient with respect to the bf16-rounded parameters (host grad[CFD_MLP_PARAMS],
+ * may be NULL).  d_m (per-output weights) may be NULL (all 1). */
+int cfd_mlp_loss_grad(cfd_mlp_t m, const float* d_x, const float* d_t, const float* d_m, long long n, double* loss,
+                      float* grad);
+/* `steps` Adam steps (beta 0.9 / 0.999) on minibatches of `batch` rows drawn
+ * from the n rows with a seeded counter hash; loss_hist[steps] (host, may be
+ * NULL) receives each minibatch's loss. */
+int cfd_mlp_train(cfd_mlp_t m, const float* d_x, const float* d_t, const float* d_m, long long n, int steps,
+                  int batch, float lr, unsigned long long seed, float* loss_hist);
+/* Keep each LU-SGS step's previous increment on the device (the features need it). */
+int cfd_case_track(cfd_case_t c, int on);
+/* Features of every cell (device x[12 * ncell_total]) from the last LU-SGS step. */
+int cfd_case_features(cfd_case_t c, float* d_x);
+/* Attach (m != NULL) or detach the learned relaxation; apply_cfl also applies
+ * the CFL output.  Detaching restores the constant CFL and the unit update. */
+int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl);
+
 /* Residual norm of a caller-owned device array that allocates nothing (no
  * counterpart in the reference, which has no device code).  For callers that
  * may not allocate device memory while they run: solvers that reserve all of

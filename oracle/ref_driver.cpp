@@ -181,6 +181,64 @@ int main(int argc, char** argv) {
     st->SolveTime(lu ? cfl : 0.8);
     dump("res0_dt", st->getStableTime()[0], (size_t)nc * 8);
 
+    // SST k-omega phase (environment SST_T = file of 2*nc doubles: per cell,
+    // multipliers of the freestream k and omega; optional SST_MUT = nc
+    // multipliers of the freestream mu_t).  The reference never runs
+    // this model (ViscousFlow2D::preprocessAdvanceSerial skips it and
+    // isLaminar() is true), so its functions are called here one by one on the
+    // laminar residual's arrays.  Two set-up steps make them callable:
+    //  * the model copied the flow's freestream when the flow was constructed,
+    //    before WrapSolver::setParams set Mach/Re, so it is copied again;
+    //  * FaceConvectiveTFlux / FaceViscousTFlux are allocated with 2*nCells
+    //    entries but indexed by faces (SSTKWStrategy.h:556-557 vs :805-815,
+    //    :907-913), so they are replaced by 2*nEdges arrays.
+    if (const char* sp = getenv("SST_T")) {
+        ViscousFlow2D* vf = (ViscousFlow2D*)st;
+        auto* sst = vf->d_turbulentModel;
+        sst->set_fs_variable(st);
+        sst->FaceConvectiveTFlux[0] = new double[2 * (size_t)ne];
+        sst->FaceViscousTFlux[0] = new double[2 * (size_t)ne];
+        sst->InitializeturbulenceVariable();
+        double inf[3] = {sst->fsnd_turbulenceValue[0], sst->fsnd_turbulenceValue[1], sst->fsnd_mut};
+        dump("sst_inf", inf, sizeof(inf));
+        std::vector<double> t(2 * (size_t)nc);
+        FILE* fp = fopen(sp, "rb");
+        if (!fp || fread(t.data(), 8, t.size(), fp) != t.size()) { std::cout.rdbuf(saved); fprintf(stderr, "bad SST_T\n"); return 4; }
+        fclose(fp);
+        for (int k = 0; k < nc; k++) {
+            sst->turbulenceCellValue[0][2 * k] = inf[0] * t[2 * k];
+            sst->turbulenceCellValue[0][2 * k + 1] = inf[1] * t[2 * k + 1];
+        }
+        if (const char* mp = getenv("SST_MUT")) {
+            std::vector<double> m(nc);
+            FILE* fm = fopen(mp, "rb");
+            if (!fm || fread(m.data(), 8, nc, fm) != (size_t)nc) { std::cout.rdbuf(saved); fprintf(stderr, "bad SST_MUT\n"); return 4; }
+            fclose(fm);
+            for (int k = 0; k < nc; k++) sst->vCellMut[0][k] = inf[2] * m[k];
+        }
+        dump("sst_T_in", sst->turbulenceCellValue[0], (size_t)nc * 16);
+        dump("sst_mut_in", sst->vCellMut[0], (size_t)nc * 8);
+        sst->SolveTurbulenceEquation();
+        dump("sst_tface", sst->turbulenceFaceValue[0], (size_t)ne * 16);
+        dump("sst_tgrad", sst->turbulenceCellGrad[0], (size_t)nc * 32);
+        dump("sst_f1", sst->cellF1[0], (size_t)nc * 8);
+        dump("sst_f2", sst->cellF2[0], (size_t)nc * 8);
+        dump("sst_mutf", sst->vFaceMut[0], (size_t)ne * 8);
+        dump("sst_fconv", sst->FaceConvectiveTFlux[0], (size_t)ne * 16);
+        dump("sst_fvisc", sst->FaceViscousTFlux[0], (size_t)ne * 16);
+        dump("sst_R", sst->CellTotalTFlux[0], (size_t)nc * 16);
+        std::vector<double> dg(2 * (size_t)nc);
+        double* dgp = dg.data();
+        sst->SolveDiag(&dgp);
+        dump("sst_diag", dg.data(), dg.size() * 8);
+        std::vector<double> w(2 * (size_t)nc);
+        double* wp = w.data();
+        sst->initializeConsData(&wp);
+        sst->UpdatePrimitiveVariables(&wp);
+        dump("sst_T2", sst->turbulenceCellValue[0], (size_t)nc * 16);
+        dump("sst_mut", sst->vCellMut[0], (size_t)nc * 8);
+    }
+
     // Full steps.  For LU-SGS the first step re-evaluates the same residual.
     std::vector<double> hist;
     auto t0 = std::chrono::steady_clock::now();

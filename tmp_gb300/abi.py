@@ -31,6 +31,7 @@ FIELD_SHAPE = dict(U=(4, 0), W=(4, 0), R=(4, 0), GRAD=(8, 0), PHI=(4, 0), SPEC_C
                    WALLDIST=(1, 0))
 NORM = dict(DW_RHO2=0, RK_DRHO=1, L2_R_RHO=2)
 LAYOUT_ROW, LAYOUT_COLUMN = 0, 1
+MLP_INPUTS, MLP_OUTPUTS, MLP_PARAMS = 12, 2, 5122
 
 
 class CfdError(RuntimeError):
@@ -62,7 +63,7 @@ def lib() -> C.CDLL:
         raise RuntimeError(f"{LIB_PATH} is missing: build it with tmp_gb300.build.build_library() "
                            "(there is no CPU fallback)")
     L = C.CDLL(str(LIB_PATH))
-    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    vp, ip, dp, fp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_float)
     sig = {
         "cfd_last_error": (C.c_char_p, []),
         "cfd_version": (C.c_int, []),
@@ -111,6 +112,16 @@ def lib() -> C.CDLL:
         "cfd_holemap_check": (C.c_int, [vp, C.c_longlong, dp, ip]),
         "cfd_holemap_free": (None, [vp]),
         "cfd_overset_blank": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.POINTER(vp), C.c_int, ip, ip]),
+        "cfd_mlp_create": (C.c_int, [C.c_ulonglong, C.POINTER(vp)]),
+        "cfd_mlp_free": (None, [vp]),
+        "cfd_mlp_get_params": (C.c_int, [vp, fp, fp]),
+        "cfd_mlp_set_params": (C.c_int, [vp, fp, fp]),
+        "cfd_mlp_forward": (C.c_int, [vp, vp, C.c_longlong, vp, vp]),
+        "cfd_mlp_loss_grad": (C.c_int, [vp, vp, vp, vp, C.c_longlong, dp, fp]),
+        "cfd_mlp_train": (C.c_int, [vp, vp, vp, vp, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong, fp]),
+        "cfd_case_track": (C.c_int, [vp, C.c_int]),
+        "cfd_case_features": (C.c_int, [vp, vp]),
+        "cfd_case_set_mlp": (C.c_int, [vp, vp, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -432,3 +443,69 @@ def overset_blank(block: Block, others: Sequence[Block], maps: Sequence[HoleMap 
     md = np.zeros(block.nnode, np.int32)
     check(lib().cfd_overset_blank(block.h, n, ob, mp, int(nfringe), _iptr(ib), _iptr(md)))
     return ib, md
+
+
+# ---- learned relaxation -------------------------------------------------------
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Mlp:
+    """The 12-64-64-2 relaxation network (bf16 weights, fp32 arithmetic) on the device."""
+
+    def __init__(self, seed: int = 0):
+        self.h = C.c_void_p()
+        check(lib().cfd_mlp_create(int(seed), C.byref(self.h)))
+
+    def params(self):
+        p = np.zeros(MLP_PARAMS, np.float32)
+        n = np.zeros(2 * MLP_INPUTS, np.float32)
+        check(lib().cfd_mlp_get_params(self.h, _fptr(p), _fptr(n)))
+        return p, n
+
+    def set_params(self, params=None, norm=None):
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        n = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        if p is not None and p.size != MLP_PARAMS or n is not None and n.size != 2 * MLP_INPUTS:
+            raise ValueError("wrong parameter count")
+        check(lib().cfd_mlp_set_params(self.h, _fptr(p) if p is not None else None,
+                                       _fptr(n) if n is not None else None))
+
+    def forward(self, x_ptr: int, n: int, y_ptr: int, stream: int | None = None):
+        check(lib().cfd_mlp_forward(self.h, C.c_void_p(x_ptr), int(n), C.c_void_p(y_ptr),
+                                    C.c_void_p(stream) if stream else None))
+
+    def loss_grad(self, x_ptr: int, t_ptr: int, m_ptr: int | None, n: int):
+        loss = C.c_double()
+        g = np.zeros(MLP_PARAMS, np.float32)
+        check(lib().cfd_mlp_loss_grad(self.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr),
+                                      C.c_void_p(m_ptr) if m_ptr else None, int(n), C.byref(loss), _fptr(g)))
+        return loss.value, g
+
+    def train(self, x_ptr: int, t_ptr: int, m_ptr: int | None, n: int, steps: int, batch: int, lr: float,
+              seed: int = 0) -> np.ndarray:
+        hist = np.zeros(max(steps, 1), np.float32)
+        check(lib().cfd_mlp_train(self.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), C.c_void_p(m_ptr) if m_ptr else None,
+                                  int(n), int(steps), int(batch), float(lr), int(seed), _fptr(hist)))
+        return hist[:steps]
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.cfd_mlp_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def case_track(case: "Case", on: bool = True):
+    check(lib().cfd_case_track(case.h, int(on)))
+
+
+def case_features(case: "Case", x_ptr: int):
+    check(lib().cfd_case_features(case.h, C.c_void_p(x_ptr)))
+
+
+def case_set_mlp(case: "Case", mlp: Mlp | None, apply_cfl: bool = False):
+    check(lib().cfd_case_set_mlp(case.h, mlp.h if mlp is not None else None, int(apply_cfl)))

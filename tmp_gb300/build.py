@@ -32,6 +32,7 @@ UNITS = [
     ("k_fp32.cu", []),
     ("k_misc.cu", []),
     ("k_overset.cu", ["-fmad=false"]),
+    ("k_mlp.cu", []),
     ("k_noalloc.cu", []),
 ]
 

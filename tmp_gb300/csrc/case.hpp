@@ -51,6 +51,8 @@ struct DevArrays {
     float* cflmul = nullptr;     // [nc] optional per-cell CFL multiplier (null = 1)
     d4* dW1 = nullptr;
     d4* dW = nullptr;
+    d4* dWprev = nullptr;        // [nc] previous LU-SGS increment (kept while tracking / learned)
+    float* omega = nullptr;      // [nc] relaxation of the last learned update
     // residual intermediates, binary64 form
     d4* grad = nullptr;          // [2*nc]
     d4* phi = nullptr;

@@ -15,6 +15,7 @@
 #include "../../include/cfdgb.h"
 #include "case.hpp"
 #include "mesh.hpp"
+#include "mlp.hpp"
 
 using namespace cfdgb;
 
@@ -91,6 +92,9 @@ struct cfd_case_s {
     cudaGraphExec_t gexec = nullptr;
     cudaGraph_t graph = nullptr;
     long long graph_nodes = 0;
+    bool track = false;              // keep the previous LU-SGS increment (learning features)
+    struct cfd_mlp_s* mlp = nullptr;  // learned relaxation, or null for the plain update
+    bool mlp_cfl = false;            // apply the network's CFL multipliers too
     bool viscous() const { return p.flow == CFD_FLOW_LAMINAR; }
     bool fp32() const { return p.precision == CFD_PREC_FP32; }
     bool mixed() const { return p.precision == CFD_PREC_MIXED; }
@@ -114,7 +118,7 @@ void free_case(cfd_case_s* c) {
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
                     d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.wall_ptr, d.wall_faces, d.wblocks, d.wpartial, d.wforce, d.swfcf, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
-                    d.norm_out, d.err};
+                    d.norm_out, d.err, d.dWprev, d.omega};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -177,15 +181,20 @@ void sweeps(cfd_case_s* c, bool forward) {
     }
 }
 
-// LUSGSIntegrator::UpdateSerial (LUSGS_Integrator.cpp:228-240).
+// LUSGSIntegrator::UpdateSerial (LUSGS_Integrator.cpp:228-240).  With a
+// learned network attached the final update is the fused learned one.
+void learned_update(cfd_case_s* c);
 void lusgs_step(cfd_case_s* c) {
-    residual_pass(c);
-    update_pass(c, 2 /*UPD_LUSGS*/, c->p.cfl, 0, 0.0);
     auto L = c->L();
     const DevArrays& d = c->d;
+    if (c->track || c->mlp)
+        ck(cudaMemcpyAsync(d.dWprev, d.dW, sizeof(d4) * d.nc, cudaMemcpyDeviceToDevice, c->stream), "dWprev");
+    residual_pass(c);
+    update_pass(c, 2 /*UPD_LUSGS*/, c->p.cfl, 0, 0.0);
     sweeps(c, true);
     sweeps(c, false);
-    launch_lusgs_update(d, L, c->fp32());
+    if (c->mlp) learned_update(c);
+    else launch_lusgs_update(d, L, c->fp32());
 }
 
 void one_step(cfd_case_s* c) {
@@ -861,6 +870,203 @@ int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host) {
     launch_cons_from_prim(c->d, L, off, off + n);
     if (c->fp32()) launch_to_fp32(c->d, L, false);
     ck(cudaGetLastError(), "launch");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Learned relaxation (k_mlp.cu)
+// ---------------------------------------------------------------------------
+
+struct cfd_mlp_s {
+    MlpNet net;
+    cudaStream_t stream = nullptr;
+    double* d_loss = nullptr;
+    ~cfd_mlp_s() {
+        if (d_loss) cudaFree(d_loss);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+void learned_update(cfd_case_s* c) { launch_learned_update(c->d, c->L(), c->mlp->net, c->mlp_cfl, c->fp32()); }
+}  // namespace
+
+namespace {
+unsigned long long splitmix(unsigned long long& z) {
+    unsigned long long r = (z += 0x9e3779b97f4a7c15ull);
+    r = (r ^ (r >> 30)) * 0xbf58476d1ce4e5b9ull;
+    r = (r ^ (r >> 27)) * 0x94d049bb133111ebull;
+    return r ^ (r >> 31);
+}
+}  // namespace
+
+extern "C" {
+
+int cfd_mlp_create(unsigned long long seed, cfd_mlp_t* out) {
+    if (!out) return fail(CFD_ERR_ARG, "null output");
+    *out = nullptr;
+    cfd_mlp_s* m = new (std::nothrow) cfd_mlp_s;
+    if (!m) return fail(CFD_ERR_ARG, "out of host memory");
+    try {
+    ck(m->net.init(), "cudaMalloc");
+    ck(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    // uniform(-a, a) with a = sqrt(6 / fan_in) (He); the first output's bias
+    // starts at -4 so an untrained network relaxes by ~1.04.
+    std::vector<float> p(kMlpParams, 0.f);
+    const int NI = kMlpIn, NH = kMlpHidden;
+    unsigned long long z = seed;
+    auto uni = [&](double a) { return (float)(a * (2.0 * ((splitmix(z) >> 11) * 0x1.0p-53) - 1.0)); };
+    int o = 0;
+    for (int i = 0; i < NH * NI; i++) p[o++] = uni(std::sqrt(6.0 / NI));
+    o += NH;
+    for (int i = 0; i < NH * NH; i++) p[o++] = uni(std::sqrt(6.0 / NH));
+    o += NH;
+    for (int i = 0; i < kMlpOut * NH; i++) p[o++] = uni(std::sqrt(1.0 / NH));
+    p[o] = -4.f;
+    std::vector<float> norm(2 * NI, 0.f);
+    for (int i = 0; i < NI; i++) norm[NI + i] = 1.f;
+    ck(cudaMemcpy(m->net.p, p.data(), p.size() * 4, cudaMemcpyHostToDevice), "upload");
+    ck(cudaMemcpy(m->net.norm, norm.data(), norm.size() * 4, cudaMemcpyHostToDevice), "upload");
+    m->net.quantize(m->stream);
+    ck(cudaStreamSynchronize(m->stream), "sync");
+    *out = m;
+    return CFD_OK;
+    } catch (const std::exception& ex) {
+        delete m;
+        return fail(CFD_ERR_CUDA, ex.what());
+    }
+}
+
+void cfd_mlp_free(cfd_mlp_t m) { delete m; }
+
+int cfd_mlp_get_params(cfd_mlp_t m, float* params, float* norm) {
+    if (!m) return fail(CFD_ERR_ARG, "null network");
+    ABI_TRY
+    if (params) ck(cudaMemcpy(params, m->net.p, kMlpParams * 4, cudaMemcpyDeviceToHost), "download");
+    if (norm) ck(cudaMemcpy(norm, m->net.norm, 2 * kMlpIn * 4, cudaMemcpyDeviceToHost), "download");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_mlp_set_params(cfd_mlp_t m, const float* params, const float* norm) {
+    if (!m) return fail(CFD_ERR_ARG, "null network");
+    ABI_TRY
+    if (params) {
+        for (int i = 0; i < kMlpParams; i++)
+            if (!std::isfinite(params[i])) return fail(CFD_ERR_ARG, "non-finite parameter");
+        ck(cudaMemcpy(m->net.p, params, kMlpParams * 4, cudaMemcpyHostToDevice), "upload");
+        m->net.quantize(m->stream);
+        ck(cudaStreamSynchronize(m->stream), "sync");
+    }
+    if (norm) ck(cudaMemcpy(m->net.norm, norm, 2 * kMlpIn * 4, cudaMemcpyHostToDevice), "upload");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_mlp_forward(cfd_mlp_t m, const float* d_x, long long n, float* d_y, void* stream) {
+    if (!m || n < 0 || (n > 0 && (!d_x || !d_y))) return fail(CFD_ERR_ARG, "cfd_mlp_forward: bad argument");
+    ABI_TRY
+    ck(mlp_forward(m->net, d_x, n, d_y, stream ? (cudaStream_t)stream : m->stream), "k_mlp_forward");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_mlp_loss_grad(cfd_mlp_t m, const float* d_x, const float* d_t, const float* d_m, long long n, double* loss,
+                      float* grad) {
+    if (!m || n <= 0 || n > (1 << 20) || !d_x || !d_t) return fail(CFD_ERR_ARG, "cfd_mlp_loss_grad: bad argument");
+    ABI_TRY
+    if (!m->d_loss) dalloc(&m->d_loss, 1);
+    ck(mlp_batch_grad(m->net, nullptr, (int)n, d_x, d_t, d_m, (float)(1.0 / n), m->d_loss, m->stream), "grad");
+    if (loss) ck(cudaMemcpyAsync(loss, m->d_loss, 8, cudaMemcpyDeviceToHost, m->stream), "download");
+    if (grad) ck(cudaMemcpyAsync(grad, m->net.G, kMlpParams * 4, cudaMemcpyDeviceToHost, m->stream), "download");
+    ck(cudaStreamSynchronize(m->stream), "sync");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_mlp_train(cfd_mlp_t m, const float* d_x, const float* d_t, const float* d_m, long long n, int steps, int batch,
+                  float lr, unsigned long long seed, float* loss_hist) {
+    if (!m || n <= 0 || n >= (1ll << 31) || steps < 0 || batch <= 0 || batch > (1 << 20) || !(lr > 0) || !d_x || !d_t)
+        return fail(CFD_ERR_ARG, "cfd_mlp_train: bad argument");
+    ABI_TRY
+    MlpNet& net = m->net;
+    if (net.losses_cap < steps) {
+        if (net.losses) cudaFree(net.losses);
+        net.losses = nullptr;
+        dalloc(&net.losses, std::max(steps, 1));
+        net.losses_cap = steps;
+    }
+    for (int k = 0; k < steps; k++) {
+        ck(mlp_batch_rows(net, batch, n, seed + 0x632be59bd9b4e019ull * (unsigned long long)(k + 1), m->stream),
+           "rows");
+        ck(mlp_batch_grad(net, net.idx, batch, d_x, d_t, d_m, 1.f / batch, net.losses + k, m->stream), "grad");
+        ck(mlp_adam(net, lr, m->stream), "adam");
+    }
+    if (loss_hist && steps > 0) {
+        std::vector<double> h(steps);
+        ck(cudaMemcpyAsync(h.data(), net.losses, steps * 8, cudaMemcpyDeviceToHost, m->stream), "download");
+        ck(cudaStreamSynchronize(m->stream), "sync");
+        for (int k = 0; k < steps; k++) loss_hist[k] = (float)h[k];
+    }
+    ck(cudaStreamSynchronize(m->stream), "sync");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_case_track(cfd_case_t c, int on) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (c->p.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_STATE, "tracking needs the LU-SGS integrator");
+    ABI_TRY
+    DevArrays& d = c->d;
+    if (!d.dWprev) {
+        dalloc(&d.dWprev, d.nc);
+        dalloc(&d.omega, d.nc);
+        ck(cudaMemsetAsync(d.dWprev, 0, sizeof(d4) * d.nc, c->stream), "memset");
+        ck(cudaMemsetAsync(d.dW, 0, sizeof(d4) * d.nc, c->stream), "memset");
+        std::vector<float> one(d.nc, 1.0f);
+        ck(cudaMemcpyAsync(d.omega, one.data(), one.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+    }
+    if (c->track != (on != 0)) c->drop_graph();
+    c->track = on != 0;
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_case_features(cfd_case_t c, float* d_x) {
+    if (!c || !d_x) return fail(CFD_ERR_ARG, "null argument");
+    if (!c->d.dWprev) return fail(CFD_ERR_STATE, "call cfd_case_track first");
+    ABI_TRY
+    launch_case_features(c->d, c->L(), d_x);
+    ck(cudaGetLastError(), "k_case_features");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (c->p.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_STATE, "the learned relaxation needs the LU-SGS integrator");
+    ABI_TRY
+    if (m) {
+        int rc = cfd_case_track(c, c->track ? 1 : 0);
+        if (rc != CFD_OK) return rc;
+        if (!c->d.cflmul) {
+            dalloc(&c->d.cflmul, c->d.nc);
+            std::vector<float> one(c->d.nc, 1.0f);
+            ck(cudaMemcpyAsync(c->d.cflmul, one.data(), one.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+            ck(cudaStreamSynchronize(c->stream), "sync");
+        }
+    } else if (c->d.cflmul) {
+        std::vector<float> one(c->d.nc, 1.0f);  // back to the constant CFL
+        ck(cudaMemcpyAsync(c->d.cflmul, one.data(), one.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+    }
+    c->drop_graph();
+    c->mlp = m;
+    c->mlp_cfl = apply_cfl != 0;
     return CFD_OK;
     ABI_CATCH
 }

@@ -1,0 +1,404 @@
+// Learned per-cell LU-SGS relaxation and local CFL: a 12-64-64-2 multilayer
+// perceptron with bf16 weights and fp32 arithmetic, its training kernels
+// (forward, backward, Adam) and the fused step kernel that evaluates it on
+// every cell of a case.  No reference counterpart: the reference advances
+// every cell with one constant CFL (LUSGS_Integrator.h:18) and a unit update
+// (LUSGS_Integrator.cpp:242-255).
+//
+// Network.  x (12 features) -> h1 = relu(W1 x^ + b1) -> h2 = relu(W2 h1 + b2)
+// -> o = W3 h2 + b3, with x^ = (x - mean) * scale.  The forward pass uses the
+// bf16-rounded weights; training keeps fp32 master weights, takes gradients
+// with respect to the rounded weights (straight through) and updates the
+// masters with Adam.  Gradients are plain sums over the batch computed one
+// parameter per thread in a fixed order, so they are deterministic.
+//
+// Outputs.  omega = 1 + 2 * sigmoid(o0) scales the cell's LU-SGS increment
+// (W += omega * dW); cflmul = 2^(2 * tanh(o1)) multiplies its next time step.
+// Neither changes the fixed point of the iteration: at convergence dW = 0.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/cfdgb.h"
+#include "case.hpp"
+#include "mlp.hpp"
+
+namespace cfdgb {
+namespace {
+
+constexpr int NI = kMlpIn, NH = kMlpHidden, NO = kMlpOut;
+constexpr int OFF_W1 = 0, OFF_B1 = NH * NI, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH,
+              OFF_B3 = OFF_W3 + NO * NH, NPAR = OFF_B3 + NO;
+static_assert(NPAR == kMlpParams, "parameter layout");
+
+__device__ __forceinline__ float bf(const __nv_bfloat16* w, int i) { return __bfloat162float(w[i]); }
+
+// Network state in shared memory: bf16 weights, fp32 biases and input transform.
+struct SmemNet {
+    __nv_bfloat16 w1[NH * NI], w2[NH * NH], w3[NO * NH];
+    float b1[NH], b2[NH], b3[NO], mean[NI], scale[NI];
+};
+
+__device__ void load_net(SmemNet& s, const __nv_bfloat16* __restrict__ wq, const float* __restrict__ p,
+                         const float* __restrict__ norm) {
+    for (int i = threadIdx.x; i < NH * NI; i += blockDim.x) s.w1[i] = wq[OFF_W1 + i];
+    for (int i = threadIdx.x; i < NH * NH; i += blockDim.x) s.w2[i] = wq[OFF_W2 + i];
+    for (int i = threadIdx.x; i < NO * NH; i += blockDim.x) s.w3[i] = wq[OFF_W3 + i];
+    for (int i = threadIdx.x; i < NH; i += blockDim.x) {
+        s.b1[i] = p[OFF_B1 + i];
+        s.b2[i] = p[OFF_B2 + i];
+    }
+    if (threadIdx.x < NO) s.b3[threadIdx.x] = p[OFF_B3 + threadIdx.x];
+    if (threadIdx.x < NI) {
+        s.mean[threadIdx.x] = norm[threadIdx.x];
+        s.scale[threadIdx.x] = norm[NI + threadIdx.x];
+    }
+    __syncthreads();
+}
+
+// Forward pass of one sample; h1 / h2 keep the post-activation values.
+__device__ __forceinline__ void net_forward(const SmemNet& s, const float* x, float* xh, float* h1, float* h2,
+                                            float* o) {
+    // Loops that index the per-thread arrays are fully unrolled so that the
+    // arrays stay in registers.
+#pragma unroll
+    for (int k = 0; k < NI; k++) xh[k] = (x[k] - s.mean[k]) * s.scale[k];
+#pragma unroll
+    for (int j = 0; j < NH; j++) {
+        float a = s.b1[j];
+#pragma unroll
+        for (int k = 0; k < NI; k++) a = fmaf(bf(s.w1, j * NI + k), xh[k], a);
+        h1[j] = fmaxf(a, 0.f);
+    }
+    float o0 = s.b3[0], o1 = s.b3[1];
+#pragma unroll 1
+    for (int j = 0; j < NH; j++) {
+        float a = s.b2[j];
+#pragma unroll
+        for (int k = 0; k < NH; k++) a = fmaf(bf(s.w2, j * NH + k), h1[k], a);
+        a = fmaxf(a, 0.f);
+        if (h2) h2[j] = a;
+        o0 = fmaf(bf(s.w3, j), a, o0);
+        o1 = fmaf(bf(s.w3, NH + j), a, o1);
+    }
+    o[0] = o0;
+    o[1] = o1;
+}
+
+__global__ void k_quantize(const float* __restrict__ p, __nv_bfloat16* __restrict__ wq) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < NPAR) wq[i] = __float2bfloat16_rn(p[i]);
+}
+
+__global__ void __launch_bounds__(128) k_mlp_forward(long long n, const float* __restrict__ X,
+                                                     const __nv_bfloat16* __restrict__ wq,
+                                                     const float* __restrict__ p, const float* __restrict__ norm,
+                                                     float* __restrict__ Y) {
+    __shared__ SmemNet s;
+    load_net(s, wq, p, norm);
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float x[NI], xh[NI], h1[NH], o[NO];
+#pragma unroll
+    for (int k = 0; k < NI; k++) x[k] = X[i * NI + k];
+    net_forward(s, x, xh, h1, nullptr, o);
+    Y[2 * i] = o[0];
+    Y[2 * i + 1] = o[1];
+}
+
+// Training forward + output and hidden deltas for a batch (rows idx[b] of X).
+// Loss = sum_b sum_o M[b,o] (y - t)^2 / msum.
+__global__ void __launch_bounds__(128) k_mlp_train_fwd(int B, const int* __restrict__ idx,
+                                                       const float* __restrict__ X, const float* __restrict__ T,
+                                                       const float* __restrict__ M,
+                                                       const __nv_bfloat16* __restrict__ wq,
+                                                       const float* __restrict__ p, const float* __restrict__ norm,
+                                                       float inv_msum, float* __restrict__ XH, float* __restrict__ H1,
+                                                       float* __restrict__ H2, float* __restrict__ D1,
+                                                       float* __restrict__ D2, float* __restrict__ DO,
+                                                       float* __restrict__ L) {
+    __shared__ SmemNet s;
+    load_net(s, wq, p, norm);
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const long long r = idx ? idx[b] : b;
+    float x[NI], xh[NI], h1[NH], h2[NH], o[NO];
+#pragma unroll
+    for (int k = 0; k < NI; k++) x[k] = X[r * NI + k];
+    net_forward(s, x, xh, h1, h2, o);
+    float d[NO], loss = 0.f;
+#pragma unroll
+    for (int q = 0; q < NO; q++) {
+        const float e = o[q] - T[r * NO + q];
+        const float m = M ? M[r * NO + q] : 1.f;
+        loss += m * e * e;
+        d[q] = 2.f * m * e * inv_msum;
+        DO[(long long)b * NO + q] = d[q];
+    }
+    L[b] = loss * inv_msum;
+    for (int k = 0; k < NI; k++) XH[(long long)b * NI + k] = xh[k];
+    // dL/dh2 through the relu (kept in h2's registers), then dL/dh1
+    for (int j = 0; j < NH; j++) {
+        H1[(long long)b * NH + j] = h1[j];
+        H2[(long long)b * NH + j] = h2[j];
+        h2[j] = h2[j] > 0.f ? d[0] * bf(s.w3, j) + d[1] * bf(s.w3, NH + j) : 0.f;
+        D2[(long long)b * NH + j] = h2[j];
+    }
+    for (int k = 0; k < NH; k++) {
+        float a = 0.f;
+        if (h1[k] > 0.f) {
+#pragma unroll 16
+            for (int j = 0; j < NH; j++) a = fmaf(h2[j], bf(s.w2, j * NH + k), a);
+        }
+        D1[(long long)b * NH + k] = a;
+    }
+}
+
+// One thread per parameter: its gradient as a batch sum in row order.
+__global__ void k_mlp_wgrad(int B, const float* __restrict__ XH, const float* __restrict__ H1,
+                            const float* __restrict__ H2, const float* __restrict__ D1, const float* __restrict__ D2,
+                            const float* __restrict__ DO, float* __restrict__ G) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= NPAR) return;
+    const float *a, *c = nullptr;
+    int sa, sc = 0;
+    if (t < OFF_B1) {
+        const int j = t / NI, k = t % NI;
+        a = D1 + j; sa = NH; c = XH + k; sc = NI;
+    } else if (t < OFF_W2) {
+        a = D1 + (t - OFF_B1); sa = NH;
+    } else if (t < OFF_B2) {
+        const int j = (t - OFF_W2) / NH, k = (t - OFF_W2) % NH;
+        a = D2 + j; sa = NH; c = H1 + k; sc = NH;
+    } else if (t < OFF_W3) {
+        a = D2 + (t - OFF_B2); sa = NH;
+    } else if (t < OFF_B3) {
+        const int q = (t - OFF_W3) / NH, k = (t - OFF_W3) % NH;
+        a = DO + q; sa = NO; c = H2 + k; sc = NH;
+    } else {
+        a = DO + (t - OFF_B3); sa = NO;
+    }
+    float g = 0.f;
+    if (c)
+        for (int b = 0; b < B; b++) g = fmaf(a[(long long)b * sa], c[(long long)b * sc], g);
+    else
+        for (int b = 0; b < B; b++) g += a[(long long)b * sa];
+    G[t] = g;
+}
+
+__global__ void k_sum(int n, const float* __restrict__ v, double* __restrict__ out) {
+    __shared__ double s[256];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) a += v[i];
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) s[threadIdx.x] += s[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = s[0];
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, float lr, float b1, float b2, float c1, float c2, float eps) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NPAR) return;
+    const float gi = g[i];
+    const float a = b1 * m1[i] + (1.f - b1) * gi;
+    const float v = b2 * m2[i] + (1.f - b2) * gi * gi;
+    m1[i] = a;
+    m2[i] = v;
+    p[i] -= lr * (a / c1) / (sqrtf(v / c2) + eps);
+}
+
+// Minibatch rows from a counter-based hash (splitmix64 of seed and position).
+__global__ void k_batch_rows(int B, long long n, unsigned long long seed, int* __restrict__ idx) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    unsigned long long z = seed + 0x9e3779b97f4a7c15ull * (unsigned long long)(b + 1);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    idx[b] = (int)(z % (unsigned long long)n);
+}
+
+// ---- features of one cell ---------------------------------------------------
+
+__device__ __forceinline__ float safe_log10(float v) { return log10f(fmaxf(v, 1e-30f)); }
+
+// The 12 inputs of cell c from the state after its LU-SGS sweeps.
+__device__ void cell_features(const DevArrays& d, int c, float* f) {
+    const d4 w = d.W[c], u = d.U[c], dw = d.dW[c], dp = d.dWprev[c], r = d.R[c];
+    const double vol = d.cgeo[c].x;
+    const float rho = (float)u.x, p = (float)u.y, ux = (float)u.z, uy = (float)u.w;
+    const float cs = sqrtf(fmaxf(1.4f * p / rho, 1e-30f));
+    const float vm = sqrtf(ux * ux + uy * uy);
+    const float ref[4] = {rho, fmaxf((float)fabs(w.y), 1e-30f), rho * (vm + cs), rho * (vm + cs)};
+    const float a[4] = {(float)dw.x / ref[0], (float)dw.y / ref[1], (float)dw.z / ref[2], (float)dw.w / ref[3]};
+    const float b[4] = {(float)dp.x / ref[0], (float)dp.y / ref[1], (float)dp.z / ref[2], (float)dp.w / ref[3]};
+    float aa = 0.f, bb = 0.f, ab = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        aa += a[k] * a[k];
+        bb += b[k] * b[k];
+        ab += a[k] * b[k];
+    }
+    const double dt = d.dt[c];
+    const float sc = d.specc ? (float)d.specc[c] : d.speccf[c];
+    const float sv = d.specv ? (float)d.specv[c] : (d.specvf ? d.specvf[c] : 0.f);
+    float phimin = 1.f;
+    if (d.phi) {
+        const d4 ph = d.phi[c];
+        phimin = (float)fmin(fmin(ph.x, ph.y), fmin(ph.z, ph.w));
+    } else if (d.phif) {
+        const float4 ph = d.phif[c];
+        phimin = fminf(fminf(ph.x, ph.y), fminf(ph.z, ph.w));
+    }
+    f[0] = safe_log10(sqrtf(aa));
+    f[1] = safe_log10(sqrtf(bb));
+    f[2] = fminf(fmaxf(ab / fmaxf(bb, 1e-30f), -4.f), 4.f);
+    f[3] = ab / fmaxf(sqrtf(aa * bb), 1e-30f);
+    f[4] = safe_log10((float)(fabs(r.x) * dt / (vol * u.x)));
+    f[5] = safe_log10(sv / fmaxf(sc, 1e-30f) + 1e-12f);
+    f[6] = vm / cs;
+    f[7] = phimin;
+    f[8] = safe_log10((float)(d.diag[c] * dt / vol));
+    f[9] = d.walld ? safe_log10((float)(d.walld[c] / sqrt(vol)) + 1e-6f) : 0.f;
+    f[10] = rho - 1.f;
+    f[11] = p - 1.f;
+}
+
+__global__ void k_case_features(DevArrays d, float* __restrict__ X) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nc) return;
+    float f[NI];
+    cell_features(d, c, f);
+#pragma unroll
+    for (int k = 0; k < NI; k++) X[(long long)c * NI + k] = f[k];
+}
+
+// Fused learned update: features -> network -> W += omega * dW, U = prim(W),
+// next step's CFL multiplier.  apply_cfl = 0 leaves the multipliers at 1.
+__global__ void __launch_bounds__(128) k_learned_update(DevArrays d, const __nv_bfloat16* __restrict__ wq,
+                                                        const float* __restrict__ p,
+                                                        const float* __restrict__ norm, int apply_cfl,
+                                                        float4* __restrict__ Uf) {
+    __shared__ SmemNet s;
+    load_net(s, wq, p, norm);
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nc) return;
+    float x[NI], xh[NI], h1[NH], o[NO];
+    cell_features(d, c, x);
+    net_forward(s, x, xh, h1, nullptr, o);
+    const double omega = 1.0 + 2.0 / (1.0 + exp(-(double)o[0]));
+    const d4 dw = d.dW[c];
+    double w[4] = {d.W[c].x + omega * dw.x, d.W[c].y + omega * dw.y, d.W[c].z + omega * dw.z,
+                   d.W[c].w + omega * dw.w};
+    double u[4];
+    prim_from_cons<double>(w, u);
+    d.W[c] = d4{w[0], w[1], w[2], w[3]};
+    d.U[c] = d4{u[0], u[1], u[2], u[3]};
+    if (Uf) Uf[c] = make_float4((float)u[0], (float)u[1], (float)u[2], (float)u[3]);
+    if (d.cflmul) d.cflmul[c] = apply_cfl ? exp2f(2.f * tanhf(o[1])) : 1.f;
+    if (d.omega) d.omega[c] = (float)omega;
+    if (!(u[0] > 0.0) || !(u[1] > 0.0)) atomicOr(d.err, ERR_NONPHYS);
+}
+
+inline unsigned nb(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+}  // namespace
+
+// ---- host side ----------------------------------------------------------------
+
+MlpNet::~MlpNet() {
+    for (void* q : {(void*)p, (void*)m1, (void*)m2, (void*)G, (void*)norm, (void*)wq, (void*)XH, (void*)H1,
+                    (void*)H2, (void*)D1, (void*)D2, (void*)DO, (void*)L, (void*)idx, (void*)losses})
+        if (q) cudaFree(q);
+}
+
+cudaError_t MlpNet::init() {
+    cudaError_t e;
+    if ((e = cudaMalloc(&p, NPAR * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&m1, NPAR * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&m2, NPAR * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&G, NPAR * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&norm, 2 * NI * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&wq, NPAR * sizeof(__nv_bfloat16)))) return e;
+    if ((e = cudaMemset(m1, 0, NPAR * sizeof(float)))) return e;
+    if ((e = cudaMemset(m2, 0, NPAR * sizeof(float)))) return e;
+    return cudaSuccess;
+}
+
+cudaError_t MlpNet::reserve(int B) {
+    if (B <= cap) return cudaSuccess;
+    for (float** q : {&XH, &H1, &H2, &D1, &D2, &DO, &L}) {
+        if (*q) cudaFree(*q);
+        *q = nullptr;
+    }
+    if (idx) cudaFree(idx);
+    idx = nullptr;
+    cap = 0;
+    cudaError_t e;
+    const size_t b = (size_t)B;
+    if ((e = cudaMalloc(&XH, b * NI * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&H1, b * NH * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&H2, b * NH * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&D1, b * NH * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&D2, b * NH * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&DO, b * NO * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&L, b * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&idx, b * sizeof(int)))) return e;
+    cap = B;
+    return cudaSuccess;
+}
+
+void MlpNet::quantize(cudaStream_t s) const { k_quantize<<<nb(NPAR, 256), 256, 0, s>>>(p, wq); }
+
+void launch_case_features(const DevArrays& d, const LaunchCfg& L, float* X) {
+    k_case_features<<<nb(d.nc, 128), 128, 0, L.stream>>>(d, X);
+    *L.counter += 1;
+}
+
+void launch_learned_update(const DevArrays& d, const LaunchCfg& L, const MlpNet& net, bool apply_cfl,
+                           bool fp32_copy) {
+    k_learned_update<<<nb(d.nc, 128), 128, 0, L.stream>>>(d, net.wq, net.p, net.norm, apply_cfl ? 1 : 0,
+                                                          fp32_copy ? d.Uf : nullptr);
+    *L.counter += 1;
+}
+
+cudaError_t mlp_forward(const MlpNet& net, const float* X, long long n, float* Y, cudaStream_t s) {
+    if (n > 0) k_mlp_forward<<<nb(n, 128), 128, 0, s>>>(n, X, net.wq, net.p, net.norm, Y);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_batch_grad(MlpNet& net, const int* idx, int B, const float* X, const float* T, const float* M,
+                           float inv_msum, double* d_loss, cudaStream_t s) {
+    if (cudaError_t e = net.reserve(B)) return e;
+    k_mlp_train_fwd<<<nb(B, 128), 128, 0, s>>>(B, idx, X, T, M, net.wq, net.p, net.norm, inv_msum, net.XH, net.H1,
+                                                net.H2, net.D1, net.D2, net.DO, net.L);
+    k_mlp_wgrad<<<nb(NPAR, 128), 128, 0, s>>>(B, net.XH, net.H1, net.H2, net.D1, net.D2, net.DO, net.G);
+    if (d_loss) k_sum<<<1, 256, 0, s>>>(B, net.L, d_loss);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_adam(MlpNet& net, float lr, cudaStream_t s) {
+    net.t += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)net.t), c2 = 1.f - powf(b2, (float)net.t);
+    k_adam<<<nb(NPAR, 256), 256, 0, s>>>(net.p, net.G, net.m1, net.m2, lr, b1, b2, c1, c2, 1e-8f);
+    k_quantize<<<nb(NPAR, 256), 256, 0, s>>>(net.p, net.wq);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_batch_rows(MlpNet& net, int B, long long n, unsigned long long seed, cudaStream_t s) {
+    if (cudaError_t e = net.reserve(B)) return e;
+    k_batch_rows<<<nb(B, 256), 256, 0, s>>>(B, n, seed, net.idx);
+    return cudaGetLastError();
+}
+
+}  // namespace cfdgb

@@ -1,0 +1,191 @@
+"""Learned per-cell LU-SGS relaxation: training data from the solver's own
+convergence histories, training on the device, and the driver that runs a
+case with the network and falls back to the plain update.
+
+Data.  A case is advanced with the plain LU-SGS update while the library
+keeps each step's previous increment.  At snapshot iterations n the 12
+features of every cell are taken (cfd_case_features); the solver then runs K
+more plain steps.  With a = dW_n and s = dW_n + ... + dW_{n+K-1} (each scaled
+per equation as the features are), the cell's relaxation target is the
+extrapolation factor omega* = clip((s.a)/(a.a), 1, 3): in a cell whose
+increments keep their direction, a step of omega* * dW_n covers what the next
+steps would add.  The CFL target is the switched-evolution factor of the
+cell's own residual over the window, m* = clip((|R_{n+K}| / |R_n|)^(-1/2),
+1/4, 4).  Targets are stored as the network's raw outputs (inverse of
+omega = 1 + 2 sigmoid(o0), cflmul = 2^(2 tanh(o1))).
+
+Run.  run_to_drop() attaches the network after a few plain steps and watches
+the L2 density residual every `chunk` steps; if it rises above `fallback`
+times the best value seen, the network is detached and the run continues
+with the plain update (the reference's method), which also decides the
+converged state.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi, configs, meshgen
+
+
+@dataclass
+class CaseSpec:
+    """One training or evaluation case: a cylinder mixed mesh and a flow."""
+
+    nbody: int = 64
+    nlayer: int = 12
+    seed: int = 7
+    mach: float = 0.2
+    aoa: float = 0.0
+    re: float = 40.0
+    cfl: float = 50.0
+    flow: str = "laminar"
+
+    def mesh(self) -> abi.Mesh:
+        m = meshgen.mixed_mesh(configs.cylinder(self.nbody), nlayer=self.nlayer, dr1=1e-2, growth=1.1, rfar=15.0,
+                               seed=self.seed, density=1.0, grade=0.82)
+        import tempfile
+        from pathlib import Path
+        p = Path(tempfile.mkdtemp()) / "m.grd"
+        meshgen.write_grd(p, m)
+        return abi.Mesh.load_grd(p, -1, -2)
+
+    def case(self, mesh: abi.Mesh, precision: int = abi.PREC_FP64) -> abi.Case:
+        c = abi.Case([mesh], [dict(mach=self.mach, aoa_deg=self.aoa, reynolds=self.re)],
+                     abi.FLOW_LAMINAR if self.flow == "laminar" else abi.FLOW_EULER, abi.ADV_LUSGS, precision,
+                     cfl=self.cfl)
+        c.init_freestream()
+        return c
+
+
+def sweep_specs(n: int, seed: int = 0) -> list[CaseSpec]:
+    """Seeded Mach / AoA / Reynolds sweep of small cylinder cases."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        out.append(CaseSpec(nbody=int(rng.choice([48, 64, 80])), nlayer=int(rng.integers(10, 16)),
+                            seed=int(rng.integers(1, 1 << 20)), mach=float(rng.uniform(0.15, 0.4)),
+                            aoa=float(rng.uniform(-4, 10)), re=float(rng.choice([20.0, 40.0, 100.0])),
+                            cfl=50.0))
+    return out
+
+
+def _ref_scale(U: np.ndarray, W: np.ndarray) -> np.ndarray:
+    rho, p, u, v = U.T
+    c = np.sqrt(np.maximum(1.4 * p / rho, 1e-30))
+    vm = np.hypot(u, v)
+    return np.stack([rho, np.maximum(np.abs(W[:, 1]), 1e-30), rho * (vm + c), rho * (vm + c)], 1)
+
+
+def generate(specs, snapshots=(30, 60, 120, 240, 480, 960), K: int = 8, precision: int = abi.PREC_FP64):
+    """(X, T, M) numpy arrays: features, raw-output targets and weights."""
+    import torch
+
+    Xs, Ts, Ms = [], [], []
+    for spec in specs:
+        mesh = spec.mesh()
+        case = spec.case(mesh, precision)
+        abi.case_track(case, True)
+        nc = case.ncell
+        feat = torch.empty(nc * abi.MLP_INPUTS, dtype=torch.float32, device="cuda")
+        it = 0
+        for n in snapshots:
+            if n > it:
+                case.step_graph(n - it)
+            case.sync()
+            abi.case_features(case, feat.data_ptr())
+            case.sync()
+            X = feat.view(nc, abi.MLP_INPUTS).cpu().numpy().copy()
+            U, W = case.get("U"), case.get("W")
+            a = case.get("DW")
+            r0 = np.abs(case.get("R")[:, 0])
+            s = a.copy()
+            for _ in range(K - 1):
+                case.step_graph(1)
+                s += case.get("DW")
+            r1 = np.abs(case.get("R")[:, 0])
+            it = n + K
+            ref = _ref_scale(U, W)
+            an, sn = a / ref, s / ref
+            aa = (an * an).sum(1)
+            om = np.clip((sn * an).sum(1) / np.maximum(aa, 1e-300), 1.0, 3.0)
+            q = np.clip((om - 1.0) / 2.0, 1e-3, 1 - 1e-3)
+            t0 = np.log(q / (1 - q))
+            mstar = np.clip(np.sqrt(np.maximum(r0, 1e-300) / np.maximum(r1, 1e-300)), 0.25, 4.0)
+            t1 = np.arctanh(np.clip(np.log2(mstar) / 2.0, -0.96, 0.96))
+            ok = np.isfinite(X).all(1) & (aa > 1e-28) & np.isfinite(t0) & np.isfinite(t1)
+            Xs.append(X[ok])
+            Ts.append(np.stack([t0, t1], 1)[ok].astype(np.float32))
+            Ms.append(np.ones((ok.sum(), 2), np.float32))
+        case.close()
+    return np.concatenate(Xs), np.concatenate(Ts), np.concatenate(Ms)
+
+
+def fit(X, T, M, steps: int = 3000, batch: int = 4096, lr: float = 2e-3, seed: int = 1):
+    """Train a fresh network on the device; returns (mlp, loss history)."""
+    import torch
+
+    mlp = abi.Mlp(seed)
+    mean = X.mean(0)
+    std = X.std(0)
+    p, _ = mlp.params()
+    mlp.set_params(p, np.concatenate([mean, 1.0 / np.maximum(std, 1e-6)]).astype(np.float32))
+    dx = torch.tensor(X, dtype=torch.float32, device="cuda")
+    dt = torch.tensor(T, dtype=torch.float32, device="cuda")
+    dm = torch.tensor(M, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    hist = mlp.train(dx.data_ptr(), dt.data_ptr(), dm.data_ptr(), len(X), steps, min(batch, len(X)), lr, seed)
+    return mlp, hist
+
+
+@dataclass
+class RunResult:
+    reached: bool
+    iterations: int
+    seconds: float
+    history: list
+    fell_back: bool
+
+
+def run_to_drop(case: abi.Case, target: float, max_iters: int, mlp: abi.Mlp | None = None, apply_cfl: bool = False,
+                chunk: int = 25, warm: int = 20, fallback: float = 10.0) -> RunResult:
+    """Iterate until the L2 density residual falls by `target` (relative to iteration 1)."""
+    abi.case_track(case, True)
+    case.step_graph(1)
+    r0 = case.norm("L2_R_RHO")
+    it, best, fell = 1, 1.0, False
+    hist = [(1, 1.0)]
+    attached = False
+    saved = None
+    t0 = time.perf_counter()
+    while it < max_iters:
+        if mlp is not None and not attached and not fell and it >= warm:
+            abi.case_set_mlp(case, mlp, apply_cfl)
+            attached = True
+        if attached:
+            saved = (it, case.get("U"))  # restart point should the learned chunk fail
+        try:
+            case.step_graph(chunk)
+            it += chunk
+            r = case.norm("L2_R_RHO") / r0
+        except abi.CfdError:
+            if not attached:
+                raise
+            r = float("nan")
+        hist.append((it, r))
+        if attached and not (r <= fallback * best):
+            abi.case_set_mlp(case, None)  # the plain update from here on
+            attached, fell = False, True
+            if not r == r:  # non-finite state: restart the plain update from the saved one
+                it = saved[0]
+                case.put("U", saved[1])
+                continue
+        best = min(best, r) if r == r else best
+        if r <= target:
+            break
+    el = time.perf_counter() - t0
+    if attached:
+        abi.case_set_mlp(case, None)
+    return RunResult(bool(hist[-1][1] <= target), it, el, hist, fell)
