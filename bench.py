@@ -401,10 +401,26 @@ def run_ours(args):
         t = traffic_bytes(p, args.precision, nc)
         if t:
             rows[p]["traffic"] = t["bytes"]
+    # the sweeps are latency bound: time per dependency level against the measured
+    # floor of one hand-off through global memory (wait, compute, publish)
+    try:
+        floor = abi.hop_latency_us(300, 0, stream.cuda_stream)
+    except abi.CfdError:
+        floor = None
+    for p, lev in (("sweep_fwd", nlev[0]), ("sweep_bwd", nlev[1])):
+        if p in rows:
+            rows[p]["levels"] = lev
+            rows[p]["us_per_level"] = round(1e3 * per[p] / lev, 3)
+            rows[p]["floor_us_per_hop"] = round(floor, 3) if floor else None
     db = alg_bytes(dominant, nc, nf, viscous, args.precision)
     achieved = db / (per[dominant] * 1e-3) / 1e9
     tr = traffic_bytes(dominant, args.precision, nc)
-    roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+    latency = None
+    if dominant in ("sweep_fwd", "sweep_bwd"):
+        latency = {"levels": rows[dominant]["levels"], "us_per_level": rows[dominant]["us_per_level"],
+                   "floor_us_per_hop": rows[dominant]["floor_us_per_hop"],
+                   "note": "dependency-level latency bound: one level's cells wait for lower levels' increments"}
+    roofline = {"bound": "hbm", "kernel": dominant, "latency": latency, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": tr["bytes"] if tr else None, "traffic_source": tr, "alg_bytes_per_launch": db,
                 "per_pass": rows}

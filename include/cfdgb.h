@@ -73,6 +73,18 @@ extern "C" {
 #define CFD_FIELD_AREA    18  /* face length, 1/face (read only)                    */
 #define CFD_FIELD_ECENTER 19  /* face centre, 2/face (read only)                    */
 #define CFD_FIELD_WALLDIST 20 /* projected wall distance, 1/cell (read only)        */
+/* SST k-omega fields (after cfd_sst_enable); T and MUT are writable. */
+#define CFD_FIELD_SST_T     21 /* k, omega, 2/cell (turbulenceCellValue)           */
+#define CFD_FIELD_SST_TFACE 22 /* face k, omega, 2/face (turbulenceFaceValue)      */
+#define CFD_FIELD_SST_TGRAD 23 /* grad k, grad omega, 4/cell [kx, ky, wx, wy]      */
+#define CFD_FIELD_SST_F1    24 /* blending function F1, 1/cell                      */
+#define CFD_FIELD_SST_F2    25 /* blending function F2, 1/cell                      */
+#define CFD_FIELD_SST_MUT   26 /* eddy viscosity, 1/cell (vCellMut)                 */
+#define CFD_FIELD_SST_MUTF  27 /* face eddy viscosity, 1/face (vFaceMut)            */
+#define CFD_FIELD_SST_FCONV 28 /* convective face flux of k, omega, 2/face          */
+#define CFD_FIELD_SST_FVISC 29 /* viscous face flux of k, omega, 2/face             */
+#define CFD_FIELD_SST_R     30 /* residual of k, omega, 2/cell (CellTotalTFlux)     */
+#define CFD_FIELD_SST_DIAG  31 /* LU-SGS diagonal of k, omega, 2/cell (SolveDiag)   */
 
 /* Residual-norm selectors for cfd_residual_norm. */
 #define CFD_NORM_DW_RHO2   0  /* sum dW_rho^2 (LUSGSIntegrator::postprocessUpdate) */
@@ -191,6 +203,12 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
  * dataflow LU-SGS sweep waits on its neighbours.  Returns CFD_ERR_TIMEOUT when
  * the bounded wait gave up (the expected outcome) and leaves the case usable. */
 int cfd_selftest_bounded_wait(cfd_case_t c, long long polls);
+/* Measurement helper: the latency floor of the dataflow sweeps' hand-off.  A
+ * cooperative chain of `hops` one-warp blocks, each waiting (bounded) for the
+ * previous block's value in global memory, running fp64_ops dependent binary64
+ * FMAs on it and publishing its own; us_per_hop = best of 4 timed chains /
+ * (hops - 1).  2 <= hops <= 1024.  stream may be NULL. */
+int cfd_measure_hop_latency(void* stream, int hops, int fp64_ops, double* us_per_hop);
 
 /* ---- overset connectivity and fringe exchange (UniTioga MeshBlock) ------- */
 /* Layouts of a node array for the fringe update (dataUpdate.cpp:4-5). */
@@ -277,6 +295,23 @@ void cfd_holemap_free(cfd_holemap_t h);
 int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, const cfd_holemap_t* maps,
                       int nfringe, int* iblank, int* mandatory);
 
+/* ---- SST k-omega (SSTkomegaModel, UnstructSolver/SSTKWStrategy.h) -------- */
+/* The reference builds this model but never runs it (ViscousFlow2D's serial
+ * residual skips it and isLaminar() is true); these calls evaluate its
+ * functions on the device from the laminar residual's arrays.
+ * cfd_sst_enable: allocate the k-omega arrays of a laminar case (binary64
+ * residual: FP64 or MIXED) and set k, omega and mu_t to the freestream values
+ * (InitializeturbulenceVariable, :582-613).  cfd_sst_freestream: out3 = {k,
+ * omega, mu_t} of that freestream.  cfd_sst_residual: SolveTurbulenceEquation
+ * (:515-524) and SolveDiag (:170-192) from the current face states,
+ * gradients, viscosities, spectral radii and time steps (call cfd_residual and
+ * cfd_local_dt first).  cfd_sst_update_mut: the eddy viscosity update of
+ * UpdatePrimitiveVariables (:194-223) from W = rho (k, omega). */
+int cfd_sst_enable(cfd_case_t c);
+int cfd_sst_freestream(cfd_case_t c, int mesh, double* out3);
+int cfd_sst_residual(cfd_case_t c);
+int cfd_sst_update_mut(cfd_case_t c);
+
 /* ---- learned relaxation (no reference counterpart) ------------------------- */
 /* A 12-64-64-2 perceptron (relu, bf16 weights, fp32 arithmetic) that maps 12
  * features of a cell after its LU-SGS sweeps to o = (o0, o1): the cell's update
@@ -291,7 +326,8 @@ int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, c
  * 2 (dW.dW_prev)/|dW_prev|^2 clipped to [-4, 4], 3 cos(dW, dW_prev),
  * 4 log10(|R_rho| dt/(vol rho)), 5 log10(spec_v/spec_c + 1e-12), 6 Mach,
  * 7 min limiter, 8 log10(D dt/vol), 9 log10(wall distance/sqrt(vol) + 1e-6),
- * 10 rho - 1, 11 p - 1. */
+ * 10 rho - 1, 11 p - 1.  The learned update is three launches: the network per
+ * cell, the mean factor per mesh, and the bounded update. */
 #define CFD_MLP_INPUTS  12
 #define CFD_MLP_OUTPUTS 2
 #define CFD_MLP_PARAMS  5122
@@ -319,8 +355,10 @@ int cfd_case_track(cfd_case_t c, int on);
 /* Features of every cell (device x[12 * ncell_total]) from the last LU-SGS step. */
 int cfd_case_features(cfd_case_t c, float* d_x);
 /* Attach (m != NULL) or detach the learned relaxation; apply_cfl also applies
- * the CFL output.  Detaching restores the constant CFL and the unit update. */
-int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl);
+ * the CFL output.  spread >= 0 bounds each cell's factor to the mesh mean of
+ * the predicted factors +- spread (spread < 0: each cell uses its own).
+ * Detaching restores the constant CFL and the unit update. */
+int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl, double spread);
 
 /* Residual norm of a caller-owned device array that allocates nothing (no
  * counterpart in the reference, which has no device code).  For callers that

@@ -5,7 +5,7 @@ oracle/build_ref.sh into oracle/_ref/ref_driver) on small generated meshes and
 stores every dumped array in one .npz per case, next to the .grd mesh it used.
 The fixtures pin both the C restatement in oracle/ and the CUDA kernels.
 
-usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+usage: python tests/golden/make_golden.py [REFERENCE_ROOT [sst]]   ("sst": only the SST fixtures)
 """
 from __future__ import annotations
 
@@ -64,10 +64,53 @@ def centroids(m: meshgen.GrdMesh) -> np.ndarray:
     return acc / cnt[:, None]
 
 
-def main(ref_root: str = "/root/reference"):
+# SST k-omega phase: name -> (mesh, mach, aoa, re, seed).  The driver runs one
+# laminar residual from a perturbed state and then the reference's SST
+# functions on it, from per-cell multipliers of the freestream k, omega and mu_t.
+SST_CASES = {
+    "mixed_lam_sst": ("mixed", 0.4, 5.0, 1000.0, 9),
+    "omesh_lam_sst": ("omesh", 0.2, 0.0, 40.0, 10),
+}
+SST_FILES = ["sst_inf", "sst_T_in", "sst_mut_in", "sst_tface", "sst_tgrad", "sst_f1", "sst_f2", "sst_mutf",
+             "sst_fconv", "sst_fvisc", "sst_R", "sst_diag", "sst_T2", "sst_mut", "res0_U", "res0_Uedge",
+             "res0_grad", "res0_mu", "res0_muedge", "res0_specc", "res0_specv", "res0_dt", "geo_wall"]
+
+
+def sst_main(ms, drv):
+    for case, (mname, ma, aoa, re, seed) in SST_CASES.items():
+        m = ms[mname]
+        g = 1.4
+        a = 3.141593 * aoa / 180
+        fs = np.array([1.0, 1.0, ma * np.sqrt(g) * np.cos(a), ma * np.sqrt(g) * np.sin(a)])
+        U0 = meshgen.perturbed_state(m.ncell, centroids(m), fs, amp=0.05, seed=seed)
+        rng = np.random.default_rng(seed)
+        tm = np.exp(rng.uniform(-1.0, 1.0, 2 * m.ncell))
+        mm = np.exp(rng.uniform(-1.0, 2.0, m.ncell))
+        with tempfile.TemporaryDirectory() as td:
+            td = Path(td)
+            U0.astype(np.float64).tofile(td / "u0.bin")
+            tm.tofile(td / "t.bin")
+            mm.tofile(td / "m.bin")
+            env = dict(os.environ, SST_T=str(td / "t.bin"), SST_MUT=str(td / "m.bin"))
+            r = subprocess.run([str(drv), str(HERE / f"{mname}.grd"), str(m.wall_tag), str(m.far_tag), "viscous",
+                                "lusgs", repr(ma), repr(aoa), repr(re), "50.0", "0", str(td / "out"),
+                                str(td / "u0.bin"), "0"], capture_output=True, text=True, env=env)
+            if r.returncode != 0:
+                raise RuntimeError(f"{case}: reference driver failed\n{r.stdout}\n{r.stderr}")
+            arrs = {"init_U": U0}
+            for f in SST_FILES:
+                arrs[f] = np.fromfile(td / "out" / f"{f}.bin", np.float64)
+        np.savez_compressed(HERE / f"{case}.npz", **arrs)
+        print(case, m.ncell, "cells")
+
+
+def main(ref_root: str = "/root/reference", only: str = ""):
     drv = ROOT / "oracle" / "_ref" / "ref_driver"
     subprocess.run(["bash", str(ROOT / "oracle" / "build_ref.sh"), ref_root], check=True)
     ms = meshes()
+    if only == "sst":
+        sst_main(ms, drv)
+        return
     for name, m in ms.items():
         meshgen.write_grd(HERE / f"{name}.grd", m)
     manifest = {}
@@ -97,6 +140,7 @@ def main(ref_root: str = "/root/reference"):
                               ncell=int(m.ncell), nedge=int(m.nedge))
         print(case, m.ncell, "cells", json.loads(r.stdout.strip().splitlines()[-1]))
     (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1) + "\n")
+    sst_main(ms, drv)
 
 
 if __name__ == "__main__":

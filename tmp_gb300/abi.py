@@ -23,12 +23,16 @@ FLOW_EULER, FLOW_LAMINAR = 0, 1
 ADV_RK5, ADV_LUSGS = 0, 1
 PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
 FIELD = dict(U=0, W=1, R=2, GRAD=3, PHI=4, SPEC_C=5, SPEC_V=6, DT=7, DIAG=8, DW1=9, DW=10, GRADT=11, MU=12,
-             UEDGE=13, MUEDGE=14, VOL=15, CENTER=16, NORMAL=17, AREA=18, ECENTER=19, WALLDIST=20)
+             UEDGE=13, MUEDGE=14, VOL=15, CENTER=16, NORMAL=17, AREA=18, ECENTER=19, WALLDIST=20, SST_T=21,
+             SST_TFACE=22, SST_TGRAD=23, SST_F1=24, SST_F2=25, SST_MUT=26, SST_MUTF=27, SST_FCONV=28,
+             SST_FVISC=29, SST_R=30, SST_DIAG=31)
 # values per element and whether the field lives on faces
 FIELD_SHAPE = dict(U=(4, 0), W=(4, 0), R=(4, 0), GRAD=(8, 0), PHI=(4, 0), SPEC_C=(1, 0), SPEC_V=(1, 0),
                    DT=(1, 0), DIAG=(1, 0), DW1=(4, 0), DW=(4, 0), GRADT=(2, 0), MU=(1, 0), UEDGE=(4, 1),
                    MUEDGE=(1, 1), VOL=(1, 0), CENTER=(2, 0), NORMAL=(2, 1), AREA=(1, 1), ECENTER=(2, 1),
-                   WALLDIST=(1, 0))
+                   WALLDIST=(1, 0), SST_T=(2, 0), SST_TFACE=(2, 1), SST_TGRAD=(4, 0), SST_F1=(1, 0), SST_F2=(1, 0),
+                   SST_MUT=(1, 0), SST_MUTF=(1, 1), SST_FCONV=(2, 1), SST_FVISC=(2, 1), SST_R=(2, 0),
+                   SST_DIAG=(2, 0))
 NORM = dict(DW_RHO2=0, RK_DRHO=1, L2_R_RHO=2)
 LAYOUT_ROW, LAYOUT_COLUMN = 0, 1
 MLP_INPUTS, MLP_OUTPUTS, MLP_PARAMS = 12, 2, 5122
@@ -121,7 +125,12 @@ def lib() -> C.CDLL:
         "cfd_mlp_train": (C.c_int, [vp, vp, vp, vp, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong, fp]),
         "cfd_case_track": (C.c_int, [vp, C.c_int]),
         "cfd_case_features": (C.c_int, [vp, vp]),
-        "cfd_case_set_mlp": (C.c_int, [vp, vp, C.c_int]),
+        "cfd_case_set_mlp": (C.c_int, [vp, vp, C.c_int, C.c_double]),
+        "cfd_measure_hop_latency": (C.c_int, [vp, C.c_int, C.c_int, dp]),
+        "cfd_sst_enable": (C.c_int, [vp]),
+        "cfd_sst_freestream": (C.c_int, [vp, C.c_int, dp]),
+        "cfd_sst_residual": (C.c_int, [vp]),
+        "cfd_sst_update_mut": (C.c_int, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -507,5 +516,30 @@ def case_features(case: "Case", x_ptr: int):
     check(lib().cfd_case_features(case.h, C.c_void_p(x_ptr)))
 
 
-def case_set_mlp(case: "Case", mlp: Mlp | None, apply_cfl: bool = False):
-    check(lib().cfd_case_set_mlp(case.h, mlp.h if mlp is not None else None, int(apply_cfl)))
+def case_set_mlp(case: "Case", mlp: Mlp | None, apply_cfl: bool = False, spread: float = 0.1):
+    check(lib().cfd_case_set_mlp(case.h, mlp.h if mlp is not None else None, int(apply_cfl), float(spread)))
+
+
+# ---- SST k-omega ----------------------------------------------------------------
+
+def sst_enable(case: "Case") -> np.ndarray:
+    """Allocate the k-omega arrays; returns the freestream (k, omega, mu_t) of mesh 0."""
+    check(lib().cfd_sst_enable(case.h))
+    out = np.zeros(3)
+    check(lib().cfd_sst_freestream(case.h, 0, _dptr(out)))
+    return out
+
+
+def sst_residual(case: "Case"):
+    check(lib().cfd_sst_residual(case.h))
+
+
+def sst_update_mut(case: "Case"):
+    check(lib().cfd_sst_update_mut(case.h))
+
+
+def hop_latency_us(hops: int = 300, fp64_ops: int = 0, stream: int | None = None) -> float:
+    """Latency floor of one dataflow hand-off (wait, compute, publish), in microseconds."""
+    v = C.c_double()
+    check(lib().cfd_measure_hop_latency(C.c_void_p(stream) if stream else None, int(hops), int(fp64_ops), C.byref(v)))
+    return v.value

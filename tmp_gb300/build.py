@@ -33,6 +33,7 @@ UNITS = [
     ("k_misc.cu", []),
     ("k_overset.cu", ["-fmad=false"]),
     ("k_mlp.cu", []),
+    ("k_sst.cu", ["-fmad=false"]),
     ("k_noalloc.cu", []),
 ]
 

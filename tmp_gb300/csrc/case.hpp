@@ -52,7 +52,21 @@ struct DevArrays {
     d4* dW1 = nullptr;
     d4* dW = nullptr;
     d4* dWprev = nullptr;        // [nc] previous LU-SGS increment (kept while tracking / learned)
+    // SST k-omega (k_sst.cu), allocated by cfd_sst_enable
+    double* sstT = nullptr;      // [2*nc] k, omega
+    double* sstTf = nullptr;     // [2*nf] face k, omega
+    double* sstG = nullptr;      // [4*nc] grad k, grad omega
+    double* sstF1 = nullptr;     // [nc]
+    double* sstF2 = nullptr;     // [nc]
+    double* sstMut = nullptr;    // [nc] eddy viscosity
+    double* sstMutf = nullptr;   // [nf]
+    double* sstFc = nullptr;     // [2*nf] convective face flux
+    double* sstFv = nullptr;     // [2*nf] viscous face flux
+    double* sstR = nullptr;      // [2*nc] residual
+    double* sstD = nullptr;      // [2*nc] LU-SGS diagonal
     float* omega = nullptr;      // [nc] relaxation of the last learned update
+    float* omega_mean = nullptr; // [nmesh] its mean per mesh
+    int* mesh_coff = nullptr;    // [nmesh+1] first cell of each mesh
     // residual intermediates, binary64 form
     d4* grad = nullptr;          // [2*nc]
     d4* phi = nullptr;
@@ -128,6 +142,9 @@ void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, in
 void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, bool fp32);
 void launch_wall_distance(const DevArrays& d, const LaunchCfg& L);
 void launch_wall_force(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32);
+// ---- k_sst.cu (compiled with -fmad=false) ----
+void launch_sst_residual(const DevArrays& d, const LaunchCfg& L);
+void launch_sst_update_mut(const DevArrays& d, const LaunchCfg& L);
 // ---- k_fp32.cu ----
 void launch_residual_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);

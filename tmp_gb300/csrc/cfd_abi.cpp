@@ -95,6 +95,9 @@ struct cfd_case_s {
     bool track = false;              // keep the previous LU-SGS increment (learning features)
     struct cfd_mlp_s* mlp = nullptr;  // learned relaxation, or null for the plain update
     bool mlp_cfl = false;            // apply the network's CFL multipliers too
+    float mlp_spread = 0.1f;         // bound on |omega - mesh mean| (negative: none)
+    std::vector<cfd_freestream_t> fs_in;  // the freestreams the case was created with
+    bool sst = false;                // SST k-omega arrays allocated
     bool viscous() const { return p.flow == CFD_FLOW_LAMINAR; }
     bool fp32() const { return p.precision == CFD_PREC_FP32; }
     bool mixed() const { return p.precision == CFD_PREC_MIXED; }
@@ -118,7 +121,8 @@ void free_case(cfd_case_s* c) {
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
                     d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.wall_ptr, d.wall_faces, d.wblocks, d.wpartial, d.wforce, d.swfcf, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
-                    d.norm_out, d.err, d.dWprev, d.omega};
+                    d.norm_out, d.err, d.dWprev, d.omega, d.omega_mean, d.mesh_coff, d.sstT, d.sstTf, d.sstG, d.sstF1, d.sstF2,
+                    d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -336,6 +340,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             nf += m.nedge;
             nn += m.nnode;
             c->prm.push_back(make_prm(fs[i], visc));
+            c->fs_in.push_back(fs[i]);
         }
         if (nc >= (1LL << 31) - 1 || nf >= (1LL << 31) - 1) throw std::runtime_error("case too large for 32-bit indices");
         c->coff[nmesh] = (int)nc;
@@ -793,6 +798,17 @@ FieldRef field_ref(cfd_case_s* c, int which) {
         case CFD_FIELD_MU: return {f ? nullptr : d.mu, f ? d.muf : nullptr, 1, false, false};
         case CFD_FIELD_UEDGE: return {f ? nullptr : d.Ue, f ? d.Uef : nullptr, 4, true, false};
         case CFD_FIELD_MUEDGE: return {f ? nullptr : d.mue, f ? d.muef : nullptr, 1, true, false};
+        case CFD_FIELD_SST_T: return {d.sstT, nullptr, 2, false, true};
+        case CFD_FIELD_SST_TFACE: return {d.sstTf, nullptr, 2, true, false};
+        case CFD_FIELD_SST_TGRAD: return {d.sstG, nullptr, 4, false, false};
+        case CFD_FIELD_SST_F1: return {d.sstF1, nullptr, 1, false, false};
+        case CFD_FIELD_SST_F2: return {d.sstF2, nullptr, 1, false, false};
+        case CFD_FIELD_SST_MUT: return {d.sstMut, nullptr, 1, false, true};
+        case CFD_FIELD_SST_MUTF: return {d.sstMutf, nullptr, 1, true, false};
+        case CFD_FIELD_SST_FCONV: return {d.sstFc, nullptr, 2, true, false};
+        case CFD_FIELD_SST_FVISC: return {d.sstFv, nullptr, 2, true, false};
+        case CFD_FIELD_SST_R: return {d.sstR, nullptr, 2, false, false};
+        case CFD_FIELD_SST_DIAG: return {d.sstD, nullptr, 2, false, false};
         default: return {nullptr, nullptr, 0, false, false};
     }
 }
@@ -862,7 +878,18 @@ int cfd_get_field(cfd_case_t c, int mesh, int which, double* host) {
 int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host) {
     if (!c || !host) return fail(CFD_ERR_ARG, "null argument");
     if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
-    if (which != CFD_FIELD_U) return fail(CFD_ERR_ARG, "only the primitive field U can be written");
+    if (which == CFD_FIELD_SST_T || which == CFD_FIELD_SST_MUT) {
+        if (!c->sst) return fail(CFD_ERR_STATE, "call cfd_sst_enable first");
+        ABI_TRY
+        int off = c->coff[mesh], n = c->coff[mesh + 1] - off;
+        const int w = which == CFD_FIELD_SST_T ? 2 : 1;
+        double* dst = which == CFD_FIELD_SST_T ? c->d.sstT : c->d.sstMut;
+        ck(cudaMemcpyAsync(dst + (size_t)off * w, host, (size_t)n * w * 8, cudaMemcpyHostToDevice, c->stream), "upload");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+        return CFD_OK;
+        ABI_CATCH
+    }
+    if (which != CFD_FIELD_U) return fail(CFD_ERR_ARG, "writable fields: U, SST_T, SST_MUT");
     ABI_TRY
     int off = c->coff[mesh], n = c->coff[mesh + 1] - off;
     ck(cudaMemcpyAsync(c->d.U + off, host, (size_t)n * 32, cudaMemcpyHostToDevice, c->stream), "upload");
@@ -891,7 +918,9 @@ struct cfd_mlp_s {
 };
 
 namespace {
-void learned_update(cfd_case_s* c) { launch_learned_update(c->d, c->L(), c->mlp->net, c->mlp_cfl, c->fp32()); }
+void learned_update(cfd_case_s* c) {
+    launch_learned_update(c->d, c->L(), c->mlp->net, c->mlp_cfl, c->mlp_spread, c->d.mesh_coff, c->fp32());
+}
 }  // namespace
 
 namespace {
@@ -1024,6 +1053,10 @@ int cfd_case_track(cfd_case_t c, int on) {
     if (!d.dWprev) {
         dalloc(&d.dWprev, d.nc);
         dalloc(&d.omega, d.nc);
+        dalloc(&d.omega_mean, c->nmesh);
+        dalloc(&d.mesh_coff, c->nmesh + 1);
+        ck(cudaMemcpyAsync(d.mesh_coff, c->coff.data(), (c->nmesh + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+           "upload");
         ck(cudaMemsetAsync(d.dWprev, 0, sizeof(d4) * d.nc, c->stream), "memset");
         ck(cudaMemsetAsync(d.dW, 0, sizeof(d4) * d.nc, c->stream), "memset");
         std::vector<float> one(d.nc, 1.0f);
@@ -1046,7 +1079,7 @@ int cfd_case_features(cfd_case_t c, float* d_x) {
     ABI_CATCH
 }
 
-int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl) {
+int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl, double spread) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
     if (c->p.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_STATE, "the learned relaxation needs the LU-SGS integrator");
     ABI_TRY
@@ -1067,7 +1100,93 @@ int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl) {
     c->drop_graph();
     c->mlp = m;
     c->mlp_cfl = apply_cfl != 0;
+    c->mlp_spread = (float)spread;
     return CFD_OK;
+    ABI_CATCH
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// SST k-omega (k_sst.cu)
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+int cfd_sst_enable(cfd_case_t c) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (!c->viscous() || c->fp32())
+        return fail(CFD_ERR_STATE, "the SST model needs a laminar case with the binary64 residual (FP64 or MIXED)");
+    ABI_TRY
+    DevArrays& d = c->d;
+    if (!c->sst) {
+        const size_t nc = d.nc, nf = d.nf;
+        dalloc(&d.sstT, 2 * nc); dalloc(&d.sstTf, 2 * nf); dalloc(&d.sstG, 4 * nc);
+        dalloc(&d.sstF1, nc); dalloc(&d.sstF2, nc); dalloc(&d.sstMut, nc); dalloc(&d.sstMutf, nf);
+        dalloc(&d.sstFc, 2 * nf); dalloc(&d.sstFv, 2 * nf); dalloc(&d.sstR, 2 * nc); dalloc(&d.sstD, 2 * nc);
+        c->sst = true;
+    }
+    // Freestream k, omega and mu_t: TopologyHolderStrategy::set_fs_variable2
+    // (.cpp:325-352) then SSTkomegaModel::InitializeturbulenceVariable
+    // (SSTKWStrategy.h:582-613), with Gamma = 1.4, R = 287, L = 1.
+    for (int m = 0; m < c->nmesh; m++) {
+        const cfd_freestream_t& fs = c->fs_in[m];
+        const double Gamma = 1.4, R = 287.0, L = 1.0;
+        const double fs_soundSpeed = sqrt(Gamma * fs.pressure / fs.density);
+        const double fs_Temperature = fs.pressure / (R * fs.density);
+        const double fs_mu = 1.458e-6 * pow(fs_Temperature, 1.5) / (fs_Temperature + 110.5);
+        const double fs_mut = fs_mu * 0.035;
+        const double fsnd_mut = fs_mut / fs_mu * sqrt(Gamma) * fs.mach / fs.reynolds;
+        const double k = 1.5 * fs.mach * fs_soundSpeed * 0.01 * fs.mach * fs_soundSpeed * 0.01;
+        const double w = fs.density * k / (0.035 * fs_mu);
+        c->prm[m].sst_k = Gamma * k / (fs_soundSpeed * fs_soundSpeed);
+        c->prm[m].sst_w = sqrt(Gamma) * L * w / fs_soundSpeed;
+        c->prm[m].sst_mut = fsnd_mut;
+    }
+    ck(cudaMemcpyAsync(d.prm, c->prm.data(), c->nmesh * sizeof(MeshPrm), cudaMemcpyHostToDevice, c->stream), "upload");
+    // uniform freestream turbulence and eddy viscosity
+    std::vector<double> t(2 * (size_t)d.nc), mut((size_t)d.nc);
+    for (int m = 0; m < c->nmesh; m++)
+        for (int k = c->coff[m]; k < c->coff[m + 1]; k++) {
+            t[2 * (size_t)k] = c->prm[m].sst_k;
+            t[2 * (size_t)k + 1] = c->prm[m].sst_w;
+            mut[k] = c->prm[m].sst_mut;
+        }
+    ck(cudaMemcpyAsync(d.sstT, t.data(), t.size() * 8, cudaMemcpyHostToDevice, c->stream), "upload");
+    ck(cudaMemcpyAsync(d.sstMut, mut.data(), mut.size() * 8, cudaMemcpyHostToDevice, c->stream), "upload");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    c->drop_graph();
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_sst_freestream(cfd_case_t c, int mesh, double* out3) {
+    if (!c || !out3) return fail(CFD_ERR_ARG, "null argument");
+    if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
+    if (!c->sst) return fail(CFD_ERR_STATE, "call cfd_sst_enable first");
+    out3[0] = c->prm[mesh].sst_k;
+    out3[1] = c->prm[mesh].sst_w;
+    out3[2] = c->prm[mesh].sst_mut;
+    return CFD_OK;
+}
+
+int cfd_sst_residual(cfd_case_t c) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (!c->sst) return fail(CFD_ERR_STATE, "call cfd_sst_enable first");
+    ABI_TRY
+    launch_sst_residual(c->d, c->L());
+    ck(cudaGetLastError(), "SST residual");
+    return check_errors(c);
+    ABI_CATCH
+}
+
+int cfd_sst_update_mut(cfd_case_t c) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (!c->sst) return fail(CFD_ERR_STATE, "call cfd_sst_enable first");
+    ABI_TRY
+    launch_sst_update_mut(c->d, c->L());
+    ck(cudaGetLastError(), "SST eddy viscosity");
+    return check_errors(c);
     ABI_CATCH
 }
 

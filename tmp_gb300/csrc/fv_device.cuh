@@ -44,6 +44,7 @@ struct MeshPrm {
     double sqrt_gamma;                           // sqrtf64(Gamma)
     int viscous;
     int pad;
+    double sst_k, sst_w, sst_mut;                // SST freestream k, omega, mu_t (nondimensional)
 };
 
 template <class T> struct C {

@@ -4,6 +4,7 @@
 // (one block each, fixed tree order) writes one partial per chunk, a second pass
 // adds each mesh's partials in chunk order.  The same inputs give the same bits
 // on every run.
+#include "../../include/cfdgb.h"
 #include "case.hpp"
 #include "fv_kernels.cuh"
 
@@ -85,3 +86,97 @@ void launch_norm(const DevArrays& d, const LaunchCfg& L, int which) {
 }
 
 }  // namespace cfdgb
+
+// ---------------------------------------------------------------------------
+// Hand-off latency floor of the dataflow sweeps (measurement helper)
+// ---------------------------------------------------------------------------
+namespace cfdgb {
+namespace {
+
+constexpr unsigned long long kHopSentinel = 0x7ff4c0ffee5eed11ULL;  // a signalling NaN nothing computes
+
+__global__ void k_hop_reset(double2* data, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) data[i] = make_double2(__longlong_as_double((long long)kHopSentinel), 0.0);
+}
+
+// Block k waits (bounded) until block k-1 has published its value, runs
+// `ops` dependent binary64 multiply-adds on it and publishes its own: the
+// shortest possible chain of the sweeps' wait / compute / publish pattern.
+__global__ void k_hop_chain(double2* data, int n, int ops, unsigned* err) {
+    const int k = blockIdx.x;
+    double v = 1.0;
+    if (k > 0) {
+        const double2* q = data + (k - 1);
+        double2 a = __ldcv(q);
+        long long it = 0;
+        while ((unsigned long long)__double_as_longlong(a.x) == kHopSentinel) {
+            if (++it > (1LL << 22)) {
+                atomicOr(err, 1u);
+                return;
+            }
+            a = __ldcv(q);
+        }
+        v = a.x;
+    }
+#pragma unroll 1
+    for (int i = 0; i < ops; i++) v = fma(v, 0.999999, 1e-9);
+    if (threadIdx.x == 0) __stcg(data + k, make_double2(v, (double)k));
+}
+
+}  // namespace
+}  // namespace cfdgb
+
+extern "C" int cfd_measure_hop_latency(void* stream, int hops, int fp64_ops, double* us_per_hop) {
+    using namespace cfdgb;
+    if (hops < 2 || hops > 1024 || fp64_ops < 0 || !us_per_hop)
+        return set_last_error(CFD_ERR_ARG, "cfd_measure_hop_latency: 2 <= hops <= 1024 and fp64_ops >= 0");
+    cudaStream_t s = (cudaStream_t)stream;
+    double2* data = nullptr;
+    unsigned* err = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = CFD_OK;
+    auto fail_cuda = [&](cudaError_t e) { rc = set_last_error(CFD_ERR_CUDA, cudaGetErrorString(e)); };
+    cudaError_t e;
+    if ((e = cudaMalloc(&data, hops * sizeof(double2))) || (e = cudaMalloc(&err, sizeof(unsigned))) ||
+        (e = cudaEventCreate(&e0)) || (e = cudaEventCreate(&e1))) {
+        fail_cuda(e);
+    } else {
+        // all blocks must be resident at once: a cooperative launch guarantees it or fails
+        int nb_sm = 0, dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, k_hop_chain, 32, 0);
+        if ((long long)nb_sm * nsm < hops) {
+            rc = set_last_error(CFD_ERR_ARG, "cfd_measure_hop_latency: more hops than co-resident blocks");
+        } else {
+            double best = 1e300;
+            cudaMemsetAsync(err, 0, sizeof(unsigned), s);
+            for (int rep = 0; rep < 5 && rc == CFD_OK; rep++) {
+                k_hop_reset<<<(hops + 255) / 256, 256, 0, s>>>(data, hops);
+                int n = hops, ops = fp64_ops;
+                void* args[] = {&data, &n, &ops, &err};
+                cudaEventRecord(e0, s);
+                e = cudaLaunchCooperativeKernel((const void*)k_hop_chain, dim3(hops), dim3(32), args, 0, s);
+                cudaEventRecord(e1, s);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                if (e != cudaSuccess) {
+                    fail_cuda(e);
+                    break;
+                }
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0 && ms < best) best = ms;  // the first launch is a warm-up
+            }
+            unsigned h = 0;
+            if (rc == CFD_OK) cudaMemcpy(&h, err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+            if (h) rc = set_last_error(CFD_ERR_TIMEOUT, "cfd_measure_hop_latency: a bounded wait gave up");
+            if (rc == CFD_OK) *us_per_hop = best * 1e3 / (hops - 1);
+        }
+    }
+    if (data) cudaFree(data);
+    if (err) cudaFree(err);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return rc;
+}

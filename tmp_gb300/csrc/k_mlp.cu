@@ -282,12 +282,16 @@ __global__ void k_case_features(DevArrays d, float* __restrict__ X) {
     for (int k = 0; k < NI; k++) X[(long long)c * NI + k] = f[k];
 }
 
-// Fused learned update: features -> network -> W += omega * dW, U = prim(W),
-// next step's CFL multiplier.  apply_cfl = 0 leaves the multipliers at 1.
-__global__ void __launch_bounds__(128) k_learned_update(DevArrays d, const __nv_bfloat16* __restrict__ wq,
-                                                        const float* __restrict__ p,
-                                                        const float* __restrict__ norm, int apply_cfl,
-                                                        float4* __restrict__ Uf) {
+// Learned update, three launches: (1) features -> network -> the cell's
+// relaxation factor omega = 1 + 2 sigmoid(o0) and next CFL multiplier;
+// (2) the mean factor of each mesh (one block per mesh, fixed order);
+// (3) omega' = mean + clamp(omega - mean, -spread, spread) (spread < 0: omega
+// itself), W += omega' dW, U = prim(W).  A spread bounds how far neighbouring
+// cells' factors differ: unbounded per-cell factors were measured to stall the
+// iteration where factors of 1.0 and 1.6 meet.
+__global__ void __launch_bounds__(128) k_learned_eval(DevArrays d, const __nv_bfloat16* __restrict__ wq,
+                                                      const float* __restrict__ p, const float* __restrict__ norm,
+                                                      int apply_cfl) {
     __shared__ SmemNet s;
     load_net(s, wq, p, norm);
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -295,7 +299,35 @@ __global__ void __launch_bounds__(128) k_learned_update(DevArrays d, const __nv_
     float x[NI], xh[NI], h1[NH], o[NO];
     cell_features(d, c, x);
     net_forward(s, x, xh, h1, nullptr, o);
-    const double omega = 1.0 + 2.0 / (1.0 + exp(-(double)o[0]));
+    d.omega[c] = 1.f + 2.f / (1.f + expf(-o[0]));
+    if (d.cflmul) d.cflmul[c] = apply_cfl ? exp2f(2.f * tanhf(o[1])) : 1.f;
+}
+
+__global__ void k_omega_mean(const int* __restrict__ mesh_off, const float* __restrict__ omega,
+                             float* __restrict__ mean) {
+    __shared__ double sh[256];
+    const int m = blockIdx.x;
+    const int b = mesh_off[m], e = mesh_off[m + 1];
+    double a = 0.0;
+    for (int i = b + threadIdx.x; i < e; i += blockDim.x) a += omega[i];
+    sh[threadIdx.x] = a;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) mean[m] = e > b ? (float)(sh[0] / (e - b)) : 1.f;
+}
+
+__global__ void k_learned_apply(DevArrays d, const float* __restrict__ mean, float spread, float4* __restrict__ Uf) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nc) return;
+    float om = d.omega[c];
+    if (spread >= 0.f) {
+        const float mu = mean[d.cmesh[c]];
+        om = mu + fminf(fmaxf(om - mu, -spread), spread);
+    }
+    const double omega = om;
     const d4 dw = d.dW[c];
     double w[4] = {d.W[c].x + omega * dw.x, d.W[c].y + omega * dw.y, d.W[c].z + omega * dw.z,
                    d.W[c].w + omega * dw.w};
@@ -304,8 +336,6 @@ __global__ void __launch_bounds__(128) k_learned_update(DevArrays d, const __nv_
     d.W[c] = d4{w[0], w[1], w[2], w[3]};
     d.U[c] = d4{u[0], u[1], u[2], u[3]};
     if (Uf) Uf[c] = make_float4((float)u[0], (float)u[1], (float)u[2], (float)u[3]);
-    if (d.cflmul) d.cflmul[c] = apply_cfl ? exp2f(2.f * tanhf(o[1])) : 1.f;
-    if (d.omega) d.omega[c] = (float)omega;
     if (!(u[0] > 0.0) || !(u[1] > 0.0)) atomicOr(d.err, ERR_NONPHYS);
 }
 
@@ -364,11 +394,12 @@ void launch_case_features(const DevArrays& d, const LaunchCfg& L, float* X) {
     *L.counter += 1;
 }
 
-void launch_learned_update(const DevArrays& d, const LaunchCfg& L, const MlpNet& net, bool apply_cfl,
-                           bool fp32_copy) {
-    k_learned_update<<<nb(d.nc, 128), 128, 0, L.stream>>>(d, net.wq, net.p, net.norm, apply_cfl ? 1 : 0,
-                                                          fp32_copy ? d.Uf : nullptr);
-    *L.counter += 1;
+void launch_learned_update(const DevArrays& d, const LaunchCfg& L, const MlpNet& net, bool apply_cfl, float spread,
+                           const int* mesh_off, bool fp32_copy) {
+    k_learned_eval<<<nb(d.nc, 128), 128, 0, L.stream>>>(d, net.wq, net.p, net.norm, apply_cfl ? 1 : 0);
+    k_omega_mean<<<d.nmesh, 256, 0, L.stream>>>(mesh_off, d.omega, d.omega_mean);
+    k_learned_apply<<<nb(d.nc, 256), 256, 0, L.stream>>>(d, d.omega_mean, spread, fp32_copy ? d.Uf : nullptr);
+    *L.counter += 3;
 }
 
 cudaError_t mlp_forward(const MlpNet& net, const float* X, long long n, float* Y, cudaStream_t s) {

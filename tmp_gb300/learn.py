@@ -4,15 +4,18 @@ case with the network and falls back to the plain update.
 
 Data.  A case is advanced with the plain LU-SGS update while the library
 keeps each step's previous increment.  At snapshot iterations n the 12
-features of every cell are taken (cfd_case_features); the solver then runs K
-more plain steps.  With a = dW_n and s = dW_n + ... + dW_{n+K-1} (each scaled
-per equation as the features are), the cell's relaxation target is the
-extrapolation factor omega* = clip((s.a)/(a.a), 1, 3): in a cell whose
-increments keep their direction, a step of omega* * dW_n covers what the next
-steps would add.  The CFL target is the switched-evolution factor of the
-cell's own residual over the window, m* = clip((|R_{n+K}| / |R_n|)^(-1/2),
-1/4, 4).  Targets are stored as the network's raw outputs (inverse of
-omega = 1 + 2 sigmoid(o0), cflmul = 2^(2 tanh(o1))).
+features of every cell are taken (cfd_case_features); then, from the saved
+state, the solver runs K steps once per candidate relaxation factor applied
+to every cell (1.0, 1.2, 1.4, 1.6: the range in which a uniform factor stays
+stable on these cases), and the target of every cell is the candidate after
+which the case's L2 density residual is smallest (per-cell outcomes proved
+too noisy: half the cells pointed at 1.0, half at 1.6, and a network fitted
+to them mixed neighbouring factors into an unstable field).  The run then continues from the saved
+state with the plain update.  Targets are stored as the network's raw
+outputs (the inverse of omega = 1 + 2 sigmoid(o0)); the CFL output is trained
+towards a multiplier of 1, since on these viscous cases the time step barely
+moves the LU-SGS diagonal (measured: CFL x0.5 and x2 change the iteration
+count by under 5%).
 
 Run.  run_to_drop() attaches the network after a few plain steps and watches
 the L2 density residual every `chunk` steps; if it rises above `fallback`
@@ -72,17 +75,29 @@ def sweep_specs(n: int, seed: int = 0) -> list[CaseSpec]:
     return out
 
 
-def _ref_scale(U: np.ndarray, W: np.ndarray) -> np.ndarray:
-    rho, p, u, v = U.T
-    c = np.sqrt(np.maximum(1.4 * p / rho, 1e-30))
-    vm = np.hypot(u, v)
-    return np.stack([rho, np.maximum(np.abs(W[:, 1]), 1e-30), rho * (vm + c), rho * (vm + c)], 1)
+def constant_net(omega: float) -> abi.Mlp:
+    """A network whose output is the same relaxation factor in every cell."""
+    m = abi.Mlp(0)
+    p, norm = m.params()
+    p[:] = 0
+    q = (omega - 1.0) / 2.0
+    p[-2] = np.log(q / (1.0 - q))
+    m.set_params(p, norm)
+    return m
 
 
-def generate(specs, snapshots=(30, 60, 120, 240, 480, 960), K: int = 8, precision: int = abi.PREC_FP64):
-    """(X, T, M) numpy arrays: features, raw-output targets and weights."""
+def generate(specs, snapshots=(40, 80, 160, 320, 640, 1000), K: int = 30,
+             candidates=(1.0, 1.1, 1.2, 1.3, 1.4, 1.5, 1.6),
+             precision: int = abi.PREC_FP64):
+    """(X, T, M) numpy arrays: features, raw-output targets and weights.
+
+    At every snapshot the state is saved and advanced K steps once per
+    candidate relaxation factor (applied uniformly); every cell's target is
+    the candidate after which the case's L2 density residual is smallest.
+    The CFL output is trained towards 1 (raw 0)."""
     import torch
 
+    nets = {om: constant_net(om) for om in candidates if om != 1.0}
     Xs, Ts, Ms = [], [], []
     for spec in specs:
         mesh = spec.mesh()
@@ -94,30 +109,29 @@ def generate(specs, snapshots=(30, 60, 120, 240, 480, 960), K: int = 8, precisio
         for n in snapshots:
             if n > it:
                 case.step_graph(n - it)
+            it = n
             case.sync()
             abi.case_features(case, feat.data_ptr())
             case.sync()
             X = feat.view(nc, abi.MLP_INPUTS).cpu().numpy().copy()
-            U, W = case.get("U"), case.get("W")
-            a = case.get("DW")
-            r0 = np.abs(case.get("R")[:, 0])
-            s = a.copy()
-            for _ in range(K - 1):
-                case.step_graph(1)
-                s += case.get("DW")
-            r1 = np.abs(case.get("R")[:, 0])
-            it = n + K
-            ref = _ref_scale(U, W)
-            an, sn = a / ref, s / ref
-            aa = (an * an).sum(1)
-            om = np.clip((sn * an).sum(1) / np.maximum(aa, 1e-300), 1.0, 3.0)
-            q = np.clip((om - 1.0) / 2.0, 1e-3, 1 - 1e-3)
+            U = case.get("U")
+            score = np.empty(len(candidates))
+            for j, om in enumerate(candidates):
+                case.put("U", U)
+                abi.case_set_mlp(case, nets.get(om))
+                case.step(K)
+                try:
+                    score[j] = case.norm("L2_R_RHO")
+                except abi.CfdError:
+                    score[j] = np.inf
+            abi.case_set_mlp(case, None)
+            case.put("U", U)
+            best = np.full(nc, candidates[int(np.argmin(score))])
+            q = np.clip((best - 1.0) / 2.0, 1e-3, 1 - 1e-3)
             t0 = np.log(q / (1 - q))
-            mstar = np.clip(np.sqrt(np.maximum(r0, 1e-300) / np.maximum(r1, 1e-300)), 0.25, 4.0)
-            t1 = np.arctanh(np.clip(np.log2(mstar) / 2.0, -0.96, 0.96))
-            ok = np.isfinite(X).all(1) & (aa > 1e-28) & np.isfinite(t0) & np.isfinite(t1)
+            ok = np.isfinite(X).all(1)
             Xs.append(X[ok])
-            Ts.append(np.stack([t0, t1], 1)[ok].astype(np.float32))
+            Ts.append(np.stack([t0, np.zeros_like(t0)], 1)[ok].astype(np.float32))
             Ms.append(np.ones((ok.sum(), 2), np.float32))
         case.close()
     return np.concatenate(Xs), np.concatenate(Ts), np.concatenate(Ms)
@@ -150,7 +164,7 @@ class RunResult:
 
 
 def run_to_drop(case: abi.Case, target: float, max_iters: int, mlp: abi.Mlp | None = None, apply_cfl: bool = False,
-                chunk: int = 25, warm: int = 20, fallback: float = 10.0) -> RunResult:
+                chunk: int = 25, warm: int = 20, fallback: float = 10.0, spread: float = 0.1) -> RunResult:
     """Iterate until the L2 density residual falls by `target` (relative to iteration 1)."""
     abi.case_track(case, True)
     case.step_graph(1)
@@ -162,7 +176,7 @@ def run_to_drop(case: abi.Case, target: float, max_iters: int, mlp: abi.Mlp | No
     t0 = time.perf_counter()
     while it < max_iters:
         if mlp is not None and not attached and not fell and it >= warm:
-            abi.case_set_mlp(case, mlp, apply_cfl)
+            abi.case_set_mlp(case, mlp, apply_cfl, spread)
             attached = True
         if attached:
             saved = (it, case.get("U"))  # restart point should the learned chunk fail
