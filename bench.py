@@ -13,7 +13,8 @@ Precision forms: fp64 = the plain path (every kernel in binary64, results
 equal to the reference's); fp32 = fluxes, gradients, limiter and the LU-SGS
 sweep in binary32 with the update, norms and diagonal in binary64; mixed =
 binary64 residual with the binary32 sweep (defect correction; converges to
-the binary64 solution).  `value` is the --precision form; "forms" adds the
+the binary64 solution in the same number of iterations as fp64; the default).
+`value` is the --precision form; "forms" adds the
 other two measured the same way in the same run, and "time_to_drop" the wall
 time each form takes from the freestream start to a --drop fall of the L2
 density residual (normalised by iteration 1), capped at --drop-seconds.
@@ -54,15 +55,18 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "fp32", "mixed"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--sweep-mode", type=int, default=0, help="LU-SGS schedule (0 dataflow, 1/2 per level)")
     ap.add_argument("--sweep-bpsm", type=int, default=0, help="dataflow sweep blocks per SM (0 = default)")
     ap.add_argument("--forms", default="fp64,fp32,mixed", help="precision forms timed besides --precision ('' = none)")
-    ap.add_argument("--drop", type=float, default=1e-2, help="residual fall for time_to_drop (0 = skip)")
-    ap.add_argument("--drop-seconds", type=float, default=30.0, help="cap per form for time_to_drop")
+    ap.add_argument("--drop", type=float, default=1e-3, help="residual fall for time_to_drop (0 = skip)")
+    ap.add_argument("--drop-seconds", type=float, default=40.0, help="cap per form for time_to_drop")
+    ap.add_argument("--drop-forms", default="fp64,fp32,mixed,mixed+learned,fp32>mixed+learned",
+                    help="forms for time_to_drop: PREC[>PREC2][+learned]; '>' switches at --switch-at")
+    ap.add_argument("--switch-at", type=float, default=1e-3, help="residual fall at which 'A>B' switches form")
     return ap.parse_args()
 
 
@@ -359,25 +363,28 @@ def run_ours(args):
         c2.close()
     forms[args.precision] = {"ms_per_step": 1e3 * t_local / args.steps, "value": nc * args.steps / t_local}
 
-    # wall time from the freestream start to a residual fall of args.drop, per form
+    # wall time from the freestream start to a residual fall of args.drop, per
+    # form, and with the committed learned relaxation on the mixed form
     drop = None
     if args.drop > 0 and rank == 0:
-        drop = {"target": args.drop, "norm": "L2 density residual / iteration 1", "cap_s": args.drop_seconds}
-        for f in forms:
-            c2 = make_case(f)
-            c2.step_graph(1)
-            r0 = c2.norm("L2_R_RHO")
-            chunk, it, r = 50, 1, 1.0
+        from tmp_gb300 import learn
+
+        net = learn.load()
+        drop = {"target": args.drop, "norm": "L2 density residual / iteration 1", "cap_s": args.drop_seconds,
+                "learned_weights": str(learn.WEIGHTS.relative_to(ROOT)) if net else None}
+        for f in [x for x in args.drop_forms.split(",") if x]:
+            learned = f.endswith("+learned")
+            if learned and net is None:
+                continue
+            base = f[: -len("+learned")] if learned else f
+            first, _, then = base.partition(">")
+            c2 = make_case(first)
             torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            while time.perf_counter() - t0 < args.drop_seconds:
-                c2.step_graph(chunk)
-                it += chunk
-                r = c2.norm("L2_R_RHO") / r0
-                if not r < 1e3 or r <= args.drop:
-                    break
-            el = time.perf_counter() - t0
-            drop[f] = {"reached": bool(r <= args.drop), "seconds": round(el, 3), "iterations": it, "fall": r}
+            r = learn.run_to_drop(c2, args.drop, 10 ** 9, net if learned else None, chunk=50,
+                                  max_seconds=args.drop_seconds, switch_at=args.switch_at if then else None,
+                                  switch_to=prec_code[then] if then else None)
+            drop[f] = {"reached": r.reached, "seconds": round(r.seconds, 3), "iterations": r.iterations,
+                       "fall": r.history[-1][1], "fell_back": r.fell_back}
             c2.close()
 
     # per-pass device times for the roofline (L2 flushed before each rep)

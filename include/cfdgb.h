@@ -113,7 +113,9 @@ typedef struct {
     double cfl;        /* LU-SGS CFL (LUSGSIntegrator::d_CFL_number); RK uses 0.8 */
     int sweep_mode;    /* LU-SGS schedule: 0 dataflow (one cooperative launch per sweep),
                           1 one launch per level, one thread per cell,
-                          2 one launch per level, 16 lanes per cell               */
+                          2 one launch per level, 16 lanes per cell,
+                          3 dataflow with two cells per warp (binary64 form;
+                          measured 6% slower per step than 0 on C2)              */
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
                                 the occupancy limit)                             */
     int reserved[6];
@@ -158,6 +160,12 @@ int cfd_case_info(cfd_case_t c, int* nmesh, int* ncell_total, int* nedge_total);
 /* cudaStream_t the case issues on. */
 int cfd_case_stream(cfd_case_t c, void** stream);
 int cfd_set_cfl(cfd_case_t c, double cfl);
+/* Switch a live case between precision forms, keeping its state (for example
+ * binary32 while the residual is far from converged, then the binary64
+ * residual).  A case created in the FP64 form cannot switch to a form with the
+ * binary32 LU-SGS sweep (CFD_ERR_MESH); FP32 and MIXED cases can switch to any
+ * form.  Drops the captured step graph. */
+int cfd_set_precision(cfd_case_t c, int precision);
 /* Uniform freestream initial state (Euler2D/ViscousFlow2D::initializeData and
  * the integrator's initializeData). */
 int cfd_init_freestream(cfd_case_t c);
@@ -315,7 +323,7 @@ int cfd_sst_update_mut(cfd_case_t c);
 /* ---- learned relaxation (no reference counterpart) ------------------------- */
 /* A 12-64-64-2 perceptron (relu, bf16 weights, fp32 arithmetic) that maps 12
  * features of a cell after its LU-SGS sweeps to o = (o0, o1): the cell's update
- * is W += omega * dW with omega = 1 + 2*sigmoid(o0), and, when enabled, its
+ * is W += omega * dW with omega = 1 + 0.6*sigmoid(o0), and, when enabled, its
  * next time step is multiplied by 2^(2*tanh(o1)).  The reference uses one
  * constant CFL and omega = 1 (LUSGS_Integrator.h:18, .cpp:242-255), which stay
  * the fallback; neither output changes the fixed point (dW = 0 there).
@@ -332,7 +340,7 @@ int cfd_sst_update_mut(cfd_case_t c);
 #define CFD_MLP_OUTPUTS 2
 #define CFD_MLP_PARAMS  5122
 typedef struct cfd_mlp_s* cfd_mlp_t;
-/* He-uniform weights from a seed; b3[0] = -4 (omega ~ 1.04 untrained). */
+/* He-uniform weights from a seed; b3[0] = -4 (omega ~ 1.01 untrained). */
 int cfd_mlp_create(unsigned long long seed, cfd_mlp_t* out);
 void cfd_mlp_free(cfd_mlp_t m);
 /* Host copies of the fp32 parameters and the input transform (either may be NULL). */
@@ -356,7 +364,9 @@ int cfd_case_track(cfd_case_t c, int on);
 int cfd_case_features(cfd_case_t c, float* d_x);
 /* Attach (m != NULL) or detach the learned relaxation; apply_cfl also applies
  * the CFL output.  spread >= 0 bounds each cell's factor to the mesh mean of
- * the predicted factors +- spread (spread < 0: each cell uses its own).
+ * the predicted factors +- spread (spread < 0: each cell uses its own;
+ * measured: unbounded per-cell factors can stall the iteration, spread 0 is
+ * the robust choice).
  * Detaching restores the constant CFL and the unit update. */
 int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl, double spread);
 

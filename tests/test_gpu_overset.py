@@ -228,3 +228,33 @@ def test_overset_blank_matches_oracle(built_lib):
         assert (ib == 0).sum() > 0 and (nfringe == 0 or md.sum() > 0)
     ib, md = abi.overset_blank(blk_mx, [blk_om], [None], 1)
     assert np.all(ib == 1) and np.all(md == 0)
+
+
+def test_overset_edge_cases(built_lib):
+    from tmp_gb300 import abi, meshgen
+
+    blocks = _blocks(abi)
+    _, blk, topo = blocks["mx"]
+    # no points, all points far outside, a block without walls
+    d, nodes, w = blk.search(np.zeros((0, 2)))
+    assert d.size == 0
+    far = np.full((10, 2), 1e6)
+    it = abi.Interp.search(blk, far, np.arange(10))
+    assert it.info() == (0, 10)
+    m = meshgen.cart_mesh(6, 5, (0.0, 0.0), (1.0, 1.0))
+    path = GOLDEN.parent / "_cart_tmp.grd"
+    meshgen.write_grd(path, m)
+    try:
+        mesh = abi.Mesh.load_grd(path, m.wall_tag, m.far_tag)
+    finally:
+        path.unlink()
+    b2 = abi.Block(mesh)
+    with pytest.raises(abi.CfdError) as e:
+        abi.HoleMap(b2)
+    assert e.value.code == -3
+    # a Cartesian block donates to points inside it with bilinear weights
+    pts = np.array([[0.31, 0.47], [0.999, 0.001], [0.5, 0.5]])
+    d, nodes, w = b2.search(pts)
+    assert np.all(d >= 0) and np.allclose(w.sum(1), 1.0, atol=1e-14)
+    with pytest.raises(abi.CfdError):
+        abi.HoleMap(blk, isym=7)

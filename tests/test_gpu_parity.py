@@ -219,10 +219,11 @@ def test_nonphysical_state_is_reported():
     case.norm("DW_RHO2")
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 def test_sweep_schedules_agree_bitwise(mode):
-    """The dataflow sweep (default), per-level 16-lane and per-level direct sweeps
-    give identical bits: all three keep the reference's dependence exactly."""
+    """The dataflow sweep (default), the two-cells-per-warp dataflow sweep,
+    per-level 16-lane and per-level direct sweeps give identical bits: all of
+    them keep the reference's dependence exactly."""
     from tmp_gb300 import abi
 
     c, g = manifest()["mixed_lam_lusgs"], golden("mixed_lam_lusgs")

@@ -127,6 +127,7 @@ def lib() -> C.CDLL:
         "cfd_case_features": (C.c_int, [vp, vp]),
         "cfd_case_set_mlp": (C.c_int, [vp, vp, C.c_int, C.c_double]),
         "cfd_measure_hop_latency": (C.c_int, [vp, C.c_int, C.c_int, dp]),
+        "cfd_set_precision": (C.c_int, [vp, C.c_int]),
         "cfd_sst_enable": (C.c_int, [vp]),
         "cfd_sst_freestream": (C.c_int, [vp, C.c_int, dp]),
         "cfd_sst_residual": (C.c_int, [vp]),
@@ -242,6 +243,9 @@ class Case:
 
     def init_freestream(self):
         check(lib().cfd_init_freestream(self.h))
+
+    def set_precision(self, precision: int):
+        check(lib().cfd_set_precision(self.h, int(precision)))
 
     def set_cfl(self, cfl: float):
         check(lib().cfd_set_cfl(self.h, float(cfl)))
@@ -516,7 +520,7 @@ def case_features(case: "Case", x_ptr: int):
     check(lib().cfd_case_features(case.h, C.c_void_p(x_ptr)))
 
 
-def case_set_mlp(case: "Case", mlp: Mlp | None, apply_cfl: bool = False, spread: float = 0.1):
+def case_set_mlp(case: "Case", mlp: Mlp | None, apply_cfl: bool = False, spread: float = 0.0):
     check(lib().cfd_case_set_mlp(case.h, mlp.h if mlp is not None else None, int(apply_cfl), float(spread)))
 
 

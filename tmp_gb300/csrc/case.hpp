@@ -12,6 +12,7 @@ namespace cfdgb {
 
 struct DevArrays {
     int nc = 0, nf = 0, nn = 0, nmesh = 0;
+    int resid32 = 0;             // 1 while the residual runs in binary32 (the FP32 form)
     // topology
     int2* lr = nullptr;          // [nf]
     int2* enodes = nullptr;      // [nf] global node ids
@@ -66,7 +67,9 @@ struct DevArrays {
     double* sstD = nullptr;      // [2*nc] LU-SGS diagonal
     float* omega = nullptr;      // [nc] relaxation of the last learned update
     float* omega_mean = nullptr; // [nmesh] its mean per mesh
-    int* mesh_coff = nullptr;    // [nmesh+1] first cell of each mesh
+    int* mlp_samples = nullptr;  // cells the network is evaluated on, mesh by mesh
+    int* mlp_samp_off = nullptr; // [nmesh+1] each mesh's range in mlp_samples
+    int mlp_nsamp = 0;
     // residual intermediates, binary64 form
     d4* grad = nullptr;          // [2*nc]
     d4* phi = nullptr;
@@ -132,6 +135,7 @@ void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bo
 void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32, bool reset);
 void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, int begin, int end);
 cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid);
+cudaError_t launch_sweep_pair64(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
 int sweep_flow_max_grid(bool low, int blocks_per_sm);
 void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
 void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, bool mu64);

@@ -95,7 +95,7 @@ struct cfd_case_s {
     bool track = false;              // keep the previous LU-SGS increment (learning features)
     struct cfd_mlp_s* mlp = nullptr;  // learned relaxation, or null for the plain update
     bool mlp_cfl = false;            // apply the network's CFL multipliers too
-    float mlp_spread = 0.1f;         // bound on |omega - mesh mean| (negative: none)
+    float mlp_spread = 0.0f;         // bound on |omega - mesh mean| (negative: none)
     std::vector<cfd_freestream_t> fs_in;  // the freestreams the case was created with
     bool sst = false;                // SST k-omega arrays allocated
     bool viscous() const { return p.flow == CFD_FLOW_LAMINAR; }
@@ -121,7 +121,7 @@ void free_case(cfd_case_s* c) {
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
                     d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.wall_ptr, d.wall_faces, d.wblocks, d.wpartial, d.wforce, d.swfcf, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
-                    d.norm_out, d.err, d.dWprev, d.omega, d.omega_mean, d.mesh_coff, d.sstT, d.sstTf, d.sstG, d.sstF1, d.sstF2,
+                    d.norm_out, d.err, d.dWprev, d.omega, d.omega_mean, d.mlp_samples, d.mlp_samp_off, d.sstT, d.sstTf, d.sstG, d.sstF1, d.sstF2,
                     d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -167,19 +167,22 @@ void sweeps(cfd_case_s* c, bool forward) {
             launch_sweep_level(d, L, c->viscous(), forward, ptr[k], ptr[k + 1], c->fp32());
         return;
     }
-    if (forward && !(c->fast_sweep() && c->p.sweep_mode == 0))
-        launch_sweep_prep(d, L, c->viscous(), c->fp32(), c->p.sweep_mode == 0);
+    const bool dataflow = c->p.sweep_mode == 0 || c->p.sweep_mode == 3;
+    if (forward && !(c->fast_sweep() && dataflow))
+        launch_sweep_prep(d, L, c->viscous(), c->fp32(), dataflow);
     if (c->p.sweep_mode == 2) {
         for (size_t k = 0; k + 1 < ptr.size(); k++) launch_sweep16_level(d, L, forward, ptr[k], ptr[k + 1]);
         return;
     }
-    // default: one dataflow launch per direction
+    // default: one dataflow launch per direction (binary64 form, mode 3: two cells per warp)
     if (c->fast_sweep()) {
         if (forward) {
             launch_inv_diag(d, L);
             launch_sweep_prep32(d, L, c->viscous(), c->mixed());
         }
         ck(launch_sweep_flow32(d, L, forward, d.flow_grid), "cooperative sweep launch");
+    } else if (c->p.sweep_mode == 3) {
+        ck(launch_sweep_pair64(d, L, forward, d.flow_grid), "cooperative sweep launch");
     } else {
         ck(launch_sweep_flow(d, L, forward, false, d.flow_grid), "cooperative sweep launch");
     }
@@ -450,6 +453,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         dalloc(&d.prm, nmesh);
         dalloc(&d.fgeo, nf); dalloc(&d.fcen, nf); dalloc(&d.cgeo, nc); dalloc(&d.fg0, nf); dalloc(&d.fg1, nf);
         dalloc(&d.fvis, nf);
+        d.resid32 = c->fp32() ? 1 : 0;
         dalloc(&d.U, nc); dalloc(&d.W, nc); dalloc(&d.W0, nc); dalloc(&d.R, nc); dalloc(&d.dt, nc);
         dalloc(&d.diag, nc); dalloc(&d.dW1, nc); dalloc(&d.dW, nc);
         if (c->fp32()) {
@@ -468,10 +472,10 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         dalloc(&d.fwd_order, nc); dalloc(&d.bwd_order, nc);
         if (P.advance == CFD_ADV_LUSGS) {
             dalloc(&d.swfc, 16 * (size_t)nc); dalloc(&d.swra, 4 * (size_t)nc); dalloc(&d.invD, nc);
+            dalloc(&d.fwd_order2, d.npos2_fwd); dalloc(&d.bwd_order2, d.npos2_bwd);
             if (P.precision != CFD_PREC_FP64) {
                 dalloc(&d.swfcf, 16 * (size_t)nc); dalloc(&d.swraf, 4 * (size_t)nc); dalloc(&d.Wf, nc);
                 dalloc(&d.dW1f, nc); dalloc(&d.dWf, nc);
-                dalloc(&d.fwd_order2, d.npos2_fwd); dalloc(&d.bwd_order2, d.npos2_bwd);
             }
             d.flow_grid = sweep_flow_max_grid(P.precision != CFD_PREC_FP64, P.sweep_blocks_per_sm);
         }
@@ -739,7 +743,7 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
     bool visc = c->viscous(), f32 = c->fp32();
     for (int r = 0; r < reps; r++) {
         // a lone backward sweep needs the "not yet computed" markers the forward pass sets
-        if (pass == 5 && c->p.sweep_mode == 0) {
+        if (pass == 5 && (c->p.sweep_mode == 0 || c->p.sweep_mode == 3)) {
             if (c->fast_sweep()) launch_sweep_prep32(d, L, visc, c->mixed());
             else launch_sweep_prep(d, L, visc, f32, true);
         }
@@ -919,7 +923,8 @@ struct cfd_mlp_s {
 
 namespace {
 void learned_update(cfd_case_s* c) {
-    launch_learned_update(c->d, c->L(), c->mlp->net, c->mlp_cfl, c->mlp_spread, c->d.mesh_coff, c->fp32());
+    launch_learned_update(c->d, c->L(), c->mlp->net, c->mlp_cfl, c->mlp_spread, c->d.mlp_samples, c->d.mlp_samp_off,
+                          c->d.mlp_nsamp, c->fp32());
 }
 }  // namespace
 
@@ -943,7 +948,7 @@ int cfd_mlp_create(unsigned long long seed, cfd_mlp_t* out) {
     ck(m->net.init(), "cudaMalloc");
     ck(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     // uniform(-a, a) with a = sqrt(6 / fan_in) (He); the first output's bias
-    // starts at -4 so an untrained network relaxes by ~1.04.
+    // starts at -4 so an untrained network relaxes by ~1.01.
     std::vector<float> p(kMlpParams, 0.f);
     const int NI = kMlpIn, NH = kMlpHidden;
     unsigned long long z = seed;
@@ -1054,9 +1059,8 @@ int cfd_case_track(cfd_case_t c, int on) {
         dalloc(&d.dWprev, d.nc);
         dalloc(&d.omega, d.nc);
         dalloc(&d.omega_mean, c->nmesh);
-        dalloc(&d.mesh_coff, c->nmesh + 1);
-        ck(cudaMemcpyAsync(d.mesh_coff, c->coff.data(), (c->nmesh + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream),
-           "upload");
+        dalloc(&d.mlp_samples, d.nc);
+        dalloc(&d.mlp_samp_off, c->nmesh + 1);
         ck(cudaMemsetAsync(d.dWprev, 0, sizeof(d4) * d.nc, c->stream), "memset");
         ck(cudaMemsetAsync(d.dW, 0, sizeof(d4) * d.nc, c->stream), "memset");
         std::vector<float> one(d.nc, 1.0f);
@@ -1096,6 +1100,23 @@ int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl, double spread) {
         std::vector<float> one(c->d.nc, 1.0f);  // back to the constant CFL
         ck(cudaMemcpyAsync(c->d.cflmul, one.data(), one.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
         ck(cudaStreamSynchronize(c->stream), "sync");
+    }
+    if (m) {
+        // cells the network is evaluated on: every cell, or with spread 0 (only
+        // the mesh mean is applied) about 4096 evenly spaced cells per mesh
+        std::vector<int> samp, off(c->nmesh + 1, 0);
+        for (int k = 0; k < c->nmesh; k++) {
+            const int b = c->coff[k], n = c->coff[k + 1] - b;
+            const int stride = (spread == 0.0 && !apply_cfl) ? std::max(1, n / 4096) : 1;
+            for (int i = 0; i < n; i += stride) samp.push_back(b + i);
+            off[k + 1] = (int)samp.size();
+        }
+        ck(cudaMemcpyAsync(c->d.mlp_samples, samp.data(), samp.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+           "upload");
+        ck(cudaMemcpyAsync(c->d.mlp_samp_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+           "upload");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+        c->d.mlp_nsamp = (int)samp.size();
     }
     c->drop_graph();
     c->mlp = m;
@@ -1191,3 +1212,60 @@ int cfd_sst_update_mut(cfd_case_t c) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Switching the precision form of a live case
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// Allocate whatever the form `prec` needs that the case does not hold yet, and
+// fill the binary32 geometry copies when they are new.
+void ensure_precision_arrays(cfd_case_s* c, int prec) {
+    DevArrays& d = c->d;
+    const size_t nc = d.nc, nf = d.nf;
+    const bool visc = c->viscous();
+    auto L = c->L();
+    bool new_geo32 = false;
+    if (prec != CFD_PREC_FP64) {
+        if (!d.fg0f) {
+            dalloc(&d.fg0f, nf); dalloc(&d.fg1f, nf); dalloc(&d.fvisf, nf); dalloc(&d.cgeof, nc);
+            new_geo32 = true;
+        }
+        if (!d.Uf) dalloc(&d.Uf, nc);
+    }
+    if (prec == CFD_PREC_FP32 && !d.gradf) {
+        dalloc(&d.gradf, 2 * nc); dalloc(&d.phif, nc); dalloc(&d.speccf, nc);
+        dalloc(&d.Uef, nf); dalloc(&d.fspecf, nf); dalloc(&d.Fcf, nf);
+        if (visc) { dalloc(&d.specvf, nc); dalloc(&d.gradTf, nc); dalloc(&d.muf, nc); dalloc(&d.muef, nf); dalloc(&d.Fvf, nf); }
+    }
+    if (prec != CFD_PREC_FP32 && !d.grad) {
+        dalloc(&d.grad, 2 * nc); dalloc(&d.phi, nc); dalloc(&d.specc, nc);
+        dalloc(&d.Ue, nf); dalloc(&d.fspec, nf); dalloc(&d.Fc, nf);
+        if (visc) { dalloc(&d.specv, nc); dalloc(&d.gradT, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf); dalloc(&d.Fv, nf); }
+    }
+    if (c->p.advance == CFD_ADV_LUSGS && prec != CFD_PREC_FP64 && !d.swfcf)
+        throw std::runtime_error("the binary32 sweep needs a case created in the FP32 or MIXED form");
+    if (new_geo32) launch_to_fp32(d, L, true);
+    else if (prec != CFD_PREC_FP64) launch_to_fp32(d, L, false);  // binary32 copy of the current state
+    ck(cudaGetLastError(), "launch");
+}
+
+}  // namespace
+
+extern "C" int cfd_set_precision(cfd_case_t c, int precision) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (precision < CFD_PREC_FP64 || precision > CFD_PREC_MIXED) return fail(CFD_ERR_ARG, "unknown precision");
+    if (precision == c->p.precision) return CFD_OK;
+    if (c->sst && precision == CFD_PREC_FP32) return fail(CFD_ERR_STATE, "the SST model needs the binary64 residual");
+    ABI_TRY
+    ensure_precision_arrays(c, precision);
+    c->p.precision = precision;
+    c->d.resid32 = precision == CFD_PREC_FP32 ? 1 : 0;
+    if (c->p.advance == CFD_ADV_LUSGS)
+        c->d.flow_grid = sweep_flow_max_grid(precision != CFD_PREC_FP64, c->p.sweep_blocks_per_sm);
+    c->drop_graph();
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    return CFD_OK;
+    ABI_CATCH
+}

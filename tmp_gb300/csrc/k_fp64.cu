@@ -597,6 +597,123 @@ cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forwa
 }
 
 // ---------------------------------------------------------------------------
+// Plain-form dataflow sweep with two cells per warp.  Same protocol and the
+// same binary64 arithmetic per cell as k_sweep_flow (so the increments are
+// bit-identical), but each half-warp (16 lanes: 4 face slots x 4 equations)
+// carries its own cell, the two cells of a pair coming from the same level
+// (order2).  A warp-wide binary64 instruction holds its sub-partition's FP64
+// pipe for 64 cycles however many lanes are active, so serving two cells with
+// each instruction halves the pipe time per cell; but each half then computes
+// both u = w2/w0 and v = w3/w0 (two divides on its chain instead of one) and a
+// warp's two cells finish together, and on C2 the step came out 6% slower
+// than with one cell per warp, which stays the default (sweep_mode 0).
+template <bool FWD>
+__global__ void __launch_bounds__(256) k_sweep_pair64(int npos, const int* __restrict__ order2,
+                                                      const int4* __restrict__ cface, const int2* __restrict__ lr,
+                                                      const d4* __restrict__ fg0, const d4* __restrict__ W,
+                                                      const double* __restrict__ swfc,
+                                                      const double* __restrict__ swra, const d4* __restrict__ R,
+                                                      const double* __restrict__ D, d4* dW1, d4* dW, unsigned* err) {
+    const double GM1 = 1.4 - 1.0;
+    const int lane = threadIdx.x & 31;
+    const int h = lane >> 4, base = lane & 16;
+    const int s = (lane >> 2) & 3, m = lane & 3;
+    const int warp = threadIdx.x >> 5;
+    const int B = gridDim.x, NW = blockDim.x >> 5;
+    d4* dst = FWD ? dW1 : dW;
+    const int npairs = npos >> 1;
+    const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
+    for (long long q = q0;; q += NW) {
+        const long long P = (long long)blockIdx.x + (long long)B * q;
+        if (P >= npairs) break;
+        const int i = order2[2 * P + h];
+        const bool active = i >= 0;
+        const int4 cf = active ? cface[i] : make_int4(0, 0, 0, 0);
+        const int code = s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w;
+        bool use = false, left = false;
+        int f = 0, j = 0;
+        if (code != 0) {
+            f = code_face(code);
+            left = code > 0;
+            int2 e = lr[f];
+            j = left ? e.y : e.x;
+            use = FWD ? (j >= 0 && j < i) : (j > i);
+        }
+        double own = 0.0, dinv = 1.0;
+        if (active && s == 0) {
+            own = FWD ? (&R[i].x)[m] : (&dW1[i].x)[m];
+            dinv = D[i];
+        }
+        double w0[4] = {1.0, 1.0, 0.0, 0.0}, dw[4] = {0.0, 0.0, 0.0, 0.0};
+        d4 g = d4{0.0, 0.0, 0.0, 0.0};
+        double fc = 0.0, rA = 0.0;
+        if (use) {
+            to_arr(ld4(W + j), w0);
+            g = fg0[f];
+            fc = swfc[(size_t)i * 16 + s * 4 + m];
+            rA = swra[(size_t)i * 4 + s];
+            const double2* qp = reinterpret_cast<const double2*>(dst + j);
+            double2 a, b;
+            long long it = 0;
+            while (true) {
+                a = __ldcv(qp);
+                b = __ldcv(qp + 1);
+                if (!is_sentinel(a.x) && !is_sentinel(a.y) && !is_sentinel(b.x) && !is_sentinel(b.y)) break;
+                if (++it > kSpinLimit) {
+                    atomicOr(err, ERR_TIMEOUT);
+                    break;
+                }
+            }
+            dw[0] = a.x; dw[1] = a.y; dw[2] = b.x; dw[3] = b.y;
+        }
+        __syncwarp();
+        double wp[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
+        const double u = wp[2] / wp[0], v = wp[3] / wp[0];
+        double vn = dot2(u, v, g.x, g.y);
+        double pr = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
+        double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + pr) * vn : m == 2 ? wp[2] * vn + pr * g.x
+                                                                               : wp[3] * vn + pr * g.y;
+        double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
+        double dfc = left ? (fcp - fc) : (fc - fcp);
+        double df = 0.5 * (dfc - rA * dwm) * g.z;
+        double DF = use ? df : 0.0;
+        double v0 = __shfl_sync(0xffffffffu, DF, base + m);
+        double v1 = __shfl_sync(0xffffffffu, DF, base + 4 + m);
+        double v2 = __shfl_sync(0xffffffffu, DF, base + 8 + m);
+        double v3 = __shfl_sync(0xffffffffu, DF, base + 12 + m);
+        double dF = 0.0;
+        if (cf.x != 0) dF += v0;
+        if (cf.y != 0) dF += v1;
+        if (cf.z != 0) dF += v2;
+        if (cf.w != 0) dF += v3;
+        double res = 0.0;
+        if (s == 0) res = FWD ? (-own - dF) / dinv : own - dF / dinv;
+        double r1 = __shfl_sync(0xffffffffu, res, base + 1);
+        double r2 = __shfl_sync(0xffffffffu, res, base + 2);
+        double r3 = __shfl_sync(0xffffffffu, res, base + 3);
+        if (active && (lane & 15) == 0) {
+            double2* o = reinterpret_cast<double2*>(dst + i);
+            __stcg(o, make_double2(res, r1));
+            __stcg(o + 1, make_double2(r2, r3));
+        }
+    }
+}
+
+cudaError_t launch_sweep_pair64(const DevArrays& d, const LaunchCfg& L, bool forward, int grid) {
+    int npos = forward ? d.npos2_fwd : d.npos2_bwd;
+    const int* order = forward ? d.fwd_order2 : d.bwd_order2;
+    void* args[] = {(void*)&npos, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0, (void*)&d.W,
+                    (void*)&d.swfc, (void*)&d.swra, (void*)&d.R, (void*)&d.diag, (void*)&d.dW1, (void*)&d.dW,
+                    (void*)&d.err};
+    void* fn = forward ? (void*)k_sweep_pair64<true> : (void*)k_sweep_pair64<false>;
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
+    *L.counter += 1;
+    return e;
+}
+
+// ---------------------------------------------------------------------------
 // Fast-form dataflow sweep.  Same protocol as k_sweep_flow, but everything on
 // the dependence chain except the final update is binary32: float copies of
 // W (Wf), of the per-step SolveDF constants and of the increments (dW1f/dWf,
@@ -720,7 +837,8 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
         }
         __syncwarp();
         float wp0 = w0.x + dw.x, wp1 = w0.y + dw.y, wp2 = w0.z + dw.z, wp3 = w0.w + dw.w;
-        float u = wp2 / wp0, v = wp3 / wp0;
+        const float rr = 1.f / wp0;
+        float u = wp2 * rr, v = wp3 * rr;
         float vn = u * g.x + v * g.y;
         float pr = GM1 * (wp1 - 0.5f * wp0 * (u * u + v * v));
         float fcp = m == 0 ? wp0 * vn : m == 1 ? (wp1 + pr) * vn : m == 2 ? wp2 * vn + pr * g.x : wp3 * vn + pr * g.y;
@@ -736,20 +854,25 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
         if (cf.y != 0) dF += v1;
         if (cf.z != 0) dF += v2;
         if (cf.w != 0) dF += v3;
-        double res = 0.0;
-        if (s == 0) res = FWD ? (-own - (double)dF) * dinv : own - (double)dF * dinv;
-        float resf = (float)res;
-        double r1 = __shfl_sync(0xffffffffu, res, base + 1);
-        double r2 = __shfl_sync(0xffffffffu, res, base + 2);
-        double r3 = __shfl_sync(0xffffffffu, res, base + 3);
+        // The binary32 copy that the next levels wait for is computed and
+        // published first, in binary32; the binary64 increment (used only by
+        // the backward sweep and the update, after this launch) follows off
+        // the critical path.
+        const float ownf = (float)own, dinvf = (float)dinv;
+        const float resf = FWD ? (-ownf - dF) * dinvf : ownf - dF * dinvf;
         float f1 = __shfl_sync(0xffffffffu, resf, base + 1);
         float f2 = __shfl_sync(0xffffffffu, resf, base + 2);
         float f3 = __shfl_sync(0xffffffffu, resf, base + 3);
+        if (active && (lane & 15) == 0) __stcg(dstf + i, make_float4(resf, f1, f2, f3));
+        double res = 0.0;
+        if (s == 0) res = FWD ? (-own - (double)dF) * dinv : own - (double)dF * dinv;
+        double r1 = __shfl_sync(0xffffffffu, res, base + 1);
+        double r2 = __shfl_sync(0xffffffffu, res, base + 2);
+        double r3 = __shfl_sync(0xffffffffu, res, base + 3);
         if (active && (lane & 15) == 0) {
             double2* o = reinterpret_cast<double2*>(dst + i);
             __stcg(o, make_double2(res, r1));
             __stcg(o + 1, make_double2(r2, r3));
-            __stcg(dstf + i, make_float4(resf, f1, f2, f3));
         }
     }
 }
@@ -775,6 +898,12 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, fn2, 256, 0);
     per = per < per2 ? per : per2;
+    if (!low) {  // the plain form's paired kernels run on the same grid
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_pair64<true>, 256, 0);
+        per = per < per2 ? per : per2;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_pair64<false>, 256, 0);
+        per = per < per2 ? per : per2;
+    }
     if (per < 1) per = 1;
     int want = blocks_per_sm > 0 ? blocks_per_sm : 2;
     return sms * (want < per ? want : per);

@@ -35,9 +35,10 @@ struct MlpNet {
 };
 
 void launch_case_features(const DevArrays& d, const LaunchCfg& L, float* X);
-// mesh_off: device array of the meshes' first cells (nmesh + 1 entries).
+// samples[nsamp]: the cells the network is evaluated on, mesh by mesh;
+// samp_off[nmesh + 1]: each mesh's range in samples.
 void launch_learned_update(const DevArrays& d, const LaunchCfg& L, const MlpNet& net, bool apply_cfl, float spread,
-                           const int* mesh_off, bool fp32_copy);
+                           const int* samples, const int* samp_off, int nsamp, bool fp32_copy);
 cudaError_t mlp_forward(const MlpNet& net, const float* X, long long n, float* Y, cudaStream_t s);
 // Loss and gradient of B rows (idx[b], or rows 0..B-1 when idx is null); the
 // loss (sum over rows of M-weighted squared errors times inv_msum) goes to d_loss.
