@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--sweep-mode", type=int, default=0, help="LU-SGS schedule (0 dataflow, 1/2 per level)")
-    ap.add_argument("--sweep-bpsm", type=int, default=0, help="dataflow sweep blocks per SM (0 = default)")
+    ap.add_argument("--sweep-bpsm", type=int, default=0, help="dataflow sweep blocks per SM (0 = autotune)")
+    ap.add_argument("--sweep-poll-ns", type=int, default=0, help="dataflow sweep back-off between polls (ns)")
     ap.add_argument("--forms", default="fp64,fp32,mixed", help="precision forms timed besides --precision ('' = none)")
     ap.add_argument("--drop", type=float, default=1e-3, help="residual fall for time_to_drop (0 = skip)")
     ap.add_argument("--drop-seconds", type=float, default=40.0, help="cap per form for time_to_drop")
@@ -285,8 +286,12 @@ def run_ours(args):
                      abi.FLOW_LAMINAR if viscous else abi.FLOW_EULER,
                      abi.ADV_LUSGS if w.advance == "lusgs" else abi.ADV_RK5,
                      prec_code[precision], cfl=w.cfl, stream=stream.cuda_stream,
-                     sweep_mode=args.sweep_mode, sweep_blocks_per_sm=args.sweep_bpsm)
+                     sweep_mode=args.sweep_mode, sweep_blocks_per_sm=args.sweep_bpsm,
+                     sweep_poll_ns=args.sweep_poll_ns)
         c.init_freestream()
+        c.tuned = None
+        if args.sweep_bpsm == 0 and w.advance == "lusgs" and args.sweep_mode in (0, 3):
+            c.tuned = c.autotune(3)[0]  # the sweeps' blocks per SM, by timing whole steps
         return c
 
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -356,12 +361,14 @@ def run_ours(args):
 
     # the other precision forms, timed the same way
     forms = {}
-    for f in [x for x in args.forms.split(",") if x and x != args.precision]:
+    for f in [x for x in args.forms.split(",") if x and x != args.precision and (w.advance == "lusgs" or x != "mixed")]:
         c2 = make_case(f)
         fm, _ = timed_steps(c2, args.steps)
-        forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3)}
+        forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3),
+                    "sweep_blocks_per_sm": c2.tuned}
         c2.close()
-    forms[args.precision] = {"ms_per_step": 1e3 * t_local / args.steps, "value": nc * args.steps / t_local}
+    forms[args.precision] = {"ms_per_step": 1e3 * t_local / args.steps, "value": nc * args.steps / t_local,
+                             "sweep_blocks_per_sm": case.tuned}
 
     # wall time from the freestream start to a residual fall of args.drop, per
     # form, and with the committed learned relaxation on the mixed form
@@ -374,7 +381,9 @@ def run_ours(args):
                 "learned_weights": str(learn.WEIGHTS.relative_to(ROOT)) if net else None}
         for f in [x for x in args.drop_forms.split(",") if x]:
             learned = f.endswith("+learned")
-            if learned and net is None:
+            if learned and (net is None or w.advance != "lusgs"):
+                continue
+            if w.advance != "lusgs" and ("mixed" in f):  # the mixed form is a LU-SGS form
                 continue
             base = f[: -len("+learned")] if learned else f
             first, _, then = base.partition(">")

@@ -118,7 +118,9 @@ typedef struct {
                           measured 6% slower per step than 0 on C2)              */
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
                                 the occupancy limit)                             */
-    int reserved[6];
+    int sweep_poll_ns; /* dataflow sweep: pause between polls of a neighbour's
+                          increment in ns (__nanosleep; 0 = spin)                */
+    int reserved[5];
 } cfd_params_t;
 
 /* ---- errors -------------------------------------------------------------- */
@@ -206,6 +208,11 @@ long long cfd_launch_count(cfd_case_t c);
  * pass: 0 face_state, 1 cell_grad, 2 face_flux, 3 cell_update, 4 forward sweep
  * (all levels), 5 backward sweep (all levels), 6 LU-SGS update, 7 whole step. */
 int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms);
+/* Autotuner of the dataflow sweeps' launch shape (no reference counterpart):
+ * times `reps` whole LU-SGS steps for each co-resident block count per SM
+ * (1, 2, ... up to the occupancy limit), keeps the fastest for the case and
+ * reports it; the case's state is restored afterwards. */
+int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_ms);
 /* Failure-detection self-test (no reference counterpart): launch a kernel that
  * waits, at most `polls` polls, on a device flag nothing sets, exactly as the
  * dataflow LU-SGS sweep waits on its neighbours.  Returns CFD_ERR_TIMEOUT when

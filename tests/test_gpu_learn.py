@@ -163,3 +163,19 @@ def test_precision_switch_keeps_the_state(built_lib):
     f = spec.case(mesh, abi.PREC_FP64)
     with pytest.raises(abi.CfdError):
         f.set_precision(abi.PREC_FP32)
+
+
+def test_autotune_restores_state(built_lib):
+    from tmp_gb300 import abi, learn
+
+    spec = learn.CaseSpec(nbody=48, nlayer=10, seed=6)
+    mesh = spec.mesh()
+    for prec in (abi.PREC_FP64, abi.PREC_MIXED):
+        c = spec.case(mesh, prec)
+        c.step_graph(20)
+        U = c.get("U")
+        bpsm, ms = c.autotune(2)
+        assert bpsm >= 1 and ms > 0
+        assert np.array_equal(c.get("U"), U)
+        c.step_graph(5)  # still steps after the launch shape changed
+        assert np.isfinite(c.get("U")).all()

@@ -52,7 +52,7 @@ class Freestream(C.Structure):
 class Params(C.Structure):
     _fields_ = [("flow", C.c_int), ("advance", C.c_int), ("precision", C.c_int), ("first_order", C.c_int),
                 ("cfl", C.c_double), ("sweep_mode", C.c_int), ("sweep_blocks_per_sm", C.c_int),
-                ("reserved", C.c_int * 6)]
+                ("sweep_poll_ns", C.c_int), ("reserved", C.c_int * 5)]
 
 
 _lib = None
@@ -128,6 +128,7 @@ def lib() -> C.CDLL:
         "cfd_case_set_mlp": (C.c_int, [vp, vp, C.c_int, C.c_double]),
         "cfd_measure_hop_latency": (C.c_int, [vp, C.c_int, C.c_int, dp]),
         "cfd_set_precision": (C.c_int, [vp, C.c_int]),
+        "cfd_autotune": (C.c_int, [vp, C.c_int, ip, dp]),
         "cfd_sst_enable": (C.c_int, [vp]),
         "cfd_sst_freestream": (C.c_int, [vp, C.c_int, dp]),
         "cfd_sst_residual": (C.c_int, [vp]),
@@ -205,13 +206,14 @@ class Case:
 
     def __init__(self, meshes: Sequence[Mesh], freestreams: Sequence[dict], flow: int, advance: int,
                  precision: int = PREC_FP64, cfl: float = 1.0, first_order: bool = False, stream: int | None = None,
-                 sweep_mode: int = 0, sweep_blocks_per_sm: int = 0):
+                 sweep_mode: int = 0, sweep_blocks_per_sm: int = 0, sweep_poll_ns: int = 0):
         self.meshes = list(meshes)
         arr = (C.c_void_p * len(meshes))(*[m.h.value for m in meshes])
         fs = (Freestream * len(meshes))(*[Freestream(f["mach"], f.get("aoa_deg", 0.0), f.get("reynolds", 1.0),
                                                      f.get("density", 1.225), f.get("pressure", 101325.0))
                                           for f in freestreams])
-        p = Params(flow, advance, precision, int(first_order), float(cfl), int(sweep_mode), int(sweep_blocks_per_sm))
+        p = Params(flow, advance, precision, int(first_order), float(cfl), int(sweep_mode), int(sweep_blocks_per_sm),
+                   int(sweep_poll_ns))
         h = C.c_void_p()
         check(lib().cfd_case_create(arr, len(meshes), fs, C.byref(p), C.c_void_p(stream) if stream else None,
                                     C.byref(h)))
@@ -243,6 +245,12 @@ class Case:
 
     def init_freestream(self):
         check(lib().cfd_init_freestream(self.h))
+
+    def autotune(self, reps: int = 5):
+        """Pick the sweeps' blocks per SM by timing whole steps; returns (blocks_per_sm, ms)."""
+        b, t = C.c_int(), C.c_double()
+        check(lib().cfd_autotune(self.h, int(reps), C.byref(b), C.byref(t)))
+        return b.value, t.value
 
     def set_precision(self, precision: int):
         check(lib().cfd_set_precision(self.h, int(precision)))

@@ -100,7 +100,6 @@ struct DevArrays {
     double* swra = nullptr;      // [4*nc]  r_A at i*4+s
     double* invD = nullptr;      // [nc] 1/D (fast form's sweep)
     // fast-form sweep: binary32 copies and level-paired order
-    float* swfcf = nullptr;      // [16*nc]
     float* swraf = nullptr;      // [4*nc]
     float4* Wf = nullptr;        // [nc]
     float4* dW1f = nullptr;      // [nc]
@@ -109,6 +108,7 @@ struct DevArrays {
     int* bwd_order2 = nullptr;
     int npos2_fwd = 0, npos2_bwd = 0;
     int flow_grid = 0;           // co-resident blocks of the dataflow sweep
+    int poll_ns = 0;             // back-off between a dataflow sweep's polls (ns, 0 = spin)
     // LU-SGS level schedule (all meshes merged level by level)
     int* fwd_order = nullptr;
     int* bwd_order = nullptr;
@@ -134,7 +134,7 @@ void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, in
 void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bool forward, int begin, int end, bool fp32);
 void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32, bool reset);
 void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, int begin, int end);
-cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid);
+cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
 cudaError_t launch_sweep_pair64(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
 int sweep_flow_max_grid(bool low, int blocks_per_sm);
 void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);

@@ -120,7 +120,7 @@ void free_case(cfd_case_s* c) {
                     d.cgeo, d.fg0, d.fg1, d.fvis, d.walld, d.fg0f, d.fg1f, d.fvisf, d.cgeof, d.U, d.W, d.W0, d.R,
                     d.dt, d.diag, d.dW1, d.dW, d.grad, d.phi, d.specc, d.specv, d.gradT, d.mu, d.Ue, d.fspec,
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
-                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.wall_ptr, d.wall_faces, d.wblocks, d.wpartial, d.wforce, d.swfcf, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
+                    d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.wall_ptr, d.wall_faces, d.wblocks, d.wpartial, d.wforce, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err, d.dWprev, d.omega, d.omega_mean, d.mlp_samples, d.mlp_samp_off, d.sstT, d.sstTf, d.sstG, d.sstF1, d.sstF2,
                     d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD};
     for (void* q : ptrs)
@@ -184,7 +184,7 @@ void sweeps(cfd_case_s* c, bool forward) {
     } else if (c->p.sweep_mode == 3) {
         ck(launch_sweep_pair64(d, L, forward, d.flow_grid), "cooperative sweep launch");
     } else {
-        ck(launch_sweep_flow(d, L, forward, false, d.flow_grid), "cooperative sweep launch");
+        ck(launch_sweep_flow(d, L, forward, d.flow_grid), "cooperative sweep launch");
     }
 }
 
@@ -474,10 +474,11 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             dalloc(&d.swfc, 16 * (size_t)nc); dalloc(&d.swra, 4 * (size_t)nc); dalloc(&d.invD, nc);
             dalloc(&d.fwd_order2, d.npos2_fwd); dalloc(&d.bwd_order2, d.npos2_bwd);
             if (P.precision != CFD_PREC_FP64) {
-                dalloc(&d.swfcf, 16 * (size_t)nc); dalloc(&d.swraf, 4 * (size_t)nc); dalloc(&d.Wf, nc);
+                dalloc(&d.swraf, 4 * (size_t)nc); dalloc(&d.Wf, nc);
                 dalloc(&d.dW1f, nc); dalloc(&d.dWf, nc);
             }
             d.flow_grid = sweep_flow_max_grid(P.precision != CFD_PREC_FP64, P.sweep_blocks_per_sm);
+            d.poll_ns = P.sweep_poll_ns < 0 ? 0 : (P.sweep_poll_ns > 10000 ? 10000 : P.sweep_poll_ns);
         }
         dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
         dalloc(&d.err, 2);
@@ -1244,7 +1245,7 @@ void ensure_precision_arrays(cfd_case_s* c, int prec) {
         dalloc(&d.Ue, nf); dalloc(&d.fspec, nf); dalloc(&d.Fc, nf);
         if (visc) { dalloc(&d.specv, nc); dalloc(&d.gradT, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf); dalloc(&d.Fv, nf); }
     }
-    if (c->p.advance == CFD_ADV_LUSGS && prec != CFD_PREC_FP64 && !d.swfcf)
+    if (c->p.advance == CFD_ADV_LUSGS && prec != CFD_PREC_FP64 && !d.swraf)
         throw std::runtime_error("the binary32 sweep needs a case created in the FP32 or MIXED form");
     if (new_geo32) launch_to_fp32(d, L, true);
     else if (prec != CFD_PREC_FP64) launch_to_fp32(d, L, false);  // binary32 copy of the current state
@@ -1267,5 +1268,57 @@ extern "C" int cfd_set_precision(cfd_case_t c, int precision) {
     c->drop_graph();
     ck(cudaStreamSynchronize(c->stream), "sync");
     return CFD_OK;
+    ABI_CATCH
+}
+
+// ---------------------------------------------------------------------------
+// Autotuning the dataflow sweeps' launch shape
+// ---------------------------------------------------------------------------
+
+extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_ms) {
+    if (!c || reps <= 0) return fail(CFD_ERR_ARG, "cfd_autotune: null case or reps <= 0");
+    if (c->p.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_STATE, "cfd_autotune: only the LU-SGS sweeps are tuned");
+    ABI_TRY
+    DevArrays& d = c->d;
+    const size_t nc = d.nc;
+    // the trial steps advance the state: keep it and put it back afterwards
+    d4 *U0 = nullptr, *W0 = nullptr;
+    dalloc(&U0, nc);
+    dalloc(&W0, nc);
+    ck(cudaMemcpyAsync(U0, d.U, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "save");
+    ck(cudaMemcpyAsync(W0, d.W, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "save");
+    const bool low = c->p.precision != CFD_PREC_FP64;
+    const int max_grid = sweep_flow_max_grid(low, 64);  // occupancy limit
+    int best = 0, last_grid = -1;
+    double best_t = 1e300;
+    int rc = CFD_OK;
+    for (int bpsm = 1; bpsm <= 8; bpsm++) {
+        const int grid = sweep_flow_max_grid(low, bpsm);
+        if (grid == last_grid || grid > max_grid) break;  // capped by occupancy: nothing new to try
+        last_grid = grid;
+        d.flow_grid = grid;
+        c->drop_graph();
+        double ms = 0;
+        rc = cfd_bench_pass(c, 7, reps, 0, &ms);
+        if (rc != CFD_OK) break;
+        if (ms < best_t) {
+            best_t = ms;
+            best = bpsm;
+        }
+    }
+    if (rc == CFD_OK) {
+        c->p.sweep_blocks_per_sm = best;
+        d.flow_grid = sweep_flow_max_grid(low, best);
+        c->drop_graph();
+        if (best_blocks_per_sm) *best_blocks_per_sm = best;
+        if (best_ms) *best_ms = best_t;
+    }
+    ck(cudaMemcpyAsync(d.U, U0, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "restore");
+    ck(cudaMemcpyAsync(d.W, W0, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "restore");
+    if (c->fp32() || c->mixed()) launch_to_fp32(d, c->L(), false);
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    cudaFree(U0);
+    cudaFree(W0);
+    return rc;
     ABI_CATCH
 }

@@ -408,8 +408,6 @@ void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, 
 // proceed.  Every wait is bounded: after kSpinLimit polls the kernel raises
 // ERR_TIMEOUT and goes on, so it always terminates.  Arithmetic never produces
 // the sentinel (NaN results are quiet NaNs), so a NaN state cannot stall it.
-// LOW selects the fast form: the SolveDF combination in binary32, the sum
-// widened, and dW = (-R - sum) * (1/D) with 1/D from binary64.
 constexpr long long kSpinLimit = 1LL << 22;
 
 __device__ __forceinline__ bool is_sentinel(double x) {
@@ -453,14 +451,14 @@ void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limi
     *L.counter += 1;
 }
 
-template <bool FWD, bool LOW>
+template <bool FWD>
 __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restrict__ order,
                                                     const int4* __restrict__ cface, const int2* __restrict__ lr,
                                                     const d4* __restrict__ fg0, const d4* __restrict__ W,
                                                     const double* __restrict__ swfc, const double* __restrict__ swra,
                                                     const d4* __restrict__ R, const double* __restrict__ D,
                                                     const double* __restrict__ invD, d4* dW1, d4* dW,
-                                                    unsigned* err) {
+                                                    unsigned* err, int poll_ns) {
     // One warp per cell.  Lanes 0..15: (face slot s, equation m); lanes 16..31
     // mirror them and only help with the divide (v = w3/w0 beside u = w2/w0).
     const double GM1 = 1.4 - 1.0;
@@ -496,7 +494,7 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
         double own = 0.0, dinv = 1.0;
         if (lane < 4) {
             own = FWD ? (&R[i].x)[m] : (&dW1[i].x)[m];
-            dinv = LOW ? invD[i] : D[i];
+            dinv = D[i];
         }
         // lanes without a contributing neighbour compute on harmless values and
         // are masked at the end, so the arithmetic below is issued once per warp
@@ -522,40 +520,26 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
                     atomicOr(err, ERR_TIMEOUT);
                     break;
                 }
+                if (poll_ns) __nanosleep(poll_ns);
             }
             dw[0] = a.x; dw[1] = a.y; dw[2] = b.x; dw[3] = b.y;
         }
         __syncwarp();  // reconverge before the arithmetic
-        double DF;
-        if (LOW) {
-            float wp0 = (float)w0[0] + (float)dw[0], wp1 = (float)w0[1] + (float)dw[1];
-            float wp2 = (float)w0[2] + (float)dw[2], wp3 = (float)w0[3] + (float)dw[3];
-            float nx = (float)g.x, ny = (float)g.y;
-            float u = wp2 / wp0, v = wp3 / wp0;
-            float vn = u * nx + v * ny;
-            float pr = (1.4f - 1.0f) * (wp1 - 0.5f * wp0 * (u * u + v * v));
-            float fcp = m == 0 ? wp0 * vn : m == 1 ? (wp1 + pr) * vn : m == 2 ? wp2 * vn + pr * nx : wp3 * vn + pr * ny;
-            float dwm = (float)(m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3]);
-            float dfc = left ? (fcp - (float)fc) : ((float)fc - fcp);
-            float df = 0.5f * (dfc - (float)rA * dwm) * (float)g.z;
-            DF = use ? (double)df : 0.0;
-        } else {
-            double wp[4];
+        double wp[4];
 #pragma unroll
-            for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
-            // one divide per half-warp, exchanged
-            double q = (hv ? wp[3] : wp[2]) / wp[0];
-            double u = __shfl_sync(0xffffffffu, q, lane & 15);
-            double v = __shfl_sync(0xffffffffu, q, (lane & 15) | 16);
-            double vn = dot2(u, v, g.x, g.y);
-            double pr = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
-            double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + pr) * vn : m == 2 ? wp[2] * vn + pr * g.x
-                                                                                   : wp[3] * vn + pr * g.y;
-            double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
-            double dfc = left ? (fcp - fc) : (fc - fcp);
-            double df = 0.5 * (dfc - rA * dwm) * g.z;
-            DF = use ? df : 0.0;
-        }
+        for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
+        // one divide per half-warp, exchanged
+        const double quo = (hv ? wp[3] : wp[2]) / wp[0];
+        const double u = __shfl_sync(0xffffffffu, quo, lane & 15);
+        const double v = __shfl_sync(0xffffffffu, quo, (lane & 15) | 16);
+        double vn = dot2(u, v, g.x, g.y);
+        double pr = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
+        double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + pr) * vn : m == 2 ? wp[2] * vn + pr * g.x
+                                                                               : wp[3] * vn + pr * g.y;
+        double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
+        double dfc = left ? (fcp - fc) : (fc - fcp);
+        double df = 0.5 * (dfc - rA * dwm) * g.z;
+        const double DF = use ? df : 0.0;
         // ordered sum over the 4 face slots (lanes m, m+4, m+8, m+12)
         double v0 = __shfl_sync(0xffffffffu, DF, m);
         double v1 = __shfl_sync(0xffffffffu, DF, 4 + m);
@@ -568,8 +552,8 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
         if (cf.w != 0) dF += v3;
         double res = 0.0;
         if (lane < 4) {
-            if (FWD) res = LOW ? (-own - dF) * dinv : (-own - dF) / dinv;
-            else res = LOW ? own - dF * dinv : own - dF / dinv;
+            if (FWD) res = (-own - dF) / dinv;
+            else res = own - dF / dinv;
         }
         double r1 = __shfl_sync(0xffffffffu, res, 1);
         double r2 = __shfl_sync(0xffffffffu, res, 2);
@@ -582,15 +566,13 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
     }
 }
 
-cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, bool low, int grid) {
+cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, int grid) {
     int nc = d.nc;
     const int* order = forward ? d.fwd_order : d.bwd_order;
     void* args[] = {(void*)&nc, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0, (void*)&d.W,
                     (void*)&d.swfc, (void*)&d.swra, (void*)&d.R, (void*)&d.diag, (void*)&d.invD, (void*)&d.dW1,
-                    (void*)&d.dW, (void*)&d.err};
-    void* fn;
-    if (forward) fn = low ? (void*)k_sweep_flow<true, true> : (void*)k_sweep_flow<true, false>;
-    else fn = low ? (void*)k_sweep_flow<false, true> : (void*)k_sweep_flow<false, false>;
+                    (void*)&d.dW, (void*)&d.err, (void*)&d.poll_ns};
+    void* fn = forward ? (void*)k_sweep_flow<true> : (void*)k_sweep_flow<false>;
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
     *L.counter += 1;
     return e;
@@ -613,7 +595,8 @@ __global__ void __launch_bounds__(256) k_sweep_pair64(int npos, const int* __res
                                                       const d4* __restrict__ fg0, const d4* __restrict__ W,
                                                       const double* __restrict__ swfc,
                                                       const double* __restrict__ swra, const d4* __restrict__ R,
-                                                      const double* __restrict__ D, d4* dW1, d4* dW, unsigned* err) {
+                                                      const double* __restrict__ D, d4* dW1, d4* dW, unsigned* err,
+                                                      int poll_ns) {
     const double GM1 = 1.4 - 1.0;
     const int lane = threadIdx.x & 31;
     const int h = lane >> 4, base = lane & 16;
@@ -663,6 +646,7 @@ __global__ void __launch_bounds__(256) k_sweep_pair64(int npos, const int* __res
                     atomicOr(err, ERR_TIMEOUT);
                     break;
                 }
+                if (poll_ns) __nanosleep(poll_ns);
             }
             dw[0] = a.x; dw[1] = a.y; dw[2] = b.x; dw[3] = b.y;
         }
@@ -706,7 +690,7 @@ cudaError_t launch_sweep_pair64(const DevArrays& d, const LaunchCfg& L, bool for
     const int* order = forward ? d.fwd_order2 : d.bwd_order2;
     void* args[] = {(void*)&npos, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0, (void*)&d.W,
                     (void*)&d.swfc, (void*)&d.swra, (void*)&d.R, (void*)&d.diag, (void*)&d.dW1, (void*)&d.dW,
-                    (void*)&d.err};
+                    (void*)&d.err, (void*)&d.poll_ns};
     void* fn = forward ? (void*)k_sweep_pair64<true> : (void*)k_sweep_pair64<false>;
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
     *L.counter += 1;
@@ -716,7 +700,7 @@ cudaError_t launch_sweep_pair64(const DevArrays& d, const LaunchCfg& L, bool for
 // ---------------------------------------------------------------------------
 // Fast-form dataflow sweep.  Same protocol as k_sweep_flow, but everything on
 // the dependence chain except the final update is binary32: float copies of
-// W (Wf), of the per-step SolveDF constants and of the increments (dW1f/dWf,
+// W (Wf), of the per-step r_A constants and of the increments (dW1f/dWf,
 // published beside the binary64 increments and polled instead of them), so
 // the binary64 pipe only sees the widening of the slot sum and
 // dW = (-R - sum) * (1/D).  Two cells per warp (16 lanes each): the cells of a
@@ -730,7 +714,7 @@ template <bool VISC, class MuT>
 __global__ void __launch_bounds__(256) k_sweep_prep32(int nc, const int4* __restrict__ cface, const int2* __restrict__ lr,
                                                       const float4* __restrict__ fg0f, const float4* __restrict__ fvisf,
                                                       const d4* __restrict__ W, const d4* __restrict__ U,
-                                                      const MuT* __restrict__ mu, float* __restrict__ swfcf,
+                                                      const MuT* __restrict__ mu,
                                                       float* __restrict__ swraf, float4* __restrict__ Wf,
                                                       float* __restrict__ dW1f, float* __restrict__ dWf) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -744,24 +728,21 @@ __global__ void __launch_bounds__(256) k_sweep_prep32(int nc, const int4* __rest
         Wf[i] = make_float4((float)w.x, (float)w.y, (float)w.z, (float)w.w);
     }
     int code = (&cface[i].x)[s];
-    float fc[4] = {0.f, 0.f, 0.f, 0.f}, rA = 0.f;
+    float rA = 0.f;
     if (code != 0) {
         int f = code_face(code);
         int2 e = lr[f];
         int j = code > 0 ? e.y : e.x;
         if (j >= 0) {
-            d4 wd = ld4(W + j), ud = ld4(U + j);
-            float w0[4] = {(float)wd.x, (float)wd.y, (float)wd.z, (float)wd.w};
+            d4 ud = ld4(U + j);
             float uj[4] = {(float)ud.x, (float)ud.y, (float)ud.z, (float)ud.w};
             float4 g = fg0f[f];
-            conv_flux_w<float>(w0, g.x, g.y, fc);
             float vn = uj[2] * g.x + uj[3] * g.y;
             float c = sqrtf(G * uj[1] / uj[0]);
             rA = 1.5f * (fabsf(vn) + c);
             if (VISC) rA += fmaxf(4.f / (3.f * uj[0]), G / uj[0]) * ((float)mu[i] / 0.72f) / sqrtf(fvisf[f].z);
         }
     }
-    reinterpret_cast<float4*>(swfcf)[t] = make_float4(fc[0], fc[1], fc[2], fc[3]);
     swraf[t] = rA;
 }
 
@@ -770,11 +751,11 @@ void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, b
     float* a = reinterpret_cast<float*>(d.dW1f);
     float* b = reinterpret_cast<float*>(d.dWf);
     if (viscous && mu64)
-        k_sweep_prep32<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.mu, d.swfcf, d.swraf, d.Wf, a, b);
+        k_sweep_prep32<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.mu, d.swraf, d.Wf, a, b);
     else if (viscous)
-        k_sweep_prep32<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muf, d.swfcf, d.swraf, d.Wf, a, b);
+        k_sweep_prep32<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muf, d.swraf, d.Wf, a, b);
     else
-        k_sweep_prep32<false, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, (const float*)nullptr, d.swfcf, d.swraf, d.Wf, a, b);
+        k_sweep_prep32<false, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, (const float*)nullptr, d.swraf, d.Wf, a, b);
     *L.counter += 1;
 }
 
@@ -782,9 +763,10 @@ template <bool FWD>
 __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __restrict__ order2,
                                                       const int4* __restrict__ cface, const int2* __restrict__ lr,
                                                       const float4* __restrict__ fg0f, const float4* __restrict__ Wf,
-                                                      const float* __restrict__ swfcf, const float* __restrict__ swraf,
+                                                      const float* __restrict__ swraf,
                                                       const d4* __restrict__ R, const double* __restrict__ invD,
-                                                      d4* dW1, d4* dW, float4* dW1f, float4* dWf, unsigned* err) {
+                                                      d4* dW1, d4* dW, float4* dW1f, float4* dWf, unsigned* err,
+                                                      int poll_ns) {
     const float GM1 = 1.4f - 1.0f;
     const int lane = threadIdx.x & 31;
     const int h = lane >> 4, base = lane & 16;
@@ -818,12 +800,19 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
         }
         float4 w0 = make_float4(1.f, 1.f, 0.f, 0.f), dw = make_float4(0.f, 0.f, 0.f, 0.f);
         float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-        float fc = 0.f, rA = 0.f;
+        float rA = 0.f;
+        // base values of the neighbour's flux, formed before the wait so that
+        // only the difference terms remain on the dependence chain
+        float u = 0.f, v = 0.f, vv = 0.f, p = 0.f, vn = 0.f;
         if (use) {
             w0 = Wf[j];
             g = fg0f[f];
-            fc = swfcf[(size_t)i * 16 + s * 4 + m];
             rA = swraf[(size_t)i * 4 + s];
+            u = w0.z / w0.x;
+            v = w0.w / w0.x;
+            vv = u * u + v * v;
+            p = GM1 * (w0.y - 0.5f * w0.x * vv);
+            vn = u * g.x + v * g.y;
             const float4* qf = (FWD ? dW1f : dWf) + j;
             long long it = 0;
             while (true) {
@@ -833,17 +822,29 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
                     atomicOr(err, ERR_TIMEOUT);
                     break;
                 }
+                if (poll_ns) __nanosleep(poll_ns);
             }
         }
         __syncwarp();
-        float wp0 = w0.x + dw.x, wp1 = w0.y + dw.y, wp2 = w0.z + dw.z, wp3 = w0.w + dw.w;
-        const float rr = 1.f / wp0;
-        float u = wp2 * rr, v = wp3 * rr;
-        float vn = u * g.x + v * g.y;
-        float pr = GM1 * (wp1 - 0.5f * wp0 * (u * u + v * v));
-        float fcp = m == 0 ? wp0 * vn : m == 1 ? (wp1 + pr) * vn : m == 2 ? wp2 * vn + pr * g.x : wp3 * vn + pr * g.y;
+        // F(W + dW) - F(W) as an exact difference: every term is a product of a
+        // difference with base or updated values, so its relative error does
+        // not grow as dW shrinks below W's binary32 resolution (subtracting two
+        // binary32 fluxes would leave a noise of ~1e-7 |F| that stalls the
+        // mixed form's convergence near a 5e-5 residual fall).
+        const float rho = w0.x, E = w0.y, mx = w0.z, my = w0.w;
+        const float d0 = dw.x, d1 = dw.y, d2 = dw.z, d3 = dw.w;
+        const float rp = 1.f / (rho + d0);
+        const float du = (d2 - u * d0) * rp, dv = (d3 - v * d0) * rp;
+        const float dq = du * (u + u + du) + dv * (v + v + dv);
+        const float dp = GM1 * (d1 - 0.5f * (d0 * (vv + dq) + rho * dq));
+        const float dvn = du * g.x + dv * g.y;
+        const float vnp = vn + dvn;
+        const float dfm = m == 0 ? d2 * g.x + d3 * g.y
+                        : m == 1 ? (d1 + dp) * vnp + (E + p) * dvn
+                        : m == 2 ? d2 * vnp + mx * dvn + dp * g.x
+                                 : d3 * vnp + my * dvn + dp * g.y;
         float dwm = m == 0 ? dw.x : m == 1 ? dw.y : m == 2 ? dw.z : dw.w;
-        float dfc = left ? (fcp - fc) : (fc - fcp);
+        float dfc = left ? dfm : -dfm;
         float DF = use ? 0.5f * (dfc - rA * dwm) * g.z : 0.f;
         float v0 = __shfl_sync(0xffffffffu, DF, base + m);
         float v1 = __shfl_sync(0xffffffffu, DF, base + 4 + m);
@@ -881,8 +882,8 @@ cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool for
     int npos = forward ? d.npos2_fwd : d.npos2_bwd;
     const int* order = forward ? d.fwd_order2 : d.bwd_order2;
     void* args[] = {(void*)&npos, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0f, (void*)&d.Wf,
-                    (void*)&d.swfcf, (void*)&d.swraf, (void*)&d.R, (void*)&d.invD, (void*)&d.dW1, (void*)&d.dW,
-                    (void*)&d.dW1f, (void*)&d.dWf, (void*)&d.err};
+                    (void*)&d.swraf, (void*)&d.R, (void*)&d.invD, (void*)&d.dW1, (void*)&d.dW,
+                    (void*)&d.dW1f, (void*)&d.dWf, (void*)&d.err, (void*)&d.poll_ns};
     void* fn = forward ? (void*)k_sweep_flow32<true> : (void*)k_sweep_flow32<false>;
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
     *L.counter += 1;
@@ -893,8 +894,8 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
     int dev = 0, sms = 0, per = 0, per2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    void* fn = low ? (void*)k_sweep_flow32<true> : (void*)k_sweep_flow<true, false>;
-    void* fn2 = low ? (void*)k_sweep_flow32<false> : (void*)k_sweep_flow<false, false>;
+    void* fn = low ? (void*)k_sweep_flow32<true> : (void*)k_sweep_flow<true>;
+    void* fn2 = low ? (void*)k_sweep_flow32<false> : (void*)k_sweep_flow<false>;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, fn2, 256, 0);
     per = per < per2 ? per : per2;

@@ -192,7 +192,11 @@ def run_to_drop(case: abi.Case, target: float, max_iters: int, mlp: abi.Mlp | No
     switch_at / switch_to: once the residual has fallen by switch_at, the case
     switches to the precision form switch_to (cfd_set_precision), e.g. from the
     binary32 form, whose residual stalls near 1e-4, to the mixed form."""
-    abi.case_track(case, True)
+    lusgs = case.advance == abi.ADV_LUSGS
+    if lusgs:
+        abi.case_track(case, True)
+    elif mlp is not None:
+        raise ValueError("the learned relaxation needs the LU-SGS integrator")
     case.step_graph(1)
     r0 = case.norm("L2_R_RHO")
     it, best, fell = 1, 1.0, False
