@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--drop-forms", default="fp64,fp32,mixed,mixed+learned,fp32>mixed+learned",
                     help="forms for time_to_drop: PREC[>PREC2][+learned]; '>' switches at --switch-at")
     ap.add_argument("--switch-at", type=float, default=1e-3, help="residual fall at which 'A>B' switches form")
+    ap.add_argument("--no-overset", action="store_true", help="skip the overset connectivity / exchange leg")
     return ap.parse_args()
 
 
@@ -174,6 +175,86 @@ def traffic_bytes(pass_name: str, precision: str, nc: int):
 
 
 # ---------------------------------------------------------------------------
+def overset_leg(stream) -> dict:
+    """Overset connectivity and fringe exchange at the two-component size: a
+    1024 x 1024 Cartesian background on [-10, 10]^2 and a 512 x 128 O-grid
+    around a unit cylinder out to r = 1.5 (synthetic, no dataset).  Times the
+    device connectivity (bins, hole map, blanking of the background's nodes,
+    donor search of both receptor sets) and one fringe exchange each way, and
+    checks size-independent properties: weights in [-TOL, 1+TOL] summing to 1,
+    and exact interpolation of a linear field."""
+    import numpy as np
+    import torch
+
+    from tmp_gb300 import abi, meshgen
+
+    bg_m = meshgen.cart_mesh(1024, 1024, (-10.0, -10.0), (10.0, 10.0))
+    og_m = meshgen.o_mesh(512, 128, r0=0.5, dr1=1e-3, rout=1.5)
+    paths = []
+    meshes = []
+    for m, name in ((bg_m, "bg"), (og_m, "og")):
+        p = Path(tempfile.gettempdir()) / f"tmp_gb300_overset_{name}.grd"
+        meshgen.write_grd(p, m)
+        paths.append(p)
+        meshes.append(abi.Mesh.load_grd(p, m.wall_tag, m.far_tag))
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    out = {"workload": "Cartesian 1024x1024 + O-grid 512x128 (r 0.5 to 1.5)",
+           "cells": [meshes[0].ncell, meshes[1].ncell], "nodes": [meshes[0].nnode, meshes[1].nnode]}
+    t0, t1 = ev(), ev()
+    t0.record(stream)
+    bg, og = abi.Block(meshes[0], stream.cuda_stream), abi.Block(meshes[1], stream.cuda_stream)
+    hm = abi.HoleMap(og)
+    iblank, mand = abi.overset_blank(bg, [og], [hm], nfringe=2)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    out["connectivity_ms"] = round(t0.elapsed_time(t1), 3)
+    out["holes"] = int((iblank == 0).sum())
+    out["mandatory"] = int(mand.sum())
+    bxy = bg_m.xy
+    oxy = og_m.xy
+    rec_b = np.flatnonzero(mand == 1).astype(np.int32)
+    r = np.hypot(oxy[:, 0], oxy[:, 1])
+    rec_o = np.flatnonzero(r > 1.5 - 1e-9).astype(np.int32)
+    t0.record(stream)
+    it_b = abi.Interp.search(og, bxy[rec_b], rec_b)   # background fringe <- O-grid
+    it_o = abi.Interp.search(bg, oxy[rec_o], rec_o)   # O-grid outer ring <- background
+    t1.record(stream)
+    torch.cuda.synchronize()
+    out["search_ms"] = round(t0.elapsed_time(t1), 3)
+    out["receptors"] = [int(it_b.info()[0]), int(it_o.info()[0])]
+    out["receptors_requested"] = [int(rec_b.size), int(rec_o.size)]
+    # properties: convex weights summing to 1, linear fields reproduced
+    ok = True
+    for itp, src_xy, rec_xy in ((it_b, oxy, bxy), (it_o, bxy, oxy)):
+        recv, _, inode, w = itp.get()
+        nw = np.where(inode[:, 3] < 0, 3, 4)
+        wsum = w.sum(1)
+        ok &= bool(np.all(w >= -1e-10) and np.all(w <= 1 + 1e-10) and np.max(np.abs(wsum - 1)) < 1e-12)
+        lin = lambda xy: 1.0 + 0.3 * xy[:, 0] - 0.7 * xy[:, 1]  # noqa: E731
+        q = lin(src_xy)
+        est = np.array([np.dot(w[i, :nw[i]], q[inode[i, :nw[i]]]) for i in range(0, len(recv), max(1, len(recv) // 2000))])
+        ref = lin(rec_xy[recv[:: max(1, len(recv) // 2000)]])
+        ok &= bool(np.max(np.abs(est - ref)) < 1e-11 * max(1.0, np.abs(ref).max()))
+    out["properties_ok"] = ok
+    # one fringe exchange each way, ROW layout, 4 variables per node
+    qb = torch.rand(4 * meshes[0].nnode, dtype=torch.float64, device="cuda")
+    qo = torch.rand(4 * meshes[1].nnode, dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        it_b.update(qo.data_ptr(), meshes[1].nnode, qb.data_ptr(), meshes[0].nnode, 4, stream=stream.cuda_stream)
+        it_o.update(qb.data_ptr(), meshes[0].nnode, qo.data_ptr(), meshes[1].nnode, 4, stream=stream.cuda_stream)
+    reps = 100
+    t0.record(stream)
+    for _ in range(reps):
+        it_b.update(qo.data_ptr(), meshes[1].nnode, qb.data_ptr(), meshes[0].nnode, 4, stream=stream.cuda_stream)
+        it_o.update(qb.data_ptr(), meshes[0].nnode, qo.data_ptr(), meshes[1].nnode, 4, stream=stream.cuda_stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    out["exchange_us"] = round(1e3 * t0.elapsed_time(t1) / reps, 2)
+    for p in paths:
+        p.unlink()
+    return out
+
+
 def cpu_baseline(grd_path: str, w, seconds: float) -> dict:
     """C restatement of the reference's serial LU-SGS path on one host core."""
     import oracle
@@ -290,7 +371,7 @@ def run_ours(args):
                      sweep_poll_ns=args.sweep_poll_ns)
         c.init_freestream()
         c.tuned = None
-        if args.sweep_bpsm == 0 and w.advance == "lusgs" and args.sweep_mode in (0, 3):
+        if args.sweep_bpsm == 0 and w.advance == "lusgs" and args.sweep_mode in (0, 3, 4):
             c.tuned = c.autotune(3)[0]  # the sweeps' blocks per SM, by timing whole steps
         return c
 
@@ -406,7 +487,7 @@ def run_ours(args):
         per_step = {p: 5 * v for p, v in per.items()}
     dominant = max(per_step, key=per_step.get)
     nlev = mesh.levels()
-    per_level = args.sweep_mode != 0  # modes 1 and 2 launch once per level; the dataflow sweep once per direction
+    per_level = args.sweep_mode in (1, 2)  # modes 1 and 2 launch once per level; the dataflow sweeps once per direction
     launches_of = {"sweep_fwd": nlev[0] if per_level else 1, "sweep_bwd": nlev[1] if per_level else 1}
     peak, peak_kind = measured_peak_gbs()
     rows = {}
@@ -449,6 +530,8 @@ def run_ours(args):
                        "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "forms": forms,
             "time_to_drop": drop}
+    if rank == 0 and not args.no_overset:
+        line["overset"] = overset_leg(stream)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(str(path), w, args.cpu_seconds)
     if rank == 0:

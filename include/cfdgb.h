@@ -115,7 +115,9 @@ typedef struct {
                           1 one launch per level, one thread per cell,
                           2 one launch per level, 16 lanes per cell,
                           3 dataflow with two cells per warp (binary64 form;
-                          measured 6% slower per step than 0 on C2)              */
+                          measured 6% slower per step than 0 on C2),
+                          4 binary32 dataflow whose two half-warps wait and
+                          exchange independently                                */
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
                                 the occupancy limit)                             */
     int sweep_poll_ns; /* dataflow sweep: pause between polls of a neighbour's

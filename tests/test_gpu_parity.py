@@ -301,3 +301,24 @@ def test_wall_force_and_distance(name, built_oracle):
     scale = max(abs(fo[0]), abs(fo[1]))
     assert abs(f["fx"] - fo[0]) <= 1e-12 * scale and abs(f["fy"] - fo[1]) <= 1e-12 * scale
     assert np.isfinite(f["cl"]) and np.isfinite(f["cd"])
+
+
+@pytest.mark.parametrize("prec", ["FP32", "MIXED"])
+def test_fast_sweep_independent_halves_bitwise(prec):
+    """The binary32 dataflow sweep with independently synchronising half-warps
+    (sweep_mode 4) computes every cell with the same arithmetic as the default
+    one: identical bits after the fixture's steps."""
+    from tmp_gb300 import abi
+
+    c, g = manifest()["mixed_lam_lusgs"], golden("mixed_lam_lusgs")
+    m = abi.Mesh.load_grd(GOLDEN / c["mesh"], c["wall_tag"], c["far_tag"])
+    out = []
+    for sm in (0, 4):
+        case = abi.Case([m], [dict(mach=c["mach"], aoa_deg=c["aoa"], reynolds=c["re"])], abi.FLOW_LAMINAR,
+                        abi.ADV_LUSGS, getattr(abi, f"PREC_{prec}"), cfl=c["cfl"], sweep_mode=sm)
+        case.put("U", g["init_U"])
+        case.step(3)
+        case.sync()
+        out.append((case.get("U"), case.get("DW1"), case.get("DW")))
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)

@@ -167,7 +167,7 @@ void sweeps(cfd_case_s* c, bool forward) {
             launch_sweep_level(d, L, c->viscous(), forward, ptr[k], ptr[k + 1], c->fp32());
         return;
     }
-    const bool dataflow = c->p.sweep_mode == 0 || c->p.sweep_mode == 3;
+    const bool dataflow = c->p.sweep_mode == 0 || c->p.sweep_mode >= 3;
     if (forward && !(c->fast_sweep() && dataflow))
         launch_sweep_prep(d, L, c->viscous(), c->fp32(), dataflow);
     if (c->p.sweep_mode == 2) {
@@ -180,7 +180,7 @@ void sweeps(cfd_case_s* c, bool forward) {
             launch_inv_diag(d, L);
             launch_sweep_prep32(d, L, c->viscous(), c->mixed());
         }
-        ck(launch_sweep_flow32(d, L, forward, d.flow_grid), "cooperative sweep launch");
+        ck(launch_sweep_flow32(d, L, forward, d.flow_grid, c->p.sweep_mode == 4), "cooperative sweep launch");
     } else if (c->p.sweep_mode == 3) {
         ck(launch_sweep_pair64(d, L, forward, d.flow_grid), "cooperative sweep launch");
     } else {
@@ -744,7 +744,7 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
     bool visc = c->viscous(), f32 = c->fp32();
     for (int r = 0; r < reps; r++) {
         // a lone backward sweep needs the "not yet computed" markers the forward pass sets
-        if (pass == 5 && (c->p.sweep_mode == 0 || c->p.sweep_mode == 3)) {
+        if (pass == 5 && (c->p.sweep_mode == 0 || c->p.sweep_mode >= 3)) {
             if (c->fast_sweep()) launch_sweep_prep32(d, L, visc, c->mixed());
             else launch_sweep_prep(d, L, visc, f32, true);
         }

@@ -759,7 +759,7 @@ void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, b
     *L.counter += 1;
 }
 
-template <bool FWD>
+template <bool FWD, bool IND>
 __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __restrict__ order2,
                                                       const int4* __restrict__ cface, const int2* __restrict__ lr,
                                                       const float4* __restrict__ fg0f, const float4* __restrict__ Wf,
@@ -776,6 +776,9 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
     d4* dst = FWD ? dW1 : dW;
     float4* dstf = FWD ? dW1f : dWf;
     const int npairs = npos >> 1;
+    // IND: the two half-warps synchronise and exchange only among themselves,
+    // so a cell whose neighbours are ready does not wait for its pair partner
+    const unsigned mask = IND ? (h ? 0xffff0000u : 0x0000ffffu) : 0xffffffffu;
     const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
     for (long long q = q0;; q += NW) {
         const long long P = (long long)blockIdx.x + (long long)B * q;  // pair index, same mapping as k_sweep_flow
@@ -825,7 +828,7 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
                 if (poll_ns) __nanosleep(poll_ns);
             }
         }
-        __syncwarp();
+        __syncwarp(mask);
         // F(W + dW) - F(W) as an exact difference: every term is a product of a
         // difference with base or updated values, so its relative error does
         // not grow as dW shrinks below W's binary32 resolution (subtracting two
@@ -846,10 +849,10 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
         float dwm = m == 0 ? dw.x : m == 1 ? dw.y : m == 2 ? dw.z : dw.w;
         float dfc = left ? dfm : -dfm;
         float DF = use ? 0.5f * (dfc - rA * dwm) * g.z : 0.f;
-        float v0 = __shfl_sync(0xffffffffu, DF, base + m);
-        float v1 = __shfl_sync(0xffffffffu, DF, base + 4 + m);
-        float v2 = __shfl_sync(0xffffffffu, DF, base + 8 + m);
-        float v3 = __shfl_sync(0xffffffffu, DF, base + 12 + m);
+        float v0 = __shfl_sync(mask, DF, base + m);
+        float v1 = __shfl_sync(mask, DF, base + 4 + m);
+        float v2 = __shfl_sync(mask, DF, base + 8 + m);
+        float v3 = __shfl_sync(mask, DF, base + 12 + m);
         float dF = 0.f;
         if (cf.x != 0) dF += v0;
         if (cf.y != 0) dF += v1;
@@ -861,15 +864,15 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
         // the critical path.
         const float ownf = (float)own, dinvf = (float)dinv;
         const float resf = FWD ? (-ownf - dF) * dinvf : ownf - dF * dinvf;
-        float f1 = __shfl_sync(0xffffffffu, resf, base + 1);
-        float f2 = __shfl_sync(0xffffffffu, resf, base + 2);
-        float f3 = __shfl_sync(0xffffffffu, resf, base + 3);
+        float f1 = __shfl_sync(mask, resf, base + 1);
+        float f2 = __shfl_sync(mask, resf, base + 2);
+        float f3 = __shfl_sync(mask, resf, base + 3);
         if (active && (lane & 15) == 0) __stcg(dstf + i, make_float4(resf, f1, f2, f3));
         double res = 0.0;
         if (s == 0) res = FWD ? (-own - (double)dF) * dinv : own - (double)dF * dinv;
-        double r1 = __shfl_sync(0xffffffffu, res, base + 1);
-        double r2 = __shfl_sync(0xffffffffu, res, base + 2);
-        double r3 = __shfl_sync(0xffffffffu, res, base + 3);
+        double r1 = __shfl_sync(mask, res, base + 1);
+        double r2 = __shfl_sync(mask, res, base + 2);
+        double r3 = __shfl_sync(mask, res, base + 3);
         if (active && (lane & 15) == 0) {
             double2* o = reinterpret_cast<double2*>(dst + i);
             __stcg(o, make_double2(res, r1));
@@ -878,13 +881,14 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
     }
 }
 
-cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid) {
+cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool independent) {
     int npos = forward ? d.npos2_fwd : d.npos2_bwd;
     const int* order = forward ? d.fwd_order2 : d.bwd_order2;
     void* args[] = {(void*)&npos, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0f, (void*)&d.Wf,
                     (void*)&d.swraf, (void*)&d.R, (void*)&d.invD, (void*)&d.dW1, (void*)&d.dW,
                     (void*)&d.dW1f, (void*)&d.dWf, (void*)&d.err, (void*)&d.poll_ns};
-    void* fn = forward ? (void*)k_sweep_flow32<true> : (void*)k_sweep_flow32<false>;
+    void* fn = independent ? (forward ? (void*)k_sweep_flow32<true, true> : (void*)k_sweep_flow32<false, true>)
+                           : (forward ? (void*)k_sweep_flow32<true, false> : (void*)k_sweep_flow32<false, false>);
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
     *L.counter += 1;
     return e;
@@ -894,11 +898,17 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
     int dev = 0, sms = 0, per = 0, per2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    void* fn = low ? (void*)k_sweep_flow32<true> : (void*)k_sweep_flow<true>;
-    void* fn2 = low ? (void*)k_sweep_flow32<false> : (void*)k_sweep_flow<false>;
+    void* fn = low ? (void*)k_sweep_flow32<true, false> : (void*)k_sweep_flow<true>;
+    void* fn2 = low ? (void*)k_sweep_flow32<false, false> : (void*)k_sweep_flow<false>;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, fn2, 256, 0);
     per = per < per2 ? per : per2;
+    if (low) {  // the independent-halves variant runs on the same grid
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_flow32<true, true>, 256, 0);
+        per = per < per2 ? per : per2;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_flow32<false, true>, 256, 0);
+        per = per < per2 ? per : per2;
+    }
     if (!low) {  // the plain form's paired kernels run on the same grid
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_pair64<true>, 256, 0);
         per = per < per2 ? per : per2;
