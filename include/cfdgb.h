@@ -117,7 +117,8 @@ typedef struct {
                           3 dataflow with two cells per warp (binary64 form;
                           measured 6% slower per step than 0 on C2),
                           4 binary32 dataflow whose two half-warps wait and
-                          exchange independently                                */
+                          exchange independently (measured 7-10% slower per step
+                          than 0: the diverged halves issue one after the other) */
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
                                 the occupancy limit)                             */
     int sweep_poll_ns; /* dataflow sweep: pause between polls of a neighbour's
@@ -311,6 +312,11 @@ void cfd_holemap_free(cfd_holemap_t h);
  * 0.  Host output arrays of the block's node count; mandatory may be NULL. */
 int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, const cfd_holemap_t* maps,
                       int nfringe, int* iblank, int* mandatory);
+/* Cell blanking from node blanking (MeshBlock::getCellIblanks,
+ * bookkeeping.cpp:654-705): cell_iblank[c] = 0 if any of its nodes is 0 (hole),
+ * -1 if all of its nodes are -1 (receptors), else 1.  Host arrays of the
+ * block's node / cell counts. */
+int cfd_cell_iblank(cfd_block_t b, const int* node_iblank, int* cell_iblank);
 
 /* ---- SST k-omega (SSTkomegaModel, UnstructSolver/SSTKWStrategy.h) -------- */
 /* The reference builds this model but never runs it (ViscousFlow2D's serial

@@ -227,3 +227,19 @@ def wall_nodes(topo):
     lr = topo.lr.reshape(-1, 2)
     en = topo.edge_nodes.reshape(-1, 2)
     return np.unique(en[lr[:, 1] == -2].reshape(-1)).astype(np.int32)
+
+
+def cell_iblank(cell_verts, cell_nvert, node_iblank):
+    """MeshBlock::getCellIblanks (bookkeeping.cpp:654-705): 0 if any node is 0,
+    else -1 if every node is -1, else 1 (nodes visited in vertex order)."""
+    cv = np.asarray(cell_verts).reshape(-1, 4)
+    ibl = np.asarray(node_iblank)
+    out = np.ones(len(cv), np.int32)
+    for c in range(len(cv)):
+        n = int(cell_nvert[c])
+        vals = ibl[cv[c, :n]]
+        if np.any(vals == 0):
+            out[c] = 0
+        elif np.all(vals == -1):
+            out[c] = -1
+    return out

@@ -37,7 +37,7 @@ for p in "${pids[@]}"; do wait "$p"; done
 # the overset search, weights and data update (UniTioga + mathTools) in a second driver
 # (MeshBlock.cpp reaches MPI types only through its HDF5 writer: the MPI stand-in is force-included)
 OVS=(UniTioga/search UniTioga/utils UniTioga/ADT UniTioga/recursiveADT UniTioga/checkContainment
-     UniTioga/dataUpdate UniTioga/MeshBlock UniTioga/write UniTioga/linkList UniTioga/holeMap
+     UniTioga/dataUpdate UniTioga/MeshBlock UniTioga/write UniTioga/linkList UniTioga/holeMap UniTioga/bookkeeping
      mathTools/math mathTools/median mathTools/kaiser)
 OOBJS=()
 pids=()

@@ -21,6 +21,8 @@
 //     (utils.cpp:645-670) of the points
 //     WALL: int32 isym, nwall; int32 wall_nodes[nwall] (0-based)
 //     OUT:  int32 nx[2]; double extents[4]; int32 sam[nx*ny]; int32 inside[n]
+//   ref_overset celliblank MESH IBL OUT   MeshBlock::getCellIblanks (UniTioga/bookkeeping.cpp:654-705)
+//     IBL: int32 iblank[nnode];  OUT: int32 iblank_cell[ncell] in the mesh's own cell numbering
 #include <cstdio>
 #include <cstdlib>
 #include <stdexcept>
@@ -194,6 +196,27 @@ static int do_holemap(const char* meshf, const char* wallf, const char* ptsf, co
     return 0;  // tg and the block are left allocated: the driver exits next
 }
 
+static int do_celliblank(const char* meshf, const char* iblf, const char* out) {
+    static BlockData d;
+    if (!read_block(meshf, d)) return 3;
+    static std::vector<int> ibl(d.nnode);
+    FILE* fi = fopen(iblf, "rb");
+    if (!fi || !rd(fi, ibl.data(), ibl.size())) return 3;
+    fclose(fi);
+    MeshBlock* mb = make_block(d);
+    mb->iblank = ibl.data();
+    mb->iblank_reduced = nullptr;
+    mb->iblank_cell = nullptr;
+    mb->getCellIblanks();
+    std::vector<int> res(d.ncell);
+    for (int k = 0; k < d.ncell; k++) res[d.order[k]] = mb->iblank_cell[k];
+    FILE* fo = fopen(out, "wb");
+    if (!fo) return 4;
+    fwrite(res.data(), 4, res.size(), fo);
+    fclose(fo);
+    return 0;
+}
+
 static int do_interp(const char* listf, const char* out) {
     FILE* fl = fopen(listf, "rb");
     if (!fl) return 3;
@@ -262,6 +285,7 @@ int main(int argc, char** argv) {
     if (mode == "search" && argc == 5) return do_search(argv[2], argv[3], argv[4]);
     if (mode == "interp" && argc == 4) return do_interp(argv[2], argv[3]);
     if (mode == "holemap" && argc == 6) return do_holemap(argv[2], argv[3], argv[4], argv[5]);
+    if (mode == "celliblank" && argc == 5) return do_celliblank(argv[2], argv[3], argv[4]);
     fprintf(stderr, "bad arguments\n");
     return 2;
 }

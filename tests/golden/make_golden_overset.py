@@ -16,6 +16,8 @@ mathTools sources by oracle/build_ref.sh) on seeded inputs:
   holemap   tioga::getHoleMap (markWallBoundary + fillHoleMap) of each golden
             mesh's walls for isym = 3, 1, 2, and checkHoleMap of random points
             and of the other mesh's nodes
+  celliblank MeshBlock::getCellIblanks of random node blanking (holes,
+            receptors, field nodes in clusters) on both golden meshes
 
 usage: python tests/golden/make_golden_overset.py [REFERENCE_ROOT]
 """
@@ -206,6 +208,23 @@ def main():
                 out.update({f"h_{name}_{isym}_nx": nxy, f"h_{name}_{isym}_ext": geo,
                             f"h_{name}_{isym}_sam": sam, f"h_{name}_{isym}_in": inside})
             out[f"h_{name}_pts"] = pts
+        for name, m in (("mx", mx), ("om", om)):
+            xy = m.xy.reshape(-1, 2)
+            # clustered blanking: holes near one point, receptors in a ring around it
+            c0 = xy[rng.integers(m.nnode)]
+            dist = np.hypot(*(xy - c0).T)
+            r0 = np.quantile(dist, 0.1)
+            ibl = np.ones(m.nnode, np.int32)
+            ibl[dist < r0] = 0
+            ring = (dist >= r0) & (dist < 1.6 * r0)
+            ibl[ring] = -1
+            flip = rng.random(m.nnode) < 0.03
+            ibl[flip] = rng.choice([-1, 0, 1], flip.sum())
+            write_mesh(td / "m.bin", m)
+            ibl.tofile(td / "ibl.bin")
+            _run("celliblank", td / "m.bin", td / "ibl.bin", td / "c.out", cwd=td)
+            out[f"c_{name}_node"] = ibl
+            out[f"c_{name}_cell"] = np.fromfile(td / "c.out", np.int32)
     np.savez_compressed(HERE / "overset.npz", **out)
     print(f"wrote {HERE / 'overset.npz'}: {nv.size} weight cases, "
           f"{sum(v.size for k, v in out.items() if k.endswith('_donor'))} search points")

@@ -258,3 +258,10 @@ def test_overset_edge_cases(built_lib):
     assert np.all(d >= 0) and np.allclose(w.sum(1), 1.0, atol=1e-14)
     with pytest.raises(abi.CfdError):
         abi.HoleMap(blk, isym=7)
+
+
+def test_cell_iblank_matches_reference(built_lib, ov):
+    from tmp_gb300 import abi
+
+    for name, (mesh, blk, topo) in _blocks(abi).items():
+        assert np.array_equal(blk.cell_iblank(ov[f"c_{name}_node"]), ov[f"c_{name}_cell"])

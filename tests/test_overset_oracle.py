@@ -72,3 +72,10 @@ def test_holemap_bitwise(ov, isym):
         inside = oracle.holemap_check(nxy, geo, sam, ov[f"h_{name}_pts"])
         assert np.array_equal(inside, ov[f"h_{name}_{isym}_in"])
         assert 0 < inside.sum() < inside.size
+
+
+def test_cell_iblank(ov):
+    for name, m in _meshes().items():
+        got = oracle.cell_iblank(m.cell_verts, m.cell_nvert, ov[f"c_{name}_node"])
+        assert np.array_equal(got, ov[f"c_{name}_cell"])
+        assert set(np.unique(got)) == {-1, 0, 1}

@@ -116,6 +116,7 @@ def lib() -> C.CDLL:
         "cfd_holemap_check": (C.c_int, [vp, C.c_longlong, dp, ip]),
         "cfd_holemap_free": (None, [vp]),
         "cfd_overset_blank": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.POINTER(vp), C.c_int, ip, ip]),
+        "cfd_cell_iblank": (C.c_int, [vp, ip, ip]),
         "cfd_mlp_create": (C.c_int, [C.c_ulonglong, C.POINTER(vp)]),
         "cfd_mlp_free": (None, [vp]),
         "cfd_mlp_get_params": (C.c_int, [vp, fp, fp]),
@@ -351,6 +352,15 @@ class Block:
         w = np.zeros(4 * n)
         check(lib().cfd_block_search(self.h, n, _dptr(p), _iptr(d), _iptr(nodes), _dptr(w)))
         return d, nodes.reshape(n, 4), w.reshape(n, 4)
+
+    def cell_iblank(self, node_iblank: np.ndarray) -> np.ndarray:
+        """getCellIblanks: 0 if any node is a hole, -1 if all nodes are receptors, else 1."""
+        n = np.ascontiguousarray(node_iblank, dtype=np.int32)
+        if n.size != self.nnode:
+            raise ValueError("node_iblank needs one value per node")
+        out = np.zeros(self.ncell, np.int32)
+        check(lib().cfd_cell_iblank(self.h, _iptr(n), _iptr(out)))
+        return out
 
     def node_to_cell(self, q_node_ptr: int, nvar: int, q_cell_ptr: int, stream: int | None = None):
         """Device arrays (raw pointers) in ROW layout."""

@@ -520,6 +520,29 @@ __global__ void k_hole_check(long long n, const double* __restrict__ pts, MapGeo
     inside[i] = hole_at(pts[2 * i], pts[2 * i + 1], g, sam);
 }
 
+// getCellIblanks (bookkeeping.cpp:654-705): a cell is a hole (0) if any of
+// its nodes is, a receptor (-1) if all of its nodes are, else a field cell (1).
+__global__ void k_cell_iblank(int ncell, const int4* __restrict__ cv, const int* __restrict__ ibl,
+                              int* __restrict__ icell) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int4 v = cv[c];
+    const int nv = v.w < 0 ? 3 : 4;
+    const int id[4] = {v.x, v.y, v.z, v.w};
+    int out = 1, nrec = 0;
+    for (int m = 0; m < 4; m++) {
+        if (m >= nv) break;
+        const int b = ibl[id[m]];
+        if (b == 0) {
+            out = 0;
+            break;
+        }
+        nrec += b == -1;
+    }
+    if (out != 0 && nrec == nv) out = -1;
+    icell[c] = out;
+}
+
 // processDonors' hole test for one other block: a node without a donor cell
 // in that block and inside its map is blanked.
 __global__ void k_blank_nodes(int n, const double* __restrict__ xy, const int* __restrict__ donor, MapGeom g,
@@ -1143,6 +1166,27 @@ int cfd_holemap_check(cfd_holemap_t h, long long n, const double* xy, int* insid
 }
 
 void cfd_holemap_free(cfd_holemap_t h) { delete h; }
+
+int cfd_cell_iblank(cfd_block_t b, const int* node_iblank, int* cell_iblank) {
+    if (!b || !node_iblank || !cell_iblank) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_cell_iblank: null argument");
+    int *d_n = nullptr, *d_c = nullptr;
+    int rc = CFD_OK;
+    try {
+        cudaStream_t s = b->stream;
+        dalloc(&d_n, b->nnode);
+        dalloc(&d_c, b->ncell);
+        ck(cudaMemcpyAsync(d_n, node_iblank, b->nnode * sizeof(int), cudaMemcpyHostToDevice, s), "copy");
+        k_cell_iblank<<<blocks_for(b->ncell, 256), 256, 0, s>>>(b->ncell, b->cv, d_n, d_c);
+        ck(cudaGetLastError(), "k_cell_iblank");
+        ck(cudaMemcpyAsync(cell_iblank, d_c, b->ncell * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+        ck(cudaStreamSynchronize(s), "sync");
+    } catch (const OversetError& e) {
+        rc = report(e);
+    }
+    dfree(d_n);
+    dfree(d_c);
+    return rc;
+}
 
 int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, const cfd_holemap_t* maps,
                       int nfringe, int* iblank, int* mandatory) {
