@@ -69,6 +69,8 @@ def parse():
                     help="forms for time_to_drop: PREC[>PREC2][+learned]; '>' switches at --switch-at")
     ap.add_argument("--switch-at", type=float, default=1e-3, help="residual fall at which 'A>B' switches form")
     ap.add_argument("--no-overset", action="store_true", help="skip the overset connectivity / exchange leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch leg (256 packed cases)")
+    ap.add_argument("--batch-meshes", type=int, default=256, help="meshes in the uneven-batch leg")
     return ap.parse_args()
 
 
@@ -253,6 +255,80 @@ def overset_leg(stream) -> dict:
     for p in paths:
         p.unlink()
     return out
+
+
+def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5) -> dict:
+    """The uneven batch: `nmesh` independent meshes of 5k-200k cells (sizes
+    log-uniform from a seed, cylinder or NACA 0012 bodies, quads + triangles),
+    half Euler and half viscous, advanced by LU-SGS.  Each flow family is one
+    packed case (all its meshes concatenated: one launch per pass, the sweep
+    levels of all meshes merged, blocks per SM autotuned, steps replayed from a
+    CUDA graph); the same meshes are then advanced as separate cases one after
+    another, and once more packed with the learned relaxation attached."""
+    import torch
+
+    from tmp_gb300 import abi, configs, learn
+
+    cases = configs.c5_cases(nmesh)
+    grds = configs.c5_meshes(cases)
+    meshes = [abi.Mesh.from_arrays(g.xy, g.edge_nodes, g.edge_cells, g.ncell, g.wall_tag, g.far_tag) for g in grds]
+    del grds
+    groups = {}
+    for bc, m in zip(cases, meshes):
+        groups.setdefault(bc.flow, []).append((m, dict(mach=bc.mach, aoa_deg=bc.aoa, reynolds=bc.re)))
+    flow_code = dict(euler=abi.FLOW_EULER, laminar=abi.FLOW_LAMINAR)
+    cfl = 10.0
+    ncell = sum(m.ncell for m in meshes)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def run(case_list):
+        for c in case_list:
+            c.init_freestream()
+            c.step_graph(2)
+        torch.cuda.synchronize()
+        t0, t1 = ev(), ev()
+        t0.record(stream)
+        for c in case_list:
+            c.step_graph(steps)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        for c in case_list:
+            try:
+                c.sync()
+            except abi.CfdError as ex:
+                errors.append(str(ex))
+        return t0.elapsed_time(t1) / steps
+
+    errors: list[str] = []
+    packed = [abi.Case([m for m, _ in g], [f for _, f in g], flow_code[fl], abi.ADV_LUSGS, precision, cfl=cfl,
+                       stream=stream.cuda_stream) for fl, g in groups.items()]
+    tuned = [c.autotune(2)[0] for c in packed]
+    ms_packed = run(packed)
+    net = learn.load()
+    ms_learned = None
+    if net is not None:
+        for c in packed:
+            abi.case_track(c, True)
+            abi.case_set_mlp(c, net, False)
+        ms_learned = run(packed)
+    for c in packed:
+        c.close()
+    separate = [abi.Case([m], [f], flow_code[fl], abi.ADV_LUSGS, precision, cfl=cfl, stream=stream.cuda_stream)
+                for fl, g in groups.items() for m, f in g]
+    ms_sep = run(separate)
+    for c in separate:
+        c.close()
+    levels = [m.levels()[0] for m in meshes]
+    sizes = sorted(m.ncell for m in meshes)
+    return {"workload": f"{nmesh} meshes, 5k-200k cells log-uniform (seed 5005), half Euler / half laminar, LU-SGS CFL {cfl:g}",
+            "meshes": nmesh, "cells": ncell, "cells_min_median_max": [sizes[0], sizes[len(sizes) // 2], sizes[-1]],
+            "packed_cases": {fl: len(g) for fl, g in groups.items()}, "sweep_blocks_per_sm": tuned,
+            "forward_levels_max_sum": [max(levels), sum(levels)], "steps": steps,
+            "packed_ms_per_step": round(ms_packed, 3), "packed_cell_iters_per_s": ncell / (ms_packed * 1e-3),
+            "packed_learned_ms_per_step": round(ms_learned, 3) if ms_learned else None,
+            "packed_learned_cell_iters_per_s": ncell / (ms_learned * 1e-3) if ms_learned else None,
+            "separate_ms_per_step": round(ms_sep, 3), "separate_cell_iters_per_s": ncell / (ms_sep * 1e-3),
+            "solver_errors": sorted(set(errors))}
 
 
 def cpu_baseline(grd_path: str, w, seconds: float) -> dict:
@@ -532,6 +608,11 @@ def run_ours(args):
             "time_to_drop": drop}
     if rank == 0 and not args.no_overset:
         line["overset"] = overset_leg(stream)
+    if rank == 0 and not args.no_batch and w.advance == "lusgs":
+        try:
+            line["batch"] = batch_leg(stream, prec_code[args.precision], args.batch_meshes)
+        except Exception as ex:  # the leg is reported beside the headline, never instead of it
+            line["batch"] = {"error": f"{type(ex).__name__}: {ex}"}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(str(path), w, args.cpu_seconds)
     if rank == 0:

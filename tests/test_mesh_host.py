@@ -105,3 +105,23 @@ def test_reference_shipped_mesh_if_present(built_lib):
         pytest.skip("reference meshes not present")
     m = abi.Mesh.load_grd(p, -1, -2)
     assert (m.nnode, m.nedge, m.ncell) == (40359, 80308, 39949)
+
+
+def test_uneven_batch_definition():
+    """The uneven batch: seeded, sizes log-uniform within the bounds, the
+    generated meshes near their target sizes, half Euler and half viscous."""
+    from tmp_gb300 import configs
+
+    a, b = configs.c5_cases(), configs.c5_cases()
+    assert a == b and len(a) == 256
+    t = np.array([c.target_cells for c in a])
+    assert t.min() >= 5_000 and t.max() <= 200_000
+    # log-uniform: the median of the log sizes sits near the middle of the range
+    mid = 0.5 * (np.log(5e3) + np.log(2e5))
+    assert abs(np.median(np.log(t)) - mid) < 0.35
+    assert [c.flow for c in a].count("euler") == 128
+    assert all(0.2 <= c.mach <= 0.8 and -4 <= c.aoa <= 10 and 1e5 <= c.re <= 1e7 for c in a)
+    small = configs.c5_cases(6, seed=3, lo=2_000, hi=20_000)
+    for c in small:
+        g = c.grd()
+        assert 0.6 < g.ncell / c.target_cells < 1.6, (c, g.ncell)

@@ -6,6 +6,10 @@ C1  Euler, O-grid 128 x 64 around a unit-diameter cylinder, first spacing 1e-3 D
 C2  laminar NS, 48 quad layers (first spacing 5e-3 D) around the cylinder plus
     a seeded Delaunay triangle fill to 30 D, ~130k cells, Re 40, M 0.2,
     LU-SGS at CFL 50.
+C5  256 independent cases of uneven size (5k-200k cells, log-uniform from a
+    seed), cylinder or NACA 0012 bodies with quad layers and a triangle fill,
+    M ~ U[0.2, 0.8], AoA ~ U[-4, 10] deg, half Euler and half viscous with
+    Re log-uniform in [1e5, 1e7], all advanced by LU-SGS.
 """
 from __future__ import annotations
 
@@ -57,6 +61,63 @@ def c2big() -> Workload:
 
 
 WORKLOADS = {"c1": c1, "c2": c2, "c2big": c2big}
+
+
+@dataclass
+class BatchCase:
+    """One case of the uneven batch: body kind, target size and flow."""
+
+    index: int
+    body: str          # "cylinder" | "naca0012"
+    target_cells: int
+    nbody: int
+    seed: int
+    flow: str          # "euler" | "laminar"
+    mach: float
+    aoa: float
+    re: float
+
+    def grd(self) -> meshgen.GrdMesh:
+        body = cylinder(self.nbody) if self.body == "cylinder" else meshgen.naca_body(self.nbody)
+        dr1 = 5e-3 if self.body == "cylinder" else 2e-3
+        return meshgen.mixed_mesh(body, nlayer=16, dr1=dr1, growth=1.08, rfar=30.0, seed=self.seed, density=1.0,
+                                  grade=0.82)
+
+
+def c5_cases(n: int = 256, seed: int = 5005, lo: int = 5_000, hi: int = 200_000) -> list[BatchCase]:
+    """The uneven batch.  Sizes are drawn log-uniform in [lo, hi]; the body
+    resolution that gives a size follows the generator's own scaling (cells
+    ~ 2.8 nbody^2 for the cylinder recipe, ~ 6.1 nbody^2 for the airfoil, with
+    16 quad layers and the triangle fill to 30 body lengths).  The first half
+    of the cases (in index order) is Euler, the second half viscous."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        target = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+        body = "cylinder" if rng.uniform() < 0.5 else "naca0012"
+        nbody = max(16, int(round(np.sqrt(target / (2.8 if body == "cylinder" else 6.1)))))
+        out.append(BatchCase(index=i, body=body, target_cells=target, nbody=nbody,
+                             seed=int(rng.integers(1, 1 << 30)), flow="euler" if i < n // 2 else "laminar",
+                             mach=float(rng.uniform(0.2, 0.8)), aoa=float(rng.uniform(-4.0, 10.0)),
+                             re=float(np.exp(rng.uniform(np.log(1e5), np.log(1e7))))))
+    return out
+
+
+def _batch_grd(case: BatchCase) -> meshgen.GrdMesh:
+    return case.grd()
+
+
+def c5_meshes(cases: list[BatchCase], workers: int = 0) -> list[meshgen.GrdMesh]:
+    """Generate the batch's meshes, in parallel over host cores (a spawned
+    process pool, safe after CUDA has been initialised in the caller)."""
+    workers = workers or min(len(cases), os.cpu_count() or 1, 16)
+    if workers <= 1:
+        return [c.grd() for c in cases]
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    with ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_batch_grd, cases, chunksize=1))
 
 
 def grd_path(w: Workload, cache_dir: str | os.PathLike | None = None) -> Path:
