@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--sweep-mode", type=int, default=0, help="LU-SGS schedule (0 dataflow, 1/2 per level)")
+    ap.add_argument("--sweep-mode", type=int, default=0, help="LU-SGS schedule (0 dataflow, 1/2 per level, 5 chain-scheduled binary32 dataflow)")
     ap.add_argument("--sweep-bpsm", type=int, default=0, help="dataflow sweep blocks per SM (0 = autotune)")
     ap.add_argument("--sweep-poll-ns", type=int, default=0, help="dataflow sweep back-off between polls (ns)")
     ap.add_argument("--forms", default="fp64,fp32,mixed", help="precision forms timed besides --precision ('' = none)")
@@ -447,7 +447,7 @@ def run_ours(args):
                      sweep_poll_ns=args.sweep_poll_ns)
         c.init_freestream()
         c.tuned = None
-        if args.sweep_bpsm == 0 and w.advance == "lusgs" and args.sweep_mode in (0, 3, 4):
+        if args.sweep_bpsm == 0 and w.advance == "lusgs" and args.sweep_mode in (0, 3, 4, 5):
             c.tuned = c.autotune(3)[0]  # the sweeps' blocks per SM, by timing whole steps
         return c
 

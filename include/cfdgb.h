@@ -118,7 +118,11 @@ typedef struct {
                           measured 6% slower per step than 0 on C2),
                           4 binary32 dataflow whose two half-warps wait and
                           exchange independently (measured 7-10% slower per step
-                          than 0: the diverged halves issue one after the other) */
+                          than 0: the diverged halves issue one after the other),
+                          5 binary32 forms: dataflow over a chain schedule (each
+                          half-warp runs its own list of cells and passes the
+                          increment of its previous cell in registers; the
+                          binary64 form runs mode 0). All modes give the same bits */
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
                                 the occupancy limit)                             */
     int sweep_poll_ns; /* dataflow sweep: pause between polls of a neighbour's

@@ -179,3 +179,22 @@ def test_autotune_restores_state(built_lib):
         assert np.array_equal(c.get("U"), U)
         c.step_graph(5)  # still steps after the launch shape changed
         assert np.isfinite(c.get("U")).all()
+
+
+def test_autotune_before_initialisation_changes_nothing(built_lib):
+    """Tuning a freshly created case (state not yet set) raises no solver
+    error, and the steps that follow give the same bits as an untuned case."""
+    from tmp_gb300 import abi, learn
+
+    spec = learn.CaseSpec(nbody=48, nlayer=10, seed=8)
+    mesh = spec.mesh()
+    fs = [dict(mach=spec.mach, aoa_deg=spec.aoa, reynolds=spec.re)]
+    for prec in (abi.PREC_FP64, abi.PREC_MIXED):
+        tuned = abi.Case([mesh], fs, abi.FLOW_LAMINAR, abi.ADV_LUSGS, prec, cfl=spec.cfl)
+        tuned.autotune(1)
+        tuned.init_freestream()
+        plain = spec.case(mesh, prec)
+        for c in (tuned, plain):
+            c.step_graph(6)
+            c.sync()
+        assert np.array_equal(tuned.get("U"), plain.get("U"))

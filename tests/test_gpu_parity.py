@@ -322,3 +322,37 @@ def test_fast_sweep_independent_halves_bitwise(prec):
         out.append((case.get("U"), case.get("DW1"), case.get("DW")))
     for a, b in zip(*out):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", ["FP32", "MIXED"])
+@pytest.mark.parametrize("bpsm", [1, 4])
+def test_fast_sweep_chain_schedule_bitwise(prec, bpsm):
+    """The chain-scheduled binary32 sweep (sweep_mode 5: cells dealt to
+    half-warps so that a dependency on the previous cell of the same
+    half-warp is taken from registers) gives the same bits as the default
+    dataflow sweep, on the fixture mesh and on a cylinder mesh of ~25k cells
+    whose quad rows form long chains, at two grid sizes (two schedules), both
+    through plain steps and through the graph-captured step."""
+    from tmp_gb300 import abi, learn
+
+    c, g = manifest()["mixed_lam_lusgs"], golden("mixed_lam_lusgs")
+    fixture = abi.Mesh.load_grd(GOLDEN / c["mesh"], c["wall_tag"], c["far_tag"])
+    spec = learn.CaseSpec(nbody=96, nlayer=24, seed=12, dr1=5e-3, growth=1.05, rfar=30.0)
+    cyl = spec.mesh()
+    fs_fix = dict(mach=c["mach"], aoa_deg=c["aoa"], reynolds=c["re"])
+    fs_cyl = dict(mach=spec.mach, aoa_deg=spec.aoa, reynolds=spec.re)
+    for mesh, fs, init in [(fixture, fs_fix, g["init_U"]), (cyl, fs_cyl, None)]:
+        out = []
+        for sm in (0, 5):
+            case = abi.Case([mesh], [fs], abi.FLOW_LAMINAR, abi.ADV_LUSGS, getattr(abi, f"PREC_{prec}"),
+                            cfl=c["cfl"], sweep_mode=sm, sweep_blocks_per_sm=bpsm)
+            if init is None:
+                case.init_freestream()
+            else:
+                case.put("U", init)
+            case.step(2)
+            case.step_graph(2)
+            case.sync()
+            out.append((case.get("U"), case.get("DW1"), case.get("DW")))
+        for a, b in zip(*out):
+            np.testing.assert_array_equal(a, b)

@@ -108,6 +108,14 @@ struct DevArrays {
     int* bwd_order2 = nullptr;
     int npos2_fwd = 0, npos2_bwd = 0;
     int flow_grid = 0;           // co-resident blocks of the dataflow sweep
+    // chain-scheduled fast-form sweep (sweep_mode 5), index 0 forward, 1 backward
+    int chain_nh = 0;            // half-warps the schedule was built for (0: not built)
+    int* chain_ptr[2] = {nullptr, nullptr};    // [chain_nh+1] each half-warp's range of positions
+    int* chain_cells[2] = {nullptr, nullptr};  // [nc] cell at each position
+    int2* chain_rec[2] = {nullptr, nullptr};   // [4*nc] (lower/upper neighbour or -1, face code) per slot
+    float4* chain_own = nullptr;  // [nc] binary32 own term: R (forward), dW1 (backward)
+    float* chain_invDf = nullptr; // [nc] binary32 1/D
+    float4* chain_dF = nullptr;   // [nc] binary32 slot sums of the last chain sweep
     int poll_ns = 0;             // back-off between a dataflow sweep's polls (ns, 0 = spin)
     // LU-SGS level schedule (all meshes merged level by level)
     int* fwd_order = nullptr;
@@ -140,6 +148,8 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm);
 void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
 void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, bool mu64);
 cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool independent);
+int sweep_chain_max_grid(int blocks_per_sm);
+cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
 void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
 void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);

@@ -98,6 +98,11 @@ struct cfd_case_s {
     float mlp_spread = 0.0f;         // bound on |omega - mesh mean| (negative: none)
     std::vector<cfd_freestream_t> fs_in;  // the freestreams the case was created with
     bool sst = false;                // SST k-omega arrays allocated
+    // host copies kept for the chain sweep schedule (LU-SGS cases)
+    std::vector<int4> h_cface;
+    std::vector<int2> h_lr;
+    std::vector<int> h_order[2];     // merged level orders, forward and backward
+    int chain_cap = 0;               // co-resident blocks of the chain sweep (0: not queried)
     bool viscous() const { return p.flow == CFD_FLOW_LAMINAR; }
     bool fp32() const { return p.precision == CFD_PREC_FP32; }
     bool mixed() const { return p.precision == CFD_PREC_MIXED; }
@@ -122,7 +127,9 @@ void free_case(cfd_case_s* c) {
                     d.mue, d.Fc, d.Fv, d.Uf, d.gradf, d.phif, d.speccf, d.specvf, d.gradTf, d.muf, d.Uef,
                     d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.wall_ptr, d.wall_faces, d.wblocks, d.wpartial, d.wforce, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err, d.dWprev, d.omega, d.omega_mean, d.mlp_samples, d.mlp_samp_off, d.sstT, d.sstTf, d.sstG, d.sstF1, d.sstF2,
-                    d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD};
+                    d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD, d.chain_ptr[0], d.chain_ptr[1],
+                    d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_own,
+                    d.chain_invDf, d.chain_dF};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -155,6 +162,131 @@ void rk_step(cfd_case_s* c) {
     }
 }
 
+// Chain schedule of the binary32 sweep (sweep_mode 5) for nh half-warps.
+// Cells are dealt in level order (the merged order of the level schedule); a
+// cell goes to the half-warp whose previous item is one of its dependencies
+// (the one of the highest level; among equals the highest cell id forward,
+// the lowest backward: a quad row along the body then stays on one half-warp)
+// unless that half-warp already holds a cell of this level, else to the next
+// half-warp round-robin that holds none.  Every half-warp's list is thus in
+// ascending level, at most one cell per level while the level is no wider
+// than nh.  rec holds per position and face slot the neighbour the cell waits
+// for (-1: none) and the slot's face code.
+void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, const std::vector<int4>& cface,
+                 const std::vector<int2>& lr, bool fwd, int nh, std::vector<int>& hptr, std::vector<int>& cells,
+                 std::vector<int2>& rec) {
+    const int nc = (int)order.size();
+    std::vector<int> level(nc), hw_of(nc, -1), last(nh, -1), cnt(nh + 1, 0);
+    std::vector<long long> mark(nh, -1);
+    for (size_t k = 0; k + 1 < lptr.size(); k++)
+        for (int q = lptr[k]; q < lptr[k + 1]; q++) level[order[q]] = (int)k;
+    auto dep = [&](int c, int s, int& j) {
+        const int code = (&cface[c].x)[s];
+        j = -1;
+        if (code == 0) return code;
+        const int f = (code > 0 ? code : -code) - 1;
+        const int2 e = lr[f];
+        const int nbr = code > 0 ? e.y : e.x;
+        if (fwd ? (nbr >= 0 && nbr < c) : (nbr > c)) j = nbr;
+        return code;
+    };
+    int rr = 0;
+    for (size_t k = 0; k + 1 < lptr.size(); k++) {
+        long long round = 0, key = ((long long)k << 24) | round;
+        for (int q = lptr[k]; q < lptr[k + 1]; q++) {
+            const int c = order[q];
+            int best = -1, best_lv = -1, best_j = -1;
+            for (int s = 0; s < 4; s++) {
+                int j;
+                dep(c, s, j);
+                if (j < 0) continue;
+                const int h = hw_of[j];
+                if (last[h] != j || mark[h] == key) continue;
+                const int lv = level[j];
+                if (lv > best_lv || (lv == best_lv && (fwd ? j > best_j : j < best_j))) {
+                    best = h;
+                    best_lv = lv;
+                    best_j = j;
+                }
+            }
+            if (best < 0) {
+                for (int t = 0; t < nh && best < 0; t++) {
+                    const int h = rr;
+                    rr = rr + 1 == nh ? 0 : rr + 1;
+                    if (mark[h] != key) best = h;
+                }
+                if (best < 0) {  // the level is wider than nh: start another round
+                    key = ((long long)k << 24) | ++round;
+                    best = rr;
+                    rr = rr + 1 == nh ? 0 : rr + 1;
+                }
+            }
+            hw_of[c] = best;
+            last[best] = c;
+            mark[best] = key;
+            cnt[best + 1]++;
+        }
+    }
+    for (int h = 0; h < nh; h++) cnt[h + 1] += cnt[h];
+    hptr = cnt;
+    cells.assign(nc, 0);
+    rec.assign(4 * (size_t)nc, make_int2(-1, 0));
+    std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+    for (int q = 0; q < nc; q++) {  // stable: each list keeps the level order
+        const int c = order[q];
+        const int at = pos[hw_of[c]]++;
+        cells[at] = c;
+        for (int s = 0; s < 4; s++) {
+            int j;
+            const int code = dep(c, s, j);
+            rec[4 * (size_t)at + s] = make_int2(j, code);
+        }
+    }
+}
+
+int chain_grid(cfd_case_s* c) {
+    if (!c->chain_cap) c->chain_cap = sweep_chain_max_grid(64);
+    return std::min(c->d.flow_grid, c->chain_cap);
+}
+
+// (Re)build the chain schedules for the current grid.  Uploads synchronously,
+// so it must run outside stream capture; a capture that would need it fails.
+void ensure_chain(cfd_case_s* c) {
+    DevArrays& d = c->d;
+    const int nh = chain_grid(c) * 16;
+    if (d.chain_nh == nh) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    ck(cudaStreamIsCapturing(c->stream, &cs), "cudaStreamIsCapturing");
+    if (cs != cudaStreamCaptureStatusNone)
+        throw std::runtime_error("the chain sweep schedule must be built before graph capture");
+    if (c->h_cface.empty()) throw std::runtime_error("chain sweep: no host topology kept for this case");
+    if (!d.chain_own) {
+        dalloc(&d.chain_own, d.nc);
+        dalloc(&d.chain_invDf, d.nc);
+        dalloc(&d.chain_dF, d.nc);
+        for (int k = 0; k < 2; k++) {
+            dalloc(&d.chain_cells[k], d.nc);
+            dalloc(&d.chain_rec[k], 4 * (size_t)d.nc);
+        }
+    }
+    for (int k = 0; k < 2; k++) {
+        std::vector<int> hptr, cells;
+        std::vector<int2> rec;
+        build_chain(c->h_order[k], k == 0 ? d.fwd_ptr : d.bwd_ptr, c->h_cface, c->h_lr, k == 0, nh, hptr, cells, rec);
+        if (d.chain_ptr[k]) cudaFree(d.chain_ptr[k]);
+        d.chain_ptr[k] = nullptr;
+        dalloc(&d.chain_ptr[k], nh + 1);
+        ck(cudaMemcpyAsync(d.chain_ptr[k], hptr.data(), hptr.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+           "upload");
+        ck(cudaMemcpyAsync(d.chain_cells[k], cells.data(), cells.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           c->stream), "upload");
+        ck(cudaMemcpyAsync(d.chain_rec[k], rec.data(), rec.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream),
+           "upload");
+        ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    }
+    d.chain_nh = nh;
+}
+
 // Forward or backward sweep over all levels.  sweep_mode 1 keeps one thread per
 // cell (the direct form); otherwise the per-step SolveDF constants are computed
 // once (before the forward sweep) and each level runs 16 lanes per cell.
@@ -176,11 +308,15 @@ void sweeps(cfd_case_s* c, bool forward) {
     }
     // default: one dataflow launch per direction (binary64 form, mode 3: two cells per warp)
     if (c->fast_sweep()) {
+        if (c->p.sweep_mode == 5) ensure_chain(c);
         if (forward) {
             launch_inv_diag(d, L);
             launch_sweep_prep32(d, L, c->viscous(), c->mixed());
         }
-        ck(launch_sweep_flow32(d, L, forward, d.flow_grid, c->p.sweep_mode == 4), "cooperative sweep launch");
+        if (c->p.sweep_mode == 5)
+            ck(launch_sweep_chain32(d, L, forward, chain_grid(c)), "cooperative sweep launch");
+        else
+            ck(launch_sweep_flow32(d, L, forward, d.flow_grid, c->p.sweep_mode == 4), "cooperative sweep launch");
     } else if (c->p.sweep_mode == 3) {
         ck(launch_sweep_pair64(d, L, forward, d.flow_grid), "cooperative sweep launch");
     } else {
@@ -220,6 +356,7 @@ int check_errors(cfd_case_s* c) {
         if (e & ERR_WALLTAN) return fail(CFD_ERR_WALLTAN, "Something wrong with Vector computation: wall tangential velocity not tangent");
         if (e & ERR_NONPHYS) return fail(CFD_ERR_NONPHYSICAL, "non-physical state: NaN or non-positive density/pressure");
         if (e & ERR_TIMEOUT) return fail(CFD_ERR_TIMEOUT, "a bounded device wait gave up");
+        if (e & ERR_SCHED) return fail(CFD_ERR_STATE, "a sweep schedule was launched on a grid it was not built for");
     }
     return CFD_OK;
 }
@@ -321,6 +458,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
     if (P.advance != CFD_ADV_RK5 && P.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_ARG, "Undefined Advance Type");
     if (P.precision != CFD_PREC_FP64 && P.precision != CFD_PREC_FP32 && P.precision != CFD_PREC_MIXED)
         return fail(CFD_ERR_ARG, "unknown precision");
+    if (P.sweep_mode < 0 || P.sweep_mode > 5) return fail(CFD_ERR_ARG, "unknown sweep mode");
     for (int i = 0; i < nmesh; i++)
         if (!(fs[i].density > 0) || !(fs[i].pressure > 0) || !(fs[i].mach > 0))
             return fail(CFD_ERR_ARG, "freestream density, pressure and Mach must be positive");
@@ -480,6 +618,12 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             d.flow_grid = sweep_flow_max_grid(P.precision != CFD_PREC_FP64, P.sweep_blocks_per_sm);
             d.poll_ns = P.sweep_poll_ns < 0 ? 0 : (P.sweep_poll_ns > 10000 ? 10000 : P.sweep_poll_ns);
         }
+        if (P.advance == CFD_ADV_LUSGS) {  // for the chain sweep schedule, built on first use
+            c->h_cface = cface;
+            c->h_lr = lr;
+            c->h_order[0] = fo_;
+            c->h_order[1] = bo_;
+        }
         dalloc(&d.norm_blocks, nb.size()); dalloc(&d.norm_partial, nb.size()); dalloc(&d.norm_out, nmesh);
         dalloc(&d.err, 2);
         dalloc(&d.walld, nc); dalloc(&d.wall_ptr, nmesh + 1); dalloc(&d.wall_faces, wfaces.size());
@@ -554,9 +698,9 @@ int cfd_set_cfl(cfd_case_t c, double cfl) {
     return CFD_OK;
 }
 
-int cfd_init_freestream(cfd_case_t c) {
-    if (!c) return fail(CFD_ERR_ARG, "null case");
-    ABI_TRY
+// Every mesh's freestream into U and W; synchronises the stream (the host
+// staging vector must outlive the copy).
+static void upload_freestream(cfd_case_t c) {
     std::vector<d4> u(c->d.nc);
     for (int m = 0; m < c->nmesh; m++) {
         const MeshPrm& p = c->prm[m];
@@ -568,6 +712,12 @@ int cfd_init_freestream(cfd_case_t c) {
     if (c->fp32()) launch_to_fp32(c->d, L, false);
     ck(cudaGetLastError(), "launch");
     ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+}
+
+int cfd_init_freestream(cfd_case_t c) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    ABI_TRY
+    upload_freestream(c);
     return CFD_OK;
     ABI_CATCH
 }
@@ -617,6 +767,7 @@ int cfd_step_graph(cfd_case_t c, int nsteps) {
     if (!c || nsteps < 0) return fail(CFD_ERR_ARG, "null case or negative step count");
     ABI_TRY
     if (!c->gexec) {
+        if (c->fast_sweep() && c->p.sweep_mode == 5) ensure_chain(c);
         ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
         long long before = c->launches;
         one_step(c);
@@ -1281,12 +1432,20 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
     ABI_TRY
     DevArrays& d = c->d;
     const size_t nc = d.nc;
-    // the trial steps advance the state: keep it and put it back afterwards
-    d4 *U0 = nullptr, *W0 = nullptr;
+    // The trial steps run from the freestream (a valid state whatever the case
+    // holds, even before its first initialisation; a step costs the same on any
+    // state) and advance it: keep the caller's state, increments and error
+    // flags and put them back afterwards, so tuning changes no result.
+    d4 *U0 = nullptr, *W0 = nullptr, *dW0 = nullptr;
     dalloc(&U0, nc);
     dalloc(&W0, nc);
+    dalloc(&dW0, nc);
+    unsigned err0 = 0;
     ck(cudaMemcpyAsync(U0, d.U, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "save");
     ck(cudaMemcpyAsync(W0, d.W, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "save");
+    ck(cudaMemcpyAsync(dW0, d.dW, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "save");
+    ck(cudaMemcpyAsync(&err0, d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream), "save");
+    upload_freestream(c);  // synchronises: err0 is valid from here
     const bool low = c->p.precision != CFD_PREC_FP64;
     const int max_grid = sweep_flow_max_grid(low, 64);  // occupancy limit
     int best = 0, last_grid = -1;
@@ -1315,10 +1474,13 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
     }
     ck(cudaMemcpyAsync(d.U, U0, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "restore");
     ck(cudaMemcpyAsync(d.W, W0, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "restore");
+    ck(cudaMemcpyAsync(d.dW, dW0, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "restore");
+    ck(cudaMemcpyAsync(d.err, &err0, sizeof(unsigned), cudaMemcpyHostToDevice, c->stream), "restore");
     if (c->fp32() || c->mixed()) launch_to_fp32(d, c->L(), false);
     ck(cudaStreamSynchronize(c->stream), "sync");
     cudaFree(U0);
     cudaFree(W0);
+    cudaFree(dW0);
     return rc;
     ABI_CATCH
 }

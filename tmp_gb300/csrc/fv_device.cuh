@@ -29,6 +29,7 @@ enum : unsigned {
     ERR_NONPHYS = 2u,      // NaN / non-positive rho or p
     ERR_WALLTAN = 4u,      // BoundaryStrategy.h:250-256 check
     ERR_TIMEOUT = 8u,      // bounded device wait gave up
+    ERR_SCHED = 16u,       // a sweep schedule launched on a grid it was not built for
 };
 
 // Boundary codes (edge3d<2>::BoundaryType).

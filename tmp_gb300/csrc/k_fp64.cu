@@ -920,6 +920,248 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
     return sms * (want < per ? want : per);
 }
 
+// ---------------------------------------------------------------------------
+// Chain-scheduled fast-form sweep (sweep_mode 5).
+//
+// The dataflow sweeps above deal cells to warps round-robin in level order, so
+// every dependency, even one on the cell that was finished just before, makes
+// the round trip publish -> L2 -> poll, and each level of the dependence chain
+// costs one such round trip plus the arithmetic.  Here a host schedule gives
+// each half-warp its own list of cells (ascending level), and a cell goes,
+// where it can, to the half-warp that ran its latest-level dependency as its
+// previous item.  The half-warp keeps its last two results in registers and
+// takes a dependency on them without touching memory, so a chain of such cells
+// (a quad row along the body, for instance) advances at the speed of the
+// arithmetic; only dependencies between half-warps pay the round trip.
+//
+// The arithmetic of a cell is that of k_sweep_flow32 operation for operation
+// (same TU, same -fmad=false), so both give identical bits.  The binary64
+// increments are not formed on the chain: the sweep stores its binary32 slot
+// sums and k_chain_mid / k_chain_finish form dW1 = (-R - sum) / D and
+// dW = dW1 - sum / D with the expressions of k_sweep_flow32.
+//
+// Progress: all half-warps are co-resident (cooperative launch, schedule built
+// for exactly this grid), each runs its list in ascending level and every
+// dependency lies on a strictly lower level, so the lowest unfinished cell can
+// always proceed.  Every wait is bounded (kSpinLimit); after one gives up the
+// half-warp stops waiting and the error word carries ERR_TIMEOUT.
+struct ChainItem {
+    int i, j, code;
+    float4 w0, g;
+    float rA, own, dinv;
+};
+
+__device__ __forceinline__ void chain_load(ChainItem& it, int i, int2 r, int s, int m,
+                                           const float4* __restrict__ fg0f, const float4* __restrict__ Wf,
+                                           const float* __restrict__ swraf, const float4* __restrict__ ownf,
+                                           const float* __restrict__ invDf) {
+    it.i = i;
+    it.j = r.x;
+    it.code = r.y;
+    it.w0 = make_float4(1.f, 1.f, 0.f, 0.f);
+    it.g = make_float4(0.f, 0.f, 0.f, 0.f);
+    it.rA = 0.f;
+    if (r.x >= 0) {
+        it.w0 = Wf[r.x];
+        it.g = fg0f[code_face(r.y)];
+        it.rA = swraf[(size_t)i * 4 + s];
+    }
+    it.own = (&ownf[i].x)[m];
+    it.dinv = invDf[i];
+}
+
+template <bool FWD>
+__global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __restrict__ hptr,
+                                                       const int* __restrict__ cells, const int2* __restrict__ rec,
+                                                       const float4* __restrict__ fg0f, const float4* __restrict__ Wf,
+                                                       const float* __restrict__ swraf, const float4* __restrict__ ownf,
+                                                       const float* __restrict__ invDf, float4* pub,
+                                                       float4* __restrict__ dFout, unsigned* err, int poll_ns) {
+    const float GM1 = 1.4f - 1.0f;
+    const int lane = threadIdx.x & 31;
+    const int h = lane >> 4, base = lane & 16;
+    const int s = (lane >> 2) & 3, m = lane & 3;
+    const unsigned mask = h ? 0xffff0000u : 0x0000ffffu;
+    if ((int)(gridDim.x * (blockDim.x >> 4)) != nh) {  // a schedule built for another grid
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_SCHED);
+        return;
+    }
+    const int hw = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 2 + h;
+    const int p0 = hptr[hw], p1 = hptr[hw + 1];
+    if (p0 >= p1) return;
+    int hi1 = -1, hi2 = -1;  // this half-warp's last two cells and their increments
+    float4 hd1 = make_float4(0.f, 0.f, 0.f, 0.f), hd2 = hd1;
+    bool gave_up = false;
+    // two-stage prefetch: the record of item p+2 and the data of item p+1 are
+    // in flight while item p waits and computes
+    ChainItem cur;
+    chain_load(cur, cells[p0], rec[4 * p0 + s], s, m, fg0f, Wf, swraf, ownf, invDf);
+    ChainItem nxt = cur;
+    int iB = -1;
+    int2 rB = make_int2(-1, 0);
+    if (p0 + 1 < p1) {
+        iB = cells[p0 + 1];
+        rB = rec[4 * (p0 + 1) + s];
+    }
+    for (int p = p0; p < p1; p++) {
+        if (p + 1 < p1) chain_load(nxt, iB, rB, s, m, fg0f, Wf, swraf, ownf, invDf);
+        if (p + 2 < p1) {
+            iB = cells[p + 2];
+            rB = rec[4 * (p + 2) + s];
+        }
+        const int i = cur.i, j = cur.j;
+        const bool use = j >= 0, left = cur.code > 0;
+        const unsigned ex = __ballot_sync(mask, cur.code != 0);
+        const float4 w0 = cur.w0, g = cur.g;
+        float u = 0.f, v = 0.f, vv = 0.f, pb = 0.f, vn = 0.f;
+        float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (use) {
+            u = w0.z / w0.x;
+            v = w0.w / w0.x;
+            vv = u * u + v * v;
+            pb = GM1 * (w0.y - 0.5f * w0.x * vv);
+            vn = u * g.x + v * g.y;
+            if (j == hi1) {
+                dw = hd1;
+            } else if (j == hi2) {
+                dw = hd2;
+            } else {
+                const float4* qf = pub + j;
+                long long it = 0;
+                while (true) {
+                    dw = __ldcv(qf);
+                    if (gave_up) break;
+                    if (!is_sentinel_f(dw.x) && !is_sentinel_f(dw.y) && !is_sentinel_f(dw.z) && !is_sentinel_f(dw.w))
+                        break;
+                    if (++it > kSpinLimit) {
+                        atomicOr(err, ERR_TIMEOUT);
+                        gave_up = true;
+                        break;
+                    }
+                    if (poll_ns) __nanosleep(poll_ns);
+                }
+            }
+        }
+        __syncwarp(mask);
+        const float rho = w0.x, E = w0.y, mx = w0.z, my = w0.w;
+        const float d0 = dw.x, d1 = dw.y, d2 = dw.z, d3 = dw.w;
+        const float rp = 1.f / (rho + d0);
+        const float du = (d2 - u * d0) * rp, dv = (d3 - v * d0) * rp;
+        const float dq = du * (u + u + du) + dv * (v + v + dv);
+        const float dp = GM1 * (d1 - 0.5f * (d0 * (vv + dq) + rho * dq));
+        const float dvn = du * g.x + dv * g.y;
+        const float vnp = vn + dvn;
+        const float dfm = m == 0 ? d2 * g.x + d3 * g.y
+                        : m == 1 ? (d1 + dp) * vnp + (E + pb) * dvn
+                        : m == 2 ? d2 * vnp + mx * dvn + dp * g.x
+                                 : d3 * vnp + my * dvn + dp * g.y;
+        float dwm = m == 0 ? dw.x : m == 1 ? dw.y : m == 2 ? dw.z : dw.w;
+        float dfc = left ? dfm : -dfm;
+        float DF = use ? 0.5f * (dfc - cur.rA * dwm) * g.z : 0.f;
+        float v0 = __shfl_sync(mask, DF, base + m);
+        float v1 = __shfl_sync(mask, DF, base + 4 + m);
+        float v2 = __shfl_sync(mask, DF, base + 8 + m);
+        float v3 = __shfl_sync(mask, DF, base + 12 + m);
+        float dF = 0.f;
+        if (ex & (1u << base)) dF += v0;
+        if (ex & (1u << (base + 4))) dF += v1;
+        if (ex & (1u << (base + 8))) dF += v2;
+        if (ex & (1u << (base + 12))) dF += v3;
+        const float ownf_ = cur.own, dinvf = cur.dinv;
+        const float resf = FWD ? (-ownf_ - dF) * dinvf : ownf_ - dF * dinvf;
+        const float r0 = __shfl_sync(mask, resf, base);
+        const float r1 = __shfl_sync(mask, resf, base + 1);
+        const float r2 = __shfl_sync(mask, resf, base + 2);
+        const float r3 = __shfl_sync(mask, resf, base + 3);
+        if ((lane & 15) == 0) __stcg(pub + i, make_float4(r0, r1, r2, r3));
+        if (s == 0) (&dFout[i].x)[m] = dF;
+        hi2 = hi1;
+        hd2 = hd1;
+        hi1 = i;
+        hd1 = make_float4(r0, r1, r2, r3);
+        cur = nxt;
+    }
+}
+
+// binary32 own terms of the forward chain sweep: R and 1/D
+__global__ void k_chain_own(int nc, const d4* __restrict__ R, const double* __restrict__ invD,
+                            float4* __restrict__ ownf, float* __restrict__ invDf) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    d4 r = ld4(R + c);
+    ownf[c] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
+    invDf[c] = (float)invD[c];
+}
+
+// dW1 = (-R - sum) * (1/D) in binary64 (k_sweep_flow32's forward expression),
+// and its binary32 copy, the own term of the backward chain sweep
+__global__ void k_chain_mid(int nc, const d4* __restrict__ R, const double* __restrict__ invD,
+                            const float4* __restrict__ dF, d4* __restrict__ dW1, float4* __restrict__ ownf) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    d4 r = ld4(R + c);
+    const double dinv = invD[c];
+    const float4 f = dF[c];
+    d4 o;
+    o.x = (-r.x - (double)f.x) * dinv;
+    o.y = (-r.y - (double)f.y) * dinv;
+    o.z = (-r.z - (double)f.z) * dinv;
+    o.w = (-r.w - (double)f.w) * dinv;
+    dW1[c] = o;
+    ownf[c] = make_float4((float)o.x, (float)o.y, (float)o.z, (float)o.w);
+}
+
+// dW = dW1 - sum * (1/D) in binary64 (k_sweep_flow32's backward expression)
+__global__ void k_chain_finish(int nc, const d4* __restrict__ dW1, const double* __restrict__ invD,
+                               const float4* __restrict__ dF, d4* __restrict__ dW) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    d4 a = ld4(dW1 + c);
+    const double dinv = invD[c];
+    const float4 f = dF[c];
+    d4 o;
+    o.x = a.x - (double)f.x * dinv;
+    o.y = a.y - (double)f.y * dinv;
+    o.z = a.z - (double)f.z * dinv;
+    o.w = a.w - (double)f.w * dinv;
+    dW[c] = o;
+}
+
+int sweep_chain_max_grid(int blocks_per_sm) {
+    int dev = 0, sms = 0, per = 0, per2 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (void*)k_sweep_chain32<true>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_chain32<false>, 256, 0);
+    per = per < per2 ? per : per2;
+    if (per < 1) per = 1;
+    int want = blocks_per_sm > 0 ? blocks_per_sm : 2;
+    return sms * (want < per ? want : per);
+}
+
+cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid) {
+    const int k = forward ? 0 : 1;
+    int nh = d.chain_nh;
+    float4* pub = forward ? d.dW1f : d.dWf;
+    if (forward) {
+        k_chain_own<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.R, d.invD, d.chain_own, d.chain_invDf);
+        *L.counter += 1;
+    }
+    void* args[] = {(void*)&nh, (void*)&d.chain_ptr[k], (void*)&d.chain_cells[k], (void*)&d.chain_rec[k],
+                    (void*)&d.fg0f, (void*)&d.Wf, (void*)&d.swraf, (void*)&d.chain_own, (void*)&d.chain_invDf,
+                    (void*)&pub, (void*)&d.chain_dF, (void*)&d.err, (void*)&d.poll_ns};
+    void* fn = forward ? (void*)k_sweep_chain32<true> : (void*)k_sweep_chain32<false>;
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
+    *L.counter += 1;
+    if (e != cudaSuccess) return e;
+    if (forward)
+        k_chain_mid<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.R, d.invD, d.chain_dF, d.dW1, d.chain_own);
+    else
+        k_chain_finish<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.dW1, d.invD, d.chain_dF, d.dW);
+    *L.counter += 1;
+    return cudaSuccess;
+}
+
 // 1/D for the fast form's sweep (binary64)
 __global__ void k_inv_diag(int nc, const double* __restrict__ D, double* __restrict__ invD) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
