@@ -54,15 +54,19 @@ def test_uneven_batch_packed_matches_separate(precision, sweep_mode, flow):
 
 def test_uneven_batch_learned_packed_matches_separate():
     """With the learned relaxation attached, each mesh's pooled factor comes
-    from its own sampled cells only."""
+    from its own sampled cells only.  The relaxation is attached after 30 plain
+    steps: over-relaxing the impulsive start diverges on the high-Mach
+    cylinders of the batch (the oracle's plain steps with W += 1.6 dW fail
+    there at step 2 from the freestream, and pass after the 30 steps)."""
     from tmp_gb300 import abi, learn
 
     net = learn.load()
     if net is None:
         pytest.skip("no committed relaxation weights")
-    _, meshes, fs = _batch(seed=78)
+    _, meshes, fs = _batch()
     packed = abi.Case(meshes, fs, abi.FLOW_LAMINAR, abi.ADV_LUSGS, abi.PREC_MIXED, cfl=10.0)
     packed.init_freestream()
+    packed.step_graph(30)
     abi.case_track(packed, True)
     abi.case_set_mlp(packed, net, False)
     packed.step_graph(5)
@@ -70,6 +74,7 @@ def test_uneven_batch_learned_packed_matches_separate():
     for k, (m, f) in enumerate(zip(meshes, fs)):
         single = abi.Case([m], [f], abi.FLOW_LAMINAR, abi.ADV_LUSGS, abi.PREC_MIXED, cfl=10.0)
         single.init_freestream()
+        single.step_graph(30)
         abi.case_track(single, True)
         abi.case_set_mlp(single, net, False)
         single.step_graph(5)
