@@ -113,8 +113,8 @@ struct DevArrays {
     int* chain_ptr[2] = {nullptr, nullptr};    // [chain_nh+1] each half-warp's range of positions
     int* chain_cells[2] = {nullptr, nullptr};  // [nc] cell at each position
     int2* chain_rec[2] = {nullptr, nullptr};   // [4*nc] (lower/upper neighbour or -1, face code) per slot
-    float4* chain_own = nullptr;  // [nc] binary32 own term: R (forward), dW1 (backward)
-    float* chain_invDf = nullptr; // [nc] binary32 1/D
+    float4* chain_stage[2] = {nullptr, nullptr};  // [12*nc] per-position stage records (k_fp64.cu)
+    int* chain_posb = nullptr;    // [nc] position of each cell in the backward schedule
     float4* chain_dF = nullptr;   // [nc] binary32 slot sums of the last chain sweep
     int poll_ns = 0;             // back-off between a dataflow sweep's polls (ns, 0 = spin)
     // LU-SGS level schedule (all meshes merged level by level)
@@ -150,6 +150,7 @@ void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, b
 cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool independent);
 int sweep_chain_max_grid(int blocks_per_sm);
 cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
+void launch_chain_static(const DevArrays& d, const LaunchCfg& L);
 void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
 void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);

@@ -128,8 +128,8 @@ void free_case(cfd_case_s* c) {
                     d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.wall_ptr, d.wall_faces, d.wblocks, d.wpartial, d.wforce, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err, d.dWprev, d.omega, d.omega_mean, d.mlp_samples, d.mlp_samp_off, d.sstT, d.sstTf, d.sstG, d.sstF1, d.sstF2,
                     d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD, d.chain_ptr[0], d.chain_ptr[1],
-                    d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_own,
-                    d.chain_invDf, d.chain_dF};
+                    d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_stage[0],
+                    d.chain_stage[1], d.chain_posb, d.chain_dF};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -260,13 +260,13 @@ void ensure_chain(cfd_case_s* c) {
     if (cs != cudaStreamCaptureStatusNone)
         throw std::runtime_error("the chain sweep schedule must be built before graph capture");
     if (c->h_cface.empty()) throw std::runtime_error("chain sweep: no host topology kept for this case");
-    if (!d.chain_own) {
-        dalloc(&d.chain_own, d.nc);
-        dalloc(&d.chain_invDf, d.nc);
+    if (!d.chain_dF) {
         dalloc(&d.chain_dF, d.nc);
+        dalloc(&d.chain_posb, d.nc);
         for (int k = 0; k < 2; k++) {
             dalloc(&d.chain_cells[k], d.nc);
             dalloc(&d.chain_rec[k], 4 * (size_t)d.nc);
+            dalloc(&d.chain_stage[k], 12 * (size_t)d.nc);
         }
     }
     for (int k = 0; k < 2; k++) {
@@ -282,6 +282,14 @@ void ensure_chain(cfd_case_s* c) {
                            c->stream), "upload");
         ck(cudaMemcpyAsync(d.chain_rec[k], rec.data(), rec.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream),
            "upload");
+        if (k == 1) {
+            std::vector<int> posb(d.nc);
+            for (int q = 0; q < d.nc; q++) posb[cells[q]] = q;
+            ck(cudaMemcpyAsync(d.chain_posb, posb.data(), posb.size() * sizeof(int), cudaMemcpyHostToDevice,
+                               c->stream), "upload");
+            launch_chain_static(d, c->L());
+            ck(cudaGetLastError(), "k_chain_static");
+        }
         ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
     }
     d.chain_nh = nh;

@@ -940,46 +940,44 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 // sums and k_chain_mid / k_chain_finish form dW1 = (-R - sum) / D and
 // dW = dW1 - sum / D with the expressions of k_sweep_flow32.
 //
+// Per-item data are staged per step in schedule order (12 float4 per
+// position, k_chain_stage) and copied ahead into a shared-memory ring of
+// kChainDepth items per half-warp with cp.async, so a half-warp that does not
+// wait is bound by its arithmetic, not by the L2 latency of its gathers.
+//
 // Progress: all half-warps are co-resident (cooperative launch, schedule built
 // for exactly this grid), each runs its list in ascending level and every
 // dependency lies on a strictly lower level, so the lowest unfinished cell can
 // always proceed.  Every wait is bounded (kSpinLimit); after one gives up the
 // half-warp stops waiting and the error word carries ERR_TIMEOUT.
-struct ChainItem {
-    int i, j, code;
-    float4 w0, g;
-    float rA, own, dinv;
-};
+//
+// Stage record of position p (float4 index p*12 + k):
+//   k 0-3   W_j of slot k's neighbour (binary32; (1,1,0,0) if none)  per step
+//   k 4-7   (nx, ny, A) of slot k-4's face; r_A in .w                 static; per step
+//   k 8     own term (R forward, dW1 backward, binary32)              per step
+//   k 9     (1/D, cell id bits, 0, 0)                                 per step; static
+//   k 10-11 (j, face code) bits of slots 0,1 and 2,3                  static
+constexpr int kChainDepth = 8;
+constexpr int kStageW = 12;
 
-__device__ __forceinline__ void chain_load(ChainItem& it, int i, int2 r, int s, int m,
-                                           const float4* __restrict__ fg0f, const float4* __restrict__ Wf,
-                                           const float* __restrict__ swraf, const float4* __restrict__ ownf,
-                                           const float* __restrict__ invDf) {
-    it.i = i;
-    it.j = r.x;
-    it.code = r.y;
-    it.w0 = make_float4(1.f, 1.f, 0.f, 0.f);
-    it.g = make_float4(0.f, 0.f, 0.f, 0.f);
-    it.rA = 0.f;
-    if (r.x >= 0) {
-        it.w0 = Wf[r.x];
-        it.g = fg0f[code_face(r.y)];
-        it.rA = swraf[(size_t)i * 4 + s];
-    }
-    it.own = (&ownf[i].x)[m];
-    it.dinv = invDf[i];
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 template <bool FWD>
 __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __restrict__ hptr,
-                                                       const int* __restrict__ cells, const int2* __restrict__ rec,
-                                                       const float4* __restrict__ fg0f, const float4* __restrict__ Wf,
-                                                       const float* __restrict__ swraf, const float4* __restrict__ ownf,
-                                                       const float* __restrict__ invDf, float4* pub,
+                                                       const float4* __restrict__ stage, float4* pub,
                                                        float4* __restrict__ dFout, unsigned* err, int poll_ns) {
+    __shared__ __align__(16) float4 ring[16][kChainDepth][kStageW];
     const float GM1 = 1.4f - 1.0f;
     const int lane = threadIdx.x & 31;
-    const int h = lane >> 4, base = lane & 16;
+    const int h = lane >> 4, base = lane & 16, l16 = lane & 15;
     const int s = (lane >> 2) & 3, m = lane & 3;
     const unsigned mask = h ? 0xffff0000u : 0x0000ffffu;
     if ((int)(gridDim.x * (blockDim.x >> 4)) != nh) {  // a schedule built for another grid
@@ -989,30 +987,37 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
     const int hw = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 2 + h;
     const int p0 = hptr[hw], p1 = hptr[hw + 1];
     if (p0 >= p1) return;
+    float4(*R)[kStageW] = ring[threadIdx.x >> 4];
+#pragma unroll
+    for (int k = 0; k < kChainDepth; k++) {
+        if (p0 + k < p1 && l16 < kStageW) cp_async16(&R[k][l16], stage + (size_t)(p0 + k) * kStageW + l16);
+        cp_async_commit();
+    }
     int hi1 = -1, hi2 = -1;  // this half-warp's last two cells and their increments
     float4 hd1 = make_float4(0.f, 0.f, 0.f, 0.f), hd2 = hd1;
     bool gave_up = false;
-    // two-stage prefetch: the record of item p+2 and the data of item p+1 are
-    // in flight while item p waits and computes
-    ChainItem cur;
-    chain_load(cur, cells[p0], rec[4 * p0 + s], s, m, fg0f, Wf, swraf, ownf, invDf);
-    ChainItem nxt = cur;
-    int iB = -1;
-    int2 rB = make_int2(-1, 0);
-    if (p0 + 1 < p1) {
-        iB = cells[p0 + 1];
-        rB = rec[4 * (p0 + 1) + s];
-    }
+    int slot = 0;
     for (int p = p0; p < p1; p++) {
-        if (p + 1 < p1) chain_load(nxt, iB, rB, s, m, fg0f, Wf, swraf, ownf, invDf);
-        if (p + 2 < p1) {
-            iB = cells[p + 2];
-            rB = rec[4 * (p + 2) + s];
-        }
-        const int i = cur.i, j = cur.j;
-        const bool use = j >= 0, left = cur.code > 0;
-        const unsigned ex = __ballot_sync(mask, cur.code != 0);
-        const float4 w0 = cur.w0, g = cur.g;
+        cp_async_wait<kChainDepth - 1>();
+        __syncwarp(mask);
+        const float4 w0 = R[slot][s];
+        const float4 gr = R[slot][4 + s];
+        const float ownf_ = (&R[slot][8].x)[m];
+        const float4 misc = R[slot][9];
+        const float4 jc01 = R[slot][10], jc23 = R[slot][11];
+        __syncwarp(mask);  // every lane has read the slot before it is refilled
+        if (p + kChainDepth < p1 && l16 < kStageW)
+            cp_async16(&R[slot][l16], stage + (size_t)(p + kChainDepth) * kStageW + l16);
+        cp_async_commit();
+        slot = slot + 1 == kChainDepth ? 0 : slot + 1;
+        const int i = __float_as_int(misc.y);
+        const float dinvf = misc.x;
+        const float4 jc = s < 2 ? jc01 : jc23;
+        const int j = __float_as_int((s & 1) ? jc.z : jc.x);
+        const int code = __float_as_int((s & 1) ? jc.w : jc.y);
+        const bool use = j >= 0, left = code > 0;
+        const bool ex0 = __float_as_int(jc01.y) != 0, ex1 = __float_as_int(jc01.w) != 0;
+        const bool ex2 = __float_as_int(jc23.y) != 0, ex3 = __float_as_int(jc23.w) != 0;
         float u = 0.f, v = 0.f, vv = 0.f, pb = 0.f, vn = 0.f;
         float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
         if (use) {
@@ -1020,7 +1025,7 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
             v = w0.w / w0.x;
             vv = u * u + v * v;
             pb = GM1 * (w0.y - 0.5f * w0.x * vv);
-            vn = u * g.x + v * g.y;
+            vn = u * gr.x + v * gr.y;
             if (j == hi1) {
                 dw = hd1;
             } else if (j == hi2) {
@@ -1049,54 +1054,92 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         const float du = (d2 - u * d0) * rp, dv = (d3 - v * d0) * rp;
         const float dq = du * (u + u + du) + dv * (v + v + dv);
         const float dp = GM1 * (d1 - 0.5f * (d0 * (vv + dq) + rho * dq));
-        const float dvn = du * g.x + dv * g.y;
+        const float dvn = du * gr.x + dv * gr.y;
         const float vnp = vn + dvn;
-        const float dfm = m == 0 ? d2 * g.x + d3 * g.y
+        const float dfm = m == 0 ? d2 * gr.x + d3 * gr.y
                         : m == 1 ? (d1 + dp) * vnp + (E + pb) * dvn
-                        : m == 2 ? d2 * vnp + mx * dvn + dp * g.x
-                                 : d3 * vnp + my * dvn + dp * g.y;
+                        : m == 2 ? d2 * vnp + mx * dvn + dp * gr.x
+                                 : d3 * vnp + my * dvn + dp * gr.y;
         float dwm = m == 0 ? dw.x : m == 1 ? dw.y : m == 2 ? dw.z : dw.w;
         float dfc = left ? dfm : -dfm;
-        float DF = use ? 0.5f * (dfc - cur.rA * dwm) * g.z : 0.f;
+        float DF = use ? 0.5f * (dfc - gr.w * dwm) * gr.z : 0.f;
         float v0 = __shfl_sync(mask, DF, base + m);
         float v1 = __shfl_sync(mask, DF, base + 4 + m);
         float v2 = __shfl_sync(mask, DF, base + 8 + m);
         float v3 = __shfl_sync(mask, DF, base + 12 + m);
         float dF = 0.f;
-        if (ex & (1u << base)) dF += v0;
-        if (ex & (1u << (base + 4))) dF += v1;
-        if (ex & (1u << (base + 8))) dF += v2;
-        if (ex & (1u << (base + 12))) dF += v3;
-        const float ownf_ = cur.own, dinvf = cur.dinv;
+        if (ex0) dF += v0;
+        if (ex1) dF += v1;
+        if (ex2) dF += v2;
+        if (ex3) dF += v3;
         const float resf = FWD ? (-ownf_ - dF) * dinvf : ownf_ - dF * dinvf;
         const float r0 = __shfl_sync(mask, resf, base);
         const float r1 = __shfl_sync(mask, resf, base + 1);
         const float r2 = __shfl_sync(mask, resf, base + 2);
         const float r3 = __shfl_sync(mask, resf, base + 3);
-        if ((lane & 15) == 0) __stcg(pub + i, make_float4(r0, r1, r2, r3));
+        if (l16 == 0) __stcg(pub + i, make_float4(r0, r1, r2, r3));
         if (s == 0) (&dFout[i].x)[m] = dF;
         hi2 = hi1;
         hd2 = hd1;
         hi1 = i;
         hd1 = make_float4(r0, r1, r2, r3);
-        cur = nxt;
+    }
+    cp_async_wait<0>();
+}
+
+// Static part of the stage records, once per schedule: cell ids, neighbour /
+// face-code pairs and binary32 face geometry.
+__global__ void k_chain_static(int nc, const int* __restrict__ cells, const int2* __restrict__ rec,
+                               const float4* __restrict__ fg0f, float4* __restrict__ stage) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4LL * nc) return;
+    const int p = (int)(t >> 2), s = (int)(t & 3);
+    float4* st = stage + (size_t)p * kStageW;
+    const int2 r = rec[t];
+    float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (r.x >= 0) g = fg0f[code_face(r.y)];
+    st[4 + s] = make_float4(g.x, g.y, g.z, 0.f);
+    reinterpret_cast<float2*>(st + 10 + (s >> 1))[s & 1] = make_float2(__int_as_float(r.x), __int_as_float(r.y));
+    if (s == 0) st[9] = make_float4(0.f, __int_as_float(cells[p]), 0.f, 0.f);
+}
+
+// Per-step part of both directions' stage records, after k_sweep_prep32 and
+// k_inv_diag: the neighbours' binary32 W, r_A, 1/D and the forward own term R.
+// (The backward own term, dW1, is written by k_chain_mid.)
+__global__ void k_chain_stage(int nc, float4* __restrict__ stage_f, float4* __restrict__ stage_b,
+                              const float4* __restrict__ Wf, const float* __restrict__ swraf,
+                              const d4* __restrict__ R, const double* __restrict__ invD) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 8LL * nc) return;
+    const int dir = t >= 4LL * nc;
+    const long long q = dir ? t - 4LL * nc : t;
+    const int p = (int)(q >> 2), s = (int)(q & 3);
+    float4* st = (dir ? stage_b : stage_f) + (size_t)p * kStageW;
+    const float4 jc = st[10 + (s >> 1)];
+    const int j = __float_as_int((s & 1) ? jc.z : jc.x);
+    const int i = __float_as_int(st[9].y);
+    float4 w0 = make_float4(1.f, 1.f, 0.f, 0.f);
+    float rA = 0.f;
+    if (j >= 0) {
+        w0 = Wf[j];
+        rA = swraf[(size_t)i * 4 + s];
+    }
+    st[s] = w0;
+    st[4 + s].w = rA;
+    if (s == 0) {
+        st[9].x = (float)invD[i];
+        if (!dir) {
+            const d4 r = ld4(R + i);
+            st[8] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
+        }
     }
 }
 
-// binary32 own terms of the forward chain sweep: R and 1/D
-__global__ void k_chain_own(int nc, const d4* __restrict__ R, const double* __restrict__ invD,
-                            float4* __restrict__ ownf, float* __restrict__ invDf) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nc) return;
-    d4 r = ld4(R + c);
-    ownf[c] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
-    invDf[c] = (float)invD[c];
-}
-
 // dW1 = (-R - sum) * (1/D) in binary64 (k_sweep_flow32's forward expression),
-// and its binary32 copy, the own term of the backward chain sweep
+// and its binary32 copy, the own term of the backward stage records
 __global__ void k_chain_mid(int nc, const d4* __restrict__ R, const double* __restrict__ invD,
-                            const float4* __restrict__ dF, d4* __restrict__ dW1, float4* __restrict__ ownf) {
+                            const float4* __restrict__ dF, const int* __restrict__ posb, d4* __restrict__ dW1,
+                            float4* __restrict__ stage_b) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     d4 r = ld4(R + c);
@@ -1108,7 +1151,7 @@ __global__ void k_chain_mid(int nc, const d4* __restrict__ R, const double* __re
     o.z = (-r.z - (double)f.z) * dinv;
     o.w = (-r.w - (double)f.w) * dinv;
     dW1[c] = o;
-    ownf[c] = make_float4((float)o.x, (float)o.y, (float)o.z, (float)o.w);
+    stage_b[(size_t)posb[c] * kStageW + 8] = make_float4((float)o.x, (float)o.y, (float)o.z, (float)o.w);
 }
 
 // dW = dW1 - sum * (1/D) in binary64 (k_sweep_flow32's backward expression)
@@ -1139,23 +1182,31 @@ int sweep_chain_max_grid(int blocks_per_sm) {
     return sms * (want < per ? want : per);
 }
 
+void launch_chain_static(const DevArrays& d, const LaunchCfg& L) {
+    for (int k = 0; k < 2; k++)
+        k_chain_static<<<nblk(4 * d.nc, 256), 256, 0, L.stream>>>(d.nc, d.chain_cells[k], d.chain_rec[k], d.fg0f,
+                                                                  d.chain_stage[k]);
+    *L.counter += 2;
+}
+
 cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid) {
     const int k = forward ? 0 : 1;
     int nh = d.chain_nh;
     float4* pub = forward ? d.dW1f : d.dWf;
     if (forward) {
-        k_chain_own<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.R, d.invD, d.chain_own, d.chain_invDf);
+        k_chain_stage<<<nblk(8 * d.nc, 256), 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1], d.Wf,
+                                                                 d.swraf, d.R, d.invD);
         *L.counter += 1;
     }
-    void* args[] = {(void*)&nh, (void*)&d.chain_ptr[k], (void*)&d.chain_cells[k], (void*)&d.chain_rec[k],
-                    (void*)&d.fg0f, (void*)&d.Wf, (void*)&d.swraf, (void*)&d.chain_own, (void*)&d.chain_invDf,
-                    (void*)&pub, (void*)&d.chain_dF, (void*)&d.err, (void*)&d.poll_ns};
+    void* args[] = {(void*)&nh, (void*)&d.chain_ptr[k], (void*)&d.chain_stage[k], (void*)&pub, (void*)&d.chain_dF,
+                    (void*)&d.err, (void*)&d.poll_ns};
     void* fn = forward ? (void*)k_sweep_chain32<true> : (void*)k_sweep_chain32<false>;
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
     *L.counter += 1;
     if (e != cudaSuccess) return e;
     if (forward)
-        k_chain_mid<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.R, d.invD, d.chain_dF, d.dW1, d.chain_own);
+        k_chain_mid<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.R, d.invD, d.chain_dF, d.chain_posb, d.dW1,
+                                                           d.chain_stage[1]);
     else
         k_chain_finish<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.dW1, d.invD, d.chain_dF, d.dW);
     *L.counter += 1;
