@@ -942,8 +942,11 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 //
 // Per-item data are staged per step in schedule order (12 float4 per
 // position, k_chain_stage) and copied ahead into a shared-memory ring of
-// kChainDepth items per half-warp with cp.async, so a half-warp that does not
-// wait is bound by its arithmetic, not by the L2 latency of its gathers.
+// kChainDepth items per half-warp with cp.async; the increment of a remote
+// dependency is also read early, kChainAhead items ahead, into shared memory
+// (if it is not published yet the cell polls L2 as before).  A half-warp whose
+// dependencies are ready is then bound by its arithmetic, not by the L2
+// latency of its reads.
 //
 // Progress: all half-warps are co-resident (cooperative launch, schedule built
 // for exactly this grid), each runs its list in ascending level and every
@@ -957,8 +960,10 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 //   k 8     own term (R forward, dW1 backward, binary32)              per step
 //   k 9     (1/D, cell id bits, 0, 0)                                 per step; static
 //   k 10-11 (j, face code) bits of slots 0,1 and 2,3                  static
-constexpr int kChainDepth = 8;
+constexpr int kChainDepth = 8;  // stage records in flight per half-warp
+constexpr int kChainAhead = 3;  // items ahead at which a remote dependency is read early
 constexpr int kStageW = 12;
+static_assert(2 * kChainAhead <= kChainDepth && kChainAhead >= 2, "ring accounting");
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -975,6 +980,7 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
                                                        const float4* __restrict__ stage, float4* pub,
                                                        float4* __restrict__ dFout, unsigned* err, int poll_ns) {
     __shared__ __align__(16) float4 ring[16][kChainDepth][kStageW];
+    __shared__ __align__(16) float4 spec[16][kChainDepth][4];
     const float GM1 = 1.4f - 1.0f;
     const int lane = threadIdx.x & 31;
     const int h = lane >> 4, base = lane & 16, l16 = lane & 15;
@@ -987,29 +993,49 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
     const int hw = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 2 + h;
     const int p0 = hptr[hw], p1 = hptr[hw + 1];
     if (p0 >= p1) return;
+    const int n = p1 - p0;
     float4(*R)[kStageW] = ring[threadIdx.x >> 4];
+    float4(*S)[4] = spec[threadIdx.x >> 4];
+    // cp.async group g holds the stage record of item g (g < kChainDepth: the
+    // prologue; later the refill issued while item g - kChainDepth ran) and
+    // the early read of item g - kChainDepth + kChainAhead's remote dependency
 #pragma unroll
     for (int k = 0; k < kChainDepth; k++) {
-        if (p0 + k < p1 && l16 < kStageW) cp_async16(&R[k][l16], stage + (size_t)(p0 + k) * kStageW + l16);
+        if (k < n && l16 < kStageW) cp_async16(&R[k][l16], stage + (size_t)(p0 + k) * kStageW + l16);
         cp_async_commit();
     }
     int hi1 = -1, hi2 = -1;  // this half-warp's last two cells and their increments
     float4 hd1 = make_float4(0.f, 0.f, 0.f, 0.f), hd2 = hd1;
+    const float sent = __uint_as_float(kSentinelF);
     bool gave_up = false;
-    int slot = 0;
-    for (int p = p0; p < p1; p++) {
-        cp_async_wait<kChainDepth - 1>();
+    for (int k = 0; k < n; k++) {
+        const int slot = k % kChainDepth;
+        // groups up to kChainDepth + k - kChainAhead are complete: this item's
+        // record and early read, and the record of item k + kChainAhead
+        cp_async_wait<kChainAhead - 1>();
         __syncwarp(mask);
         const float4 w0 = R[slot][s];
         const float4 gr = R[slot][4 + s];
         const float ownf_ = (&R[slot][8].x)[m];
         const float4 misc = R[slot][9];
         const float4 jc01 = R[slot][10], jc23 = R[slot][11];
+        const float4 early = k >= kChainAhead ? S[slot][s] : make_float4(sent, sent, sent, sent);
+        // the item kChainAhead positions on: its neighbour, and the two cells
+        // that will be this half-warp's history when it runs
+        int ja = -1, ida1 = -1, ida2 = -1;
+        if (k + kChainAhead < n) {
+            const int sa = (k + kChainAhead) % kChainDepth;
+            const float4 jca = R[sa][10 + (s >> 1)];
+            ja = __float_as_int((s & 1) ? jca.z : jca.x);
+            ida1 = __float_as_int(R[(k + kChainAhead - 1) % kChainDepth][9].y);
+            ida2 = __float_as_int(R[(k + kChainAhead - 2) % kChainDepth][9].y);
+        }
         __syncwarp(mask);  // every lane has read the slot before it is refilled
-        if (p + kChainDepth < p1 && l16 < kStageW)
-            cp_async16(&R[slot][l16], stage + (size_t)(p + kChainDepth) * kStageW + l16);
+        if (k + kChainDepth < n && l16 < kStageW)
+            cp_async16(&R[slot][l16], stage + (size_t)(p0 + k + kChainDepth) * kStageW + l16);
+        if (m == 0 && ja >= 0 && ja != ida1 && ja != ida2)
+            cp_async16(&S[(k + kChainAhead) % kChainDepth][s], pub + ja);
         cp_async_commit();
-        slot = slot + 1 == kChainDepth ? 0 : slot + 1;
         const int i = __float_as_int(misc.y);
         const float dinvf = misc.x;
         const float4 jc = s < 2 ? jc01 : jc23;
@@ -1031,13 +1057,12 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
             } else if (j == hi2) {
                 dw = hd2;
             } else {
+                dw = early;
                 const float4* qf = pub + j;
                 long long it = 0;
-                while (true) {
+                while (is_sentinel_f(dw.x) || is_sentinel_f(dw.y) || is_sentinel_f(dw.z) || is_sentinel_f(dw.w)) {
                     dw = __ldcv(qf);
                     if (gave_up) break;
-                    if (!is_sentinel_f(dw.x) && !is_sentinel_f(dw.y) && !is_sentinel_f(dw.z) && !is_sentinel_f(dw.w))
-                        break;
                     if (++it > kSpinLimit) {
                         atomicOr(err, ERR_TIMEOUT);
                         gave_up = true;
