@@ -120,7 +120,7 @@ typedef struct {
                           exchange independently (measured 7-10% slower per step
                           than 0: the diverged halves issue one after the other),
                           5 binary32 forms: dataflow over a chain schedule (each
-                          half-warp runs its own list of cells and passes the
+                          warp runs its own list of cells and passes the
                           increment of its previous cell in registers; the
                           binary64 form runs mode 0). All modes give the same bits */
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at

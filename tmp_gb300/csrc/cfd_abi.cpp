@@ -162,16 +162,16 @@ void rk_step(cfd_case_s* c) {
     }
 }
 
-// Chain schedule of the binary32 sweep (sweep_mode 5) for nh half-warps.
-// Cells are dealt in level order (the merged order of the level schedule); a
-// cell goes to the half-warp whose previous item is one of its dependencies
-// (the one of the highest level; among equals the highest cell id forward,
-// the lowest backward: a quad row along the body then stays on one half-warp)
-// unless that half-warp already holds a cell of this level, else to the next
-// half-warp round-robin that holds none.  Every half-warp's list is thus in
-// ascending level, at most one cell per level while the level is no wider
-// than nh.  rec holds per position and face slot the neighbour the cell waits
-// for (-1: none) and the slot's face code.
+// Chain schedule of the binary32 sweep (sweep_mode 5) for nh lists (one per
+// warp of the launch).  Cells are dealt in level order (the merged order of
+// the level schedule); a cell goes to the list whose previous item is one of
+// its dependencies (the one of the highest level; among equals the highest
+// cell id forward, the lowest backward: a quad row along the body then stays
+// on one list) unless that list already holds a cell of this level, else to
+// the next list round-robin that holds none.  Every list is thus in ascending
+// level, at most one cell per level while the level is no wider than nh.  rec
+// holds per position and face slot the neighbour the cell waits for (-1:
+// none) and the slot's face code.
 void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, const std::vector<int4>& cface,
                  const std::vector<int2>& lr, bool fwd, int nh, std::vector<int>& hptr, std::vector<int>& cells,
                  std::vector<int2>& rec) {
@@ -253,7 +253,7 @@ int chain_grid(cfd_case_s* c) {
 // so it must run outside stream capture; a capture that would need it fails.
 void ensure_chain(cfd_case_s* c) {
     DevArrays& d = c->d;
-    const int nh = chain_grid(c) * 16;
+    const int nh = chain_grid(c) * 8;  // one list per warp
     if (d.chain_nh == nh) return;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     ck(cudaStreamIsCapturing(c->stream, &cs), "cudaStreamIsCapturing");
@@ -266,7 +266,7 @@ void ensure_chain(cfd_case_s* c) {
         for (int k = 0; k < 2; k++) {
             dalloc(&d.chain_cells[k], d.nc);
             dalloc(&d.chain_rec[k], 4 * (size_t)d.nc);
-            dalloc(&d.chain_stage[k], 12 * (size_t)d.nc);
+            dalloc(&d.chain_stage[k], 16 * (size_t)d.nc);
         }
     }
     for (int k = 0; k < 2; k++) {

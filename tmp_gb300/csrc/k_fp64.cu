@@ -940,29 +940,33 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 // sums and k_chain_mid / k_chain_finish form dW1 = (-R - sum) / D and
 // dW = dW1 - sum / D with the expressions of k_sweep_flow32.
 //
-// Per-item data are staged per step in schedule order (12 float4 per
-// position, k_chain_stage) and copied ahead into a shared-memory ring of
-// kChainDepth items per half-warp with cp.async; the increment of a remote
-// dependency is also read early, kChainAhead items ahead, into shared memory
-// (if it is not published yet the cell polls L2 as before).  A half-warp whose
-// dependencies are ready is then bound by its arithmetic, not by the L2
-// latency of its reads.
+// Per-item data are staged per step in schedule order (16 float4 per
+// position, k_chain_stage, which also forms the neighbour's velocity, pressure
+// and normal velocity: the terms of the flux difference that do not depend on
+// the increment) and copied ahead into a shared-memory ring of kChainDepth
+// items per warp with cp.async; the increment of a remote dependency is also
+// read early, kChainAhead items ahead, into shared memory (if it is not
+// published yet the cell polls L2 as before).  One list per warp, 16 lanes: two
+// lists sharing a warp would issue one after the other.
 //
-// Progress: all half-warps are co-resident (cooperative launch, schedule built
-// for exactly this grid), each runs its list in ascending level and every
+// Progress: all warps are co-resident (cooperative launch, schedule built for
+// exactly this grid), each runs its list in ascending level and every
 // dependency lies on a strictly lower level, so the lowest unfinished cell can
 // always proceed.  Every wait is bounded (kSpinLimit); after one gives up the
-// half-warp stops waiting and the error word carries ERR_TIMEOUT.
+// warp stops waiting and the error word carries ERR_TIMEOUT.
 //
-// Stage record of position p (float4 index p*12 + k):
-//   k 0-3   W_j of slot k's neighbour (binary32; (1,1,0,0) if none)  per step
-//   k 4-7   (nx, ny, A) of slot k-4's face; r_A in .w                 static; per step
-//   k 8     own term (R forward, dW1 backward, binary32)              per step
-//   k 9     (1/D, cell id bits, 0, 0)                                 per step; static
-//   k 10-11 (j, face code) bits of slots 0,1 and 2,3                  static
-constexpr int kChainDepth = 8;  // stage records in flight per half-warp
+// Stage record of position p (float4 index p*16 + k), slot s = face slot:
+//   k 0-3   (rho, E + p, rho u, rho v) of slot s's neighbour (binary32)   per step
+//   k 4-7   (u, v, u^2 + v^2, u nx + v ny) of the same                    per step
+//   k 8-11  (nx, ny, A) of slot s's face; r_A in .w                      static; per step
+//   k 12    own term (R forward, dW1 backward, binary32)                 per step
+//   k 13    (1/D, cell id bits, 0, 0)                                    per step; static
+//   k 14-15 (j, face code) bits of slots 0,1 and 2,3 (j = -1: no wait)   static
+// Slots without a dependency hold the neutral state (1, 1, 0, 0).
+constexpr int kChainDepth = 8;  // stage records in flight per warp
 constexpr int kChainAhead = 3;  // items ahead at which a remote dependency is read early
-constexpr int kStageW = 12;
+constexpr int kStageW = 16;
+constexpr int kChainWarps = 8;  // warps (lists) per block
 static_assert(2 * kChainAhead <= kChainDepth && kChainAhead >= 2, "ring accounting");
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -979,32 +983,33 @@ template <bool FWD>
 __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __restrict__ hptr,
                                                        const float4* __restrict__ stage, float4* pub,
                                                        float4* __restrict__ dFout, unsigned* err, int poll_ns) {
-    __shared__ __align__(16) float4 ring[16][kChainDepth][kStageW];
-    __shared__ __align__(16) float4 spec[16][kChainDepth][4];
+    __shared__ __align__(16) float4 ring[kChainWarps][kChainDepth][kStageW];
+    __shared__ __align__(16) float4 spec[kChainWarps][kChainDepth][4];
     const float GM1 = 1.4f - 1.0f;
     const int lane = threadIdx.x & 31;
-    const int h = lane >> 4, base = lane & 16, l16 = lane & 15;
     const int s = (lane >> 2) & 3, m = lane & 3;
-    const unsigned mask = h ? 0xffff0000u : 0x0000ffffu;
-    if ((int)(gridDim.x * (blockDim.x >> 4)) != nh) {  // a schedule built for another grid
+    constexpr unsigned mask = 0x0000ffffu;
+    if ((int)(gridDim.x * (blockDim.x >> 5)) != nh) {  // a schedule built for another grid
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_SCHED);
         return;
     }
-    const int hw = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 2 + h;
+    if (lane >= 16) return;
+    const int warp = threadIdx.x >> 5;
+    const int hw = blockIdx.x * (blockDim.x >> 5) + warp;
     const int p0 = hptr[hw], p1 = hptr[hw + 1];
     if (p0 >= p1) return;
     const int n = p1 - p0;
-    float4(*R)[kStageW] = ring[threadIdx.x >> 4];
-    float4(*S)[4] = spec[threadIdx.x >> 4];
+    float4(*R)[kStageW] = ring[warp];
+    float4(*S)[4] = spec[warp];
     // cp.async group g holds the stage record of item g (g < kChainDepth: the
     // prologue; later the refill issued while item g - kChainDepth ran) and
     // the early read of item g - kChainDepth + kChainAhead's remote dependency
 #pragma unroll
     for (int k = 0; k < kChainDepth; k++) {
-        if (k < n && l16 < kStageW) cp_async16(&R[k][l16], stage + (size_t)(p0 + k) * kStageW + l16);
+        if (k < n) cp_async16(&R[k][lane], stage + (size_t)(p0 + k) * kStageW + lane);
         cp_async_commit();
     }
-    int hi1 = -1, hi2 = -1;  // this half-warp's last two cells and their increments
+    int hi1 = -1, hi2 = -1;  // this warp's last two cells and their increments
     float4 hd1 = make_float4(0.f, 0.f, 0.f, 0.f), hd2 = hd1;
     const float sent = __uint_as_float(kSentinelF);
     bool gave_up = false;
@@ -1014,27 +1019,26 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         // record and early read, and the record of item k + kChainAhead
         cp_async_wait<kChainAhead - 1>();
         __syncwarp(mask);
-        const float4 w0 = R[slot][s];
-        const float4 gr = R[slot][4 + s];
-        const float ownf_ = (&R[slot][8].x)[m];
-        const float4 misc = R[slot][9];
-        const float4 jc01 = R[slot][10], jc23 = R[slot][11];
+        const float4 A = R[slot][s];
+        const float4 B = R[slot][4 + s];
+        const float4 gr = R[slot][8 + s];
+        const float ownf_ = (&R[slot][12].x)[m];
+        const float4 misc = R[slot][13];
+        const float4 jc01 = R[slot][14], jc23 = R[slot][15];
         const float4 early = k >= kChainAhead ? S[slot][s] : make_float4(sent, sent, sent, sent);
         // the item kChainAhead positions on: its neighbour, and the two cells
-        // that will be this half-warp's history when it runs
+        // that will be this warp's history when it runs
         int ja = -1, ida1 = -1, ida2 = -1;
         if (k + kChainAhead < n) {
             const int sa = (k + kChainAhead) % kChainDepth;
-            const float4 jca = R[sa][10 + (s >> 1)];
+            const float4 jca = R[sa][14 + (s >> 1)];
             ja = __float_as_int((s & 1) ? jca.z : jca.x);
-            ida1 = __float_as_int(R[(k + kChainAhead - 1) % kChainDepth][9].y);
-            ida2 = __float_as_int(R[(k + kChainAhead - 2) % kChainDepth][9].y);
+            ida1 = __float_as_int(R[(k + kChainAhead - 1) % kChainDepth][13].y);
+            ida2 = __float_as_int(R[(k + kChainAhead - 2) % kChainDepth][13].y);
         }
         __syncwarp(mask);  // every lane has read the slot before it is refilled
-        if (k + kChainDepth < n && l16 < kStageW)
-            cp_async16(&R[slot][l16], stage + (size_t)(p0 + k + kChainDepth) * kStageW + l16);
-        if (m == 0 && ja >= 0 && ja != ida1 && ja != ida2)
-            cp_async16(&S[(k + kChainAhead) % kChainDepth][s], pub + ja);
+        if (k + kChainDepth < n) cp_async16(&R[slot][lane], stage + (size_t)(p0 + k + kChainDepth) * kStageW + lane);
+        if (m == 0 && ja >= 0 && ja != ida1 && ja != ida2) cp_async16(&S[(k + kChainAhead) % kChainDepth][s], pub + ja);
         cp_async_commit();
         const int i = __float_as_int(misc.y);
         const float dinvf = misc.x;
@@ -1044,14 +1048,8 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         const bool use = j >= 0, left = code > 0;
         const bool ex0 = __float_as_int(jc01.y) != 0, ex1 = __float_as_int(jc01.w) != 0;
         const bool ex2 = __float_as_int(jc23.y) != 0, ex3 = __float_as_int(jc23.w) != 0;
-        float u = 0.f, v = 0.f, vv = 0.f, pb = 0.f, vn = 0.f;
         float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
         if (use) {
-            u = w0.z / w0.x;
-            v = w0.w / w0.x;
-            vv = u * u + v * v;
-            pb = GM1 * (w0.y - 0.5f * w0.x * vv);
-            vn = u * gr.x + v * gr.y;
             if (j == hi1) {
                 dw = hd1;
             } else if (j == hi2) {
@@ -1073,7 +1071,8 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
             }
         }
         __syncwarp(mask);
-        const float rho = w0.x, E = w0.y, mx = w0.z, my = w0.w;
+        const float rho = A.x, Ep = A.y, mx = A.z, my = A.w;
+        const float u = B.x, v = B.y, vv = B.z, vn = B.w;
         const float d0 = dw.x, d1 = dw.y, d2 = dw.z, d3 = dw.w;
         const float rp = 1.f / (rho + d0);
         const float du = (d2 - u * d0) * rp, dv = (d3 - v * d0) * rp;
@@ -1082,27 +1081,27 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         const float dvn = du * gr.x + dv * gr.y;
         const float vnp = vn + dvn;
         const float dfm = m == 0 ? d2 * gr.x + d3 * gr.y
-                        : m == 1 ? (d1 + dp) * vnp + (E + pb) * dvn
+                        : m == 1 ? (d1 + dp) * vnp + Ep * dvn
                         : m == 2 ? d2 * vnp + mx * dvn + dp * gr.x
                                  : d3 * vnp + my * dvn + dp * gr.y;
         float dwm = m == 0 ? dw.x : m == 1 ? dw.y : m == 2 ? dw.z : dw.w;
         float dfc = left ? dfm : -dfm;
         float DF = use ? 0.5f * (dfc - gr.w * dwm) * gr.z : 0.f;
-        float v0 = __shfl_sync(mask, DF, base + m);
-        float v1 = __shfl_sync(mask, DF, base + 4 + m);
-        float v2 = __shfl_sync(mask, DF, base + 8 + m);
-        float v3 = __shfl_sync(mask, DF, base + 12 + m);
+        float v0 = __shfl_sync(mask, DF, m);
+        float v1 = __shfl_sync(mask, DF, 4 + m);
+        float v2 = __shfl_sync(mask, DF, 8 + m);
+        float v3 = __shfl_sync(mask, DF, 12 + m);
         float dF = 0.f;
         if (ex0) dF += v0;
         if (ex1) dF += v1;
         if (ex2) dF += v2;
         if (ex3) dF += v3;
         const float resf = FWD ? (-ownf_ - dF) * dinvf : ownf_ - dF * dinvf;
-        const float r0 = __shfl_sync(mask, resf, base);
-        const float r1 = __shfl_sync(mask, resf, base + 1);
-        const float r2 = __shfl_sync(mask, resf, base + 2);
-        const float r3 = __shfl_sync(mask, resf, base + 3);
-        if (l16 == 0) __stcg(pub + i, make_float4(r0, r1, r2, r3));
+        const float r0 = __shfl_sync(mask, resf, 0);
+        const float r1 = __shfl_sync(mask, resf, 1);
+        const float r2 = __shfl_sync(mask, resf, 2);
+        const float r3 = __shfl_sync(mask, resf, 3);
+        if (lane == 0) __stcg(pub + i, make_float4(r0, r1, r2, r3));
         if (s == 0) (&dFout[i].x)[m] = dF;
         hi2 = hi1;
         hd2 = hd1;
@@ -1123,39 +1122,48 @@ __global__ void k_chain_static(int nc, const int* __restrict__ cells, const int2
     const int2 r = rec[t];
     float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
     if (r.x >= 0) g = fg0f[code_face(r.y)];
-    st[4 + s] = make_float4(g.x, g.y, g.z, 0.f);
-    reinterpret_cast<float2*>(st + 10 + (s >> 1))[s & 1] = make_float2(__int_as_float(r.x), __int_as_float(r.y));
-    if (s == 0) st[9] = make_float4(0.f, __int_as_float(cells[p]), 0.f, 0.f);
+    st[8 + s] = make_float4(g.x, g.y, g.z, 0.f);
+    reinterpret_cast<float2*>(st + 14 + (s >> 1))[s & 1] = make_float2(__int_as_float(r.x), __int_as_float(r.y));
+    if (s == 0) st[13] = make_float4(0.f, __int_as_float(cells[p]), 0.f, 0.f);
 }
 
 // Per-step part of both directions' stage records, after k_sweep_prep32 and
-// k_inv_diag: the neighbours' binary32 W, r_A, 1/D and the forward own term R.
-// (The backward own term, dW1, is written by k_chain_mid.)
+// k_inv_diag: the neighbours' binary32 state and its increment-free terms
+// (k_sweep_flow32's expressions), r_A, 1/D and the forward own term R.  (The
+// backward own term, dW1, is written by k_chain_mid.)
 __global__ void k_chain_stage(int nc, float4* __restrict__ stage_f, float4* __restrict__ stage_b,
                               const float4* __restrict__ Wf, const float* __restrict__ swraf,
                               const d4* __restrict__ R, const double* __restrict__ invD) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 8LL * nc) return;
+    const float GM1 = 1.4f - 1.0f;
     const int dir = t >= 4LL * nc;
     const long long q = dir ? t - 4LL * nc : t;
     const int p = (int)(q >> 2), s = (int)(q & 3);
     float4* st = (dir ? stage_b : stage_f) + (size_t)p * kStageW;
-    const float4 jc = st[10 + (s >> 1)];
+    const float4 jc = st[14 + (s >> 1)];
     const int j = __float_as_int((s & 1) ? jc.z : jc.x);
-    const int i = __float_as_int(st[9].y);
+    const int i = __float_as_int(st[13].y);
     float4 w0 = make_float4(1.f, 1.f, 0.f, 0.f);
-    float rA = 0.f;
+    float rA = 0.f, u = 0.f, v = 0.f, vv = 0.f, pb = 0.f, vn = 0.f;
     if (j >= 0) {
+        const float4 g = st[8 + s];
         w0 = Wf[j];
         rA = swraf[(size_t)i * 4 + s];
+        u = w0.z / w0.x;
+        v = w0.w / w0.x;
+        vv = u * u + v * v;
+        pb = GM1 * (w0.y - 0.5f * w0.x * vv);
+        vn = u * g.x + v * g.y;
     }
-    st[s] = w0;
-    st[4 + s].w = rA;
+    st[s] = make_float4(w0.x, w0.y + pb, w0.z, w0.w);
+    st[4 + s] = make_float4(u, v, vv, vn);
+    st[8 + s].w = rA;
     if (s == 0) {
-        st[9].x = (float)invD[i];
+        st[13].x = (float)invD[i];
         if (!dir) {
             const d4 r = ld4(R + i);
-            st[8] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
+            st[12] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
         }
     }
 }
@@ -1176,7 +1184,7 @@ __global__ void k_chain_mid(int nc, const d4* __restrict__ R, const double* __re
     o.z = (-r.z - (double)f.z) * dinv;
     o.w = (-r.w - (double)f.w) * dinv;
     dW1[c] = o;
-    stage_b[(size_t)posb[c] * kStageW + 8] = make_float4((float)o.x, (float)o.y, (float)o.z, (float)o.w);
+    stage_b[(size_t)posb[c] * kStageW + 12] = make_float4((float)o.x, (float)o.y, (float)o.z, (float)o.w);
 }
 
 // dW = dW1 - sum * (1/D) in binary64 (k_sweep_flow32's backward expression)
