@@ -171,7 +171,7 @@ void rk_step(cfd_case_s* c) {
 // the next list round-robin that holds none.  Every list is thus in ascending
 // level, at most one cell per level while the level is no wider than nh.  rec
 // holds per position and face slot the neighbour the cell waits for (-1:
-// none) and the slot's face code.
+// none) and the slot's face code.  nh is a multiple of 8 (warps per block).
 void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, const std::vector<int4>& cface,
                  const std::vector<int2>& lr, bool fwd, int nh, std::vector<int>& hptr, std::vector<int>& cells,
                  std::vector<int2>& rec) {
@@ -224,8 +224,16 @@ void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, co
             hw_of[c] = best;
             last[best] = c;
             mark[best] = key;
-            cnt[best + 1]++;
         }
+    }
+    // lists are numbered round-robin; spread consecutive numbers over blocks
+    // (warp w of block b runs list b + w * nblocks) so that the few long lists
+    // of a thin mesh region do not share one SM's issue slots
+    const int nblocks = nh / 8;
+    for (int c = 0; c < nc; c++) {
+        const int q = hw_of[c];
+        hw_of[c] = (q % nblocks) * 8 + q / nblocks;
+        cnt[hw_of[c] + 1]++;
     }
     for (int h = 0; h < nh; h++) cnt[h + 1] += cnt[h];
     hptr = cnt;
