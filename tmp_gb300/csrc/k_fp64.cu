@@ -960,11 +960,11 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 //   k 4-7   (u, v, u^2 + v^2, u nx + v ny) of the same                    per step
 //   k 8-11  (nx, ny, A) of slot s's face; r_A in .w                      static; per step
 //   k 12    own term (R forward, dW1 backward, binary32)                 per step
-//   k 13    (1/D, cell id bits, 0, 0)                                    per step; static
+//   k 13    (1/D, cell id bits, bits of the existing face slots, 0)      per step; static
 //   k 14-15 (j, face code) bits of slots 0,1 and 2,3 (j = -1: no wait)   static
 // Slots without a dependency hold the neutral state (1, 1, 0, 0).
 constexpr int kChainDepth = 8;  // stage records in flight per warp
-constexpr int kChainAhead = 3;  // items ahead at which a remote dependency is read early
+constexpr int kChainAhead = 2;  // items ahead at which a remote dependency is read early
 constexpr int kStageW = 16;
 constexpr int kChainWarps = 8;  // warps (lists) per block
 static_assert(2 * kChainAhead <= kChainDepth && kChainAhead >= 2, "ring accounting");
@@ -1046,8 +1046,7 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         const int j = __float_as_int((s & 1) ? jc.z : jc.x);
         const int code = __float_as_int((s & 1) ? jc.w : jc.y);
         const bool use = j >= 0, left = code > 0;
-        const bool ex0 = __float_as_int(jc01.y) != 0, ex1 = __float_as_int(jc01.w) != 0;
-        const bool ex2 = __float_as_int(jc23.y) != 0, ex3 = __float_as_int(jc23.w) != 0;
+        const int exm = __float_as_int(misc.z);  // bit s: face slot s exists
         float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
         if (use) {
             if (j == hi1) {
@@ -1092,10 +1091,10 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         float v2 = __shfl_sync(mask, DF, 8 + m);
         float v3 = __shfl_sync(mask, DF, 12 + m);
         float dF = 0.f;
-        if (ex0) dF += v0;
-        if (ex1) dF += v1;
-        if (ex2) dF += v2;
-        if (ex3) dF += v3;
+        if (exm & 1) dF += v0;
+        if (exm & 2) dF += v1;
+        if (exm & 4) dF += v2;
+        if (exm & 8) dF += v3;
         const float resf = FWD ? (-ownf_ - dF) * dinvf : ownf_ - dF * dinvf;
         const float r0 = __shfl_sync(mask, resf, 0);
         const float r1 = __shfl_sync(mask, resf, 1);
@@ -1124,7 +1123,11 @@ __global__ void k_chain_static(int nc, const int* __restrict__ cells, const int2
     if (r.x >= 0) g = fg0f[code_face(r.y)];
     st[8 + s] = make_float4(g.x, g.y, g.z, 0.f);
     reinterpret_cast<float2*>(st + 14 + (s >> 1))[s & 1] = make_float2(__int_as_float(r.x), __int_as_float(r.y));
-    if (s == 0) st[13] = make_float4(0.f, __int_as_float(cells[p]), 0.f, 0.f);
+    if (s == 0) {
+        int exm = 0;
+        for (int k = 0; k < 4; k++) exm |= (rec[4 * (long long)p + k].y != 0) << k;
+        st[13] = make_float4(0.f, __int_as_float(cells[p]), __int_as_float(exm), 0.f);
+    }
 }
 
 // Per-step part of both directions' stage records, after k_sweep_prep32 and
