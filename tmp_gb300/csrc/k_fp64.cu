@@ -967,7 +967,7 @@ constexpr int kChainDepth = 8;  // stage records in flight per warp
 constexpr int kChainAhead = 2;  // items ahead at which a remote dependency is read early
 constexpr int kStageW = 16;
 constexpr int kChainWarps = 8;  // warps (lists) per block
-static_assert(2 * kChainAhead <= kChainDepth && kChainAhead >= 2, "ring accounting");
+static_assert(2 * kChainAhead < kChainDepth && kChainAhead >= 2, "ring accounting");
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -1001,9 +1001,11 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
     const int n = p1 - p0;
     float4(*R)[kStageW] = ring[warp];
     float4(*S)[4] = spec[warp];
-    // cp.async group g holds the stage record of item g (g < kChainDepth: the
-    // prologue; later the refill issued while item g - kChainDepth ran) and
-    // the early read of item g - kChainDepth + kChainAhead's remote dependency
+    // cp.async groups: the prologue commits one group per record of items
+    // 0 .. kChainDepth-1; item k then commits the early read for item
+    // k + kChainAhead and, separately and after it, the refill with item
+    // k + kChainDepth, so that waiting for an early read does not wait for the
+    // refill issued beside it
 #pragma unroll
     for (int k = 0; k < kChainDepth; k++) {
         if (k < n) cp_async16(&R[k][lane], stage + (size_t)(p0 + k) * kStageW + lane);
@@ -1015,9 +1017,9 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
     bool gave_up = false;
     for (int k = 0; k < n; k++) {
         const int slot = k % kChainDepth;
-        // groups up to kChainDepth + k - kChainAhead are complete: this item's
-        // record and early read, and the record of item k + kChainAhead
-        cp_async_wait<kChainAhead - 1>();
+        // all but the 2*kChainAhead-1 latest groups are complete: this item's
+        // early read and every refill up to item k + kChainAhead's record
+        cp_async_wait<2 * kChainAhead - 1>();
         __syncwarp(mask);
         const float4 A = R[slot][s];
         const float4 B = R[slot][4 + s];
@@ -1037,8 +1039,9 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
             ida2 = __float_as_int(R[(k + kChainAhead - 2) % kChainDepth][13].y);
         }
         __syncwarp(mask);  // every lane has read the slot before it is refilled
-        if (k + kChainDepth < n) cp_async16(&R[slot][lane], stage + (size_t)(p0 + k + kChainDepth) * kStageW + lane);
         if (m == 0 && ja >= 0 && ja != ida1 && ja != ida2) cp_async16(&S[(k + kChainAhead) % kChainDepth][s], pub + ja);
+        cp_async_commit();
+        if (k + kChainDepth < n) cp_async16(&R[slot][lane], stage + (size_t)(p0 + k + kChainDepth) * kStageW + lane);
         cp_async_commit();
         const int i = __float_as_int(misc.y);
         const float dinvf = misc.x;
