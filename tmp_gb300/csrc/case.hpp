@@ -111,7 +111,7 @@ struct DevArrays {
     // chain-scheduled fast-form sweep (sweep_mode 5), index 0 forward, 1 backward
     int chain_nh = 0;            // warps (lists) the schedule was built for (0: not built)
     int* chain_ptr[2] = {nullptr, nullptr};    // [chain_nh+1] each warp's range of positions
-    int* chain_cells[2] = {nullptr, nullptr};  // [nc] cell at each position
+    int2* chain_cells[2] = {nullptr, nullptr}; // [nc] (cell, local-dependency bits) at each position
     int2* chain_rec[2] = {nullptr, nullptr};   // [4*nc] (lower/upper neighbour or -1, face code) per slot
     float4* chain_stage[2] = {nullptr, nullptr};  // [16*nc] per-position stage records (k_fp64.cu)
     int* chain_posb = nullptr;    // [nc] position of each cell in the backward schedule

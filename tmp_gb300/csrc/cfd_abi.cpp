@@ -173,7 +173,7 @@ void rk_step(cfd_case_s* c) {
 // holds per position and face slot the neighbour the cell waits for (-1:
 // none) and the slot's face code.  nh is a multiple of 8 (warps per block).
 void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, const std::vector<int4>& cface,
-                 const std::vector<int2>& lr, bool fwd, int nh, std::vector<int>& hptr, std::vector<int>& cells,
+                 const std::vector<int2>& lr, bool fwd, int nh, std::vector<int>& hptr, std::vector<int2>& cells,
                  std::vector<int2>& rec) {
     const int nc = (int)order.size();
     std::vector<int> level(nc), hw_of(nc, -1), last(nh, -1), cnt(nh + 1, 0);
@@ -237,18 +237,24 @@ void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, co
     }
     for (int h = 0; h < nh; h++) cnt[h + 1] += cnt[h];
     hptr = cnt;
-    cells.assign(nc, 0);
+    cells.assign(nc, make_int2(0, 0));
     rec.assign(4 * (size_t)nc, make_int2(-1, 0));
     std::vector<int> pos(cnt.begin(), cnt.end() - 1);
     for (int q = 0; q < nc; q++) {  // stable: each list keeps the level order
         const int c = order[q];
-        const int at = pos[hw_of[c]]++;
-        cells[at] = c;
+        const int h = hw_of[c];
+        const int at = pos[h]++;
+        // bits 2s..2s+1 of .y: slot s waits for the list's previous cell (1)
+        // or the one before it (2), which the kernel keeps in registers
+        int lm = 0;
         for (int s = 0; s < 4; s++) {
             int j;
             const int code = dep(c, s, j);
             rec[4 * (size_t)at + s] = make_int2(j, code);
+            if (j >= 0 && at - 1 >= hptr[h] && cells[at - 1].x == j) lm |= 1 << (2 * s);
+            else if (j >= 0 && at - 2 >= hptr[h] && cells[at - 2].x == j) lm |= 2 << (2 * s);
         }
+        cells[at] = make_int2(c, lm);
     }
 }
 
@@ -278,21 +284,21 @@ void ensure_chain(cfd_case_s* c) {
         }
     }
     for (int k = 0; k < 2; k++) {
-        std::vector<int> hptr, cells;
-        std::vector<int2> rec;
+        std::vector<int> hptr;
+        std::vector<int2> cells, rec;
         build_chain(c->h_order[k], k == 0 ? d.fwd_ptr : d.bwd_ptr, c->h_cface, c->h_lr, k == 0, nh, hptr, cells, rec);
         if (d.chain_ptr[k]) cudaFree(d.chain_ptr[k]);
         d.chain_ptr[k] = nullptr;
         dalloc(&d.chain_ptr[k], nh + 1);
         ck(cudaMemcpyAsync(d.chain_ptr[k], hptr.data(), hptr.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
            "upload");
-        ck(cudaMemcpyAsync(d.chain_cells[k], cells.data(), cells.size() * sizeof(int), cudaMemcpyHostToDevice,
+        ck(cudaMemcpyAsync(d.chain_cells[k], cells.data(), cells.size() * sizeof(int2), cudaMemcpyHostToDevice,
                            c->stream), "upload");
         ck(cudaMemcpyAsync(d.chain_rec[k], rec.data(), rec.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream),
            "upload");
         if (k == 1) {
             std::vector<int> posb(d.nc);
-            for (int q = 0; q < d.nc; q++) posb[cells[q]] = q;
+            for (int q = 0; q < d.nc; q++) posb[cells[q].x] = q;
             ck(cudaMemcpyAsync(d.chain_posb, posb.data(), posb.size() * sizeof(int), cudaMemcpyHostToDevice,
                                c->stream), "upload");
             launch_chain_static(d, c->L());

@@ -960,14 +960,17 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 //   k 4-7   (u, v, u^2 + v^2, u nx + v ny) of the same                    per step
 //   k 8-11  (nx, ny, A) of slot s's face; r_A in .w                      static; per step
 //   k 12    own term (R forward, dW1 backward, binary32)                 per step
-//   k 13    (1/D, cell id bits, bits of the existing face slots, 0)      per step; static
+//   k 13    (1/D, cell id, existing-slot bits, local-dependency bits)   per step; static
 //   k 14-15 (j, face code) bits of slots 0,1 and 2,3 (j = -1: no wait)   static
+// Local-dependency bits 2s..2s+1: slot s waits for the list's previous cell
+// (1) or the one before it (2), whose increments the warp holds in registers.
 // Slots without a dependency hold the neutral state (1, 1, 0, 0).
 constexpr int kChainDepth = 8;  // stage records in flight per warp
 constexpr int kChainAhead = 2;  // items ahead at which a remote dependency is read early
 constexpr int kStageW = 16;
 constexpr int kChainWarps = 8;  // warps (lists) per block
-static_assert(2 * kChainAhead < kChainDepth && kChainAhead >= 2, "ring accounting");
+static_assert(2 * kChainAhead + 1 < kChainDepth && kChainAhead >= 2 && (kChainDepth & (kChainDepth - 1)) == 0,
+              "ring accounting");
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -1003,22 +1006,23 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
     float4(*S)[4] = spec[warp];
     // cp.async groups: the prologue commits one group per record of items
     // 0 .. kChainDepth-1; item k then commits the early read for item
-    // k + kChainAhead and, separately and after it, the refill with item
-    // k + kChainDepth, so that waiting for an early read does not wait for the
-    // refill issued beside it
+    // k + kChainAhead and, separately and after it, the refill of item k-1's
+    // slot with item k-1 + kChainDepth, so that waiting for an early read does
+    // not wait for the refill issued beside it
 #pragma unroll
     for (int k = 0; k < kChainDepth; k++) {
         if (k < n) cp_async16(&R[k][lane], stage + (size_t)(p0 + k) * kStageW + lane);
         cp_async_commit();
     }
-    int hi1 = -1, hi2 = -1;  // this warp's last two cells and their increments
-    float4 hd1 = make_float4(0.f, 0.f, 0.f, 0.f), hd2 = hd1;
+    float4 hd1 = make_float4(0.f, 0.f, 0.f, 0.f), hd2 = hd1;  // increments of the last two cells
     const float sent = __uint_as_float(kSentinelF);
     bool gave_up = false;
     for (int k = 0; k < n; k++) {
-        const int slot = k % kChainDepth;
+        const int slot = k & (kChainDepth - 1);
         // all but the 2*kChainAhead-1 latest groups are complete: this item's
-        // early read and every refill up to item k + kChainAhead's record
+        // early read and every refill up to item k + kChainAhead's record.
+        // The barrier also orders the previous item's reads of its slot
+        // before the refill of that slot below.
         cp_async_wait<2 * kChainAhead - 1>();
         __syncwarp(mask);
         const float4 A = R[slot][s];
@@ -1026,35 +1030,34 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         const float4 gr = R[slot][8 + s];
         const float ownf_ = (&R[slot][12].x)[m];
         const float4 misc = R[slot][13];
-        const float4 jc01 = R[slot][14], jc23 = R[slot][15];
+        const float4 jc = R[slot][14 + (s >> 1)];
         const float4 early = k >= kChainAhead ? S[slot][s] : make_float4(sent, sent, sent, sent);
-        // the item kChainAhead positions on: its neighbour, and the two cells
-        // that will be this warp's history when it runs
-        int ja = -1, ida1 = -1, ida2 = -1;
+        // early read for the item kChainAhead positions on, when it waits for
+        // another warp's cell
+        int ja = -1;
         if (k + kChainAhead < n) {
-            const int sa = (k + kChainAhead) % kChainDepth;
+            const int sa = (k + kChainAhead) & (kChainDepth - 1);
             const float4 jca = R[sa][14 + (s >> 1)];
-            ja = __float_as_int((s & 1) ? jca.z : jca.x);
-            ida1 = __float_as_int(R[(k + kChainAhead - 1) % kChainDepth][13].y);
-            ida2 = __float_as_int(R[(k + kChainAhead - 2) % kChainDepth][13].y);
+            const int lma = (__float_as_int(R[sa][13].w) >> (2 * s)) & 3;
+            ja = lma ? -1 : __float_as_int((s & 1) ? jca.z : jca.x);
         }
-        __syncwarp(mask);  // every lane has read the slot before it is refilled
-        if (m == 0 && ja >= 0 && ja != ida1 && ja != ida2) cp_async16(&S[(k + kChainAhead) % kChainDepth][s], pub + ja);
+        if (m == 0 && ja >= 0) cp_async16(&S[(k + kChainAhead) & (kChainDepth - 1)][s], pub + ja);
         cp_async_commit();
-        if (k + kChainDepth < n) cp_async16(&R[slot][lane], stage + (size_t)(p0 + k + kChainDepth) * kStageW + lane);
+        if (k > 0 && k - 1 + kChainDepth < n)
+            cp_async16(&R[(k - 1) & (kChainDepth - 1)][lane], stage + (size_t)(p0 + k - 1 + kChainDepth) * kStageW + lane);
         cp_async_commit();
         const int i = __float_as_int(misc.y);
         const float dinvf = misc.x;
-        const float4 jc = s < 2 ? jc01 : jc23;
+        const int exm = __float_as_int(misc.z);  // bit s: face slot s exists
+        const int lm = (__float_as_int(misc.w) >> (2 * s)) & 3;
         const int j = __float_as_int((s & 1) ? jc.z : jc.x);
         const int code = __float_as_int((s & 1) ? jc.w : jc.y);
         const bool use = j >= 0, left = code > 0;
-        const int exm = __float_as_int(misc.z);  // bit s: face slot s exists
         float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
         if (use) {
-            if (j == hi1) {
+            if (lm == 1) {
                 dw = hd1;
-            } else if (j == hi2) {
+            } else if (lm == 2) {
                 dw = hd2;
             } else {
                 dw = early;
@@ -1072,7 +1075,6 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
                 }
             }
         }
-        __syncwarp(mask);
         const float rho = A.x, Ep = A.y, mx = A.z, my = A.w;
         const float u = B.x, v = B.y, vv = B.z, vn = B.w;
         const float d0 = dw.x, d1 = dw.y, d2 = dw.z, d3 = dw.w;
@@ -1105,9 +1107,7 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         const float r3 = __shfl_sync(mask, resf, 3);
         if (lane == 0) __stcg(pub + i, make_float4(r0, r1, r2, r3));
         if (s == 0) (&dFout[i].x)[m] = dF;
-        hi2 = hi1;
         hd2 = hd1;
-        hi1 = i;
         hd1 = make_float4(r0, r1, r2, r3);
     }
     cp_async_wait<0>();
@@ -1115,7 +1115,7 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
 
 // Static part of the stage records, once per schedule: cell ids, neighbour /
 // face-code pairs and binary32 face geometry.
-__global__ void k_chain_static(int nc, const int* __restrict__ cells, const int2* __restrict__ rec,
+__global__ void k_chain_static(int nc, const int2* __restrict__ cells, const int2* __restrict__ rec,
                                const float4* __restrict__ fg0f, float4* __restrict__ stage) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 4LL * nc) return;
@@ -1129,7 +1129,8 @@ __global__ void k_chain_static(int nc, const int* __restrict__ cells, const int2
     if (s == 0) {
         int exm = 0;
         for (int k = 0; k < 4; k++) exm |= (rec[4 * (long long)p + k].y != 0) << k;
-        st[13] = make_float4(0.f, __int_as_float(cells[p]), __int_as_float(exm), 0.f);
+        const int2 cl = cells[p];
+        st[13] = make_float4(0.f, __int_as_float(cl.x), __int_as_float(exm), __int_as_float(cl.y));
     }
 }
 
