@@ -960,10 +960,10 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 //   k 4-7   (u, v, u^2 + v^2, u nx + v ny) of the same                    per step
 //   k 8-11  (nx, ny, A) of slot s's face; r_A in .w                      static; per step
 //   k 12    own term (R forward, dW1 backward, binary32)                 per step
-//   k 13    (1/D, cell id, existing-slot bits, local-dependency bits)   per step; static
-//   k 14-15 (j, face code) bits of slots 0,1 and 2,3 (j = -1: no wait)   static
-// Local-dependency bits 2s..2s+1: slot s waits for the list's previous cell
-// (1) or the one before it (2), whose increments the warp holds in registers.
+//   k 13    (1/D, cell id, existing-slot bits, 0)                        per step; static
+//   k 14-15 (j, face code) bits of slots 0,1 and 2,3                    static
+// j: the cell slot s waits for, -1 none, -2 / -3 the list's previous cell /
+// the one before it (the warp holds their increments in registers).
 // Slots without a dependency hold the neutral state (1, 1, 0, 0).
 constexpr int kChainDepth = 8;  // stage records in flight per warp
 constexpr int kChainAhead = 2;  // items ahead at which a remote dependency is read early
@@ -1030,16 +1030,14 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         const float4 gr = R[slot][8 + s];
         const float ownf_ = (&R[slot][12].x)[m];
         const float4 misc = R[slot][13];
-        const float4 jc = R[slot][14 + (s >> 1)];
+        const float4 jc01 = R[slot][14], jc23 = R[slot][15];
         const float4 early = k >= kChainAhead ? S[slot][s] : make_float4(sent, sent, sent, sent);
         // early read for the item kChainAhead positions on, when it waits for
         // another warp's cell
         int ja = -1;
         if (k + kChainAhead < n) {
-            const int sa = (k + kChainAhead) & (kChainDepth - 1);
-            const float4 jca = R[sa][14 + (s >> 1)];
-            const int lma = (__float_as_int(R[sa][13].w) >> (2 * s)) & 3;
-            ja = lma ? -1 : __float_as_int((s & 1) ? jca.z : jca.x);
+            const float4 jca = R[(k + kChainAhead) & (kChainDepth - 1)][14 + (s >> 1)];
+            ja = __float_as_int((s & 1) ? jca.z : jca.x);
         }
         if (m == 0 && ja >= 0) cp_async16(&S[(k + kChainAhead) & (kChainDepth - 1)][s], pub + ja);
         cp_async_commit();
@@ -1048,16 +1046,16 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         cp_async_commit();
         const int i = __float_as_int(misc.y);
         const float dinvf = misc.x;
-        const int exm = __float_as_int(misc.z);  // bit s: face slot s exists
-        const int lm = (__float_as_int(misc.w) >> (2 * s)) & 3;
+        const float4 jc = s < 2 ? jc01 : jc23;
         const int j = __float_as_int((s & 1) ? jc.z : jc.x);
         const int code = __float_as_int((s & 1) ? jc.w : jc.y);
-        const bool use = j >= 0, left = code > 0;
+        const bool use = j != -1, left = code > 0;
+        const int exm = __float_as_int(misc.z);  // bit s: face slot s exists
         float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
         if (use) {
-            if (lm == 1) {
+            if (j == -2) {
                 dw = hd1;
-            } else if (lm == 2) {
+            } else if (j == -3) {
                 dw = hd2;
             } else {
                 dw = early;
@@ -1125,12 +1123,14 @@ __global__ void k_chain_static(int nc, const int2* __restrict__ cells, const int
     float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
     if (r.x >= 0) g = fg0f[code_face(r.y)];
     st[8 + s] = make_float4(g.x, g.y, g.z, 0.f);
-    reinterpret_cast<float2*>(st + 14 + (s >> 1))[s & 1] = make_float2(__int_as_float(r.x), __int_as_float(r.y));
+    const int2 cl = cells[p];
+    const int lm = (cl.y >> (2 * s)) & 3;
+    const int jenc = lm == 1 ? -2 : lm == 2 ? -3 : r.x;  // -2 / -3: the list's previous cell / the one before
+    reinterpret_cast<float2*>(st + 14 + (s >> 1))[s & 1] = make_float2(__int_as_float(jenc), __int_as_float(r.y));
     if (s == 0) {
         int exm = 0;
         for (int k = 0; k < 4; k++) exm |= (rec[4 * (long long)p + k].y != 0) << k;
-        const int2 cl = cells[p];
-        st[13] = make_float4(0.f, __int_as_float(cl.x), __int_as_float(exm), __int_as_float(cl.y));
+        st[13] = make_float4(0.f, __int_as_float(cl.x), __int_as_float(exm), 0.f);
     }
 }
 
@@ -1139,6 +1139,7 @@ __global__ void k_chain_static(int nc, const int2* __restrict__ cells, const int
 // (k_sweep_flow32's expressions), r_A, 1/D and the forward own term R.  (The
 // backward own term, dW1, is written by k_chain_mid.)
 __global__ void k_chain_stage(int nc, float4* __restrict__ stage_f, float4* __restrict__ stage_b,
+                              const int2* __restrict__ rec_f, const int2* __restrict__ rec_b,
                               const float4* __restrict__ Wf, const float* __restrict__ swraf,
                               const d4* __restrict__ R, const double* __restrict__ invD) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1148,8 +1149,7 @@ __global__ void k_chain_stage(int nc, float4* __restrict__ stage_f, float4* __re
     const long long q = dir ? t - 4LL * nc : t;
     const int p = (int)(q >> 2), s = (int)(q & 3);
     float4* st = (dir ? stage_b : stage_f) + (size_t)p * kStageW;
-    const float4 jc = st[14 + (s >> 1)];
-    const int j = __float_as_int((s & 1) ? jc.z : jc.x);
+    const int j = (dir ? rec_b : rec_f)[q].x;
     const int i = __float_as_int(st[13].y);
     float4 w0 = make_float4(1.f, 1.f, 0.f, 0.f);
     float rA = 0.f, u = 0.f, v = 0.f, vv = 0.f, pb = 0.f, vn = 0.f;
@@ -1234,8 +1234,9 @@ cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool fo
     int nh = d.chain_nh;
     float4* pub = forward ? d.dW1f : d.dWf;
     if (forward) {
-        k_chain_stage<<<nblk(8 * d.nc, 256), 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1], d.Wf,
-                                                                 d.swraf, d.R, d.invD);
+        k_chain_stage<<<nblk(8 * d.nc, 256), 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
+                                                                 d.chain_rec[0], d.chain_rec[1], d.Wf, d.swraf,
+                                                                 d.R, d.invD);
         *L.counter += 1;
     }
     void* args[] = {(void*)&nh, (void*)&d.chain_ptr[k], (void*)&d.chain_stage[k], (void*)&pub, (void*)&d.chain_dF,
