@@ -149,7 +149,7 @@ void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
 void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, bool mu64);
 cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool independent);
 int sweep_chain_max_grid(int blocks_per_sm);
-cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
+cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool viscous, bool mu64);
 void launch_chain_static(const DevArrays& d, const LaunchCfg& L);
 void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);

@@ -329,16 +329,15 @@ void sweeps(cfd_case_s* c, bool forward) {
         return;
     }
     // default: one dataflow launch per direction (binary64 form, mode 3: two cells per warp)
-    if (c->fast_sweep()) {
-        if (c->p.sweep_mode == 5) ensure_chain(c);
+    if (c->fast_sweep() && c->p.sweep_mode == 5) {  // the staging pass replaces 1/D and the sweep constants
+        ensure_chain(c);
+        ck(launch_sweep_chain32(d, L, forward, chain_grid(c), c->viscous(), c->mixed()), "cooperative sweep launch");
+    } else if (c->fast_sweep()) {
         if (forward) {
             launch_inv_diag(d, L);
             launch_sweep_prep32(d, L, c->viscous(), c->mixed());
         }
-        if (c->p.sweep_mode == 5)
-            ck(launch_sweep_chain32(d, L, forward, chain_grid(c)), "cooperative sweep launch");
-        else
-            ck(launch_sweep_flow32(d, L, forward, d.flow_grid, c->p.sweep_mode == 4), "cooperative sweep launch");
+        ck(launch_sweep_flow32(d, L, forward, d.flow_grid, c->p.sweep_mode == 4), "cooperative sweep launch");
     } else if (c->p.sweep_mode == 3) {
         ck(launch_sweep_pair64(d, L, forward, d.flow_grid), "cooperative sweep launch");
     } else {

@@ -941,7 +941,7 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 // dW = dW1 - sum / D with the expressions of k_sweep_flow32.
 //
 // Per-item data are staged per step in schedule order (16 float4 per
-// position, k_chain_stage, which also forms the neighbour's velocity, pressure
+// position, k_chain_prep, which also forms the neighbour's velocity, pressure
 // and normal velocity: the terms of the flux difference that do not depend on
 // the increment) and copied ahead into a shared-memory ring of kChainDepth
 // items per warp with cp.async; the increment of a remote dependency is also
@@ -956,7 +956,7 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 // warp stops waiting and the error word carries ERR_TIMEOUT.
 //
 // Stage record of position p (float4 index p*16 + k), slot s = face slot:
-//   k 0-3   (rho, E + p, rho u, rho v) of slot s's neighbour (binary32)   per step
+//   k 0-3   (rho, E + p, rho u, rho v) of slot s's neighbour (binary32)   per step (k_chain_prep)
 //   k 4-7   (u, v, u^2 + v^2, u nx + v ny) of the same                    per step
 //   k 8-11  (nx, ny, A) of slot s's face; r_A in .w                      static; per step
 //   k 12    own term (R forward, dW1 backward, binary32)                 per step
@@ -1134,29 +1134,43 @@ __global__ void k_chain_static(int nc, const int2* __restrict__ cells, const int
     }
 }
 
-// Per-step part of both directions' stage records, after k_sweep_prep32 and
-// k_inv_diag: the neighbours' binary32 state and its increment-free terms
-// (k_sweep_flow32's expressions), r_A, 1/D and the forward own term R.  (The
+// Per-step part of both directions' stage records, in place of k_inv_diag and
+// k_sweep_prep32 for the chain sweep: the neighbours' binary32 state and its
+// increment-free terms, r_A, 1/D (also kept in binary64 for k_chain_mid /
+// k_chain_finish) and the forward own term R, every value with the
+// expression those kernels and k_sweep_flow32 use; it also resets both
+// directions' published increments to the "not yet computed" sentinel.  (The
 // backward own term, dW1, is written by k_chain_mid.)
-__global__ void k_chain_stage(int nc, float4* __restrict__ stage_f, float4* __restrict__ stage_b,
-                              const int2* __restrict__ rec_f, const int2* __restrict__ rec_b,
-                              const float4* __restrict__ Wf, const float* __restrict__ swraf,
-                              const d4* __restrict__ R, const double* __restrict__ invD) {
+template <bool VISC, class MuT>
+__global__ void k_chain_prep(int nc, float4* __restrict__ stage_f, float4* __restrict__ stage_b,
+                             const int2* __restrict__ rec_f, const int2* __restrict__ rec_b,
+                             const float4* __restrict__ fvisf, const d4* __restrict__ W, const d4* __restrict__ U,
+                             const MuT* __restrict__ mu, const d4* __restrict__ R, const double* __restrict__ D,
+                             double* __restrict__ invD, float* __restrict__ pub_f, float* __restrict__ pub_b) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 8LL * nc) return;
     const float GM1 = 1.4f - 1.0f;
+    const float G = 1.4f;
     const int dir = t >= 4LL * nc;
     const long long q = dir ? t - 4LL * nc : t;
     const int p = (int)(q >> 2), s = (int)(q & 3);
     float4* st = (dir ? stage_b : stage_f) + (size_t)p * kStageW;
-    const int j = (dir ? rec_b : rec_f)[q].x;
+    const int2 r = (dir ? rec_b : rec_f)[q];
+    const int j = r.x;
     const int i = __float_as_int(st[13].y);
+    (dir ? pub_b : pub_f)[(size_t)i * 4 + s] = __uint_as_float(kSentinelF);
     float4 w0 = make_float4(1.f, 1.f, 0.f, 0.f);
     float rA = 0.f, u = 0.f, v = 0.f, vv = 0.f, pb = 0.f, vn = 0.f;
     if (j >= 0) {
         const float4 g = st[8 + s];
-        w0 = Wf[j];
-        rA = swraf[(size_t)i * 4 + s];
+        const d4 w = ld4(W + j);
+        w0 = make_float4((float)w.x, (float)w.y, (float)w.z, (float)w.w);
+        const d4 ud = ld4(U + j);
+        const float uj[4] = {(float)ud.x, (float)ud.y, (float)ud.z, (float)ud.w};
+        const float vr = uj[2] * g.x + uj[3] * g.y;
+        const float c = sqrtf(G * uj[1] / uj[0]);
+        rA = 1.5f * (fabsf(vr) + c);
+        if (VISC) rA += fmaxf(4.f / (3.f * uj[0]), G / uj[0]) * ((float)mu[i] / 0.72f) / sqrtf(fvisf[code_face(r.y)].z);
         u = w0.z / w0.x;
         v = w0.w / w0.x;
         vv = u * u + v * v;
@@ -1167,10 +1181,12 @@ __global__ void k_chain_stage(int nc, float4* __restrict__ stage_f, float4* __re
     st[4 + s] = make_float4(u, v, vv, vn);
     st[8 + s].w = rA;
     if (s == 0) {
-        st[13].x = (float)invD[i];
+        const double dinv = 1.0 / D[i];
+        st[13].x = (float)dinv;
         if (!dir) {
-            const d4 r = ld4(R + i);
-            st[12] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
+            invD[i] = dinv;
+            const d4 rr = ld4(R + i);
+            st[12] = make_float4((float)rr.x, (float)rr.y, (float)rr.z, (float)rr.w);
         }
     }
 }
@@ -1229,14 +1245,27 @@ void launch_chain_static(const DevArrays& d, const LaunchCfg& L) {
     *L.counter += 2;
 }
 
-cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid) {
+cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool viscous,
+                                 bool mu64) {
     const int k = forward ? 0 : 1;
     int nh = d.chain_nh;
     float4* pub = forward ? d.dW1f : d.dWf;
     if (forward) {
-        k_chain_stage<<<nblk(8 * d.nc, 256), 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
-                                                                 d.chain_rec[0], d.chain_rec[1], d.Wf, d.swraf,
-                                                                 d.R, d.invD);
+        float* pf = reinterpret_cast<float*>(d.dW1f);
+        float* pb = reinterpret_cast<float*>(d.dWf);
+        const int nb = nblk(8 * d.nc, 256);
+        if (viscous && mu64)
+            k_chain_prep<true, double><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
+                                                                 d.chain_rec[0], d.chain_rec[1], d.fvisf, d.W, d.U,
+                                                                 d.mu, d.R, d.diag, d.invD, pf, pb);
+        else if (viscous)
+            k_chain_prep<true, float><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
+                                                                d.chain_rec[0], d.chain_rec[1], d.fvisf, d.W, d.U,
+                                                                d.muf, d.R, d.diag, d.invD, pf, pb);
+        else
+            k_chain_prep<false, float><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
+                                                                 d.chain_rec[0], d.chain_rec[1], d.fvisf, d.W, d.U,
+                                                                 (const float*)nullptr, d.R, d.diag, d.invD, pf, pb);
         *L.counter += 1;
     }
     void* args[] = {(void*)&nh, (void*)&d.chain_ptr[k], (void*)&d.chain_stage[k], (void*)&pub, (void*)&d.chain_dF,
