@@ -59,7 +59,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--sweep-mode", type=int, default=0, help="LU-SGS schedule (0 dataflow, 1/2 per level, 5 chain-scheduled binary32 dataflow)")
+    ap.add_argument("--sweep-mode", type=int, default=-1,
+                    help="LU-SGS schedule (-1 auto: 5 for the binary32-sweep forms, 0 for fp64; 0 dataflow, "
+                         "1/2 per level, 5 chain-scheduled binary32 dataflow)")
     ap.add_argument("--sweep-bpsm", type=int, default=0, help="dataflow sweep blocks per SM (0 = autotune)")
     ap.add_argument("--sweep-poll-ns", type=int, default=0, help="dataflow sweep back-off between polls (ns)")
     ap.add_argument("--forms", default="fp64,fp32,mixed", help="precision forms timed besides --precision ('' = none)")
@@ -257,7 +259,7 @@ def overset_leg(stream) -> dict:
     return out
 
 
-def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5) -> dict:
+def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5, mode: int = 0) -> dict:
     """The uneven batch: `nmesh` independent meshes of 5k-200k cells (sizes
     log-uniform from a seed, cylinder or NACA 0012 bodies, quads + triangles),
     half Euler and half viscous, advanced by LU-SGS.  Each flow family is one
@@ -302,7 +304,7 @@ def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5) -> dict:
 
     errors: list[str] = []
     packed = [abi.Case([m for m, _ in g], [f for _, f in g], flow_code[fl], abi.ADV_LUSGS, precision, cfl=cfl,
-                       stream=stream.cuda_stream) for fl, g in groups.items()]
+                       stream=stream.cuda_stream, sweep_mode=mode) for fl, g in groups.items()]
     tuned = [c.autotune(2)[0] for c in packed]
     ms_packed = run(packed)
     net = learn.load()
@@ -318,14 +320,15 @@ def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5) -> dict:
         ms_learned = run(packed, init=False)
     for c in packed:
         c.close()
-    separate = [abi.Case([m], [f], flow_code[fl], abi.ADV_LUSGS, precision, cfl=cfl, stream=stream.cuda_stream)
-                for fl, g in groups.items() for m, f in g]
+    separate = [abi.Case([m], [f], flow_code[fl], abi.ADV_LUSGS, precision, cfl=cfl, stream=stream.cuda_stream,
+                         sweep_mode=mode) for fl, g in groups.items() for m, f in g]
     ms_sep = run(separate)
     for c in separate:
         c.close()
     levels = [m.levels()[0] for m in meshes]
     sizes = sorted(m.ncell for m in meshes)
     return {"workload": f"{nmesh} meshes, 5k-200k cells log-uniform (seed 5005), half Euler / half laminar, LU-SGS CFL {cfl:g}",
+            "sweep_mode": mode,
             "meshes": nmesh, "cells": ncell, "cells_min_median_max": [sizes[0], sizes[len(sizes) // 2], sizes[-1]],
             "packed_cases": {fl: len(g) for fl, g in groups.items()}, "sweep_blocks_per_sm": tuned,
             "forward_levels_max_sum": [max(levels), sum(levels)], "steps": steps,
@@ -443,16 +446,22 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     prec_code = dict(fp64=abi.PREC_FP64, fp32=abi.PREC_FP32, mixed=abi.PREC_MIXED)
 
+    def sweep_mode_for(precision):
+        if args.sweep_mode >= 0:
+            return args.sweep_mode
+        return 5 if precision in ("fp32", "mixed") else 0
+
     def make_case(precision):
+        mode = sweep_mode_for(precision)
         c = abi.Case([mesh], [dict(mach=w.mach, aoa_deg=w.aoa, reynolds=w.re)],
                      abi.FLOW_LAMINAR if viscous else abi.FLOW_EULER,
                      abi.ADV_LUSGS if w.advance == "lusgs" else abi.ADV_RK5,
                      prec_code[precision], cfl=w.cfl, stream=stream.cuda_stream,
-                     sweep_mode=args.sweep_mode, sweep_blocks_per_sm=args.sweep_bpsm,
+                     sweep_mode=mode, sweep_blocks_per_sm=args.sweep_bpsm,
                      sweep_poll_ns=args.sweep_poll_ns)
         c.init_freestream()
         c.tuned = None
-        if args.sweep_bpsm == 0 and w.advance == "lusgs" and args.sweep_mode in (0, 3, 4, 5):
+        if args.sweep_bpsm == 0 and w.advance == "lusgs" and mode in (0, 3, 4, 5):
             c.tuned = c.autotune(3)[0]  # the sweeps' blocks per SM, by timing whole steps
         return c
 
@@ -562,14 +571,20 @@ def run_ours(args):
     passes = ["face_state", "cell_grad", "face_flux", "cell_update"]
     if w.advance == "lusgs":
         passes += ["sweep_fwd", "sweep_bwd", "lusgs_update"]
-    per = {p: case.bench_pass(p, 5, FLUSH_BYTES) for p in passes}
+    mode = sweep_mode_for(args.precision)
+    per, launches_of = {}, {}
+    for p in passes:
+        l0 = case.launches()
+        per[p] = case.bench_pass(p, 5, FLUSH_BYTES)
+        n_l = round((case.launches() - l0) / 5)
+        if p == "sweep_bwd" and mode not in (1, 2):
+            n_l -= 1  # the untimed reset that a lone backward sweep needs
+        launches_of[p] = n_l
     per_step = dict(per)
     if w.advance == "rk5":
         per_step = {p: 5 * v for p, v in per.items()}
     dominant = max(per_step, key=per_step.get)
     nlev = mesh.levels()
-    per_level = args.sweep_mode in (1, 2)  # modes 1 and 2 launch once per level; the dataflow sweeps once per direction
-    launches_of = {"sweep_fwd": nlev[0] if per_level else 1, "sweep_bwd": nlev[1] if per_level else 1}
     peak, peak_kind = measured_peak_gbs()
     rows = {}
     for p, v in per.items():
@@ -607,7 +622,7 @@ def run_ours(args):
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
             "config": {"workload": w.name, "ncell": nc, "nedge": nf, "levels": list(nlev), "mach": w.mach,
-                       "re": w.re, "cfl": w.cfl, "precision": args.precision,
+                       "re": w.re, "cfl": w.cfl, "precision": args.precision, "sweep_mode": mode,
                        "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "forms": forms,
             "time_to_drop": drop}
@@ -615,7 +630,7 @@ def run_ours(args):
         line["overset"] = overset_leg(stream)
     if rank == 0 and not args.no_batch and w.advance == "lusgs":
         try:
-            line["batch"] = batch_leg(stream, prec_code[args.precision], args.batch_meshes)
+            line["batch"] = batch_leg(stream, prec_code[args.precision], args.batch_meshes, mode=mode)
         except Exception as ex:  # the leg is reported beside the headline, never instead of it
             line["batch"] = {"error": f"{type(ex).__name__}: {ex}"}
     if rank == 0 and not args.no_cpu_baseline:
