@@ -305,7 +305,10 @@ def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5, mode: in
     errors: list[str] = []
     packed = [abi.Case([m for m, _ in g], [f for _, f in g], flow_code[fl], abi.ADV_LUSGS, precision, cfl=cfl,
                        stream=stream.cuda_stream, sweep_mode=mode) for fl, g in groups.items()]
-    tuned = [c.autotune(2)[0] for c in packed]
+    tuned = []
+    for c in packed:
+        c.autotune(2)
+        tuned.append(dict(zip(("mode", "blocks_per_sm"), c.sweep_config())))
     ms_packed = run(packed)
     net = learn.load()
     ms_learned = None
@@ -328,14 +331,13 @@ def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5, mode: in
     levels = [m.levels()[0] for m in meshes]
     sizes = sorted(m.ncell for m in meshes)
     return {"workload": f"{nmesh} meshes, 5k-200k cells log-uniform (seed 5005), half Euler / half laminar, LU-SGS CFL {cfl:g}",
-            "sweep_mode": mode,
             "meshes": nmesh, "cells": ncell, "cells_min_median_max": [sizes[0], sizes[len(sizes) // 2], sizes[-1]],
-            "packed_cases": {fl: len(g) for fl, g in groups.items()}, "sweep_blocks_per_sm": tuned,
+            "packed_cases": {fl: len(g) for fl, g in groups.items()}, "packed_sweep": tuned,
             "forward_levels_max_sum": [max(levels), sum(levels)], "steps": steps,
             "packed_ms_per_step": round(ms_packed, 3), "packed_cell_iters_per_s": ncell / (ms_packed * 1e-3),
             "packed_learned_ms_per_step": round(ms_learned, 3) if ms_learned else None,
             "packed_learned_cell_iters_per_s": ncell / (ms_learned * 1e-3) if ms_learned else None,
-            "separate_ms_per_step": round(ms_sep, 3), "separate_cell_iters_per_s": ncell / (ms_sep * 1e-3),
+            "separate_sweep_mode": mode, "separate_ms_per_step": round(ms_sep, 3), "separate_cell_iters_per_s": ncell / (ms_sep * 1e-3),
             "solver_errors": sorted(set(errors))}
 
 
@@ -462,7 +464,8 @@ def run_ours(args):
         c.init_freestream()
         c.tuned = None
         if args.sweep_bpsm == 0 and w.advance == "lusgs" and mode in (0, 3, 4, 5):
-            c.tuned = c.autotune(3)[0]  # the sweeps' blocks per SM, by timing whole steps
+            c.autotune(3)  # the sweeps' blocks per SM (and mode 0 or 5), by timing whole steps
+            c.tuned = c.sweep_config()
         return c
 
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -536,10 +539,10 @@ def run_ours(args):
         c2 = make_case(f)
         fm, _ = timed_steps(c2, args.steps)
         forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3),
-                    "sweep_blocks_per_sm": c2.tuned}
+                    "sweep": dict(zip(("mode", "blocks_per_sm"), c2.sweep_config()))}
         c2.close()
     forms[args.precision] = {"ms_per_step": 1e3 * t_local / args.steps, "value": nc * args.steps / t_local,
-                             "sweep_blocks_per_sm": case.tuned}
+                             "sweep": dict(zip(("mode", "blocks_per_sm"), case.sweep_config()))}
 
     # wall time from the freestream start to a residual fall of args.drop, per
     # form, and with the committed learned relaxation on the mixed form
@@ -622,7 +625,8 @@ def run_ours(args):
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
             "config": {"workload": w.name, "ncell": nc, "nedge": nf, "levels": list(nlev), "mach": w.mach,
-                       "re": w.re, "cfl": w.cfl, "precision": args.precision, "sweep_mode": mode,
+                       "re": w.re, "cfl": w.cfl, "precision": args.precision,
+                       "sweep": dict(zip(("mode", "blocks_per_sm"), case.sweep_config())),
                        "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "forms": forms,
             "time_to_drop": drop}

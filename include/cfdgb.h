@@ -218,8 +218,13 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
 /* Autotuner of the dataflow sweeps' launch shape (no reference counterpart):
  * times `reps` whole LU-SGS steps for each co-resident block count per SM
  * (1, 2, ... up to the occupancy limit), keeps the fastest for the case and
- * reports it; the case's state is restored afterwards. */
+ * reports it; the case's state is restored afterwards.  For the binary32-sweep
+ * forms of a case created with sweep_mode 0 or 5 it also picks between those
+ * two schedules (cfd_case_sweep reads the choice). */
 int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_ms);
+/* The case's current LU-SGS schedule: sweep_mode and blocks per SM (after
+ * cfd_autotune, the ones it chose). No reference counterpart. */
+int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm);
 /* Failure-detection self-test (no reference counterpart): launch a kernel that
  * waits, at most `polls` polls, on a device flag nothing sets, exactly as the
  * dataflow LU-SGS sweep waits on its neighbours.  Returns CFD_ERR_TIMEOUT when

@@ -130,6 +130,7 @@ def lib() -> C.CDLL:
         "cfd_measure_hop_latency": (C.c_int, [vp, C.c_int, C.c_int, dp]),
         "cfd_set_precision": (C.c_int, [vp, C.c_int]),
         "cfd_autotune": (C.c_int, [vp, C.c_int, ip, dp]),
+        "cfd_case_sweep": (C.c_int, [vp, ip, ip]),
         "cfd_sst_enable": (C.c_int, [vp]),
         "cfd_sst_freestream": (C.c_int, [vp, C.c_int, dp]),
         "cfd_sst_residual": (C.c_int, [vp]),
@@ -252,6 +253,12 @@ class Case:
         b, t = C.c_int(), C.c_double()
         check(lib().cfd_autotune(self.h, int(reps), C.byref(b), C.byref(t)))
         return b.value, t.value
+
+    def sweep_config(self):
+        """(sweep_mode, blocks_per_sm) in use, e.g. after autotune()."""
+        a, b = C.c_int(), C.c_int()
+        check(lib().cfd_case_sweep(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_precision(self, precision: int):
         check(lib().cfd_set_precision(self.h, int(precision)))

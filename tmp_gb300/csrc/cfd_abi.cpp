@@ -1447,6 +1447,13 @@ extern "C" int cfd_set_precision(cfd_case_t c, int precision) {
 // Autotuning the dataflow sweeps' launch shape
 // ---------------------------------------------------------------------------
 
+extern "C" int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (sweep_mode) *sweep_mode = c->p.sweep_mode;
+    if (blocks_per_sm) *blocks_per_sm = c->p.sweep_blocks_per_sm;
+    return CFD_OK;
+}
+
 extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_ms) {
     if (!c || reps <= 0) return fail(CFD_ERR_ARG, "cfd_autotune: null case or reps <= 0");
     if (c->p.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_STATE, "cfd_autotune: only the LU-SGS sweeps are tuned");
@@ -1469,23 +1476,36 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
     upload_freestream(c);  // synchronises: err0 is valid from here
     const bool low = c->p.precision != CFD_PREC_FP64;
     const int max_grid = sweep_flow_max_grid(low, 64);  // occupancy limit
-    int best = 0, last_grid = -1;
+    // the binary32 forms also choose between the round-robin dataflow sweep
+    // (mode 0: wide levels, many cells in flight) and the chain schedule
+    // (mode 5: narrow levels, long dependence chains)
+    std::vector<int> modes{c->p.sweep_mode};
+    if (c->fast_sweep() && (c->p.sweep_mode == 0 || c->p.sweep_mode == 5)) modes = {0, 5};
+    const int mode0 = c->p.sweep_mode;
+    int best = 0, best_mode = mode0;
     double best_t = 1e300;
     int rc = CFD_OK;
-    for (int bpsm = 1; bpsm <= 8; bpsm++) {
-        const int grid = sweep_flow_max_grid(low, bpsm);
-        if (grid == last_grid || grid > max_grid) break;  // capped by occupancy: nothing new to try
-        last_grid = grid;
-        d.flow_grid = grid;
-        c->drop_graph();
-        double ms = 0;
-        rc = cfd_bench_pass(c, 7, reps, 0, &ms);
-        if (rc != CFD_OK) break;
-        if (ms < best_t) {
-            best_t = ms;
-            best = bpsm;
+    for (int mode : modes) {
+        c->p.sweep_mode = mode;
+        int last_grid = -1;
+        for (int bpsm = 1; bpsm <= 8 && rc == CFD_OK; bpsm++) {
+            const int grid = sweep_flow_max_grid(low, bpsm);
+            if (grid > max_grid) break;
+            d.flow_grid = grid;
+            const int eff = mode == 5 && c->fast_sweep() ? chain_grid(c) : grid;
+            if (eff == last_grid) break;  // capped by occupancy: nothing new to try
+            last_grid = eff;
+            c->drop_graph();
+            double ms = 0;
+            rc = cfd_bench_pass(c, 7, reps, 0, &ms);
+            if (rc == CFD_OK && ms < best_t) {
+                best_t = ms;
+                best = bpsm;
+                best_mode = mode;
+            }
         }
     }
+    c->p.sweep_mode = rc == CFD_OK ? best_mode : mode0;
     if (rc == CFD_OK) {
         c->p.sweep_blocks_per_sm = best;
         d.flow_grid = sweep_flow_max_grid(low, best);
