@@ -941,7 +941,7 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 // dW = dW1 - sum / D with the expressions of k_sweep_flow32.
 //
 // Per-item data are staged per step in schedule order (16 float4 per
-// position, k_chain_prep, which also forms the neighbour's velocity, pressure
+// position, k_chain_cell and k_chain_prep, which also form the neighbour's velocity, pressure
 // and normal velocity: the terms of the flux difference that do not depend on
 // the increment) and copied ahead into a shared-memory ring of kChainDepth
 // items per warp with cp.async; the increment of a remote dependency is also
@@ -956,7 +956,7 @@ int sweep_flow_max_grid(bool low, int blocks_per_sm) {
 // warp stops waiting and the error word carries ERR_TIMEOUT.
 //
 // Stage record of position p (float4 index p*16 + k), slot s = face slot:
-//   k 0-3   (rho, E + p, rho u, rho v) of slot s's neighbour (binary32)   per step (k_chain_prep)
+//   k 0-3   (rho, E + p, rho u, rho v) of slot s's neighbour (binary32)   per step (k_chain_cell / _prep)
 //   k 4-7   (u, v, u^2 + v^2, u nx + v ny) of the same                    per step
 //   k 8-11  (nx, ny, A) of slot s's face; r_A in .w                      static; per step
 //   k 12    own term (R forward, dW1 backward, binary32)                 per step
@@ -1134,19 +1134,47 @@ __global__ void k_chain_static(int nc, const int2* __restrict__ cells, const int
     }
 }
 
-// Per-step part of both directions' stage records, in place of k_inv_diag and
-// k_sweep_prep32 for the chain sweep: the neighbours' binary32 state and its
-// increment-free terms, r_A, 1/D (also kept in binary64 for k_chain_mid /
-// k_chain_finish) and the forward own term R, every value with the
-// expression those kernels and k_sweep_flow32 use; it also resets both
-// directions' published increments to the "not yet computed" sentinel.  (The
-// backward own term, dW1, is written by k_chain_mid.)
+// Per-step cell pass of the chain sweep, in place of k_inv_diag and the cell
+// part of k_sweep_prep32: binary32 copies of W and U (each converted once,
+// with the conversions those kernels use), 1/D in binary64 (for k_chain_mid /
+// k_chain_finish) and binary32 (both directions' stage records), the forward
+// own term R, and the "not yet computed" sentinel in both directions'
+// published increments.
+__global__ void k_chain_cell(int nc, const d4* __restrict__ W, const d4* __restrict__ U, const d4* __restrict__ R,
+                             const double* __restrict__ D, const int* __restrict__ posf,
+                             const int* __restrict__ posb, float4* __restrict__ Wf, float4* __restrict__ Uf,
+                             double* __restrict__ invD, float4* __restrict__ stage_f, float4* __restrict__ stage_b,
+                             float4* __restrict__ pub_f, float4* __restrict__ pub_b) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const d4 w = ld4(W + c), u = ld4(U + c), r = ld4(R + c);
+    Wf[c] = make_float4((float)w.x, (float)w.y, (float)w.z, (float)w.w);
+    Uf[c] = make_float4((float)u.x, (float)u.y, (float)u.z, (float)u.w);
+    const double dinv = 1.0 / D[c];
+    invD[c] = dinv;
+    const float dinvf = (float)dinv;
+    float4* sf = stage_f + (size_t)posf[c] * kStageW;
+    float4* sb = stage_b + (size_t)posb[c] * kStageW;
+    sf[12] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
+    float4 mf = sf[13], mb = sb[13];
+    mf.x = dinvf;
+    mb.x = dinvf;
+    sf[13] = mf;
+    sb[13] = mb;
+    const float sent = __uint_as_float(kSentinelF);
+    pub_f[c] = make_float4(sent, sent, sent, sent);
+    pub_b[c] = make_float4(sent, sent, sent, sent);
+}
+
+// Per-step slot pass of both directions' stage records, after k_chain_cell:
+// the neighbours' binary32 state, its increment-free terms and r_A, each with
+// the expression k_sweep_prep32 and k_sweep_flow32 use.  (The backward own
+// term, dW1, is written by k_chain_mid.)
 template <bool VISC, class MuT>
 __global__ void k_chain_prep(int nc, float4* __restrict__ stage_f, float4* __restrict__ stage_b,
                              const int2* __restrict__ rec_f, const int2* __restrict__ rec_b,
-                             const float4* __restrict__ fvisf, const d4* __restrict__ W, const d4* __restrict__ U,
-                             const MuT* __restrict__ mu, const d4* __restrict__ R, const double* __restrict__ D,
-                             double* __restrict__ invD, float* __restrict__ pub_f, float* __restrict__ pub_b) {
+                             const float4* __restrict__ fvisf, const float4* __restrict__ Wf,
+                             const float4* __restrict__ Uf, const MuT* __restrict__ mu) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 8LL * nc) return;
     const float GM1 = 1.4f - 1.0f;
@@ -1157,16 +1185,14 @@ __global__ void k_chain_prep(int nc, float4* __restrict__ stage_f, float4* __res
     float4* st = (dir ? stage_b : stage_f) + (size_t)p * kStageW;
     const int2 r = (dir ? rec_b : rec_f)[q];
     const int j = r.x;
-    const int i = __float_as_int(st[13].y);
-    (dir ? pub_b : pub_f)[(size_t)i * 4 + s] = __uint_as_float(kSentinelF);
+    const float4 g = st[8 + s];
     float4 w0 = make_float4(1.f, 1.f, 0.f, 0.f);
     float rA = 0.f, u = 0.f, v = 0.f, vv = 0.f, pb = 0.f, vn = 0.f;
     if (j >= 0) {
-        const float4 g = st[8 + s];
-        const d4 w = ld4(W + j);
-        w0 = make_float4((float)w.x, (float)w.y, (float)w.z, (float)w.w);
-        const d4 ud = ld4(U + j);
-        const float uj[4] = {(float)ud.x, (float)ud.y, (float)ud.z, (float)ud.w};
+        const int i = __float_as_int(st[13].y);
+        w0 = Wf[j];
+        const float4 uf = Uf[j];
+        const float uj[4] = {uf.x, uf.y, uf.z, uf.w};
         const float vr = uj[2] * g.x + uj[3] * g.y;
         const float c = sqrtf(G * uj[1] / uj[0]);
         rA = 1.5f * (fabsf(vr) + c);
@@ -1179,16 +1205,7 @@ __global__ void k_chain_prep(int nc, float4* __restrict__ stage_f, float4* __res
     }
     st[s] = make_float4(w0.x, w0.y + pb, w0.z, w0.w);
     st[4 + s] = make_float4(u, v, vv, vn);
-    st[8 + s].w = rA;
-    if (s == 0) {
-        const double dinv = 1.0 / D[i];
-        st[13].x = (float)dinv;
-        if (!dir) {
-            invD[i] = dinv;
-            const d4 rr = ld4(R + i);
-            st[12] = make_float4((float)rr.x, (float)rr.y, (float)rr.z, (float)rr.w);
-        }
-    }
+    st[8 + s] = make_float4(g.x, g.y, g.z, rA);
 }
 
 // dW1 = (-R - sum) * (1/D) in binary64 (k_sweep_flow32's forward expression),
@@ -1251,22 +1268,23 @@ cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool fo
     int nh = d.chain_nh;
     float4* pub = forward ? d.dW1f : d.dWf;
     if (forward) {
-        float* pf = reinterpret_cast<float*>(d.dW1f);
-        float* pb = reinterpret_cast<float*>(d.dWf);
+        k_chain_cell<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.W, d.U, d.R, d.diag, d.chain_posf, d.chain_posb,
+                                                            d.Wf, d.Uf, d.invD, d.chain_stage[0], d.chain_stage[1],
+                                                            d.dW1f, d.dWf);
         const int nb = nblk(8 * d.nc, 256);
         if (viscous && mu64)
             k_chain_prep<true, double><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
-                                                                 d.chain_rec[0], d.chain_rec[1], d.fvisf, d.W, d.U,
-                                                                 d.mu, d.R, d.diag, d.invD, pf, pb);
+                                                                 d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
+                                                                 d.mu);
         else if (viscous)
             k_chain_prep<true, float><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
-                                                                d.chain_rec[0], d.chain_rec[1], d.fvisf, d.W, d.U,
-                                                                d.muf, d.R, d.diag, d.invD, pf, pb);
+                                                                d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
+                                                                d.muf);
         else
             k_chain_prep<false, float><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
-                                                                 d.chain_rec[0], d.chain_rec[1], d.fvisf, d.W, d.U,
-                                                                 (const float*)nullptr, d.R, d.diag, d.invD, pf, pb);
-        *L.counter += 1;
+                                                                 d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
+                                                                 (const float*)nullptr);
+        *L.counter += 2;
     }
     void* args[] = {(void*)&nh, (void*)&d.chain_ptr[k], (void*)&d.chain_stage[k], (void*)&pub, (void*)&d.chain_dF,
                     (void*)&d.err, (void*)&d.poll_ns};
