@@ -174,8 +174,11 @@ def traffic_bytes(pass_name: str, precision: str, nc: int):
     row = traffic_table().get(f"{form}_{'sweep_fwd' if sweep else pass_name}")
     if not row:
         return None
-    return {"bytes": round(row["bytes_per_cell"] * nc), "from": row["source"],
-            "note": "DRAM read+write of one launch on C2big (947,090 cells), scaled by the cell count"}
+    out = {"bytes": round(row["bytes_per_cell"] * nc), "from": row["source"],
+           "note": "DRAM read+write of one launch on C2big (947,090 cells), scaled by the cell count"}
+    if "fp64_pipe_pct" in row:
+        out["fp64_pipe_pct"] = row["fp64_pipe_pct"]
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -616,7 +619,14 @@ def run_ours(args):
         latency = {"levels": rows[dominant]["levels"], "us_per_level": rows[dominant]["us_per_level"],
                    "floor_us_per_hop": rows[dominant]["floor_us_per_hop"],
                    "note": "dependency-level latency bound: one level's cells wait for lower levels' increments"}
-    roofline = {"bound": "hbm", "kernel": dominant, "latency": latency, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+    compute = None
+    if tr and "fp64_pipe_pct" in tr:
+        compute = {"pipe": "fp64", "active_pct_of_peak": tr["fp64_pipe_pct"], "from": tr["from"],
+                   "note": "binary64 residual pass: FP64-issue bound on GB300 (DFMA 1.0 TFLOP/s measured, a warp-wide "
+                           "FP64 instruction holds its sub-partition for 64 cycles); DRAM traffic equals its "
+                           "algorithmic bytes"}
+    roofline = {"bound": "hbm", "kernel": dominant, "latency": latency, "compute": compute,
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": tr["bytes"] if tr else None, "traffic_source": tr, "alg_bytes_per_launch": db,
                 "per_pass": rows}
