@@ -114,7 +114,6 @@ struct DevArrays {
     int2* chain_cells[2] = {nullptr, nullptr}; // [nc] (cell, local-dependency bits) at each position
     int2* chain_rec[2] = {nullptr, nullptr};   // [4*nc] (lower/upper neighbour or -1, face code) per slot
     float4* chain_stage[2] = {nullptr, nullptr};  // [16*nc] per-position stage records (k_fp64.cu)
-    int* chain_posf = nullptr;    // [nc] position of each cell in the forward schedule
     int* chain_posb = nullptr;    // [nc] position of each cell in the backward schedule
     float4* chain_dF = nullptr;   // [nc] binary32 slot sums of the last chain sweep
     int poll_ns = 0;             // back-off between a dataflow sweep's polls (ns, 0 = spin)

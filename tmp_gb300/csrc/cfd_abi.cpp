@@ -129,7 +129,7 @@ void free_case(cfd_case_s* c) {
                     d.norm_out, d.err, d.dWprev, d.omega, d.omega_mean, d.mlp_samples, d.mlp_samp_off, d.sstT, d.sstTf, d.sstG, d.sstF1, d.sstF2,
                     d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD, d.chain_ptr[0], d.chain_ptr[1],
                     d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_stage[0],
-                    d.chain_stage[1], d.chain_posf, d.chain_posb, d.chain_dF};
+                    d.chain_stage[1], d.chain_posb, d.chain_dF};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -276,7 +276,6 @@ void ensure_chain(cfd_case_s* c) {
     if (c->h_cface.empty()) throw std::runtime_error("chain sweep: no host topology kept for this case");
     if (!d.chain_dF) {
         dalloc(&d.chain_dF, d.nc);
-        dalloc(&d.chain_posf, d.nc);
         dalloc(&d.chain_posb, d.nc);
         for (int k = 0; k < 2; k++) {
             dalloc(&d.chain_cells[k], d.nc);
@@ -297,11 +296,11 @@ void ensure_chain(cfd_case_s* c) {
                            c->stream), "upload");
         ck(cudaMemcpyAsync(d.chain_rec[k], rec.data(), rec.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream),
            "upload");
-        std::vector<int> pos(d.nc);
-        for (int q = 0; q < d.nc; q++) pos[cells[q].x] = q;
-        ck(cudaMemcpyAsync(k == 0 ? d.chain_posf : d.chain_posb, pos.data(), pos.size() * sizeof(int),
-                           cudaMemcpyHostToDevice, c->stream), "upload");
         if (k == 1) {
+            std::vector<int> posb(d.nc);
+            for (int q = 0; q < d.nc; q++) posb[cells[q].x] = q;
+            ck(cudaMemcpyAsync(d.chain_posb, posb.data(), posb.size() * sizeof(int), cudaMemcpyHostToDevice,
+                               c->stream), "upload");
             launch_chain_static(d, c->L());
             ck(cudaGetLastError(), "k_chain_static");
         }

@@ -1136,45 +1136,33 @@ __global__ void k_chain_static(int nc, const int2* __restrict__ cells, const int
 
 // Per-step cell pass of the chain sweep, in place of k_inv_diag and the cell
 // part of k_sweep_prep32: binary32 copies of W and U (each converted once,
-// with the conversions those kernels use), 1/D in binary64 (for k_chain_mid /
-// k_chain_finish) and binary32 (both directions' stage records), the forward
-// own term R, and the "not yet computed" sentinel in both directions'
-// published increments.
-__global__ void k_chain_cell(int nc, const d4* __restrict__ W, const d4* __restrict__ U, const d4* __restrict__ R,
-                             const double* __restrict__ D, const int* __restrict__ posf,
-                             const int* __restrict__ posb, float4* __restrict__ Wf, float4* __restrict__ Uf,
-                             double* __restrict__ invD, float4* __restrict__ stage_f, float4* __restrict__ stage_b,
-                             float4* __restrict__ pub_f, float4* __restrict__ pub_b) {
+// with the conversions those kernels use), 1/D in binary64, and the "not yet
+// computed" sentinel in both directions' published increments.
+__global__ void k_chain_cell(int nc, const d4* __restrict__ W, const d4* __restrict__ U,
+                             const double* __restrict__ D, float4* __restrict__ Wf, float4* __restrict__ Uf,
+                             double* __restrict__ invD, float4* __restrict__ pub_f, float4* __restrict__ pub_b) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
-    const d4 w = ld4(W + c), u = ld4(U + c), r = ld4(R + c);
+    const d4 w = ld4(W + c), u = ld4(U + c);
     Wf[c] = make_float4((float)w.x, (float)w.y, (float)w.z, (float)w.w);
     Uf[c] = make_float4((float)u.x, (float)u.y, (float)u.z, (float)u.w);
-    const double dinv = 1.0 / D[c];
-    invD[c] = dinv;
-    const float dinvf = (float)dinv;
-    float4* sf = stage_f + (size_t)posf[c] * kStageW;
-    float4* sb = stage_b + (size_t)posb[c] * kStageW;
-    sf[12] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
-    float4 mf = sf[13], mb = sb[13];
-    mf.x = dinvf;
-    mb.x = dinvf;
-    sf[13] = mf;
-    sb[13] = mb;
+    invD[c] = 1.0 / D[c];
     const float sent = __uint_as_float(kSentinelF);
     pub_f[c] = make_float4(sent, sent, sent, sent);
     pub_b[c] = make_float4(sent, sent, sent, sent);
 }
 
-// Per-step slot pass of both directions' stage records, after k_chain_cell:
-// the neighbours' binary32 state, its increment-free terms and r_A, each with
-// the expression k_sweep_prep32 and k_sweep_flow32 use.  (The backward own
-// term, dW1, is written by k_chain_mid.)
+// Per-step slot pass of both directions' stage records, after k_chain_cell,
+// in schedule order (coalesced writes): the neighbours' binary32 state, its
+// increment-free terms and r_A, each with the expression k_sweep_prep32 and
+// k_sweep_flow32 use; binary32 1/D and the forward own term R.  (The backward
+// own term, dW1, is written by k_chain_mid.)
 template <bool VISC, class MuT>
 __global__ void k_chain_prep(int nc, float4* __restrict__ stage_f, float4* __restrict__ stage_b,
                              const int2* __restrict__ rec_f, const int2* __restrict__ rec_b,
                              const float4* __restrict__ fvisf, const float4* __restrict__ Wf,
-                             const float4* __restrict__ Uf, const MuT* __restrict__ mu) {
+                             const float4* __restrict__ Uf, const MuT* __restrict__ mu, const d4* __restrict__ R,
+                             const double* __restrict__ invD) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 8LL * nc) return;
     const float GM1 = 1.4f - 1.0f;
@@ -1206,6 +1194,16 @@ __global__ void k_chain_prep(int nc, float4* __restrict__ stage_f, float4* __res
     st[s] = make_float4(w0.x, w0.y + pb, w0.z, w0.w);
     st[4 + s] = make_float4(u, v, vv, vn);
     st[8 + s] = make_float4(g.x, g.y, g.z, rA);
+    if (s == 0) {
+        float4 misc = st[13];
+        const int i = __float_as_int(misc.y);
+        misc.x = (float)invD[i];
+        st[13] = misc;
+        if (!dir) {
+            const d4 rr = ld4(R + i);
+            st[12] = make_float4((float)rr.x, (float)rr.y, (float)rr.z, (float)rr.w);
+        }
+    }
 }
 
 // dW1 = (-R - sum) * (1/D) in binary64 (k_sweep_flow32's forward expression),
@@ -1268,22 +1266,21 @@ cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool fo
     int nh = d.chain_nh;
     float4* pub = forward ? d.dW1f : d.dWf;
     if (forward) {
-        k_chain_cell<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.W, d.U, d.R, d.diag, d.chain_posf, d.chain_posb,
-                                                            d.Wf, d.Uf, d.invD, d.chain_stage[0], d.chain_stage[1],
-                                                            d.dW1f, d.dWf);
+        k_chain_cell<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.W, d.U, d.diag, d.Wf, d.Uf, d.invD, d.dW1f,
+                                                            d.dWf);
         const int nb = nblk(8 * d.nc, 256);
         if (viscous && mu64)
             k_chain_prep<true, double><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
                                                                  d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
-                                                                 d.mu);
+                                                                 d.mu, d.R, d.invD);
         else if (viscous)
             k_chain_prep<true, float><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
                                                                 d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
-                                                                d.muf);
+                                                                d.muf, d.R, d.invD);
         else
             k_chain_prep<false, float><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
                                                                  d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
-                                                                 (const float*)nullptr);
+                                                                 (const float*)nullptr, d.R, d.invD);
         *L.counter += 2;
     }
     void* args[] = {(void*)&nh, (void*)&d.chain_ptr[k], (void*)&d.chain_stage[k], (void*)&pub, (void*)&d.chain_dF,
