@@ -167,11 +167,15 @@ def traffic_table() -> dict:
         return {}
 
 
-def traffic_bytes(pass_name: str, precision: str, nc: int):
-    """DRAM bytes of one launch from the committed ncu capture (per cell, scaled by the cell count)."""
+def traffic_bytes(pass_name: str, precision: str, nc: int, sweep_mode: int = 0):
+    """DRAM bytes of one launch (one pass for the chain-scheduled sweep) from the committed ncu capture (per cell,
+    scaled by the cell count)."""
     sweep = pass_name in ("sweep_fwd", "sweep_bwd")
     form = "fp32" if precision == "fp32" or (precision == "mixed" and sweep) else "fp64"
-    row = traffic_table().get(f"{form}_{'sweep_fwd' if sweep else pass_name}")
+    if sweep and form == "fp32" and sweep_mode == 5:
+        row = traffic_table().get(f"fp32_chain_{pass_name}")
+    else:
+        row = traffic_table().get(f"{form}_{'sweep_fwd' if sweep else pass_name}")
     if not row:
         return None
     out = {"bytes": round(row["bytes_per_cell"] * nc), "from": row["source"],
@@ -597,7 +601,7 @@ def run_ours(args):
         b = alg_bytes(p, nc, nf, viscous, args.precision)
         rows[p] = {"ms": round(v, 5), "alg_bytes": b, "gbs": round(b / (v * 1e-3) / 1e9, 1),
                    "frac": round(b / (v * 1e-3) / 1e9 / peak, 4), "launches": launches_of.get(p, 1)}
-        t = traffic_bytes(p, args.precision, nc)
+        t = traffic_bytes(p, args.precision, nc, case.sweep_config()[0])
         if t:
             rows[p]["traffic"] = t["bytes"]
     # the sweeps are latency bound: time per dependency level against the measured
@@ -613,7 +617,7 @@ def run_ours(args):
             rows[p]["floor_us_per_hop"] = round(floor, 3) if floor else None
     db = alg_bytes(dominant, nc, nf, viscous, args.precision)
     achieved = db / (per[dominant] * 1e-3) / 1e9
-    tr = traffic_bytes(dominant, args.precision, nc)
+    tr = traffic_bytes(dominant, args.precision, nc, case.sweep_config()[0])
     latency = None
     if dominant in ("sweep_fwd", "sweep_bwd"):
         latency = {"levels": rows[dominant]["levels"], "us_per_level": rows[dominant]["us_per_level"],
