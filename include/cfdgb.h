@@ -321,6 +321,32 @@ void cfd_holemap_free(cfd_holemap_t h);
  * 0.  Host output arrays of the block's node count; mandatory may be NULL. */
 int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, const cfd_holemap_t* maps,
                       int nfringe, int* iblank, int* mandatory);
+/* Overset assembly of nblocks blocks on this device (one rank's
+ * tioga::performConnectivity, tioga.cpp:153-262, with MeshBlock::preprocess,
+ * MeshBlock.cpp:135-425; processDonors / findInterpData / cancellation /
+ * reduce_fringes, bookkeeping.cpp:75-705; exchangeDonors' order,
+ * exchangeDonor.cpp:24-347).  maps[b]: block b's hole map or NULL (no walls);
+ * obc_nodes[b][nobc[b]]: block b's overset-boundary nodes (host, 0-based;
+ * they and their cells' nodes become mandatory receptors, and mexclude layers
+ * of cells around them unacceptable donors); nfringe: layers of mandatory
+ * receptors around holes and, plus one, receptors kept by the fringe
+ * reduction (tioga defaults: nfringe 1, mexclude 3).  Distance-scaled
+ * resolutions (MeshBlock::reResolution) are not applied, as tioga's default.
+ * Donor search ties follow cfd_block_search (the lowest-numbered cell). */
+typedef struct cfd_connect_s* cfd_connect_t;
+int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holemap_t* maps, const int* const* obc_nodes,
+                        const int* nobc, int nfringe, int mexclude, cfd_connect_t* out);
+/* Final node iblank (1 field, 0 hole, -1 receptor) and cell iblank
+ * (getCellIblanks) of one block; host arrays, either may be NULL. */
+int cfd_connect_iblank(cfd_connect_t c, int block, int* node_iblank, int* cell_iblank);
+/* The interpolations a donor block serves (interpList entries not cancelled,
+ * in the reference's order): count, then host arrays of that length
+ * (inode / weights: 4 per entry, -1 / 0 in a triangle's unused slot); any
+ * pointer may be NULL.  cfd_interp_create_list builds the exchange. */
+int cfd_connect_interp_count(cfd_connect_t c, int donor_block, long long* n);
+int cfd_connect_interp_get(cfd_connect_t c, int donor_block, int* recv_block, int* recv_node, int* donor_cell,
+                           int* nweights, int* inode, double* weights);
+void cfd_connect_free(cfd_connect_t c);
 /* Cell blanking from node blanking (MeshBlock::getCellIblanks,
  * bookkeeping.cpp:654-705): cell_iblank[c] = 0 if any of its nodes is 0 (hole),
  * -1 if all of its nodes are -1 (receptors), else 1.  Host arrays of the

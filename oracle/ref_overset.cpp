@@ -23,6 +23,7 @@
 //     OUT:  int32 nx[2]; double extents[4]; int32 sam[nx*ny]; int32 inside[n]
 //   ref_overset celliblank MESH IBL OUT   MeshBlock::getCellIblanks (UniTioga/bookkeeping.cpp:654-705)
 //     IBL: int32 iblank[nnode];  OUT: int32 iblank_cell[ncell] in the mesh's own cell numbering
+//   ref_overset connect CONN OUT   one rank's overset assembly (see do_connect)
 #include <cstdio>
 #include <cstdlib>
 #include <stdexcept>
@@ -275,6 +276,180 @@ static int do_interp(const char* listf, const char* out) {
     return 0;
 }
 
+// One rank's overset assembly with the reference's own MeshBlock code, in the
+// order tioga::performConnectivity runs it (tioga.cpp:153-262): profile
+// (MeshBlock::preprocess: resolutions, overset-boundary receptors, mexclude),
+// getHoleMap, search of every other block's nodes, then exchangeDonors
+// (exchangeDonor.cpp:24-347) and tioga::reduce_fringes (tioga.cpp:474-600)
+// with each packet exchange done as the single-rank loop it reduces to, and
+// getCellIblanks.  Distance-scaled resolutions are off (the tioga default).
+//   CONN: int32 nblocks, nfringe, mexclude, isym; per block: int32 nnode, ncell;
+//         double xy[2*nnode]; int32 nvert[ncell]; int32 verts[4*ncell];
+//         int32 nwall; int32 wall[nwall]; int32 nobc; int32 obc[nobc] (0-based)
+//   OUT:  per block int32 iblank[nnode], int32 iblank_cell[ncell] (mesh cell order);
+//         then per donor block int32 n and n records {int32 recv_block, recv_node,
+//         donor_cell (mesh order), nweights, inode[4]; double w[4]} of its
+//         interpolations that were not cancelled
+static int do_connect(const char* inf, const char* out) {
+    FILE* f = fopen(inf, "rb");
+    if (!f) return 3;
+    int nb, nfringe, mexclude, isym;
+    if (!rd(f, &nb, 1) || !rd(f, &nfringe, 1) || !rd(f, &mexclude, 1) || !rd(f, &isym, 1) || nb < 1 || nb > 64)
+        return 3;
+    static std::vector<BlockData> bd(nb);
+    static std::vector<std::vector<int>> wall(nb), obc(nb), ibl(nb), iblc(nb);
+    std::vector<MeshBlock*> mbs(nb);
+    for (int b = 0; b < nb; b++) {
+        BlockData& d = bd[b];
+        if (!rd(f, &d.nnode, 1) || !rd(f, &d.ncell, 1)) return 3;
+        d.xy.resize(2 * (size_t)d.nnode);
+        d.nvert.resize(d.ncell);
+        d.verts.resize(4 * (size_t)d.ncell);
+        if (!rd(f, d.xy.data(), d.xy.size()) || !rd(f, d.nvert.data(), d.ncell) || !rd(f, d.verts.data(), d.verts.size()))
+            return 3;
+        int nw, no;
+        if (!rd(f, &nw, 1)) return 3;
+        wall[b].resize(nw);
+        if (nw && !rd(f, wall[b].data(), nw)) return 3;
+        if (!rd(f, &no, 1)) return 3;
+        obc[b].resize(no);
+        if (no && !rd(f, obc[b].data(), no)) return 3;
+        for (int& w : wall[b]) w += BASE;
+        for (int& o : obc[b]) o += BASE;
+        MeshBlock* mb = make_block(d);
+        mb->meshtag = b + 1;
+        mb->cellRes = nullptr;  // tagBoundary allocates its own
+        mb->nodeRes = nullptr;
+        mb->nwbc = nw;
+        mb->wbcnode = wall[b].data();
+        mb->nobc = no;
+        mb->obcnode = obc[b].data();
+        ibl[b].assign(d.nnode, 1);
+        mb->iblank = ibl[b].data();
+        mb->iblank_reduced = nullptr;
+        mb->iblank_cell = nullptr;
+        mb->mexclude = mexclude;
+        mb->nfringe = nfringe;
+        mb->preprocess();
+        mbs[b] = mb;
+    }
+    fclose(f);
+    TIOGA::tioga* tg = new TIOGA::tioga();
+    tg->d_dim = 2;
+    tg->isym = isym;
+    tg->scomm = MPI_COMM_WORLD;
+    tg->nblocks = nb;
+    for (int b = 0; b < nb; b++) {
+        tg->mblocks.emplace_back(mbs[b]);
+        tg->mtags.push_back(b + 1);
+    }
+    tg->getHoleMap();
+    const int nmesh = nb;
+    // search: every other block's nodes, block by block, node by node (exchangeSearchData)
+    static std::vector<std::vector<double>> xs(nb), rs(nb);
+    static std::vector<std::vector<int>> is(nb), ts(nb);
+    for (int d = 0; d < nb; d++) {
+        for (int r = 0; r < nb; r++) {
+            if (r == d) continue;
+            for (int v = 0; v < bd[r].nnode; v++) {
+                xs[d].push_back(bd[r].xy[2 * (size_t)v]);
+                xs[d].push_back(bd[r].xy[2 * (size_t)v + 1]);
+                is[d].push_back(0);
+                is[d].push_back(v);
+                is[d].push_back(r);
+                ts[d].push_back(r + 1);
+                rs[d].push_back(mbs[r]->nodeRes[v]);
+            }
+        }
+        MeshBlock* mb = mbs[d];
+        mb->nsearch = (int)ts[d].size();
+        mb->xsearch = xs[d].data();
+        mb->isearch = is[d].data();
+        mb->tagsearch = ts[d].data();
+        mb->res_search = rs[d].data();
+        mb->search();
+    }
+    // exchangeDonors, comm 1: donors to the receptor blocks
+    for (int b = 0; b < nb; b++) mbs[b]->initializeDonorList();
+    for (int d = 0; d < nb; d++) {
+        MeshBlock* mb = mbs[d];
+        for (int i = 0; i < mb->nsearch; i++) {
+            if (mb->donorId[i] < 0) continue;
+            mbs[mb->isearch[3 * i + 2]]->insertAndSort(mb->isearch[3 * i + 1], 0, mb->meshtag, i,
+                                                       mb->cellRes[mb->donorId[i]], mb->res_search[mb->xtag[i]]);
+        }
+    }
+    std::vector<int> nrec(nb, 0);
+    std::vector<int*> drec(nb, nullptr);
+    std::vector<double*> rres(nb, nullptr);
+    for (int b = 0; b < nb; b++) mbs[b]->processDonors(tg->holeMap, nmesh, &drec[b], &rres[b], &nrec[b]);
+    // comm 2: accepted receptors to their donors
+    std::vector<int> ninterp(nb, 0);
+    for (int n = 0; n < nb; n++)
+        for (int i = 0; i < nrec[n]; i++) ninterp[drec[n][3 * i + 2] - 1]++;
+    for (int b = 0; b < nb; b++) mbs[b]->initializeInterpList(ninterp[b]);
+    std::fill(ninterp.begin(), ninterp.end(), 0);
+    for (int n = 0; n < nb; n++)
+        for (int i = 0; i < nrec[n]; i++) {
+            const int ib = drec[n][3 * i + 2] - 1;
+            mbs[ib]->findInterpData(&ninterp[ib], drec[n][3 * i + 1], rres[n][i]);
+        }
+    for (int b = 0; b < nb; b++) mbs[b]->set_ninterp(ninterp[b]);
+    // comm 3: cancellations, comm 4: final receptors
+    auto cancel_and_set = [&](bool reduced) {
+        for (int b = 0; b < nb; b++) {
+            int nr = 0;
+            int* rec = nullptr;
+            if (reduced) mbs[b]->getCancellationReduce(&nr, &rec);
+            else mbs[b]->getCancellationData(&nr, &rec);
+            for (int i = 0; i < nr; i++) mbs[rec[3 * i + 2] - 1]->cancelDonor(rec[3 * i + 1]);
+        }
+        for (int b = 0; b < nb; b++) mbs[b]->resetCoincident();
+        std::vector<std::vector<int>> fin(nb);
+        for (int b = 0; b < nb; b++) {
+            int nr = 0;
+            int* rec = nullptr;
+            mbs[b]->getInterpData(&nr, &rec);
+            for (int i = 0; i < nr; i++) fin[b].push_back(rec[3 * i + 1]), fin[b].push_back(rec[3 * i + 2]);
+        }
+        for (int b = 0; b < nb; b++) mbs[b]->clearIblanks();
+        for (int b = 0; b < nb; b++)
+            for (size_t i = 0; i < fin[b].size(); i += 2) mbs[fin[b][i + 1]]->setIblanks(fin[b][i]);
+    };
+    cancel_and_set(false);
+    for (int b = 0; b < nb; b++) mbs[b]->reduce_fringes();
+    cancel_and_set(true);
+    FILE* fo = fopen(out, "wb");
+    if (!fo) return 4;
+    for (int b = 0; b < nb; b++) {
+        MeshBlock* mb = mbs[b];
+        mb->getCellIblanks();
+        std::vector<int> cres(bd[b].ncell);
+        for (int k = 0; k < bd[b].ncell; k++) cres[bd[b].order[k]] = mb->iblank_cell[k];
+        fwrite(mb->iblank, 4, bd[b].nnode, fo);
+        fwrite(cres.data(), 4, cres.size(), fo);
+    }
+    for (int d = 0; d < nb; d++) {
+        MeshBlock* mb = mbs[d];
+        int n = 0;
+        for (int i = 0; i < mb->ninterp; i++) n += !mb->interpList[i].cancel;
+        fwrite(&n, 4, 1, fo);
+        for (int i = 0; i < mb->ninterp; i++) {
+            const INTERPLIST& e = mb->interpList[i];
+            if (e.cancel) continue;
+            int head[4] = {e.receptorInfo[2], e.receptorInfo[1], bd[d].order[e.inode[e.nweights]], e.nweights};
+            int nodes[4] = {-1, -1, -1, -1};
+            double w[4] = {0, 0, 0, 0};
+            for (int m = 0; m < e.nweights; m++) nodes[m] = e.inode[m], w[m] = e.weights[m];
+            fwrite(head, 4, 4, fo);
+            fwrite(nodes, 4, 4, fo);
+            fwrite(w, 8, 4, fo);
+        }
+    }
+    fclose(fo);
+    return 0;  // the blocks are left allocated: the driver exits next
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) {
         fprintf(stderr, "usage: %s weights|search|interp ...\n", argv[0]);
@@ -286,6 +461,7 @@ int main(int argc, char** argv) {
     if (mode == "interp" && argc == 4) return do_interp(argv[2], argv[3]);
     if (mode == "holemap" && argc == 6) return do_holemap(argv[2], argv[3], argv[4], argv[5]);
     if (mode == "celliblank" && argc == 5) return do_celliblank(argv[2], argv[3], argv[4]);
+    if (mode == "connect" && argc == 4) return do_connect(argv[2], argv[3]);
     fprintf(stderr, "bad arguments\n");
     return 2;
 }

@@ -117,6 +117,12 @@ def lib() -> C.CDLL:
         "cfd_holemap_free": (None, [vp]),
         "cfd_overset_blank": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.POINTER(vp), C.c_int, ip, ip]),
         "cfd_cell_iblank": (C.c_int, [vp, ip, ip]),
+        "cfd_overset_connect": (C.c_int, [C.c_int, C.POINTER(vp), C.POINTER(vp), C.POINTER(ip), ip, C.c_int, C.c_int,
+                                          C.POINTER(vp)]),
+        "cfd_connect_iblank": (C.c_int, [vp, C.c_int, ip, ip]),
+        "cfd_connect_interp_count": (C.c_int, [vp, C.c_int, C.POINTER(C.c_longlong)]),
+        "cfd_connect_interp_get": (C.c_int, [vp, C.c_int, ip, ip, ip, ip, ip, dp]),
+        "cfd_connect_free": (None, [vp]),
         "cfd_mlp_create": (C.c_int, [C.c_ulonglong, C.POINTER(vp)]),
         "cfd_mlp_free": (None, [vp]),
         "cfd_mlp_get_params": (C.c_int, [vp, fp, fp]),
@@ -481,6 +487,44 @@ def overset_blank(block: Block, others: Sequence[Block], maps: Sequence[HoleMap 
     md = np.zeros(block.nnode, np.int32)
     check(lib().cfd_overset_blank(block.h, n, ob, mp, int(nfringe), _iptr(ib), _iptr(md)))
     return ib, md
+
+
+def overset_connect(blocks: Sequence[Block], maps: Sequence[HoleMap | None], obc_nodes: Sequence[np.ndarray],
+                    nfringe: int = 1, mexclude: int = 3) -> dict:
+    """Overset assembly of the blocks (tioga::performConnectivity on one rank).
+
+    Returns {"iblank": [node iblank per block], "cell_iblank": [...],
+    "interp": [per donor block dict(recv_block, recv_node, donor_cell,
+    nweights, inode (n,4), weights (n,4))]}."""
+    n = len(blocks)
+    bl = (C.c_void_p * n)(*[b.h.value for b in blocks])
+    mp = (C.c_void_p * n)(*[(m.h.value if m is not None else None) for m in maps])
+    obc = [np.ascontiguousarray(o, dtype=np.int32) for o in obc_nodes]
+    op = (C.POINTER(C.c_int) * n)(*[_iptr(o) for o in obc])
+    no = np.array([len(o) for o in obc], np.int32)
+    h = C.c_void_p()
+    check(lib().cfd_overset_connect(n, bl, mp, op, _iptr(no), int(nfringe), int(mexclude), C.byref(h)))
+    try:
+        out = {"iblank": [], "cell_iblank": [], "interp": []}
+        for k, b in enumerate(blocks):
+            ib = np.zeros(b.nnode, np.int32)
+            ic = np.zeros(b.ncell, np.int32)
+            check(lib().cfd_connect_iblank(h, k, _iptr(ib), _iptr(ic)))
+            out["iblank"].append(ib)
+            out["cell_iblank"].append(ic)
+            cnt = C.c_longlong()
+            check(lib().cfd_connect_interp_count(h, k, C.byref(cnt)))
+            m = cnt.value
+            rb, rn, dc, nw = (np.zeros(m, np.int32) for _ in range(4))
+            inode = np.zeros((m, 4), np.int32)
+            w = np.zeros((m, 4))
+            if m:
+                check(lib().cfd_connect_interp_get(h, k, _iptr(rb), _iptr(rn), _iptr(dc), _iptr(nw), _iptr(inode),
+                                                   _dptr(w)))
+            out["interp"].append(dict(recv_block=rb, recv_node=rn, donor_cell=dc, nweights=nw, inode=inode, weights=w))
+        return out
+    finally:
+        lib().cfd_connect_free(h)
 
 
 # ---- learned relaxation -------------------------------------------------------

@@ -520,6 +520,65 @@ __global__ void k_hole_check(long long n, const double* __restrict__ pts, MapGeo
     inside[i] = hole_at(pts[2 * i], pts[2 * i + 1], g, sam);
 }
 
+// Cell resolution of the assembly: computeCellVolume2D (mathTools/
+// cellVolume.cpp:6-75) of the cell's vertices in their own order: a triangle's
+// area by the shoelace sum of triangle_area, a quadrilateral split along the
+// diagonal the cross-product sign tests pick (Vector3D::cross_product /
+// dot_product, vector3d.cpp:43-97, in 3-D with zero z).
+__device__ double ref_triangle_area(const double* p1, const double* p2, const double* p3) {
+    double area = 0.5 * ((p1[0] - p2[0]) * (p1[1] + p2[1]) + (p2[0] - p3[0]) * (p2[1] + p3[1]) +
+                         (p3[0] - p1[0]) * (p3[1] + p1[1]));
+    if (area < 0) area = -area;
+    return area;
+}
+
+__device__ double ref_cross_dot(const double* a, const double* b, const double* c, const double* d) {
+    // (a x b) . (c x d) for in-plane vectors: z components only, as the 3-D
+    // products with zero z give them
+    const double z1 = a[0] * b[1] - a[1] * b[0];
+    const double z2 = c[0] * d[1] - c[1] * d[0];
+    double r = 0;
+    r += (a[1] * 0.0 - 0.0 * b[1]) * (c[1] * 0.0 - 0.0 * d[1]);
+    r += (0.0 * b[0] - a[0] * 0.0) * (0.0 * d[0] - c[0] * 0.0);
+    r += z1 * z2;
+    return r;
+}
+
+__global__ void k_cell_volume(int ncell, const double* __restrict__ xy, const int4* __restrict__ cv,
+                              double* __restrict__ vol) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int4 v = cv[c];
+    double x[4][2];
+    const int ids[4] = {v.x, v.y, v.z, v.w};
+    const int nv = v.w < 0 ? 3 : 4;
+    for (int m = 0; m < nv; m++) {
+        x[m][0] = xy[2 * ids[m]];
+        x[m][1] = xy[2 * ids[m] + 1];
+    }
+    if (nv == 3) {
+        vol[c] = ref_triangle_area(x[0], x[1], x[2]);
+        return;
+    }
+    const double AB[2] = {x[1][0] - x[0][0], x[1][1] - x[0][1]};
+    const double AC[2] = {x[2][0] - x[0][0], x[2][1] - x[0][1]};
+    const double AD[2] = {x[3][0] - x[0][0], x[3][1] - x[0][1]};
+    double area = 0;
+    if (ref_cross_dot(AB, AC, AB, AD) > 0) {
+        if (ref_cross_dot(AC, AD, AB, AD) > 0) {
+            area += ref_triangle_area(x[0], x[2], x[1]);
+            area += ref_triangle_area(x[0], x[2], x[3]);
+        } else {
+            area += ref_triangle_area(x[0], x[3], x[1]);
+            area += ref_triangle_area(x[0], x[3], x[2]);
+        }
+    } else {
+        area += ref_triangle_area(x[0], x[1], x[2]);
+        area += ref_triangle_area(x[0], x[1], x[3]);
+    }
+    vol[c] = area;
+}
+
 // getCellIblanks (bookkeeping.cpp:654-705): a cell is a hole (0) if any of
 // its nodes is, a receptor (-1) if all of its nodes are, else a field cell (1).
 __global__ void k_cell_iblank(int ncell, const int4* __restrict__ cv, const int* __restrict__ ibl,
@@ -1187,6 +1246,405 @@ int cfd_cell_iblank(cfd_block_t b, const int* node_iblank, int* cell_iblank) {
     dfree(d_c);
     return rc;
 }
+
+// ---------------------------------------------------------------------------
+// Overset assembly of several blocks on one device: the sequence of
+// tioga::performConnectivity (tioga.cpp:153-262) for one rank, with the
+// searches, hole-map tests and cell volumes on the GPU and the bookkeeping
+// (resolutions, donor lists, fringe choice, donor cancellation, fringe
+// reduction) on the host in the reference's order.
+//   profile      MeshBlock::preprocess / tagBoundary (MeshBlock.cpp:135-425):
+//                cellRes = cell volume, nodeRes = mean of the node's cells'
+//                cellRes (cells triangles first, then quadrilaterals, as
+//                MeshBlock numbers them); nodes of cells touching an overset-
+//                boundary node get nodeRes = BIGVALUE (mandatory receptors),
+//                and mexclude layers of cells around them cellRes = BIGVALUE
+//                (unacceptable donors)
+//   search       every other block's nodes in each block (MeshBlock::search)
+//   donor lists  MeshBlock::insertAndSort / insertInList (linkList.cpp:62-105):
+//                ascending donor resolution, ties in block order
+//   processDonors (bookkeeping.cpp:75-277): holes, nfringe layers of
+//                mandatory receptors, then each remaining node with a donor
+//                of finer resolution than its own becomes a receptor
+//   findInterpData (bookkeeping.cpp:310-428): the donor rejects a receptor
+//                when one of its cell's nodes is a mandatory or a receptor of
+//                the receptor's own mesh; a mandatory receptor releases the
+//                donor cell's receptor nodes
+//   exchangeDonors (exchangeDonor.cpp:24-347) cancellations and final
+//                receptors; tioga::reduce_fringes (tioga.cpp:474-600,
+//                bookkeeping.cpp:572-652): receptors beyond nfringe+1 layers
+//                from field nodes become holes; getCellIblanks.
+// Coincident search points only merge within one receptor mesh
+// (uniqNodesTree, utils.cpp:484-620), so with distinct node coordinates
+// resetCoincident changes nothing and is not restated.  Distance-scaled
+// resolutions (MeshBlock::reResolution) are off, as tioga's default.
+struct cfd_connect_s {
+    std::vector<std::vector<int>> ibl, iblc;
+    struct Rec {
+        int recv_block, recv_node, donor_cell, nw;
+        int inode[4];
+        double w[4];
+    };
+    std::vector<std::vector<Rec>> interps;  // per donor block, interpList order, not cancelled
+};
+
+namespace {
+constexpr double kBig = 1.0e15;  // BIGVALUE (codetypes.h)
+
+struct ConnDonor {
+    int d;          // donor block
+    int cell;       // donor cell
+    double res;     // donor cellRes
+};
+}  // namespace
+
+int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holemap_t* maps, const int* const* obc_nodes,
+                        const int* nobc, int nfringe, int mexclude, cfd_connect_t* out) {
+    if (nblocks < 2 || !blocks || !maps || !nobc || !obc_nodes || nfringe < 0 || mexclude < 0 || !out)
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_connect: bad argument");
+    for (int b = 0; b < nblocks; b++) {
+        if (!blocks[b]) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_connect: null block");
+        if (nobc[b] < 0 || (nobc[b] > 0 && !obc_nodes[b]))
+            return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_connect: bad overset-boundary list");
+        for (int k = 0; k < nobc[b]; k++)
+            if (obc_nodes[b][k] < 0 || obc_nodes[b][k] >= blocks[b]->nnode)
+                return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_connect: overset-boundary node out of range");
+        for (int c = 0; c < b; c++)
+            if (blocks[c] == blocks[b]) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_connect: a block twice");
+    }
+    *out = nullptr;
+    const int nb = nblocks;
+    std::vector<std::vector<double>> hxy(nb), cellRes(nb), nodeRes(nb);
+    std::vector<std::vector<int4>> hcv(nb);
+    std::vector<std::vector<int>> tm(nb);  // MeshBlock cell order: triangles, then quadrilaterals
+    // donor[d][r]: donor cell in block d of every node of block r (-1: none), with its weights
+    std::vector<std::vector<std::vector<int>>> dcell(nb, std::vector<std::vector<int>>(nb));
+    std::vector<std::vector<std::vector<double>>> dw(nb, std::vector<std::vector<double>>(nb));
+    std::vector<std::vector<std::vector<int>>> inside(nb, std::vector<std::vector<int>>(nb));
+    double *d_vol = nullptr, *d_w = nullptr;
+    int *d_donor = nullptr, *d_in = nullptr;
+    int rc = CFD_OK;
+    cfd_connect_s* res = new cfd_connect_s;
+    try {
+        size_t nmax = 0;
+        for (int b = 0; b < nb; b++) nmax = std::max(nmax, (size_t)std::max(blocks[b]->nnode, blocks[b]->ncell));
+        dalloc(&d_vol, nmax);
+        dalloc(&d_donor, nmax);
+        dalloc(&d_in, nmax);
+        dalloc(&d_w, 4 * nmax);
+        for (int b = 0; b < nb; b++) {
+            cfd_block_s* B = blocks[b];
+            cudaStream_t s = B->stream;
+            hxy[b].resize(2 * (size_t)B->nnode);
+            hcv[b].resize(B->ncell);
+            cellRes[b].resize(B->ncell);
+            ck(cudaMemcpyAsync(hxy[b].data(), B->xy, hxy[b].size() * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
+            ck(cudaMemcpyAsync(hcv[b].data(), B->cv, hcv[b].size() * sizeof(int4), cudaMemcpyDeviceToHost, s), "copy");
+            k_cell_volume<<<blocks_for(B->ncell, 256), 256, 0, s>>>(B->ncell, B->xy, B->cv, d_vol);
+            ck(cudaGetLastError(), "k_cell_volume");
+            ck(cudaMemcpyAsync(cellRes[b].data(), d_vol, B->ncell * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
+            ck(cudaStreamSynchronize(s), "sync");
+            for (int pass = 0; pass < 2; pass++)
+                for (int c = 0; c < B->ncell; c++)
+                    if ((hcv[b][c].w < 0) == (pass == 0)) tm[b].push_back(c);
+        }
+        // searches and hole-map tests, all on the device
+        for (int d = 0; d < nb; d++)
+            for (int r = 0; r < nb; r++) {
+                if (r == d) continue;
+                const int n = blocks[r]->nnode;
+                ck(cudaStreamSynchronize(blocks[r]->stream), "sync");
+                search_device(blocks[d], n, blocks[r]->xy, d_donor, nullptr, d_w);
+                dcell[d][r].resize(n);
+                dw[d][r].resize(4 * (size_t)n);
+                ck(cudaMemcpyAsync(dcell[d][r].data(), d_donor, n * sizeof(int), cudaMemcpyDeviceToHost,
+                                   blocks[d]->stream), "copy");
+                ck(cudaMemcpyAsync(dw[d][r].data(), d_w, 4 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                                   blocks[d]->stream), "copy");
+                ck(cudaStreamSynchronize(blocks[d]->stream), "sync");
+                if (maps[d]) {
+                    k_hole_check<<<blocks_for(n, 256), 256, 0, maps[d]->stream>>>(n, blocks[r]->xy, maps[d]->g,
+                                                                                  maps[d]->sam, d_in);
+                    ck(cudaGetLastError(), "k_hole_check");
+                    inside[d][r].resize(n);
+                    ck(cudaMemcpyAsync(inside[d][r].data(), d_in, n * sizeof(int), cudaMemcpyDeviceToHost,
+                                       maps[d]->stream), "copy");
+                    ck(cudaStreamSynchronize(maps[d]->stream), "sync");
+                }
+            }
+        // ---- profile: resolutions, mandatory overset-boundary receptors, mexclude
+        auto verts = [&](int b, int c, int* v) {
+            const int4 q = hcv[b][c];
+            v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+            return q.w < 0 ? 3 : 4;
+        };
+        for (int b = 0; b < nb; b++) {
+            const int nn = blocks[b]->nnode;
+            std::vector<int> cnt(nn, 0), iflag(nn, 0), iex(nn, 0), iex1(nn, 0);
+            nodeRes[b].assign(nn, 0.0);
+            int v[4];
+            for (int c : tm[b]) {
+                const int nv = verts(b, c, v);
+                for (int m = 0; m < nv; m++) {
+                    cnt[v[m]]++;
+                    nodeRes[b][v[m]] += cellRes[b][c];
+                }
+            }
+            for (int i = 0; i < nn; i++)
+                if (cnt[i]) nodeRes[b][i] = nodeRes[b][i] / cnt[i];
+            for (int k = 0; k < nobc[b]; k++) iflag[obc_nodes[b][k]] = 1;
+            for (int c : tm[b]) {
+                const int nv = verts(b, c, v);
+                int itag = 0;
+                for (int m = 0; m < nv; m++) itag |= iflag[v[m]];
+                if (itag)
+                    for (int m = 0; m < nv; m++) nodeRes[b][v[m]] = kBig, iex[v[m]] = iex1[v[m]] = 1;
+            }
+            for (int it = 0; it < mexclude; it++) {
+                for (int c : tm[b]) {
+                    const int nv = verts(b, c, v);
+                    for (int m = 0; m < nv; m++)
+                        if (iex[v[m]] == 1) {
+                            cellRes[b][c] = kBig;
+                            break;
+                        }
+                    if (cellRes[b][c] == kBig)
+                        for (int m = 0; m < nv; m++)
+                            if (iex[v[m]] != 1) iex1[v[m]] = 1;
+                }
+                iex = iex1;
+            }
+        }
+        // ---- donor lists (ascending donor resolution, ties in block order)
+        std::vector<std::vector<std::vector<ConnDonor>>> dl(nb);
+        for (int r = 0; r < nb; r++) dl[r].resize(blocks[r]->nnode);
+        for (int d = 0; d < nb; d++)
+            for (int r = 0; r < nb; r++) {
+                if (r == d) continue;
+                for (int v = 0; v < blocks[r]->nnode; v++) {
+                    const int c = dcell[d][r][v];
+                    if (c < 0) continue;
+                    auto& L = dl[r][v];
+                    ConnDonor e{d, c, cellRes[d][c]};
+                    size_t at = 0;
+                    while (at < L.size() && !(std::fabs(L[at].res) > e.res)) at++;
+                    L.insert(L.begin() + at, e);
+                }
+            }
+        // ---- processDonors
+        std::vector<std::vector<int>>& ibl = res->ibl;
+        ibl.resize(nb);
+        struct Acc {
+            int r, v;
+            double rres;
+        };
+        std::vector<std::vector<Acc>> accepted(nb);  // records in receptor order, per receptor block
+        std::vector<int> acc_donor;                   // donor block of each accepted record, in the same order
+        for (int r = 0; r < nb; r++) {
+            const int nn = blocks[r]->nnode;
+            ibl[r].assign(nn, 1);
+            for (int i = 0; i < nn; i++) {
+                std::vector<char> has(nb, 0);
+                for (const auto& e : dl[r][i]) has[e.d] = 1;
+                for (int j = 0; j < nb; j++) {
+                    if (j == r || !maps[j] || has[j]) continue;
+                    if (inside[j][r][i]) {
+                        ibl[r][i] = 0;
+                        break;
+                    }
+                }
+            }
+            std::vector<int> mtag(nn), mtag1(nn);
+            for (int i = 0; i < nn; i++) mtag[i] = mtag1[i] = ibl[r][i] == 0;
+            int v[4];
+            for (int it = 0; it < nfringe; it++) {
+                for (int c : tm[r]) {
+                    const int nv = verts(r, c, v);
+                    for (int m = 0; m < nv; m++)
+                        if (mtag[v[m]] == 1)
+                            for (int mm = 0; mm < nv; mm++)
+                                if (m != mm && mtag[v[mm]] != 1) mtag1[v[mm]] = 1;
+                }
+                mtag = mtag1;
+            }
+            for (int i = 0; i < nn; i++)
+                if (mtag1[i] && ibl[r][i]) nodeRes[r][i] = kBig;
+            for (int i = 0; i < nn; i++) {
+                if (dl[r][i].empty() || ibl[r][i] == 0) continue;
+                for (const auto& e : dl[r][i])
+                    if (e.res < nodeRes[r][i]) {
+                        ibl[r][i] = -(e.d + 1);
+                        accepted[r].push_back({r, i, nodeRes[r][i]});
+                        break;
+                    }
+            }
+        }
+        // ---- findInterpData, in the order the receptor blocks send their records
+        struct Interp {
+            int r, v, cell, nw, cancel;
+            int inode[4];
+            double w[4];
+        };
+        std::vector<std::vector<Interp>> il(nb);
+        // interp index of each (donor d, receptor r, node v), -1: none (interp2donor)
+        std::vector<std::vector<std::vector<int>>> i2d(nb, std::vector<std::vector<int>>(nb));
+        for (int d = 0; d < nb; d++)
+            for (int r = 0; r < nb; r++)
+                if (r != d) i2d[d][r].assign(blocks[r]->nnode, -1);
+        std::vector<std::vector<int>> cancel_list(nb);
+        for (int r = 0; r < nb; r++)
+            for (const Acc& a : accepted[r]) {
+                const ConnDonor& e = dl[r][a.v].front();  // the accepted donor heads the list
+                const int d = e.d, c = e.cell;
+                int v[4];
+                const int nv = verts(d, c, v);
+                int accept = 1;
+                for (int m = 0; m < nv; m++) {
+                    const int u = v[m];
+                    if (ibl[d][u] <= 0 && a.rres > 0.0) {
+                        if (nodeRes[d][u] == kBig) accept = 0;
+                        if (std::abs(ibl[d][u]) == r + 1) accept = 0;
+                    }
+                }
+                if (a.rres == kBig)
+                    for (int m = 0; m < nv; m++) {
+                        const int u = v[m];
+                        if (ibl[d][u] <= 0 && nodeRes[d][u] != kBig) {
+                            if (ibl[d][u] < 0) ibl[d][u] = 1;
+                            cancel_list[d].push_back(u);
+                        }
+                    }
+                Interp it{};
+                it.r = r;
+                it.v = a.v;
+                it.cell = c;
+                it.nw = nv;
+                for (int m = 0; m < 4; m++) {
+                    it.inode[m] = m < nv ? v[m] : -1;
+                    it.w[m] = m < nv ? dw[d][r][4 * (size_t)a.v + m] : 0.0;
+                }
+                it.cancel = (accept == 0 && a.rres != kBig) ? 1 : 0;
+                i2d[d][r][a.v] = (int)il[d].size();
+                il[d].push_back(it);
+            }
+        auto cancel_donor_of = [&](int b, int u) {
+            // the head of node u's donor list names the donor block and record
+            if (dl[b][u].empty()) return;
+            const int d = dl[b][u].front().d;
+            const int k = i2d[d][b][u];
+            if (k > -1) il[d][k].cancel = 1;
+        };
+        auto final_receptors = [&](const std::vector<std::vector<int>>* reduced) {
+            for (int b = 0; b < nb; b++)
+                for (int i = 0; i < blocks[b]->nnode; i++) {
+                    if (ibl[b][i] < 0) ibl[b][i] = 1;
+                    if (reduced && (*reduced)[b][i] == 0) ibl[b][i] = 0;
+                }
+            for (int d = 0; d < nb; d++)
+                for (const Interp& it : il[d])
+                    if (!it.cancel) ibl[it.r][it.v] = -1;
+        };
+        for (int b = 0; b < nb; b++)
+            for (int u : cancel_list[b]) cancel_donor_of(b, u);
+        final_receptors(nullptr);
+        // ---- reduce_fringes
+        std::vector<std::vector<int>> red(nb);
+        for (int b = 0; b < nb; b++) {
+            const int nn = blocks[b]->nnode;
+            red[b].resize(nn);
+            for (int i = 0; i < nn; i++) red[b][i] = ibl[b][i] > 0 ? ibl[b][i] : 0;
+            std::vector<int> tmp = red[b];
+            int v[4];
+            for (int it = 0; it < nfringe + 1; it++) {
+                for (int c : tm[b]) {
+                    const int nv = verts(b, c, v);
+                    int ncount = 0;
+                    for (int m = 0; m < nv; m++) ncount += (red[b][v[m]] == 1 || red[b][v[m]] < 0);
+                    if (ncount > 0 && ncount < nv)
+                        for (int m = 0; m < nv; m++)
+                            if (tmp[v[m]] == 0 && ibl[b][v[m]] < 0) tmp[v[m]] = ibl[b][v[m]];
+                }
+                red[b] = tmp;
+            }
+        }
+        for (int b = 0; b < nb; b++)
+            for (int i = 0; i < blocks[b]->nnode; i++)
+                if (ibl[b][i] < 0 && red[b][i] == 0) cancel_donor_of(b, i);
+        final_receptors(&red);
+        // ---- outputs: cell iblanks on the device, surviving interpolations
+        res->iblc.resize(nb);
+        res->interps.resize(nb);
+        for (int b = 0; b < nb; b++) {
+            cfd_block_s* B = blocks[b];
+            cudaStream_t s = B->stream;
+            ck(cudaMemcpyAsync(d_in, ibl[b].data(), B->nnode * sizeof(int), cudaMemcpyHostToDevice, s), "copy");
+            k_cell_iblank<<<blocks_for(B->ncell, 256), 256, 0, s>>>(B->ncell, B->cv, d_in, d_donor);
+            ck(cudaGetLastError(), "k_cell_iblank");
+            res->iblc[b].resize(B->ncell);
+            ck(cudaMemcpyAsync(res->iblc[b].data(), d_donor, B->ncell * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+            ck(cudaStreamSynchronize(s), "sync");
+            for (const Interp& it : il[b]) {
+                if (it.cancel) continue;
+                cfd_connect_s::Rec q{};
+                q.recv_block = it.r;
+                q.recv_node = it.v;
+                q.donor_cell = it.cell;
+                q.nw = it.nw;
+                for (int m = 0; m < 4; m++) q.inode[m] = it.inode[m], q.w[m] = it.w[m];
+                res->interps[b].push_back(q);
+            }
+        }
+    } catch (const OversetError& e) {
+        rc = report(e);
+    } catch (const std::bad_alloc&) {
+        rc = cfdgb::set_last_error(CFD_ERR_CUDA, "cfd_overset_connect: host allocation failed");
+    }
+    dfree(d_vol);
+    dfree(d_w);
+    dfree(d_donor);
+    dfree(d_in);
+    if (rc != CFD_OK) {
+        delete res;
+        return rc;
+    }
+    *out = res;
+    return CFD_OK;
+}
+
+int cfd_connect_iblank(cfd_connect_t c, int block, int* node_iblank, int* cell_iblank) {
+    if (!c || block < 0 || block >= (int)c->ibl.size())
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_connect_iblank: bad argument");
+    if (node_iblank) std::copy(c->ibl[block].begin(), c->ibl[block].end(), node_iblank);
+    if (cell_iblank) std::copy(c->iblc[block].begin(), c->iblc[block].end(), cell_iblank);
+    return CFD_OK;
+}
+
+int cfd_connect_interp_count(cfd_connect_t c, int donor_block, long long* n) {
+    if (!c || !n || donor_block < 0 || donor_block >= (int)c->interps.size())
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_connect_interp_count: bad argument");
+    *n = (long long)c->interps[donor_block].size();
+    return CFD_OK;
+}
+
+int cfd_connect_interp_get(cfd_connect_t c, int donor_block, int* recv_block, int* recv_node, int* donor_cell,
+                           int* nweights, int* inode, double* weights) {
+    if (!c || donor_block < 0 || donor_block >= (int)c->interps.size())
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_connect_interp_get: bad argument");
+    const auto& L = c->interps[donor_block];
+    for (size_t i = 0; i < L.size(); i++) {
+        if (recv_block) recv_block[i] = L[i].recv_block;
+        if (recv_node) recv_node[i] = L[i].recv_node;
+        if (donor_cell) donor_cell[i] = L[i].donor_cell;
+        if (nweights) nweights[i] = L[i].nw;
+        for (int m = 0; m < 4; m++) {
+            if (inode) inode[4 * i + m] = L[i].inode[m];
+            if (weights) weights[4 * i + m] = L[i].w[m];
+        }
+    }
+    return CFD_OK;
+}
+
+void cfd_connect_free(cfd_connect_t c) { delete c; }
 
 int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, const cfd_holemap_t* maps,
                       int nfringe, int* iblank, int* mandatory) {
