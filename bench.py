@@ -261,6 +261,36 @@ def overset_leg(stream) -> dict:
     t1.record(stream)
     torch.cuda.synchronize()
     out["exchange_us"] = round(1e3 * t0.elapsed_time(t1) / reps, 2)
+    # the full assembly (holes, resolution-based fringes, cancellations, fringe
+    # reduction, double fringe) and an exchange through the lists it returns
+    obc = [np.zeros(0, np.int32), rec_o]
+    tw = time.perf_counter()
+    asm = abi.overset_connect([bg, og], [None, hm], obc, nfringe=2, mexclude=3)
+    out_a = {"ms": round(1e3 * (time.perf_counter() - tw), 1), "nfringe": 2, "mexclude": 3}
+    out_a["holes"] = [int((i == 0).sum()) for i in asm["iblank"]]
+    out_a["receptors"] = [int((i == -1).sum()) for i in asm["iblank"]]
+    served = [sum(int((asm["interp"][d]["recv_block"] == k).sum()) for d in range(2)) for k in range(2)]
+    ok_a = served == out_a["receptors"]
+    lists = []
+    for d, (src_xy, rec_xy, r_k) in enumerate(((bxy, oxy, 1), (oxy, bxy, 0))):
+        it = asm["interp"][d]
+        sel = it["recv_block"] == r_k
+        w, inode, nw, recv = it["weights"][sel], it["inode"][sel], it["nweights"][sel], it["recv_node"][sel]
+        ok_a &= bool(np.all(w >= -1e-10) and np.all(w <= 1 + 1e-10) and np.max(np.abs(w.sum(1) - 1), initial=0) < 1e-12)
+        lin = lambda xy: 1.0 + 0.3 * xy[:, 0] - 0.7 * xy[:, 1]  # noqa: E731
+        q = lin(src_xy)
+        est = np.array([np.dot(w[i, :nw[i]], q[inode[i, :nw[i]]]) for i in range(len(recv))])
+        ok_a &= bool(len(recv) == 0 or np.max(np.abs(est - lin(rec_xy[recv]))) < 1e-11 * max(1.0, np.abs(q).max()))
+        lists.append(abi.Interp.from_list(recv, nw, inode, w, stream=stream.cuda_stream))
+    out_a["properties_ok"] = ok_a
+    t0.record(stream)
+    for _ in range(reps):
+        lists[0].update(qb.data_ptr(), meshes[0].nnode, qo.data_ptr(), meshes[1].nnode, 4, stream=stream.cuda_stream)
+        lists[1].update(qo.data_ptr(), meshes[1].nnode, qb.data_ptr(), meshes[0].nnode, 4, stream=stream.cuda_stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    out_a["exchange_us"] = round(1e3 * t0.elapsed_time(t1) / reps, 2)
+    out["assembly"] = out_a
     for p in paths:
         p.unlink()
     return out

@@ -321,7 +321,7 @@ void cfd_holemap_free(cfd_holemap_t h);
  * 0.  Host output arrays of the block's node count; mandatory may be NULL. */
 int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, const cfd_holemap_t* maps,
                       int nfringe, int* iblank, int* mandatory);
-/* Overset assembly of nblocks blocks on this device (one rank's
+/* Overset assembly of nblocks (2 to 64) blocks on this device (one rank's
  * tioga::performConnectivity, tioga.cpp:153-262, with MeshBlock::preprocess,
  * MeshBlock.cpp:135-425; processDonors / findInterpData / cancellation /
  * reduce_fringes, bookkeeping.cpp:75-705; exchangeDonors' order,

@@ -1300,8 +1300,8 @@ struct ConnDonor {
 
 int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holemap_t* maps, const int* const* obc_nodes,
                         const int* nobc, int nfringe, int mexclude, cfd_connect_t* out) {
-    if (nblocks < 2 || !blocks || !maps || !nobc || !obc_nodes || nfringe < 0 || mexclude < 0 || !out)
-        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_connect: bad argument");
+    if (nblocks < 2 || nblocks > 64 || !blocks || !maps || !nobc || !obc_nodes || nfringe < 0 || mexclude < 0 || !out)
+        return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_connect: bad argument (2 to 64 blocks)");
     for (int b = 0; b < nblocks; b++) {
         if (!blocks[b]) return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_overset_connect: null block");
         if (nobc[b] < 0 || (nobc[b] > 0 && !obc_nodes[b]))
@@ -1444,10 +1444,10 @@ int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holema
             const int nn = blocks[r]->nnode;
             ibl[r].assign(nn, 1);
             for (int i = 0; i < nn; i++) {
-                std::vector<char> has(nb, 0);
-                for (const auto& e : dl[r][i]) has[e.d] = 1;
+                unsigned long long has = 0;  // blocks that gave node i a donor
+                for (const auto& e : dl[r][i]) has |= 1ull << e.d;
                 for (int j = 0; j < nb; j++) {
-                    if (j == r || !maps[j] || has[j]) continue;
+                    if (j == r || !maps[j] || ((has >> j) & 1)) continue;
                     if (inside[j][r][i]) {
                         ibl[r][i] = 0;
                         break;
