@@ -237,6 +237,20 @@ int cfd_selftest_bounded_wait(cfd_case_t c, long long polls);
  * (hops - 1).  2 <= hops <= 1024.  stream may be NULL. */
 int cfd_measure_hop_latency(void* stream, int hops, int fp64_ops, double* us_per_hop);
 
+/* ---- field dumps (TopologyHolderStrategyOutput.cpp) ---------------------- */
+/* Tecplot files in the reference's layouts, byte for byte: node coordinates,
+ * the data, each cell's 1-based vertices padded to four; numbers in the C++
+ * stream's default format.
+ * cfd_write_cell_data: writeCellData (:466-554) of mesh `mesh` of the case
+ *   (density, pressure, u, v, Cp, Mach per cell; Cp and Mach formed on the
+ *   device), file filename_<mesh+1>_<proc+1>; m must be that mesh.
+ * cfd_write_node_data: writeNOdeData (:556-630), node_q[4*node + k] (host).
+ * cfd_write_tioga_format: writeTiogaFormat (:410-464), one int per cell
+ *   (host), file filename<mesh><proc>. */
+int cfd_write_cell_data(cfd_case_t c, int mesh, cfd_mesh_t m, const char* filename, int proc);
+int cfd_write_node_data(cfd_mesh_t m, int mesh, const char* filename, int proc, const double* node_q);
+int cfd_write_tioga_format(cfd_mesh_t m, int mesh, const char* filename, int proc, const int* cell_data);
+
 /* ---- overset connectivity and fringe exchange (UniTioga MeshBlock) ------- */
 /* Layouts of a node array for the fringe update (dataUpdate.cpp:4-5). */
 #define CFD_LAYOUT_ROW     0  /* q[node*nvar + k]   */

@@ -8,6 +8,7 @@
 //              [INIT_U.bin|-] [FIRST_ORDER]
 //   FLOW    = euler | viscous          (Euler2D / ViscousFlow2D)
 //   ADVANCE = rk5 | lusgs              (RungeKuttaStrategy(5) / LUSGSIntegrator)
+//   environment WRITE_TECPLOT=1: also the reference's Tecplot field dumps (end of main)
 //
 // Setup follows WrapSolver::setParams/init (UnstructSolver/SolverWrapper.h:27-69):
 // default-constructed strategy, set_fs_variable2(Ma, AoA, 1.225, 101325, Re),
@@ -269,6 +270,21 @@ int main(int argc, char** argv) {
         } else {
             dump("end_W0", rk->W_scratch[0], (size_t)nc * 32);
         }
+    }
+    // Field dumps in the reference's Tecplot layouts (environment WRITE_TECPLOT
+    // set): TopologyHolderStrategy::writeCellData of the final cell state,
+    // writeNOdeData of node data (node i, variable k: 0.001*i + k), and
+    // writeTiogaFormat of cell data (cell c: c % 3 - 1), all into OUTDIR.
+    if (getenv("WRITE_TECPLOT")) {
+        st->writeCellData(g_out + "/cells", 0, 0, st->getU());
+        std::vector<double> nodeq(4 * (size_t)np);
+        for (int i = 0; i < np; i++)
+            for (int k = 0; k < 4; k++) nodeq[4 * (size_t)i + k] = 0.001 * i + k;
+        double* nq[1] = {nodeq.data()};
+        st->writeNOdeData(g_out + "/nodes", 0, 0, nq);
+        std::vector<int> ic(nc);
+        for (int c = 0; c < nc; c++) ic[c] = c % 3 - 1;
+        st->writeTiogaFormat(g_out + "/tioga", 0, 0, ic.data());
     }
     std::cout.rdbuf(saved);
     printf("{\"ncell\": %d, \"nedge\": %d, \"nsteps\": %d, \"seconds\": %.6f, \"cell_iters_per_s\": %.6e}\n",

@@ -356,3 +356,17 @@ def test_fast_sweep_chain_schedule_bitwise(prec, bpsm):
             out.append((case.get("U"), case.get("DW1"), case.get("DW")))
         for a, b in zip(*out):
             np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["mixed_lam_lusgs", "omesh_euler_rk5"])
+def test_tecplot_cell_dump_matches_reference(tmp_path, name):
+    """writeCellData: the state of the fixture's initial field, Cp and Mach
+    formed on the device, written byte for byte as the reference writes it."""
+    from tmp_gb300 import abi
+
+    c, g = manifest()[name], golden(name)
+    tec = np.load(GOLDEN / "tecplot.npz")
+    _, case = make_case(c)
+    case.put("U", g["init_U"])
+    case.write_cell_data(str(tmp_path / "cells"))
+    assert (tmp_path / "cells_1_1").read_bytes() == bytes(tec[f"{name}/cells"])

@@ -125,3 +125,22 @@ def test_uneven_batch_definition():
     for c in small:
         g = c.grd()
         assert 0.6 < g.ncell / c.target_cells < 1.6, (c, g.ncell)
+
+
+@pytest.mark.parametrize("name", ["mixed_lam_lusgs", "omesh_euler_rk5"])
+def test_tecplot_node_and_tioga_dumps_match_reference(tmp_path, name):
+    """writeNOdeData / writeTiogaFormat layouts, byte for byte against the
+    reference's own files (tests/golden/tecplot.npz)."""
+    import json
+
+    from tmp_gb300 import abi
+
+    golden = GOLDEN
+    c = json.loads((golden / "manifest.json").read_text())[name]
+    tec = np.load(golden / "tecplot.npz")
+    m = abi.Mesh.load_grd(golden / c["mesh"], c["wall_tag"], c["far_tag"])
+    node_q = np.array([[0.001 * i + k for k in range(4)] for i in range(m.nnode)])
+    abi.write_node_data(m, str(tmp_path / "nodes"), node_q)
+    assert (tmp_path / "nodes_1_1").read_bytes() == bytes(tec[f"{name}/nodes"])
+    abi.write_tioga_format(m, str(tmp_path / "tioga"), np.arange(m.ncell) % 3 - 1)
+    assert (tmp_path / "tioga00").read_bytes() == bytes(tec[f"{name}/tioga"])

@@ -123,6 +123,9 @@ def lib() -> C.CDLL:
         "cfd_connect_interp_count": (C.c_int, [vp, C.c_int, C.POINTER(C.c_longlong)]),
         "cfd_connect_interp_get": (C.c_int, [vp, C.c_int, ip, ip, ip, ip, ip, dp]),
         "cfd_connect_free": (None, [vp]),
+        "cfd_write_cell_data": (C.c_int, [vp, C.c_int, vp, C.c_char_p, C.c_int]),
+        "cfd_write_node_data": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int, dp]),
+        "cfd_write_tioga_format": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int, ip]),
         "cfd_mlp_create": (C.c_int, [C.c_ulonglong, C.POINTER(vp)]),
         "cfd_mlp_free": (None, [vp]),
         "cfd_mlp_get_params": (C.c_int, [vp, fp, fp]),
@@ -236,6 +239,10 @@ class Case:
         s = C.c_void_p()
         check(lib().cfd_case_stream(self.h, C.byref(s)))
         return s.value or 0
+
+    def write_cell_data(self, filename: str, mesh: int = 0, proc: int = 0):
+        """Tecplot cell dump of one mesh (TopologyHolderStrategy::writeCellData)."""
+        check(lib().cfd_write_cell_data(self.h, int(mesh), self.meshes[mesh].h, str(filename).encode(), int(proc)))
 
     def wall_force(self, mesh: int = 0, ref_length: float = 1.0) -> dict:
         """Wall force of the current state: Fx, Fy, CL, CD."""
@@ -487,6 +494,18 @@ def overset_blank(block: Block, others: Sequence[Block], maps: Sequence[HoleMap 
     md = np.zeros(block.nnode, np.int32)
     check(lib().cfd_overset_blank(block.h, n, ob, mp, int(nfringe), _iptr(ib), _iptr(md)))
     return ib, md
+
+
+def write_node_data(mesh: Mesh, filename: str, node_q: np.ndarray, mesh_index: int = 0, proc: int = 0):
+    """Tecplot node dump (TopologyHolderStrategy::writeNOdeData), node_q (nnode, 4)."""
+    q = np.ascontiguousarray(node_q, dtype=np.float64).reshape(-1)
+    check(lib().cfd_write_node_data(mesh.h, int(mesh_index), str(filename).encode(), int(proc), _dptr(q)))
+
+
+def write_tioga_format(mesh: Mesh, filename: str, cell_data: np.ndarray, mesh_index: int = 0, proc: int = 0):
+    """Tecplot cell-integer dump (TopologyHolderStrategy::writeTiogaFormat)."""
+    a = np.ascontiguousarray(cell_data, dtype=np.int32)
+    check(lib().cfd_write_tioga_format(mesh.h, int(mesh_index), str(filename).encode(), int(proc), _iptr(a)))
 
 
 def overset_connect(blocks: Sequence[Block], maps: Sequence[HoleMap | None], obc_nodes: Sequence[np.ndarray],

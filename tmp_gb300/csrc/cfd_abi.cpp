@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -835,6 +836,112 @@ int cfd_sync(cfd_case_t c) {
 }
 
 long long cfd_launch_count(cfd_case_t c) { return c ? c->launches : -1; }
+
+// Tecplot field dumps in the reference's layouts (TopologyHolderStrategyOutput.cpp:410-631):
+// node coordinates (FEBLOCK), the data, then every cell's 1-based vertices,
+// padded to four with its last vertex; numbers with the stream defaults.
+namespace {
+void tec_nodes_and_cells(std::ofstream& f, const cfdgb::HostMesh& m, int part) {
+    if (part == 0) {
+        for (int j = 0; j < 2; j++)
+            for (int i = 0; i < m.nnode; i++) f << m.xy[2 * (size_t)i + j] << '\n';
+        return;
+    }
+    for (int c = 0; c < m.ncell; c++) {
+        const int nv = m.cell_nvert[c];
+        for (int j = 0; j < nv; j++) f << m.cell_verts[4 * (size_t)c + j] + 1 << '\t';
+        for (int j = 0; j < 4 - nv; j++) f << m.cell_verts[4 * (size_t)c + nv - 1] + 1 << '\t';
+        f << '\n';
+    }
+}
+}  // namespace
+
+int cfd_write_cell_data(cfd_case_t c, int mesh, cfd_mesh_t m, const char* filename, int proc) {
+    if (!c || !m || !filename) return fail(CFD_ERR_ARG, "null argument");
+    if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
+    const int b = c->coff[mesh], e = c->coff[mesh + 1];
+    if (m->m.ncell != e - b) return fail(CFD_ERR_ARG, "cfd_write_cell_data: the mesh is not the case's mesh");
+    ABI_TRY
+    const int nc = e - b;
+    std::vector<d4> u(nc);
+    std::vector<double> cpma(2 * (size_t)nc);
+    double* d_out = nullptr;
+    dalloc(&d_out, 2 * (size_t)nc);
+    const MeshPrm& p = c->prm[mesh];
+    launch_cp_ma(c->d, c->L(), b, e, p.p_inf, p.u_inf, p.v_inf, d_out);
+    ck(cudaGetLastError(), "k_cp_ma");
+    ck(cudaMemcpyAsync(cpma.data(), d_out, cpma.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "copy");
+    ck(cudaMemcpyAsync(u.data(), c->d.U + b, nc * sizeof(d4), cudaMemcpyDeviceToHost, c->stream), "copy");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    cudaFree(d_out);
+    const std::string name = std::string(filename) + "_" + std::to_string(mesh + 1) + "_" + std::to_string(proc + 1);
+    std::ofstream f(name, std::ios::out);
+    if (!f.is_open()) return fail(CFD_ERR_ARG, "Open file failure");
+    f << "TITLE =\"Tioga output\"\n";
+    f << "VARIABLES=\"X\",\"Y\",";
+    f << "\"Density\",\"Pressure\",\"U\",\"V\",\n";
+    f << "\"Cp\",\"Ma\"";
+    f << "ZONE T=\"VOL_MIXED\",N=" << m->m.nnode << " E=" << nc;
+    f << " ET = QUADRILATERAL, F = FEBLOCK\n";
+    f << "VARLOCATION =  (";
+    for (int i = 0; i < 2; i++) f << i + 1 << "=NODAL,";
+    for (int i = 0; i < 5; i++) f << 3 + i << "=CELLCENTERED,";
+    f << 8 << "=CELLCENTERED)\n";
+    tec_nodes_and_cells(f, m->m, 0);
+    for (int k = 0; k < 4; k++)
+        for (int j = 0; j < nc; j++) f << (&u[j].x)[k] << '\n';
+    for (int j = 0; j < nc; j++) f << cpma[2 * (size_t)j] << '\n';
+    for (int j = 0; j < nc; j++) f << cpma[2 * (size_t)j + 1] << '\n';
+    tec_nodes_and_cells(f, m->m, 1);
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_write_node_data(cfd_mesh_t m, int mesh, const char* filename, int proc, const double* node_q) {
+    if (!m || !filename || !node_q || mesh < 0) return fail(CFD_ERR_ARG, "null argument");
+    ABI_TRY
+    const std::string name = std::string(filename) + "_" + std::to_string(mesh + 1) + "_" + std::to_string(proc + 1);
+    std::ofstream f(name, std::ios::out);
+    if (!f.is_open()) return fail(CFD_ERR_ARG, "Open file failure");
+    const int nequ = 4;
+    f << "TITLE =\"Tioga output\"\n";
+    f << "VARIABLES=\"X\",\"Y\",";
+    for (int i = 0; i < nequ - 1; i++) f << "\"Variable" << i + 1 << "\",";
+    f << "\"Variable\"";
+    f << "ZONE T=\"VOL_MIXED\",N=" << m->m.nnode << " E=" << m->m.ncell;
+    f << " ET = QUADRILATERAL, F = FEBLOCK\n";
+    f << "VARLOCATION =  (";
+    for (int i = 0; i < 2; i++) f << i + 1 << "=NODAL,";
+    for (int i = 0; i < nequ - 1; i++) f << 3 + i << "=NODAL,";
+    f << 2 + nequ << "=NODAL)\n";
+    tec_nodes_and_cells(f, m->m, 0);
+    for (int k = 0; k < nequ; k++)
+        for (int j = 0; j < m->m.nnode; j++) f << node_q[k + nequ * (size_t)j] << '\n';
+    tec_nodes_and_cells(f, m->m, 1);
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_write_tioga_format(cfd_mesh_t m, int mesh, const char* filename, int proc, const int* cell_data) {
+    if (!m || !filename || !cell_data || mesh < 0) return fail(CFD_ERR_ARG, "null argument");
+    ABI_TRY
+    const std::string name = std::string(filename) + std::to_string(mesh) + std::to_string(proc);
+    std::ofstream f(name);
+    if (!f.is_open()) return fail(CFD_ERR_ARG, "Open file failure");
+    f << "TITLE =\"Tioga output\"\n";
+    f << "VARIABLES=\"X\",\"Y\",";
+    f << "\"IBLANK\"\n";
+    f << "ZONE T=\"VOL_MIXED\",N=" << m->m.nnode << " E=" << m->m.ncell;
+    f << " ET = QUADRILATERAL, F = FEBLOCK\n";
+    f << "VARLOCATION =  (";
+    for (int i = 0; i < 2; i++) f << i + 1 << "=NODAL,";
+    f << 3 << "=CELLCENTERED)\n";
+    tec_nodes_and_cells(f, m->m, 0);
+    for (int i = 0; i < m->m.ncell; i++) f << cell_data[i] << '\n';
+    tec_nodes_and_cells(f, m->m, 1);
+    return CFD_OK;
+    ABI_CATCH
+}
 
 int cfd_wall_force(cfd_case_t c, int mesh, double ref_length, double* out4) {
     if (!c || !out4) return fail(CFD_ERR_ARG, "null argument");

@@ -1298,6 +1298,32 @@ cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool fo
     return cudaSuccess;
 }
 
+// Cp and Mach number of cells [begin, end) as TopologyHolderStrategy::
+// writeCellData forms them (TopologyHolderStrategyOutput.cpp:523-538):
+// Cp = 2 (p - p_inf) / (u_inf^2 + v_inf^2) and Ma = |u| / sqrt(p / rho).
+__global__ void k_cp_ma(int begin, int end, const d4* __restrict__ U, double pinf, double uinf, double vinf,
+                        double* __restrict__ out) {
+    const int c = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= end) return;
+    const d4 u = ld4(U + c);
+    const double vm = uinf * uinf + vinf * vinf;
+    const double cp = 2 * (u.y - pinf) / vm;
+    const double cs = sqrt(u.y / u.x);
+    double vel = 0;
+    vel += u.z * u.z;
+    vel += u.w * u.w;
+    vel = sqrt(vel);
+    out[2 * (size_t)(c - begin)] = cp;
+    out[2 * (size_t)(c - begin) + 1] = vel / cs;
+}
+
+void launch_cp_ma(const DevArrays& d, const LaunchCfg& L, int begin, int end, double pinf, double uinf, double vinf,
+                  double* out) {
+    if (end <= begin) return;
+    k_cp_ma<<<nblk(end - begin, 256), 256, 0, L.stream>>>(begin, end, d.U, pinf, uinf, vinf, out);
+    *L.counter += 1;
+}
+
 // 1/D for the fast form's sweep (binary64)
 __global__ void k_inv_diag(int nc, const double* __restrict__ D, double* __restrict__ invD) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
