@@ -203,13 +203,14 @@ def run_to_drop(case: abi.Case, target: float, max_iters: int, mlp: abi.Mlp | No
     hist = [(1, 1.0)]
     attached = False
     saved = None
+    save_every = 500  # iterations between restart points (each is a device-to-host copy of the state)
     t0 = time.perf_counter()
     while it < max_iters and (max_seconds is None or time.perf_counter() - t0 < max_seconds):
         if mlp is not None and not attached and not fell and it >= warm:
             abi.case_set_mlp(case, mlp, apply_cfl, spread)
             attached = True
-        if attached:
-            saved = (it, case.get("U"))  # restart point should the learned chunk fail
+        if attached and (saved is None or it - saved[0] >= save_every):
+            saved = (it, case.get("U"))  # restart point should a learned chunk fail
         try:
             case.step_graph(chunk)
             it += chunk
