@@ -69,7 +69,8 @@ def parse():
     ap.add_argument("--drop-seconds", type=float, default=40.0, help="cap per form for time_to_drop")
     ap.add_argument("--drop-forms", default="fp64,fp32,mixed,mixed+learned,fp32>mixed+learned",
                     help="forms for time_to_drop: PREC[>PREC2][+learned]; '>' switches at --switch-at")
-    ap.add_argument("--switch-at", type=float, default=1e-3, help="residual fall at which 'A>B' switches form")
+    ap.add_argument("--switch-at", type=float, default=3e-4,
+                    help="residual fall at which 'A>B' switches form (or earlier, once A's residual stalls)")
     ap.add_argument("--no-overset", action="store_true", help="skip the overset connectivity / exchange leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch leg (256 packed cases)")
     ap.add_argument("--batch-meshes", type=int, default=256, help="meshes in the uneven-batch leg")

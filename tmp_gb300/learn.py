@@ -189,9 +189,10 @@ def run_to_drop(case: abi.Case, target: float, max_iters: int, mlp: abi.Mlp | No
                 switch_to: int | None = None) -> RunResult:
     """Iterate until the L2 density residual falls by `target` (relative to iteration 1).
 
-    switch_at / switch_to: once the residual has fallen by switch_at, the case
-    switches to the precision form switch_to (cfd_set_precision), e.g. from the
-    binary32 form, whose residual stalls near 1e-4, to the mixed form."""
+    switch_at / switch_to: once the residual has fallen by switch_at, or has
+    fallen by less than 5% over the last 1000 iterations, the case switches to
+    the precision form switch_to (cfd_set_precision), e.g. from the binary32
+    form, whose residual stalls near 1e-4, to the mixed form."""
     lusgs = case.advance == abi.ADV_LUSGS
     if lusgs:
         abi.case_track(case, True)
@@ -228,9 +229,14 @@ def run_to_drop(case: abi.Case, target: float, max_iters: int, mlp: abi.Mlp | No
                 case.put("U", saved[1])
                 continue
         best = min(best, r) if r == r else best
-        if switch_at is not None and switch_to is not None and r <= switch_at:
-            case.set_precision(switch_to)
-            switch_at = None
+        if switch_at is not None and switch_to is not None:
+            # switch at the given fall, or earlier if the residual has stopped
+            # falling (less than 5% over the last 1000 iterations)
+            back = [h for h in hist if h[0] <= it - 1000]
+            stalled = bool(back) and not (r < 0.95 * back[-1][1])
+            if r <= switch_at or stalled:
+                case.set_precision(switch_to)
+                switch_at = None
         if r <= target:
             break
     el = time.perf_counter() - t0
