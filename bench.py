@@ -67,7 +67,7 @@ def parse():
     ap.add_argument("--forms", default="fp64,fp32,mixed", help="precision forms timed besides --precision ('' = none)")
     ap.add_argument("--drop", type=float, default=1e-3, help="residual fall for time_to_drop (0 = skip)")
     ap.add_argument("--drop-seconds", type=float, default=40.0, help="cap per form for time_to_drop")
-    ap.add_argument("--drop-forms", default="fp64,fp32,mixed,mixed+learned,fp32>mixed+learned",
+    ap.add_argument("--drop-forms", default="fp64,fp32,mixed,mixed+learned,fp32>mixed+learned,fp32+learned>mixed",
                     help="forms for time_to_drop: PREC[>PREC2][+learned]; '>' switches at --switch-at")
     ap.add_argument("--switch-at", type=float, default=3e-4,
                     help="residual fall at which 'A>B' switches form (or earlier, once A's residual stalls)")
@@ -592,18 +592,22 @@ def run_ours(args):
         drop = {"target": args.drop, "norm": "L2 density residual / iteration 1", "cap_s": args.drop_seconds,
                 "learned_weights": str(learn.WEIGHTS.relative_to(ROOT)) if net else None}
         for f in [x for x in args.drop_forms.split(",") if x]:
-            learned = f.endswith("+learned")
+            # "A>B" switches form A to B; "+learned" at the end keeps the learned
+            # relaxation on throughout, "A+learned>B" only until the switch
+            learned = "+learned" in f
             if learned and (net is None or w.advance != "lusgs"):
                 continue
             if w.advance != "lusgs" and ("mixed" in f):  # the mixed form is a LU-SGS form
                 continue
-            base = f[: -len("+learned")] if learned else f
-            first, _, then = base.partition(">")
+            first, _, then = f.partition(">")
+            until_switch = first.endswith("+learned")
+            first = first.replace("+learned", "")
+            then = then.replace("+learned", "")
             c2 = make_case(first)
             torch.cuda.synchronize()
             r = learn.run_to_drop(c2, args.drop, 10 ** 9, net if learned else None, chunk=50,
                                   max_seconds=args.drop_seconds, switch_at=args.switch_at if then else None,
-                                  switch_to=prec_code[then] if then else None)
+                                  switch_to=prec_code[then] if then else None, detach_at_switch=until_switch)
             drop[f] = {"reached": r.reached, "seconds": round(r.seconds, 3), "iterations": r.iterations,
                        "fall": r.history[-1][1], "fell_back": r.fell_back}
             c2.close()

@@ -186,13 +186,14 @@ class RunResult:
 def run_to_drop(case: abi.Case, target: float, max_iters: int, mlp: abi.Mlp | None = None, apply_cfl: bool = False,
                 chunk: int = 25, warm: int = 20, fallback: float = 10.0, spread: float = 0.0,
                 max_seconds: float | None = None, switch_at: float | None = None,
-                switch_to: int | None = None) -> RunResult:
+                switch_to: int | None = None, detach_at_switch: bool = False) -> RunResult:
     """Iterate until the L2 density residual falls by `target` (relative to iteration 1).
 
     switch_at / switch_to: once the residual has fallen by switch_at, or has
     fallen by less than 5% over the last 1000 iterations, the case switches to
     the precision form switch_to (cfd_set_precision), e.g. from the binary32
-    form, whose residual stalls near 1e-4, to the mixed form."""
+    form, whose residual stalls near 1e-4, to the mixed form.  detach_at_switch:
+    the learned relaxation only runs until the switch."""
     lusgs = case.advance == abi.ADV_LUSGS
     if lusgs:
         abi.case_track(case, True)
@@ -237,6 +238,10 @@ def run_to_drop(case: abi.Case, target: float, max_iters: int, mlp: abi.Mlp | No
             if r <= switch_at or stalled:
                 case.set_precision(switch_to)
                 switch_at = None
+                if detach_at_switch and attached:
+                    abi.case_set_mlp(case, None)  # the plain update in the second form
+                    attached = False
+                    mlp = None
         if r <= target:
             break
     el = time.perf_counter() - t0
