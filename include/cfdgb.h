@@ -192,6 +192,13 @@ int cfd_step_graph(cfd_case_t c, int nsteps);
 /* Norm of the last step for one mesh (synchronises; also reports device-side
  * error flags as CFD_ERR_PSTAR / CFD_ERR_NONPHYSICAL / CFD_ERR_WALLTAN). */
 int cfd_residual_norm(cfd_case_t c, int mesh, int which, double* out);
+/* One call for a host-driven loop (no reference counterpart): optionally the
+ * whole case's primitive field from host memory (host_u[4*ncell_total], the
+ * meshes one after another; pinned memory makes the copy asynchronous), then
+ * nsteps graph-replayed steps (cfd_step_graph), then, if host_norms is not
+ * NULL, every mesh's norm `which` into host_norms[nmesh]; synchronises once
+ * and reports device errors as cfd_sync does. */
+int cfd_step_io(cfd_case_t c, const double* host_u, int nsteps, int which, double* host_norms);
 /* Copy a field of one mesh to / from host memory (layout above). */
 int cfd_get_field(cfd_case_t c, int mesh, int which, double* host);
 int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host);

@@ -370,3 +370,21 @@ def test_tecplot_cell_dump_matches_reference(tmp_path, name):
     case.put("U", g["init_U"])
     case.write_cell_data(str(tmp_path / "cells"))
     assert (tmp_path / "cells_1_1").read_bytes() == bytes(tec[f"{name}/cells"])
+
+
+def test_step_io_equals_separate_calls():
+    """cfd_step_io (field in, graph steps, norms out, one sync) gives the bits
+    of the separate put / step_graph / norm calls."""
+    from tmp_gb300 import abi
+
+    c, g = manifest()["mixed_lam_lusgs"], golden("mixed_lam_lusgs")
+    _, a = make_case(c)
+    _, b = make_case(c)
+    u = np.ascontiguousarray(g["init_U"], np.float64).reshape(-1)
+    for _ in range(2):
+        n1 = a.step_io(u, 3, "L2_R_RHO")
+        b.put("U", u)
+        b.step_graph(3)
+        n2 = b.norm("L2_R_RHO")
+        assert n1[0] == n2
+        np.testing.assert_array_equal(a.get("U"), b.get("U"))

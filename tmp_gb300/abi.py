@@ -91,6 +91,7 @@ def lib() -> C.CDLL:
         "cfd_lusgs_step": (C.c_int, [vp]),
         "cfd_step_graph": (C.c_int, [vp, C.c_int]),
         "cfd_residual_norm": (C.c_int, [vp, C.c_int, C.c_int, dp]),
+        "cfd_step_io": (C.c_int, [vp, dp, C.c_int, C.c_int, dp]),
         "cfd_get_field": (C.c_int, [vp, C.c_int, C.c_int, dp]),
         "cfd_put_field": (C.c_int, [vp, C.c_int, C.c_int, dp]),
         "cfd_sync": (C.c_int, [vp]),
@@ -290,6 +291,16 @@ class Case:
 
     def step_graph(self, n: int = 1):
         check(lib().cfd_step_graph(self.h, int(n)))
+
+    def step_io(self, u_host: np.ndarray | None, nsteps: int = 1, which: str | None = "DW_RHO2",
+                out: np.ndarray | None = None) -> np.ndarray | None:
+        """Upload the primitive field (host, all meshes), step, read every mesh's norm: one call, one sync."""
+        up = _dptr(u_host) if u_host is not None else None
+        if which is not None and out is None:
+            out = np.zeros(self.nmesh)
+        check(lib().cfd_step_io(self.h, up, int(nsteps), NORM[which] if which else 0,
+                                _dptr(out) if which is not None else None))
+        return out
 
     def sync(self):
         check(lib().cfd_sync(self.h))

@@ -812,6 +812,34 @@ int cfd_step_graph(cfd_case_t c, int nsteps) {
     ABI_CATCH
 }
 
+int cfd_step_io(cfd_case_t c, const double* host_u, int nsteps, int which, double* host_norms) {
+    if (!c || nsteps < 0) return fail(CFD_ERR_ARG, "null case or negative step count");
+    if (host_norms && (which < 0 || which > 2)) return fail(CFD_ERR_ARG, "unknown norm");
+    ABI_TRY
+    auto L = c->L();
+    if (host_u) {
+        ck(cudaMemcpyAsync(c->d.U, host_u, (size_t)c->d.nc * 32, cudaMemcpyHostToDevice, c->stream), "upload");
+        launch_cons_from_prim(c->d, L, 0, c->d.nc);
+        if (c->fp32()) launch_to_fp32(c->d, L, false);
+        ck(cudaGetLastError(), "launch");
+    }
+    if (nsteps > 0) {
+        const int rc = cfd_step_graph(c, nsteps);
+        if (rc != CFD_OK) return rc;
+    }
+    if (host_norms) {
+        launch_norm(c->d, L, which);
+        ck(cudaGetLastError(), "norm launch");
+        ck(cudaMemcpyAsync(host_norms, c->d.norm_out, (size_t)c->nmesh * sizeof(double), cudaMemcpyDeviceToHost,
+                           c->stream), "norm readback");
+    }
+    const int st = check_errors(c);  // synchronises the stream
+    if (host_norms && which == CFD_NORM_L2_R_RHO)
+        for (int m = 0; m < c->nmesh; m++) host_norms[m] = sqrt(host_norms[m] / (double)(c->coff[m + 1] - c->coff[m]));
+    return st;
+    ABI_CATCH
+}
+
 int cfd_residual_norm(cfd_case_t c, int mesh, int which, double* out) {
     if (!c || !out) return fail(CFD_ERR_ARG, "null argument");
     if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
