@@ -893,15 +893,19 @@ int cfd_write_cell_data(cfd_case_t c, int mesh, cfd_mesh_t m, const char* filena
     const int nc = e - b;
     std::vector<d4> u(nc);
     std::vector<double> cpma(2 * (size_t)nc);
-    double* d_out = nullptr;
-    dalloc(&d_out, 2 * (size_t)nc);
+    struct DevBuf {
+        double* p = nullptr;
+        ~DevBuf() {
+            if (p) cudaFree(p);
+        }
+    } out;
+    dalloc(&out.p, 2 * (size_t)nc);
     const MeshPrm& p = c->prm[mesh];
-    launch_cp_ma(c->d, c->L(), b, e, p.p_inf, p.u_inf, p.v_inf, d_out);
+    launch_cp_ma(c->d, c->L(), b, e, p.p_inf, p.u_inf, p.v_inf, out.p);
     ck(cudaGetLastError(), "k_cp_ma");
-    ck(cudaMemcpyAsync(cpma.data(), d_out, cpma.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "copy");
+    ck(cudaMemcpyAsync(cpma.data(), out.p, cpma.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "copy");
     ck(cudaMemcpyAsync(u.data(), c->d.U + b, nc * sizeof(d4), cudaMemcpyDeviceToHost, c->stream), "copy");
     ck(cudaStreamSynchronize(c->stream), "sync");
-    cudaFree(d_out);
     const std::string name = std::string(filename) + "_" + std::to_string(mesh + 1) + "_" + std::to_string(proc + 1);
     std::ofstream f(name, std::ios::out);
     if (!f.is_open()) return fail(CFD_ERR_ARG, "Open file failure");
