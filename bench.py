@@ -463,7 +463,7 @@ def run_ours(args):
     import numpy as np
     import torch
 
-    from tmp_gb300 import abi, configs
+    from tmp_gb300 import abi, configs, replicas
     from tmp_gb300.build import build_library
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -541,11 +541,7 @@ def run_ours(args):
         dist.barrier()
     clocks = sampler.stop()
     t_local = sum(ms) / 1e3
-    t = torch.tensor([t_local], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    t_max = float(t.item())
-    value = nc * args.steps * world / t_max
+    t_max, value = replicas.job_rate(nc * args.steps, t_local, world, dist, device="cuda")
     case.sync()
 
     # end to end through the C ABI: pinned host field in, norm out, per step
@@ -563,10 +559,7 @@ def run_ours(args):
             # the step's field in from pinned host memory, one step, its residual norm back (one call, one sync)
             case.step_io(hv, 1, "DW_RHO2", nrm)
         el = time.perf_counter() - t0
-        te = torch.tensor([el], dtype=torch.float64, device="cuda")
-        if dist:
-            dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        e2e = {"value": nc * args.steps * world / float(te.item()), "unit": UNIT,
+        e2e = {"value": replicas.job_rate(nc * args.steps, el, world, dist, device="cuda")[1], "unit": UNIT,
                "h2d_bytes_per_step": nc * 32, "d2h_bytes_per_step": 8}
 
     # the other precision forms, timed the same way
