@@ -29,6 +29,7 @@ UNITS = [
     ("mesh.cpp", []),
     ("cfd_abi.cpp", []),
     ("k_fp64.cu", ["-fmad=false"]),
+    ("k_fp64fma.cu", []),
     ("k_fp32.cu", []),
     ("k_misc.cu", []),
     ("k_overset.cu", ["-fmad=false"]),

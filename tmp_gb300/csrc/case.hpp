@@ -138,6 +138,8 @@ struct LaunchCfg {
 void launch_geometry(const DevArrays& d, const LaunchCfg& L);
 // which: -1 = all three residual passes, 0 = face_state, 1 = cell_grad, 2 = face_flux
 void launch_residual_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
+// ---- k_fp64fma.cu (the same binary64 residual with multiply-add contraction: the mixed form) ----
+void launch_residual_fp64_contracted(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);
 void launch_sweep_level(const DevArrays& d, const LaunchCfg& L, bool viscous, bool forward, int begin, int end, bool fp32);
 void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32, bool reset);

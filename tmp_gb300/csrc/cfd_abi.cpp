@@ -138,13 +138,18 @@ void free_case(cfd_case_s* c) {
 }
 
 // Integrator steps -------------------------------------------------------------
+// The mixed form's binary64 residual is the contracted build (k_fp64fma.cu);
+// the plain form's reproduces the reference's roundings (k_fp64.cu).
 void residual_pass(cfd_case_s* c) {
     auto L = c->L();
     if (c->fp32()) launch_residual_fp32(c->d, L, c->viscous(), c->p.first_order);
+    else if (c->mixed()) launch_residual_fp64_contracted(c->d, L, c->viscous(), c->p.first_order);
     else launch_residual_fp64(c->d, L, c->viscous(), c->p.first_order);
 }
-void launch_pass(const DevArrays& d, const LaunchCfg& L, bool visc, bool f32, int which, int first_order) {
+void launch_pass(const DevArrays& d, const LaunchCfg& L, bool visc, bool f32, int which, int first_order,
+                 bool mixed = false) {
     if (f32) launch_residual_fp32(d, L, visc, first_order, which);
+    else if (mixed) launch_residual_fp64_contracted(d, L, visc, first_order, which);
     else launch_residual_fp64(d, L, visc, first_order, which);
 }
 void update_pass(cfd_case_s* c, int mode, double cfl, int stage, double alpha) {
@@ -1063,9 +1068,9 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
         if (flush) ck(cudaMemsetAsync(flush, r & 0xff, (size_t)flush_bytes, c->stream), "flush");
         ck(cudaEventRecord(e0, c->stream), "cudaEventRecord");
         switch (pass) {
-            case 0: launch_pass(d, L, visc, f32, 0, c->p.first_order); break;  // face_state
-            case 1: launch_pass(d, L, visc, f32, 1, c->p.first_order); break;  // cell_grad
-            case 2: launch_pass(d, L, visc, f32, 2, c->p.first_order); break;  // face_flux
+            case 0: launch_pass(d, L, visc, f32, 0, c->p.first_order, c->mixed()); break;  // face_state
+            case 1: launch_pass(d, L, visc, f32, 1, c->p.first_order, c->mixed()); break;  // cell_grad
+            case 2: launch_pass(d, L, visc, f32, 2, c->p.first_order, c->mixed()); break;  // face_flux
             case 3: update_pass(c, c->p.advance == CFD_ADV_RK5 ? 0 : 2, c->p.cfl, 0, 0.0); break;
             case 4: sweeps(c, true); break;   // includes the SolveDF constant pass
             case 5: sweeps(c, false); break;

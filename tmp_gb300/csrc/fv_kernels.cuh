@@ -33,7 +33,7 @@ __device__ __forceinline__ int code_face(int code) { return (code > 0 ? code : -
 // face_state: BoundaryStrategy::HandleBoundary + the per-edge part of
 // solveSpectralRadius (Euler2D.cpp:242-267, ViscousFlow2D.cpp:220-253) and of
 // LaminarFluxStrategy::computeMu for edges.
-template <class T, bool VISC>
+template <class T, bool VISC, int CONTRACT = 0>
 __global__ void __launch_bounds__(256) k_face_state(int nf, const int2* __restrict__ lr, const int* __restrict__ fmesh,
                                                     const MeshPrm* __restrict__ prm, const v4<T>* __restrict__ fg0,
                                                     const v4<T>* __restrict__ U, v4<T>* __restrict__ Ue,
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) k_face_state(int nf, const int2* __restri
 // cell_grad: solveGradient (Euler2D.cpp:209-240 / ViscousFlow2D.cpp:181-218),
 // the per-cell sums of solveSpectralRadius, computeMu for cells, and the
 // Venkatakrishnan limiter (Vankatakrishnan_Limiter.hpp:69-177,186-200).
-template <class T, bool VISC>
+template <class T, bool VISC, int CONTRACT = 0>
 __global__ void __launch_bounds__(256) k_cell_grad(
     int nc, const int4* __restrict__ cface, const int2* __restrict__ lr, const int* __restrict__ cmesh,
     const MeshPrm* __restrict__ prm, const v4<T>* __restrict__ cgeo, const v4<T>* __restrict__ fg0,
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) k_cell_grad(
 // LaminarFluxStrategy::computeFlux(int) (LaminarFluxStrategy.h:110-216).
 // Writes the convective and the viscous flux of each face separately so the
 // gather can add them in the reference's two-loop order.
-template <class T, bool VISC>
+template <class T, bool VISC, int CONTRACT = 0>
 __global__ void __launch_bounds__(256) k_face_flux(
     int nf, const int2* __restrict__ lr, const v4<T>* __restrict__ fg0, const v4<T>* __restrict__ fg1,
     const v4<T>* __restrict__ fvis, const v4<T>* __restrict__ U, const v4<T>* __restrict__ grad,
@@ -269,6 +269,11 @@ __global__ void __launch_bounds__(256) k_face_flux(
     v.w = (txy * nx + tyy * ny) * A;
     st4(Fv + f, v);
 }
+
+// (CONTRACT only names the instantiation: the binary64 residual is built twice,
+// in k_fp64.cu without multiply-add contraction (the reference's bits) and in
+// k_fp64fma.cu with it (the mixed form, whose residual need not equal the
+// reference's bits), and distinct template arguments keep the two apart.)
 
 // ---------------------------------------------------------------------------
 // cell_update: residual gather (R[lC] += F, R[rC] -= F in HLLCFluxStrategy.cpp:
