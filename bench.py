@@ -175,6 +175,9 @@ def traffic_bytes(pass_name: str, precision: str, nc: int, sweep_mode: int = 0):
     form = "fp32" if precision == "fp32" or (precision == "mixed" and sweep) else "fp64"
     if sweep and form == "fp32" and sweep_mode == 5:
         row = traffic_table().get(f"fp32_chain_{pass_name}")
+    elif precision == "mixed" and not sweep and f"fp64c_{pass_name}" in traffic_table():
+        # the mixed form's residual passes are the contracted binary64 build
+        row = traffic_table().get(f"fp64c_{pass_name}")
     else:
         row = traffic_table().get(f"{form}_{'sweep_fwd' if sweep else pass_name}")
     if not row:
