@@ -7,15 +7,18 @@ Workload (default, config C2): laminar Navier-Stokes around a cylinder on a
 LU-SGS at CFL 50.  One step = one LU-SGS iteration (residual, local dt,
 diagonal, forward + backward level-scheduled sweeps, update) over the mesh.
 
-  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--precision fp64|fp32|mixed]
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--precision fp64|fp32|mixed|mixff]
 
 Precision forms: fp64 = the plain path (every kernel in binary64, results
 equal to the reference's); fp32 = fluxes, gradients, limiter and the LU-SGS
 sweep in binary32 with the update, norms and diagonal in binary64; mixed =
 binary64 residual with the binary32 sweep (defect correction; converges to
-the binary64 solution in the same number of iterations as fp64; the default).
+the binary64 solution in the same number of iterations as fp64); mixff = the
+mixed form with fluxes, gradients and limiter in float-float pairs of binary32
+numbers (48-bit significands on the binary32 pipe, residual summed into
+binary64; the same iterations as mixed to a 1e-3 fall; the default).
 `value` is the --precision form; "forms" adds the
-other two measured the same way in the same run, and "time_to_drop" the wall
+others measured the same way in the same run, and "time_to_drop" the wall
 time each form takes from the freestream start to a --drop fall of the L2
 density residual (normalised by iteration 1), capped at --drop-seconds.
 
@@ -45,6 +48,9 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "cell-iters/s and time-to-1e-8 residual drop: FP32+learned vs FP64 plain"
 UNIT = "cell-iters/s"
+# arithmetic of each form: residual (fluxes, gradients, limiter) + sweep + update/norms/diagonal
+DTYPE = {"fp64": "f64", "fp32": "f32+f64", "mixed": "f64 residual+f32 sweep+f64",
+         "mixff": "f32-pair residual+f32 sweep+f64"}
 FLUSH_BYTES = 256 << 20  # > 129 MB L2
 
 
@@ -55,7 +61,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2")
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "fp32", "mixed"])
+    ap.add_argument("--precision", default="mixff", choices=["fp64", "fp32", "mixed", "mixff"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -67,7 +73,7 @@ def parse():
     ap.add_argument("--forms", default="fp64,fp32,mixed", help="precision forms timed besides --precision ('' = none)")
     ap.add_argument("--drop", type=float, default=1e-3, help="residual fall for time_to_drop (0 = skip)")
     ap.add_argument("--drop-seconds", type=float, default=40.0, help="cap per form for time_to_drop")
-    ap.add_argument("--drop-forms", default="fp64,fp32,mixed,mixed+learned,fp32>mixed+learned,fp32+learned>mixed",
+    ap.add_argument("--drop-forms", default="fp64,fp32,mixed,mixff,mixed+learned,fp32+learned>mixed,fp32+learned>mixff",
                     help="forms for time_to_drop: PREC[>PREC2][+learned]; '>' switches at --switch-at")
     ap.add_argument("--switch-at", type=float, default=3e-4,
                     help="residual fall at which 'A>B' switches form (or earlier, once A's residual stalls)")
@@ -139,10 +145,11 @@ def measured_peak_gbs() -> tuple[float, str]:
 def alg_bytes(pass_name: str, nc: int, nf: int, viscous: bool, precision: str) -> int:
     """Compulsory bytes of one launch: each array the kernel touches, once.
 
-    The residual passes run in binary32 only in the fp32 form; the LU-SGS
-    sweeps in both the fp32 and mixed forms."""
+    The residual passes run in binary32 only in the fp32 form (float-float
+    pairs in the mixff form take binary64's 8 bytes); the LU-SGS sweeps in
+    binary32 in the fp32, mixed and mixff forms."""
     sweep = pass_name in ("sweep_fwd", "sweep_bwd", "lusgs_update")
-    fp32 = precision == "fp32" or (precision == "mixed" and sweep)
+    fp32 = precision == "fp32" or (precision in ("mixed", "mixff") and sweep)
     s = 4 if fp32 else 8
     v = 1 if viscous else 0
     if pass_name == "face_state":
@@ -172,12 +179,14 @@ def traffic_bytes(pass_name: str, precision: str, nc: int, sweep_mode: int = 0):
     """DRAM bytes of one launch (one pass for the chain-scheduled sweep) from the committed ncu capture (per cell,
     scaled by the cell count)."""
     sweep = pass_name in ("sweep_fwd", "sweep_bwd")
-    form = "fp32" if precision == "fp32" or (precision == "mixed" and sweep) else "fp64"
+    form = "fp32" if precision == "fp32" or (precision in ("mixed", "mixff") and sweep) else "fp64"
     if sweep and form == "fp32" and sweep_mode == 5:
         row = traffic_table().get(f"fp32_chain_{pass_name}")
     elif precision == "mixed" and not sweep and f"fp64c_{pass_name}" in traffic_table():
         # the mixed form's residual passes are the contracted binary64 build
         row = traffic_table().get(f"fp64c_{pass_name}")
+    elif precision == "mixff" and not sweep:
+        row = traffic_table().get(f"ffq_{pass_name}")  # the float-float residual
     else:
         row = traffic_table().get(f"{form}_{'sweep_fwd' if sweep else pass_name}")
     if not row:
@@ -487,12 +496,12 @@ def run_ours(args):
     viscous = w.flow == "laminar"
     stream = torch.cuda.Stream()  # a real stream: graph capture is not allowed on the legacy default stream
     torch.cuda.set_stream(stream)
-    prec_code = dict(fp64=abi.PREC_FP64, fp32=abi.PREC_FP32, mixed=abi.PREC_MIXED)
+    prec_code = dict(fp64=abi.PREC_FP64, fp32=abi.PREC_FP32, mixed=abi.PREC_MIXED, mixff=abi.PREC_MIXFF)
 
     def sweep_mode_for(precision):
         if args.sweep_mode >= 0:
             return args.sweep_mode
-        return 5 if precision in ("fp32", "mixed") else 0
+        return 5 if precision in ("fp32", "mixed", "mixff") else 0
 
     def make_case(precision):
         mode = sweep_mode_for(precision)
@@ -567,7 +576,7 @@ def run_ours(args):
 
     # the other precision forms, timed the same way
     forms = {}
-    for f in [x for x in args.forms.split(",") if x and x != args.precision and (w.advance == "lusgs" or x != "mixed")]:
+    for f in [x for x in args.forms.split(",") if x and x != args.precision and (w.advance == "lusgs" or "mix" not in x)]:
         c2 = make_case(f)
         fm, _ = timed_steps(c2, args.steps)
         forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3),
@@ -591,7 +600,7 @@ def run_ours(args):
             learned = "+learned" in f
             if learned and (net is None or w.advance != "lusgs"):
                 continue
-            if w.advance != "lusgs" and ("mixed" in f):  # the mixed form is a LU-SGS form
+            if w.advance != "lusgs" and ("mix" in f):  # the mixed forms are LU-SGS forms
                 continue
             first, _, then = f.partition(">")
             until_switch = first.endswith("+learned")
@@ -666,7 +675,7 @@ def run_ours(args):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision], "data": "synthetic",
             "config": {"workload": w.name, "ncell": nc, "nedge": nf, "levels": list(nlev), "mach": w.mach,
                        "re": w.re, "cfl": w.cfl, "precision": args.precision,
                        "sweep": dict(zip(("mode", "blocks_per_sm"), case.sweep_config())),

@@ -49,6 +49,13 @@ extern "C" {
                                  CFD_PREC_FP64) with the binary32 LU-SGS
                                  sweep as the implicit operator; converges
                                  to the binary64 solution                 */
+#define CFD_PREC_MIXFF    3   /* CFD_PREC_MIXED with the residual's face
+                                 states, gradients, limiter and fluxes in
+                                 float-float pairs (48-bit significands on
+                                 the binary32 pipe) summed per cell into a
+                                 binary64 residual; converges to the
+                                 binary64 solution within ~1e-14 relative.
+                                 LU-SGS sweep modes 0, 3, 4, 5 only; no SST */
 
 /* Field selectors for cfd_get_field / cfd_put_field.  Cell fields use the
  * reference's interleaved layout [NEQU*cell + eq]; face fields [4*face + eq]. */

@@ -28,12 +28,13 @@ def _batch(n=8, seed=77, lo=2_000, hi=12_000):
     return cases, meshes, fs
 
 
-@pytest.mark.parametrize("precision,sweep_mode", [("fp64", 0), ("fp32", 0), ("mixed", 0), ("fp32", 5), ("mixed", 5)])
+@pytest.mark.parametrize("precision,sweep_mode", [("fp64", 0), ("fp32", 0), ("mixed", 0), ("fp32", 5), ("mixed", 5),
+                                                   ("mixff", 5)])
 @pytest.mark.parametrize("flow", ["euler", "laminar"])
 def test_uneven_batch_packed_matches_separate(precision, sweep_mode, flow):
     from tmp_gb300 import abi
 
-    prec = dict(fp64=abi.PREC_FP64, fp32=abi.PREC_FP32, mixed=abi.PREC_MIXED)[precision]
+    prec = dict(fp64=abi.PREC_FP64, fp32=abi.PREC_FP32, mixed=abi.PREC_MIXED, mixff=abi.PREC_MIXFF)[precision]
     fl = abi.FLOW_EULER if flow == "euler" else abi.FLOW_LAMINAR
     _, meshes, fs = _batch()
     packed = abi.Case(meshes, fs, fl, abi.ADV_LUSGS, prec, cfl=10.0, sweep_mode=sweep_mode)

@@ -21,7 +21,7 @@ ERR = {-1: "ARG", -2: "IO", -3: "MESH", -4: "CUDA", -5: "PSTAR", -6: "NONPHYSICA
 BC_WALL, BC_FARFIELD = -2, -3
 FLOW_EULER, FLOW_LAMINAR = 0, 1
 ADV_RK5, ADV_LUSGS = 0, 1
-PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
+PREC_FP64, PREC_FP32, PREC_MIXED, PREC_MIXFF = 0, 1, 2, 3
 FIELD = dict(U=0, W=1, R=2, GRAD=3, PHI=4, SPEC_C=5, SPEC_V=6, DT=7, DIAG=8, DW1=9, DW=10, GRADT=11, MU=12,
              UEDGE=13, MUEDGE=14, VOL=15, CENTER=16, NORMAL=17, AREA=18, ECENTER=19, WALLDIST=20, SST_T=21,
              SST_TFACE=22, SST_TGRAD=23, SST_F1=24, SST_F2=25, SST_MUT=26, SST_MUTF=27, SST_FCONV=28,

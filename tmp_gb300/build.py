@@ -30,6 +30,7 @@ UNITS = [
     ("cfd_abi.cpp", []),
     ("k_fp64.cu", ["-fmad=false"]),
     ("k_fp64fma.cu", []),
+    ("k_ff.cu", ["-fmad=false"]),
     ("k_fp32.cu", []),
     ("k_misc.cu", []),
     ("k_overset.cu", ["-fmad=false"]),

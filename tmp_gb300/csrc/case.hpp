@@ -13,6 +13,7 @@ namespace cfdgb {
 struct DevArrays {
     int nc = 0, nf = 0, nn = 0, nmesh = 0;
     int resid32 = 0;             // 1 while the residual runs in binary32 (the FP32 form)
+    int residq = 0;              // 1 while the residual runs in float-float (the MIXFF form)
     // topology
     int2* lr = nullptr;          // [nf]
     int2* enodes = nullptr;      // [nf] global node ids
@@ -95,6 +96,23 @@ struct DevArrays {
     float* muef = nullptr;
     float4* Fcf = nullptr;
     float4* Fvf = nullptr;
+    // residual intermediates, float-float form (hi, lo pairs; same record sizes as binary64)
+    q4* Uq = nullptr;            // [nc] float-float copy of U, made at the start of each residual
+    q4* gradq = nullptr;         // [2*nc]
+    q4* phiq = nullptr;
+    ff* speccq = nullptr;
+    ff* specvq = nullptr;
+    q2* gradTq = nullptr;
+    ff* muq = nullptr;
+    q4* Ueq = nullptr;           // [nf]
+    q2* fspecq = nullptr;
+    ff* mueq = nullptr;
+    q4* Fcq = nullptr;
+    q4* Fvq = nullptr;
+    q4* fg0q = nullptr;          // float-float geometry copies
+    q4* fg1q = nullptr;
+    q4* fvisq = nullptr;
+    q4* cgeoq = nullptr;
     // LU-SGS per-step constants of SolveDF for every (cell, face slot)
     double* swfc = nullptr;      // [16*nc] F_c(W_j)[m] at (i*4+s)*4+m
     double* swra = nullptr;      // [4*nc]  r_A at i*4+s
@@ -148,25 +166,32 @@ cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forwa
 cudaError_t launch_sweep_pair64(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
 int sweep_flow_max_grid(bool low, int blocks_per_sm);
 void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
-void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, bool mu64);
+// kind of the viscosity array the binary32 sweep staging reads: the residual's form
+enum MuKind { MU_F32 = 0, MU_F64 = 1, MU_FF = 2 };
+void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mu_kind);
 cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool independent);
 int sweep_chain_max_grid(int blocks_per_sm);
-cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool viscous, bool mu64);
+cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool viscous, int mu_kind);
 void launch_chain_static(const DevArrays& d, const LaunchCfg& L);
 void launch_cp_ma(const DevArrays& d, const LaunchCfg& L, int begin, int end, double pinf, double uinf, double vinf,
                   double* out);
 void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
 void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);
-void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, bool fp32);
+// form: 0 binary64, 1 binary32, 2 float-float (the residual arrays read)
+void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, int form);
 void launch_wall_distance(const DevArrays& d, const LaunchCfg& L);
-void launch_wall_force(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32);
+void launch_wall_force(const DevArrays& d, const LaunchCfg& L, bool viscous, int form);
 // ---- k_sst.cu (compiled with -fmad=false) ----
 void launch_sst_residual(const DevArrays& d, const LaunchCfg& L);
 void launch_sst_update_mut(const DevArrays& d, const LaunchCfg& L);
 // ---- k_fp32.cu ----
 void launch_residual_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);
+// ---- k_ff.cu (float-float residual of the MIXFF form, compiled with -fmad=false) ----
+void launch_residual_ff(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
+void launch_update_ff(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);
+void launch_to_ff(const DevArrays& d, const LaunchCfg& L, bool geometry);
 // ---- k_misc.cu ----
 void launch_to_fp32(const DevArrays& d, const LaunchCfg& L, bool geometry);
 void launch_norm(const DevArrays& d, const LaunchCfg& L, int which);

@@ -43,6 +43,15 @@ void dalloc(T** p, size_t n) {
     ck(cudaMalloc((void**)p, n * sizeof(T)), "cudaMalloc");
 }
 
+// float-float residual intermediates and geometry copies (the MIXFF form)
+void alloc_ff_arrays(DevArrays& d, bool visc) {
+    const size_t nc = d.nc, nf = d.nf;
+    dalloc(&d.Uq, nc); dalloc(&d.gradq, 2 * nc); dalloc(&d.phiq, nc); dalloc(&d.speccq, nc);
+    dalloc(&d.Ueq, nf); dalloc(&d.fspecq, nf); dalloc(&d.Fcq, nf);
+    dalloc(&d.fg0q, nf); dalloc(&d.fg1q, nf); dalloc(&d.fvisq, nf); dalloc(&d.cgeoq, nc);
+    if (visc) { dalloc(&d.specvq, nc); dalloc(&d.gradTq, nc); dalloc(&d.muq, nc); dalloc(&d.mueq, nf); dalloc(&d.Fvq, nf); }
+}
+
 template <class T>
 void dfree(T*& p) {
     if (p) cudaFree((void*)p);
@@ -71,6 +80,10 @@ MeshPrm make_prm(const cfd_freestream_t& fs, bool viscous) {
     m.cc = 110.5 / temp;
     m.sqrt_gamma = sqrt(Gamma);
     m.viscous = viscous ? 1 : 0;
+    // float-float Sutherland constants (the mixed-ff form)
+    const double kk = (1.0 + m.cc) * m.sqrt_gamma * m.mach / m.re;
+    const ff qc(m.cc), qk(kk);
+    m.ffk[0] = qc.hi; m.ffk[1] = qc.lo; m.ffk[2] = qk.hi; m.ffk[3] = qk.lo;
     return m;
 }
 
@@ -106,7 +119,11 @@ struct cfd_case_s {
     int chain_cap = 0;               // co-resident blocks of the chain sweep (0: not queried)
     bool viscous() const { return p.flow == CFD_FLOW_LAMINAR; }
     bool fp32() const { return p.precision == CFD_PREC_FP32; }
-    bool mixed() const { return p.precision == CFD_PREC_MIXED; }
+    // binary64 state with the binary32 sweep: MIXED (binary64 residual) and MIXFF (float-float residual)
+    bool mixed() const { return p.precision == CFD_PREC_MIXED || p.precision == CFD_PREC_MIXFF; }
+    bool ffres() const { return p.precision == CFD_PREC_MIXFF; }
+    int mu_kind() const { return fp32() ? MU_F32 : ffres() ? MU_FF : MU_F64; }
+    int form() const { return fp32() ? 1 : ffres() ? 2 : 0; }  // residual arrays: binary64 / binary32 / float-float
     bool fast_sweep() const { return p.precision != CFD_PREC_FP64 && p.advance == CFD_ADV_LUSGS; }
     LaunchCfg L() { return LaunchCfg{stream, &launches}; }
     void drop_graph() {
@@ -130,7 +147,8 @@ void free_case(cfd_case_s* c) {
                     d.norm_out, d.err, d.dWprev, d.omega, d.omega_mean, d.mlp_samples, d.mlp_samp_off, d.sstT, d.sstTf, d.sstG, d.sstF1, d.sstF2,
                     d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD, d.chain_ptr[0], d.chain_ptr[1],
                     d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_stage[0],
-                    d.chain_stage[1], d.chain_posb, d.chain_dF};
+                    d.chain_stage[1], d.chain_posb, d.chain_dF, d.Uq, d.gradq, d.phiq, d.speccq, d.specvq, d.gradTq,
+                    d.muq, d.Ueq, d.fspecq, d.mueq, d.Fcq, d.Fvq, d.fg0q, d.fg1q, d.fvisq, d.cgeoq};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -143,18 +161,21 @@ void free_case(cfd_case_s* c) {
 void residual_pass(cfd_case_s* c) {
     auto L = c->L();
     if (c->fp32()) launch_residual_fp32(c->d, L, c->viscous(), c->p.first_order);
+    else if (c->ffres()) launch_residual_ff(c->d, L, c->viscous(), c->p.first_order);
     else if (c->mixed()) launch_residual_fp64_contracted(c->d, L, c->viscous(), c->p.first_order);
     else launch_residual_fp64(c->d, L, c->viscous(), c->p.first_order);
 }
 void launch_pass(const DevArrays& d, const LaunchCfg& L, bool visc, bool f32, int which, int first_order,
-                 bool mixed = false) {
+                 bool mixed = false, bool ffq = false) {
     if (f32) launch_residual_fp32(d, L, visc, first_order, which);
+    else if (ffq) launch_residual_ff(d, L, visc, first_order, which);
     else if (mixed) launch_residual_fp64_contracted(d, L, visc, first_order, which);
     else launch_residual_fp64(d, L, visc, first_order, which);
 }
 void update_pass(cfd_case_s* c, int mode, double cfl, int stage, double alpha) {
     auto L = c->L();
     if (c->fp32()) launch_update_fp32(c->d, L, c->viscous(), mode, cfl, stage, alpha);
+    else if (c->ffres()) launch_update_ff(c->d, L, c->viscous(), mode, cfl, stage, alpha);
     else launch_update_fp64(c->d, L, c->viscous(), mode, cfl, stage, alpha);
 }
 
@@ -337,11 +358,11 @@ void sweeps(cfd_case_s* c, bool forward) {
     // default: one dataflow launch per direction (binary64 form, mode 3: two cells per warp)
     if (c->fast_sweep() && c->p.sweep_mode == 5) {  // the staging pass replaces 1/D and the sweep constants
         ensure_chain(c);
-        ck(launch_sweep_chain32(d, L, forward, chain_grid(c), c->viscous(), c->mixed()), "cooperative sweep launch");
+        ck(launch_sweep_chain32(d, L, forward, chain_grid(c), c->viscous(), c->mu_kind()), "cooperative sweep launch");
     } else if (c->fast_sweep()) {
         if (forward) {
             launch_inv_diag(d, L);
-            launch_sweep_prep32(d, L, c->viscous(), c->mixed());
+            launch_sweep_prep32(d, L, c->viscous(), c->mu_kind());
         }
         ck(launch_sweep_flow32(d, L, forward, d.flow_grid, c->p.sweep_mode == 4), "cooperative sweep launch");
     } else if (c->p.sweep_mode == 3) {
@@ -483,9 +504,10 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
     const cfd_params_t& P = *params;
     if (P.flow != CFD_FLOW_EULER && P.flow != CFD_FLOW_LAMINAR) return fail(CFD_ERR_ARG, "Undefined Flow Type");
     if (P.advance != CFD_ADV_RK5 && P.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_ARG, "Undefined Advance Type");
-    if (P.precision != CFD_PREC_FP64 && P.precision != CFD_PREC_FP32 && P.precision != CFD_PREC_MIXED)
-        return fail(CFD_ERR_ARG, "unknown precision");
+    if (P.precision < CFD_PREC_FP64 || P.precision > CFD_PREC_MIXFF) return fail(CFD_ERR_ARG, "unknown precision");
     if (P.sweep_mode < 0 || P.sweep_mode > 5) return fail(CFD_ERR_ARG, "unknown sweep mode");
+    if (P.precision == CFD_PREC_MIXFF && P.advance == CFD_ADV_LUSGS && (P.sweep_mode == 1 || P.sweep_mode == 2))
+        return fail(CFD_ERR_ARG, "the MIXFF form runs the binary32 dataflow sweeps (sweep modes 0, 3, 4, 5)");
     for (int i = 0; i < nmesh; i++)
         if (!(fs[i].density > 0) || !(fs[i].pressure > 0) || !(fs[i].mach > 0))
             return fail(CFD_ERR_ARG, "freestream density, pressure and Mach must be positive");
@@ -619,6 +641,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         dalloc(&d.fgeo, nf); dalloc(&d.fcen, nf); dalloc(&d.cgeo, nc); dalloc(&d.fg0, nf); dalloc(&d.fg1, nf);
         dalloc(&d.fvis, nf);
         d.resid32 = c->fp32() ? 1 : 0;
+        d.residq = c->ffres() ? 1 : 0;
         dalloc(&d.U, nc); dalloc(&d.W, nc); dalloc(&d.W0, nc); dalloc(&d.R, nc); dalloc(&d.dt, nc);
         dalloc(&d.diag, nc); dalloc(&d.dW1, nc); dalloc(&d.dW, nc);
         if (c->fp32()) {
@@ -626,6 +649,8 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             dalloc(&d.Uf, nc); dalloc(&d.gradf, 2 * (size_t)nc); dalloc(&d.phif, nc); dalloc(&d.speccf, nc);
             dalloc(&d.Uef, nf); dalloc(&d.fspecf, nf); dalloc(&d.Fcf, nf);
             if (visc) { dalloc(&d.specvf, nc); dalloc(&d.gradTf, nc); dalloc(&d.muf, nc); dalloc(&d.muef, nf); dalloc(&d.Fvf, nf); }
+        } else if (c->ffres()) {
+            alloc_ff_arrays(d, visc);
         } else {
             dalloc(&d.grad, 2 * (size_t)nc); dalloc(&d.phi, nc); dalloc(&d.specc, nc);
             dalloc(&d.Ue, nf); dalloc(&d.fspec, nf); dalloc(&d.Fc, nf);
@@ -686,6 +711,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         launch_wall_distance(d, L);
         if (c->fp32()) launch_to_fp32(d, L, true);
         else if (c->mixed()) launch_to_fp32(d, L, true);  // binary32 geometry for the sweep
+        if (c->ffres()) launch_to_ff(d, L, true);          // float-float geometry for the residual
         ck(cudaGetLastError(), "geometry launch");
         ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
         *out = c;
@@ -763,7 +789,7 @@ int cfd_residual(cfd_case_t c, int stage) {
 int cfd_local_dt(cfd_case_t c, double cfl) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
     ABI_TRY
-    launch_local_dt(c->d, c->L(), cfl, c->fp32());
+    launch_local_dt(c->d, c->L(), cfl, c->form());
     ck(cudaGetLastError(), "launch");
     return CFD_OK;
     ABI_CATCH
@@ -987,7 +1013,7 @@ int cfd_wall_force(cfd_case_t c, int mesh, double ref_length, double* out4) {
     ABI_TRY
     auto L = c->L();
     residual_pass(c);  // fluxes of the current state
-    launch_wall_force(c->d, L, c->viscous(), c->fp32());
+    launch_wall_force(c->d, L, c->viscous(), c->form());
     ck(cudaGetLastError(), "wall force launch");
     double f[2];
     ck(cudaMemcpyAsync(f, c->d.wforce + 2 * mesh, sizeof(f), cudaMemcpyDeviceToHost, c->stream), "download");
@@ -1062,15 +1088,15 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
     for (int r = 0; r < reps; r++) {
         // a lone backward sweep needs the "not yet computed" markers the forward pass sets
         if (pass == 5 && (c->p.sweep_mode == 0 || c->p.sweep_mode >= 3)) {
-            if (c->fast_sweep()) launch_sweep_prep32(d, L, visc, c->mixed());
+            if (c->fast_sweep()) launch_sweep_prep32(d, L, visc, c->mu_kind());
             else launch_sweep_prep(d, L, visc, f32, true);
         }
         if (flush) ck(cudaMemsetAsync(flush, r & 0xff, (size_t)flush_bytes, c->stream), "flush");
         ck(cudaEventRecord(e0, c->stream), "cudaEventRecord");
         switch (pass) {
-            case 0: launch_pass(d, L, visc, f32, 0, c->p.first_order, c->mixed()); break;  // face_state
-            case 1: launch_pass(d, L, visc, f32, 1, c->p.first_order, c->mixed()); break;  // cell_grad
-            case 2: launch_pass(d, L, visc, f32, 2, c->p.first_order, c->mixed()); break;  // face_flux
+            case 0: launch_pass(d, L, visc, f32, 0, c->p.first_order, c->mixed(), c->ffres()); break;  // face_state
+            case 1: launch_pass(d, L, visc, f32, 1, c->p.first_order, c->mixed(), c->ffres()); break;  // cell_grad
+            case 2: launch_pass(d, L, visc, f32, 2, c->p.first_order, c->mixed(), c->ffres()); break;  // face_flux
             case 3: update_pass(c, c->p.advance == CFD_ADV_RK5 ? 0 : 2, c->p.cfl, 0, 0.0); break;
             case 4: sweeps(c, true); break;   // includes the SolveDF constant pass
             case 5: sweeps(c, false); break;
@@ -1099,11 +1125,25 @@ struct FieldRef {
     int width;           // values per element
     bool per_face;
     bool writable;
+    const void* pq = nullptr;  // float-float array (MIXFF form), read back as hi + lo
 };
 
 FieldRef field_ref(cfd_case_s* c, int which) {
     DevArrays& d = c->d;
     bool f = c->fp32();
+    if (c->ffres()) {
+        switch (which) {
+            case CFD_FIELD_GRAD: return {nullptr, nullptr, 8, false, false, d.gradq};
+            case CFD_FIELD_PHI: return {nullptr, nullptr, 4, false, false, d.phiq};
+            case CFD_FIELD_SPEC_C: return {nullptr, nullptr, 1, false, false, d.speccq};
+            case CFD_FIELD_SPEC_V: return {nullptr, nullptr, 1, false, false, d.specvq};
+            case CFD_FIELD_GRADT: return {nullptr, nullptr, 2, false, false, d.gradTq};
+            case CFD_FIELD_MU: return {nullptr, nullptr, 1, false, false, d.muq};
+            case CFD_FIELD_UEDGE: return {nullptr, nullptr, 4, true, false, d.Ueq};
+            case CFD_FIELD_MUEDGE: return {nullptr, nullptr, 1, true, false, d.mueq};
+            default: break;
+        }
+    }
     switch (which) {
         case CFD_FIELD_U: return {d.U, nullptr, 4, false, true};
         case CFD_FIELD_W: return {d.W, nullptr, 4, false, true};
@@ -1180,11 +1220,16 @@ int cfd_get_field(cfd_case_t c, int mesh, int which, double* host) {
         return CFD_OK;
     }
     FieldRef r = field_ref(c, which);
-    if (!r.p64 && !r.p32) return fail(CFD_ERR_ARG, "field not available for this case (flow type, precision or id)");
+    if (!r.p64 && !r.p32 && !r.pq) return fail(CFD_ERR_ARG, "field not available for this case (flow type, precision or id)");
     int off = r.per_face ? c->foff[mesh] : c->coff[mesh];
     int n = r.per_face ? (c->foff[mesh + 1] - off) : (c->coff[mesh + 1] - off);
     size_t cnt = (size_t)n * r.width;
-    if (r.p64) {
+    if (r.pq) {
+        std::vector<float> tmp(2 * cnt);
+        ck(cudaMemcpyAsync(tmp.data(), (const float*)r.pq + 2 * (size_t)off * r.width, cnt * 8, cudaMemcpyDeviceToHost, c->stream), "download");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+        for (size_t i = 0; i < cnt; i++) host[i] = (double)tmp[2 * i] + (double)tmp[2 * i + 1];
+    } else if (r.p64) {
         ck(cudaMemcpyAsync(host, (const double*)r.p64 + (size_t)off * r.width, cnt * 8, cudaMemcpyDeviceToHost, c->stream), "download");
         ck(cudaStreamSynchronize(c->stream), "sync");
     } else {
@@ -1454,7 +1499,7 @@ extern "C" {
 
 int cfd_sst_enable(cfd_case_t c) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
-    if (!c->viscous() || c->fp32())
+    if (!c->viscous() || c->fp32() || c->ffres())
         return fail(CFD_ERR_STATE, "the SST model needs a laminar case with the binary64 residual (FP64 or MIXED)");
     ABI_TRY
     DevArrays& d = c->d;
@@ -1552,12 +1597,16 @@ void ensure_precision_arrays(cfd_case_s* c, int prec) {
         }
         if (!d.Uf) dalloc(&d.Uf, nc);
     }
+    if (prec == CFD_PREC_MIXFF && !d.Uq) {
+        alloc_ff_arrays(d, visc);
+        launch_to_ff(d, L, true);
+    }
     if (prec == CFD_PREC_FP32 && !d.gradf) {
         dalloc(&d.gradf, 2 * nc); dalloc(&d.phif, nc); dalloc(&d.speccf, nc);
         dalloc(&d.Uef, nf); dalloc(&d.fspecf, nf); dalloc(&d.Fcf, nf);
         if (visc) { dalloc(&d.specvf, nc); dalloc(&d.gradTf, nc); dalloc(&d.muf, nc); dalloc(&d.muef, nf); dalloc(&d.Fvf, nf); }
     }
-    if (prec != CFD_PREC_FP32 && !d.grad) {
+    if ((prec == CFD_PREC_FP64 || prec == CFD_PREC_MIXED) && !d.grad) {
         dalloc(&d.grad, 2 * nc); dalloc(&d.phi, nc); dalloc(&d.specc, nc);
         dalloc(&d.Ue, nf); dalloc(&d.fspec, nf); dalloc(&d.Fc, nf);
         if (visc) { dalloc(&d.specv, nc); dalloc(&d.gradT, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf); dalloc(&d.Fv, nf); }
@@ -1573,13 +1622,17 @@ void ensure_precision_arrays(cfd_case_s* c, int prec) {
 
 extern "C" int cfd_set_precision(cfd_case_t c, int precision) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
-    if (precision < CFD_PREC_FP64 || precision > CFD_PREC_MIXED) return fail(CFD_ERR_ARG, "unknown precision");
+    if (precision < CFD_PREC_FP64 || precision > CFD_PREC_MIXFF) return fail(CFD_ERR_ARG, "unknown precision");
     if (precision == c->p.precision) return CFD_OK;
-    if (c->sst && precision == CFD_PREC_FP32) return fail(CFD_ERR_STATE, "the SST model needs the binary64 residual");
+    if (c->sst && (precision == CFD_PREC_FP32 || precision == CFD_PREC_MIXFF))
+        return fail(CFD_ERR_STATE, "the SST model needs the binary64 residual");
+    if (precision == CFD_PREC_MIXFF && c->p.advance == CFD_ADV_LUSGS && (c->p.sweep_mode == 1 || c->p.sweep_mode == 2))
+        return fail(CFD_ERR_STATE, "the MIXFF form runs the binary32 dataflow sweeps (sweep modes 0, 3, 4, 5)");
     ABI_TRY
     ensure_precision_arrays(c, precision);
     c->p.precision = precision;
     c->d.resid32 = precision == CFD_PREC_FP32 ? 1 : 0;
+    c->d.residq = precision == CFD_PREC_MIXFF ? 1 : 0;
     if (c->p.advance == CFD_ADV_LUSGS)
         c->d.flow_grid = sweep_flow_max_grid(precision != CFD_PREC_FP64, c->p.sweep_blocks_per_sm);
     c->drop_graph();

@@ -46,6 +46,7 @@ struct MeshPrm {
     int viscous;
     int pad;
     double sst_k, sst_w, sst_mut;                // SST freestream k, omega, mu_t (nondimensional)
+    float ffk[4];                                // float-float cc and (1+cc)*sqrt(Gamma)*Ma/Re (hi, lo each)
 };
 
 template <class T> struct C {
@@ -68,6 +69,12 @@ __device__ __forceinline__ void st4(d4* p, const d4& v) {
 }
 __device__ __forceinline__ float4 ld4(const float4* p) { return *p; }
 __device__ __forceinline__ void st4(float4* p, const float4& v) { *p = v; }
+
+// Accumulator type of the residual gather and the widening into it: binary64
+// for binary64 and binary32 fluxes (the float-float one is in fv_ff.cuh).
+template <class T> struct Acc { typedef double type; };
+__device__ __forceinline__ double acc_widen(double x) { return x; }
+__device__ __forceinline__ double acc_widen(float x) { return (double)x; }
 
 template <class T, class Q> __device__ __forceinline__ void to_arr(const Q& v, T* a) {
     a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w;
@@ -273,3 +280,5 @@ template <class T> __device__ __forceinline__ void conv_flux_w(const T* w, T nx,
 }
 
 }  // namespace cfdgb
+
+#include "fv_ff.cuh"

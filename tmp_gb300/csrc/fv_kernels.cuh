@@ -292,7 +292,8 @@ __global__ void __launch_bounds__(256) k_cell_update(
     if (c >= nc) return;
     int4 cf = cface[c];
     int codes[4] = {cf.x, cf.y, cf.z, cf.w};
-    double r[4] = {0.0, 0.0, 0.0, 0.0};
+    typedef typename Acc<T>::type A;  // binary64, or float-float for float-float fluxes
+    A ra[4] = {A(0.0), A(0.0), A(0.0), A(0.0)};
 #pragma unroll
     for (int s = 0; s < 4; s++) {
         int code = codes[s];
@@ -301,8 +302,8 @@ __global__ void __launch_bounds__(256) k_cell_update(
         to_arr(ld4(Fc + code_face(code)), fl);
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            if (code > 0) r[j] += (double)fl[j];
-            else r[j] -= (double)fl[j];
+            if (code > 0) ra[j] += acc_widen(fl[j]);
+            else ra[j] -= acc_widen(fl[j]);
         }
     }
     if (VISC) {
@@ -314,11 +315,12 @@ __global__ void __launch_bounds__(256) k_cell_update(
             to_arr(ld4(Fv + code_face(code)), fl);
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                if (code > 0) r[j] -= (double)fl[j];
-                else r[j] += (double)fl[j];
+                if (code > 0) ra[j] -= acc_widen(fl[j]);
+                else ra[j] += acc_widen(fl[j]);
             }
         }
     }
+    const double r[4] = {(double)ra[0], (double)ra[1], (double)ra[2], (double)ra[3]};
     st4(R + c, d4{r[0], r[1], r[2], r[3]});
     if (MODE == UPD_RESID) return;
     double vol = cgeo64[c].x;

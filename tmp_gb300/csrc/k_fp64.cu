@@ -746,12 +746,14 @@ __global__ void __launch_bounds__(256) k_sweep_prep32(int nc, const int4* __rest
     swraf[t] = rA;
 }
 
-void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, bool mu64) {
+void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mu_kind) {
     int n = 4 * d.nc;
     float* a = reinterpret_cast<float*>(d.dW1f);
     float* b = reinterpret_cast<float*>(d.dWf);
-    if (viscous && mu64)
+    if (viscous && mu_kind == MU_F64)
         k_sweep_prep32<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.mu, d.swraf, d.Wf, a, b);
+    else if (viscous && mu_kind == MU_FF)
+        k_sweep_prep32<true, ff><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muq, d.swraf, d.Wf, a, b);
     else if (viscous)
         k_sweep_prep32<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muf, d.swraf, d.Wf, a, b);
     else
@@ -1261,7 +1263,7 @@ void launch_chain_static(const DevArrays& d, const LaunchCfg& L) {
 }
 
 cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool viscous,
-                                 bool mu64) {
+                                 int mu_kind) {
     const int k = forward ? 0 : 1;
     int nh = d.chain_nh;
     float4* pub = forward ? d.dW1f : d.dWf;
@@ -1269,10 +1271,14 @@ cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool fo
         k_chain_cell<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.W, d.U, d.diag, d.Wf, d.Uf, d.invD, d.dW1f,
                                                             d.dWf);
         const int nb = nblk(8 * d.nc, 256);
-        if (viscous && mu64)
+        if (viscous && mu_kind == MU_F64)
             k_chain_prep<true, double><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
                                                                  d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
                                                                  d.mu, d.R, d.invD);
+        else if (viscous && mu_kind == MU_FF)
+            k_chain_prep<true, ff><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
+                                                             d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
+                                                             d.muq, d.R, d.invD);
         else if (viscous)
             k_chain_prep<true, float><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
                                                                 d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
@@ -1378,8 +1384,9 @@ __global__ void k_local_dt(int nc, const d4* __restrict__ cgeo, const T* __restr
     if (c >= nc) return;
     dt[c] = cfl * cgeo[c].x / (double)specc[c];
 }
-void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, bool fp32) {
-    if (fp32) k_local_dt<float><<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.cgeo, d.speccf, cfl, d.dt);
+void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, int form) {
+    if (form == 1) k_local_dt<float><<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.cgeo, d.speccf, cfl, d.dt);
+    else if (form == 2) k_local_dt<ff><<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.cgeo, d.speccq, cfl, d.dt);
     else k_local_dt<double><<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.cgeo, d.specc, cfl, d.dt);
     *L.counter += 1;
 }
@@ -1495,9 +1502,12 @@ __global__ void k_wall_force_final(int nblk_total, const int4* __restrict__ wblo
     out[2 * m + 1] = fy;
 }
 
-void launch_wall_force(const DevArrays& d, const LaunchCfg& L, bool viscous, bool fp32) {
+void launch_wall_force(const DevArrays& d, const LaunchCfg& L, bool viscous, int form) {
     if (d.nwblk > 0) {
-        if (fp32) {
+        if (form == 2) {
+            if (viscous) k_wall_force<ff, true><<<d.nwblk, 256, 0, L.stream>>>(d.wall_ptr, d.wall_faces, d.wblocks, d.Fcq, d.Fvq, d.wpartial);
+            else k_wall_force<ff, false><<<d.nwblk, 256, 0, L.stream>>>(d.wall_ptr, d.wall_faces, d.wblocks, d.Fcq, d.Fvq, d.wpartial);
+        } else if (form == 1) {
             if (viscous) k_wall_force<float, true><<<d.nwblk, 256, 0, L.stream>>>(d.wall_ptr, d.wall_faces, d.wblocks, d.Fcf, d.Fvf, d.wpartial);
             else k_wall_force<float, false><<<d.nwblk, 256, 0, L.stream>>>(d.wall_ptr, d.wall_faces, d.wblocks, d.Fcf, d.Fvf, d.wpartial);
         } else {

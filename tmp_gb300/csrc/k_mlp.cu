@@ -252,11 +252,19 @@ __device__ void cell_features(const DevArrays& d, int c, float* f) {
         ab += a[k] * b[k];
     }
     const double dt = d.dt[c];
-    const bool r32 = d.resid32 != 0;
-    const float sc = r32 ? d.speccf[c] : (float)d.specc[c];
-    const float sv = r32 ? (d.specvf ? d.specvf[c] : 0.f) : (d.specv ? (float)d.specv[c] : 0.f);
-    float phimin;
-    if (r32) {
+    const bool r32 = d.resid32 != 0, rq = d.residq != 0;
+    float sc, sv, phimin;
+    if (rq) {  // float-float residual arrays: their high parts
+        sc = d.speccq[c].hi;
+        sv = d.specvq ? d.specvq[c].hi : 0.f;
+    } else {
+        sc = r32 ? d.speccf[c] : (float)d.specc[c];
+        sv = r32 ? (d.specvf ? d.specvf[c] : 0.f) : (d.specv ? (float)d.specv[c] : 0.f);
+    }
+    if (rq) {
+        const q4 ph = ld4(d.phiq + c);
+        phimin = fminf(fminf(ph.x.hi, ph.y.hi), fminf(ph.z.hi, ph.w.hi));
+    } else if (r32) {
         const float4 ph = d.phif[c];
         phimin = fminf(fminf(ph.x, ph.y), fminf(ph.z, ph.w));
     } else {
