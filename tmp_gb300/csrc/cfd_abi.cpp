@@ -84,6 +84,12 @@ MeshPrm make_prm(const cfd_freestream_t& fs, bool viscous) {
     const double kk = (1.0 + m.cc) * m.sqrt_gamma * m.mach / m.re;
     const ff qc(m.cc), qk(kk);
     m.ffk[0] = qc.hi; m.ffk[1] = qc.lo; m.ffk[2] = qk.hi; m.ffk[3] = qk.lo;
+    const double inf[6] = {m.rho_inf, m.p_inf, m.u_inf, m.v_inf, m.c_inf, m.p_inf / pow(m.rho_inf, Gamma)};
+    for (int k = 0; k < 6; k++) {
+        const ff q(inf[k]);
+        m.fff[2 * k] = q.hi;
+        m.fff[2 * k + 1] = q.lo;
+    }
     return m;
 }
 

@@ -47,6 +47,7 @@ struct MeshPrm {
     int pad;
     double sst_k, sst_w, sst_mut;                // SST freestream k, omega, mu_t (nondimensional)
     float ffk[4];                                // float-float cc and (1+cc)*sqrt(Gamma)*Ma/Re (hi, lo each)
+    float fff[12];                               // float-float rho, p, u, v, c at infinity and p/rho^Gamma there
 };
 
 template <class T> struct C {

@@ -1,8 +1,8 @@
-// Float-float instantiation support for the residual kernels (the mixed-ff
-// form): record types, loads/stores, constants and the two device functions
-// whose generic forms would call pow() — Sutherland's law, whose exponent 1.5
-// is T*sqrt(T) here, and the far-field boundary state, evaluated in binary64
-// on the few boundary faces and rounded back.
+// Float-float instantiation support for the residual kernels (the MIXFF form):
+// record types, loads/stores, constants and the two device functions whose
+// generic forms call pow() — Sutherland's law (T^1.5 = T*sqrt(T)) and the
+// far-field boundary state (rho^1.4 and t^2.5) — written without it, so that
+// no warp of the float-float residual waits on the binary64 pipe.
 #pragma once
 #include "ff_arith.h"
 
@@ -47,15 +47,68 @@ template <> __device__ __forceinline__ ff sutherland<ff>(ff temp, const MeshPrm&
     return k * (temp * ff_sqrt(temp)) / (temp + cc);
 }
 
+// x^0.4 for x > 0: a binary32 seed refined by two Newton steps on y^5 = x^2,
+// y <- (4y + x^2/y^4)/5, each of which squares the seed's relative error.
+__device__ __forceinline__ ff ff_pow04(ff x) {
+    ff y(powf(x.hi, 0.4f), 0.f);
+    const ff x2 = x * x;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const ff y2 = y * y;
+        y = (ff(4) * y + x2 / (y2 * y2)) / ff(5);
+    }
+    return y;
+}
+
+// Face state of a boundary face in pairs: the generic expressions
+// (HandleViscousBoundary / HandleInvicidBoundary, BoundaryStrategy.h:73-335)
+// with the reference's pow() calls rewritten for Gamma = 1.4 — rho^Gamma as
+// rho * rho^0.4 and t^(1/(Gamma-1)) = t^2.5 as t*t*sqrt(t) — and the
+// freestream values and entropy taken as per-mesh pairs.
 template <>
 __device__ __forceinline__ unsigned boundary_state<ff>(int bc, bool viscous, const ff* ul, ff nx, ff ny,
                                                        const MeshPrm& m, ff* ue) {
-    double a[4], e[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) a[j] = (double)ul[j];
-    const unsigned err = boundary_state<double>(bc, viscous, a, (double)nx, (double)ny, m, e);
-#pragma unroll
-    for (int j = 0; j < 4; j++) ue[j] = ff(e[j]);
+    const ff G = ff(C<ff>::gamma), GM1 = ff(C<ff>::gm1);
+    unsigned err = 0;
+    if (bc == BC_WALL) {
+        if (viscous) {
+            ue[0] = ul[0]; ue[1] = ul[1]; ue[2] = ff(0); ue[3] = ff(0);
+        } else {
+            const ff vnl = dot2(ul[2], ul[3], nx, ny);
+            const ff t0 = ul[2] - nx * vnl, t1 = ul[3] - ny * vnl;
+            if (dot2(t0, t1, nx, ny) > ff(1.0e-7)) err |= ERR_WALLTAN;  // the reference's binary64 bound
+            ue[0] = ul[0]; ue[1] = ul[1]; ue[2] = t0; ue[3] = t1;
+        }
+        return err;
+    }
+    const ff rinf(m.fff[0], m.fff[1]), pinf(m.fff[2], m.fff[3]), uinf(m.fff[4], m.fff[5]),
+        vinf(m.fff[6], m.fff[7]), cinf(m.fff[8], m.fff[9]), s_inf(m.fff[10], m.fff[11]);
+    const ff vnl = dot2(ul[2], ul[3], nx, ny);
+    const ff tl0 = ul[2] - nx * vnl, tl1 = ul[3] - ny * vnl;
+    const ff vnr = dot2(uinf, vinf, nx, ny);
+    const ff tr0 = uinf - nx * vnr, tr1 = vinf - ny * vnr;
+    const ff rl = ul[0], pl = ul[1];
+    if (ff_abs(vnr) < cinf) {
+        const ff cl = ff_sqrt(G * pl / rl);
+        const ff vnb = (vnl + vnr + ff(2) * (cl - cinf) / GM1) / ff(2);
+        const ff cb = (vnl - vnr + ff(2) * (cinf + cl) / GM1) * GM1 / ff(4);
+        ff sb, e0, e1;
+        if (vnr >= ff(0)) {
+            sb = pl / (rl * ff_pow04(rl));
+            e0 = tl0 + nx * vnb; e1 = tl1 + ny * vnb;
+        } else {
+            sb = s_inf;
+            e0 = tr0 + nx * vnb; e1 = tr1 + ny * vnb;
+        }
+        const ff t = cb * cb / (G * sb);
+        ue[0] = t * t * ff_sqrt(t);
+        ue[1] = ue[0] * cb * cb / G;
+        ue[2] = e0; ue[3] = e1;
+    } else if (vnr >= ff(0)) {
+        ue[0] = ul[0]; ue[1] = ul[1]; ue[2] = ul[2]; ue[3] = ul[3];
+    } else {
+        ue[0] = rinf; ue[1] = pinf; ue[2] = uinf; ue[3] = vinf;
+    }
     return err;
 }
 
