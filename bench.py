@@ -180,7 +180,7 @@ def traffic_bytes(pass_name: str, precision: str, nc: int, sweep_mode: int = 0):
     scaled by the cell count)."""
     sweep = pass_name in ("sweep_fwd", "sweep_bwd")
     form = "fp32" if precision == "fp32" or (precision in ("mixed", "mixff") and sweep) else "fp64"
-    if sweep and form == "fp32" and sweep_mode == 5:
+    if sweep and form == "fp32" and sweep_mode in (5, 6):
         row = traffic_table().get(f"fp32_chain_{pass_name}")
     elif precision == "mixed" and not sweep and f"fp64c_{pass_name}" in traffic_table():
         # the mixed form's residual passes are the contracted binary64 build

@@ -129,7 +129,14 @@ typedef struct {
                           5 binary32 forms: dataflow over a chain schedule (each
                           warp runs its own list of cells and passes the
                           increment of its previous cell in registers; the
-                          binary64 form runs mode 0). All modes give the same bits */
+                          binary64 form runs mode 0),
+                          6 binary32 forms: the chain schedule with groups of
+                          four consecutive lists in one block (one per SM
+                          sub-partition), a slot whose producer runs in the
+                          same block waiting on a shared-memory table instead
+                          of global memory (without the table when it would
+                          not leave the grid co-resident).
+                          All modes give the same bits */
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
                                 the occupancy limit)                             */
     int sweep_poll_ns; /* dataflow sweep: pause between polls of a neighbour's
@@ -233,8 +240,8 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
  * times `reps` whole LU-SGS steps for each co-resident block count per SM
  * (1, 2, ... up to the occupancy limit), keeps the fastest for the case and
  * reports it; the case's state is restored afterwards.  For the binary32-sweep
- * forms of a case created with sweep_mode 0 or 5 it also picks between those
- * two schedules (cfd_case_sweep reads the choice). */
+ * forms of a case created with sweep_mode 0, 5 or 6 it also picks among those
+ * three schedules (cfd_case_sweep reads the choice). */
 int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_ms);
 /* The case's current LU-SGS schedule: sweep_mode and blocks per SM (after
  * cfd_autotune, the ones it chose). No reference counterpart. */

@@ -29,7 +29,7 @@ def _batch(n=8, seed=77, lo=2_000, hi=12_000):
 
 
 @pytest.mark.parametrize("precision,sweep_mode", [("fp64", 0), ("fp32", 0), ("mixed", 0), ("fp32", 5), ("mixed", 5),
-                                                   ("mixff", 5)])
+                                                   ("mixff", 5), ("fp32", 6), ("mixff", 6)])
 @pytest.mark.parametrize("flow", ["euler", "laminar"])
 def test_uneven_batch_packed_matches_separate(precision, sweep_mode, flow):
     from tmp_gb300 import abi

@@ -98,7 +98,7 @@ def _cylinder():
     return spec.mesh(), dict(mach=spec.mach, aoa_deg=spec.aoa, reynolds=spec.re)
 
 
-@pytest.mark.parametrize("sweep_mode", [0, 5])
+@pytest.mark.parametrize("sweep_mode", [0, 5, 6])
 def test_mixff_long_run_follows_mixed(sweep_mode):
     """600 graph-replayed LU-SGS steps from the freestream on a ~25k-cell
     cylinder mesh: the residual history and the final state of the MIXFF form

@@ -327,10 +327,11 @@ def test_fast_sweep_independent_halves_bitwise(prec):
 @pytest.mark.parametrize("prec", ["FP32", "MIXED"])
 @pytest.mark.parametrize("bpsm", [1, 4])
 def test_fast_sweep_chain_schedule_bitwise(prec, bpsm):
-    """The chain-scheduled binary32 sweep (sweep_mode 5: cells dealt to
+    """The chain-scheduled binary32 sweeps (sweep_mode 5: cells dealt to
     half-warps so that a dependency on the previous cell of the same
-    half-warp is taken from registers) gives the same bits as the default
-    dataflow sweep, on the fixture mesh and on a cylinder mesh of ~25k cells
+    half-warp is taken from registers; sweep_mode 6: the same with a block's
+    lists consecutive and same-block dependencies handed over in shared
+    memory) give the same bits as the default dataflow sweep, on the fixture mesh and on a cylinder mesh of ~25k cells
     whose quad rows form long chains, at two grid sizes (two schedules), both
     through plain steps and through the graph-captured step."""
     from tmp_gb300 import abi, learn
@@ -343,7 +344,7 @@ def test_fast_sweep_chain_schedule_bitwise(prec, bpsm):
     fs_cyl = dict(mach=spec.mach, aoa_deg=spec.aoa, reynolds=spec.re)
     for mesh, fs, init in [(fixture, fs_fix, g["init_U"]), (cyl, fs_cyl, None)]:
         out = []
-        for sm in (0, 5):
+        for sm in (0, 5, 6):
             case = abi.Case([mesh], [fs], abi.FLOW_LAMINAR, abi.ADV_LUSGS, getattr(abi, f"PREC_{prec}"),
                             cfl=c["cfl"], sweep_mode=sm, sweep_blocks_per_sm=bpsm)
             if init is None:
@@ -354,8 +355,9 @@ def test_fast_sweep_chain_schedule_bitwise(prec, bpsm):
             case.step_graph(2)
             case.sync()
             out.append((case.get("U"), case.get("DW1"), case.get("DW")))
-        for a, b in zip(*out):
-            np.testing.assert_array_equal(a, b)
+        for other in out[1:]:
+            for a, b in zip(out[0], other):
+                np.testing.assert_array_equal(a, b)
 
 
 @pytest.mark.parametrize("name", ["mixed_lam_lusgs", "omesh_euler_rk5"])

@@ -132,6 +132,9 @@ struct DevArrays {
     int2* chain_cells[2] = {nullptr, nullptr}; // [nc] (cell, local-dependency bits) at each position
     int2* chain_rec[2] = {nullptr, nullptr};   // [4*nc] (lower/upper neighbour or -1, face code) per slot
     float4* chain_stage[2] = {nullptr, nullptr};  // [16*nc] per-position stage records (k_fp64.cu)
+    int* chain_jenc[2] = {nullptr, nullptr};   // [4*nc] each slot's dependency as the sweep reads it
+    int chain_tbl = 0;            // shared-memory hand-off entries per block (mode 6; 0 = none)
+    int chain_local = 0;          // the schedule keeps a block's lists consecutive (mode 6)
     int* chain_posb = nullptr;    // [nc] position of each cell in the backward schedule
     float4* chain_dF = nullptr;   // [nc] binary32 slot sums of the last chain sweep
     int poll_ns = 0;             // back-off between a dataflow sweep's polls (ns, 0 = spin)
@@ -171,6 +174,7 @@ enum MuKind { MU_F32 = 0, MU_F64 = 1, MU_FF = 2 };
 void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mu_kind);
 cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool independent);
 int sweep_chain_max_grid(int blocks_per_sm);
+bool sweep_chain_fits(int grid, int tbl_bytes);
 cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool forward, int grid, bool viscous, int mu_kind);
 void launch_chain_static(const DevArrays& d, const LaunchCfg& L);
 void launch_cp_ma(const DevArrays& d, const LaunchCfg& L, int begin, int end, double pinf, double uinf, double vinf,

@@ -131,6 +131,8 @@ struct cfd_case_s {
     int mu_kind() const { return fp32() ? MU_F32 : ffres() ? MU_FF : MU_F64; }
     int form() const { return fp32() ? 1 : ffres() ? 2 : 0; }  // residual arrays: binary64 / binary32 / float-float
     bool fast_sweep() const { return p.precision != CFD_PREC_FP64 && p.advance == CFD_ADV_LUSGS; }
+    // the binary32 sweep over a chain schedule: mode 5 (lists spread over blocks) or 6 (block-local lists)
+    bool chain_sweep() const { return fast_sweep() && (p.sweep_mode == 5 || p.sweep_mode == 6); }
     LaunchCfg L() { return LaunchCfg{stream, &launches}; }
     void drop_graph() {
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -152,7 +154,7 @@ void free_case(cfd_case_s* c) {
                     d.fspecf, d.muef, d.Fcf, d.Fvf, d.swfc, d.swra, d.invD, d.cflmul, d.wall_ptr, d.wall_faces, d.wblocks, d.wpartial, d.wforce, d.swraf, d.Wf, d.dW1f, d.dWf, d.fwd_order2, d.bwd_order2, d.fwd_order, d.bwd_order, d.norm_blocks, d.norm_partial,
                     d.norm_out, d.err, d.dWprev, d.omega, d.omega_mean, d.mlp_samples, d.mlp_samp_off, d.sstT, d.sstTf, d.sstG, d.sstF1, d.sstF2,
                     d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD, d.chain_ptr[0], d.chain_ptr[1],
-                    d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_stage[0],
+                    d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_jenc[0], d.chain_jenc[1], d.chain_stage[0],
                     d.chain_stage[1], d.chain_posb, d.chain_dF, d.Uq, d.gradq, d.phiq, d.speccq, d.specvq, d.gradTq,
                     d.muq, d.Ueq, d.fspecq, d.mueq, d.Fcq, d.Fvq, d.fg0q, d.fg1q, d.fvisq, d.cgeoq};
     for (void* q : ptrs)
@@ -206,8 +208,8 @@ void rk_step(cfd_case_s* c) {
 // holds per position and face slot the neighbour the cell waits for (-1:
 // none) and the slot's face code.  nh is a multiple of 8 (warps per block).
 void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, const std::vector<int4>& cface,
-                 const std::vector<int2>& lr, bool fwd, int nh, std::vector<int>& hptr, std::vector<int2>& cells,
-                 std::vector<int2>& rec) {
+                 const std::vector<int2>& lr, bool fwd, int nh, bool local, std::vector<int>& hptr,
+                 std::vector<int2>& cells, std::vector<int2>& rec) {
     const int nc = (int)order.size();
     std::vector<int> level(nc), hw_of(nc, -1), last(nh, -1), cnt(nh + 1, 0);
     std::vector<long long> mark(nh, -1);
@@ -259,13 +261,23 @@ void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, co
             mark[best] = key;
         }
     }
-    // lists are numbered round-robin; spread consecutive numbers over blocks
-    // (warp w of block b runs list b + w * nblocks) so that the few long lists
-    // of a thin mesh region do not share one SM's issue slots
+    // lists are numbered round-robin, so consecutive numbers are usually rows
+    // that feed each other.  Sweep mode 5 spreads consecutive numbers over
+    // blocks (warp w of block b runs list b + w * nblocks) so that the few long
+    // lists of a thin mesh region do not share one SM's issue slots.  Mode 6
+    // (local) puts groups of four consecutive lists on warps 0-3 of one block
+    // (one per SM sub-partition: they do not share issue slots either) and a
+    // second, distant group on warps 4-7, so that three of four hand-offs
+    // between consecutive lists stay inside a block, in shared memory
     const int nblocks = nh / 8;
     for (int c = 0; c < nc; c++) {
         const int q = hw_of[c];
-        hw_of[c] = (q % nblocks) * 8 + q / nblocks;
+        if (local) {
+            const int g = q / 4;
+            hw_of[c] = (g % nblocks) * 8 + (g / nblocks) * 4 + (q & 3);
+        } else {
+            hw_of[c] = (q % nblocks) * 8 + q / nblocks;
+        }
         cnt[hw_of[c] + 1]++;
     }
     for (int h = 0; h < nh; h++) cnt[h + 1] += cnt[h];
@@ -291,6 +303,35 @@ void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, co
     }
 }
 
+// Each slot's dependency as the sweep reads it (k_chain_static stores it in the
+// stage record): -1 none, -2 / -3 the list's previous cell / the one before
+// (kept in registers), -4 - t the block-local hand-off table's entry t (the
+// producer runs in the same block, sweep mode 6 with a table), else the cell id
+// (waited for in global memory).  Table entries are positions relative to the
+// block's first position.
+std::vector<int> encode_chain(const std::vector<int>& hptr, const std::vector<int2>& cells,
+                              const std::vector<int2>& rec, bool table) {
+    const int nc = (int)cells.size(), nh = (int)hptr.size() - 1;
+    std::vector<int> pos(nc), list(nc), jenc(4 * (size_t)nc, -1);
+    for (int h = 0; h < nh; h++)
+        for (int q = hptr[h]; q < hptr[h + 1]; q++) list[q] = h;
+    for (int q = 0; q < nc; q++) pos[cells[q].x] = q;
+    for (int at = 0; at < nc; at++) {
+        const int h = list[at];
+        for (int s = 0; s < 4; s++) {
+            const int j = rec[4 * (size_t)at + s].x;
+            const int lm = (cells[at].y >> (2 * s)) & 3;
+            int e = j;
+            if (j < 0) e = -1;
+            else if (lm == 1) e = -2;
+            else if (lm == 2) e = -3;
+            else if (table && list[pos[j]] / 8 == h / 8) e = -4 - (pos[j] - hptr[8 * (h / 8)]);
+            jenc[4 * (size_t)at + s] = e;
+        }
+    }
+    return jenc;
+}
+
 int chain_grid(cfd_case_s* c) {
     if (!c->chain_cap) c->chain_cap = sweep_chain_max_grid(64);
     return std::min(c->d.flow_grid, c->chain_cap);
@@ -300,8 +341,9 @@ int chain_grid(cfd_case_s* c) {
 // so it must run outside stream capture; a capture that would need it fails.
 void ensure_chain(cfd_case_s* c) {
     DevArrays& d = c->d;
-    const int nh = chain_grid(c) * 8;  // one list per warp
-    if (d.chain_nh == nh) return;
+    const int grid = chain_grid(c), nh = grid * 8;  // one list per warp
+    const bool local = c->p.sweep_mode == 6;
+    if (d.chain_nh == nh && d.chain_local == (int)local) return;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     ck(cudaStreamIsCapturing(c->stream, &cs), "cudaStreamIsCapturing");
     if (cs != cudaStreamCaptureStatusNone)
@@ -313,33 +355,46 @@ void ensure_chain(cfd_case_s* c) {
         for (int k = 0; k < 2; k++) {
             dalloc(&d.chain_cells[k], d.nc);
             dalloc(&d.chain_rec[k], 4 * (size_t)d.nc);
+            dalloc(&d.chain_jenc[k], 4 * (size_t)d.nc);
             dalloc(&d.chain_stage[k], 16 * (size_t)d.nc);
         }
     }
+    std::vector<int> hptr[2];
+    std::vector<int2> cells[2], rec[2];
+    int tbl = 0;  // table entries per block: the largest block range of either direction
     for (int k = 0; k < 2; k++) {
-        std::vector<int> hptr;
-        std::vector<int2> cells, rec;
-        build_chain(c->h_order[k], k == 0 ? d.fwd_ptr : d.bwd_ptr, c->h_cface, c->h_lr, k == 0, nh, hptr, cells, rec);
+        build_chain(c->h_order[k], k == 0 ? d.fwd_ptr : d.bwd_ptr, c->h_cface, c->h_lr, k == 0, nh, local, hptr[k],
+                    cells[k], rec[k]);
+        if (local)
+            for (int b = 0; b < grid; b++) tbl = std::max(tbl, hptr[k][std::min(8 * b + 8, nh)] - hptr[k][8 * b]);
+    }
+    // a table that would keep the grid's blocks from being co-resident is not used
+    if (tbl > 0 && !sweep_chain_fits(grid, tbl * (int)sizeof(float4))) tbl = 0;
+    for (int k = 0; k < 2; k++) {
+        const std::vector<int> jenc = encode_chain(hptr[k], cells[k], rec[k], tbl > 0);
         if (d.chain_ptr[k]) cudaFree(d.chain_ptr[k]);
         d.chain_ptr[k] = nullptr;
         dalloc(&d.chain_ptr[k], nh + 1);
-        ck(cudaMemcpyAsync(d.chain_ptr[k], hptr.data(), hptr.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
-           "upload");
-        ck(cudaMemcpyAsync(d.chain_cells[k], cells.data(), cells.size() * sizeof(int2), cudaMemcpyHostToDevice,
+        ck(cudaMemcpyAsync(d.chain_ptr[k], hptr[k].data(), hptr[k].size() * sizeof(int), cudaMemcpyHostToDevice,
                            c->stream), "upload");
-        ck(cudaMemcpyAsync(d.chain_rec[k], rec.data(), rec.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream),
-           "upload");
-        if (k == 1) {
-            std::vector<int> posb(d.nc);
-            for (int q = 0; q < d.nc; q++) posb[cells[q].x] = q;
-            ck(cudaMemcpyAsync(d.chain_posb, posb.data(), posb.size() * sizeof(int), cudaMemcpyHostToDevice,
-                               c->stream), "upload");
-            launch_chain_static(d, c->L());
-            ck(cudaGetLastError(), "k_chain_static");
-        }
-        ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+        ck(cudaMemcpyAsync(d.chain_cells[k], cells[k].data(), cells[k].size() * sizeof(int2), cudaMemcpyHostToDevice,
+                           c->stream), "upload");
+        ck(cudaMemcpyAsync(d.chain_rec[k], rec[k].data(), rec[k].size() * sizeof(int2), cudaMemcpyHostToDevice,
+                           c->stream), "upload");
+        ck(cudaMemcpyAsync(d.chain_jenc[k], jenc.data(), jenc.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           c->stream), "upload");
+        ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");  // the host vectors go out of scope
     }
+    std::vector<int> posb(d.nc);
+    for (int q = 0; q < d.nc; q++) posb[cells[1][q].x] = q;
+    ck(cudaMemcpyAsync(d.chain_posb, posb.data(), posb.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+       "upload");
+    launch_chain_static(d, c->L());
+    ck(cudaGetLastError(), "k_chain_static");
+    ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
     d.chain_nh = nh;
+    d.chain_local = local ? 1 : 0;
+    d.chain_tbl = tbl;
 }
 
 // Forward or backward sweep over all levels.  sweep_mode 1 keeps one thread per
@@ -362,7 +417,7 @@ void sweeps(cfd_case_s* c, bool forward) {
         return;
     }
     // default: one dataflow launch per direction (binary64 form, mode 3: two cells per warp)
-    if (c->fast_sweep() && c->p.sweep_mode == 5) {  // the staging pass replaces 1/D and the sweep constants
+    if (c->chain_sweep()) {  // the staging pass replaces 1/D and the sweep constants
         ensure_chain(c);
         ck(launch_sweep_chain32(d, L, forward, chain_grid(c), c->viscous(), c->mu_kind()), "cooperative sweep launch");
     } else if (c->fast_sweep()) {
@@ -511,9 +566,9 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
     if (P.flow != CFD_FLOW_EULER && P.flow != CFD_FLOW_LAMINAR) return fail(CFD_ERR_ARG, "Undefined Flow Type");
     if (P.advance != CFD_ADV_RK5 && P.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_ARG, "Undefined Advance Type");
     if (P.precision < CFD_PREC_FP64 || P.precision > CFD_PREC_MIXFF) return fail(CFD_ERR_ARG, "unknown precision");
-    if (P.sweep_mode < 0 || P.sweep_mode > 5) return fail(CFD_ERR_ARG, "unknown sweep mode");
+    if (P.sweep_mode < 0 || P.sweep_mode > 6) return fail(CFD_ERR_ARG, "unknown sweep mode");
     if (P.precision == CFD_PREC_MIXFF && P.advance == CFD_ADV_LUSGS && (P.sweep_mode == 1 || P.sweep_mode == 2))
-        return fail(CFD_ERR_ARG, "the MIXFF form runs the binary32 dataflow sweeps (sweep modes 0, 3, 4, 5)");
+        return fail(CFD_ERR_ARG, "the MIXFF form runs the binary32 dataflow sweeps (sweep modes 0, 3, 4, 5, 6)");
     for (int i = 0; i < nmesh; i++)
         if (!(fs[i].density > 0) || !(fs[i].pressure > 0) || !(fs[i].mach > 0))
             return fail(CFD_ERR_ARG, "freestream density, pressure and Mach must be positive");
@@ -826,7 +881,7 @@ int cfd_step_graph(cfd_case_t c, int nsteps) {
     if (!c || nsteps < 0) return fail(CFD_ERR_ARG, "null case or negative step count");
     ABI_TRY
     if (!c->gexec) {
-        if (c->fast_sweep() && c->p.sweep_mode == 5) ensure_chain(c);
+        if (c->chain_sweep()) ensure_chain(c);
         ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
         long long before = c->launches;
         one_step(c);
@@ -1090,7 +1145,7 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
     ck(cudaEventCreate(&e1), "cudaEventCreate");
     double total = 0;
     bool visc = c->viscous(), f32 = c->fp32();
-    if (c->fast_sweep() && c->p.sweep_mode == 5) ensure_chain(c);  // host work, outside the timed region
+    if (c->chain_sweep()) ensure_chain(c);  // host work, outside the timed region
     for (int r = 0; r < reps; r++) {
         // a lone backward sweep needs the "not yet computed" markers the forward pass sets
         if (pass == 5 && (c->p.sweep_mode == 0 || c->p.sweep_mode >= 3)) {
@@ -1633,7 +1688,7 @@ extern "C" int cfd_set_precision(cfd_case_t c, int precision) {
     if (c->sst && (precision == CFD_PREC_FP32 || precision == CFD_PREC_MIXFF))
         return fail(CFD_ERR_STATE, "the SST model needs the binary64 residual");
     if (precision == CFD_PREC_MIXFF && c->p.advance == CFD_ADV_LUSGS && (c->p.sweep_mode == 1 || c->p.sweep_mode == 2))
-        return fail(CFD_ERR_STATE, "the MIXFF form runs the binary32 dataflow sweeps (sweep modes 0, 3, 4, 5)");
+        return fail(CFD_ERR_STATE, "the MIXFF form runs the binary32 dataflow sweeps (sweep modes 0, 3, 4, 5, 6)");
     ABI_TRY
     ensure_precision_arrays(c, precision);
     c->p.precision = precision;
@@ -1681,10 +1736,11 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
     const bool low = c->p.precision != CFD_PREC_FP64;
     const int max_grid = sweep_flow_max_grid(low, 64);  // occupancy limit
     // the binary32 forms also choose between the round-robin dataflow sweep
-    // (mode 0: wide levels, many cells in flight) and the chain schedule
-    // (mode 5: narrow levels, long dependence chains)
+    // (mode 0: wide levels, many cells in flight) and the chain schedules
+    // (narrow levels, long dependence chains; mode 5 spreads a block's lists,
+    // mode 6 keeps neighbouring lists in one block with a shared-memory hand-off)
     std::vector<int> modes{c->p.sweep_mode};
-    if (c->fast_sweep() && (c->p.sweep_mode == 0 || c->p.sweep_mode == 5)) modes = {0, 5};
+    if (c->fast_sweep() && (c->p.sweep_mode == 0 || c->p.sweep_mode == 5 || c->p.sweep_mode == 6)) modes = {0, 5, 6};
     const int mode0 = c->p.sweep_mode;
     int best = 0, best_mode = mode0;
     double best_t = 1e300;
@@ -1696,7 +1752,7 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
             const int grid = sweep_flow_max_grid(low, bpsm);
             if (grid > max_grid) break;
             d.flow_grid = grid;
-            const int eff = mode == 5 && c->fast_sweep() ? chain_grid(c) : grid;
+            const int eff = c->chain_sweep() ? chain_grid(c) : grid;
             if (eff == last_grid) break;  // capped by occupancy: nothing new to try
             last_grid = eff;
             c->drop_graph();

@@ -987,9 +987,14 @@ __device__ __forceinline__ void cp_async_wait() {
 template <bool FWD>
 __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __restrict__ hptr,
                                                        const float4* __restrict__ stage, float4* pub,
-                                                       float4* __restrict__ dFout, unsigned* err, int poll_ns) {
+                                                       float4* __restrict__ dFout, unsigned* err, int poll_ns,
+                                                       int tbl_n) {
     __shared__ __align__(16) float4 ring[kChainWarps][kChainDepth][kStageW];
     __shared__ __align__(16) float4 spec[kChainWarps][kChainDepth][4];
+    // block-local hand-off table (sweep mode 6): the increment of every cell
+    // of this block's lists, by position within the block's range; a slot
+    // whose producer runs in this block waits here instead of in global memory
+    extern __shared__ __align__(16) float4 tbl[];
     const float GM1 = 1.4f - 1.0f;
     const int lane = threadIdx.x & 31;
     const int s = (lane >> 2) & 3, m = lane & 3;
@@ -998,6 +1003,9 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_SCHED);
         return;
     }
+    const float sent = __uint_as_float(kSentinelF);
+    for (int t = threadIdx.x; t < tbl_n; t += blockDim.x) tbl[t] = make_float4(sent, sent, sent, sent);
+    __syncthreads();
     if (lane >= 16) return;
     const int warp = threadIdx.x >> 5;
     const int hw = blockIdx.x * (blockDim.x >> 5) + warp;
@@ -1017,7 +1025,7 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         cp_async_commit();
     }
     float4 hd1 = make_float4(0.f, 0.f, 0.f, 0.f), hd2 = hd1;  // increments of the last two cells
-    const float sent = __uint_as_float(kSentinelF);
+    const int b0 = hptr[blockIdx.x * kChainWarps];  // first position of this block's lists
     bool gave_up = false;
     for (int k = 0; k < n; k++) {
         const int slot = k & (kChainDepth - 1);
@@ -1059,6 +1067,19 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
                 dw = hd1;
             } else if (j == -3) {
                 dw = hd2;
+            } else if (j <= -4) {  // produced in this block: wait on the shared-memory table
+                const volatile float* q = reinterpret_cast<const volatile float*>(tbl + (-4 - j));
+                dw = make_float4(q[0], q[1], q[2], q[3]);
+                long long it = 0;
+                while (is_sentinel_f(dw.x) || is_sentinel_f(dw.y) || is_sentinel_f(dw.z) || is_sentinel_f(dw.w)) {
+                    if (gave_up) break;
+                    if (++it > kSpinLimit) {
+                        atomicOr(err, ERR_TIMEOUT);
+                        gave_up = true;
+                        break;
+                    }
+                    dw = make_float4(q[0], q[1], q[2], q[3]);
+                }
             } else {
                 dw = early;
                 const float4* qf = pub + j;
@@ -1105,7 +1126,13 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         const float r1 = __shfl_sync(mask, resf, 1);
         const float r2 = __shfl_sync(mask, resf, 2);
         const float r3 = __shfl_sync(mask, resf, 3);
-        if (lane == 0) __stcg(pub + i, make_float4(r0, r1, r2, r3));
+        if (lane == 0) {
+            __stcg(pub + i, make_float4(r0, r1, r2, r3));
+            if (tbl_n) {
+                volatile float* q = reinterpret_cast<volatile float*>(tbl + (p0 + k - b0));
+                q[0] = r0; q[1] = r1; q[2] = r2; q[3] = r3;
+            }
+        }
         if (s == 0) (&dFout[i].x)[m] = dF;
         hd2 = hd1;
         hd1 = make_float4(r0, r1, r2, r3);
@@ -1116,7 +1143,8 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
 // Static part of the stage records, once per schedule: cell ids, neighbour /
 // face-code pairs and binary32 face geometry.
 __global__ void k_chain_static(int nc, const int2* __restrict__ cells, const int2* __restrict__ rec,
-                               const float4* __restrict__ fg0f, float4* __restrict__ stage) {
+                               const int* __restrict__ jenc, const float4* __restrict__ fg0f,
+                               float4* __restrict__ stage) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 4LL * nc) return;
     const int p = (int)(t >> 2), s = (int)(t & 3);
@@ -1126,9 +1154,10 @@ __global__ void k_chain_static(int nc, const int2* __restrict__ cells, const int
     if (r.x >= 0) g = fg0f[code_face(r.y)];
     st[8 + s] = make_float4(g.x, g.y, g.z, 0.f);
     const int2 cl = cells[p];
-    const int lm = (cl.y >> (2 * s)) & 3;
-    const int jenc = lm == 1 ? -2 : lm == 2 ? -3 : r.x;  // -2 / -3: the list's previous cell / the one before
-    reinterpret_cast<float2*>(st + 14 + (s >> 1))[s & 1] = make_float2(__int_as_float(jenc), __int_as_float(r.y));
+    // -1 none, -2 / -3 the list's previous cell / the one before (registers),
+    // <= -4 a cell of the same block (shared-memory table index -4 - j), else the cell id
+    const int j = jenc[t];
+    reinterpret_cast<float2*>(st + 14 + (s >> 1))[s & 1] = make_float2(__int_as_float(j), __int_as_float(r.y));
     if (s == 0) {
         int exm = 0;
         for (int k = 0; k < 4; k++) exm |= (rec[4 * (long long)p + k].y != 0) << k;
@@ -1243,6 +1272,27 @@ __global__ void k_chain_finish(int nc, const d4* __restrict__ dW1, const double*
     dW[c] = o;
 }
 
+// Whether `grid` blocks of the chain sweep, each with `tbl_bytes` of dynamic
+// shared memory, are co-resident (a cooperative launch needs all of them).
+bool sweep_chain_fits(int grid, int tbl_bytes) {
+    int dev = 0, sms = 0, per = 0, per2 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (tbl_bytes > 48 * 1024) {
+        if (cudaFuncSetAttribute((void*)k_sweep_chain32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tbl_bytes) ||
+            cudaFuncSetAttribute((void*)k_sweep_chain32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tbl_bytes)) {
+            cudaGetLastError();
+            return false;
+        }
+    }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (void*)k_sweep_chain32<true>, 256, tbl_bytes) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_chain32<false>, 256, tbl_bytes)) {
+        cudaGetLastError();
+        return false;
+    }
+    return (long long)sms * (per < per2 ? per : per2) >= grid;
+}
+
 int sweep_chain_max_grid(int blocks_per_sm) {
     int dev = 0, sms = 0, per = 0, per2 = 0;
     cudaGetDevice(&dev);
@@ -1257,8 +1307,8 @@ int sweep_chain_max_grid(int blocks_per_sm) {
 
 void launch_chain_static(const DevArrays& d, const LaunchCfg& L) {
     for (int k = 0; k < 2; k++)
-        k_chain_static<<<nblk(4 * d.nc, 256), 256, 0, L.stream>>>(d.nc, d.chain_cells[k], d.chain_rec[k], d.fg0f,
-                                                                  d.chain_stage[k]);
+        k_chain_static<<<nblk(4 * d.nc, 256), 256, 0, L.stream>>>(d.nc, d.chain_cells[k], d.chain_rec[k],
+                                                                  d.chain_jenc[k], d.fg0f, d.chain_stage[k]);
     *L.counter += 2;
 }
 
@@ -1289,10 +1339,12 @@ cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool fo
                                                                  (const float*)nullptr, d.R, d.invD);
         *L.counter += 2;
     }
+    int tbl_n = d.chain_tbl;
     void* args[] = {(void*)&nh, (void*)&d.chain_ptr[k], (void*)&d.chain_stage[k], (void*)&pub, (void*)&d.chain_dF,
-                    (void*)&d.err, (void*)&d.poll_ns};
+                    (void*)&d.err, (void*)&d.poll_ns, (void*)&tbl_n};
     void* fn = forward ? (void*)k_sweep_chain32<true> : (void*)k_sweep_chain32<false>;
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, (size_t)tbl_n * sizeof(float4),
+                                                L.stream);
     *L.counter += 1;
     if (e != cudaSuccess) return e;
     if (forward)
