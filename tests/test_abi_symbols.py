@@ -31,3 +31,29 @@ def test_version_and_error_text(built_lib):
     assert L.cfd_version() >= 10000
     assert L.cfd_mesh_info(None, None, None, None) == -1
     assert b"null" in L.cfd_last_error()
+
+
+def _defines():
+    out = {}
+    for h in (ROOT / "include").glob("*.h"):
+        for name, val in re.findall(r"^#define\s+(CFD_\w+)\s+(-?\d+)\b", h.read_text(), flags=re.M):
+            out[name] = int(val)
+    return out
+
+
+def test_header_constants_match_bindings():
+    """The enum values the Python bindings pass across the C ABI are the
+    header's (flow, integrator, precision forms, fields, norms, layouts)."""
+    from tmp_gb300 import abi
+
+    d = _defines()
+    pairs = {"CFD_FLOW_EULER": abi.FLOW_EULER, "CFD_FLOW_LAMINAR": abi.FLOW_LAMINAR,
+             "CFD_ADV_RK5": abi.ADV_RK5, "CFD_ADV_LUSGS": abi.ADV_LUSGS,
+             "CFD_PREC_FP64": abi.PREC_FP64, "CFD_PREC_FP32": abi.PREC_FP32,
+             "CFD_PREC_MIXED": abi.PREC_MIXED, "CFD_PREC_MIXFF": abi.PREC_MIXFF}
+    pairs.update({f"CFD_FIELD_{k}": v for k, v in abi.FIELD.items()})
+    pairs.update({f"CFD_NORM_{k}": v for k, v in abi.NORM.items()})
+    missing = [k for k in pairs if k not in d]
+    assert not missing, missing
+    wrong = {k: (d[k], v) for k, v in pairs.items() if d[k] != v}
+    assert not wrong, wrong
