@@ -613,7 +613,20 @@ def run_ours(args):
                                   switch_to=prec_code[then] if then else None, detach_at_switch=until_switch)
             drop[f] = {"reached": r.reached, "seconds": round(r.seconds, 3), "iterations": r.iterations,
                        "fall": r.history[-1][1], "fell_back": r.fell_back}
+            try:  # lift and drag of the state reached (wall force in the form's own arithmetic)
+                wf = c2.wall_force()
+                drop[f]["cl"], drop[f]["cd"] = wf["cl"], wf["cd"]
+            except abi.CfdError:
+                pass
             c2.close()
+        ref = drop.get("fp64")
+        if isinstance(ref, dict) and "cd" in ref:
+            # each form's lift and drag at its final state against the plain binary64 run's (CL is
+            # compared absolutely: it is near zero on a symmetric body)
+            drop["vs_fp64"] = {f: {"cl_abs_diff": abs(v["cl"] - ref["cl"]),
+                                   "cd_rel_diff": abs(v["cd"] - ref["cd"]) / max(abs(ref["cd"]), 1e-300),
+                                   "fall_ratio": v["fall"] / ref["fall"]}
+                               for f, v in drop.items() if isinstance(v, dict) and "cd" in v and f != "fp64"}
 
     # per-pass device times for the roofline (L2 flushed before each rep)
     passes = ["face_state", "cell_grad", "face_flux", "cell_update"]
