@@ -243,6 +243,19 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
  * forms of a case created with sweep_mode 0, 5 or 6 it also picks among those
  * three schedules (cfd_case_sweep reads the choice). */
 int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_ms);
+/* Host-side chain schedule of the binary32 LU-SGS sweep (sweep modes 5 and 6)
+ * for one mesh, as a case holding that mesh builds it (no reference
+ * counterpart; needs no GPU).  forward: 1 forward sweep, 0 backward; nlists:
+ * warps of the launch (a multiple of 8); local: mode 6's block-local list
+ * numbering; table: encode same-block dependencies as shared-memory table
+ * entries.  Outputs: hptr[nlists+1] each list's range of positions;
+ * cells[2*ncell] per position (cell, bits 2s..2s+1 = 1/2 when slot s waits
+ * for the list's previous cell / the one before); rec[8*ncell] per position
+ * and face slot (neighbour waited for or -1, signed face code); jenc[4*ncell]
+ * the dependency as the sweep reads it (-1 none, -2/-3 registers, -4-t table
+ * entry t, else the cell id); *table_entries the table's entries per block. */
+int cfd_chain_schedule(cfd_mesh_t mesh, int forward, int nlists, int local, int table, int* hptr,
+                       int* cells, int* rec, int* jenc, int* table_entries);
 /* The case's current LU-SGS schedule: sweep_mode and blocks per SM (after
  * cfd_autotune, the ones it chose). No reference counterpart. */
 int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm);

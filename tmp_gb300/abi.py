@@ -141,6 +141,7 @@ def lib() -> C.CDLL:
         "cfd_set_precision": (C.c_int, [vp, C.c_int]),
         "cfd_autotune": (C.c_int, [vp, C.c_int, ip, dp]),
         "cfd_case_sweep": (C.c_int, [vp, ip, ip]),
+        "cfd_chain_schedule": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, ip, ip, ip, ip, ip]),
         "cfd_sst_enable": (C.c_int, [vp]),
         "cfd_sst_freestream": (C.c_int, [vp, C.c_int, dp]),
         "cfd_sst_residual": (C.c_int, [vp]),
@@ -206,6 +207,21 @@ class Mesh:
         a, b = C.c_int(), C.c_int()
         check(lib().cfd_mesh_levels(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def chain_schedule(self, forward: bool, nlists: int, local: bool = False, table: bool = False) -> dict:
+        """The binary32 sweep's chain schedule of this mesh (host only): per-list
+        position ranges, (cell, register bits) per position, (neighbour, face
+        code) per slot, each slot's dependency encoding and the table size."""
+        nc = self.ncell
+        hptr = np.empty(nlists + 1, np.int32)
+        cells = np.empty(2 * nc, np.int32)
+        rec = np.empty(8 * nc, np.int32)
+        jenc = np.empty(4 * nc, np.int32)
+        tbl = C.c_int()
+        check(lib().cfd_chain_schedule(self.h, int(bool(forward)), int(nlists), int(bool(local)), int(bool(table)),
+                                       _iptr(hptr), _iptr(cells), _iptr(rec), _iptr(jenc), C.byref(tbl)))
+        return dict(hptr=hptr, cells=cells.reshape(-1, 2), rec=rec.reshape(-1, 4, 2), jenc=jenc.reshape(-1, 4),
+                    table_entries=tbl.value)
 
     def __del__(self):
         if getattr(self, "h", None) is not None and self.h.value and _lib is not None:

@@ -1706,6 +1706,61 @@ extern "C" int cfd_set_precision(cfd_case_t c, int precision) {
 // Autotuning the dataflow sweeps' launch shape
 // ---------------------------------------------------------------------------
 
+// Host-side chain schedule of one mesh, as ensure_chain builds it for a case
+// holding that mesh alone (no GPU involved).
+extern "C" int cfd_chain_schedule(cfd_mesh_t mesh, int forward, int nlists, int local, int table, int* hptr,
+                                  int* cells, int* rec, int* jenc, int* table_entries) {
+    if (!mesh || !hptr || !cells || !rec || !jenc || !table_entries) return fail(CFD_ERR_ARG, "null argument");
+    if (nlists <= 0 || nlists % 8) return fail(CFD_ERR_ARG, "nlists must be a positive multiple of 8");
+    try {
+        const HostMesh& m = mesh->m;
+        const int nc = m.ncell;
+        const bool fwd = forward != 0;
+        const std::vector<int>& lev = fwd ? m.lev_fwd : m.lev_bwd;
+        const int nlev = fwd ? m.n_lev_fwd : m.n_lev_bwd;
+        std::vector<int> lptr(nlev + 1, 0), order(nc);
+        for (int k = 0; k < nc; k++) lptr[lev[k] + 1]++;
+        for (int k = 0; k < nlev; k++) lptr[k + 1] += lptr[k];
+        std::vector<int> at(lptr.begin(), lptr.end() - 1);
+        if (fwd)
+            for (int k = 0; k < nc; k++) order[at[lev[k]]++] = k;
+        else
+            for (int k = nc - 1; k >= 0; k--) order[at[lev[k]]++] = k;
+        std::vector<int2> lr(m.nedge);
+        for (int k = 0; k < m.nedge; k++) lr[k] = make_int2(m.lr[2 * k], m.lr[2 * k + 1]);
+        std::vector<int4> cface(nc);
+        for (int k = 0; k < nc; k++) {
+            int code[4] = {0, 0, 0, 0};
+            for (int s = 0; s < m.cell_nedge[k]; s++) {
+                const int e = m.cell_edges[4 * k + s];
+                code[s] = (m.lr[2 * e] == k) ? (e + 1) : -(e + 1);
+            }
+            cface[k] = make_int4(code[0], code[1], code[2], code[3]);
+        }
+        std::vector<int> hp;
+        std::vector<int2> cl, rc;
+        build_chain(order, lptr, cface, lr, fwd, nlists, local != 0, hp, cl, rc);
+        int tbl = 0;
+        if (local && table)
+            for (int b = 0; b < nlists / 8; b++) tbl = std::max(tbl, hp[8 * b + 8] - hp[8 * b]);
+        const std::vector<int> je = encode_chain(hp, cl, rc, tbl > 0);
+        for (int h = 0; h <= nlists; h++) hptr[h] = hp[h];
+        for (int q = 0; q < nc; q++) {
+            cells[2 * q] = cl[q].x;
+            cells[2 * q + 1] = cl[q].y;
+        }
+        for (size_t q = 0; q < rc.size(); q++) {
+            rec[2 * q] = rc[q].x;
+            rec[2 * q + 1] = rc[q].y;
+        }
+        for (size_t q = 0; q < je.size(); q++) jenc[q] = je[q];
+        *table_entries = tbl;
+        return CFD_OK;
+    } catch (const std::exception& ex) {
+        return fail(CFD_ERR_MESH, ex.what());
+    }
+}
+
 extern "C" int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
     if (sweep_mode) *sweep_mode = c->p.sweep_mode;
