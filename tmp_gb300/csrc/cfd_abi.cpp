@@ -1673,7 +1673,7 @@ void ensure_precision_arrays(cfd_case_s* c, int prec) {
         if (visc) { dalloc(&d.specv, nc); dalloc(&d.gradT, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf); dalloc(&d.Fv, nf); }
     }
     if (c->p.advance == CFD_ADV_LUSGS && prec != CFD_PREC_FP64 && !d.swraf)
-        throw std::runtime_error("the binary32 sweep needs a case created in the FP32 or MIXED form");
+        throw std::runtime_error("the binary32 sweep needs a case created in the FP32, MIXED or MIXFF form");
     if (new_geo32) launch_to_fp32(d, L, true);
     else if (prec != CFD_PREC_FP64) launch_to_fp32(d, L, false);  // binary32 copy of the current state
     ck(cudaGetLastError(), "launch");
