@@ -38,7 +38,8 @@ template <> struct C<ff> {
 
 __device__ __forceinline__ ff dsqrt(ff x) { return ff_sqrt(x); }
 __device__ __forceinline__ ff dabs(ff x) { return ff_abs(x); }
-__device__ __forceinline__ ff dpow(ff x, ff y) { return ff(pow((double)x, (double)y)); }
+// (no dpow for pairs: the two generic functions that call pow() are specialised
+// below, so a new use fails to compile instead of reaching the binary64 pipe)
 
 // mu = (1+cc)/(T+cc) * T^1.5 * sqrt(Gamma) * Ma / Re as K * T*sqrt(T) / (T+cc),
 // with K = (1+cc)*sqrt(Gamma)*Ma/Re and cc held per mesh as pairs (ffk).
