@@ -448,7 +448,7 @@ def run_reference(args):
     path = str(configs.grd_path(w))
     ncores = os.cpu_count() or 1
     steps = max(1, min(args.steps, 10))
-    warm = min(args.warmup, 1)
+    warm = max(3, min(args.warmup, 5))  # at least three untimed steps per copy (each ~0.1 s)
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(ncores) as pool:
