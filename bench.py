@@ -71,10 +71,11 @@ def parse():
     ap.add_argument("--sweep-bpsm", type=int, default=0, help="dataflow sweep blocks per SM (0 = autotune)")
     ap.add_argument("--sweep-poll-ns", type=int, default=0, help="dataflow sweep back-off between polls (ns)")
     ap.add_argument("--forms", default="fp64,fp32,mixed", help="precision forms timed besides --precision ('' = none)")
-    ap.add_argument("--drop", type=float, default=1e-3, help="residual fall for time_to_drop (0 = skip)")
-    ap.add_argument("--drop-seconds", type=float, default=40.0, help="cap per form for time_to_drop")
-    ap.add_argument("--drop-forms", default="fp64,fp32,mixed,mixff,mixed+learned,fp32+learned>mixed,fp32+learned>mixff",
-                    help="forms for time_to_drop: PREC[>PREC2][+learned]; '>' switches at --switch-at")
+    ap.add_argument("--drop", type=float, default=1e-8, help="residual fall for time_to_drop (0 = skip)")
+    ap.add_argument("--drop-seconds", type=float, default=200.0, help="cap per form for time_to_drop")
+    ap.add_argument("--drop-forms", default="fp64,mixff,fp32+learned>mixff",
+                    help="forms for time_to_drop: PREC[>PREC2][+learned]; '>' switches at --switch-at "
+                         "(others: fp32, mixed, mixed+learned, fp32+learned>mixed)")
     ap.add_argument("--switch-at", type=float, default=3e-4,
                     help="residual fall at which 'A>B' switches form (or earlier, once A's residual stalls)")
     ap.add_argument("--no-overset", action="store_true", help="skip the overset connectivity / exchange leg")
@@ -413,7 +414,7 @@ def cpu_baseline(grd_path: str, w, seconds: float) -> dict:
 
 
 def _ref_worker(args):
-    grd_path, cfg_name, steps, warmup = args
+    grd_path, cfg_name, steps, warmup, barrier = args
     sys.path.insert(0, str(ROOT))
     from tmp_gb300 import configs
     import oracle
@@ -425,6 +426,7 @@ def _ref_worker(args):
     step = (lambda: o.lusgs_step(w.cfl)) if w.advance == "lusgs" else (lambda: o.rk_step())
     for _ in range(warmup):
         step()
+    barrier.wait()  # every copy times the same contended window of the host's memory system
     t0 = time.perf_counter()
     for _ in range(steps):
         step()
@@ -447,12 +449,13 @@ def run_reference(args):
     w = configs.WORKLOADS[args.config]()
     path = str(configs.grd_path(w))
     ncores = os.cpu_count() or 1
-    steps = max(1, min(args.steps, 10))
-    warm = max(3, min(args.warmup, 5))  # at least three untimed steps per copy (each ~0.1 s)
+    steps = max(1, args.steps)  # the same timed steps as the GPU arm
+    warm = max(3, args.warmup)  # at least three untimed steps per copy
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
-    with ctx.Pool(ncores) as pool:
-        res = pool.map(_ref_worker, [(path, args.config, steps, warm)] * ncores)
+    with ctx.Manager() as mgr, ctx.Pool(ncores) as pool:
+        barrier = mgr.Barrier(ncores)
+        res = pool.map(_ref_worker, [(path, args.config, steps, warm, barrier)] * ncores, chunksize=1)
     wall = time.perf_counter() - t0
     cells = sum(r[0] for r in res)
     slowest = max(r[1] for r in res)
@@ -556,23 +559,25 @@ def run_ours(args):
     t_max, value = replicas.job_rate(nc * args.steps, t_local, world, dist, device="cuda")
     case.sync()
 
-    # end to end through the C ABI: pinned host field in, norm out, per step
-    e2e = None
-    if not args.no_e2e:
+    # end to end through the C ABI: the step's field in from pinned host memory, one step, its residual norm
+    # and the updated field back to pinned host memory (one call, one synchronisation)
+    def e2e_of(c):
         host = torch.from_numpy(U0.reshape(-1)).pin_memory()
         hv = host.numpy()
-        nrm = torch.zeros(case.nmesh, dtype=torch.float64).pin_memory().numpy()
-        case.step_io(hv, 1, "DW_RHO2", nrm)
+        back = torch.zeros(4 * nc, dtype=torch.float64).pin_memory().numpy()
+        nrm = torch.zeros(c.nmesh, dtype=torch.float64).pin_memory().numpy()
+        c.step_io(hv, 1, "DW_RHO2", nrm, u_out=back)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            # the step's field in from pinned host memory, one step, its residual norm back (one call, one sync)
-            case.step_io(hv, 1, "DW_RHO2", nrm)
+            c.step_io(hv, 1, "DW_RHO2", nrm, u_out=back)
         el = time.perf_counter() - t0
-        e2e = {"value": replicas.job_rate(nc * args.steps, el, world, dist, device="cuda")[1], "unit": UNIT,
-               "h2d_bytes_per_step": nc * 32, "d2h_bytes_per_step": 8}
+        return {"value": replicas.job_rate(nc * args.steps, el, world, dist, device="cuda")[1], "unit": UNIT,
+                "h2d_bytes_per_step": hv.nbytes, "d2h_bytes_per_step": back.nbytes + nrm.nbytes}
+
+    e2e = None if args.no_e2e else e2e_of(case)
 
     # the other precision forms, timed the same way
     forms = {}
@@ -581,9 +586,13 @@ def run_ours(args):
         fm, _ = timed_steps(c2, args.steps)
         forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3),
                     "sweep": dict(zip(("mode", "blocks_per_sm"), c2.sweep_config()))}
+        if f == "fp64" and not args.no_e2e:
+            forms[f]["e2e"] = e2e_of(c2)
         c2.close()
     forms[args.precision] = {"ms_per_step": 1e3 * t_local / args.steps, "value": nc * args.steps / t_local,
-                             "sweep": dict(zip(("mode", "blocks_per_sm"), case.sweep_config()))}
+                             "sweep": dict(zip(("mode", "blocks_per_sm"), case.sweep_config())), "e2e": e2e}
+    # the plain binary64 form (results equal to the reference's) next to the headline form
+    plain = forms.get("fp64")
 
     # wall time from the freestream start to a residual fall of args.drop, per
     # form, and with the committed learned relaxation on the mixed form
@@ -693,8 +702,10 @@ def run_ours(args):
                        "re": w.re, "cfl": w.cfl, "precision": args.precision,
                        "sweep": dict(zip(("mode", "blocks_per_sm"), case.sweep_config())),
                        "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
-            "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "forms": forms,
-            "time_to_drop": drop}
+            "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
+            "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms_per_step"], "e2e": plain.get("e2e"),
+                           "note": "every kernel in binary64, results equal to the reference's"} if plain else None,
+            "forms": forms, "time_to_drop": drop}
     if rank == 0 and not args.no_overset:
         line["overset"] = overset_leg(stream)
     if rank == 0 and not args.no_batch and w.advance == "lusgs":

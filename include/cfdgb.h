@@ -92,6 +92,11 @@ extern "C" {
 #define CFD_FIELD_SST_FVISC 29 /* viscous face flux of k, omega, 2/face             */
 #define CFD_FIELD_SST_R     30 /* residual of k, omega, 2/cell (CellTotalTFlux)     */
 #define CFD_FIELD_SST_DIAG  31 /* LU-SGS diagonal of k, omega, 2/cell (SolveDiag)   */
+/* Limited face states of the last residual (HLLCFluxStrategy UL / UR after
+ * updateLeftRight), 4/face; formed on request from the binary64 residual's
+ * arrays (FP64 and MIXED forms; read only). */
+#define CFD_FIELD_UL        32
+#define CFD_FIELD_UR        33
 
 /* Residual-norm selectors for cfd_residual_norm. */
 #define CFD_NORM_DW_RHO2   0  /* sum dW_rho^2 (LUSGSIntegrator::postprocessUpdate) */
@@ -210,9 +215,11 @@ int cfd_residual_norm(cfd_case_t c, int mesh, int which, double* out);
  * whole case's primitive field from host memory (host_u[4*ncell_total], the
  * meshes one after another; pinned memory makes the copy asynchronous), then
  * nsteps graph-replayed steps (cfd_step_graph), then, if host_norms is not
- * NULL, every mesh's norm `which` into host_norms[nmesh]; synchronises once
+ * NULL, every mesh's norm `which` into host_norms[nmesh], and, if host_u_out
+ * is not NULL, the updated primitive field into host_u_out[4*ncell_total]
+ * (the same layout as host_u; it may be the same buffer); synchronises once
  * and reports device errors as cfd_sync does. */
-int cfd_step_io(cfd_case_t c, const double* host_u, int nsteps, int which, double* host_norms);
+int cfd_step_io(cfd_case_t c, const double* host_u, int nsteps, int which, double* host_norms, double* host_u_out);
 /* Copy a field of one mesh to / from host memory (layout above). */
 int cfd_get_field(cfd_case_t c, int mesh, int which, double* host);
 int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host);
@@ -471,14 +478,18 @@ int cfd_case_set_mlp(cfd_case_t c, cfd_mlp_t m, int apply_cfl, double spread);
 /* Residual norm of a caller-owned device array that allocates nothing (no
  * counterpart in the reference, which has no device code).  For callers that
  * may not allocate device memory while they run: solvers that reserve all of
- * it at start-up, hosts whose memory pool owns the device, or a time loop
- * being captured into a CUDA graph.  d_records: n records of 4 doubles
- * ([4*cell + eq], component 0 is reduced); which: CFD_NORM_DW_RHO2 (sum x^2) or
- * CFD_NORM_L2_R_RHO (sqrt(sum x^2 / n)); the result is written to d_out[0] on
- * the device, asynchronously on `stream`.  The scratch is a static 32 KiB
- * device array shared by all calls: n is limited to 33,554,432 records
- * (CFD_ERR_ARG beyond), overlapping calls race, and the first call on each
- * device looks up the array's address (make it before any stream capture). */
+ * it at start-up, or hosts whose own memory pool owns the device.
+ * d_records: n records of 4 doubles ([4*cell + eq], component 0 is reduced);
+ * which: CFD_NORM_DW_RHO2 (sum x^2) or CFD_NORM_L2_R_RHO (sqrt(sum x^2 / n));
+ * the result is written to d_out[0] on the device, asynchronously on `stream`.
+ * The scratch is a static 32 KiB device array shared by all calls: n is
+ * limited to 33,554,432 records (CFD_ERR_ARG beyond), overlapping calls race,
+ * and the first call on each device looks up the array's address (make it
+ * before any stream capture); that address is kept for the life of the
+ * process, so a device reset (cudaDeviceReset) while the library is loaded is
+ * not supported.  A NaN record gives a NaN result with CFD_OK: unlike
+ * cfd_residual_norm there is no device error word to raise
+ * CFD_ERR_NONPHYSICAL. */
 int cfd_residual_norm_noalloc(const double* d_records, int n, int which, double* d_out, void* stream);
 
 #ifdef __cplusplus

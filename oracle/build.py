@@ -33,9 +33,16 @@ def build(verbose: bool = False) -> Path:
     return LIB
 
 
-def build_ref(verbose: bool = False, reference_root: str = "/root/reference") -> Path | None:
+def reference_root() -> Path:
+    """Where the reference's sources are read from: $REFERENCE_ROOT, else the
+    container's read-only mount."""
+    return Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
+
+
+def build_ref(verbose: bool = False, reference_root: str | os.PathLike | None = None) -> Path | None:
     """Compile the reference's own serial path (oracle/_ref/ref_driver) when its
     sources are present; returns None when they are not."""
+    reference_root = str(reference_root or globals()["reference_root"]())
     if not (Path(reference_root) / "src" / "UnstructSolver").is_dir():
         return None
     r = subprocess.run(["bash", str(HERE / "build_ref.sh"), reference_root], capture_output=True, text=True)

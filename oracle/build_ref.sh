@@ -1,13 +1,14 @@
 #!/usr/bin/env bash
 # Compile the reference solver's serial path, straight from its sources, into
 # an oracle binary under oracle/_ref/ (git-ignored).  Test infrastructure only.
-#   usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+#   usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   (default: $REFERENCE_ROOT, else /root/reference)
 # Needs only g++: MPI, HDF5 and SAMRAI are replaced by the stand-in headers in
 # oracle/shims/.  -ffp-contract=off keeps every a*b+c as two rounded operations
 # on both x86-64 and aarch64, so the oracle's results do not depend on the host.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${REFERENCE_ROOT:-/root/reference}}"
 SRC="$REF/src"
 OUT="$HERE/_ref"
 if [ ! -d "$SRC/UnstructSolver" ]; then

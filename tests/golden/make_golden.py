@@ -104,7 +104,10 @@ def sst_main(ms, drv):
         print(case, m.ncell, "cells")
 
 
-def main(ref_root: str = "/root/reference", only: str = ""):
+def main(ref_root: str = "", only: str = ""):
+    from oracle.build import reference_root
+
+    ref_root = ref_root or str(reference_root())
     drv = ROOT / "oracle" / "_ref" / "ref_driver"
     subprocess.run(["bash", str(ROOT / "oracle" / "build_ref.sh"), ref_root], check=True)
     ms = meshes()

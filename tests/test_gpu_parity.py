@@ -68,7 +68,7 @@ def test_residual_phase(name):
     case.residual()
     case.sync()
     pairs = [("R", "res0_R"), ("UEDGE", "res0_Uedge"), ("GRAD", "res0_grad"), ("PHI", "res0_phi"),
-             ("SPEC_C", "res0_specc")]
+             ("SPEC_C", "res0_specc"), ("UL", "res0_UL"), ("UR", "res0_UR")]
     if c["flow"] == "viscous":
         pairs += [("GRADT", "res0_gradT"), ("SPEC_V", "res0_specv"), ("MU", "res0_mu"), ("MUEDGE", "res0_muedge")]
     for fld, key in pairs:
@@ -383,10 +383,12 @@ def test_step_io_equals_separate_calls():
     _, a = make_case(c)
     _, b = make_case(c)
     u = np.ascontiguousarray(g["init_U"], np.float64).reshape(-1)
+    back = np.zeros_like(u)
     for _ in range(2):
-        n1 = a.step_io(u, 3, "L2_R_RHO")
+        n1 = a.step_io(u, 3, "L2_R_RHO", u_out=back)
         b.put("U", u)
         b.step_graph(3)
         n2 = b.norm("L2_R_RHO")
         assert n1[0] == n2
         np.testing.assert_array_equal(a.get("U"), b.get("U"))
+        np.testing.assert_array_equal(back.reshape(-1, 4), b.get("U").reshape(-1, 4))

@@ -96,11 +96,10 @@ def test_truncated_file_is_mesh_error(built_lib, tmp_path):
 
 
 def test_reference_shipped_mesh_if_present(built_lib):
-    from pathlib import Path
-
+    from oracle.build import reference_root
     from tmp_gb300 import abi
 
-    p = Path("/root/reference/mix_element_laminar.grd")
+    p = reference_root() / "mix_element_laminar.grd"
     if not p.exists():
         pytest.skip("reference meshes not present")
     m = abi.Mesh.load_grd(p, -1, -2)

@@ -25,14 +25,14 @@ PREC_FP64, PREC_FP32, PREC_MIXED, PREC_MIXFF = 0, 1, 2, 3
 FIELD = dict(U=0, W=1, R=2, GRAD=3, PHI=4, SPEC_C=5, SPEC_V=6, DT=7, DIAG=8, DW1=9, DW=10, GRADT=11, MU=12,
              UEDGE=13, MUEDGE=14, VOL=15, CENTER=16, NORMAL=17, AREA=18, ECENTER=19, WALLDIST=20, SST_T=21,
              SST_TFACE=22, SST_TGRAD=23, SST_F1=24, SST_F2=25, SST_MUT=26, SST_MUTF=27, SST_FCONV=28,
-             SST_FVISC=29, SST_R=30, SST_DIAG=31)
+             SST_FVISC=29, SST_R=30, SST_DIAG=31, UL=32, UR=33)
 # values per element and whether the field lives on faces
 FIELD_SHAPE = dict(U=(4, 0), W=(4, 0), R=(4, 0), GRAD=(8, 0), PHI=(4, 0), SPEC_C=(1, 0), SPEC_V=(1, 0),
                    DT=(1, 0), DIAG=(1, 0), DW1=(4, 0), DW=(4, 0), GRADT=(2, 0), MU=(1, 0), UEDGE=(4, 1),
                    MUEDGE=(1, 1), VOL=(1, 0), CENTER=(2, 0), NORMAL=(2, 1), AREA=(1, 1), ECENTER=(2, 1),
                    WALLDIST=(1, 0), SST_T=(2, 0), SST_TFACE=(2, 1), SST_TGRAD=(4, 0), SST_F1=(1, 0), SST_F2=(1, 0),
                    SST_MUT=(1, 0), SST_MUTF=(1, 1), SST_FCONV=(2, 1), SST_FVISC=(2, 1), SST_R=(2, 0),
-                   SST_DIAG=(2, 0))
+                   SST_DIAG=(2, 0), UL=(4, 1), UR=(4, 1))
 NORM = dict(DW_RHO2=0, RK_DRHO=1, L2_R_RHO=2)
 LAYOUT_ROW, LAYOUT_COLUMN = 0, 1
 MLP_INPUTS, MLP_OUTPUTS, MLP_PARAMS = 12, 2, 5122
@@ -91,7 +91,7 @@ def lib() -> C.CDLL:
         "cfd_lusgs_step": (C.c_int, [vp]),
         "cfd_step_graph": (C.c_int, [vp, C.c_int]),
         "cfd_residual_norm": (C.c_int, [vp, C.c_int, C.c_int, dp]),
-        "cfd_step_io": (C.c_int, [vp, dp, C.c_int, C.c_int, dp]),
+        "cfd_step_io": (C.c_int, [vp, dp, C.c_int, C.c_int, dp, dp]),
         "cfd_get_field": (C.c_int, [vp, C.c_int, C.c_int, dp]),
         "cfd_put_field": (C.c_int, [vp, C.c_int, C.c_int, dp]),
         "cfd_sync": (C.c_int, [vp]),
@@ -309,13 +309,17 @@ class Case:
         check(lib().cfd_step_graph(self.h, int(n)))
 
     def step_io(self, u_host: np.ndarray | None, nsteps: int = 1, which: str | None = "DW_RHO2",
-                out: np.ndarray | None = None) -> np.ndarray | None:
-        """Upload the primitive field (host, all meshes), step, read every mesh's norm: one call, one sync."""
+                out: np.ndarray | None = None, u_out: np.ndarray | None = None) -> np.ndarray | None:
+        """Upload the primitive field (host, all meshes), step, read every mesh's norm and, when u_out is
+        given (float64, 4*ncell_total, contiguous), the updated field back: one call, one sync."""
         up = _dptr(u_host) if u_host is not None else None
         if which is not None and out is None:
             out = np.zeros(self.nmesh)
+        if u_out is not None:
+            assert u_out.dtype == np.float64 and u_out.flags.c_contiguous and u_out.size == 4 * self.ncell
         check(lib().cfd_step_io(self.h, up, int(nsteps), NORM[which] if which else 0,
-                                _dptr(out) if which is not None else None))
+                                _dptr(out) if which is not None else None,
+                                _dptr(u_out) if u_out is not None else None))
         return out
 
     def sync(self):

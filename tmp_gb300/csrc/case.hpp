@@ -179,6 +179,7 @@ cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool fo
 void launch_chain_static(const DevArrays& d, const LaunchCfg& L);
 void launch_cp_ma(const DevArrays& d, const LaunchCfg& L, int begin, int end, double pinf, double uinf, double vinf,
                   double* out);
+void launch_face_lr(const DevArrays& d, const LaunchCfg& L, int begin, int end, bool right, d4* out);
 void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
 void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);

@@ -904,7 +904,7 @@ int cfd_step_graph(cfd_case_t c, int nsteps) {
     ABI_CATCH
 }
 
-int cfd_step_io(cfd_case_t c, const double* host_u, int nsteps, int which, double* host_norms) {
+int cfd_step_io(cfd_case_t c, const double* host_u, int nsteps, int which, double* host_norms, double* host_u_out) {
     if (!c || nsteps < 0) return fail(CFD_ERR_ARG, "null case or negative step count");
     if (host_norms && (which < 0 || which > 2)) return fail(CFD_ERR_ARG, "unknown norm");
     ABI_TRY
@@ -925,6 +925,9 @@ int cfd_step_io(cfd_case_t c, const double* host_u, int nsteps, int which, doubl
         ck(cudaMemcpyAsync(host_norms, c->d.norm_out, (size_t)c->nmesh * sizeof(double), cudaMemcpyDeviceToHost,
                            c->stream), "norm readback");
     }
+    if (host_u_out)
+        ck(cudaMemcpyAsync(host_u_out, c->d.U, (size_t)c->d.nc * 32, cudaMemcpyDeviceToHost, c->stream),
+           "field readback");
     const int st = check_errors(c);  // synchronises the stream
     if (host_norms && which == CFD_NORM_L2_R_RHO)
         for (int m = 0; m < c->nmesh; m++) host_norms[m] = sqrt(host_norms[m] / (double)(c->coff[m + 1] - c->coff[m]));
@@ -1278,6 +1281,22 @@ int cfd_get_field(cfd_case_t c, int mesh, int which, double* host) {
         int off = c->coff[mesh], n = c->coff[mesh + 1] - off;
         ck(cudaMemcpyAsync(host, c->d.walld + off, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream), "download");
         ck(cudaStreamSynchronize(c->stream), "sync");
+        return CFD_OK;
+    }
+    if (which == CFD_FIELD_UL || which == CFD_FIELD_UR) {
+        if (c->fp32() || c->ffres())
+            return fail(CFD_ERR_ARG, "UL / UR are formed from the binary64 residual (FP64 and MIXED forms)");
+        const int off = c->foff[mesh], n = c->foff[mesh + 1] - off;
+        d4* tmp = nullptr;
+        ck(cudaMalloc(&tmp, (size_t)n * sizeof(d4) + 32), "alloc");
+        launch_face_lr(c->d, c->L(), off, off + n, which == CFD_FIELD_UR, tmp);
+        cudaError_t e1 = cudaGetLastError();
+        cudaError_t e2 = e1 == cudaSuccess ? cudaMemcpyAsync(host, tmp, (size_t)n * 32, cudaMemcpyDeviceToHost, c->stream)
+                                           : e1;
+        cudaError_t e3 = cudaStreamSynchronize(c->stream);
+        cudaFree(tmp);
+        ck(e2, "face states");
+        ck(e3, "sync");
         return CFD_OK;
     }
     FieldRef r = field_ref(c, which);

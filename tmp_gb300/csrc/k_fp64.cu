@@ -1382,6 +1382,41 @@ void launch_cp_ma(const DevArrays& d, const LaunchCfg& L, int begin, int end, do
     *L.counter += 1;
 }
 
+// Limited left / right face states (HLLCFluxStrategy::updateLeftRight,
+// HLLCFluxStrategy.h:35-100) of faces [begin, end) from the last binary64
+// residual's U, gradients and limiter, with k_face_flux's expressions:
+// interior q = (grad q . (x_f - x_c)) * phi + U of that side; boundary faces
+// take the face state U_edge on both sides.  out[(f - begin)] = 4 values.
+__global__ void k_face_lr(int begin, int end, int right, const int2* __restrict__ lr, const d4* __restrict__ fg1,
+                          const d4* __restrict__ U, const d4* __restrict__ grad, const d4* __restrict__ phi,
+                          const d4* __restrict__ Ue, d4* __restrict__ out) {
+    const int f = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= end) return;
+    const int2 e = lr[f];
+    d4 o;
+    if (e.y >= 0) {
+        const int c = right ? e.y : e.x;
+        const d4 d = ld4(fg1 + f);
+        const double dx = right ? d.z : d.x, dy = right ? d.w : d.y;
+        const d4 g0 = ld4(grad + 2 * (size_t)c), g1 = ld4(grad + 2 * (size_t)c + 1);
+        const double gx[4] = {g0.x, g0.z, g1.x, g1.z}, gy[4] = {g0.y, g0.w, g1.y, g1.w};
+        double u[4], p[4], q[4];
+        to_arr(ld4(U + c), u);
+        to_arr(ld4(phi + c), p);
+        for (int j = 0; j < 4; j++) q[j] = dot2(gx[j], gy[j], dx, dy) * p[j] + u[j];
+        o = d4{q[0], q[1], q[2], q[3]};
+    } else {
+        o = ld4(Ue + f);
+    }
+    out[f - begin] = o;
+}
+void launch_face_lr(const DevArrays& d, const LaunchCfg& L, int begin, int end, bool right, d4* out) {
+    if (end <= begin) return;
+    k_face_lr<<<nblk(end - begin, 256), 256, 0, L.stream>>>(begin, end, right ? 1 : 0, d.lr, d.fg1, d.U, d.grad,
+                                                             d.phi, d.Ue, out);
+    *L.counter += 1;
+}
+
 // 1/D for the fast form's sweep (binary64)
 __global__ void k_inv_diag(int nc, const double* __restrict__ D, double* __restrict__ invD) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;

@@ -2,11 +2,10 @@
 //
 // Some callers cannot allocate device memory while they run: a host solver
 // that reserves all of its device memory at start-up and forbids allocation
-// inside the time loop (fixed footprint, no allocator stalls), code that
-// issues work while another framework's pool owns the device memory, or a
-// time loop being recorded into a CUDA graph, where cudaMalloc would break the
-// capture.  This entry point serves them: the only scratch it needs (one
-// partial sum per 8192-record chunk) lives in a file-scope __device__ array.
+// inside the time loop (fixed footprint, no allocator stalls), or code that
+// issues work while another framework's pool owns the device memory.  This
+// entry point serves them: the only scratch it needs (one partial sum per
+// 8192-record chunk) lives in a file-scope __device__ array.
 //
 // Limits and sharing rules:
 //   * at most kNoAllocMaxChunks chunks, i.e. n <= 4096 * 8192 = 33,554,432
@@ -19,7 +18,10 @@
 //   * every GPU that loads the library holds the 32 KiB array until exit;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, with that device current), so make
-//     that first call before any stream capture begins.
+//     that first call before any stream capture begins; the address is cached
+//     for the life of the process, so a device reset while the library is
+//     loaded is not supported;
+//   * a NaN record gives a NaN result and CFD_OK (no device error word here).
 #include <cuda_runtime.h>
 
 #include <mutex>
