@@ -37,6 +37,14 @@ extern "C" {
 /* ---- enums --------------------------------------------------------------- */
 #define CFD_FLOW_EULER    0   /* Euler2D                                   */
 #define CFD_FLOW_LAMINAR  1   /* ViscousFlow2D (laminar branch)            */
+#define CFD_FLOW_SST      2   /* ViscousFlow2D with the SST k-omega model
+                                 coupled into every LU-SGS step (the
+                                 isLaminar() == false branch, which the
+                                 reference never runs): mu + mu_t in the
+                                 viscous flux and radii, dt = CFL vol /
+                                 (spec_c + 4 spec_v), a two-equation
+                                 turbulence sweep after the flow's.  LU-SGS
+                                 with the FP64 or MIXED form only          */
 #define CFD_ADV_RK5       0   /* RungeKuttaStrategy(5)                     */
 #define CFD_ADV_LUSGS     1   /* LUSGSIntegrator                           */
 #define CFD_PREC_FP64     0   /* plain: every kernel in binary64           */
@@ -421,6 +429,12 @@ int cfd_cell_iblank(cfd_block_t b, const int* node_iblank, int* cell_iblank);
  * cfd_local_dt first).  cfd_sst_update_mut: the eddy viscosity update of
  * UpdatePrimitiveVariables (:194-223) from W = rho (k, omega). */
 int cfd_sst_enable(cfd_case_t c);
+/* Freestream turbulence of the model: intensity tu and eddy-viscosity ratio
+ * mu_t / mu (InitializeturbulenceVariable, SSTKWStrategy.h:582-613, fixes them
+ * at 0.01 and 0.035): k = 1.5 (tu |V|)^2, omega = rho k / (ratio mu), mu_t =
+ * ratio mu.  Sets the far-field values (and the floors of the coupled model);
+ * cfd_init_freestream then starts from them.  No reference counterpart. */
+int cfd_sst_set_inflow(cfd_case_t c, double intensity, double viscosity_ratio);
 int cfd_sst_freestream(cfd_case_t c, int mesh, double* out3);
 int cfd_sst_residual(cfd_case_t c);
 int cfd_sst_update_mut(cfd_case_t c);

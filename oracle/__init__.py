@@ -66,6 +66,11 @@ def _load():
         L.orc_holemap.restype = C.c_int
         L.orc_holemap_check.argtypes = [ip, dp, ip, C.c_long, dp, ip]
         L.orc_interp_update.argtypes = [C.c_long, ip, ip, ip, dp, dp, C.c_long, dp, C.c_long, C.c_int, C.c_int]
+        L.orc_sst_enable.argtypes = [vp, C.c_int, C.c_double, C.c_double]
+        for f in ("orc_sst_cons", "orc_sst_equation", "orc_sst_diag", "orc_sst_update_mut"):
+            getattr(L, f).argtypes = [vp]
+        L.orc_sst_field.argtypes = [vp, C.c_int]
+        L.orc_sst_field.restype = dp
         _lib = L
     return _lib
 
@@ -104,6 +109,36 @@ class Oracle:
 
     def lusgs_step(self, cfl: float, first_order: bool = False) -> int:
         return _load().orc_lusgs_step(self.h, cfl, int(first_order))
+
+    # SST k-omega: arrays by name, (values per element, per face)
+    SST = dict(SST_T=(21, 2, 0), SST_TFACE=(22, 2, 1), SST_TGRAD=(23, 4, 0), SST_F1=(24, 1, 0), SST_F2=(25, 1, 0),
+               SST_MUT=(26, 1, 0), SST_MUTF=(27, 1, 1), SST_FCONV=(28, 2, 1), SST_FVISC=(29, 2, 1), SST_R=(30, 2, 0),
+               SST_DIAG=(31, 2, 0), SST_W=(40, 2, 0), SST_DW1=(41, 2, 0), SST_DW=(42, 2, 0))
+
+    def sst_enable(self, coupled: bool, tu: float = 0.01, ratio: float = 0.035):
+        """Allocate the SST arrays and set the freestream k, omega, mu_t; coupled: every LU-SGS step then runs the
+        turbulence model with the flow (the build's turbulent path), else its functions are called one by one."""
+        L = _load()
+        L.orc_sst_enable(self.h, int(coupled), float(tu), float(ratio))
+        L.orc_sst_cons(self.h)
+
+    def sst_cons(self):
+        _load().orc_sst_cons(self.h)
+
+    def sst_equation(self):
+        _load().orc_sst_equation(self.h)
+
+    def sst_diag(self):
+        _load().orc_sst_diag(self.h)
+
+    def sst_update_mut(self):
+        _load().orc_sst_update_mut(self.h)
+
+    def sst_field(self, name: str) -> np.ndarray:
+        fid, width, per_face = self.SST[name]
+        n = (self.m.nedge if per_face else self.m.ncell) * width
+        a = np.ctypeslib.as_array(_load().orc_sst_field(self.h, fid), shape=(n,))
+        return a.reshape(-1, width) if width > 1 else a
 
     def wall_force(self) -> np.ndarray:
         """(Fx, Fy) through the wall faces in the last residual evaluation."""

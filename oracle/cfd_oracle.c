@@ -44,6 +44,13 @@ typedef struct {
     /* integrators */
     double *W, *Wnow, *D, *dW1, *dW;
     double force[2]; /* momentum flux through wall faces of the last residual */
+    /* SST k-omega (allocated by orc_sst_enable): coupled = 1 when the model
+     * runs inside every LU-SGS step (the build's turbulent path), 0 when its
+     * functions are only evaluated one by one (the reference's own code) */
+    int sst, coupled;
+    double density, pressure;          /* dimensional freestream */
+    double sst_k, sst_w, sst_mut;       /* nondimensional freestream k, omega, mu_t */
+    double *T, *Tw, *Tf, *TG, *F1, *F2, *mut, *mutf, *Tfc, *Tfv, *TR, *TD, *TdW1, *TdW;
 } orc_t;
 
 static const double Gamma = 1.4;
@@ -78,7 +85,8 @@ void orc_free(orc_t* o) {
     if (!o) return;
     double* p[] = {o->vol, o->cen, o->nrm, o->area, o->ecen, o->walld, o->U, o->Ue, o->grad, o->gradT, o->specc,
                    o->specv, o->R, o->dt, o->mu, o->mue, o->phi, o->UL, o->UR, o->umax, o->umin, o->W, o->Wnow,
-                   o->D, o->dW1, o->dW};
+                   o->D, o->dW1, o->dW, o->T, o->Tw, o->Tf, o->TG, o->F1, o->F2, o->mut, o->mutf, o->Tfc, o->Tfv,
+                   o->TR, o->TD, o->TdW1, o->TdW};
     for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++) free(p[i]);
     free(o);
 }
@@ -168,6 +176,8 @@ void orc_set_freestream(orc_t* o, double Ma, double AOA, double Re, double densi
     o->re = Re;
     o->t_inf = T;
     o->viscous = viscous;
+    o->density = density;
+    o->pressure = pressure;
 }
 
 void orc_init_freestream(orc_t* o) {
@@ -202,6 +212,18 @@ static double sutherland(const orc_t* o, double T) {
     double cc = 110.5 / o->t_inf;
     return (1.0 + cc) / (T + cc) * pow(T, 1.5) * sqrt(Gamma) * o->mach / o->re;
 }
+
+/* mu/Pr at a face and a cell (getMuOverPrEdge / getMuOverPrCell): laminar,
+ * plus mu_t / Prt when the SST model is coupled (ViscousFlow2D.h:138-154 with
+ * isLaminar() false; Pr = 0.72, Prt = 0.9, TopologyHolderStrategy.h:40-41). */
+static int turb(const orc_t* o) { return o->sst && o->coupled; }
+static double mpr_face(const orc_t* o, int k) {
+    return turb(o) ? o->mue[k] / 0.72 + o->mutf[k] / 0.9 : o->mue[k] / 0.72;
+}
+static double mpr_cell(const orc_t* o, int c) {
+    return turb(o) ? o->mu[c] / 0.72 + o->mut[c] / 0.9 : o->mu[c] / 0.72;
+}
+static void sst_equation(orc_t* o);
 
 /* BoundaryStrategy::HandleInvicidBoundary / HandleViscousBoundary
  * (BoundaryStrategy.h:73-335).  Returns 1 when the slip-wall check fails. */
@@ -348,6 +370,9 @@ int orc_residual(orc_t* o, int first_order) {
         for (int c = 0; c < nc; c++) o->mu[c] = sutherland(o, o->U[4 * c + 1] / o->U[4 * c]);
         for (int k = 0; k < ne; k++) o->mue[k] = sutherland(o, o->Ue[4 * k + 1] / o->Ue[4 * k]);
     }
+    /* the turbulence equation's residual, between computeMu and the spectral
+     * radii as in ViscousFlow2D::preprocessAdvance (ViscousFlow2D.h:163-190) */
+    if (turb(o)) sst_equation(o);
     /* solveSpectralRadius */
     for (int k = 0; k < ne; k++) {
         int l = o->lr[2 * k], r = o->lr[2 * k + 1];
@@ -359,7 +384,7 @@ int orc_residual(orc_t* o, int first_order) {
         o->specc[l] += s;
         if (r >= 0) o->specc[r] += s;
         if (o->viscous) {
-            s = dmax(4 / (3.0 * ue[0]), Gamma / ue[0]) * (o->mue[k] / 0.72) * A * A;
+            s = dmax(4 / (3.0 * ue[0]), Gamma / ue[0]) * mpr_face(o, k) * A * A;
             o->specv[l] += s / o->vol[l];
             if (r >= 0) o->specv[r] += s / o->vol[r];
         }
@@ -431,7 +456,7 @@ int orc_residual(orc_t* o, int first_order) {
         for (int k = 0; k < ne; k++) {
             int l = o->lr[2 * k], r = o->lr[2 * k + 1];
             double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1], A = o->area[k];
-            double mu = o->mue[k], eff = 2.0 / 3.0 * mu;
+            double mu = turb(o) ? o->mue[k] + o->mutf[k] : o->mue[k], eff = 2.0 / 3.0 * mu;
             double g[3][2];
             if (r >= 0) {
                 double lx = o->cen[2 * r] - o->cen[2 * l], ly = o->cen[2 * r + 1] - o->cen[2 * l + 1];
@@ -455,8 +480,8 @@ int orc_residual(orc_t* o, int first_order) {
             double txx = eff * (2.0 * g[0][0] - g[1][1]);
             double tyy = eff * (2.0 * g[1][1] - g[0][0]);
             double txy = mu * (g[0][1] + g[1][0]);
-            double qx = -Gamma / (Gamma - 1) * (mu / 0.72) * g[2][0];
-            double qy = -Gamma / (Gamma - 1) * (mu / 0.72) * g[2][1];
+            double qx = -Gamma / (Gamma - 1) * mpr_face(o, k) * g[2][0];
+            double qy = -Gamma / (Gamma - 1) * mpr_face(o, k) * g[2][1];
             double Fv[4];
             Fv[0] = 0.0;
             Fv[1] = ((ve0 * txx + ve1 * txy - qx) * nx + (ve0 * txy + ve1 * tyy - qy) * ny) * A;
@@ -471,9 +496,12 @@ int orc_residual(orc_t* o, int first_order) {
     return err;
 }
 
-/* Euler2D/ViscousFlow2D::SolveTime, laminar branch (Euler2D.h:67-77, ViscousFlow2D.h:223-242) */
+/* Euler2D/ViscousFlow2D::SolveTime (Euler2D.h:67-77, ViscousFlow2D.h:223-242):
+ * the laminar branch, or with the SST model coupled the turbulent one,
+ * dt = CFL vol / (spec_c + 4 spec_v). */
 void orc_solve_time(orc_t* o, double cfl) {
-    for (int c = 0; c < o->ncell; c++) o->dt[c] = cfl * o->vol[c] / o->specc[c];
+    for (int c = 0; c < o->ncell; c++)
+        o->dt[c] = turb(o) ? cfl * o->vol[c] / (o->specc[c] + 4.0 * o->specv[c]) : cfl * o->vol[c] / o->specc[c];
 }
 
 /* RungeKuttaStrategy::singleStepSerial (RungeKuttaStrategy.h:74-86,39-72). */
@@ -502,6 +530,9 @@ static void conv_flux(const double* w, double nx, double ny, double* F) {
     F[0] = w[0] * vn; F[1] = (w[1] + p) * vn; F[2] = w[2] * vn + p * nx; F[3] = w[3] * vn + p * ny;
 }
 
+static void sst_step_sweeps(orc_t* o);
+static void sst_step_update(orc_t* o);
+
 /* SolveDF + SolveViscousFlux (TopologyHolderStrategy.cpp:143-323) for cell i,
  * face k, forward (fb = 1) or backward (fb = 0), increment array dWx. */
 static void solve_df(const orc_t* o, int i, int k, const double* dWx, int fb, double* DF) {
@@ -525,7 +556,7 @@ static void solve_df(const orc_t* o, int i, int k, const double* dWx, int fb, do
     double vn = dot2(uj[2], uj[3], nx, ny);
     double c = sqrt(Gamma * uj[1] / uj[0]);
     double rA = 1.5 * (fabs(vn) + c);
-    if (o->viscous) rA += dmax(4 / (3 * uj[0]), Gamma / uj[0]) * (o->mu[i] / 0.72) / sqrt(dot2(lx, ly, lx, ly));
+    if (o->viscous) rA += dmax(4 / (3 * uj[0]), Gamma / uj[0]) * mpr_cell(o, i) / sqrt(dot2(lx, ly, lx, ly));
     for (int m = 0; m < 4; m++) {
         double fv = rA * dw[m];
         double dfc = left ? (fcp[m] - fc[m]) : (fc[m] - fcp[m]);
@@ -561,11 +592,336 @@ int orc_lusgs_step(orc_t* o, double cfl, int first_order) {
         }
         for (int m = 0; m < 4; m++) o->dW[4 * c + m] = o->dW1[4 * c + m] - s[m] / o->D[c];
     }
+    if (turb(o)) sst_step_sweeps(o);
     for (int c = 0; c < o->ncell; c++) {
         for (int m = 0; m < 4; m++) o->W[4 * c + m] = o->W[4 * c + m] + o->dW[4 * c + m];
         prim_from_cons(o->W + 4 * c, o->U + 4 * c);
     }
+    if (turb(o)) sst_step_update(o);
     return err;
+}
+
+/* ------------------------------------------------------------------------
+ * SST k-omega (SSTkomegaModel, UnstructSolver/SSTKWStrategy.h).
+ *
+ * The functions below restate the model's residual (:615-1013), diagonal
+ * (:170-192) and eddy-viscosity update (:194-223) in the reference's operation
+ * order; they are pinned to the reference's own outputs by
+ * tests/test_oracle_sst.py.  The reference never runs the model (isLaminar()
+ * is true), and its turbulence LU-SGS step cannot run as written, so the
+ * coupled step (orc_sst_enable with coupled = 1) is the build's definition,
+ * with these departures from the written code, each a defect of the dead path:
+ *   - the residual is sum(Fc - Fv) - Q vol: SolveTotalTFlux (:969-1013) adds
+ *     +Q vol, which with LU-SGS's dW = -R/D turns production into destruction;
+ *   - SolveDF (:251-474) reads the neighbour's k, omega and their increments at
+ *     [j + 2 cell] for j = 4, 5 (past the cell's own pair); the cell's pair is
+ *     used;
+ *   - in its right-cell branch SolveDF passes the current cell as the
+ *     neighbour to SolveViscousFlux (:377), whose centre line is then zero
+ *     (r_A divides by sqrt(0)); the left neighbour is passed;
+ *   - k and omega are kept above 1e-4 of their freestream values after each
+ *     update (the reference's clip at :206-215 is commented out);
+ *   - the flow state and flow increments SolveDF reads (its extern pointers,
+ *     never set by any caller) are the flow's W before the update and the
+ *     flow's dW1 / dW of the same step, so the turbulence sweep follows the
+ *     flow's sweeps and the update of k, omega follows the flow's update, as
+ *     UpdatePrimitiveVariables asks (:196).
+ * ------------------------------------------------------------------------ */
+static const double sst_beta1 = 0.075, sst_beta2 = 0.0828, sst_sk1 = 0.85, sst_sk2 = 1.0, sst_sw1 = 0.5,
+                    sst_sw2 = 0.856, sst_cw1 = 0.533, sst_cw2 = 0.440, sst_a1 = 0.31, sst_bstar = 0.09;
+
+/* InitializeturbulenceVariable (:582-613) with the turbulence intensity tu
+ * (the reference: 0.01) and eddy-viscosity ratio (the reference: 0.035) as
+ * parameters: k = 1.5 (tu |V|)^2, omega = rho k / (ratio mu), mu_t = ratio mu. */
+void orc_sst_enable(orc_t* o, int coupled, double tu, double ratio) {
+    size_t c = (size_t)o->ncell, e = (size_t)o->nedge;
+    if (!o->sst) {
+        o->T = calloc(2 * c, 8); o->Tw = calloc(2 * c, 8); o->Tf = calloc(2 * e, 8); o->TG = calloc(4 * c, 8);
+        o->F1 = calloc(c, 8); o->F2 = calloc(c, 8); o->mut = calloc(c, 8); o->mutf = calloc(e, 8);
+        o->Tfc = calloc(2 * e, 8); o->Tfv = calloc(2 * e, 8); o->TR = calloc(2 * c, 8); o->TD = calloc(2 * c, 8);
+        o->TdW1 = calloc(2 * c, 8); o->TdW = calloc(2 * c, 8);
+    }
+    o->sst = 1;
+    o->coupled = coupled;
+    const double R = 287.0, L = 1.0;
+    double cs = sqrt(Gamma * o->pressure / o->density);
+    double T = o->pressure / (R * o->density);
+    double mu = 1.458e-6 * pow(T, 1.5) / (T + 110.5);
+    double fs_mut = mu * ratio;
+    o->sst_mut = fs_mut / mu * sqrt(Gamma) * o->mach / o->re;
+    double k = 1.5 * o->mach * cs * tu * o->mach * cs * tu;
+    double w = o->density * k / (ratio * mu);
+    o->sst_k = Gamma * k / (cs * cs);
+    o->sst_w = sqrt(Gamma) * L * w / cs;
+    for (int i = 0; i < o->ncell; i++) {
+        o->T[2 * i] = o->sst_k;
+        o->T[2 * i + 1] = o->sst_w;
+        o->mut[i] = o->sst_mut;
+    }
+}
+
+/* initializeConsData (:97-109): conservative rho k, rho omega from the flow's rho */
+void orc_sst_cons(orc_t* o) {
+    for (int i = 0; i < o->ncell; i++) {
+        double rho = o->U[4 * i];
+        o->Tw[2 * i] = o->T[2 * i] * rho;
+        o->Tw[2 * i + 1] = o->T[2 * i + 1] * rho;
+    }
+}
+
+/* SolveTurbulenceEquation (:515-524): ComputeFaceTValue, ComputeCellTGradient,
+ * ComputeSSTf1f2, ComputeTurbulenceViscousCoefficient (face loop),
+ * SolveConvectiveTFlux, SolveViscousTFlux, SolveTotalTFlux, on the flow's
+ * face states, gradients and laminar viscosities of the current residual. */
+static void sst_equation(orc_t* o) {
+    int nc = o->ncell, ne = o->nedge;
+    for (int k = 0; k < ne; k++) { /* :615-659 */
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        if (r >= 0) {
+            o->Tf[2 * k] = 0.5 * (o->T[2 * l] + o->T[2 * r]);
+            o->Tf[2 * k + 1] = 0.5 * (o->T[2 * l + 1] + o->T[2 * r + 1]);
+        } else if (r == BC_WALL) {
+            double dis = o->walld[l];
+            o->Tf[2 * k] = 0.0;
+            o->Tf[2 * k + 1] = 10.0 * 6.0 * o->mue[k] / (o->Ue[4 * k] * sst_beta1 * dis * dis);
+        } else {
+            double vn = dot2(o->Ue[4 * k + 2], o->Ue[4 * k + 3], o->nrm[2 * k], o->nrm[2 * k + 1]);
+            o->Tf[2 * k] = vn > 0.0 ? o->T[2 * l] : o->sst_k;
+            o->Tf[2 * k + 1] = vn > 0.0 ? o->T[2 * l + 1] : o->sst_w;
+        }
+    }
+    memset(o->TG, 0, 4 * 8 * (size_t)nc); /* :662-692 */
+    for (int k = 0; k < ne; k++) {
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1], A = o->area[k];
+        for (int q = 0; q < 2; q++) {
+            double a = A * o->Tf[2 * k + q];
+            o->TG[4 * l + 2 * q] = o->TG[4 * l + 2 * q] + nx * a;
+            o->TG[4 * l + 2 * q + 1] = o->TG[4 * l + 2 * q + 1] + ny * a;
+            if (r >= 0) {
+                o->TG[4 * r + 2 * q] = o->TG[4 * r + 2 * q] - nx * a;
+                o->TG[4 * r + 2 * q + 1] = o->TG[4 * r + 2 * q + 1] - ny * a;
+            }
+        }
+    }
+    for (int c = 0; c < nc; c++)
+        for (int q = 0; q < 4; q++) o->TG[4 * c + q] = o->TG[4 * c + q] / o->vol[c];
+    for (int c = 0; c < nc; c++) { /* :695-722 */
+        double gv = dot2(o->TG[4 * c], o->TG[4 * c + 1], o->TG[4 * c + 2], o->TG[4 * c + 3]);
+        double rho = o->U[4 * c], dis = o->walld[c], K = o->T[2 * c], w = o->T[2 * c + 1], muL = o->mu[c];
+        double cdkw = dmax(2.0 * rho * sst_sw2 / w * gv, 1.0e-20);
+        double arg1 = dmax(sqrt(K) / (0.09 * w * dis), 500.0 * muL / (rho * w * dis * dis));
+        arg1 = dmin(arg1, 4.0 * rho * sst_sw2 * K / (cdkw * dis * dis));
+        double arg2 = dmax(2.0 * sqrt(K) / (0.09 * w * dis), 500.0 * muL / (rho * w * dis * dis));
+        o->F1[c] = tanh(arg1 * arg1 * arg1 * arg1);
+        o->F2[c] = tanh(arg2 * arg2);
+    }
+    for (int k = 0; k < ne; k++) { /* :749-777 */
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        if (r >= 0) o->mutf[k] = 0.5 * (o->mut[l] + o->mut[r]);
+        else if (r == BC_WALL) o->mutf[k] = 0.0;
+        else {
+            double vn = dot2(o->Ue[4 * k + 2], o->Ue[4 * k + 3], o->nrm[2 * k], o->nrm[2 * k + 1]);
+            o->mutf[k] = vn > 0.0 ? o->mut[l] : o->sst_mut;
+        }
+    }
+    for (int k = 0; k < ne; k++) { /* :783-831 and :834-920 */
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1], A = o->area[k];
+        double vn = dot2(o->Ue[4 * k + 2], o->Ue[4 * k + 3], nx, ny);
+        double g[2][2], ff1;
+        if (r >= 0) {
+            double vp = 0.5 * (vn + fabs(vn)), vs = 0.5 * (vn - fabs(vn));
+            double rl = o->U[4 * l], rr = o->U[4 * r];
+            o->Tfc[2 * k] = o->T[2 * l] * rl * vp * A + o->T[2 * r] * rr * vs * A;
+            o->Tfc[2 * k + 1] = o->T[2 * l + 1] * rl * vp * A + o->T[2 * r + 1] * rr * vs * A;
+            double l0 = o->cen[2 * r] - o->cen[2 * l], l1 = o->cen[2 * r + 1] - o->cen[2 * l + 1];
+            double L2 = dot2(l0, l1, l0, l1);
+            ff1 = 0.5 * (o->F1[l] + o->F1[r]);
+            for (int q = 0; q < 2; q++) {
+                g[q][0] = (o->TG[4 * l + 2 * q] + o->TG[4 * r + 2 * q]) * 0.5;
+                g[q][1] = (o->TG[4 * l + 2 * q + 1] + o->TG[4 * r + 2 * q + 1]) * 0.5;
+                double dq = o->T[2 * r + q] - o->T[2 * l + q];
+                /* x first, then y with the corrected x (:857-861) */
+                g[q][0] = g[q][0] + ((dq) - (g[q][0] * l0 + g[q][1] * l1)) * l0 / L2;
+                g[q][1] = g[q][1] + ((dq) - (g[q][0] * l0 + g[q][1] * l1)) * l1 / L2;
+            }
+        } else {
+            o->Tfc[2 * k] = vn * o->Ue[4 * k] * o->Tf[2 * k] * A;
+            o->Tfc[2 * k + 1] = vn * o->Ue[4 * k] * o->Tf[2 * k + 1] * A;
+            ff1 = o->F1[l];
+            for (int q = 0; q < 2; q++) { g[q][0] = o->TG[4 * l + 2 * q]; g[q][1] = o->TG[4 * l + 2 * q + 1]; }
+        }
+        double sk = ff1 * sst_sk1 + (1 - ff1) * sst_sk2;
+        double sw = ff1 * sst_sw1 + (1 - ff1) * sst_sw2;
+        double ml = o->mue[k], mt = o->mutf[k];
+        double txk = (ml + sk * mt) * g[0][0], tyk = (ml + sk * mt) * g[0][1];
+        double txw = (ml + sw * mt) * g[1][0], tyw = (ml + sw * mt) * g[1][1];
+        double v0 = txk * nx + tyk * ny, v1 = txw * nx + tyw * ny;
+        o->Tfv[2 * k] = v0 * A;
+        o->Tfv[2 * k + 1] = v1 * A;
+    }
+    for (int c = 0; c < nc; c++) { /* rans_P_Solver (:923-966) and SolveTotalTFlux (:969-1013) */
+        const double* gr = o->grad + 8 * c;
+        double ux = gr[4], uy = gr[5], vx = gr[6], vy = gr[7];
+        double f1 = o->F1[c];
+        double rdiv = dot2(o->TG[4 * c], o->TG[4 * c + 1], o->TG[4 * c + 2], o->TG[4 * c + 3]);
+        double cw = f1 * sst_cw1 + (1.0 - f1) * sst_cw2;
+        double beta = f1 * sst_beta1 + (1.0 - f1) * sst_beta2;
+        double rho = o->U[4 * c], k = o->T[2 * c], w = o->T[2 * c + 1], mt = o->mut[c];
+        double d0 = 2.0 / 3.0 * ((ux - vy) * (ux - vy));
+        double d1 = (uy + vx) * (uy + vx);
+        double d2 = 2.0 / 3.0 * rho * k * (ux + vy);
+        double P = (d0 + d1) * mt - d2;
+        double q0 = P - sst_bstar * rho * k * w;
+        double q1 = cw * rho * P / mt - beta * rho * w * w + 2 * (1 - f1) * rho * sst_sw2 / w * rdiv;
+        if (o->coupled) { /* sum(Fc - Fv) - Q vol: the source with the sign of dW = -R/D */
+            o->TR[2 * c] = -(q0 * o->vol[c]);
+            o->TR[2 * c + 1] = -(q1 * o->vol[c]);
+        } else { /* as written (:1001-1002) */
+            o->TR[2 * c] = q0 * o->vol[c];
+            o->TR[2 * c + 1] = q1 * o->vol[c];
+        }
+    }
+    for (int k = 0; k < ne; k++) {
+        int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+        for (int q = 0; q < 2; q++) {
+            o->TR[2 * l + q] += o->Tfc[2 * k + q] - o->Tfv[2 * k + q];
+            if (r >= 0) o->TR[2 * r + q] -= o->Tfc[2 * k + q] - o->Tfv[2 * k + q];
+        }
+    }
+}
+
+/* The reference's functions one by one (no coupling): SolveTurbulenceEquation
+ * on the current residual's arrays. */
+void orc_sst_equation(orc_t* o) { sst_equation(o); }
+
+/* SSTkomegaModel::SolveDiag (:170-192), after SolveTime */
+void orc_sst_diag(orc_t* o) {
+    for (int c = 0; c < o->ncell; c++) {
+        double OMEGAN = 1.5, vol = o->vol[c];
+        double diag = vol / o->dt[c] + 0.5 * OMEGAN * o->specc[c] + o->specv[c];
+        o->TD[2 * c] = diag + 2.0 * sst_bstar * o->T[2 * c + 1] * vol;
+        double gv = dot2(o->TG[4 * c], o->TG[4 * c + 1], o->TG[4 * c + 2], o->TG[4 * c + 3]);
+        double f1 = o->F1[c];
+        double beta = f1 * sst_beta1 + (1 - f1) * sst_beta2;
+        double w = o->T[2 * c + 1];
+        o->TD[2 * c + 1] = diag + vol * fabs(2.0 * beta * w + 2.0 * sst_sw2 * (1 - f1) * gv / (w * w));
+    }
+}
+
+/* initializeConsData + UpdatePrimitiveVariables (:97-109, :194-223) as the
+ * reference runs them on its own conservative copy: k, omega = W / rho and
+ * mu_t = a1 W_k / max(a1 W_omega / rho, F2 |dv/dx - du/dy|). */
+void orc_sst_update_mut(orc_t* o) {
+    for (int c = 0; c < o->ncell; c++) {
+        double rho = o->U[4 * c];
+        double w0 = o->T[2 * c] * rho, w1 = o->T[2 * c + 1] * rho;
+        o->T[2 * c] = w0 / rho;
+        o->T[2 * c + 1] = w1 / rho;
+        double curl = fabs(o->grad[8 * c + 6] - o->grad[8 * c + 5]);
+        double h = dmax(sst_a1 * w1 / rho, o->F2[c] * curl);
+        o->mut[c] = sst_a1 * w0 / h;
+    }
+}
+
+/* SSTkomegaModel::SolveDF + ConservativeParam2ConvectiveFlux + SolveViscousFlux
+ * (:251-474) for cell i, face k, with the departures listed above: the
+ * neighbour's flow state W_j + dW_j, its k, omega pair and increment, and the
+ * neighbour passed to the viscous part on both sides. */
+static void sst_solve_df(const orc_t* o, int i, int k, const double* dWf, const double* dWt, int fb, double* DF) {
+    int l = o->lr[2 * k], r = o->lr[2 * k + 1];
+    int j, left;
+    DF[0] = 0; DF[1] = 0;
+    if (i == l) {
+        if (!(r >= 0 && (int)(r < l) == fb)) return;
+        j = r; left = 1;
+    } else {
+        if (!((int)(l < r) == fb)) return;
+        j = l; left = 0;
+    }
+    double w0[4], wp[4], t0[2], dt[2], tp[2];
+    for (int m = 0; m < 4; m++) { w0[m] = o->W[4 * j + m]; wp[m] = w0[m] + dWf[4 * j + m]; }
+    for (int m = 0; m < 2; m++) { t0[m] = o->Tw[2 * j + m]; dt[m] = dWt[2 * j + m]; tp[m] = t0[m] + dt[m]; }
+    double nx = o->nrm[2 * k], ny = o->nrm[2 * k + 1], A = o->area[k];
+    double vn0 = dot2(w0[2] / w0[0], w0[3] / w0[0], nx, ny);
+    double vnp = dot2(wp[2] / wp[0], wp[3] / wp[0], nx, ny);
+    const double* uj = o->U + 4 * j;
+    double lx = o->cen[2 * j] - o->cen[2 * i], ly = o->cen[2 * j + 1] - o->cen[2 * i + 1];
+    double vn = dot2(uj[2], uj[3], nx, ny);
+    double c = sqrt(Gamma * uj[1] / uj[0]);
+    double rA = 1.5 * (fabs(vn) + c);
+    rA += dmax(4 / (3 * uj[0]), Gamma / uj[0]) * mpr_cell(o, i) / sqrt(dot2(lx, ly, lx, ly));
+    for (int m = 0; m < 2; m++) {
+        double fc = t0[m] * vn0, fcp = tp[m] * vnp;
+        double dfc = left ? (fcp - fc) : (fc - fcp);
+        DF[m] = 0.5 * (dfc - rA * dt[m]) * A;
+    }
+}
+
+/* The turbulence LU-SGS sweeps of a coupled step (LUSGSIntegrator's serial
+ * sweeps, LUSGS_Integrator.cpp:492-560, with two equations), after the flow's
+ * sweeps and before its update. */
+static void sst_step_sweeps(orc_t* o) {
+    orc_sst_diag(o);
+    double DF[2];
+    for (int c = 0; c < o->ncell; c++) {
+        double s[2] = {0, 0};
+        for (int e = 0; e < o->cne[c]; e++) {
+            sst_solve_df(o, c, o->ce[4 * c + e], o->dW1, o->TdW1, 1, DF);
+            s[0] += DF[0]; s[1] += DF[1];
+        }
+        for (int m = 0; m < 2; m++) o->TdW1[2 * c + m] = (-o->TR[2 * c + m] - s[m]) / o->TD[2 * c + m];
+    }
+    for (int c = o->ncell - 1; c >= 0; c--) {
+        double s[2] = {0, 0};
+        for (int e = 0; e < o->cne[c]; e++) {
+            sst_solve_df(o, c, o->ce[4 * c + e], o->dW, o->TdW, 0, DF);
+            s[0] += DF[0]; s[1] += DF[1];
+        }
+        for (int m = 0; m < 2; m++) o->TdW[2 * c + m] = o->TdW1[2 * c + m] - s[m] / o->TD[2 * c + m];
+    }
+}
+
+/* W_t += dW_t, then k, omega = W_t / rho with the flow's updated rho, floored
+ * at 1e-4 of the freestream values, and mu_t from them (:194-223). */
+static void sst_step_update(orc_t* o) {
+    const double kmin = 1e-4 * o->sst_k, wmin = 1e-4 * o->sst_w;
+    for (int c = 0; c < o->ncell; c++) {
+        double rho = o->U[4 * c];
+        double w0 = o->Tw[2 * c] + o->TdW[2 * c], w1 = o->Tw[2 * c + 1] + o->TdW[2 * c + 1];
+        double k = w0 / rho, w = w1 / rho;
+        if (!(k >= kmin)) { k = kmin; w0 = rho * kmin; }
+        if (!(w >= wmin)) { w = wmin; w1 = rho * wmin; }
+        o->Tw[2 * c] = w0;
+        o->Tw[2 * c + 1] = w1;
+        o->T[2 * c] = k;
+        o->T[2 * c + 1] = w;
+        double curl = fabs(o->grad[8 * c + 6] - o->grad[8 * c + 5]);
+        double h = dmax(sst_a1 * w1 / rho, o->F2[c] * curl);
+        o->mut[c] = sst_a1 * w0 / h;
+    }
+}
+
+/* SST arrays by id (the CFD_FIELD_SST_* numbering of include/cfdgb.h) */
+double* orc_sst_field(orc_t* o, int which) {
+    switch (which) {
+        case 21: return o->T;
+        case 22: return o->Tf;
+        case 23: return o->TG;
+        case 24: return o->F1;
+        case 25: return o->F2;
+        case 26: return o->mut;
+        case 27: return o->mutf;
+        case 28: return o->Tfc;
+        case 29: return o->Tfv;
+        case 30: return o->TR;
+        case 31: return o->TD;
+        case 40: return o->Tw;
+        case 41: return o->TdW1;
+        case 42: return o->TdW;
+        default: return 0;
+    }
 }
 
 /* Wall force of the last residual evaluation (Fx, Fy): not in the reference,

@@ -47,7 +47,7 @@ def test_header_constants_match_bindings():
     from tmp_gb300 import abi
 
     d = _defines()
-    pairs = {"CFD_FLOW_EULER": abi.FLOW_EULER, "CFD_FLOW_LAMINAR": abi.FLOW_LAMINAR,
+    pairs = {"CFD_FLOW_EULER": abi.FLOW_EULER, "CFD_FLOW_LAMINAR": abi.FLOW_LAMINAR, "CFD_FLOW_SST": abi.FLOW_SST,
              "CFD_ADV_RK5": abi.ADV_RK5, "CFD_ADV_LUSGS": abi.ADV_LUSGS,
              "CFD_PREC_FP64": abi.PREC_FP64, "CFD_PREC_FP32": abi.PREC_FP32,
              "CFD_PREC_MIXED": abi.PREC_MIXED, "CFD_PREC_MIXFF": abi.PREC_MIXFF}

@@ -19,7 +19,7 @@ OK = 0
 ERR = {-1: "ARG", -2: "IO", -3: "MESH", -4: "CUDA", -5: "PSTAR", -6: "NONPHYSICAL", -7: "TIMEOUT",
        -8: "STATE", -9: "WALLTAN"}
 BC_WALL, BC_FARFIELD = -2, -3
-FLOW_EULER, FLOW_LAMINAR = 0, 1
+FLOW_EULER, FLOW_LAMINAR, FLOW_SST = 0, 1, 2
 ADV_RK5, ADV_LUSGS = 0, 1
 PREC_FP64, PREC_FP32, PREC_MIXED, PREC_MIXFF = 0, 1, 2, 3
 FIELD = dict(U=0, W=1, R=2, GRAD=3, PHI=4, SPEC_C=5, SPEC_V=6, DT=7, DIAG=8, DW1=9, DW=10, GRADT=11, MU=12,
@@ -146,6 +146,7 @@ def lib() -> C.CDLL:
         "cfd_sst_freestream": (C.c_int, [vp, C.c_int, dp]),
         "cfd_sst_residual": (C.c_int, [vp]),
         "cfd_sst_update_mut": (C.c_int, [vp]),
+        "cfd_sst_set_inflow": (C.c_int, [vp, C.c_double, C.c_double]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -650,6 +651,17 @@ def sst_enable(case: "Case") -> np.ndarray:
     check(lib().cfd_sst_enable(case.h))
     out = np.zeros(3)
     check(lib().cfd_sst_freestream(case.h, 0, _dptr(out)))
+    return out
+
+
+def sst_set_inflow(case: "Case", intensity: float, viscosity_ratio: float):
+    """Freestream turbulence intensity and mu_t / mu of the SST model (the reference: 0.01, 0.035)."""
+    check(lib().cfd_sst_set_inflow(case.h, float(intensity), float(viscosity_ratio)))
+
+
+def sst_freestream(case: "Case", mesh: int = 0) -> np.ndarray:
+    out = np.zeros(3)
+    check(lib().cfd_sst_freestream(case.h, int(mesh), _dptr(out)))
     return out
 
 

@@ -13,6 +13,7 @@ namespace cfdgb {
 struct DevArrays {
     int nc = 0, nf = 0, nn = 0, nmesh = 0;
     int resid32 = 0;             // 1 while the residual runs in binary32 (the FP32 form)
+    int turb = 0;                // 1 when the SST k-omega model is coupled into every step (CFD_FLOW_SST)
     int residq = 0;              // 1 while the residual runs in float-float (the MIXFF form)
     // topology
     int2* lr = nullptr;          // [nf]
@@ -66,6 +67,17 @@ struct DevArrays {
     double* sstFv = nullptr;     // [2*nf] viscous face flux
     double* sstR = nullptr;      // [2*nc] residual
     double* sstD = nullptr;      // [2*nc] LU-SGS diagonal
+    // coupled SST LU-SGS (CFD_FLOW_SST; k_sst.cu)
+    double* sstW = nullptr;      // [2*nc] rho k, rho omega: the turbulence equations' conservative state
+    double* sstDW1 = nullptr;    // [2*nc] forward-sweep increment
+    double* sstDW = nullptr;     // [2*nc] backward-sweep increment
+    double* sstFcs = nullptr;    // [8*nc] per (cell, slot): the neighbour's convective flux W_t,j Vn(W_j), 2 values
+    double* sstRA = nullptr;     // [4*nc] per (cell, slot): r_A of SolveViscousFlux
+    double* sstVnp = nullptr;    // [4*nc] per (cell, slot): Vn(W_j + dW_j) with the flow's increment of that sweep
+    double* sstDinv = nullptr;   // [2*nc] 1 / diagonal (the binary32 sweep)
+    float2* sstDW1f = nullptr;   // [nc] binary32 copies published by the binary32 sweep
+    float2* sstDWf = nullptr;    // [nc]
+    int sst_grid = 0;            // co-resident blocks of the turbulence sweeps
     float* omega = nullptr;      // [nc] relaxation of the last learned update
     float* omega_mean = nullptr; // [nmesh] its mean per mesh
     int* mlp_samples = nullptr;  // cells the network is evaluated on, mesh by mesh
@@ -190,6 +202,17 @@ void launch_wall_force(const DevArrays& d, const LaunchCfg& L, bool viscous, int
 // ---- k_sst.cu (compiled with -fmad=false) ----
 void launch_sst_residual(const DevArrays& d, const LaunchCfg& L);
 void launch_sst_update_mut(const DevArrays& d, const LaunchCfg& L);
+// one pass of the coupled model's residual: 0 face values, 1 gradients + F1/F2,
+// 2 face fluxes, 3 residual (sum(Fc - Fv) - Q vol) and diagonal
+void launch_sst_stage(const DevArrays& d, const LaunchCfg& L, int stage);
+// the turbulence LU-SGS sweeps of a coupled step (after the flow's sweeps):
+// per-slot constants, forward and backward dataflow sweeps, binary64 or binary32
+cudaError_t launch_sst_sweeps(const DevArrays& d, const LaunchCfg& L, bool fp32);
+// W_t += dW_t, k and omega from the updated rho (floored), mu_t (after the flow's update)
+void launch_sst_update(const DevArrays& d, const LaunchCfg& L);
+// W_t = rho (k, omega) from the current U and k, omega
+void launch_sst_cons(const DevArrays& d, const LaunchCfg& L);
+int sst_sweep_max_grid(int blocks_per_sm);
 // ---- k_fp32.cu ----
 void launch_residual_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);

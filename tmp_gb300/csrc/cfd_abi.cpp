@@ -123,7 +123,9 @@ struct cfd_case_s {
     std::vector<int2> h_lr;
     std::vector<int> h_order[2];     // merged level orders, forward and backward
     int chain_cap = 0;               // co-resident blocks of the chain sweep (0: not queried)
-    bool viscous() const { return p.flow == CFD_FLOW_LAMINAR; }
+    bool viscous() const { return p.flow == CFD_FLOW_LAMINAR || p.flow == CFD_FLOW_SST; }
+    bool turb() const { return p.flow == CFD_FLOW_SST; }  // the SST model coupled into every step
+    double sst_tu = 0.01, sst_ratio = 0.035;  // freestream turbulence intensity and mu_t / mu
     bool fp32() const { return p.precision == CFD_PREC_FP32; }
     // binary64 state with the binary32 sweep: MIXED (binary64 residual) and MIXFF (float-float residual)
     bool mixed() const { return p.precision == CFD_PREC_MIXED || p.precision == CFD_PREC_MIXFF; }
@@ -142,6 +144,10 @@ struct cfd_case_s {
     }
 };
 
+static void sst_alloc(cfd_case_s* c);
+static void sst_freestream(cfd_case_s* c);
+static void sst_init_state(cfd_case_s* c);
+
 namespace {
 
 void free_case(cfd_case_s* c) {
@@ -156,7 +162,8 @@ void free_case(cfd_case_s* c) {
                     d.sstMut, d.sstMutf, d.sstFc, d.sstFv, d.sstR, d.sstD, d.chain_ptr[0], d.chain_ptr[1],
                     d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_jenc[0], d.chain_jenc[1], d.chain_stage[0],
                     d.chain_stage[1], d.chain_posb, d.chain_dF, d.Uq, d.gradq, d.phiq, d.speccq, d.specvq, d.gradTq,
-                    d.muq, d.Ueq, d.fspecq, d.mueq, d.Fcq, d.Fvq, d.fg0q, d.fg1q, d.fvisq, d.cgeoq};
+                    d.muq, d.Ueq, d.fspecq, d.mueq, d.Fcq, d.Fvq, d.fg0q, d.fg1q, d.fvisq, d.cgeoq, d.sstW, d.sstDW1,
+                    d.sstDW, d.sstFcs, d.sstRA, d.sstVnp, d.sstDinv, d.sstDW1f, d.sstDWf};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -166,15 +173,27 @@ void free_case(cfd_case_s* c) {
 // Integrator steps -------------------------------------------------------------
 // The mixed form's binary64 residual is the contracted build (k_fp64fma.cu);
 // the plain form's reproduces the reference's roundings (k_fp64.cu).
+void launch_pass(const DevArrays& d, const LaunchCfg& L, bool visc, bool f32, int which, int first_order,
+                 bool mixed, bool ffq);
 void residual_pass(cfd_case_s* c) {
     auto L = c->L();
+    if (c->turb()) {
+        // ViscousFlow2D::preprocessAdvance with the model (ViscousFlow2D.h:163-190): the
+        // face states (with each face's mu_t), the turbulence face values, the gradients
+        // (with mu and F1 / F2 of the model), then the flow's and the model's face fluxes
+        for (int which = 0; which < 3; which++) {
+            launch_pass(c->d, L, true, false, which, c->p.first_order, c->mixed(), false);
+            launch_sst_stage(c->d, L, which);
+        }
+        return;
+    }
     if (c->fp32()) launch_residual_fp32(c->d, L, c->viscous(), c->p.first_order);
     else if (c->ffres()) launch_residual_ff(c->d, L, c->viscous(), c->p.first_order);
     else if (c->mixed()) launch_residual_fp64_contracted(c->d, L, c->viscous(), c->p.first_order);
     else launch_residual_fp64(c->d, L, c->viscous(), c->p.first_order);
 }
 void launch_pass(const DevArrays& d, const LaunchCfg& L, bool visc, bool f32, int which, int first_order,
-                 bool mixed = false, bool ffq = false) {
+                 bool mixed, bool ffq) {
     if (f32) launch_residual_fp32(d, L, visc, first_order, which);
     else if (ffq) launch_residual_ff(d, L, visc, first_order, which);
     else if (mixed) launch_residual_fp64_contracted(d, L, visc, first_order, which);
@@ -443,10 +462,14 @@ void lusgs_step(cfd_case_s* c) {
         ck(cudaMemcpyAsync(d.dWprev, d.dW, sizeof(d4) * d.nc, cudaMemcpyDeviceToDevice, c->stream), "dWprev");
     residual_pass(c);
     update_pass(c, 2 /*UPD_LUSGS*/, c->p.cfl, 0, 0.0);
+    if (c->turb()) launch_sst_stage(d, L, 3);  // the model's residual and diagonal (needs dt and the radii)
     sweeps(c, true);
     sweeps(c, false);
+    // the turbulence sweeps read the flow's W before the update and its increments of this step
+    if (c->turb()) ck(launch_sst_sweeps(d, L, c->fast_sweep()), "cooperative turbulence sweep launch");
     if (c->mlp) learned_update(c);
     else launch_lusgs_update(d, L, c->fp32());
+    if (c->turb()) launch_sst_update(d, L);  // with rho after the flow's update
 }
 
 void one_step(cfd_case_s* c) {
@@ -563,7 +586,11 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
     for (int i = 0; i < nmesh; i++)
         if (!meshes[i]) return fail(CFD_ERR_ARG, "null mesh in list");
     const cfd_params_t& P = *params;
-    if (P.flow != CFD_FLOW_EULER && P.flow != CFD_FLOW_LAMINAR) return fail(CFD_ERR_ARG, "Undefined Flow Type");
+    if (P.flow != CFD_FLOW_EULER && P.flow != CFD_FLOW_LAMINAR && P.flow != CFD_FLOW_SST)
+        return fail(CFD_ERR_ARG, "Undefined Flow Type");
+    if (P.flow == CFD_FLOW_SST && (P.advance != CFD_ADV_LUSGS ||
+                                   (P.precision != CFD_PREC_FP64 && P.precision != CFD_PREC_MIXED)))
+        return fail(CFD_ERR_ARG, "the coupled SST model runs with LU-SGS in the FP64 or MIXED form");
     if (P.advance != CFD_ADV_RK5 && P.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_ARG, "Undefined Advance Type");
     if (P.precision < CFD_PREC_FP64 || P.precision > CFD_PREC_MIXFF) return fail(CFD_ERR_ARG, "unknown precision");
     if (P.sweep_mode < 0 || P.sweep_mode > 6) return fail(CFD_ERR_ARG, "unknown sweep mode");
@@ -577,7 +604,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
     try {
         c->nmesh = nmesh;
         c->p = P;
-        bool visc = P.flow == CFD_FLOW_LAMINAR;
+        bool visc = P.flow == CFD_FLOW_LAMINAR || P.flow == CFD_FLOW_SST;
         c->coff.assign(nmesh + 1, 0);
         c->foff.assign(nmesh + 1, 0);
         c->noff.assign(nmesh + 1, 0);
@@ -767,6 +794,12 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             ck(cudaMemcpyAsync(d.wall_faces, wfaces.data(), wfaces.size() * sizeof(int), cudaMemcpyHostToDevice, s), "upload");
         if (!wb.empty())
             ck(cudaMemcpyAsync(d.wblocks, wb.data(), wb.size() * sizeof(int4), cudaMemcpyHostToDevice, s), "upload");
+        if (c->turb()) {
+            sst_alloc(c);
+            d.turb = 1;
+            d.sst_grid = sst_sweep_max_grid(P.sweep_blocks_per_sm > 0 ? P.sweep_blocks_per_sm : 4);
+            sst_freestream(c);
+        }
         auto L = c->L();
         launch_geometry(d, L);
         launch_wall_distance(d, L);
@@ -814,6 +847,71 @@ int cfd_set_cfl(cfd_case_t c, double cfl) {
 
 // Every mesh's freestream into U and W; synchronises the stream (the host
 // staging vector must outlive the copy).
+}  // extern "C"
+
+// SST k-omega arrays: the model's (k_sst.cu residual) and, for a coupled case,
+// the turbulence LU-SGS state, increments and per-slot constants.
+static void sst_alloc(cfd_case_s* c) {
+    DevArrays& d = c->d;
+    const size_t nc = d.nc, nf = d.nf;
+    if (!c->sst) {
+        dalloc(&d.sstT, 2 * nc); dalloc(&d.sstTf, 2 * nf); dalloc(&d.sstG, 4 * nc);
+        dalloc(&d.sstF1, nc); dalloc(&d.sstF2, nc); dalloc(&d.sstMut, nc); dalloc(&d.sstMutf, nf);
+        dalloc(&d.sstFc, 2 * nf); dalloc(&d.sstFv, 2 * nf); dalloc(&d.sstR, 2 * nc); dalloc(&d.sstD, 2 * nc);
+        c->sst = true;
+    }
+    if (c->turb() && !d.sstW) {
+        dalloc(&d.sstW, 2 * nc); dalloc(&d.sstDW1, 2 * nc); dalloc(&d.sstDW, 2 * nc);
+        dalloc(&d.sstFcs, 8 * nc); dalloc(&d.sstRA, 4 * nc); dalloc(&d.sstVnp, 4 * nc);
+        dalloc(&d.sstDinv, 2 * nc); dalloc(&d.sstDW1f, nc); dalloc(&d.sstDWf, nc);
+        ck(cudaMemsetAsync(d.sstDW, 0, 2 * nc * sizeof(double), c->stream), "memset");
+        ck(cudaMemsetAsync(d.sstDW1, 0, 2 * nc * sizeof(double), c->stream), "memset");
+    }
+}
+
+// Freestream k, omega and mu_t of every mesh: TopologyHolderStrategy::
+// set_fs_variable2 (.cpp:325-352) then SSTkomegaModel::InitializeturbulenceVariable
+// (SSTKWStrategy.h:582-613), with Gamma = 1.4, R = 287, L = 1, and the
+// turbulence intensity (the reference: 0.01) and mu_t / mu (the reference:
+// 0.035) as the case's settings: k = 1.5 (tu |V|)^2, omega = rho k / (ratio mu).
+static void sst_freestream(cfd_case_s* c) {
+    for (int m = 0; m < c->nmesh; m++) {
+        const cfd_freestream_t& fs = c->fs_in[m];
+        const double Gamma = 1.4, R = 287.0, L = 1.0, tu = c->sst_tu, ratio = c->sst_ratio;
+        const double fs_soundSpeed = sqrt(Gamma * fs.pressure / fs.density);
+        const double fs_Temperature = fs.pressure / (R * fs.density);
+        const double fs_mu = 1.458e-6 * pow(fs_Temperature, 1.5) / (fs_Temperature + 110.5);
+        const double fs_mut = fs_mu * ratio;
+        const double fsnd_mut = fs_mut / fs_mu * sqrt(Gamma) * fs.mach / fs.reynolds;
+        const double k = 1.5 * fs.mach * fs_soundSpeed * tu * fs.mach * fs_soundSpeed * tu;
+        const double w = fs.density * k / (ratio * fs_mu);
+        c->prm[m].sst_k = Gamma * k / (fs_soundSpeed * fs_soundSpeed);
+        c->prm[m].sst_w = sqrt(Gamma) * L * w / fs_soundSpeed;
+        c->prm[m].sst_mut = fsnd_mut;
+    }
+    ck(cudaMemcpyAsync(c->d.prm, c->prm.data(), c->nmesh * sizeof(MeshPrm), cudaMemcpyHostToDevice, c->stream),
+       "upload");
+}
+
+// Uniform freestream k, omega and mu_t (and, coupled, W_t = rho (k, omega))
+static void sst_init_state(cfd_case_s* c) {
+    DevArrays& d = c->d;
+    std::vector<double> t(2 * (size_t)d.nc), mut((size_t)d.nc);
+    for (int m = 0; m < c->nmesh; m++)
+        for (int k = c->coff[m]; k < c->coff[m + 1]; k++) {
+            t[2 * (size_t)k] = c->prm[m].sst_k;
+            t[2 * (size_t)k + 1] = c->prm[m].sst_w;
+            mut[k] = c->prm[m].sst_mut;
+        }
+    ck(cudaMemcpyAsync(d.sstT, t.data(), t.size() * 8, cudaMemcpyHostToDevice, c->stream), "upload");
+    ck(cudaMemcpyAsync(d.sstMut, mut.data(), mut.size() * 8, cudaMemcpyHostToDevice, c->stream), "upload");
+    if (c->turb()) launch_sst_cons(d, c->L());
+    ck(cudaGetLastError(), "launch");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+}
+
+extern "C" {
+
 static void upload_freestream(cfd_case_t c) {
     std::vector<d4> u(c->d.nc);
     for (int m = 0; m < c->nmesh; m++) {
@@ -826,6 +924,7 @@ static void upload_freestream(cfd_case_t c) {
     if (c->fp32()) launch_to_fp32(c->d, L, false);
     ck(cudaGetLastError(), "launch");
     ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (c->turb()) sst_init_state(c);
 }
 
 int cfd_init_freestream(cfd_case_t c) {
@@ -913,6 +1012,7 @@ int cfd_step_io(cfd_case_t c, const double* host_u, int nsteps, int which, doubl
         ck(cudaMemcpyAsync(c->d.U, host_u, (size_t)c->d.nc * 32, cudaMemcpyHostToDevice, c->stream), "upload");
         launch_cons_from_prim(c->d, L, 0, c->d.nc);
         if (c->fp32()) launch_to_fp32(c->d, L, false);
+        if (c->turb()) launch_sst_cons(c->d, L);
         ck(cudaGetLastError(), "launch");
     }
     if (nsteps > 0) {
@@ -1332,6 +1432,8 @@ int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host) {
         const int w = which == CFD_FIELD_SST_T ? 2 : 1;
         double* dst = which == CFD_FIELD_SST_T ? c->d.sstT : c->d.sstMut;
         ck(cudaMemcpyAsync(dst + (size_t)off * w, host, (size_t)n * w * 8, cudaMemcpyHostToDevice, c->stream), "upload");
+        if (c->turb() && which == CFD_FIELD_SST_T) launch_sst_cons(c->d, c->L());  // W_t = rho (k, omega)
+        ck(cudaGetLastError(), "launch");
         ck(cudaStreamSynchronize(c->stream), "sync");
         return CFD_OK;
         ABI_CATCH
@@ -1343,6 +1445,7 @@ int cfd_put_field(cfd_case_t c, int mesh, int which, const double* host) {
     auto L = c->L();
     launch_cons_from_prim(c->d, L, off, off + n);
     if (c->fp32()) launch_to_fp32(c->d, L, false);
+    if (c->turb()) launch_sst_cons(c->d, L);  // the turbulence equations' W_t = rho (k, omega) with the new rho
     ck(cudaGetLastError(), "launch");
     return CFD_OK;
     ABI_CATCH
@@ -1580,44 +1683,24 @@ extern "C" {
 int cfd_sst_enable(cfd_case_t c) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
     if (!c->viscous() || c->fp32() || c->ffres())
-        return fail(CFD_ERR_STATE, "the SST model needs a laminar case with the binary64 residual (FP64 or MIXED)");
+        return fail(CFD_ERR_STATE, "the SST model needs a viscous case with the binary64 residual (FP64 or MIXED)");
     ABI_TRY
-    DevArrays& d = c->d;
-    if (!c->sst) {
-        const size_t nc = d.nc, nf = d.nf;
-        dalloc(&d.sstT, 2 * nc); dalloc(&d.sstTf, 2 * nf); dalloc(&d.sstG, 4 * nc);
-        dalloc(&d.sstF1, nc); dalloc(&d.sstF2, nc); dalloc(&d.sstMut, nc); dalloc(&d.sstMutf, nf);
-        dalloc(&d.sstFc, 2 * nf); dalloc(&d.sstFv, 2 * nf); dalloc(&d.sstR, 2 * nc); dalloc(&d.sstD, 2 * nc);
-        c->sst = true;
-    }
-    // Freestream k, omega and mu_t: TopologyHolderStrategy::set_fs_variable2
-    // (.cpp:325-352) then SSTkomegaModel::InitializeturbulenceVariable
-    // (SSTKWStrategy.h:582-613), with Gamma = 1.4, R = 287, L = 1.
-    for (int m = 0; m < c->nmesh; m++) {
-        const cfd_freestream_t& fs = c->fs_in[m];
-        const double Gamma = 1.4, R = 287.0, L = 1.0;
-        const double fs_soundSpeed = sqrt(Gamma * fs.pressure / fs.density);
-        const double fs_Temperature = fs.pressure / (R * fs.density);
-        const double fs_mu = 1.458e-6 * pow(fs_Temperature, 1.5) / (fs_Temperature + 110.5);
-        const double fs_mut = fs_mu * 0.035;
-        const double fsnd_mut = fs_mut / fs_mu * sqrt(Gamma) * fs.mach / fs.reynolds;
-        const double k = 1.5 * fs.mach * fs_soundSpeed * 0.01 * fs.mach * fs_soundSpeed * 0.01;
-        const double w = fs.density * k / (0.035 * fs_mu);
-        c->prm[m].sst_k = Gamma * k / (fs_soundSpeed * fs_soundSpeed);
-        c->prm[m].sst_w = sqrt(Gamma) * L * w / fs_soundSpeed;
-        c->prm[m].sst_mut = fsnd_mut;
-    }
-    ck(cudaMemcpyAsync(d.prm, c->prm.data(), c->nmesh * sizeof(MeshPrm), cudaMemcpyHostToDevice, c->stream), "upload");
-    // uniform freestream turbulence and eddy viscosity
-    std::vector<double> t(2 * (size_t)d.nc), mut((size_t)d.nc);
-    for (int m = 0; m < c->nmesh; m++)
-        for (int k = c->coff[m]; k < c->coff[m + 1]; k++) {
-            t[2 * (size_t)k] = c->prm[m].sst_k;
-            t[2 * (size_t)k + 1] = c->prm[m].sst_w;
-            mut[k] = c->prm[m].sst_mut;
-        }
-    ck(cudaMemcpyAsync(d.sstT, t.data(), t.size() * 8, cudaMemcpyHostToDevice, c->stream), "upload");
-    ck(cudaMemcpyAsync(d.sstMut, mut.data(), mut.size() * 8, cudaMemcpyHostToDevice, c->stream), "upload");
+    sst_alloc(c);
+    sst_freestream(c);
+    sst_init_state(c);
+    c->drop_graph();
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_sst_set_inflow(cfd_case_t c, double intensity, double viscosity_ratio) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (!(intensity > 0) || !(viscosity_ratio > 0)) return fail(CFD_ERR_ARG, "intensity and ratio must be positive");
+    if (!c->sst) return fail(CFD_ERR_STATE, "call cfd_sst_enable first (or create a CFD_FLOW_SST case)");
+    ABI_TRY
+    c->sst_tu = intensity;
+    c->sst_ratio = viscosity_ratio;
+    sst_freestream(c);
     ck(cudaStreamSynchronize(c->stream), "sync");
     c->drop_graph();
     return CFD_OK;

@@ -20,6 +20,8 @@
 // Every per-cell sum visits the cell's faces in ascending face index, the order
 // in which the reference's face loops reach that cell, so sums round the same.
 #pragma once
+#include <type_traits>
+
 #include "fv_device.cuh"
 
 namespace cfdgb {
@@ -33,12 +35,19 @@ __device__ __forceinline__ int code_face(int code) { return (code > 0 ? code : -
 // face_state: BoundaryStrategy::HandleBoundary + the per-edge part of
 // solveSpectralRadius (Euler2D.cpp:242-267, ViscousFlow2D.cpp:220-253) and of
 // LaminarFluxStrategy::computeMu for edges.
+//
+// With the SST model coupled (mutc != null, binary64 only: ViscousFlow2D with
+// isLaminar() false, ViscousFlow2D.h:118-154) the face also gets its eddy
+// viscosity (ComputeTurbulenceViscousCoefficient's face loop,
+// SSTKWStrategy.h:749-777) into mutf, and the viscous spectral radius uses
+// mu/Pr + mu_t/Prt.
 template <class T, bool VISC, int CONTRACT = 0>
 __global__ void __launch_bounds__(256) k_face_state(int nf, const int2* __restrict__ lr, const int* __restrict__ fmesh,
                                                     const MeshPrm* __restrict__ prm, const v4<T>* __restrict__ fg0,
                                                     const v4<T>* __restrict__ U, v4<T>* __restrict__ Ue,
                                                     v2<T>* __restrict__ fspec, T* __restrict__ mue,
-                                                    unsigned* __restrict__ err) {
+                                                    unsigned* __restrict__ err, const T* __restrict__ mutc,
+                                                    T* __restrict__ mutf) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf) return;
     const T G = C<T>::gamma;
@@ -71,7 +80,18 @@ __global__ void __launch_bounds__(256) k_face_state(int nf, const int2* __restri
         MeshPrm m = prm[fmesh[f]];
         T mu = sutherland<T>(ue[1] / ue[0], m);
         mue[f] = mu;
-        s.y = smax(T(4) / (T(3.0) * ue[0]), G / ue[0]) * (mu / C<T>::pr) * A * A;
+        T mpr = mu / C<T>::pr;
+        if constexpr (std::is_same<T, double>::value) {
+            if (mutc) {
+                double mf;
+                if (e.y >= 0) mf = 0.5 * (mutc[e.x] + mutc[e.y]);
+                else if (e.y == BC_WALL) mf = 0.0;
+                else mf = dot2(ue[2], ue[3], nx, ny) > 0.0 ? mutc[e.x] : m.sst_mut;
+                mutf[f] = mf;
+                mpr = mu / C<T>::pr + mf / 0.9;
+            }
+        }
+        s.y = smax(T(4) / (T(3.0) * ue[0]), G / ue[0]) * mpr * A * A;
     }
     fspec[f] = s;
 }
@@ -182,13 +202,16 @@ __global__ void __launch_bounds__(256) k_cell_grad(
 // (HLLCFluxStrategy.h:35-100, HLLCFluxStrategy.cpp:4-170) and
 // LaminarFluxStrategy::computeFlux(int) (LaminarFluxStrategy.h:110-216).
 // Writes the convective and the viscous flux of each face separately so the
-// gather can add them in the reference's two-loop order.
+// gather can add them in the reference's two-loop order.  With the SST model
+// coupled (mutf != null, binary64 only) the viscous flux uses mu + mu_t and
+// mu/Pr + mu_t/Prt (getMuEdge / getMuOverPrEdge, ViscousFlow2D.h:128-145).
 template <class T, bool VISC, int CONTRACT = 0>
 __global__ void __launch_bounds__(256) k_face_flux(
     int nf, const int2* __restrict__ lr, const v4<T>* __restrict__ fg0, const v4<T>* __restrict__ fg1,
     const v4<T>* __restrict__ fvis, const v4<T>* __restrict__ U, const v4<T>* __restrict__ grad,
     const v4<T>* __restrict__ phi, const v4<T>* __restrict__ Ue, const T* __restrict__ mue,
-    const v2<T>* __restrict__ gradT, v4<T>* __restrict__ Fc, v4<T>* __restrict__ Fv, unsigned* __restrict__ err) {
+    const v2<T>* __restrict__ gradT, v4<T>* __restrict__ Fc, v4<T>* __restrict__ Fv, unsigned* __restrict__ err,
+    const T* __restrict__ mutf) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf) return;
     const T G = C<T>::gamma, GM1 = C<T>::gm1;
@@ -231,6 +254,14 @@ __global__ void __launch_bounds__(256) k_face_flux(
     if (!VISC) return;
     // viscous flux
     T mu = mue[f];
+    T mpr = mu / C<T>::pr;
+    if constexpr (std::is_same<T, double>::value) {
+        if (mutf) {
+            const double mt = mutf[f];
+            mpr = mu / C<T>::pr + mt / 0.9;
+            mu = mu + mt;
+        }
+    }
     T eff = T(2.0) / T(3.0) * mu;
     T g0x, g0y, g1x, g1y, gtx, gty;  // d(u)/dx,dy ; d(v)/dx,dy ; dT/dx,dy at the face
     if (e.y >= 0) {
@@ -260,8 +291,8 @@ __global__ void __launch_bounds__(256) k_face_flux(
     T txx = eff * (T(2.0) * g0x - g1y);
     T tyy = eff * (T(2.0) * g1y - g0x);
     T txy = mu * (g0y + g1x);
-    T qx = -G / GM1 * (mu / C<T>::pr) * gtx;
-    T qy = -G / GM1 * (mu / C<T>::pr) * gty;
+    T qx = -G / GM1 * mpr * gtx;
+    T qy = -G / GM1 * mpr * gty;
     v4<T> v;
     v.x = T(0.0);
     v.y = ((ve0 * txx + ve1 * txy - qx) * nx + (ve0 * txy + ve1 * tyy - qy) * ny) * A;
@@ -287,7 +318,8 @@ __global__ void __launch_bounds__(256) k_cell_update(
     int nc, const int4* __restrict__ cface, const d4* __restrict__ cgeo64, const v4<T>* __restrict__ Fc,
     const v4<T>* __restrict__ Fv, const T* __restrict__ specc, const T* __restrict__ specv, double cfl,
     int stage, double alpha, d4* __restrict__ R, d4* __restrict__ U64, d4* __restrict__ W, d4* __restrict__ W0,
-    double* __restrict__ dt, double* __restrict__ diag, v4<T>* __restrict__ Ulow, const float* __restrict__ cflmul) {
+    double* __restrict__ dt, double* __restrict__ diag, v4<T>* __restrict__ Ulow, const float* __restrict__ cflmul,
+    int turb) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     int4 cf = cface[c];
@@ -353,9 +385,11 @@ __global__ void __launch_bounds__(256) k_cell_update(
         }
     } else {
         // SolveTime + TopologyHolderStrategy::SolveDiag (TopologyHolderStrategy.cpp:190-215);
-        // an optional per-cell CFL multiplier (local CFL controller) scales the CFL
+        // an optional per-cell CFL multiplier (local CFL controller) scales the CFL.
+        // With the SST model coupled, SolveTime's turbulent branch (ViscousFlow2D.h:223-242):
+        // dt = CFL vol / (spec_c + 4 spec_v).
         double cl = cflmul ? cfl * (double)cflmul[c] : cfl;
-        double dtc = cl * vol / sc;
+        double dtc = turb ? cl * vol / (sc + 4.0 * (double)specv[c]) : cl * vol / sc;
         dt[c] = dtc;
         double OMEGAN = 1.5;
         double d = vol / dtc + 0.5 * OMEGAN * sc;

@@ -42,7 +42,8 @@ static void residualq(const DevArrays& d, const LaunchCfg& L, int first_order, i
     if (which < 0 || which == 0) {
         k_to_q4<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.U, d.Uq);
         k_face_state<ff, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fmesh, d.prm, d.fg0q, d.Uq, d.Ueq,
-                                                                    d.fspecq, d.mueq, d.err);
+                                                                    d.fspecq, d.mueq, d.err, (const ff*)nullptr,
+                                                                    (ff*)nullptr);
         *L.counter += 2;
     }
     if (which < 0 || which == 1) {
@@ -55,7 +56,7 @@ static void residualq(const DevArrays& d, const LaunchCfg& L, int first_order, i
     if (which < 0 || which == 2) {
         k_face_flux<ff, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fg0q, d.fg1q, d.fvisq, d.Uq, d.gradq,
                                                                    d.phiq, d.Ueq, d.mueq, d.gradTq, d.Fcq, d.Fvq,
-                                                                   d.err);
+                                                                   d.err, (const ff*)nullptr);
         *L.counter += 1;
     }
 }
@@ -68,7 +69,7 @@ template <bool V, int M>
 static void updateq(const DevArrays& d, const LaunchCfg& L, double cfl, int stage, double alpha) {
     k_cell_update<ff, V, M><<<nblk(d.nc, 256), 256, 0, L.stream>>>(
         d.nc, d.cface, d.cgeo, d.Fcq, d.Fvq, d.speccq, d.specvq, cfl, stage, alpha, d.R, d.U, d.W, d.W0, d.dt,
-        d.diag, (q4*)nullptr, d.cflmul);
+        d.diag, (q4*)nullptr, d.cflmul, 0);
     *L.counter += 1;
 }
 void launch_update_ff(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage,

@@ -13,7 +13,8 @@ template <bool V>
 static void residual32(const DevArrays& d, const LaunchCfg& L, int first_order, int which) {
     if (which < 0 || which == 0) {
         k_face_state<float, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fmesh, d.prm, d.fg0f, d.Uf,
-                                                                       d.Uef, d.fspecf, d.muef, d.err);
+                                                                       d.Uef, d.fspecf, d.muef, d.err,
+                                                                       (const float*)nullptr, (float*)nullptr);
         *L.counter += 1;
     }
     if (which < 0 || which == 1) {
@@ -26,7 +27,7 @@ static void residual32(const DevArrays& d, const LaunchCfg& L, int first_order, 
     if (which < 0 || which == 2) {
         k_face_flux<float, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fg0f, d.fg1f, d.fvisf, d.Uf,
                                                                       d.gradf, d.phif, d.Uef, d.muef, d.gradTf, d.Fcf,
-                                                                      d.Fvf, d.err);
+                                                                      d.Fvf, d.err, (const float*)nullptr);
         *L.counter += 1;
     }
 }
@@ -39,7 +40,7 @@ template <bool V, int M>
 static void update32(const DevArrays& d, const LaunchCfg& L, double cfl, int stage, double alpha) {
     k_cell_update<float, V, M><<<nblk(d.nc, 256), 256, 0, L.stream>>>(
         d.nc, d.cface, d.cgeo, d.Fcf, d.Fvf, d.speccf, d.specvf, cfl, stage, alpha, d.R, d.U, d.W, d.W0, d.dt, d.diag,
-        d.Uf, d.cflmul);
+        d.Uf, d.cflmul, 0);
     *L.counter += 1;
 }
 void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage,

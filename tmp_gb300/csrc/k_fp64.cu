@@ -129,7 +129,9 @@ template <bool V>
 static void residual64(const DevArrays& d, const LaunchCfg& L, int first_order, int which) {
     if (which < 0 || which == 0) {
         k_face_state<double, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fmesh, d.prm, d.fg0, d.U, d.Ue,
-                                                                        d.fspec, d.mue, d.err);
+                                                                        d.fspec, d.mue, d.err,
+                                                                        d.turb ? d.sstMut : nullptr,
+                                                                        d.turb ? d.sstMutf : nullptr);
         *L.counter += 1;
     }
     if (which < 0 || which == 1) {
@@ -140,7 +142,8 @@ static void residual64(const DevArrays& d, const LaunchCfg& L, int first_order, 
     }
     if (which < 0 || which == 2) {
         k_face_flux<double, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fg0, d.fg1, d.fvis, d.U, d.grad,
-                                                                       d.phi, d.Ue, d.mue, d.gradT, d.Fc, d.Fv, d.err);
+                                                                       d.phi, d.Ue, d.mue, d.gradT, d.Fc, d.Fv, d.err,
+                                                                       d.turb ? d.sstMutf : nullptr);
         *L.counter += 1;
     }
 }
@@ -153,7 +156,7 @@ template <bool V, int M>
 static void update64(const DevArrays& d, const LaunchCfg& L, double cfl, int stage, double alpha) {
     k_cell_update<double, V, M><<<nblk(d.nc, 256), 256, 0, L.stream>>>(
         d.nc, d.cface, d.cgeo, d.Fc, d.Fv, d.specc, d.specv, cfl, stage, alpha, d.R, d.U, d.W, d.W0, d.dt, d.diag,
-        (d4*)nullptr, d.cflmul);
+        (d4*)nullptr, d.cflmul, d.turb);
     *L.counter += 1;
 }
 void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage,
@@ -177,13 +180,25 @@ void launch_update_fp64(const DevArrays& d, const LaunchCfg& L, bool viscous, in
 //   backward: dW_i  = dW1_i - sum / D_i           (LUSGS_Integrator.cpp:526-560)
 // Cells of one level have no face between them, so they run in parallel and
 // the result equals the reference's serial sweep.
+// getMuOverPrCell (TopologyHolderStrategy.h:219-223; ViscousFlow2D.h:147-154):
+// mu/Pr, plus mu_t/Prt when the SST model is coupled (mut != null)
+template <class MuT>
+__device__ __forceinline__ double mu_over_pr(const MuT* mu, const double* mut, int i) {
+    return mut ? (double)mu[i] / 0.72 + mut[i] / 0.9 : (double)mu[i] / 0.72;
+}
+template <class MuT>
+__device__ __forceinline__ float mu_over_pr_f(const MuT* mu, const double* mut, int i) {
+    return mut ? (float)mu[i] / 0.72f + (float)mut[i] / 0.9f : (float)mu[i] / 0.72f;
+}
+
 template <bool VISC, bool FWD, class MuT>
 __global__ void __launch_bounds__(128) k_sweep(int begin, int end, const int* __restrict__ order,
                                                const int4* __restrict__ cface, const int2* __restrict__ lr,
                                                const d4* __restrict__ fg0, const d4* __restrict__ fvis,
                                                const d4* __restrict__ W, const d4* __restrict__ U,
                                                const MuT* __restrict__ mu, const d4* __restrict__ R,
-                                               const double* __restrict__ D, d4* dW1, d4* dW) {
+                                               const double* __restrict__ D, d4* dW1, d4* dW,
+                                               const double* __restrict__ mut) {
     int idx = begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= end) return;
     const double G = 1.4;
@@ -215,7 +230,7 @@ __global__ void __launch_bounds__(128) k_sweep(int begin, int end, const int* __
             double vn = dot2(uj[2], uj[3], nx, ny);
             double c = sqrt(G * uj[1] / uj[0]);
             double rA = 1.5 * (fabs(vn) + c);
-            if (VISC) rA += smax(4 / (3 * uj[0]), G / uj[0]) * ((double)mu[i] / 0.72) / sqrt(fvis[f].z);
+            if (VISC) rA += smax(4 / (3 * uj[0]), G / uj[0]) * mu_over_pr(mu, mut, i) / sqrt(fvis[f].z);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 double fv = rA * dw[k];
@@ -245,11 +260,11 @@ static void sweep_t(const DevArrays& d, const LaunchCfg& L, bool viscous, bool f
     const int* order = forward ? d.fwd_order : d.bwd_order;
     dim3 grid(nblk(n, 128));
     if (viscous) {
-        if (forward) k_sweep<true, true, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW);
-        else k_sweep<true, false, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW);
+        if (forward) k_sweep<true, true, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW, d.turb ? d.sstMut : nullptr);
+        else k_sweep<true, false, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW, d.turb ? d.sstMut : nullptr);
     } else {
-        if (forward) k_sweep<false, true, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW);
-        else k_sweep<false, false, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW);
+        if (forward) k_sweep<false, true, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW, d.turb ? d.sstMut : nullptr);
+        else k_sweep<false, false, MuT><<<grid, 128, 0, L.stream>>>(begin, end, order, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, mu, d.R, d.diag, d.dW1, d.dW, d.turb ? d.sstMut : nullptr);
     }
     *L.counter += 1;
 }
@@ -277,7 +292,7 @@ __global__ void __launch_bounds__(256) k_sweep_prep(int nc, const int4* __restri
                                                     const d4* __restrict__ W, const d4* __restrict__ U,
                                                     const MuT* __restrict__ mu, double* __restrict__ swfc,
                                                     double* __restrict__ swra, double* __restrict__ dW1,
-                                                    double* __restrict__ dW, int reset) {
+                                                    double* __restrict__ dW, int reset, const double* __restrict__ mut) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 4 * nc) return;
     if (reset) {  // the dataflow sweep's "not yet computed" marker (see k_sweep_flow)
@@ -301,7 +316,7 @@ __global__ void __launch_bounds__(256) k_sweep_prep(int nc, const int4* __restri
             double vn = dot2(uj[2], uj[3], g.x, g.y);
             double c = sqrt(G * uj[1] / uj[0]);
             rA = 1.5 * (fabs(vn) + c);
-            if (VISC) rA += smax(4 / (3 * uj[0]), G / uj[0]) * ((double)mu[i] / 0.72) / sqrt(fvis[f].z);
+            if (VISC) rA += smax(4 / (3 * uj[0]), G / uj[0]) * mu_over_pr(mu, mut, i) / sqrt(fvis[f].z);
         }
     }
     st4(reinterpret_cast<d4*>(swfc) + t, d4{fc[0], fc[1], fc[2], fc[3]});
@@ -375,10 +390,10 @@ void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, boo
     double* b = reinterpret_cast<double*>(d.dW);
     int r = reset ? 1 : 0;
     if (viscous) {
-        if (fp32) k_sweep_prep<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.muf, d.swfc, d.swra, a, b, r);
-        else k_sweep_prep<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.mu, d.swfc, d.swra, a, b, r);
+        if (fp32) k_sweep_prep<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.muf, d.swfc, d.swra, a, b, r, d.turb ? d.sstMut : nullptr);
+        else k_sweep_prep<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, d.mu, d.swfc, d.swra, a, b, r, d.turb ? d.sstMut : nullptr);
     } else {
-        k_sweep_prep<false, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, (const double*)nullptr, d.swfc, d.swra, a, b, r);
+        k_sweep_prep<false, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0, d.fvis, d.W, d.U, (const double*)nullptr, d.swfc, d.swra, a, b, r, d.turb ? d.sstMut : nullptr);
     }
     *L.counter += 1;
 }
@@ -716,7 +731,8 @@ __global__ void __launch_bounds__(256) k_sweep_prep32(int nc, const int4* __rest
                                                       const d4* __restrict__ W, const d4* __restrict__ U,
                                                       const MuT* __restrict__ mu,
                                                       float* __restrict__ swraf, float4* __restrict__ Wf,
-                                                      float* __restrict__ dW1f, float* __restrict__ dWf) {
+                                                      float* __restrict__ dW1f, float* __restrict__ dWf,
+                                                      const double* __restrict__ mut) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 4 * nc) return;
     int i = t >> 2, s = t & 3;
@@ -740,7 +756,7 @@ __global__ void __launch_bounds__(256) k_sweep_prep32(int nc, const int4* __rest
             float vn = uj[2] * g.x + uj[3] * g.y;
             float c = sqrtf(G * uj[1] / uj[0]);
             rA = 1.5f * (fabsf(vn) + c);
-            if (VISC) rA += fmaxf(4.f / (3.f * uj[0]), G / uj[0]) * ((float)mu[i] / 0.72f) / sqrtf(fvisf[f].z);
+            if (VISC) rA += fmaxf(4.f / (3.f * uj[0]), G / uj[0]) * mu_over_pr_f(mu, mut, i) / sqrtf(fvisf[f].z);
         }
     }
     swraf[t] = rA;
@@ -751,13 +767,13 @@ void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, i
     float* a = reinterpret_cast<float*>(d.dW1f);
     float* b = reinterpret_cast<float*>(d.dWf);
     if (viscous && mu_kind == MU_F64)
-        k_sweep_prep32<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.mu, d.swraf, d.Wf, a, b);
+        k_sweep_prep32<true, double><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.mu, d.swraf, d.Wf, a, b, d.turb ? d.sstMut : nullptr);
     else if (viscous && mu_kind == MU_FF)
-        k_sweep_prep32<true, ff><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muq, d.swraf, d.Wf, a, b);
+        k_sweep_prep32<true, ff><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muq, d.swraf, d.Wf, a, b, d.turb ? d.sstMut : nullptr);
     else if (viscous)
-        k_sweep_prep32<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muf, d.swraf, d.Wf, a, b);
+        k_sweep_prep32<true, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, d.muf, d.swraf, d.Wf, a, b, d.turb ? d.sstMut : nullptr);
     else
-        k_sweep_prep32<false, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, (const float*)nullptr, d.swraf, d.Wf, a, b);
+        k_sweep_prep32<false, float><<<nblk(n, 256), 256, 0, L.stream>>>(d.nc, d.cface, d.lr, d.fg0f, d.fvisf, d.W, d.U, (const float*)nullptr, d.swraf, d.Wf, a, b, d.turb ? d.sstMut : nullptr);
     *L.counter += 1;
 }
 
@@ -1193,7 +1209,7 @@ __global__ void k_chain_prep(int nc, float4* __restrict__ stage_f, float4* __res
                              const int2* __restrict__ rec_f, const int2* __restrict__ rec_b,
                              const float4* __restrict__ fvisf, const float4* __restrict__ Wf,
                              const float4* __restrict__ Uf, const MuT* __restrict__ mu, const d4* __restrict__ R,
-                             const double* __restrict__ invD) {
+                             const double* __restrict__ invD, const double* __restrict__ mut) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 8LL * nc) return;
     const float GM1 = 1.4f - 1.0f;
@@ -1215,7 +1231,7 @@ __global__ void k_chain_prep(int nc, float4* __restrict__ stage_f, float4* __res
         const float vr = uj[2] * g.x + uj[3] * g.y;
         const float c = sqrtf(G * uj[1] / uj[0]);
         rA = 1.5f * (fabsf(vr) + c);
-        if (VISC) rA += fmaxf(4.f / (3.f * uj[0]), G / uj[0]) * ((float)mu[i] / 0.72f) / sqrtf(fvisf[code_face(r.y)].z);
+        if (VISC) rA += fmaxf(4.f / (3.f * uj[0]), G / uj[0]) * mu_over_pr_f(mu, mut, i) / sqrtf(fvisf[code_face(r.y)].z);
         u = w0.z / w0.x;
         v = w0.w / w0.x;
         vv = u * u + v * v;
@@ -1324,19 +1340,19 @@ cudaError_t launch_sweep_chain32(const DevArrays& d, const LaunchCfg& L, bool fo
         if (viscous && mu_kind == MU_F64)
             k_chain_prep<true, double><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
                                                                  d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
-                                                                 d.mu, d.R, d.invD);
+                                                                 d.mu, d.R, d.invD, d.turb ? d.sstMut : nullptr);
         else if (viscous && mu_kind == MU_FF)
             k_chain_prep<true, ff><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
                                                              d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
-                                                             d.muq, d.R, d.invD);
+                                                             d.muq, d.R, d.invD, d.turb ? d.sstMut : nullptr);
         else if (viscous)
             k_chain_prep<true, float><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
                                                                 d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
-                                                                d.muf, d.R, d.invD);
+                                                                d.muf, d.R, d.invD, d.turb ? d.sstMut : nullptr);
         else
             k_chain_prep<false, float><<<nb, 256, 0, L.stream>>>(d.nc, d.chain_stage[0], d.chain_stage[1],
                                                                  d.chain_rec[0], d.chain_rec[1], d.fvisf, d.Wf, d.Uf,
-                                                                 (const float*)nullptr, d.R, d.invD);
+                                                                 (const float*)nullptr, d.R, d.invD, d.turb ? d.sstMut : nullptr);
         *L.counter += 2;
     }
     int tbl_n = d.chain_tbl;

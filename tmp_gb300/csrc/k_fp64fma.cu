@@ -15,7 +15,9 @@ template <bool V>
 static void residual64c(const DevArrays& d, const LaunchCfg& L, int first_order, int which) {
     if (which < 0 || which == 0) {
         k_face_state<double, V, 1><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fmesh, d.prm, d.fg0, d.U, d.Ue,
-                                                                        d.fspec, d.mue, d.err);
+                                                                        d.fspec, d.mue, d.err,
+                                                                        d.turb ? d.sstMut : nullptr,
+                                                                        d.turb ? d.sstMutf : nullptr);
         *L.counter += 1;
     }
     if (which < 0 || which == 1) {
@@ -26,7 +28,8 @@ static void residual64c(const DevArrays& d, const LaunchCfg& L, int first_order,
     }
     if (which < 0 || which == 2) {
         k_face_flux<double, V, 1><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fg0, d.fg1, d.fvis, d.U, d.grad,
-                                                                       d.phi, d.Ue, d.mue, d.gradT, d.Fc, d.Fv, d.err);
+                                                                       d.phi, d.Ue, d.mue, d.gradT, d.Fc, d.Fv, d.err,
+                                                                       d.turb ? d.sstMutf : nullptr);
         *L.counter += 1;
     }
 }

@@ -12,6 +12,8 @@
 // reference's edge loops.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "case.hpp"
 
 namespace cfdgb {
@@ -165,7 +167,11 @@ __global__ void k_sst_flux(DevArrays d) {
 }
 
 // rans_P_Solver (:923-966), SolveTotalTFlux (:969-1013) and SolveDiag (:170-192).
-__global__ void k_sst_total(DevArrays d) {
+// coupled = 0: the residual as written, Q vol + sum(Fc - Fv); coupled = 1 (the
+// model inside every LU-SGS step): sum(Fc - Fv) - Q vol, the sign that
+// dW = -R / D needs for the sources (the written sign turns production into
+// destruction).
+__global__ void k_sst_total(DevArrays d, int coupled) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d.nc) return;
     const double f1 = d.sstF1[c];
@@ -186,7 +192,7 @@ __global__ void k_sst_total(DevArrays d) {
     const double q0 = P - beta_star * rho * k * w;
     const double q1 = Cw * rho * P / mut - beta * rho * w * w + 2 * (1 - f1) * rho * sigma_w2 / w * rdiv;
     const double vol = d.cgeo[c].x;
-    double r0 = q0 * vol, r1 = q1 * vol;
+    double r0 = coupled ? -(q0 * vol) : q0 * vol, r1 = coupled ? -(q1 * vol) : q1 * vol;
     const int4 cf = d.cface[c];
     const int codes[4] = {cf.x, cf.y, cf.z, cf.w};
     for (int s = 0; s < 4; s++) {
@@ -225,6 +231,207 @@ __global__ void k_sst_mut(DevArrays d) {
     d.sstMut[c] = a1 * W0 / h;
 }
 
+// ---------------------------------------------------------------------------
+// Coupled turbulence LU-SGS (CFD_FLOW_SST).  The reference's SSTkomegaModel
+// would run LUSGSIntegrator over its two equations (turbModelTimeStrategy,
+// ViscousFlow2D.cpp:62-63) with SolveDF (:251-474); as written that SolveDF
+// reads the neighbour's k, omega pair past the cell's own, passes the current
+// cell as the neighbour in its right-cell branch (a zero centre line) and
+// reads flow arrays no caller sets.  These kernels run the intended step: for
+// neighbour j across face f of cell i, with the flow's W_j (before the update)
+// and its increment dW_j of the same sweep direction,
+//   DF = 0.5 (+-(W_t,j + dW_t,j) Vn(W_j + dW_j) -+ W_t,j Vn(W_j) - r_A dW_t,j) A,
+// r_A as the flow's (SolveViscousFlux with mu/Pr + mu_t/Prt of cell i),
+// forward dW_t1,i = (-R_t,i - sum DF) / D_t,i, backward dW_t,i = dW_t1,i -
+// sum DF / D_t,i, in the reference's cell order (same levels as the flow).
+constexpr unsigned long long kSentT = 0x7ff4c0ffee5eed22ULL;  // signalling-NaN "not yet computed"
+constexpr unsigned kSentTf = 0x7fa0c0dfu;
+constexpr long long kSpinT = 1LL << 22;
+
+__device__ __forceinline__ bool sent_t(double x) { return (unsigned long long)__double_as_longlong(x) == kSentT; }
+__device__ __forceinline__ bool sent_tf(float x) { return __float_as_uint(x) == kSentTf; }
+
+// Per (cell i, face slot s): the increment-free terms of the turbulence SolveDF
+// - W_t,j Vn(W_j), r_A, and Vn(W_j + dW_j) with the flow increment of the
+// direction that uses this slot (forward if j < i, backward if j > i) - then
+// the "not yet computed" sentinels and 1/D_t.  After the flow's sweeps.
+__global__ void __launch_bounds__(256) k_sst_sweep_prep(DevArrays d) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * d.nc) return;
+    const int i = t >> 2, s = t & 3;
+    if (s < 2) {
+        d.sstDW1[2 * i + s] = __longlong_as_double((long long)kSentT);
+        d.sstDW[2 * i + s] = __longlong_as_double((long long)kSentT);
+        d.sstDinv[2 * i + s] = 1.0 / d.sstD[2 * i + s];
+    }
+    if (s == 0 && d.sstDW1f) {
+        const float sf = __uint_as_float(kSentTf);
+        d.sstDW1f[i] = make_float2(sf, sf);
+        d.sstDWf[i] = make_float2(sf, sf);
+    }
+    const int code = (&d.cface[i].x)[s];
+    double fc0 = 0.0, fc1 = 0.0, rA = 0.0, vnp = 0.0;
+    if (code != 0) {
+        const int f = code > 0 ? code - 1 : -code - 1;
+        const int2 e = d.lr[f];
+        const int j = code > 0 ? e.y : e.x;
+        if (j >= 0) {
+            const d4 g = d.fg0[f];
+            const d4 w0 = ld4(d.W + j);
+            const d4 dw = ld4((j < i ? d.dW1 : d.dW) + j);
+            const d4 wp = d4{w0.x + dw.x, w0.y + dw.y, w0.z + dw.z, w0.w + dw.w};
+            const double vn0 = dot2(w0.z / w0.x, w0.w / w0.x, g.x, g.y);
+            vnp = dot2(wp.z / wp.x, wp.w / wp.x, g.x, g.y);
+            fc0 = d.sstW[2 * j] * vn0;
+            fc1 = d.sstW[2 * j + 1] * vn0;
+            const d4 uj = ld4(d.U + j);
+            const double G = 1.4;
+            const double vn = dot2(uj.z, uj.w, g.x, g.y);
+            const double c = sqrt(G * uj.y / uj.x);
+            rA = 1.5 * (fabs(vn) + c);
+            rA += dmax(4 / (3 * uj.x), G / uj.x) * (d.mu[i] / 0.72 + d.sstMut[i] / 0.9) / sqrt(d.fvis[f].z);
+        }
+    }
+    d.sstFcs[2 * t] = fc0;
+    d.sstFcs[2 * t + 1] = fc1;
+    d.sstRA[t] = rA;
+    d.sstVnp[t] = vnp;
+}
+
+// One dataflow launch per direction: one warp per cell, taken in level order
+// (positions p = block + B*q, as the flow's dataflow sweep), lanes 2s+m for
+// face slot s and equation m.  A neighbour's increment is final once its
+// words are no longer the sentinel; every wait is bounded (ERR_TIMEOUT).
+// T = double: the plain form (every operation in binary64, as the C
+// restatement); T = float: the slot terms in binary32 and the published copy
+// polled in binary32, the increment itself formed in binary64 from them.
+template <bool FWD, class T>
+__global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __restrict__ order) {
+    const int lane = threadIdx.x & 31;
+    const int s = (lane >> 1) & 3, m = lane & 1;
+    const int warp = threadIdx.x >> 5;
+    const int B = gridDim.x, NW = blockDim.x >> 5;
+    double* dst = FWD ? d.sstDW1 : d.sstDW;
+    float2* dstf = FWD ? d.sstDW1f : d.sstDWf;
+    const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
+    for (long long q = q0;; q += NW) {
+        const long long p = (long long)blockIdx.x + (long long)B * q;
+        if (p >= d.nc) break;
+        const int i = order[p];
+        const int4 cf = d.cface[i];
+        const int code = lane < 8 ? (s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w) : 0;
+        bool use = false, left = false;
+        int f = 0, j = 0;
+        if (code != 0) {
+            f = code > 0 ? code - 1 : -code - 1;
+            left = code > 0;
+            const int2 e = d.lr[f];
+            j = left ? e.y : e.x;
+            use = FWD ? (j >= 0 && j < i) : (j > i);
+        }
+        double own = 0.0, dd = 1.0;
+        if (lane < 2) {
+            own = FWD ? d.sstR[2 * i + m] : d.sstDW1[2 * i + m];
+            dd = std::is_same<T, double>::value ? d.sstD[2 * i + m] : d.sstDinv[2 * i + m];
+        }
+        T DF = T(0);
+        T wt = T(0), fc = T(0), rA = T(0), vnp = T(0), A = T(0), dt = T(0);
+        if (use) {
+            const size_t t = (size_t)i * 4 + s;
+            wt = (T)d.sstW[2 * j + m];
+            fc = (T)d.sstFcs[2 * t + m];
+            rA = (T)d.sstRA[t];
+            vnp = (T)d.sstVnp[t];
+            A = (T)d.fgeo[f].z;
+            long long it = 0;
+            if (std::is_same<T, double>::value) {
+                const double2* qd = reinterpret_cast<const double2*>((FWD ? d.sstDW1 : d.sstDW) + 2 * (size_t)j);
+                double2 a;
+                while (true) {
+                    a = __ldcv(qd);
+                    if (!sent_t(a.x) && !sent_t(a.y)) break;
+                    if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
+                    if (d.poll_ns) __nanosleep(d.poll_ns);
+                }
+                dt = (T)(m ? a.y : a.x);
+            } else {
+                const float2* qf = (FWD ? d.sstDW1f : d.sstDWf) + j;
+                float2 a;
+                while (true) {
+                    a = __ldcv(qf);
+                    if (!sent_tf(a.x) && !sent_tf(a.y)) break;
+                    if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
+                    if (d.poll_ns) __nanosleep(d.poll_ns);
+                }
+                dt = (T)(m ? a.y : a.x);
+            }
+            const T fcp = (wt + dt) * vnp;
+            const T dfc = left ? (fcp - fc) : (fc - fcp);
+            DF = T(0.5) * (dfc - rA * dt) * A;
+        }
+        __syncwarp();
+        // ordered sum over the face slots (lanes m, 2+m, 4+m, 6+m)
+        const T v0 = __shfl_sync(0xffffffffu, DF, m);
+        const T v1 = __shfl_sync(0xffffffffu, DF, 2 + m);
+        const T v2 = __shfl_sync(0xffffffffu, DF, 4 + m);
+        const T v3 = __shfl_sync(0xffffffffu, DF, 6 + m);
+        T dF = T(0);
+        if (cf.x != 0) dF += v0;
+        if (cf.y != 0) dF += v1;
+        if (cf.z != 0) dF += v2;
+        if (cf.w != 0) dF += v3;
+        if (std::is_same<T, double>::value) {
+            double res = 0.0;
+            if (lane < 2) res = FWD ? (-own - (double)dF) / dd : own - (double)dF / dd;
+            const double r1 = __shfl_sync(0xffffffffu, res, 1);
+            if (lane == 0) __stcg(reinterpret_cast<double2*>(dst + 2 * (size_t)i), make_double2(res, r1));
+        } else {
+            // the binary32 copy the next levels wait for first, then the binary64 increment
+            float resf = 0.f;
+            if (lane < 2) resf = FWD ? (-(float)own - (float)dF) * (float)dd : (float)own - (float)dF * (float)dd;
+            const float f1 = __shfl_sync(0xffffffffu, resf, 1);
+            if (lane == 0) __stcg(dstf + i, make_float2(resf, f1));
+            double res = 0.0;
+            if (lane < 2) res = FWD ? (-own - (double)dF) * dd : own - (double)dF * dd;
+            const double r1 = __shfl_sync(0xffffffffu, res, 1);
+            if (lane == 0) __stcg(reinterpret_cast<double2*>(dst + 2 * (size_t)i), make_double2(res, r1));
+        }
+    }
+}
+
+// W_t += dW_t; k, omega = W_t / rho with rho after the flow's update, kept at
+// or above 1e-4 of the freestream values (the clip that SSTKWStrategy.h:206-215
+// has commented out); mu_t = a1 W_k / max(a1 W_omega / rho, F2 |dv/dx - du/dy|)
+// (UpdatePrimitiveVariables, :194-223).
+__global__ void k_sst_update(DevArrays d) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nc) return;
+    const MeshPrm& P = d.prm[d.cmesh[c]];
+    const double kmin = 1e-4 * P.sst_k, wmin = 1e-4 * P.sst_w;
+    const double rho = d.U[c].x;
+    double w0 = d.sstW[2 * c] + d.sstDW[2 * c], w1 = d.sstW[2 * c + 1] + d.sstDW[2 * c + 1];
+    double k = w0 / rho, w = w1 / rho;
+    if (!(k >= kmin)) { k = kmin; w0 = rho * kmin; }
+    if (!(w >= wmin)) { w = wmin; w1 = rho * wmin; }
+    d.sstW[2 * c] = w0;
+    d.sstW[2 * c + 1] = w1;
+    d.sstT[2 * c] = k;
+    d.sstT[2 * c + 1] = w;
+    const d4 gu = d.grad[2 * c + 1];
+    const double curl = fabs(gu.z - gu.y);
+    const double h = dmax(a1 * w1 / rho, d.sstF2[c] * curl);
+    d.sstMut[c] = a1 * w0 / h;
+}
+
+// initializeConsData (:97-109): W_t = rho (k, omega)
+__global__ void k_sst_cons(DevArrays d) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nc) return;
+    const double rho = d.U[c].x;
+    d.sstW[2 * c] = d.sstT[2 * c] * rho;
+    d.sstW[2 * c + 1] = d.sstT[2 * c + 1] * rho;
+}
+
 inline unsigned nb(int n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -233,12 +440,64 @@ void launch_sst_residual(const DevArrays& d, const LaunchCfg& L) {
     k_sst_face<<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
     k_sst_cell<<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
     k_sst_flux<<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
-    k_sst_total<<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
+    k_sst_total<<<nb(d.nc, 256), 256, 0, L.stream>>>(d, 0);
     *L.counter += 4;
+}
+
+void launch_sst_stage(const DevArrays& d, const LaunchCfg& L, int stage) {
+    if (stage == 0) k_sst_face<<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
+    else if (stage == 1) k_sst_cell<<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
+    else if (stage == 2) k_sst_flux<<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
+    else k_sst_total<<<nb(d.nc, 256), 256, 0, L.stream>>>(d, 1);
+    *L.counter += 1;
 }
 
 void launch_sst_update_mut(const DevArrays& d, const LaunchCfg& L) {
     k_sst_mut<<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
+    *L.counter += 1;
+}
+
+}  // namespace cfdgb
+
+namespace cfdgb {
+
+int sst_sweep_max_grid(int blocks_per_sm) {
+    int dev = 0, sms = 0, a = 0, b = 0, c2 = 0, d2 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, (void*)k_sst_sweep<true, double>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (void*)k_sst_sweep<false, double>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, (void*)k_sst_sweep<true, float>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d2, (void*)k_sst_sweep<false, float>, 256, 0);
+    int per = a < b ? a : b;
+    per = per < c2 ? per : c2;
+    per = per < d2 ? per : d2;
+    if (blocks_per_sm > 0 && blocks_per_sm < per) per = blocks_per_sm;
+    return per * sms;
+}
+
+cudaError_t launch_sst_sweeps(const DevArrays& d, const LaunchCfg& L, bool fp32) {
+    k_sst_sweep_prep<<<nb(4 * d.nc, 256), 256, 0, L.stream>>>(d);
+    *L.counter += 1;
+    for (int dir = 0; dir < 2; dir++) {
+        const int* order = dir == 0 ? d.fwd_order : d.bwd_order;
+        void* args[] = {(void*)&d, (void*)&order};
+        void* fn = fp32 ? (dir == 0 ? (void*)k_sst_sweep<true, float> : (void*)k_sst_sweep<false, float>)
+                        : (dir == 0 ? (void*)k_sst_sweep<true, double> : (void*)k_sst_sweep<false, double>);
+        cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(d.sst_grid), dim3(256), args, 0, L.stream);
+        *L.counter += 1;
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+void launch_sst_update(const DevArrays& d, const LaunchCfg& L) {
+    k_sst_update<<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
+    *L.counter += 1;
+}
+
+void launch_sst_cons(const DevArrays& d, const LaunchCfg& L) {
+    k_sst_cons<<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
     *L.counter += 1;
 }
 

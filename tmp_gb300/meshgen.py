@@ -170,9 +170,10 @@ def naca_body(n: int, t: float = 0.12, chord: float = 1.0) -> np.ndarray:
     return np.stack([x * chord, y * chord], 1)
 
 
-def layered_quads(body: np.ndarray, nlayer: int, dr1: float, growth: float):
+def layered_quads(body: np.ndarray, nlayer: int, dr1: float, growth: float, hmax: float | None = None):
     """Quad layers grown along smoothed outward normals of a closed CCW body
-    contour.  Returns node coordinates (layer-major) and the outer ring."""
+    contour; layer thickness starts at dr1 and grows by `growth` up to hmax.
+    Returns node coordinates (layer-major) and the outer ring."""
     n = len(body)
     pts = [body]
     cur = body.copy()
@@ -190,12 +191,14 @@ def layered_quads(body: np.ndarray, nlayer: int, dr1: float, growth: float):
         cur = cur + h * nrm
         pts.append(cur)
         h *= growth
+        if hmax is not None:
+            h = min(h, hmax)
     xy = np.concatenate(pts, 0)
     return xy, n
 
 
 def mixed_mesh(body: np.ndarray, nlayer: int, dr1: float, growth: float, rfar: float, seed: int = 0,
-               density: float = 1.0, grade: float = 1.0) -> GrdMesh:
+               density: float = 1.0, grade: float = 1.0, hmax: float | None = None) -> GrdMesh:
     """Quad layers around `body` (structured sweep numbering: along the body
     fastest, then outward), then a seeded Delaunay triangle fill out to a circle
     of radius rfar centred on the body's centroid; triangles keep the order in
@@ -203,7 +206,7 @@ def mixed_mesh(body: np.ndarray, nlayer: int, dr1: float, growth: float, rfar: f
     from scipy.spatial import Delaunay
 
     rng = np.random.default_rng(seed)
-    qxy, n = layered_quads(body, nlayer, dr1, growth)
+    qxy, n = layered_quads(body, nlayer, dr1, growth, hmax)
     j, i = np.meshgrid(np.arange(nlayer), np.arange(n), indexing="ij")
     i, j = i.ravel(), j.ravel()
     ip = (i + 1) % n
