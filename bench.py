@@ -359,7 +359,7 @@ def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5, mode: in
     tuned = []
     for c in packed:
         c.autotune(2)
-        tuned.append(dict(zip(("mode", "blocks_per_sm"), c.sweep_config())))
+        tuned.append(dict(zip(("mode", "blocks_per_sm", "threads"), c.sweep_config())))
     ms_packed = run(packed)
     net = learn.load()
     ms_learned = None
@@ -585,12 +585,12 @@ def run_ours(args):
         c2 = make_case(f)
         fm, _ = timed_steps(c2, args.steps)
         forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3),
-                    "sweep": dict(zip(("mode", "blocks_per_sm"), c2.sweep_config()))}
+                    "sweep": dict(zip(("mode", "blocks_per_sm", "threads"), c2.sweep_config()))}
         if f == "fp64" and not args.no_e2e:
             forms[f]["e2e"] = e2e_of(c2)
         c2.close()
     forms[args.precision] = {"ms_per_step": 1e3 * t_local / args.steps, "value": nc * args.steps / t_local,
-                             "sweep": dict(zip(("mode", "blocks_per_sm"), case.sweep_config())), "e2e": e2e}
+                             "sweep": dict(zip(("mode", "blocks_per_sm", "threads"), case.sweep_config())), "e2e": e2e}
     # the plain binary64 form (results equal to the reference's) next to the headline form
     plain = forms.get("fp64")
 
@@ -700,7 +700,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision], "data": "synthetic",
             "config": {"workload": w.name, "ncell": nc, "nedge": nf, "levels": list(nlev), "mach": w.mach,
                        "re": w.re, "cfl": w.cfl, "precision": args.precision,
-                       "sweep": dict(zip(("mode", "blocks_per_sm"), case.sweep_config())),
+                       "sweep": dict(zip(("mode", "blocks_per_sm", "threads"), case.sweep_config())),
                        "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
             "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms_per_step"], "e2e": plain.get("e2e"),

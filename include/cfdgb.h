@@ -154,7 +154,11 @@ typedef struct {
                                 the occupancy limit)                             */
     int sweep_poll_ns; /* dataflow sweep: pause between polls of a neighbour's
                           increment in ns (__nanosleep; 0 = spin)                */
-    int reserved[5];
+    int sweep_threads; /* round-robin dataflow sweeps (modes 0, 3, 4 and the
+                          SST turbulence sweeps): threads per block, 64, 128 or
+                          256 (0 = 256); fewer warps per block put fewer cells
+                          on one SM sub-partition's pipes at a time            */
+    int reserved[4];
 } cfd_params_t;
 
 /* ---- errors -------------------------------------------------------------- */
@@ -256,7 +260,8 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
  * (1, 2, ... up to the occupancy limit), keeps the fastest for the case and
  * reports it; the case's state is restored afterwards.  For the binary32-sweep
  * forms of a case created with sweep_mode 0, 5 or 6 it also picks among those
- * three schedules (cfd_case_sweep reads the choice). */
+ * three schedules, and for the round-robin ones among 256, 128 and 64 threads
+ * per block (cfd_case_sweep reads the choice). */
 int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_ms);
 /* Host-side chain schedule of the binary32 LU-SGS sweep (sweep modes 5 and 6)
  * for one mesh, as a case holding that mesh builds it (no reference
@@ -271,9 +276,10 @@ int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_m
  * entry t, else the cell id); *table_entries the table's entries per block. */
 int cfd_chain_schedule(cfd_mesh_t mesh, int forward, int nlists, int local, int table, int* hptr,
                        int* cells, int* rec, int* jenc, int* table_entries);
-/* The case's current LU-SGS schedule: sweep_mode and blocks per SM (after
- * cfd_autotune, the ones it chose). No reference counterpart. */
-int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm);
+/* The case's current LU-SGS schedule: sweep_mode, blocks per SM and threads
+ * per block of the round-robin dataflow sweeps (after cfd_autotune, the ones
+ * it chose); any pointer may be NULL. No reference counterpart. */
+int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm, int* threads);
 /* Failure-detection self-test (no reference counterpart): launch a kernel that
  * waits, at most `polls` polls, on a device flag nothing sets, exactly as the
  * dataflow LU-SGS sweep waits on its neighbours.  Returns CFD_ERR_TIMEOUT when
@@ -415,6 +421,29 @@ void cfd_connect_free(cfd_connect_t c);
  * -1 if all of its nodes are -1 (receptors), else 1.  Host arrays of the
  * block's node / cell counts. */
 int cfd_cell_iblank(cfd_block_t b, const int* node_iblank, int* cell_iblank);
+
+/* ---- overset components of one case ---------------------------------------- */
+/* Connectivity of a case whose meshes are overset components: one rank's
+ * tioga::performConnectivity over them (tioga.cpp:153-262; the assembly of
+ * cfd_overset_connect with hole maps of the meshes that have wall faces, isym
+ * 3).  meshes[] are the handles the case was created from, in the same order;
+ * obc_nodes[m][nobc[m]] the overset-boundary nodes of mesh m (0-based; either
+ * array may be NULL for none).  Afterwards every LU-SGS step updates only the
+ * field cells (cell iblank 1) and ends with the fringe exchange below, so a
+ * captured step (cfd_step_graph) holds the whole coupled iteration.  LU-SGS
+ * cases, 2 to 64 meshes; re-run it when the grids move. */
+int cfd_connectivity(cfd_case_t c, const cfd_mesh_t* meshes, const int* const* obc_nodes, const int* nobc,
+                     int nfringe, int mexclude);
+/* The fringe exchange of a connected case (tioga::dataUpdate between its
+ * components, tioga.cpp:326-471, dataUpdate.cpp:6-132, on node values as
+ * Orchestra::init registers them, Orchestra.cpp:201-291): the donor nodes get
+ * the mean of their cells' primitive state, every receptor node is
+ * interpolated from its donor cell (all values formed before any is written),
+ * and every receptor cell (iblank -1) takes the mean of its nodes.  nvar must
+ * be 4 (the primitive state).  Asynchronous on the case's stream. */
+int cfd_fringe_update(cfd_case_t c, int nvar);
+/* Cell iblank of one mesh of a connected case (1 field, 0 hole, -1 receptor). */
+int cfd_case_iblank(cfd_case_t c, int mesh, int* cell_iblank);
 
 /* ---- SST k-omega (SSTkomegaModel, UnstructSolver/SSTKWStrategy.h) -------- */
 /* The reference builds this model but never runs it (ViscousFlow2D's serial

@@ -52,7 +52,7 @@ class Freestream(C.Structure):
 class Params(C.Structure):
     _fields_ = [("flow", C.c_int), ("advance", C.c_int), ("precision", C.c_int), ("first_order", C.c_int),
                 ("cfl", C.c_double), ("sweep_mode", C.c_int), ("sweep_blocks_per_sm", C.c_int),
-                ("sweep_poll_ns", C.c_int), ("reserved", C.c_int * 5)]
+                ("sweep_poll_ns", C.c_int), ("sweep_threads", C.c_int), ("reserved", C.c_int * 4)]
 
 
 _lib = None
@@ -124,6 +124,9 @@ def lib() -> C.CDLL:
         "cfd_connect_interp_count": (C.c_int, [vp, C.c_int, C.POINTER(C.c_longlong)]),
         "cfd_connect_interp_get": (C.c_int, [vp, C.c_int, ip, ip, ip, ip, ip, dp]),
         "cfd_connect_free": (None, [vp]),
+        "cfd_connectivity": (C.c_int, [vp, C.POINTER(vp), C.POINTER(ip), ip, C.c_int, C.c_int]),
+        "cfd_fringe_update": (C.c_int, [vp, C.c_int]),
+        "cfd_case_iblank": (C.c_int, [vp, C.c_int, ip]),
         "cfd_write_cell_data": (C.c_int, [vp, C.c_int, vp, C.c_char_p, C.c_int]),
         "cfd_write_node_data": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int, dp]),
         "cfd_write_tioga_format": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int, ip]),
@@ -140,7 +143,7 @@ def lib() -> C.CDLL:
         "cfd_measure_hop_latency": (C.c_int, [vp, C.c_int, C.c_int, dp]),
         "cfd_set_precision": (C.c_int, [vp, C.c_int]),
         "cfd_autotune": (C.c_int, [vp, C.c_int, ip, dp]),
-        "cfd_case_sweep": (C.c_int, [vp, ip, ip]),
+        "cfd_case_sweep": (C.c_int, [vp, ip, ip, ip]),
         "cfd_chain_schedule": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, ip, ip, ip, ip, ip]),
         "cfd_sst_enable": (C.c_int, [vp]),
         "cfd_sst_freestream": (C.c_int, [vp, C.c_int, dp]),
@@ -235,14 +238,14 @@ class Case:
 
     def __init__(self, meshes: Sequence[Mesh], freestreams: Sequence[dict], flow: int, advance: int,
                  precision: int = PREC_FP64, cfl: float = 1.0, first_order: bool = False, stream: int | None = None,
-                 sweep_mode: int = 0, sweep_blocks_per_sm: int = 0, sweep_poll_ns: int = 0):
+                 sweep_mode: int = 0, sweep_blocks_per_sm: int = 0, sweep_poll_ns: int = 0, sweep_threads: int = 0):
         self.meshes = list(meshes)
         arr = (C.c_void_p * len(meshes))(*[m.h.value for m in meshes])
         fs = (Freestream * len(meshes))(*[Freestream(f["mach"], f.get("aoa_deg", 0.0), f.get("reynolds", 1.0),
                                                      f.get("density", 1.225), f.get("pressure", 101325.0))
                                           for f in freestreams])
         p = Params(flow, advance, precision, int(first_order), float(cfl), int(sweep_mode), int(sweep_blocks_per_sm),
-                   int(sweep_poll_ns))
+                   int(sweep_poll_ns), int(sweep_threads))
         h = C.c_void_p()
         check(lib().cfd_case_create(arr, len(meshes), fs, C.byref(p), C.c_void_p(stream) if stream else None,
                                     C.byref(h)))
@@ -286,10 +289,29 @@ class Case:
         return b.value, t.value
 
     def sweep_config(self):
-        """(sweep_mode, blocks_per_sm) in use, e.g. after autotune()."""
-        a, b = C.c_int(), C.c_int()
-        check(lib().cfd_case_sweep(self.h, C.byref(a), C.byref(b)))
-        return a.value, b.value
+        """(sweep_mode, blocks_per_sm, threads per block) in use, e.g. after autotune()."""
+        a, b, t = C.c_int(), C.c_int(), C.c_int()
+        check(lib().cfd_case_sweep(self.h, C.byref(a), C.byref(b), C.byref(t)))
+        return a.value, b.value, t.value
+
+    def connect(self, meshes, obc_nodes=None, nfringe: int = 1, mexclude: int = 3):
+        """Overset connectivity of the case's meshes (the handles it was created from); afterwards every LU-SGS
+        step updates the field cells and ends with the fringe exchange."""
+        n = len(meshes)
+        ms = (C.c_void_p * n)(*[m.h.value for m in meshes])
+        obc = [np.ascontiguousarray(o if o is not None else np.zeros(0), dtype=np.int32) for o in (obc_nodes or [None] * n)]
+        op = (C.POINTER(C.c_int) * n)(*[_iptr(o) for o in obc])
+        no = np.array([len(o) for o in obc], np.int32)
+        check(lib().cfd_connectivity(self.h, ms, op, _iptr(no), int(nfringe), int(mexclude)))
+
+    def fringe_update(self):
+        check(lib().cfd_fringe_update(self.h, 4))
+
+    def iblank(self, mesh: int = 0) -> np.ndarray:
+        n = self._count("VOL", mesh)
+        out = np.zeros(n, np.int32)
+        check(lib().cfd_case_iblank(self.h, int(mesh), _iptr(out)))
+        return out
 
     def set_precision(self, precision: int):
         check(lib().cfd_set_precision(self.h, int(precision)))

@@ -37,6 +37,7 @@ UNITS = [
     ("k_mlp.cu", []),
     ("k_sst.cu", ["-fmad=false"]),
     ("k_noalloc.cu", []),
+    ("k_fringe.cu", ["-fmad=false"]),
 ]
 
 

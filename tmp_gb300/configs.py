@@ -6,6 +6,11 @@ C1  Euler, O-grid 128 x 64 around a unit-diameter cylinder, first spacing 1e-3 D
 C2  laminar NS, 48 quad layers (first spacing 5e-3 D) around the cylinder plus
     a seeded Delaunay triangle fill to 30 D, ~130k cells, Re 40, M 0.2,
     LU-SGS at CFL 50.
+C3  SST k-omega RANS around a NACA 0012 (chord 1): 256 quad layers from a
+    first spacing of 2e-6 growing by 1.1 up to 4e-3, then a seeded Delaunay
+    triangle fill to 100 chords, 1,071,543 cells; Re 6e6, M 0.15, AoA 4 deg
+    (0 and 10 as variants), freestream turbulence intensity 0.1% and
+    mu_t / mu = 10, LU-SGS.
 C5  256 independent cases of uneven size (5k-200k cells, log-uniform from a
     seed), cylinder or NACA 0012 bodies with quad layers and a triangle fill,
     M ~ U[0.2, 0.8], AoA ~ U[-4, 10] deg, half Euler and half viscous with
@@ -28,7 +33,7 @@ from . import meshgen
 class Workload:
     name: str
     mesh: meshgen.GrdMesh
-    flow: str          # "euler" | "laminar"
+    flow: str          # "euler" | "laminar" | "sst"
     advance: str       # "rk5" | "lusgs"
     mach: float
     aoa: float
@@ -60,7 +65,18 @@ def c2big() -> Workload:
     return Workload("C2big cylinder mixed quad/tri ~1M laminar LU-SGS", m, "laminar", "lusgs", 0.2, 0.0, 40.0, 50.0)
 
 
-WORKLOADS = {"c1": c1, "c2": c2, "c2big": c2big}
+def c3_mesh() -> meshgen.GrdMesh:
+    return meshgen.mixed_mesh(meshgen.naca_body(1024), nlayer=256, dr1=2e-6, growth=1.1, rfar=100.0, seed=3003,
+                              density=1.0, grade=1.25, hmax=4e-3)
+
+
+def c3(aoa: float = 4.0, cfl: float = 10.0) -> Workload:
+    """The SST airfoil case; extra: freestream turbulence (intensity, mu_t / mu)."""
+    return Workload(f"C3 NACA 0012 ~1.07M SST k-omega AoA {aoa:g}", c3_mesh(), "sst", "lusgs", 0.15, aoa, 6e6, cfl,
+                    extra=dict(tu=0.001, mut_ratio=10.0))
+
+
+WORKLOADS = {"c1": c1, "c2": c2, "c2big": c2big, "c3": c3}
 
 
 @dataclass

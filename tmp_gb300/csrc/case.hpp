@@ -138,6 +138,7 @@ struct DevArrays {
     int* bwd_order2 = nullptr;
     int npos2_fwd = 0, npos2_bwd = 0;
     int flow_grid = 0;           // co-resident blocks of the dataflow sweep
+    int flow_threads = 256;      // threads per block of the round-robin dataflow sweeps
     // chain-scheduled fast-form sweep (sweep_mode 5), index 0 forward, 1 backward
     int chain_nh = 0;            // warps (lists) the schedule was built for (0: not built)
     int* chain_ptr[2] = {nullptr, nullptr};    // [chain_nh+1] each warp's range of positions
@@ -160,6 +161,25 @@ struct DevArrays {
     double* norm_partial = nullptr;
     double* norm_out = nullptr;   // [nmesh]
     unsigned* err = nullptr;      // [2] device error word; err[1] stays 0 (a flag nothing sets)
+    int* iblank_cell = nullptr;   // [nc] overset cell blanking (1 field, 0 hole, -1 receptor) or null: the
+                                  // LU-SGS update leaves every cell that is not a field cell as it is
+};
+
+// Case-level overset exchange (k_fringe.cu): device arrays built by cfd_case_connect.
+struct FringePlan {
+    int nsrc = 0;                 // donor nodes whose cell means the lists read
+    int* src_nodes = nullptr;     // [nsrc] global node ids
+    int* src_ptr = nullptr;       // [nsrc+1] ranges of src_cells
+    int* src_cells = nullptr;     // cells around each donor node, ascending
+    int nrecv = 0;                // interpolation entries (receptor nodes)
+    int* recv_node = nullptr;     // [nrecv] global receiving node
+    int* nw = nullptr;            // [nrecv] 3 or 4
+    int* inode = nullptr;         // [4*nrecv] global donor nodes
+    double* w = nullptr;          // [4*nrecv] weights
+    int ncells = 0;               // receptor cells
+    int* recv_cells = nullptr;    // [ncells] global cell ids (iblank_cell -1)
+    double* qn = nullptr;         // [4*nn] node values, ROW layout
+    double* vals = nullptr;       // [4*nrecv] interpolated values before they are written
 };
 
 struct LaunchCfg {
@@ -179,7 +199,7 @@ void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, boo
 void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, int begin, int end);
 cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
 cudaError_t launch_sweep_pair64(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
-int sweep_flow_max_grid(bool low, int blocks_per_sm);
+int sweep_flow_max_grid(bool low, int blocks_per_sm, int threads = 256);
 void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
 // kind of the viscosity array the binary32 sweep staging reads: the residual's form
 enum MuKind { MU_F32 = 0, MU_F64 = 1, MU_FF = 2 };
@@ -195,6 +215,8 @@ void launch_face_lr(const DevArrays& d, const LaunchCfg& L, int begin, int end, 
 void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limit);
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy);
 void launch_cons_from_prim(const DevArrays& d, const LaunchCfg& L, int begin, int end);
+// ---- k_fringe.cu ----
+void launch_fringe(const DevArrays& d, const FringePlan& f, const LaunchCfg& L);
 // form: 0 binary64, 1 binary32, 2 float-float (the residual arrays read)
 void launch_local_dt(const DevArrays& d, const LaunchCfg& L, double cfl, int form);
 void launch_wall_distance(const DevArrays& d, const LaunchCfg& L);
@@ -212,7 +234,7 @@ cudaError_t launch_sst_sweeps(const DevArrays& d, const LaunchCfg& L, bool fp32)
 void launch_sst_update(const DevArrays& d, const LaunchCfg& L);
 // W_t = rho (k, omega) from the current U and k, omega
 void launch_sst_cons(const DevArrays& d, const LaunchCfg& L);
-int sst_sweep_max_grid(int blocks_per_sm);
+int sst_sweep_max_grid(int blocks_per_sm, int threads = 256);
 // ---- k_fp32.cu ----
 void launch_residual_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);

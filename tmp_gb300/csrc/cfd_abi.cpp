@@ -11,6 +11,7 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/cfdgb.h"
@@ -118,6 +119,8 @@ struct cfd_case_s {
     float mlp_spread = 0.0f;         // bound on |omega - mesh mean| (negative: none)
     std::vector<cfd_freestream_t> fs_in;  // the freestreams the case was created with
     bool sst = false;                // SST k-omega arrays allocated
+    bool connected = false;          // overset components joined by cfd_connectivity
+    FringePlan fringe;               // their per-step exchange
     // host copies kept for the chain sweep schedule (LU-SGS cases)
     std::vector<int4> h_cface;
     std::vector<int2> h_lr;
@@ -145,6 +148,15 @@ struct cfd_case_s {
 };
 
 static void sst_alloc(cfd_case_s* c);
+// Launch shape of the dataflow sweeps: blocks per SM (0: the default 2) and
+// threads per block (0: 256) of the round-robin sweeps, the grids that keep
+// them co-resident (flow and, coupled SST, turbulence sweeps).
+static void set_sweep_shape(cfd_case_s* c, int bpsm, int threads) {
+    if (threads != 64 && threads != 128) threads = 256;
+    c->d.flow_threads = threads;
+    c->d.flow_grid = sweep_flow_max_grid(c->p.precision != CFD_PREC_FP64, bpsm, threads);
+    if (c->turb()) c->d.sst_grid = sst_sweep_max_grid(bpsm > 0 ? bpsm : 2, threads);
+}
 static void sst_freestream(cfd_case_s* c);
 static void sst_init_state(cfd_case_s* c);
 
@@ -163,7 +175,9 @@ void free_case(cfd_case_s* c) {
                     d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_jenc[0], d.chain_jenc[1], d.chain_stage[0],
                     d.chain_stage[1], d.chain_posb, d.chain_dF, d.Uq, d.gradq, d.phiq, d.speccq, d.specvq, d.gradTq,
                     d.muq, d.Ueq, d.fspecq, d.mueq, d.Fcq, d.Fvq, d.fg0q, d.fg1q, d.fvisq, d.cgeoq, d.sstW, d.sstDW1,
-                    d.sstDW, d.sstFcs, d.sstRA, d.sstVnp, d.sstDinv, d.sstDW1f, d.sstDWf};
+                    d.sstDW, d.sstFcs, d.sstRA, d.sstVnp, d.sstDinv, d.sstDW1f, d.sstDWf, d.iblank_cell,
+                    c->fringe.src_nodes, c->fringe.src_ptr, c->fringe.src_cells, c->fringe.recv_node, c->fringe.nw,
+                    c->fringe.inode, c->fringe.w, c->fringe.recv_cells, c->fringe.qn, c->fringe.vals};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -470,6 +484,7 @@ void lusgs_step(cfd_case_s* c) {
     if (c->mlp) learned_update(c);
     else launch_lusgs_update(d, L, c->fp32());
     if (c->turb()) launch_sst_update(d, L);  // with rho after the flow's update
+    if (c->connected) launch_fringe(d, c->fringe, L);  // the components' data update between steps
 }
 
 void one_step(cfd_case_s* c) {
@@ -755,7 +770,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
                 dalloc(&d.swraf, 4 * (size_t)nc); dalloc(&d.Wf, nc);
                 dalloc(&d.dW1f, nc); dalloc(&d.dWf, nc);
             }
-            d.flow_grid = sweep_flow_max_grid(P.precision != CFD_PREC_FP64, P.sweep_blocks_per_sm);
+            set_sweep_shape(c, P.sweep_blocks_per_sm, P.sweep_threads);
             d.poll_ns = P.sweep_poll_ns < 0 ? 0 : (P.sweep_poll_ns > 10000 ? 10000 : P.sweep_poll_ns);
         }
         if (P.advance == CFD_ADV_LUSGS) {  // for the chain sweep schedule, built on first use
@@ -797,7 +812,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
         if (c->turb()) {
             sst_alloc(c);
             d.turb = 1;
-            d.sst_grid = sst_sweep_max_grid(P.sweep_blocks_per_sm > 0 ? P.sweep_blocks_per_sm : 4);
+            set_sweep_shape(c, P.sweep_blocks_per_sm, P.sweep_threads);
             sst_freestream(c);
         }
         auto L = c->L();
@@ -1048,6 +1063,180 @@ int cfd_residual_norm(cfd_case_t c, int mesh, int which, double* out) {
     if (which == CFD_NORM_L2_R_RHO) v = sqrt(v / (double)(c->coff[mesh + 1] - c->coff[mesh]));
     *out = v;
     return st;
+    ABI_CATCH
+}
+
+int cfd_connectivity(cfd_case_t c, const cfd_mesh_t* meshes, const int* const* obc_nodes, const int* nobc,
+                     int nfringe, int mexclude) {
+    if (!c || !meshes) return fail(CFD_ERR_ARG, "null argument");
+    if (c->nmesh < 2 || c->nmesh > 64) return fail(CFD_ERR_ARG, "overset connectivity needs 2 to 64 meshes");
+    if (c->p.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_STATE, "overset cases run the LU-SGS integrator");
+    if (c->mlp) return fail(CFD_ERR_STATE, "detach the learned relaxation before connecting");
+    if (nfringe < 1 || mexclude < 0) return fail(CFD_ERR_ARG, "nfringe >= 1 and mexclude >= 0");
+    for (int m = 0; m < c->nmesh; m++) {
+        if (!meshes[m]) return fail(CFD_ERR_ARG, "null mesh in list");
+        const HostMesh& h = meshes[m]->m;
+        if (h.ncell != c->coff[m + 1] - c->coff[m] || h.nedge != c->foff[m + 1] - c->foff[m] ||
+            h.nnode != c->noff[m + 1] - c->noff[m])
+            return fail(CFD_ERR_ARG, "the meshes are not the ones the case was created from");
+    }
+    const int nb = c->nmesh;
+    std::vector<cfd_block_t> blocks(nb, nullptr);
+    std::vector<cfd_holemap_t> maps(nb, nullptr);
+    cfd_connect_t conn = nullptr;
+    auto release = [&]() {
+        if (conn) cfd_connect_free(conn);
+        for (auto h : maps) if (h) cfd_holemap_free(h);
+        for (auto b : blocks) if (b) cfd_block_free(b);
+    };
+    int rc = CFD_OK;
+    for (int m = 0; m < nb && rc == CFD_OK; m++) {
+        rc = cfd_block_create(meshes[m], c->stream, &blocks[m]);
+        const HostMesh& h = meshes[m]->m;
+        bool wall = false;
+        for (int k = 0; k < h.nedge; k++) wall = wall || h.lr[2 * k + 1] == kWall;
+        if (rc == CFD_OK && wall) rc = cfd_holemap_create(blocks[m], 3, &maps[m]);
+    }
+    std::vector<int> zero(nb, 0);
+    std::vector<const int*> obc(nb, nullptr);
+    for (int m = 0; m < nb; m++) obc[m] = obc_nodes ? obc_nodes[m] : nullptr;
+    if (rc == CFD_OK) rc = cfd_overset_connect(nb, blocks.data(), maps.data(), obc.data(), nobc ? nobc : zero.data(),
+                                               nfringe, mexclude, &conn);
+    if (rc != CFD_OK) {
+        release();
+        return rc;
+    }
+    try {
+        DevArrays& d = c->d;
+        FringePlan& f = c->fringe;
+        // cell blanking of every mesh, receptor cells
+        std::vector<int> ibc(d.nc), rcells;
+        for (int m = 0; m < nb; m++) {
+            rc = cfd_connect_iblank(conn, m, nullptr, ibc.data() + c->coff[m]);
+            if (rc != CFD_OK) throw std::runtime_error(cfd_last_error());
+        }
+        for (int k = 0; k < d.nc; k++)
+            if (ibc[k] == -1) rcells.push_back(k);
+        // interpolation entries of every donor block, with global node ids
+        std::vector<int> recv, nwv, inode;
+        std::vector<double> wv;
+        for (int b = 0; b < nb; b++) {
+            long long n = 0;
+            if (cfd_connect_interp_count(conn, b, &n) != CFD_OK) throw std::runtime_error(cfd_last_error());
+            std::vector<int> rb(n), rn(n), dc(n), nw(n), in(4 * n);
+            std::vector<double> ww(4 * n);
+            if (n > 0 && cfd_connect_interp_get(conn, b, rb.data(), rn.data(), dc.data(), nw.data(), in.data(),
+                                                ww.data()) != CFD_OK)
+                throw std::runtime_error(cfd_last_error());
+            for (long long i = 0; i < n; i++) {
+                recv.push_back(rn[i] + c->noff[rb[i]]);
+                nwv.push_back(nw[i]);
+                for (int q = 0; q < 4; q++) {
+                    inode.push_back(q < nw[i] ? in[4 * i + q] + c->noff[b] : c->noff[b]);
+                    wv.push_back(q < nw[i] ? ww[4 * i + q] : 0.0);
+                }
+            }
+        }
+        // donor nodes and the cells around each (ascending)
+        std::vector<char> need(d.nn, 0);
+        for (size_t i = 0; i < nwv.size(); i++)
+            for (int q = 0; q < nwv[i]; q++) need[inode[4 * i + q]] = 1;
+        std::vector<int> cnt(d.nn + 1, 0);
+        for (int m = 0; m < nb; m++) {
+            const HostMesh& h = meshes[m]->m;
+            for (int k = 0; k < h.ncell; k++)
+                for (int v = 0; v < h.cell_nvert[k]; v++) {
+                    const int gn = h.cell_verts[4 * k + v] + c->noff[m];
+                    if (need[gn]) cnt[gn + 1]++;
+                }
+        }
+        std::vector<int> src, sptr(1, 0), scells;
+        std::vector<int> start(d.nn, 0);
+        for (int n = 0; n < d.nn; n++) cnt[n + 1] += cnt[n];
+        scells.resize(cnt[d.nn]);
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (int m = 0; m < nb; m++) {  // cells in ascending global order
+            const HostMesh& h = meshes[m]->m;
+            for (int k = 0; k < h.ncell; k++)
+                for (int v = 0; v < h.cell_nvert[k]; v++) {
+                    const int gn = h.cell_verts[4 * k + v] + c->noff[m];
+                    if (need[gn]) scells[fill[gn]++] = k + c->coff[m];
+                }
+        }
+        for (int n = 0; n < d.nn; n++)
+            if (need[n]) {
+                src.push_back(n);
+                sptr.push_back(cnt[n + 1]);
+            }
+        // compact the cell lists to the listed nodes
+        std::vector<int> scomp;
+        std::vector<int> sp2(1, 0);
+        for (size_t i = 0; i < src.size(); i++) {
+            for (int q = cnt[src[i]]; q < cnt[src[i] + 1]; q++) scomp.push_back(scells[q]);
+            sp2.push_back((int)scomp.size());
+        }
+        auto up = [&](auto** dst, const auto& v) {
+            using T = typename std::remove_reference<decltype(v)>::type::value_type;
+            if (*dst) cudaFree(*dst);
+            *dst = nullptr;
+            dalloc(dst, std::max<size_t>(v.size(), 1));
+            if (!v.empty())
+                ck(cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream), "upload");
+        };
+        up(&d.iblank_cell, ibc);
+        up(&f.src_nodes, src);
+        up(&f.src_ptr, sp2);
+        up(&f.src_cells, scomp);
+        up(&f.recv_node, recv);
+        up(&f.nw, nwv);
+        up(&f.inode, inode);
+        up(&f.w, wv);
+        up(&f.recv_cells, rcells);
+        if (f.qn) cudaFree(f.qn);
+        f.qn = nullptr;
+        dalloc(&f.qn, 4 * (size_t)d.nn);
+        ck(cudaMemsetAsync(f.qn, 0, 4 * (size_t)d.nn * sizeof(double), c->stream), "memset");
+        if (f.vals) cudaFree(f.vals);
+        f.vals = nullptr;
+        dalloc(&f.vals, std::max<size_t>(4 * recv.size(), 1));
+        f.nsrc = (int)src.size();
+        f.nrecv = (int)recv.size();
+        f.ncells = (int)rcells.size();
+        ck(cudaStreamSynchronize(c->stream), "sync");
+        c->connected = true;
+        c->drop_graph();
+    } catch (const CudaError& ex) {
+        release();
+        return fail(CFD_ERR_CUDA, ex.what());
+    } catch (const std::exception& ex) {
+        release();
+        return fail(CFD_ERR_MESH, ex.what());
+    }
+    release();
+    return CFD_OK;
+}
+
+int cfd_fringe_update(cfd_case_t c, int nvar) {
+    if (!c) return fail(CFD_ERR_ARG, "null case");
+    if (!c->connected) return fail(CFD_ERR_STATE, "call cfd_connectivity first");
+    if (nvar != 4) return fail(CFD_ERR_ARG, "the exchange carries the 4 primitive variables");
+    ABI_TRY
+    launch_fringe(c->d, c->fringe, c->L());
+    ck(cudaGetLastError(), "fringe launch");
+    return CFD_OK;
+    ABI_CATCH
+}
+
+int cfd_case_iblank(cfd_case_t c, int mesh, int* cell_iblank) {
+    if (!c || !cell_iblank) return fail(CFD_ERR_ARG, "null argument");
+    if (mesh < 0 || mesh >= c->nmesh) return fail(CFD_ERR_ARG, "mesh index out of range");
+    if (!c->connected) return fail(CFD_ERR_STATE, "call cfd_connectivity first");
+    ABI_TRY
+    const int off = c->coff[mesh], n = c->coff[mesh + 1] - off;
+    ck(cudaMemcpyAsync(cell_iblank, c->d.iblank_cell + off, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost,
+                       c->stream), "download");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    return CFD_OK;
     ABI_CATCH
 }
 
@@ -1797,7 +1986,7 @@ extern "C" int cfd_set_precision(cfd_case_t c, int precision) {
     c->d.resid32 = precision == CFD_PREC_FP32 ? 1 : 0;
     c->d.residq = precision == CFD_PREC_MIXFF ? 1 : 0;
     if (c->p.advance == CFD_ADV_LUSGS)
-        c->d.flow_grid = sweep_flow_max_grid(precision != CFD_PREC_FP64, c->p.sweep_blocks_per_sm);
+        set_sweep_shape(c, c->p.sweep_blocks_per_sm, c->d.flow_threads);
     c->drop_graph();
     ck(cudaStreamSynchronize(c->stream), "sync");
     return CFD_OK;
@@ -1863,10 +2052,11 @@ extern "C" int cfd_chain_schedule(cfd_mesh_t mesh, int forward, int nlists, int 
     }
 }
 
-extern "C" int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm) {
+extern "C" int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm, int* threads) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
     if (sweep_mode) *sweep_mode = c->p.sweep_mode;
     if (blocks_per_sm) *blocks_per_sm = c->p.sweep_blocks_per_sm;
+    if (threads) *threads = c->d.flow_threads;
     return CFD_OK;
 }
 
@@ -1889,47 +2079,70 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
     ck(cudaMemcpyAsync(W0, d.W, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "save");
     ck(cudaMemcpyAsync(dW0, d.dW, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "save");
     ck(cudaMemcpyAsync(&err0, d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream), "save");
+    // the coupled turbulence model's state (k, omega, W_t, mu_t) too
+    std::vector<double> sst_save;
+    if (c->turb()) {
+        sst_save.resize(5 * nc);
+        ck(cudaMemcpyAsync(sst_save.data(), d.sstT, 2 * nc * 8, cudaMemcpyDeviceToHost, c->stream), "save");
+        ck(cudaMemcpyAsync(sst_save.data() + 2 * nc, d.sstW, 2 * nc * 8, cudaMemcpyDeviceToHost, c->stream), "save");
+        ck(cudaMemcpyAsync(sst_save.data() + 4 * nc, d.sstMut, nc * 8, cudaMemcpyDeviceToHost, c->stream), "save");
+    }
     upload_freestream(c);  // synchronises: err0 is valid from here
     const bool low = c->p.precision != CFD_PREC_FP64;
-    const int max_grid = sweep_flow_max_grid(low, 64);  // occupancy limit
     // the binary32 forms also choose between the round-robin dataflow sweep
     // (mode 0: wide levels, many cells in flight) and the chain schedules
     // (narrow levels, long dependence chains; mode 5 spreads a block's lists,
     // mode 6 keeps neighbouring lists in one block with a shared-memory hand-off)
     std::vector<int> modes{c->p.sweep_mode};
     if (c->fast_sweep() && (c->p.sweep_mode == 0 || c->p.sweep_mode == 5 || c->p.sweep_mode == 6)) modes = {0, 5, 6};
-    const int mode0 = c->p.sweep_mode;
-    int best = 0, best_mode = mode0;
+    const int mode0 = c->p.sweep_mode, threads0 = d.flow_threads;
+    int best = 0, best_mode = mode0, best_threads = threads0;
     double best_t = 1e300;
     int rc = CFD_OK;
     for (int mode : modes) {
         c->p.sweep_mode = mode;
-        int last_grid = -1;
-        for (int bpsm = 1; bpsm <= 8 && rc == CFD_OK; bpsm++) {
-            const int grid = sweep_flow_max_grid(low, bpsm);
-            if (grid > max_grid) break;
-            d.flow_grid = grid;
-            const int eff = c->chain_sweep() ? chain_grid(c) : grid;
-            if (eff == last_grid) break;  // capped by occupancy: nothing new to try
-            last_grid = eff;
-            c->drop_graph();
-            double ms = 0;
-            rc = cfd_bench_pass(c, 7, 1, 0, &ms);  // untimed: schedule build, first launches
-            if (rc == CFD_OK) rc = cfd_bench_pass(c, 7, reps, 0, &ms);
-            if (rc == CFD_OK && ms < best_t) {
-                best_t = ms;
-                best = bpsm;
-                best_mode = mode;
+        // the chain schedules run 256-thread blocks; the round-robin sweeps also try
+        // fewer warps per block (fewer cells sharing one sub-partition's pipes)
+        const bool chain = c->fast_sweep() && (mode == 5 || mode == 6);
+        std::vector<int> tlist = chain ? std::vector<int>{256} : std::vector<int>{256, 128, 64};
+        for (int threads : tlist) {
+            const int max_grid = sweep_flow_max_grid(low, 64, threads);  // occupancy limit
+            int last_grid = -1;
+            for (int bpsm = 1; bpsm <= 16 && rc == CFD_OK; bpsm++) {
+                set_sweep_shape(c, bpsm, threads);
+                const int grid = d.flow_grid;
+                if (grid > max_grid) break;
+                const int eff = c->chain_sweep() ? chain_grid(c) : grid;
+                if (eff == last_grid) break;  // capped by occupancy: nothing new to try
+                last_grid = eff;
+                c->drop_graph();
+                double ms = 0;
+                rc = cfd_bench_pass(c, 7, 1, 0, &ms);  // untimed: schedule build, first launches
+                if (rc == CFD_OK) rc = cfd_bench_pass(c, 7, reps, 0, &ms);
+                if (rc == CFD_OK && ms < best_t) {
+                    best_t = ms;
+                    best = bpsm;
+                    best_mode = mode;
+                    best_threads = threads;
+                }
             }
         }
     }
     c->p.sweep_mode = rc == CFD_OK ? best_mode : mode0;
     if (rc == CFD_OK) {
         c->p.sweep_blocks_per_sm = best;
-        d.flow_grid = sweep_flow_max_grid(low, best);
+        set_sweep_shape(c, best, best_threads);
         c->drop_graph();
         if (best_blocks_per_sm) *best_blocks_per_sm = best;
         if (best_ms) *best_ms = best_t;
+    } else {
+        set_sweep_shape(c, c->p.sweep_blocks_per_sm, threads0);
+        c->drop_graph();
+    }
+    if (c->turb()) {
+        ck(cudaMemcpyAsync(d.sstT, sst_save.data(), 2 * nc * 8, cudaMemcpyHostToDevice, c->stream), "restore");
+        ck(cudaMemcpyAsync(d.sstW, sst_save.data() + 2 * nc, 2 * nc * 8, cudaMemcpyHostToDevice, c->stream), "restore");
+        ck(cudaMemcpyAsync(d.sstMut, sst_save.data() + 4 * nc, nc * 8, cudaMemcpyHostToDevice, c->stream), "restore");
     }
     ck(cudaMemcpyAsync(d.U, U0, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "restore");
     ck(cudaMemcpyAsync(d.W, W0, nc * sizeof(d4), cudaMemcpyDeviceToDevice, c->stream), "restore");

@@ -588,7 +588,7 @@ cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forwa
                     (void*)&d.swfc, (void*)&d.swra, (void*)&d.R, (void*)&d.diag, (void*)&d.invD, (void*)&d.dW1,
                     (void*)&d.dW, (void*)&d.err, (void*)&d.poll_ns};
     void* fn = forward ? (void*)k_sweep_flow<true> : (void*)k_sweep_flow<false>;
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(d.flow_threads), args, 0, L.stream);
     *L.counter += 1;
     return e;
 }
@@ -707,7 +707,7 @@ cudaError_t launch_sweep_pair64(const DevArrays& d, const LaunchCfg& L, bool for
                     (void*)&d.swfc, (void*)&d.swra, (void*)&d.R, (void*)&d.diag, (void*)&d.dW1, (void*)&d.dW,
                     (void*)&d.err, (void*)&d.poll_ns};
     void* fn = forward ? (void*)k_sweep_pair64<true> : (void*)k_sweep_pair64<false>;
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(d.flow_threads), args, 0, L.stream);
     *L.counter += 1;
     return e;
 }
@@ -907,30 +907,30 @@ cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool for
                     (void*)&d.dW1f, (void*)&d.dWf, (void*)&d.err, (void*)&d.poll_ns};
     void* fn = independent ? (forward ? (void*)k_sweep_flow32<true, true> : (void*)k_sweep_flow32<false, true>)
                            : (forward ? (void*)k_sweep_flow32<true, false> : (void*)k_sweep_flow32<false, false>);
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, L.stream);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(d.flow_threads), args, 0, L.stream);
     *L.counter += 1;
     return e;
 }
 
-int sweep_flow_max_grid(bool low, int blocks_per_sm) {
+int sweep_flow_max_grid(bool low, int blocks_per_sm, int threads) {
     int dev = 0, sms = 0, per = 0, per2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     void* fn = low ? (void*)k_sweep_flow32<true, false> : (void*)k_sweep_flow<true>;
     void* fn2 = low ? (void*)k_sweep_flow32<false, false> : (void*)k_sweep_flow<false>;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, fn2, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, fn2, threads, 0);
     per = per < per2 ? per : per2;
     if (low) {  // the independent-halves variant runs on the same grid
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_flow32<true, true>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_flow32<true, true>, threads, 0);
         per = per < per2 ? per : per2;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_flow32<false, true>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_flow32<false, true>, threads, 0);
         per = per < per2 ? per : per2;
     }
     if (!low) {  // the plain form's paired kernels run on the same grid
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_pair64<true>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_pair64<true>, threads, 0);
         per = per < per2 ? per : per2;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_pair64<false>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_pair64<false>, threads, 0);
         per = per < per2 ? per : per2;
     }
     if (per < 1) per = 1;
@@ -1445,9 +1445,10 @@ void launch_inv_diag(const DevArrays& d, const LaunchCfg& L) {
 
 // W += dW, U = prim(W)  (LUSGSIntegrator::UpdatePrimitiveVariable, LUSGS_Integrator.cpp:242-255)
 __global__ void k_lusgs_update(int nc, const d4* __restrict__ dW, d4* __restrict__ W, d4* __restrict__ U,
-                               float4* __restrict__ Uf, unsigned* __restrict__ err) {
+                               float4* __restrict__ Uf, unsigned* __restrict__ err, const int* __restrict__ iblank) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
+    if (iblank && iblank[c] != 1) return;  // overset holes and receptors keep their state
     double w[4], dw[4], u[4];
     to_arr(ld4(W + c), w);
     to_arr(ld4(dW + c), dw);
@@ -1460,7 +1461,8 @@ __global__ void k_lusgs_update(int nc, const d4* __restrict__ dW, d4* __restrict
     if (!(u[0] > 0.0) || !(u[1] > 0.0)) atomicOr(err, ERR_NONPHYS);
 }
 void launch_lusgs_update(const DevArrays& d, const LaunchCfg& L, bool fp32_copy) {
-    k_lusgs_update<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.dW, d.W, d.U, fp32_copy ? d.Uf : nullptr, d.err);
+    k_lusgs_update<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.dW, d.W, d.U, fp32_copy ? d.Uf : nullptr, d.err,
+                                                          d.iblank_cell);
     *L.counter += 1;
 }
 

@@ -461,14 +461,14 @@ void launch_sst_update_mut(const DevArrays& d, const LaunchCfg& L) {
 
 namespace cfdgb {
 
-int sst_sweep_max_grid(int blocks_per_sm) {
+int sst_sweep_max_grid(int blocks_per_sm, int threads) {
     int dev = 0, sms = 0, a = 0, b = 0, c2 = 0, d2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, (void*)k_sst_sweep<true, double>, 256, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (void*)k_sst_sweep<false, double>, 256, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, (void*)k_sst_sweep<true, float>, 256, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d2, (void*)k_sst_sweep<false, float>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, (void*)k_sst_sweep<true, double>, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (void*)k_sst_sweep<false, double>, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, (void*)k_sst_sweep<true, float>, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d2, (void*)k_sst_sweep<false, float>, threads, 0);
     int per = a < b ? a : b;
     per = per < c2 ? per : c2;
     per = per < d2 ? per : d2;
@@ -484,7 +484,7 @@ cudaError_t launch_sst_sweeps(const DevArrays& d, const LaunchCfg& L, bool fp32)
         void* args[] = {(void*)&d, (void*)&order};
         void* fn = fp32 ? (dir == 0 ? (void*)k_sst_sweep<true, float> : (void*)k_sst_sweep<false, float>)
                         : (dir == 0 ? (void*)k_sst_sweep<true, double> : (void*)k_sst_sweep<false, double>);
-        cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(d.sst_grid), dim3(256), args, 0, L.stream);
+        cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(d.sst_grid), dim3(d.flow_threads), args, 0, L.stream);
         *L.counter += 1;
         if (e != cudaSuccess) return e;
     }
