@@ -60,8 +60,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2")
-    ap.add_argument("--precision", default="mixff", choices=["fp64", "fp32", "mixed", "mixff"])
+    ap.add_argument("--config", default="c3", help="workload: c3 (SST airfoil, 1.07M cells), c2, c2big, c1")
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "fp32", "mixed", "mixff"],
+                    help="headline form (auto: mixff, the float-float residual with the binary32 sweeps)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -76,6 +77,10 @@ def parse():
     ap.add_argument("--drop-forms", default="fp64,mixff,fp32+learned>mixff",
                     help="forms for time_to_drop: PREC[>PREC2][+learned]; '>' switches at --switch-at "
                          "(others: fp32, mixed, mixed+learned, fp32+learned>mixed)")
+    ap.add_argument("--sst-drop-forms", default="fp64,mixff,mixed",
+                    help="forms of the SST case's equal-fall run (the first sets the fall)")
+    ap.add_argument("--sst-drop-seconds", type=float, default=150.0,
+                    help="time the first form of the SST case runs; the others run to the fall it reached")
     ap.add_argument("--switch-at", type=float, default=3e-4,
                     help="residual fall at which 'A>B' switches form (or earlier, once A's residual stalls)")
     ap.add_argument("--no-overset", action="store_true", help="skip the overset connectivity / exchange leg")
@@ -165,6 +170,21 @@ def alg_bytes(pass_name: str, nc: int, nf: int, viscous: bool, precision: str) -
         return nc * (4 + 16 + 32 + 8 + v * s + 32 + 32 + 32 + 32) + nf * (8 + 32 + v * 32)
     if pass_name == "lusgs_update":
         return nc * (32 + 64 + 32 + (16 if fp32 else 0))
+    # the coupled SST model (binary64 arrays): its four residual passes (face values and mu_t; k, omega
+    # gradients and F1 / F2; face fluxes; sources, residual and diagonal), the turbulence sweeps (per-slot
+    # constants, then forward and backward), the k, omega, mu_t update
+    if pass_name == "sst_residual":
+        face = nf * (8 + 32 + 4 + 32 + 8 + 16 + 8) + nc * (16 + 8 + 8)
+        cell = nc * (16 + 32 + 16 + 8 + 8 + 32 + 8 + 8 + 32) + nf * (32 + 16)
+        flux = nf * (8 + 32 + 32 + 16 + 16 + 8 + 8 + 16) + nc * (16 + 32 + 32 + 8 + 32)
+        total = nc * (8 + 32 + 32 + 16 + 8 + 32 + 32 + 16 + 16 + 16 + 8 + 8 + 8) + nf * 32
+        return face + cell + flux + total
+    if pass_name == "sst_sweeps":
+        prep = nc * (16 + 32 + 32 + 32 + 16 + 32 + 8 + 8 + 16 + 64 + 32 + 32 + 32 + 16) + nf * (8 + 32 + 32)
+        sweep = nc * (4 + 16 + 16 + 64 + 32 + 32 + 16 + 16 + 16) + nf * 8
+        return prep + 2 * sweep
+    if pass_name == "sst_update":
+        return nc * (4 + 16 + 16 + 32 + 16 + 16 + 8 + 32 + 8)
     raise KeyError(pass_name)
 
 
@@ -305,6 +325,34 @@ def overset_leg(stream) -> dict:
     torch.cuda.synchronize()
     out_a["exchange_us"] = round(1e3 * t0.elapsed_time(t1) / reps, 2)
     out["assembly"] = out_a
+    # the coupled solve: both components in one case (Euler, M 0.3, LU-SGS in the MIXFF form), field cells
+    # updated, the fringe exchange (cell means at the donor nodes, interpolation, node means into the
+    # receptor cells) at the end of every graph-captured step
+    fs = dict(mach=0.3, aoa_deg=0.0, reynolds=1e6)
+    case = abi.Case(meshes, [fs, fs], abi.FLOW_EULER, abi.ADV_LUSGS, abi.PREC_MIXFF, cfl=5.0,
+                    stream=stream.cuda_stream, sweep_mode=5)
+    case.init_freestream()
+    tc = time.perf_counter()
+    case.connect(meshes, [None, rec_o], nfringe=2, mexclude=3)
+    connect_ms = 1e3 * (time.perf_counter() - tc)
+    case.autotune(2)
+    case.step_graph(5)
+    case.sync()
+    step_ms = case.bench_pass("step", 10, FLUSH_BYTES)
+    fringe_ms = case.bench_pass("fringe", 10, FLUSH_BYTES)
+    case.step_graph(200)
+    case.sync()
+    ib = [case.iblank(0), case.iblank(1)]
+    ncell = meshes[0].ncell + meshes[1].ncell
+    out["coupled"] = {"workload": "the two components in one case, Euler M 0.3, LU-SGS CFL 5, MIXFF form",
+                      "cells": ncell, "connect_ms": round(connect_ms, 1), "ms_per_step": round(step_ms, 4),
+                      "cell_iters_per_s": ncell / (step_ms * 1e-3), "fringe_ms": round(fringe_ms, 4),
+                      "hole_cells": [int((i == 0).sum()) for i in ib],
+                      "receptor_cells": [int((i == -1).sum()) for i in ib],
+                      "sweep": dict(zip(("mode", "blocks_per_sm", "threads"), case.sweep_config())),
+                      "finite_after_200_steps": bool(np.isfinite(case.get("U", 0)).all() and
+                                                     np.isfinite(case.get("U", 1)).all())}
+    case.close()
     for p in paths:
         p.unlink()
     return out
@@ -392,13 +440,23 @@ def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5, mode: in
             "solver_errors": sorted(set(errors))}
 
 
-def cpu_baseline(grd_path: str, w, seconds: float) -> dict:
-    """C restatement of the reference's serial LU-SGS path on one host core."""
+def oracle_for(w):
+    """The C restatement (the reference's serial path; with the SST model coupled as the GPU runs it) on the
+    workload's mesh, from the freestream."""
     import oracle
     from oracle import grd
 
-    t = grd.read_grd(grd_path, w.mesh.wall_tag, w.mesh.far_tag)
-    o = oracle.Oracle(t, w.mach, w.aoa, w.re, w.flow == "laminar")
+    g = w.mesh
+    t = grd.topo_from_arrays(g.xy, g.edge_nodes, g.edge_cells, g.ncell, g.wall_tag, g.far_tag)
+    o = oracle.Oracle(t, w.mach, w.aoa, w.re, w.flow in ("laminar", "sst"))
+    if w.flow == "sst":
+        o.sst_enable(True, w.extra.get("tu", 0.01), w.extra.get("mut_ratio", 0.035))
+    return t, o
+
+
+def cpu_baseline(w, seconds: float) -> dict:
+    """C restatement of the reference's serial LU-SGS path on one host core."""
+    t, o = oracle_for(w)
     o.lusgs_step(w.cfl) if w.advance == "lusgs" else o.rk_step()  # warm-up step
     n = 0
     t0 = time.perf_counter()
@@ -414,15 +472,12 @@ def cpu_baseline(grd_path: str, w, seconds: float) -> dict:
 
 
 def _ref_worker(args):
-    grd_path, cfg_name, steps, warmup, barrier = args
+    cfg_name, steps, warmup, barrier = args
     sys.path.insert(0, str(ROOT))
     from tmp_gb300 import configs
-    import oracle
-    from oracle import grd
 
     w = configs.WORKLOADS[cfg_name]()
-    t = grd.read_grd(grd_path, w.mesh.wall_tag, w.mesh.far_tag)
-    o = oracle.Oracle(t, w.mach, w.aoa, w.re, w.flow == "laminar")
+    t, o = oracle_for(w)
     step = (lambda: o.lusgs_step(w.cfl)) if w.advance == "lusgs" else (lambda: o.rk_step())
     for _ in range(warmup):
         step()
@@ -447,7 +502,6 @@ def run_reference(args):
 
     oracle.build()
     w = configs.WORKLOADS[args.config]()
-    path = str(configs.grd_path(w))
     ncores = os.cpu_count() or 1
     steps = max(1, args.steps)  # the same timed steps as the GPU arm
     warm = max(3, args.warmup)  # at least three untimed steps per copy
@@ -455,7 +509,7 @@ def run_reference(args):
     t0 = time.perf_counter()
     with ctx.Manager() as mgr, ctx.Pool(ncores) as pool:
         barrier = mgr.Barrier(ncores)
-        res = pool.map(_ref_worker, [(path, args.config, steps, warm, barrier)] * ncores, chunksize=1)
+        res = pool.map(_ref_worker, [(args.config, steps, warm, barrier)] * ncores, chunksize=1)
     wall = time.perf_counter() - t0
     cells = sum(r[0] for r in res)
     slowest = max(r[1] for r in res)
@@ -464,7 +518,7 @@ def run_reference(args):
             "steps": steps, "warmup": warm, "ms_per_step": 1e3 * slowest / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": w.name, "ncell": w.mesh.ncell, "nedge": w.mesh.nedge, "mach": w.mach,
-                       "re": w.re, "cfl": w.cfl, "copies": ncores},
+                       "aoa": w.aoa, "re": w.re, "cfl": w.cfl, "flow": w.flow, "copies": ncores},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
                              "sample": f"{ncores} independent copies x {steps} {w.advance} steps of the "
                                        f"{w.mesh.ncell}-cell workload (oracle/cfd_oracle.c, bit-exact restatement "
@@ -494,32 +548,45 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     build_library()
     w = configs.WORKLOADS[args.config]()
-    path = configs.grd_path(w)
-    mesh = abi.Mesh.load_grd(path, w.mesh.wall_tag, w.mesh.far_tag)
-    viscous = w.flow == "laminar"
+    g = w.mesh
+    mesh = abi.Mesh.from_arrays(g.xy, g.edge_nodes, g.edge_cells, g.ncell, g.wall_tag, g.far_tag)
+    viscous = w.flow in ("laminar", "sst")
+    if args.precision == "auto":
+        args.precision = "mixff"
     stream = torch.cuda.Stream()  # a real stream: graph capture is not allowed on the legacy default stream
     torch.cuda.set_stream(stream)
     prec_code = dict(fp64=abi.PREC_FP64, fp32=abi.PREC_FP32, mixed=abi.PREC_MIXED, mixff=abi.PREC_MIXFF)
+    flow_code = dict(euler=abi.FLOW_EULER, laminar=abi.FLOW_LAMINAR, sst=abi.FLOW_SST)
 
     def sweep_mode_for(precision):
         if args.sweep_mode >= 0:
             return args.sweep_mode
         return 5 if precision in ("fp32", "mixed", "mixff") else 0
 
-    def make_case(precision):
+    def make_case(precision, wl=None, msh=None):
+        wl, msh = wl or w, msh or mesh
         mode = sweep_mode_for(precision)
-        c = abi.Case([mesh], [dict(mach=w.mach, aoa_deg=w.aoa, reynolds=w.re)],
-                     abi.FLOW_LAMINAR if viscous else abi.FLOW_EULER,
-                     abi.ADV_LUSGS if w.advance == "lusgs" else abi.ADV_RK5,
-                     prec_code[precision], cfl=w.cfl, stream=stream.cuda_stream,
+        c = abi.Case([msh], [dict(mach=wl.mach, aoa_deg=wl.aoa, reynolds=wl.re)], flow_code[wl.flow],
+                     abi.ADV_LUSGS if wl.advance == "lusgs" else abi.ADV_RK5,
+                     prec_code[precision], cfl=wl.cfl, stream=stream.cuda_stream,
                      sweep_mode=mode, sweep_blocks_per_sm=args.sweep_bpsm,
                      sweep_poll_ns=args.sweep_poll_ns)
+        if wl.flow == "sst":
+            abi.sst_set_inflow(c, wl.extra.get("tu", 0.01), wl.extra.get("mut_ratio", 0.035))
         c.init_freestream()
         c.tuned = None
-        if args.sweep_bpsm == 0 and w.advance == "lusgs" and mode in (0, 3, 4, 5):
-            c.autotune(3)  # the sweeps' blocks per SM (and mode 0 or 5), by timing whole steps
+        if args.sweep_bpsm == 0 and wl.advance == "lusgs" and mode in (0, 3, 4, 5):
+            c.autotune(3)  # the sweeps' launch shape (and mode 0, 5 or 6), by timing whole steps
             c.tuned = c.sweep_config()
         return c
+
+    def form_ok(f, wl=None):
+        wl = wl or w
+        if wl.advance != "lusgs" and "mix" in f:  # the mixed forms are LU-SGS forms
+            return False
+        if wl.flow == "sst" and "fp32" in f:  # the coupled SST model runs with the binary64 or float-float residual
+            return False
+        return True
 
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
@@ -581,7 +648,7 @@ def run_ours(args):
 
     # the other precision forms, timed the same way
     forms = {}
-    for f in [x for x in args.forms.split(",") if x and x != args.precision and (w.advance == "lusgs" or "mix" not in x)]:
+    for f in [x for x in args.forms.split(",") if x and x != args.precision and form_ok(x)]:
         c2 = make_case(f)
         fm, _ = timed_steps(c2, args.steps)
         forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3),
@@ -595,52 +662,82 @@ def run_ours(args):
     plain = forms.get("fp64")
 
     # wall time from the freestream start to a residual fall of args.drop, per
-    # form, and with the committed learned relaxation on the mixed form
-    drop = None
-    if args.drop > 0 and rank == 0:
+    # form, and with the committed learned relaxation
+    def time_to_drop(wl, msh, forms, target, cap, equal_fall=False):
+        """equal_fall: the first form runs for `cap` seconds (or to `target`), the others to the fall it
+        reached (at most 3 cap), so that every form is timed to the same residual fall."""
         from tmp_gb300 import learn
 
         net = learn.load()
-        drop = {"target": args.drop, "norm": "L2 density residual / iteration 1", "cap_s": args.drop_seconds,
-                "learned_weights": str(learn.WEIGHTS.relative_to(ROOT)) if net else None}
-        for f in [x for x in args.drop_forms.split(",") if x]:
+        out = {"workload": wl.name, "target": target, "norm": "L2 density residual / iteration 1", "cap_s": cap,
+               "learned_weights": str(learn.WEIGHTS.relative_to(ROOT)) if net else None}
+        first_done = False
+        for f in [x for x in forms.split(",") if x]:
             # "A>B" switches form A to B; "+learned" at the end keeps the learned
             # relaxation on throughout, "A+learned>B" only until the switch
             learned = "+learned" in f
-            if learned and (net is None or w.advance != "lusgs"):
+            if learned and (net is None or wl.advance != "lusgs"):
                 continue
-            if w.advance != "lusgs" and ("mix" in f):  # the mixed forms are LU-SGS forms
+            if not form_ok(f, wl):
                 continue
             first, _, then = f.partition(">")
             until_switch = first.endswith("+learned")
             first = first.replace("+learned", "")
             then = then.replace("+learned", "")
-            c2 = make_case(first)
+            c2 = make_case(first, wl, msh)
             torch.cuda.synchronize()
-            r = learn.run_to_drop(c2, args.drop, 10 ** 9, net if learned else None, chunk=50,
-                                  max_seconds=args.drop_seconds, switch_at=args.switch_at if then else None,
+            r = learn.run_to_drop(c2, target, 10 ** 9, net if learned else None, chunk=50,
+                                  max_seconds=cap if not (equal_fall and first_done) else 3 * cap,
+                                  switch_at=args.switch_at if then else None,
                                   switch_to=prec_code[then] if then else None, detach_at_switch=until_switch)
-            drop[f] = {"reached": r.reached, "seconds": round(r.seconds, 3), "iterations": r.iterations,
-                       "fall": r.history[-1][1], "fell_back": r.fell_back}
+            reached = r.reached
+            if equal_fall and not first_done:
+                target = max(target, r.history[-1][1])  # the fall the first form reached in its time
+                out["equal_fall_target"] = target
+                reached = True
+            first_done = True
+            out[f] = {"reached": reached, "seconds": round(r.seconds, 3), "iterations": r.iterations,
+                      "fall": r.history[-1][1], "fell_back": r.fell_back}
             try:  # lift and drag of the state reached (wall force in the form's own arithmetic)
                 wf = c2.wall_force()
-                drop[f]["cl"], drop[f]["cd"] = wf["cl"], wf["cd"]
+                out[f]["cl"], out[f]["cd"] = wf["cl"], wf["cd"]
             except abi.CfdError:
                 pass
             c2.close()
-        ref = drop.get("fp64")
+        ref = out.get("fp64")
         if isinstance(ref, dict) and "cd" in ref:
             # each form's lift and drag at its final state against the plain binary64 run's (CL is
-            # compared absolutely: it is near zero on a symmetric body)
-            drop["vs_fp64"] = {f: {"cl_abs_diff": abs(v["cl"] - ref["cl"]),
-                                   "cd_rel_diff": abs(v["cd"] - ref["cd"]) / max(abs(ref["cd"]), 1e-300),
-                                   "fall_ratio": v["fall"] / ref["fall"]}
-                               for f, v in drop.items() if isinstance(v, dict) and "cd" in v and f != "fp64"}
+            # compared absolutely: it is near zero on a symmetric body at zero incidence)
+            out["vs_fp64"] = {f: {"cl_abs_diff": abs(v["cl"] - ref["cl"]),
+                                  "cd_rel_diff": abs(v["cd"] - ref["cd"]) / max(abs(ref["cd"]), 1e-300),
+                                  "fall_ratio": v["fall"] / ref["fall"]}
+                              for f, v in out.items() if isinstance(v, dict) and "cd" in v and f != "fp64"}
+            done = {f: v for f, v in out.items() if isinstance(v, dict) and v.get("reached")}
+            if "fp64" in done:
+                out["speedup_vs_fp64"] = {f: done["fp64"]["seconds"] / v["seconds"] for f, v in done.items()
+                                          if f != "fp64"}
+        return out
+
+    drop = None
+    drop_c2 = None
+    if args.drop > 0 and rank == 0:
+        if w.flow == "sst":
+            # the SST airfoil: both forms for a bounded time (the fall each reaches in it)
+            drop = time_to_drop(w, mesh, args.sst_drop_forms, args.drop, args.sst_drop_seconds, equal_fall=True)
+            # and the metric's 1e-8 fall, measured, on the laminar cylinder (C2)
+            w2 = configs.c2()
+            g2 = w2.mesh
+            m2 = abi.Mesh.from_arrays(g2.xy, g2.edge_nodes, g2.edge_cells, g2.ncell, g2.wall_tag, g2.far_tag)
+            drop_c2 = time_to_drop(w2, m2, args.drop_forms, args.drop, args.drop_seconds)
+        else:
+            drop = time_to_drop(w, mesh, args.drop_forms, args.drop, args.drop_seconds)
 
     # per-pass device times for the roofline (L2 flushed before each rep)
     passes = ["face_state", "cell_grad", "face_flux", "cell_update"]
     if w.advance == "lusgs":
         passes += ["sweep_fwd", "sweep_bwd", "lusgs_update"]
+    if w.flow == "sst":
+        passes += ["sst_residual", "sst_sweeps", "sst_update"]
     mode = sweep_mode_for(args.precision)
     per, launches_of = {}, {}
     for p in passes:
@@ -653,7 +750,8 @@ def run_ours(args):
     per_step = dict(per)
     if w.advance == "rk5":
         per_step = {p: 5 * v for p, v in per.items()}
-    dominant = max(per_step, key=per_step.get)
+    # the dominant single kernel (the SST rows hold several launches each)
+    dominant = max((p for p in per_step if p not in ("sst_residual", "sst_sweeps")), key=per_step.get)
     nlev = mesh.levels()
     peak, peak_kind = measured_peak_gbs()
     rows = {}
@@ -699,13 +797,15 @@ def run_ours(args):
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision], "data": "synthetic",
             "config": {"workload": w.name, "ncell": nc, "nedge": nf, "levels": list(nlev), "mach": w.mach,
-                       "re": w.re, "cfl": w.cfl, "precision": args.precision,
+                       "aoa": w.aoa, "re": w.re, "cfl": w.cfl, "flow": w.flow, **w.extra, "precision": args.precision,
                        "sweep": dict(zip(("mode", "blocks_per_sm", "threads"), case.sweep_config())),
                        "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
             "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms_per_step"], "e2e": plain.get("e2e"),
                            "note": "every kernel in binary64, results equal to the reference's"} if plain else None,
             "forms": forms, "time_to_drop": drop}
+    if drop_c2 is not None:
+        line["time_to_drop_c2"] = drop_c2
     if rank == 0 and not args.no_overset:
         line["overset"] = overset_leg(stream)
     if rank == 0 and not args.no_batch and w.advance == "lusgs":
@@ -714,7 +814,7 @@ def run_ours(args):
         except Exception as ex:  # the leg is reported beside the headline, never instead of it
             line["batch"] = {"error": f"{type(ex).__name__}: {ex}"}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(str(path), w, args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -44,7 +44,7 @@ extern "C" {
                                  viscous flux and radii, dt = CFL vol /
                                  (spec_c + 4 spec_v), a two-equation
                                  turbulence sweep after the flow's.  LU-SGS
-                                 with the FP64 or MIXED form only          */
+                                 with the FP64, MIXED or MIXFF form        */
 #define CFD_ADV_RK5       0   /* RungeKuttaStrategy(5)                     */
 #define CFD_ADV_LUSGS     1   /* LUSGSIntegrator                           */
 #define CFD_PREC_FP64     0   /* plain: every kernel in binary64           */
@@ -253,7 +253,10 @@ long long cfd_launch_count(cfd_case_t c);
  * stream, each bracketed by CUDA events, writing flush_bytes to a scratch
  * buffer before each rep to evict L2, and return the mean duration in ms.
  * pass: 0 face_state, 1 cell_grad, 2 face_flux, 3 cell_update, 4 forward sweep
- * (all levels), 5 backward sweep (all levels), 6 LU-SGS update, 7 whole step. */
+ * (all levels), 5 backward sweep (all levels), 6 LU-SGS update, 7 whole step;
+ * coupled SST cases: 8 the model's residual passes, 9 the turbulence sweeps
+ * (constants, forward, backward), 10 the k, omega, mu_t update; connected
+ * overset cases: 11 the fringe exchange. */
 int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms);
 /* Autotuner of the dataflow sweeps' launch shape (no reference counterpart):
  * times `reps` whole LU-SGS steps for each co-resident block count per SM

@@ -83,20 +83,31 @@ def test_coupled_sst_steps_match_oracle(built_lib, mesh_file, ma, aoa, re, cfl, 
     case.close()
 
 
-def test_coupled_sst_mixed_form_follows_plain(built_lib):
+@pytest.mark.parametrize("form", ["MIXED", "MIXFF"])
+def test_coupled_sst_fast_forms_follow_plain(built_lib, form):
     """The MIXED form (binary32 flow and turbulence sweeps as the implicit
-    operator, binary64 residual) converges to the plain form's state."""
+    operator, binary64 residual) and the MIXFF form (the flow residual in
+    float-float pairs, the model in binary64) converge to the plain form's
+    state."""
     from tmp_gb300 import abi
 
-    o, case = setup("mixed.grd", 0.3, 2.0, 1e5, 5.0, 0.01, 0.035, abi.PREC_MIXED, 5)
-    for _ in range(400):
-        o.lusgs_step(5.0)
-    case.step_graph(400)
+    prec = abi.PREC_MIXED if form == "MIXED" else abi.PREC_MIXFF
+    o, case = setup("mixed.grd", 0.3, 2.0, 1e5, 5.0, 0.01, 0.035, prec, 5)
+    case.residual()
     case.sync()
-    assert rel(case.get("U"), o.field("U")) <= 1e-5
-    assert rel(case.get("SST_T"), o.sst_field("SST_T")) <= 1e-3
-    r = case.norm("L2_R_RHO")
-    assert np.isfinite(r)
+    o.residual()
+    o.sst_equation()
+    # the residual of the first state: binary64 (contracted) or float-float arithmetic against binary64
+    assert rel(case.get("R"), o.field("R")) <= 1e-9
+    for _ in range(2000):
+        o.lusgs_step(5.0)
+    case.step_graph(2000)
+    case.sync()
+    # (the binary32 sweeps change the path, not the fixed point: the states differ by the
+    # iteration error left after 2000 steps)
+    assert rel(case.get("U"), o.field("U")) <= 1e-4
+    assert rel(case.get("SST_T"), o.sst_field("SST_T")) <= 1e-2
+    assert np.isfinite(case.norm("L2_R_RHO"))
     case.close()
 
 
@@ -104,6 +115,6 @@ def test_coupled_sst_rejects_other_forms(built_lib):
     from tmp_gb300 import abi
 
     mesh = abi.Mesh.load_grd(GOLDEN / "mixed.grd", -1, -2)
-    for prec, adv in ((abi.PREC_MIXFF, abi.ADV_LUSGS), (abi.PREC_FP32, abi.ADV_LUSGS), (abi.PREC_FP64, abi.ADV_RK5)):
+    for prec, adv in ((abi.PREC_FP32, abi.ADV_LUSGS), (abi.PREC_FP64, abi.ADV_RK5)):
         with pytest.raises(abi.CfdError):
             abi.Case([mesh], [dict(mach=0.3, aoa_deg=0.0, reynolds=1e5)], abi.FLOW_SST, adv, prec, cfl=5.0)

@@ -357,7 +357,7 @@ class Case:
         return int(lib().cfd_launch_count(self.h))
 
     PASSES = dict(face_state=0, cell_grad=1, face_flux=2, cell_update=3, sweep_fwd=4, sweep_bwd=5,
-                  lusgs_update=6, step=7)
+                  lusgs_update=6, step=7, sst_residual=8, sst_sweeps=9, sst_update=10, fringe=11)
 
     def bench_pass(self, name: str, reps: int, flush_bytes: int = 0) -> float:
         """Mean device time (ms) of one pass, CUDA events on the case's stream."""

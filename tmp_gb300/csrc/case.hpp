@@ -242,6 +242,8 @@ void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, in
 void launch_residual_ff(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_ff(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);
 void launch_to_ff(const DevArrays& d, const LaunchCfg& L, bool geometry);
+// binary64 copies of the float-float residual arrays the SST model reads (which: 0 after face_state, 1 after cell_grad)
+void launch_ff_to_fp64(const DevArrays& d, const LaunchCfg& L, int which);
 // ---- k_misc.cu ----
 void launch_to_fp32(const DevArrays& d, const LaunchCfg& L, bool geometry);
 void launch_norm(const DevArrays& d, const LaunchCfg& L, int which);

@@ -196,7 +196,8 @@ void residual_pass(cfd_case_s* c) {
         // face states (with each face's mu_t), the turbulence face values, the gradients
         // (with mu and F1 / F2 of the model), then the flow's and the model's face fluxes
         for (int which = 0; which < 3; which++) {
-            launch_pass(c->d, L, true, false, which, c->p.first_order, c->mixed(), false);
+            launch_pass(c->d, L, true, false, which, c->p.first_order, c->mixed(), c->ffres());
+            if (c->ffres()) launch_ff_to_fp64(c->d, L, which);  // the model reads binary64 arrays
             launch_sst_stage(c->d, L, which);
         }
         return;
@@ -603,9 +604,8 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
     const cfd_params_t& P = *params;
     if (P.flow != CFD_FLOW_EULER && P.flow != CFD_FLOW_LAMINAR && P.flow != CFD_FLOW_SST)
         return fail(CFD_ERR_ARG, "Undefined Flow Type");
-    if (P.flow == CFD_FLOW_SST && (P.advance != CFD_ADV_LUSGS ||
-                                   (P.precision != CFD_PREC_FP64 && P.precision != CFD_PREC_MIXED)))
-        return fail(CFD_ERR_ARG, "the coupled SST model runs with LU-SGS in the FP64 or MIXED form");
+    if (P.flow == CFD_FLOW_SST && (P.advance != CFD_ADV_LUSGS || P.precision == CFD_PREC_FP32))
+        return fail(CFD_ERR_ARG, "the coupled SST model runs with LU-SGS in the FP64, MIXED or MIXFF form");
     if (P.advance != CFD_ADV_RK5 && P.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_ARG, "Undefined Advance Type");
     if (P.precision < CFD_PREC_FP64 || P.precision > CFD_PREC_MIXFF) return fail(CFD_ERR_ARG, "unknown precision");
     if (P.sweep_mode < 0 || P.sweep_mode > 6) return fail(CFD_ERR_ARG, "unknown sweep mode");
@@ -754,6 +754,10 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             if (visc) { dalloc(&d.specvf, nc); dalloc(&d.gradTf, nc); dalloc(&d.muf, nc); dalloc(&d.muef, nf); dalloc(&d.Fvf, nf); }
         } else if (c->ffres()) {
             alloc_ff_arrays(d, visc);
+            if (P.flow == CFD_FLOW_SST) {  // binary64 copies of the residual arrays the SST model reads
+                dalloc(&d.grad, 2 * (size_t)nc); dalloc(&d.specc, nc); dalloc(&d.Ue, nf);
+                dalloc(&d.specv, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf);
+            }
         } else {
             dalloc(&d.grad, 2 * (size_t)nc); dalloc(&d.phi, nc); dalloc(&d.specc, nc);
             dalloc(&d.Ue, nf); dalloc(&d.fspec, nf); dalloc(&d.Fc, nf);
@@ -1426,7 +1430,9 @@ int cfd_selftest_bounded_wait(cfd_case_t c, long long polls) {
 
 int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms) {
     if (!c || !avg_ms || reps <= 0) return fail(CFD_ERR_ARG, "null argument or reps <= 0");
-    if (pass < 0 || pass > 7) return fail(CFD_ERR_ARG, "unknown pass");
+    if (pass < 0 || pass > 11) return fail(CFD_ERR_ARG, "unknown pass");
+    if (pass >= 8 && pass <= 10 && !c->turb()) return fail(CFD_ERR_STATE, "not a coupled SST case");
+    if (pass == 11 && !c->connected) return fail(CFD_ERR_STATE, "not a connected overset case");
     ABI_TRY
     DevArrays& d = c->d;
     auto L = c->L();
@@ -1455,6 +1461,12 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
             case 5: sweeps(c, false); break;
             case 6: launch_lusgs_update(d, L, f32); break;
             case 7: one_step(c); break;
+            case 8:  // the SST model's residual passes
+                for (int st = 0; st < 4; st++) launch_sst_stage(d, L, st);
+                break;
+            case 9: ck(launch_sst_sweeps(d, L, c->fast_sweep()), "turbulence sweeps"); break;
+            case 10: launch_sst_update(d, L); break;
+            case 11: launch_fringe(d, c->fringe, L); break;
         }
         ck(cudaEventRecord(e1, c->stream), "cudaEventRecord");
         ck(cudaEventSynchronize(e1), "cudaEventSynchronize");
@@ -1958,10 +1970,18 @@ void ensure_precision_arrays(cfd_case_s* c, int prec) {
         dalloc(&d.Uef, nf); dalloc(&d.fspecf, nf); dalloc(&d.Fcf, nf);
         if (visc) { dalloc(&d.specvf, nc); dalloc(&d.gradTf, nc); dalloc(&d.muf, nc); dalloc(&d.muef, nf); dalloc(&d.Fvf, nf); }
     }
-    if ((prec == CFD_PREC_FP64 || prec == CFD_PREC_MIXED) && !d.grad) {
-        dalloc(&d.grad, 2 * nc); dalloc(&d.phi, nc); dalloc(&d.specc, nc);
-        dalloc(&d.Ue, nf); dalloc(&d.fspec, nf); dalloc(&d.Fc, nf);
-        if (visc) { dalloc(&d.specv, nc); dalloc(&d.gradT, nc); dalloc(&d.mu, nc); dalloc(&d.mue, nf); dalloc(&d.Fv, nf); }
+    if ((prec == CFD_PREC_FP64 || prec == CFD_PREC_MIXED) && !d.Fc) {
+        // (an SST case created in the MIXFF form already holds binary64 copies of some of them)
+        if (!d.grad) dalloc(&d.grad, 2 * nc);
+        if (!d.specc) dalloc(&d.specc, nc);
+        if (!d.Ue) dalloc(&d.Ue, nf);
+        dalloc(&d.phi, nc); dalloc(&d.fspec, nf); dalloc(&d.Fc, nf);
+        if (visc) {
+            if (!d.specv) dalloc(&d.specv, nc);
+            if (!d.mu) dalloc(&d.mu, nc);
+            if (!d.mue) dalloc(&d.mue, nf);
+            dalloc(&d.gradT, nc); dalloc(&d.Fv, nf);
+        }
     }
     if (c->p.advance == CFD_ADV_LUSGS && prec != CFD_PREC_FP64 && !d.swraf)
         throw std::runtime_error("the binary32 sweep needs a case created in the FP32, MIXED or MIXFF form");
@@ -1976,8 +1996,8 @@ extern "C" int cfd_set_precision(cfd_case_t c, int precision) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
     if (precision < CFD_PREC_FP64 || precision > CFD_PREC_MIXFF) return fail(CFD_ERR_ARG, "unknown precision");
     if (precision == c->p.precision) return CFD_OK;
-    if (c->sst && (precision == CFD_PREC_FP32 || precision == CFD_PREC_MIXFF))
-        return fail(CFD_ERR_STATE, "the SST model needs the binary64 residual");
+    if (c->sst && (precision == CFD_PREC_FP32 || (precision == CFD_PREC_MIXFF && !c->turb())))
+        return fail(CFD_ERR_STATE, "the SST model needs the binary64 (or, coupled, the float-float) residual");
     if (precision == CFD_PREC_MIXFF && c->p.advance == CFD_ADV_LUSGS && (c->p.sweep_mode == 1 || c->p.sweep_mode == 2))
         return fail(CFD_ERR_STATE, "the MIXFF form runs the binary32 dataflow sweeps (sweep modes 0, 3, 4, 5, 6)");
     ABI_TRY

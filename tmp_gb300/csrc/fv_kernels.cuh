@@ -36,9 +36,9 @@ __device__ __forceinline__ int code_face(int code) { return (code > 0 ? code : -
 // solveSpectralRadius (Euler2D.cpp:242-267, ViscousFlow2D.cpp:220-253) and of
 // LaminarFluxStrategy::computeMu for edges.
 //
-// With the SST model coupled (mutc != null, binary64 only: ViscousFlow2D with
-// isLaminar() false, ViscousFlow2D.h:118-154) the face also gets its eddy
-// viscosity (ComputeTurbulenceViscousCoefficient's face loop,
+// With the SST model coupled (mutc != null; binary64 and float-float forms:
+// ViscousFlow2D with isLaminar() false, ViscousFlow2D.h:118-154) the face also
+// gets its eddy viscosity (ComputeTurbulenceViscousCoefficient's face loop,
 // SSTKWStrategy.h:749-777) into mutf, and the viscous spectral radius uses
 // mu/Pr + mu_t/Prt.
 template <class T, bool VISC, int CONTRACT = 0>
@@ -46,8 +46,8 @@ __global__ void __launch_bounds__(256) k_face_state(int nf, const int2* __restri
                                                     const MeshPrm* __restrict__ prm, const v4<T>* __restrict__ fg0,
                                                     const v4<T>* __restrict__ U, v4<T>* __restrict__ Ue,
                                                     v2<T>* __restrict__ fspec, T* __restrict__ mue,
-                                                    unsigned* __restrict__ err, const T* __restrict__ mutc,
-                                                    T* __restrict__ mutf) {
+                                                    unsigned* __restrict__ err, const double* __restrict__ mutc,
+                                                    double* __restrict__ mutf) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf) return;
     const T G = C<T>::gamma;
@@ -81,14 +81,14 @@ __global__ void __launch_bounds__(256) k_face_state(int nf, const int2* __restri
         T mu = sutherland<T>(ue[1] / ue[0], m);
         mue[f] = mu;
         T mpr = mu / C<T>::pr;
-        if constexpr (std::is_same<T, double>::value) {
+        if constexpr (!std::is_same<T, float>::value) {
             if (mutc) {
                 double mf;
                 if (e.y >= 0) mf = 0.5 * (mutc[e.x] + mutc[e.y]);
                 else if (e.y == BC_WALL) mf = 0.0;
-                else mf = dot2(ue[2], ue[3], nx, ny) > 0.0 ? mutc[e.x] : m.sst_mut;
+                else mf = (double)dot2(ue[2], ue[3], nx, ny) > 0.0 ? mutc[e.x] : m.sst_mut;
                 mutf[f] = mf;
-                mpr = mu / C<T>::pr + mf / 0.9;
+                mpr = mu / C<T>::pr + T(mf) / T(0.9);
             }
         }
         s.y = smax(T(4) / (T(3.0) * ue[0]), G / ue[0]) * mpr * A * A;
@@ -203,15 +203,16 @@ __global__ void __launch_bounds__(256) k_cell_grad(
 // LaminarFluxStrategy::computeFlux(int) (LaminarFluxStrategy.h:110-216).
 // Writes the convective and the viscous flux of each face separately so the
 // gather can add them in the reference's two-loop order.  With the SST model
-// coupled (mutf != null, binary64 only) the viscous flux uses mu + mu_t and
-// mu/Pr + mu_t/Prt (getMuEdge / getMuOverPrEdge, ViscousFlow2D.h:128-145).
+// coupled (mutf != null; binary64 and float-float forms) the viscous flux uses
+// mu + mu_t and mu/Pr + mu_t/Prt (getMuEdge / getMuOverPrEdge,
+// ViscousFlow2D.h:128-145).
 template <class T, bool VISC, int CONTRACT = 0>
 __global__ void __launch_bounds__(256) k_face_flux(
     int nf, const int2* __restrict__ lr, const v4<T>* __restrict__ fg0, const v4<T>* __restrict__ fg1,
     const v4<T>* __restrict__ fvis, const v4<T>* __restrict__ U, const v4<T>* __restrict__ grad,
     const v4<T>* __restrict__ phi, const v4<T>* __restrict__ Ue, const T* __restrict__ mue,
     const v2<T>* __restrict__ gradT, v4<T>* __restrict__ Fc, v4<T>* __restrict__ Fv, unsigned* __restrict__ err,
-    const T* __restrict__ mutf) {
+    const double* __restrict__ mutf) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf) return;
     const T G = C<T>::gamma, GM1 = C<T>::gm1;
@@ -255,10 +256,10 @@ __global__ void __launch_bounds__(256) k_face_flux(
     // viscous flux
     T mu = mue[f];
     T mpr = mu / C<T>::pr;
-    if constexpr (std::is_same<T, double>::value) {
+    if constexpr (!std::is_same<T, float>::value) {
         if (mutf) {
-            const double mt = mutf[f];
-            mpr = mu / C<T>::pr + mt / 0.9;
+            const T mt = T(mutf[f]);
+            mpr = mu / C<T>::pr + mt / T(0.9);
             mu = mu + mt;
         }
     }

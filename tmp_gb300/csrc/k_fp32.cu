@@ -14,7 +14,7 @@ static void residual32(const DevArrays& d, const LaunchCfg& L, int first_order, 
     if (which < 0 || which == 0) {
         k_face_state<float, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fmesh, d.prm, d.fg0f, d.Uf,
                                                                        d.Uef, d.fspecf, d.muef, d.err,
-                                                                       (const float*)nullptr, (float*)nullptr);
+                                                                       (const double*)nullptr, (double*)nullptr);
         *L.counter += 1;
     }
     if (which < 0 || which == 1) {
@@ -27,7 +27,7 @@ static void residual32(const DevArrays& d, const LaunchCfg& L, int first_order, 
     if (which < 0 || which == 2) {
         k_face_flux<float, V><<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.lr, d.fg0f, d.fg1f, d.fvisf, d.Uf,
                                                                       d.gradf, d.phif, d.Uef, d.muef, d.gradTf, d.Fcf,
-                                                                      d.Fvf, d.err, (const float*)nullptr);
+                                                                      d.Fvf, d.err, (const double*)nullptr);
         *L.counter += 1;
     }
 }

@@ -489,42 +489,67 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
     // (whose FP64 pipes are separate).  Each warp visits its positions in
     // increasing order: q = q0, q0 + NW, q0 + 2*NW, ...
     const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
-    for (long long q = q0;; q += NW) {
-        const long long p = (long long)blockIdx.x + (long long)B * q;
-        if (p >= nc) break;
-        const int i = order[p];
-        const int4 cf = cface[i];
-        const int code = s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w;
-        bool use = false, left = false;
-        int f = 0, j = 0;
+    // The inputs of a position that do not depend on a neighbour's increment
+    // (cell, face slot, neighbour, its W, the face, the per-step SolveDF
+    // constants and the cell's own term) are loaded one position ahead, while
+    // the warp waits for the current position's neighbour, so their chain of
+    // dependent loads stays off the sweep's critical path.
+    struct In {
+        int i, j;
+        int4 cf;
+        bool use, left;
+        double w0[4];
+        d4 g;
+        double fc, rA, own, dinv;
+    };
+    auto load = [&](long long p, In& x) {
+        x.i = order[p];
+        x.cf = cface[x.i];
+        const int code = s == 0 ? x.cf.x : s == 1 ? x.cf.y : s == 2 ? x.cf.z : x.cf.w;
+        x.use = false;
+        x.left = false;
+        x.j = 0;
+        int f = 0;
         if (code != 0) {
             f = code_face(code);
-            left = code > 0;
+            x.left = code > 0;
             int2 e = lr[f];
-            j = left ? e.y : e.x;
-            use = FWD ? (j >= 0 && j < i) : (j > i);
+            x.j = x.left ? e.y : e.x;
+            x.use = FWD ? (x.j >= 0 && x.j < x.i) : (x.j > x.i);
         }
-        // this cell's own inputs of the final update, loaded before any wait:
-        // R_i (forward) or dW1_i (backward), and D_i (plain) or 1/D_i (fast form)
-        double own = 0.0, dinv = 1.0;
+        // this cell's own inputs of the final update: R_i (forward) or dW1_i (backward), and D_i
+        x.own = 0.0;
+        x.dinv = 1.0;
         if (lane < 4) {
-            own = FWD ? (&R[i].x)[m] : (&dW1[i].x)[m];
-            dinv = D[i];
+            x.own = FWD ? (&R[x.i].x)[m] : (&dW1[x.i].x)[m];
+            x.dinv = D[x.i];
         }
         // lanes without a contributing neighbour compute on harmless values and
-        // are masked at the end, so the arithmetic below is issued once per warp
-        double w0[4] = {1.0, 1.0, 0.0, 0.0}, dw[4] = {0.0, 0.0, 0.0, 0.0};
-        d4 g = d4{0.0, 0.0, 0.0, 0.0};
-        double fc = 0.0, rA = 0.0;
-        if (use) {
-            // independent of the neighbour's increment: load before waiting
-            to_arr(ld4(W + j), w0);
-            g = fg0[f];
-            fc = swfc[(size_t)i * 16 + s * 4 + m];
-            rA = swra[(size_t)i * 4 + s];
+        // are masked at the end, so the arithmetic is issued once per warp
+        x.w0[0] = 1.0; x.w0[1] = 1.0; x.w0[2] = 0.0; x.w0[3] = 0.0;
+        x.g = d4{0.0, 0.0, 0.0, 0.0};
+        x.fc = 0.0;
+        x.rA = 0.0;
+        if (x.use) {
+            to_arr(ld4(W + x.j), x.w0);
+            x.g = fg0[f];
+            x.fc = swfc[(size_t)x.i * 16 + s * 4 + m];
+            x.rA = swra[(size_t)x.i * 4 + s];
+        }
+    };
+    long long p = (long long)blockIdx.x + (long long)B * q0;
+    if (p >= nc) return;
+    In cur, nxt;
+    load(p, cur);
+    for (;;) {
+        const long long pn = p + (long long)B * NW;
+        const bool more = pn < nc;
+        if (more) load(pn, nxt);
+        double dw[4] = {0.0, 0.0, 0.0, 0.0};
+        if (cur.use) {
             // the neighbour's increment is final once none of its four words is
             // the sentinel (each aligned 8-byte word is written exactly once)
-            const double2* q = reinterpret_cast<const double2*>(dst + j);
+            const double2* q = reinterpret_cast<const double2*>(dst + cur.j);
             double2 a, b;
             long long it = 0;
             while (true) {
@@ -542,42 +567,46 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
         __syncwarp();  // reconverge before the arithmetic
         double wp[4];
 #pragma unroll
-        for (int k = 0; k < 4; k++) wp[k] = w0[k] + dw[k];
+        for (int k = 0; k < 4; k++) wp[k] = cur.w0[k] + dw[k];
         // one divide per half-warp, exchanged
         const double quo = (hv ? wp[3] : wp[2]) / wp[0];
         const double u = __shfl_sync(0xffffffffu, quo, lane & 15);
         const double v = __shfl_sync(0xffffffffu, quo, (lane & 15) | 16);
+        const d4 g = cur.g;
         double vn = dot2(u, v, g.x, g.y);
         double pr = GM1 * (wp[1] - 0.5 * wp[0] * sq2(u, v));
         double fcp = m == 0 ? wp[0] * vn : m == 1 ? (wp[1] + pr) * vn : m == 2 ? wp[2] * vn + pr * g.x
                                                                                : wp[3] * vn + pr * g.y;
         double dwm = m == 0 ? dw[0] : m == 1 ? dw[1] : m == 2 ? dw[2] : dw[3];
-        double dfc = left ? (fcp - fc) : (fc - fcp);
-        double df = 0.5 * (dfc - rA * dwm) * g.z;
-        const double DF = use ? df : 0.0;
+        double dfc = cur.left ? (fcp - cur.fc) : (cur.fc - fcp);
+        double df = 0.5 * (dfc - cur.rA * dwm) * g.z;
+        const double DF = cur.use ? df : 0.0;
         // ordered sum over the 4 face slots (lanes m, m+4, m+8, m+12)
         double v0 = __shfl_sync(0xffffffffu, DF, m);
         double v1 = __shfl_sync(0xffffffffu, DF, 4 + m);
         double v2 = __shfl_sync(0xffffffffu, DF, 8 + m);
         double v3 = __shfl_sync(0xffffffffu, DF, 12 + m);
         double dF = 0.0;
-        if (cf.x != 0) dF += v0;
-        if (cf.y != 0) dF += v1;
-        if (cf.z != 0) dF += v2;
-        if (cf.w != 0) dF += v3;
+        if (cur.cf.x != 0) dF += v0;
+        if (cur.cf.y != 0) dF += v1;
+        if (cur.cf.z != 0) dF += v2;
+        if (cur.cf.w != 0) dF += v3;
         double res = 0.0;
         if (lane < 4) {
-            if (FWD) res = (-own - dF) / dinv;
-            else res = own - dF / dinv;
+            if (FWD) res = (-cur.own - dF) / cur.dinv;
+            else res = cur.own - dF / cur.dinv;
         }
         double r1 = __shfl_sync(0xffffffffu, res, 1);
         double r2 = __shfl_sync(0xffffffffu, res, 2);
         double r3 = __shfl_sync(0xffffffffu, res, 3);
         if (lane == 0) {
-            double2* o = reinterpret_cast<double2*>(dst + i);
+            double2* o = reinterpret_cast<double2*>(dst + cur.i);
             __stcg(o, make_double2(res, r1));
             __stcg(o + 1, make_double2(r2, r3));
         }
+        if (!more) break;
+        cur = nxt;
+        p = pn;
     }
 }
 
@@ -798,43 +827,67 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
     // so a cell whose neighbours are ready does not wait for its pair partner
     const unsigned mask = IND ? (h ? 0xffff0000u : 0x0000ffffu) : 0xffffffffu;
     const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
-    for (long long q = q0;; q += NW) {
-        const long long P = (long long)blockIdx.x + (long long)B * q;  // pair index, same mapping as k_sweep_flow
-        if (P >= npairs) break;
-        const int i = order2[2 * P + h];
-        const bool active = i >= 0;
-        const int4 cf = active ? cface[i] : make_int4(0, 0, 0, 0);
-        const int code = s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w;
-        bool use = false, left = false;
-        int f = 0, j = 0;
+    // The inputs of a pair position that do not depend on a neighbour's
+    // increment - its cells, slots and neighbours, the neighbour's binary32
+    // state with the base values of its flux (formed before the wait, so that
+    // only the difference terms remain on the dependence chain), r_A and the
+    // cell's own term - are loaded and formed one position ahead, while the
+    // warp waits for the current position's neighbours.
+    struct In {
+        int i, j;
+        bool active, use, left;
+        int4 cf;
+        float4 w0, g;
+        float rA, u, v, vv, p, vn;
+        double own, dinv;
+    };
+    auto load = [&](long long P, In& x) {
+        x.i = order2[2 * P + h];
+        x.active = x.i >= 0;
+        x.cf = x.active ? cface[x.i] : make_int4(0, 0, 0, 0);
+        const int code = s == 0 ? x.cf.x : s == 1 ? x.cf.y : s == 2 ? x.cf.z : x.cf.w;
+        x.use = false;
+        x.left = false;
+        x.j = 0;
+        int f = 0;
         if (code != 0) {
             f = code_face(code);
-            left = code > 0;
+            x.left = code > 0;
             int2 e = lr[f];
-            j = left ? e.y : e.x;
-            use = FWD ? (j >= 0 && j < i) : (j > i);
+            x.j = x.left ? e.y : e.x;
+            x.use = FWD ? (x.j >= 0 && x.j < x.i) : (x.j > x.i);
         }
-        double own = 0.0, dinv = 1.0;
-        if (active && s == 0) {
-            own = FWD ? (&R[i].x)[m] : (&dW1[i].x)[m];
-            dinv = invD[i];
+        x.own = 0.0;
+        x.dinv = 1.0;
+        if (x.active && s == 0) {
+            x.own = FWD ? (&R[x.i].x)[m] : (&dW1[x.i].x)[m];
+            x.dinv = invD[x.i];
         }
-        float4 w0 = make_float4(1.f, 1.f, 0.f, 0.f), dw = make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-        float rA = 0.f;
-        // base values of the neighbour's flux, formed before the wait so that
-        // only the difference terms remain on the dependence chain
-        float u = 0.f, v = 0.f, vv = 0.f, p = 0.f, vn = 0.f;
-        if (use) {
-            w0 = Wf[j];
-            g = fg0f[f];
-            rA = swraf[(size_t)i * 4 + s];
-            u = w0.z / w0.x;
-            v = w0.w / w0.x;
-            vv = u * u + v * v;
-            p = GM1 * (w0.y - 0.5f * w0.x * vv);
-            vn = u * g.x + v * g.y;
-            const float4* qf = (FWD ? dW1f : dWf) + j;
+        x.w0 = make_float4(1.f, 1.f, 0.f, 0.f);
+        x.g = make_float4(0.f, 0.f, 0.f, 0.f);
+        x.rA = x.u = x.v = x.vv = x.p = x.vn = 0.f;
+        if (x.use) {
+            x.w0 = Wf[x.j];
+            x.g = fg0f[f];
+            x.rA = swraf[(size_t)x.i * 4 + s];
+            x.u = x.w0.z / x.w0.x;
+            x.v = x.w0.w / x.w0.x;
+            x.vv = x.u * x.u + x.v * x.v;
+            x.p = GM1 * (x.w0.y - 0.5f * x.w0.x * x.vv);
+            x.vn = x.u * x.g.x + x.v * x.g.y;
+        }
+    };
+    long long P = (long long)blockIdx.x + (long long)B * q0;  // pair index, same mapping as k_sweep_flow
+    if (P >= npairs) return;
+    In cur, nxt;
+    load(P, cur);
+    for (;;) {
+        const long long Pn = P + (long long)B * NW;
+        const bool more = Pn < npairs;
+        if (more) load(Pn, nxt);
+        float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (cur.use) {
+            const float4* qf = (FWD ? dW1f : dWf) + cur.j;
             long long it = 0;
             while (true) {
                 dw = __ldcv(qf);
@@ -852,7 +905,9 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
         // not grow as dW shrinks below W's binary32 resolution (subtracting two
         // binary32 fluxes would leave a noise of ~1e-7 |F| that stalls the
         // mixed form's convergence near a 5e-5 residual fall).
-        const float rho = w0.x, E = w0.y, mx = w0.z, my = w0.w;
+        const float rho = cur.w0.x, E = cur.w0.y, mx = cur.w0.z, my = cur.w0.w;
+        const float u = cur.u, v = cur.v, vv = cur.vv, p = cur.p, vn = cur.vn;
+        const float4 g = cur.g;
         const float d0 = dw.x, d1 = dw.y, d2 = dw.z, d3 = dw.w;
         const float rp = 1.f / (rho + d0);
         const float du = (d2 - u * d0) * rp, dv = (d3 - v * d0) * rp;
@@ -865,37 +920,40 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
                         : m == 2 ? d2 * vnp + mx * dvn + dp * g.x
                                  : d3 * vnp + my * dvn + dp * g.y;
         float dwm = m == 0 ? dw.x : m == 1 ? dw.y : m == 2 ? dw.z : dw.w;
-        float dfc = left ? dfm : -dfm;
-        float DF = use ? 0.5f * (dfc - rA * dwm) * g.z : 0.f;
+        float dfc = cur.left ? dfm : -dfm;
+        float DF = cur.use ? 0.5f * (dfc - cur.rA * dwm) * g.z : 0.f;
         float v0 = __shfl_sync(mask, DF, base + m);
         float v1 = __shfl_sync(mask, DF, base + 4 + m);
         float v2 = __shfl_sync(mask, DF, base + 8 + m);
         float v3 = __shfl_sync(mask, DF, base + 12 + m);
         float dF = 0.f;
-        if (cf.x != 0) dF += v0;
-        if (cf.y != 0) dF += v1;
-        if (cf.z != 0) dF += v2;
-        if (cf.w != 0) dF += v3;
+        if (cur.cf.x != 0) dF += v0;
+        if (cur.cf.y != 0) dF += v1;
+        if (cur.cf.z != 0) dF += v2;
+        if (cur.cf.w != 0) dF += v3;
         // The binary32 copy that the next levels wait for is computed and
         // published first, in binary32; the binary64 increment (used only by
         // the backward sweep and the update, after this launch) follows off
         // the critical path.
-        const float ownf = (float)own, dinvf = (float)dinv;
+        const float ownf = (float)cur.own, dinvf = (float)cur.dinv;
         const float resf = FWD ? (-ownf - dF) * dinvf : ownf - dF * dinvf;
         float f1 = __shfl_sync(mask, resf, base + 1);
         float f2 = __shfl_sync(mask, resf, base + 2);
         float f3 = __shfl_sync(mask, resf, base + 3);
-        if (active && (lane & 15) == 0) __stcg(dstf + i, make_float4(resf, f1, f2, f3));
+        if (cur.active && (lane & 15) == 0) __stcg(dstf + cur.i, make_float4(resf, f1, f2, f3));
         double res = 0.0;
-        if (s == 0) res = FWD ? (-own - (double)dF) * dinv : own - (double)dF * dinv;
+        if (s == 0) res = FWD ? (-cur.own - (double)dF) * cur.dinv : cur.own - (double)dF * cur.dinv;
         double r1 = __shfl_sync(mask, res, base + 1);
         double r2 = __shfl_sync(mask, res, base + 2);
         double r3 = __shfl_sync(mask, res, base + 3);
-        if (active && (lane & 15) == 0) {
-            double2* o = reinterpret_cast<double2*>(dst + i);
+        if (cur.active && (lane & 15) == 0) {
+            double2* o = reinterpret_cast<double2*>(dst + cur.i);
             __stcg(o, make_double2(res, r1));
             __stcg(o + 1, make_double2(r2, r3));
         }
+        if (!more) break;
+        cur = nxt;
+        P = Pn;
     }
 }
 

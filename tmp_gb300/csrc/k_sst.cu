@@ -61,7 +61,7 @@ __global__ void k_sst_face(DevArrays d) {
     }
     d.sstTf[2 * f] = t0;
     d.sstTf[2 * f + 1] = t1;
-    d.sstMutf[f] = mf;
+    if (!d.turb) d.sstMutf[f] = mf;  // coupled, the flow's face_state pass has formed it (for the viscous radius)
 }
 
 // ComputeCellTGradient (:662-692) and ComputeSSTf1f2 (:695-722).
@@ -314,38 +314,63 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
     double* dst = FWD ? d.sstDW1 : d.sstDW;
     float2* dstf = FWD ? d.sstDW1f : d.sstDWf;
     const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
-    for (long long q = q0;; q += NW) {
-        const long long p = (long long)blockIdx.x + (long long)B * q;
-        if (p >= d.nc) break;
-        const int i = order[p];
-        const int4 cf = d.cface[i];
-        const int code = lane < 8 ? (s == 0 ? cf.x : s == 1 ? cf.y : s == 2 ? cf.z : cf.w) : 0;
-        bool use = false, left = false;
-        int f = 0, j = 0;
+    // The inputs of a position that do not depend on a neighbour's increment
+    // (its cell, face slot, neighbour and the per-slot constants) are loaded one
+    // position ahead, while the warp waits for the current position's
+    // neighbour: their chain of dependent loads (order, cell faces, face cells,
+    // then the neighbour's records) stays off the sweep's critical path.
+    struct In {
+        int i, j;
+        int4 cf;
+        bool use, left;
+        T wt, fc, rA, vnp, A;
+        double own, dd;
+    };
+    auto load = [&](long long p, In& x) {
+        x.i = order[p];
+        x.cf = d.cface[x.i];
+        const int code = lane < 8 ? (s == 0 ? x.cf.x : s == 1 ? x.cf.y : s == 2 ? x.cf.z : x.cf.w) : 0;
+        x.use = false;
+        x.left = false;
+        x.j = 0;
+        int f = 0;
         if (code != 0) {
             f = code > 0 ? code - 1 : -code - 1;
-            left = code > 0;
+            x.left = code > 0;
             const int2 e = d.lr[f];
-            j = left ? e.y : e.x;
-            use = FWD ? (j >= 0 && j < i) : (j > i);
+            x.j = x.left ? e.y : e.x;
+            x.use = FWD ? (x.j >= 0 && x.j < x.i) : (x.j > x.i);
         }
-        double own = 0.0, dd = 1.0;
+        x.own = 0.0;
+        x.dd = 1.0;
         if (lane < 2) {
-            own = FWD ? d.sstR[2 * i + m] : d.sstDW1[2 * i + m];
-            dd = std::is_same<T, double>::value ? d.sstD[2 * i + m] : d.sstDinv[2 * i + m];
+            x.own = FWD ? d.sstR[2 * x.i + m] : d.sstDW1[2 * x.i + m];
+            x.dd = std::is_same<T, double>::value ? d.sstD[2 * x.i + m] : d.sstDinv[2 * x.i + m];
         }
+        x.wt = x.fc = x.rA = x.vnp = x.A = T(0);
+        if (x.use) {
+            const size_t t = (size_t)x.i * 4 + s;
+            x.wt = (T)d.sstW[2 * x.j + m];
+            x.fc = (T)d.sstFcs[2 * t + m];
+            x.rA = (T)d.sstRA[t];
+            x.vnp = (T)d.sstVnp[t];
+            x.A = (T)d.fgeo[f].z;
+        }
+    };
+    long long p = (long long)blockIdx.x + (long long)B * q0;
+    if (p >= d.nc) return;
+    In cur, nxt;
+    load(p, cur);
+    for (;;) {
+        const long long pn = p + (long long)B * NW;
+        const bool more = pn < d.nc;
+        if (more) load(pn, nxt);
         T DF = T(0);
-        T wt = T(0), fc = T(0), rA = T(0), vnp = T(0), A = T(0), dt = T(0);
-        if (use) {
-            const size_t t = (size_t)i * 4 + s;
-            wt = (T)d.sstW[2 * j + m];
-            fc = (T)d.sstFcs[2 * t + m];
-            rA = (T)d.sstRA[t];
-            vnp = (T)d.sstVnp[t];
-            A = (T)d.fgeo[f].z;
+        if (cur.use) {
             long long it = 0;
+            T dt;
             if (std::is_same<T, double>::value) {
-                const double2* qd = reinterpret_cast<const double2*>((FWD ? d.sstDW1 : d.sstDW) + 2 * (size_t)j);
+                const double2* qd = reinterpret_cast<const double2*>((FWD ? d.sstDW1 : d.sstDW) + 2 * (size_t)cur.j);
                 double2 a;
                 while (true) {
                     a = __ldcv(qd);
@@ -355,7 +380,7 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
                 }
                 dt = (T)(m ? a.y : a.x);
             } else {
-                const float2* qf = (FWD ? d.sstDW1f : d.sstDWf) + j;
+                const float2* qf = (FWD ? d.sstDW1f : d.sstDWf) + cur.j;
                 float2 a;
                 while (true) {
                     a = __ldcv(qf);
@@ -365,9 +390,9 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
                 }
                 dt = (T)(m ? a.y : a.x);
             }
-            const T fcp = (wt + dt) * vnp;
-            const T dfc = left ? (fcp - fc) : (fc - fcp);
-            DF = T(0.5) * (dfc - rA * dt) * A;
+            const T fcp = (cur.wt + dt) * cur.vnp;
+            const T dfc = cur.left ? (fcp - cur.fc) : (cur.fc - fcp);
+            DF = T(0.5) * (dfc - cur.rA * dt) * cur.A;
         }
         __syncwarp();
         // ordered sum over the face slots (lanes m, 2+m, 4+m, 6+m)
@@ -376,26 +401,30 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
         const T v2 = __shfl_sync(0xffffffffu, DF, 4 + m);
         const T v3 = __shfl_sync(0xffffffffu, DF, 6 + m);
         T dF = T(0);
-        if (cf.x != 0) dF += v0;
-        if (cf.y != 0) dF += v1;
-        if (cf.z != 0) dF += v2;
-        if (cf.w != 0) dF += v3;
+        if (cur.cf.x != 0) dF += v0;
+        if (cur.cf.y != 0) dF += v1;
+        if (cur.cf.z != 0) dF += v2;
+        if (cur.cf.w != 0) dF += v3;
         if (std::is_same<T, double>::value) {
             double res = 0.0;
-            if (lane < 2) res = FWD ? (-own - (double)dF) / dd : own - (double)dF / dd;
+            if (lane < 2) res = FWD ? (-cur.own - (double)dF) / cur.dd : cur.own - (double)dF / cur.dd;
             const double r1 = __shfl_sync(0xffffffffu, res, 1);
-            if (lane == 0) __stcg(reinterpret_cast<double2*>(dst + 2 * (size_t)i), make_double2(res, r1));
+            if (lane == 0) __stcg(reinterpret_cast<double2*>(dst + 2 * (size_t)cur.i), make_double2(res, r1));
         } else {
             // the binary32 copy the next levels wait for first, then the binary64 increment
             float resf = 0.f;
-            if (lane < 2) resf = FWD ? (-(float)own - (float)dF) * (float)dd : (float)own - (float)dF * (float)dd;
+            if (lane < 2)
+                resf = FWD ? (-(float)cur.own - (float)dF) * (float)cur.dd : (float)cur.own - (float)dF * (float)cur.dd;
             const float f1 = __shfl_sync(0xffffffffu, resf, 1);
-            if (lane == 0) __stcg(dstf + i, make_float2(resf, f1));
+            if (lane == 0) __stcg(dstf + cur.i, make_float2(resf, f1));
             double res = 0.0;
-            if (lane < 2) res = FWD ? (-own - (double)dF) * dd : own - (double)dF * dd;
+            if (lane < 2) res = FWD ? (-cur.own - (double)dF) * cur.dd : cur.own - (double)dF * cur.dd;
             const double r1 = __shfl_sync(0xffffffffu, res, 1);
-            if (lane == 0) __stcg(reinterpret_cast<double2*>(dst + 2 * (size_t)i), make_double2(res, r1));
+            if (lane == 0) __stcg(reinterpret_cast<double2*>(dst + 2 * (size_t)cur.i), make_double2(res, r1));
         }
+        if (!more) break;
+        cur = nxt;
+        p = pn;
     }
 }
 
