@@ -79,7 +79,7 @@ def parse():
                          "(others: fp32, mixed, mixed+learned, fp32+learned>mixed)")
     ap.add_argument("--sst-drop-forms", default="fp64,mixff,mixed",
                     help="forms of the SST case's equal-fall run (the first sets the fall)")
-    ap.add_argument("--sst-drop-seconds", type=float, default=150.0,
+    ap.add_argument("--sst-drop-seconds", type=float, default=120.0,
                     help="time the first form of the SST case runs; the others run to the fall it reached")
     ap.add_argument("--switch-at", type=float, default=3e-4,
                     help="residual fall at which 'A>B' switches form (or earlier, once A's residual stalls)")
@@ -349,7 +349,7 @@ def overset_leg(stream) -> dict:
                       "cell_iters_per_s": ncell / (step_ms * 1e-3), "fringe_ms": round(fringe_ms, 4),
                       "hole_cells": [int((i == 0).sum()) for i in ib],
                       "receptor_cells": [int((i == -1).sum()) for i in ib],
-                      "sweep": dict(zip(("mode", "blocks_per_sm", "threads"), case.sweep_config())),
+                      "sweep": dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), case.sweep_config())),
                       "finite_after_200_steps": bool(np.isfinite(case.get("U", 0)).all() and
                                                      np.isfinite(case.get("U", 1)).all())}
     case.close()
@@ -407,7 +407,7 @@ def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5, mode: in
     tuned = []
     for c in packed:
         c.autotune(2)
-        tuned.append(dict(zip(("mode", "blocks_per_sm", "threads"), c.sweep_config())))
+        tuned.append(dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), c.sweep_config())))
     ms_packed = run(packed)
     net = learn.load()
     ms_learned = None
@@ -440,14 +440,16 @@ def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5, mode: in
             "solver_errors": sorted(set(errors))}
 
 
-def oracle_for(w):
+def oracle_for(w, topo=None):
     """The C restatement (the reference's serial path; with the SST model coupled as the GPU runs it) on the
-    workload's mesh, from the freestream."""
+    workload's mesh (its reader's topology `topo`, built here when not given), from the freestream."""
     import oracle
     from oracle import grd
 
-    g = w.mesh
-    t = grd.topo_from_arrays(g.xy, g.edge_nodes, g.edge_cells, g.ncell, g.wall_tag, g.far_tag)
+    if topo is None:
+        g = w.mesh
+        topo = grd.topo_from_arrays(g.xy, g.edge_nodes, g.edge_cells, g.ncell, g.wall_tag, g.far_tag)
+    t = topo
     o = oracle.Oracle(t, w.mach, w.aoa, w.re, w.flow in ("laminar", "sst"))
     if w.flow == "sst":
         o.sst_enable(True, w.extra.get("tu", 0.01), w.extra.get("mut_ratio", 0.035))
@@ -472,12 +474,19 @@ def cpu_baseline(w, seconds: float) -> dict:
 
 
 def _ref_worker(args):
-    cfg_name, steps, warmup, barrier = args
+    wd, topo_path, steps, warmup, barrier = args
     sys.path.insert(0, str(ROOT))
-    from tmp_gb300 import configs
+    import types
 
-    w = configs.WORKLOADS[cfg_name]()
-    t, o = oracle_for(w)
+    import numpy as np
+
+    from oracle import grd
+
+    w = types.SimpleNamespace(**wd)  # the workload's flow settings (its mesh comes as the topology file)
+    z = np.load(topo_path)
+    t = grd.Topo(int(z["nnode"]), int(z["nedge"]), int(z["ncell"]), z["xy"], z["edge_nodes"], z["lr"],
+                 z["cell_verts"], z["cell_nvert"], z["cell_edges"], z["cell_nedge"])
+    t, o = oracle_for(w, t)
     step = (lambda: o.lusgs_step(w.cfl)) if w.advance == "lusgs" else (lambda: o.rk_step())
     for _ in range(warmup):
         step()
@@ -500,17 +509,29 @@ def run_reference(args):
     import oracle
     from tmp_gb300 import configs
 
+    import numpy as np
+    from oracle import grd
+
     oracle.build()
     w = configs.WORKLOADS[args.config]()
     ncores = os.cpu_count() or 1
+    # the reader's topology once, shared by the copies through a file
+    g = w.mesh
+    t = grd.topo_from_arrays(g.xy, g.edge_nodes, g.edge_cells, g.ncell, g.wall_tag, g.far_tag)
+    fd, topo_path = tempfile.mkstemp(suffix=".npz")
+    os.close(fd)
+    np.savez(topo_path, nnode=t.nnode, nedge=t.nedge, ncell=t.ncell, xy=t.xy, edge_nodes=t.edge_nodes, lr=t.lr,
+             cell_verts=t.cell_verts, cell_nvert=t.cell_nvert, cell_edges=t.cell_edges, cell_nedge=t.cell_nedge)
     steps = max(1, args.steps)  # the same timed steps as the GPU arm
     warm = max(3, args.warmup)  # at least three untimed steps per copy
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Manager() as mgr, ctx.Pool(ncores) as pool:
         barrier = mgr.Barrier(ncores)
-        res = pool.map(_ref_worker, [(args.config, steps, warm, barrier)] * ncores, chunksize=1)
+        wd = dict(mach=w.mach, aoa=w.aoa, re=w.re, cfl=w.cfl, flow=w.flow, advance=w.advance, extra=w.extra)
+        res = pool.map(_ref_worker, [(wd, topo_path, steps, warm, barrier)] * ncores, chunksize=1)
     wall = time.perf_counter() - t0
+    os.unlink(topo_path)
     cells = sum(r[0] for r in res)
     slowest = max(r[1] for r in res)
     value = cells / slowest
@@ -535,6 +556,7 @@ def run_ours(args):
     from tmp_gb300 import abi, configs, replicas
     from tmp_gb300.build import build_library
 
+    t_start = time.perf_counter()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -645,6 +667,8 @@ def run_ours(args):
                 "h2d_bytes_per_step": hv.nbytes, "d2h_bytes_per_step": back.nbytes + nrm.nbytes}
 
     e2e = None if args.no_e2e else e2e_of(case)
+    legs = {"setup_and_timed": round(time.perf_counter() - t_start, 1)}
+    t_leg = time.perf_counter()
 
     # the other precision forms, timed the same way
     forms = {}
@@ -652,12 +676,12 @@ def run_ours(args):
         c2 = make_case(f)
         fm, _ = timed_steps(c2, args.steps)
         forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3),
-                    "sweep": dict(zip(("mode", "blocks_per_sm", "threads"), c2.sweep_config()))}
+                    "sweep": dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), c2.sweep_config()))}
         if f == "fp64" and not args.no_e2e:
             forms[f]["e2e"] = e2e_of(c2)
         c2.close()
     forms[args.precision] = {"ms_per_step": 1e3 * t_local / args.steps, "value": nc * args.steps / t_local,
-                             "sweep": dict(zip(("mode", "blocks_per_sm", "threads"), case.sweep_config())), "e2e": e2e}
+                             "sweep": dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), case.sweep_config())), "e2e": e2e}
     # the plain binary64 form (results equal to the reference's) next to the headline form
     plain = forms.get("fp64")
 
@@ -732,6 +756,8 @@ def run_ours(args):
         else:
             drop = time_to_drop(w, mesh, args.drop_forms, args.drop, args.drop_seconds)
 
+    legs["forms_and_time_to_drop"] = round(time.perf_counter() - t_leg, 1)
+    t_leg = time.perf_counter()
     # per-pass device times for the roofline (L2 flushed before each rep)
     passes = ["face_state", "cell_grad", "face_flux", "cell_update"]
     if w.advance == "lusgs":
@@ -798,7 +824,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision], "data": "synthetic",
             "config": {"workload": w.name, "ncell": nc, "nedge": nf, "levels": list(nlev), "mach": w.mach,
                        "aoa": w.aoa, "re": w.re, "cfl": w.cfl, "flow": w.flow, **w.extra, "precision": args.precision,
-                       "sweep": dict(zip(("mode", "blocks_per_sm", "threads"), case.sweep_config())),
+                       "sweep": dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), case.sweep_config())),
                        "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
             "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms_per_step"], "e2e": plain.get("e2e"),
@@ -806,15 +832,23 @@ def run_ours(args):
             "forms": forms, "time_to_drop": drop}
     if drop_c2 is not None:
         line["time_to_drop_c2"] = drop_c2
+    legs["per_pass"] = round(time.perf_counter() - t_leg, 1)
+    t_leg = time.perf_counter()
     if rank == 0 and not args.no_overset:
         line["overset"] = overset_leg(stream)
+        legs["overset"] = round(time.perf_counter() - t_leg, 1)
+        t_leg = time.perf_counter()
     if rank == 0 and not args.no_batch and w.advance == "lusgs":
         try:
             line["batch"] = batch_leg(stream, prec_code[args.precision], args.batch_meshes, mode=mode)
         except Exception as ex:  # the leg is reported beside the headline, never instead of it
             line["batch"] = {"error": f"{type(ex).__name__}: {ex}"}
+    legs["batch"] = round(time.perf_counter() - t_leg, 1)
+    t_leg = time.perf_counter()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+    legs["cpu_baseline"] = round(time.perf_counter() - t_leg, 1)
+    line["leg_seconds"] = legs
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -264,7 +264,8 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
  * reports it; the case's state is restored afterwards.  For the binary32-sweep
  * forms of a case created with sweep_mode 0, 5 or 6 it also picks among those
  * three schedules, and for the round-robin ones among 256, 128 and 64 threads
- * per block (cfd_case_sweep reads the choice). */
+ * per block, with and without the look-ahead loads (cfd_case_sweep reads the
+ * choice). */
 int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_ms);
 /* Host-side chain schedule of the binary32 LU-SGS sweep (sweep modes 5 and 6)
  * for one mesh, as a case holding that mesh builds it (no reference
@@ -279,10 +280,12 @@ int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_m
  * entry t, else the cell id); *table_entries the table's entries per block. */
 int cfd_chain_schedule(cfd_mesh_t mesh, int forward, int nlists, int local, int table, int* hptr,
                        int* cells, int* rec, int* jenc, int* table_entries);
-/* The case's current LU-SGS schedule: sweep_mode, blocks per SM and threads
- * per block of the round-robin dataflow sweeps (after cfd_autotune, the ones
- * it chose); any pointer may be NULL. No reference counterpart. */
-int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm, int* threads);
+/* The case's current LU-SGS schedule: sweep_mode, blocks per SM, threads per
+ * block of the round-robin dataflow sweeps and whether they load the next
+ * position's inputs while waiting (lookahead 1: more registers per thread,
+ * fewer resident warps; after cfd_autotune, the ones it chose); any pointer
+ * may be NULL. No reference counterpart. */
+int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm, int* threads, int* lookahead);
 /* Failure-detection self-test (no reference counterpart): launch a kernel that
  * waits, at most `polls` polls, on a device flag nothing sets, exactly as the
  * dataflow LU-SGS sweep waits on its neighbours.  Returns CFD_ERR_TIMEOUT when

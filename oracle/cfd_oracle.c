@@ -147,15 +147,23 @@ void orc_geometry(orc_t* o) {
         o->cen[2 * c] = cx / (double)n;
         o->cen[2 * c + 1] = cy / (double)n;
     }
+    /* the wall faces (ascending), then every cell's minimum over them */
+    int nw = 0;
+    for (int k = 0; k < o->nedge; k++) nw += o->lr[2 * k + 1] == BC_WALL;
+    int* wf = (int*)malloc(sizeof(int) * (size_t)(nw > 0 ? nw : 1));
+    nw = 0;
+    for (int k = 0; k < o->nedge; k++)
+        if (o->lr[2 * k + 1] == BC_WALL) wf[nw++] = k;
     for (int c = 0; c < o->ncell; c++) {
         double d = 100000000000.0;
-        for (int k = 0; k < o->nedge; k++) {
-            if (o->lr[2 * k + 1] != BC_WALL) continue;
+        for (int q = 0; q < nw; q++) {
+            int k = wf[q];
             double x = o->cen[2 * c] - o->ecen[2 * k], y = o->cen[2 * c + 1] - o->ecen[2 * k + 1];
             d = dmin(d, fabs(dot2(x, y, o->nrm[2 * k], o->nrm[2 * k + 1])));
         }
         o->walld[c] = d;
     }
+    free(wf);
 }
 
 /* TopologyHolderStrategy::set_fs_variable2 + update_nondim_variable

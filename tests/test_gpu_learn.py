@@ -176,9 +176,9 @@ def test_autotune_restores_state(built_lib):
         U = c.get("U")
         bpsm, ms = c.autotune(2)
         assert bpsm >= 1 and ms > 0
-        mode, b2, threads = c.sweep_config()
+        mode, b2, threads, lookahead = c.sweep_config()
         assert b2 == bpsm and mode in ((0,) if prec == abi.PREC_FP64 else (0, 5, 6))
-        assert threads in (64, 128, 256) and (threads == 256 or mode == 0)
+        assert threads in (64, 128, 256) and (threads == 256 or mode == 0) and lookahead in (0, 1)
         assert np.array_equal(c.get("U"), U)
         c.step_graph(5)  # still steps after the launch shape changed
         assert np.isfinite(c.get("U")).all()

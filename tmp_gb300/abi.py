@@ -143,7 +143,7 @@ def lib() -> C.CDLL:
         "cfd_measure_hop_latency": (C.c_int, [vp, C.c_int, C.c_int, dp]),
         "cfd_set_precision": (C.c_int, [vp, C.c_int]),
         "cfd_autotune": (C.c_int, [vp, C.c_int, ip, dp]),
-        "cfd_case_sweep": (C.c_int, [vp, ip, ip, ip]),
+        "cfd_case_sweep": (C.c_int, [vp, ip, ip, ip, ip]),
         "cfd_chain_schedule": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, ip, ip, ip, ip, ip]),
         "cfd_sst_enable": (C.c_int, [vp]),
         "cfd_sst_freestream": (C.c_int, [vp, C.c_int, dp]),
@@ -289,10 +289,10 @@ class Case:
         return b.value, t.value
 
     def sweep_config(self):
-        """(sweep_mode, blocks_per_sm, threads per block) in use, e.g. after autotune()."""
-        a, b, t = C.c_int(), C.c_int(), C.c_int()
-        check(lib().cfd_case_sweep(self.h, C.byref(a), C.byref(b), C.byref(t)))
-        return a.value, b.value, t.value
+        """(sweep_mode, blocks_per_sm, threads per block, look-ahead) in use, e.g. after autotune()."""
+        a, b, t, la = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(lib().cfd_case_sweep(self.h, C.byref(a), C.byref(b), C.byref(t), C.byref(la)))
+        return a.value, b.value, t.value, la.value
 
     def connect(self, meshes, obc_nodes=None, nfringe: int = 1, mexclude: int = 3):
         """Overset connectivity of the case's meshes (the handles it was created from); afterwards every LU-SGS

@@ -139,6 +139,7 @@ struct DevArrays {
     int npos2_fwd = 0, npos2_bwd = 0;
     int flow_grid = 0;           // co-resident blocks of the dataflow sweep
     int flow_threads = 256;      // threads per block of the round-robin dataflow sweeps
+    int flow_pf = 1;             // round-robin sweeps load the next position's inputs while waiting
     // chain-scheduled fast-form sweep (sweep_mode 5), index 0 forward, 1 backward
     int chain_nh = 0;            // warps (lists) the schedule was built for (0: not built)
     int* chain_ptr[2] = {nullptr, nullptr};    // [chain_nh+1] each warp's range of positions
@@ -199,7 +200,7 @@ void launch_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool viscous, boo
 void launch_sweep16_level(const DevArrays& d, const LaunchCfg& L, bool forward, int begin, int end);
 cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
 cudaError_t launch_sweep_pair64(const DevArrays& d, const LaunchCfg& L, bool forward, int grid);
-int sweep_flow_max_grid(bool low, int blocks_per_sm, int threads = 256);
+int sweep_flow_max_grid(bool low, int blocks_per_sm, int threads = 256, bool pf = true);
 void launch_inv_diag(const DevArrays& d, const LaunchCfg& L);
 // kind of the viscosity array the binary32 sweep staging reads: the residual's form
 enum MuKind { MU_F32 = 0, MU_F64 = 1, MU_FF = 2 };
@@ -234,7 +235,7 @@ cudaError_t launch_sst_sweeps(const DevArrays& d, const LaunchCfg& L, bool fp32)
 void launch_sst_update(const DevArrays& d, const LaunchCfg& L);
 // W_t = rho (k, omega) from the current U and k, omega
 void launch_sst_cons(const DevArrays& d, const LaunchCfg& L);
-int sst_sweep_max_grid(int blocks_per_sm, int threads = 256);
+int sst_sweep_max_grid(int blocks_per_sm, int threads = 256, bool pf = true);
 // ---- k_fp32.cu ----
 void launch_residual_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);

@@ -148,14 +148,16 @@ struct cfd_case_s {
 };
 
 static void sst_alloc(cfd_case_s* c);
-// Launch shape of the dataflow sweeps: blocks per SM (0: the default 2) and
-// threads per block (0: 256) of the round-robin sweeps, the grids that keep
-// them co-resident (flow and, coupled SST, turbulence sweeps).
-static void set_sweep_shape(cfd_case_s* c, int bpsm, int threads) {
+// Launch shape of the dataflow sweeps: blocks per SM (0: the default 2),
+// threads per block (0: 256) and whether the round-robin sweeps load the next
+// position's inputs ahead (pf; < 0 keeps the current choice), and the grids
+// that keep them co-resident (flow and, coupled SST, turbulence sweeps).
+static void set_sweep_shape(cfd_case_s* c, int bpsm, int threads, int pf = -1) {
     if (threads != 64 && threads != 128) threads = 256;
+    if (pf >= 0) c->d.flow_pf = pf ? 1 : 0;
     c->d.flow_threads = threads;
-    c->d.flow_grid = sweep_flow_max_grid(c->p.precision != CFD_PREC_FP64, bpsm, threads);
-    if (c->turb()) c->d.sst_grid = sst_sweep_max_grid(bpsm > 0 ? bpsm : 2, threads);
+    c->d.flow_grid = sweep_flow_max_grid(c->p.precision != CFD_PREC_FP64, bpsm, threads, c->d.flow_pf != 0);
+    if (c->turb()) c->d.sst_grid = sst_sweep_max_grid(bpsm > 0 ? bpsm : 2, threads, c->d.flow_pf != 0);
 }
 static void sst_freestream(cfd_case_s* c);
 static void sst_init_state(cfd_case_s* c);
@@ -2072,11 +2074,12 @@ extern "C" int cfd_chain_schedule(cfd_mesh_t mesh, int forward, int nlists, int 
     }
 }
 
-extern "C" int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm, int* threads) {
+extern "C" int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm, int* threads, int* lookahead) {
     if (!c) return fail(CFD_ERR_ARG, "null case");
     if (sweep_mode) *sweep_mode = c->p.sweep_mode;
     if (blocks_per_sm) *blocks_per_sm = c->p.sweep_blocks_per_sm;
     if (threads) *threads = c->d.flow_threads;
+    if (lookahead) *lookahead = c->d.flow_pf;
     return CFD_OK;
 }
 
@@ -2115,8 +2118,8 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
     // mode 6 keeps neighbouring lists in one block with a shared-memory hand-off)
     std::vector<int> modes{c->p.sweep_mode};
     if (c->fast_sweep() && (c->p.sweep_mode == 0 || c->p.sweep_mode == 5 || c->p.sweep_mode == 6)) modes = {0, 5, 6};
-    const int mode0 = c->p.sweep_mode, threads0 = d.flow_threads;
-    int best = 0, best_mode = mode0, best_threads = threads0;
+    const int mode0 = c->p.sweep_mode, threads0 = d.flow_threads, pf0 = d.flow_pf;
+    int best = 0, best_mode = mode0, best_threads = threads0, best_pf = pf0;
     double best_t = 1e300;
     int rc = CFD_OK;
     for (int mode : modes) {
@@ -2125,11 +2128,16 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
         // fewer warps per block (fewer cells sharing one sub-partition's pipes)
         const bool chain = c->fast_sweep() && (mode == 5 || mode == 6);
         std::vector<int> tlist = chain ? std::vector<int>{256} : std::vector<int>{256, 128, 64};
+        // (the chain schedules' staging pass is not the round-robin one: the
+        // look-ahead switch only matters to the round-robin sweeps, and to the
+        // turbulence sweeps of a coupled SST case)
+        std::vector<int> pflist = (chain && !c->turb()) ? std::vector<int>{pf0} : std::vector<int>{1, 0};
+        for (int pf : pflist)
         for (int threads : tlist) {
-            const int max_grid = sweep_flow_max_grid(low, 64, threads);  // occupancy limit
+            const int max_grid = sweep_flow_max_grid(low, 64, threads, pf != 0);  // occupancy limit
             int last_grid = -1;
             for (int bpsm = 1; bpsm <= 16 && rc == CFD_OK; bpsm++) {
-                set_sweep_shape(c, bpsm, threads);
+                set_sweep_shape(c, bpsm, threads, pf);
                 const int grid = d.flow_grid;
                 if (grid > max_grid) break;
                 const int eff = c->chain_sweep() ? chain_grid(c) : grid;
@@ -2144,6 +2152,7 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
                     best = bpsm;
                     best_mode = mode;
                     best_threads = threads;
+                    best_pf = pf;
                 }
             }
         }
@@ -2151,12 +2160,12 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
     c->p.sweep_mode = rc == CFD_OK ? best_mode : mode0;
     if (rc == CFD_OK) {
         c->p.sweep_blocks_per_sm = best;
-        set_sweep_shape(c, best, best_threads);
+        set_sweep_shape(c, best, best_threads, best_pf);
         c->drop_graph();
         if (best_blocks_per_sm) *best_blocks_per_sm = best;
         if (best_ms) *best_ms = best_t;
     } else {
-        set_sweep_shape(c, c->p.sweep_blocks_per_sm, threads0);
+        set_sweep_shape(c, c->p.sweep_blocks_per_sm, threads0, pf0);
         c->drop_graph();
     }
     if (c->turb()) {

@@ -466,7 +466,7 @@ void launch_wait_selftest(const DevArrays& d, const LaunchCfg& L, long long limi
     *L.counter += 1;
 }
 
-template <bool FWD>
+template <bool FWD, bool PF>
 __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restrict__ order,
                                                     const int4* __restrict__ cface, const int2* __restrict__ lr,
                                                     const d4* __restrict__ fg0, const d4* __restrict__ W,
@@ -489,11 +489,13 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
     // (whose FP64 pipes are separate).  Each warp visits its positions in
     // increasing order: q = q0, q0 + NW, q0 + 2*NW, ...
     const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
-    // The inputs of a position that do not depend on a neighbour's increment
-    // (cell, face slot, neighbour, its W, the face, the per-step SolveDF
-    // constants and the cell's own term) are loaded one position ahead, while
-    // the warp waits for the current position's neighbour, so their chain of
-    // dependent loads stays off the sweep's critical path.
+    // PF: the inputs of a position that do not depend on a neighbour's
+    // increment (cell, face slot, neighbour, its W, the face, the per-step
+    // SolveDF constants and the cell's own term) are loaded one position ahead,
+    // while the warp waits for the current position's neighbour, so their
+    // chain of dependent loads stays off the sweep's critical path; it costs
+    // registers (fewer resident warps), which wide levels may need more, so the
+    // autotuner tries both.
     struct In {
         int i, j;
         int4 cf;
@@ -544,7 +546,7 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
     for (;;) {
         const long long pn = p + (long long)B * NW;
         const bool more = pn < nc;
-        if (more) load(pn, nxt);
+        if (PF && more) load(pn, nxt);
         double dw[4] = {0.0, 0.0, 0.0, 0.0};
         if (cur.use) {
             // the neighbour's increment is final once none of its four words is
@@ -605,6 +607,7 @@ __global__ void __launch_bounds__(256) k_sweep_flow(int nc, const int* __restric
             __stcg(o + 1, make_double2(r2, r3));
         }
         if (!more) break;
+        if (!PF) load(pn, nxt);
         cur = nxt;
         p = pn;
     }
@@ -616,7 +619,8 @@ cudaError_t launch_sweep_flow(const DevArrays& d, const LaunchCfg& L, bool forwa
     void* args[] = {(void*)&nc, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0, (void*)&d.W,
                     (void*)&d.swfc, (void*)&d.swra, (void*)&d.R, (void*)&d.diag, (void*)&d.invD, (void*)&d.dW1,
                     (void*)&d.dW, (void*)&d.err, (void*)&d.poll_ns};
-    void* fn = forward ? (void*)k_sweep_flow<true> : (void*)k_sweep_flow<false>;
+    void* fn = d.flow_pf ? (forward ? (void*)k_sweep_flow<true, true> : (void*)k_sweep_flow<false, true>)
+                         : (forward ? (void*)k_sweep_flow<true, false> : (void*)k_sweep_flow<false, false>);
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(d.flow_threads), args, 0, L.stream);
     *L.counter += 1;
     return e;
@@ -806,7 +810,7 @@ void launch_sweep_prep32(const DevArrays& d, const LaunchCfg& L, bool viscous, i
     *L.counter += 1;
 }
 
-template <bool FWD, bool IND>
+template <bool FWD, bool IND, bool PF>
 __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __restrict__ order2,
                                                       const int4* __restrict__ cface, const int2* __restrict__ lr,
                                                       const float4* __restrict__ fg0f, const float4* __restrict__ Wf,
@@ -831,8 +835,8 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
     // increment - its cells, slots and neighbours, the neighbour's binary32
     // state with the base values of its flux (formed before the wait, so that
     // only the difference terms remain on the dependence chain), r_A and the
-    // cell's own term - are loaded and formed one position ahead, while the
-    // warp waits for the current position's neighbours.
+    // cell's own term - are loaded and formed one position ahead (PF), while
+    // the warp waits for the current position's neighbours.
     struct In {
         int i, j;
         bool active, use, left;
@@ -884,7 +888,7 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
     for (;;) {
         const long long Pn = P + (long long)B * NW;
         const bool more = Pn < npairs;
-        if (more) load(Pn, nxt);
+        if (PF && more) load(Pn, nxt);
         float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
         if (cur.use) {
             const float4* qf = (FWD ? dW1f : dWf) + cur.j;
@@ -952,6 +956,7 @@ __global__ void __launch_bounds__(256) k_sweep_flow32(int npos, const int* __res
             __stcg(o + 1, make_double2(r2, r3));
         }
         if (!more) break;
+        if (!PF) load(Pn, nxt);
         cur = nxt;
         P = Pn;
     }
@@ -963,26 +968,35 @@ cudaError_t launch_sweep_flow32(const DevArrays& d, const LaunchCfg& L, bool for
     void* args[] = {(void*)&npos, (void*)&order, (void*)&d.cface, (void*)&d.lr, (void*)&d.fg0f, (void*)&d.Wf,
                     (void*)&d.swraf, (void*)&d.R, (void*)&d.invD, (void*)&d.dW1, (void*)&d.dW,
                     (void*)&d.dW1f, (void*)&d.dWf, (void*)&d.err, (void*)&d.poll_ns};
-    void* fn = independent ? (forward ? (void*)k_sweep_flow32<true, true> : (void*)k_sweep_flow32<false, true>)
-                           : (forward ? (void*)k_sweep_flow32<true, false> : (void*)k_sweep_flow32<false, false>);
+    void* fn;
+    if (d.flow_pf)
+        fn = independent ? (forward ? (void*)k_sweep_flow32<true, true, true> : (void*)k_sweep_flow32<false, true, true>)
+                         : (forward ? (void*)k_sweep_flow32<true, false, true> : (void*)k_sweep_flow32<false, false, true>);
+    else
+        fn = independent ? (forward ? (void*)k_sweep_flow32<true, true, false> : (void*)k_sweep_flow32<false, true, false>)
+                         : (forward ? (void*)k_sweep_flow32<true, false, false> : (void*)k_sweep_flow32<false, false, false>);
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(d.flow_threads), args, 0, L.stream);
     *L.counter += 1;
     return e;
 }
 
-int sweep_flow_max_grid(bool low, int blocks_per_sm, int threads) {
+int sweep_flow_max_grid(bool low, int blocks_per_sm, int threads, bool pf) {
     int dev = 0, sms = 0, per = 0, per2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    void* fn = low ? (void*)k_sweep_flow32<true, false> : (void*)k_sweep_flow<true>;
-    void* fn2 = low ? (void*)k_sweep_flow32<false, false> : (void*)k_sweep_flow<false>;
+    void* fn = low ? (pf ? (void*)k_sweep_flow32<true, false, true> : (void*)k_sweep_flow32<true, false, false>)
+                   : (pf ? (void*)k_sweep_flow<true, true> : (void*)k_sweep_flow<true, false>);
+    void* fn2 = low ? (pf ? (void*)k_sweep_flow32<false, false, true> : (void*)k_sweep_flow32<false, false, false>)
+                    : (pf ? (void*)k_sweep_flow<false, true> : (void*)k_sweep_flow<false, false>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, fn2, threads, 0);
     per = per < per2 ? per : per2;
     if (low) {  // the independent-halves variant runs on the same grid
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_flow32<true, true>, threads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per2, pf ? (void*)k_sweep_flow32<true, true, true> : (void*)k_sweep_flow32<true, true, false>, threads, 0);
         per = per < per2 ? per : per2;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, (void*)k_sweep_flow32<false, true>, threads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per2, pf ? (void*)k_sweep_flow32<false, true, true> : (void*)k_sweep_flow32<false, true, false>, threads, 0);
         per = per < per2 ? per : per2;
     }
     if (!low) {  // the plain form's paired kernels run on the same grid

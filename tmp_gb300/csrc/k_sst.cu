@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(256) k_sst_sweep_prep(DevArrays d) {
 // T = double: the plain form (every operation in binary64, as the C
 // restatement); T = float: the slot terms in binary32 and the published copy
 // polled in binary32, the increment itself formed in binary64 from them.
-template <bool FWD, class T>
+template <bool FWD, class T, bool PF>
 __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __restrict__ order) {
     const int lane = threadIdx.x & 31;
     const int s = (lane >> 1) & 3, m = lane & 1;
@@ -314,11 +314,12 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
     double* dst = FWD ? d.sstDW1 : d.sstDW;
     float2* dstf = FWD ? d.sstDW1f : d.sstDWf;
     const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
-    // The inputs of a position that do not depend on a neighbour's increment
-    // (its cell, face slot, neighbour and the per-slot constants) are loaded one
-    // position ahead, while the warp waits for the current position's
-    // neighbour: their chain of dependent loads (order, cell faces, face cells,
-    // then the neighbour's records) stays off the sweep's critical path.
+    // PF: the inputs of a position that do not depend on a neighbour's
+    // increment (its cell, face slot, neighbour and the per-slot constants) are
+    // loaded one position ahead, while the warp waits for the current
+    // position's neighbour: their chain of dependent loads (order, cell faces,
+    // face cells, then the neighbour's records) stays off the sweep's critical
+    // path, for more registers per thread.
     struct In {
         int i, j;
         int4 cf;
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
     for (;;) {
         const long long pn = p + (long long)B * NW;
         const bool more = pn < d.nc;
-        if (more) load(pn, nxt);
+        if (PF && more) load(pn, nxt);
         T DF = T(0);
         if (cur.use) {
             long long it = 0;
@@ -423,6 +424,7 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
             if (lane == 0) __stcg(reinterpret_cast<double2*>(dst + 2 * (size_t)cur.i), make_double2(res, r1));
         }
         if (!more) break;
+        if (!PF) load(pn, nxt);
         cur = nxt;
         p = pn;
     }
@@ -490,14 +492,18 @@ void launch_sst_update_mut(const DevArrays& d, const LaunchCfg& L) {
 
 namespace cfdgb {
 
-int sst_sweep_max_grid(int blocks_per_sm, int threads) {
+int sst_sweep_max_grid(int blocks_per_sm, int threads, bool pf) {
     int dev = 0, sms = 0, a = 0, b = 0, c2 = 0, d2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, (void*)k_sst_sweep<true, double>, threads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (void*)k_sst_sweep<false, double>, threads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, (void*)k_sst_sweep<true, float>, threads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d2, (void*)k_sst_sweep<false, float>, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &a, pf ? (void*)k_sst_sweep<true, double, true> : (void*)k_sst_sweep<true, double, false>, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &b, pf ? (void*)k_sst_sweep<false, double, true> : (void*)k_sst_sweep<false, double, false>, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &c2, pf ? (void*)k_sst_sweep<true, float, true> : (void*)k_sst_sweep<true, float, false>, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &d2, pf ? (void*)k_sst_sweep<false, float, true> : (void*)k_sst_sweep<false, float, false>, threads, 0);
     int per = a < b ? a : b;
     per = per < c2 ? per : c2;
     per = per < d2 ? per : d2;
@@ -511,8 +517,13 @@ cudaError_t launch_sst_sweeps(const DevArrays& d, const LaunchCfg& L, bool fp32)
     for (int dir = 0; dir < 2; dir++) {
         const int* order = dir == 0 ? d.fwd_order : d.bwd_order;
         void* args[] = {(void*)&d, (void*)&order};
-        void* fn = fp32 ? (dir == 0 ? (void*)k_sst_sweep<true, float> : (void*)k_sst_sweep<false, float>)
-                        : (dir == 0 ? (void*)k_sst_sweep<true, double> : (void*)k_sst_sweep<false, double>);
+        void* fn;
+        if (d.flow_pf)
+            fn = fp32 ? (dir == 0 ? (void*)k_sst_sweep<true, float, true> : (void*)k_sst_sweep<false, float, true>)
+                      : (dir == 0 ? (void*)k_sst_sweep<true, double, true> : (void*)k_sst_sweep<false, double, true>);
+        else
+            fn = fp32 ? (dir == 0 ? (void*)k_sst_sweep<true, float, false> : (void*)k_sst_sweep<false, float, false>)
+                      : (dir == 0 ? (void*)k_sst_sweep<true, double, false> : (void*)k_sst_sweep<false, double, false>);
         cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(d.sst_grid), dim3(d.flow_threads), args, 0, L.stream);
         *L.counter += 1;
         if (e != cudaSuccess) return e;
