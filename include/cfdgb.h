@@ -329,16 +329,31 @@ typedef struct cfd_interp_s* cfd_interp_t;  /* an interpolation list (MeshBlock:
  * arrays are host memory. */
 int cfd_nodal_weights(long long n, const int* nvert, const double* xv, const double* xp, double* frac);
 /* Upload one mesh's nodes and cells and build its donor-search bins on the
- * device (replaces the ADT of MeshBlock::search, search.cpp:81-270). */
+ * device (the block a MeshBlock registers, tioga::registerGridData). */
 int cfd_block_create(cfd_mesh_t mesh, void* stream, cfd_block_t* out);
 void cfd_block_free(cfd_block_t b);
-/* Donor search for npts points (host xy[2*npts]): donor_cell[i] = the lowest-
- * numbered cell whose bounding box holds the point within TOL = 1e-10 and whose
- * weights all lie in [-TOL, 1+TOL] (checkContainment.cpp:4-64), else -1.
- * donor_nodes[4*i] / weights[4*i] (may be NULL) get its vertices and weights
- * (-1 / 0 when not found or in a triangle's unused slot). */
+/* Donor search for npts points (host xy[2*npts]), as MeshBlock::search
+ * (search.cpp:81-270) chooses: the cells whose boxes cross the oriented box of
+ * the points form the reference's alternating digital tree, and each point
+ * takes the first cell of that tree's walk whose box holds it within
+ * TOL = 1e-10 and whose weights all lie in [-TOL, 1+TOL] (checkContainment.cpp:
+ * 4-62), else -1; where several cells contain a point (a shared edge or
+ * vertex) the donor is the reference's.  Points closer than TOL (L1) to an
+ * earlier point take that point's donor (uniquenodes_octree).  donor_nodes[4*i]
+ * / weights[4*i] (may be NULL) get the donor's vertices and the point's weights
+ * in it (-1 / 0 when not found or in a triangle's unused slot). */
 int cfd_block_search(cfd_block_t b, long long npts, const double* xy, int* donor_cell, int* donor_nodes,
                      double* weights);
+/* The same search with the rest of MeshBlock::search's inputs: tags[i] the
+ * point's mesh tag (coincident points merge only within one tag; NULL: all 1),
+ * res[i] its resolution, merged in place over coincident points as the
+ * reference merges res_search (NULL: not used), cell_unaccept[c] = 1 for a
+ * cell whose cellRes is BIGVALUE (such a cell does not stop the walk where one
+ * of the point's weights vanishes; NULL: none), xtag[i] (may be NULL) the
+ * point whose search point i took. */
+int cfd_block_search_ex(cfd_block_t b, long long npts, const double* xy, const int* tags, double* res,
+                        const unsigned char* cell_unaccept, int* donor_cell, int* donor_nodes, double* weights,
+                        int* xtag);
 /* Cell values as the mean of their nodes' values (Orchestra.cpp:270-291), on
  * device arrays in ROW layout: q_cell[c*nvar + k] = (sum_j q_node[v_j*nvar + k]) / nvert. */
 int cfd_block_node_to_cell(cfd_block_t b, const double* d_q_node, int nvar, double* d_q_cell, void* stream);
@@ -407,7 +422,9 @@ int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, c
  * receptors around holes and, plus one, receptors kept by the fringe
  * reduction (tioga defaults: nfringe 1, mexclude 3).  Distance-scaled
  * resolutions (MeshBlock::reResolution) are not applied, as tioga's default.
- * Donor search ties follow cfd_block_search (the lowest-numbered cell). */
+ * Each block is searched once for the nodes of all other blocks, in block
+ * order, tagged by block and carrying their resolutions, as exchangeSearchData
+ * hands them to MeshBlock::search (cfd_block_search_ex). */
 typedef struct cfd_connect_s* cfd_connect_t;
 int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holemap_t* maps, const int* const* obc_nodes,
                         const int* nobc, int nfringe, int mexclude, cfd_connect_t* out);

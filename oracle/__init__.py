@@ -62,6 +62,7 @@ def _load():
         L.orc_nodal_weights.argtypes = [C.c_long, ip, dp, dp, dp]
         L.orc_nodal_weights.restype = C.c_long
         L.orc_donor_search.argtypes = [dp, C.c_int, ip, ip, C.c_long, dp, ip, ip, dp]
+        L.orc_adt_search.argtypes = [dp, C.c_int, ip, ip, C.c_char_p, C.c_long, dp, ip, dp, ip, ip]
         L.orc_holemap.argtypes = [dp, C.c_int, ip, ip, C.c_int, ip, C.c_int, ip, dp, ip, C.c_long]
         L.orc_holemap.restype = C.c_int
         L.orc_holemap_check.argtypes = [ip, dp, ip, C.c_long, dp, ip]
@@ -190,6 +191,24 @@ def donor_search(xy, cell_verts, cell_nvert, pts):
     w = np.zeros(4 * n)
     _load().orc_donor_search(_dp(x), nv.size, _ip(cv), _ip(nv), n, _dp(p), _ip(donor), _ip(cnt), _dp(w))
     return donor, cnt, w.reshape(n, 4)
+
+
+def adt_search(xy, cell_verts, cell_nvert, pts, unaccept=None, tags=None, res=None):
+    """MeshBlock::search as the reference runs it: the donor (mesh cell, -1 for none) of every point, the point
+    whose search each took (coincident points share one) and the resolutions merged over coincident points."""
+    x = np.ascontiguousarray(xy, np.float64).reshape(-1)
+    cv = np.ascontiguousarray(cell_verts, np.int32).reshape(-1)
+    nv = np.ascontiguousarray(cell_nvert, np.int32)
+    p = np.ascontiguousarray(pts, np.float64).reshape(-1)
+    n = p.size // 2
+    ua = np.zeros(nv.size, np.uint8) if unaccept is None else np.ascontiguousarray(unaccept, np.uint8)
+    tg = np.ones(n, np.int32) if tags is None else np.ascontiguousarray(tags, np.int32)
+    rt = np.ones(n) if res is None else np.array(res, np.float64)
+    donor = np.zeros(n, np.int32)
+    xtag = np.zeros(n, np.int32)
+    _load().orc_adt_search(_dp(x), nv.size, _ip(cv), _ip(nv), ua.ctypes.data_as(C.c_char_p), n, _dp(p), _ip(tg),
+                           _dp(rt), _ip(donor), _ip(xtag))
+    return donor, xtag, rt
 
 
 def interp_update(recv, nw, inode, w, q, nnodes, qr, nnodes_recv, nvar, layout):

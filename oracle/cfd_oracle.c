@@ -1115,6 +1115,502 @@ void orc_donor_search(const double* xy, int ncell, const int* cverts, const int*
     }
 }
 
+/* ---- MeshBlock::search as the reference runs it (UniTioga/search.cpp:81-270),
+ * for the parity of the donor choice where several cells contain a point.
+ * Literal restatement: the oriented box of the query points (findOBB,
+ * UniTioga/utils.cpp:43-291, with Kaiser's eigen-solver, mathTools/kaiser.cpp:
+ * 9-160), the cells whose boxes cross it pushed on a LIFO list, the
+ * alternating digital tree over their axis-aligned boxes (ADT::buildADT,
+ * ADT.cpp:15-91, buildADTrecursion, recursiveADT.cpp:8-109, median split of
+ * mathTools/median.cpp:5-240), the coincident-point hash (uniquenodes_octree,
+ * utils.cpp:484-643) and the recursive walk (searchIntersections,
+ * recursiveADT.cpp:111-156, with checkContainment, checkContainment.cpp:4-62).
+ * 2D only (d_dim = 2, ndim = 4). */
+#define OVS_BIG 1.0e+15 /* BIGVALUE, UniTioga/codetypes.h:52 */
+
+/* Jacobi rotations of kaiser() for a 2x2 matrix a (columns rotated in place),
+ * then the columns normalised by their lengths. */
+static void ovs_kaiser2(double a[2][2]) {
+    const int n = 2;
+    double ss = 0, eps, ev[2];
+    int i, j, k, it;
+    for (i = 0; i < n; i++)
+        for (j = 0; j < n; j++) ss += a[i][j] * a[i][j];
+    eps = 1.0e-12 * ss / n;
+    for (it = 0; it < 100; it++) {
+        int skip = 0;
+        for (i = 0; i < n - 1; i++)
+            for (j = i + 1; j < n; j++) {
+                double halfp = 0, q = 0, p, absp, absq, t, c, s, tmp;
+                for (k = 0; k < n; k++) {
+                    halfp += a[k][i] * a[k][j];
+                    q += (a[k][i] + a[k][j]) * (a[k][i] - a[k][j]);
+                }
+                p = 2 * halfp;
+                absp = fabs(p);
+                if (absp < eps && q >= 0) {
+                    skip++;
+                    continue;
+                }
+                absq = fabs(q);
+                if (absp <= absq) {
+                    t = absp / absq;
+                    c = 1 / sqrt(1 + t * t);
+                    s = t * c;
+                } else {
+                    t = absq / absp;
+                    s = 1 / sqrt(1 + t * t);
+                    c = s * t;
+                }
+                c = sqrt((1 + c) / 2);
+                s = s / (2 * c);
+                if (q < 0) {
+                    tmp = c;
+                    c = s;
+                    s = tmp;
+                }
+                if (p < 0) s = -s;
+                for (k = 0; k < n; k++) {
+                    tmp = a[k][i];
+                    a[k][i] = tmp * c + a[k][j] * s;
+                    a[k][j] = -tmp * s + a[k][j] * c;
+                }
+            }
+        if (skip == 0.5 * n * (n - 1)) break;
+    }
+    for (i = 0; i < n; i++) {
+        double t = 0;
+        for (j = 0; j < n; j++) t += a[j][i] * a[j][i];
+        ev[i] = sqrt(t);
+    }
+    for (i = 0; i < n; i++)
+        for (j = 0; j < n; j++) a[j][i] = ev[i] > 0 ? a[j][i] / ev[i] : 0;
+}
+
+/* findOBB in 2D: centre xc, half extents dxc, basis vec (rows). */
+static void ovs_find_obb(const double* x, long nn, double xc[2], double dxc[2], double vec[2][2]) {
+    double aa[2][2] = {{0, 0}, {0, 0}}, xmin[2], xmax[2], xd[2];
+    long i;
+    int j, k;
+    xc[0] = xc[1] = 0;
+    for (i = 0; i < nn; i++)
+        for (j = 0; j < 2; j++) xc[j] += x[2 * i + j];
+    for (j = 0; j < 2; j++) xc[j] = xc[j] / nn;
+    if (nn <= 2) {
+        vec[0][0] = vec[1][1] = 1;
+        vec[0][1] = vec[1][0] = 0;
+        for (j = 0; j < 2; j++) {
+            if (nn == 1) {
+                dxc[j] = 1e-3;
+            } else {
+                /* TIOGA_MAX(1e-3, d) * 0.5 expands to 1e-3 > d ? 1e-3 : d * 0.5 (the macro has no outer
+                 * parentheses) */
+                double d = fabs(x[2 + j] - x[j]);
+                dxc[j] = 1e-3 > d ? 1e-3 : d * 0.5;
+            }
+        }
+        return;
+    }
+    for (i = 0; i < nn; i++)
+        for (j = 0; j < 2; j++)
+            for (k = j; k < 2; k++) aa[j][k] += (x[2 * i + j] - xc[j]) * (x[2 * i + k] - xc[k]);
+    aa[1][0] = aa[0][1];
+    ovs_kaiser2(aa);
+    for (j = 0; j < 2; j++) {
+        vec[j][0] = aa[j][0];
+        vec[j][1] = aa[j][1];
+        xmax[j] = -OVS_BIG;
+        xmin[j] = OVS_BIG;
+    }
+    for (i = 0; i < nn; i++) {
+        xd[0] = xd[1] = 0;
+        for (j = 0; j < 2; j++)
+            for (k = 0; k < 2; k++) xd[j] += (x[2 * i + k] - xc[k]) * vec[j][k];
+        for (j = 0; j < 2; j++) {
+            xmax[j] = xmax[j] > xd[j] ? xmax[j] : xd[j];
+            xmin[j] = xmin[j] < xd[j] ? xmin[j] : xd[j];
+        }
+    }
+    for (j = 0; j < 2; j++) {
+        dxc[j] = (xmax[j] - xmin[j]) * 0.5 * 1.01;
+        xd[j] = (xmax[j] + xmin[j]) * 0.5;
+    }
+    for (j = 0; j < 2; j++)
+        for (k = 0; k < 2; k++) xc[j] += xd[k] * vec[k][j];
+}
+
+static void ovs_swap(int* ix, double* x, int a, int b) {
+    double t = x[a];
+    int u = ix[a];
+    x[a] = x[b];
+    x[b] = t;
+    ix[a] = ix[b];
+    ix[b] = u;
+}
+
+/* find_median (mathTools/median.cpp:5-190): partial partition of x[*ilow..*ihigh]
+ * about a clamped middle value, recursing on the side that holds the median
+ * position; *ilow / *ihigh are updated as the reference's references are. */
+static void ovs_find_median(int* ix, double* x, int n, int* ilow, int* ihigh) {
+    int low = *ilow, high = *ihigh, mid = (low + high) / 2, nby2 = (n - 1) / 2, nby2p1 = (n - 1) / 2 + 1;
+    int odd = n % 2 == 1, i, j, signal = 1;
+    double xlow = x[low], xhigh = x[high], xmed = x[mid];
+    if (xlow > xhigh) {
+        double t = xlow;
+        xlow = xhigh;
+        xhigh = t;
+    }
+    if (xmed > xhigh) xmed = xhigh;
+    else if (xmed < xlow) xmed = xlow;
+    i = low;
+    j = high;
+    while (signal) {
+        signal = 0;
+        while (!(x[i] >= xmed)) ++i;
+        while (!(x[j] <= xmed)) --j;
+        if (i < j) {
+            ovs_swap(ix, x, i, j);
+            i = i + 1;
+            j = j - 1;
+            if (i <= j) signal = 1;
+        }
+    }
+    if (!odd) {
+        if (j == nby2 && i == nby2p1) {
+            int idx = j, k;
+            for (k = 0; k < nby2; k++)
+                if (x[k] > x[idx]) idx = k;
+            if (idx != j) ovs_swap(ix, x, idx, j);
+            return;
+        }
+        if (j < nby2) low = i;
+        if (i > nby2p1) high = j;
+        if (i != j) {
+            if (low < high - 1) ovs_find_median(ix, x, n, &low, &high);
+            return;
+        }
+        if (i == nby2) low = nby2;
+        if (j == nby2p1) high = nby2p1;
+    } else {
+        if (j < nby2) low = i;
+        if (i > nby2) high = j;
+        if (i != j) {
+            if (low < high - 1) ovs_find_median(ix, x, n, &low, &high);
+            *ilow = low;
+            *ihigh = high;
+            return;
+        }
+        if (i == nby2) {
+            *ilow = low;
+            *ihigh = high;
+            return;
+        }
+    }
+    if (low < high - 1) {
+        *ilow = low;
+        *ihigh = high;
+        ovs_find_median(ix, x, n, &low, &high);
+    }
+}
+
+/* find_median_wrap (median.cpp:192-240) */
+static void ovs_median_wrap(int* ix, double* x, int n) {
+    int ilow = 0, ihigh = n - 1, nby2 = (n - 1) / 2;
+    if (n <= 2) {
+        if (n == 2 && x[0] > x[1]) ovs_swap(ix, x, 0, 1);
+        return;
+    }
+    ovs_find_median(ix, x, n, &ilow, &ihigh);
+    if (n % 2 == 0) {
+        if (x[nby2] > x[nby2 + 1]) ovs_swap(ix, x, nby2, nby2 + 1);
+    } else if (x[ilow] > x[ihigh]) {
+        ovs_swap(ix, x, ilow, ihigh);
+    }
+}
+
+typedef struct {
+    int ndim, nelem;
+    const double* coord; /* per element: min x, min y, max x, max y */
+    int* ints;           /* 4 per node: element, left child element, right child element, (node of element) */
+    double* reals;       /* ndim per node: the subtree's box */
+    double ext[4];       /* adtExtents: min x, max x, min y, max y, widened by 1% */
+    int count;
+} OvsAdt;
+
+/* buildADTrecursion */
+static void ovs_adt_rec(OvsAdt* t, double* work, int* avail, int side, int parent, int level, int nav) {
+    const int ndim = t->ndim, nd = ndim / 2;
+    int i, j;
+    if (nav > 1) {
+        int dimcut = level % ndim, nleft, node;
+        for (i = 0; i < nav; i++) work[i] = t->coord[ndim * avail[i] + dimcut];
+        ovs_median_wrap(avail, work, nav);
+        nleft = (nav + 1) / 2;
+        node = ++t->count;
+        t->ints[4 * node] = avail[nleft - 1];
+        t->ints[4 * node + 1] = t->ints[4 * node + 2] = t->ints[4 * node + 3] = -1;
+        for (j = 0; j < nd; j++) {
+            t->reals[ndim * node + j] = OVS_BIG;
+            t->reals[ndim * node + j + nd] = -OVS_BIG;
+        }
+        for (i = 0; i < nav; i++)
+            for (j = 0; j < nd; j++) {
+                double lo = t->coord[ndim * avail[i] + j], hi = t->coord[ndim * avail[i] + j + nd];
+                double* r = t->reals + ndim * node;
+                r[j] = r[j] < lo ? r[j] : lo;
+                r[j + nd] = r[j + nd] > hi ? r[j + nd] : hi;
+            }
+        if (side > 0) t->ints[4 * parent + side] = avail[nleft - 1];
+        if (nleft > 1) ovs_adt_rec(t, work, avail, 1, node, level + 1, nleft - 1);
+        ovs_adt_rec(t, work, avail + nleft, 2, node, level + 1, nav - nleft);
+    } else if (nav == 1) {
+        int node = ++t->count;
+        t->ints[4 * node] = avail[0];
+        t->ints[4 * node + 1] = t->ints[4 * node + 2] = t->ints[4 * node + 3] = -1;
+        for (j = 0; j < ndim; j++) t->reals[ndim * node + j] = t->coord[ndim * avail[0] + j];
+        if (side > 0) t->ints[4 * parent + side] = avail[0];
+    }
+}
+
+/* ADT::buildADT */
+static void ovs_adt_build(OvsAdt* t, int nelem, const double* coord) {
+    int i, j;
+    int* avail = (int*)malloc(sizeof(int) * (size_t)(nelem > 0 ? nelem : 1));
+    double* work = (double*)malloc(sizeof(double) * (size_t)(nelem > 0 ? nelem : 1));
+    t->ndim = 4;
+    t->nelem = nelem;
+    t->coord = coord;
+    t->ints = (int*)malloc(sizeof(int) * 4 * (size_t)(nelem > 0 ? nelem : 1));
+    t->reals = (double*)malloc(sizeof(double) * 4 * (size_t)(nelem > 0 ? nelem : 1));
+    for (i = 0; i < 2; i++) {
+        t->ext[2 * i] = OVS_BIG;
+        t->ext[2 * i + 1] = -OVS_BIG;
+    }
+    for (j = 0; j < nelem; j++)
+        for (i = 0; i < 2; i++) {
+            double lo = coord[4 * j + i], hi = coord[4 * j + i + 2];
+            t->ext[2 * i] = t->ext[2 * i] < lo ? t->ext[2 * i] : lo;
+            t->ext[2 * i + 1] = t->ext[2 * i + 1] > hi ? t->ext[2 * i + 1] : hi;
+        }
+    for (i = 0; i < 2; i++) {
+        double delta = 0.01 * (t->ext[2 * i + 1] - t->ext[2 * i]);
+        t->ext[2 * i] -= delta;
+        t->ext[2 * i + 1] += delta;
+    }
+    for (i = 0; i < nelem; i++) avail[i] = i;
+    t->count = -1;
+    ovs_adt_rec(t, work, avail, 0, 0, 0, nelem);
+    for (i = 0; i < nelem; i++) t->ints[4 * t->ints[4 * i] + 3] = i;
+    free(avail);
+    free(work);
+}
+
+typedef struct {
+    const double* xy;
+    const int* cverts;   /* mesh cell order, 4 per cell, 0-based */
+    const int* nvert;
+    const int* order;    /* MeshBlock cell -> mesh cell (triangles first, then quadrilaterals) */
+    const unsigned char* unaccept; /* per mesh cell: cellRes == BIGVALUE */
+    const int* elist;    /* ADT element -> MeshBlock cell */
+} OvsBlk;
+
+/* checkContainment: ci[0] = the MeshBlock cell or -1, ci[1] = 1 for a
+ * containing cell with a vanishing weight that may not donate. */
+static void ovs_check(const OvsBlk* b, int* ci, int elem, const double* p) {
+    const int icell = b->elist[elem], c = b->order[icell], nv = b->nvert[c];
+    double x[8], f[4];
+    int m;
+    for (m = 0; m < 4; m++) {
+        const int id = m < nv ? b->cverts[4 * c + m] : b->cverts[4 * c + 2];
+        x[2 * m] = b->xy[2 * id];
+        x[2 * m + 1] = b->xy[2 * id + 1];
+    }
+    ci[0] = icell;
+    ci[1] = 0;
+    if (!ovs_weights(nv, x, p[0], p[1], f)) { /* the reference throws here; taken as no containment */
+        ci[0] = -1;
+        return;
+    }
+    for (m = 0; m < nv; m++) {
+        if ((f[m] + OVS_TOL) * (f[m] - 1.0 - OVS_TOL) > 0) {
+            ci[0] = -1;
+            return;
+        }
+        if (fabs(f[m]) < OVS_TOL && b->unaccept[c]) ci[1] = 1;
+    }
+}
+
+static int ovs_in_box(const double* p, const double* e) {
+    return p[0] >= e[0] - OVS_TOL && p[1] >= e[1] - OVS_TOL && p[0] <= e[2] + OVS_TOL && p[1] <= e[3] + OVS_TOL;
+}
+
+/* searchIntersections */
+static void ovs_adt_walk(const OvsAdt* t, const OvsBlk* b, int* ci, int node, const double* p) {
+    int d;
+    if (ovs_in_box(p, t->coord + 4 * t->ints[4 * node])) {
+        ovs_check(b, ci, t->ints[4 * node], p);
+        if (ci[0] > -1 && ci[1] == 0) return;
+    }
+    for (d = 1; d < 3; d++) {
+        int child = t->ints[4 * node + d];
+        if (child > -1) {
+            child = t->ints[4 * child + 3];
+            if (ovs_in_box(p, t->reals + 4 * child)) {
+                ovs_adt_walk(t, b, ci, child, p);
+                if (ci[0] > -1 && ci[1] == 0) return;
+            }
+        }
+    }
+}
+
+/* uniqNodesTree: coincident points (L1 distance below TOL, same tag) share
+ * one itag; rtag takes the larger resolution. */
+static void ovs_uniq_tree(const double* x, int* itag, double* rtag, const int* tag, int* avail, int nav) {
+    int icheck = 1, i, j;
+    if (nav > 20) {
+        double xmin[2] = {OVS_BIG, OVS_BIG}, xmax[2] = {-OVS_BIG, -OVS_BIG}, xmid[2], dx[2];
+        int npts[4] = {0, 0, 0, 0}, cft[5];
+        icheck = 0;
+        for (i = 0; i < nav; i++)
+            for (j = 0; j < 2; j++) {
+                const double v = x[2 * avail[i] + j];
+                xmin[j] = xmin[j] < v ? xmin[j] : v;
+                xmax[j] = xmax[j] > v ? xmax[j] : v;
+            }
+        for (j = 0; j < 2; j++) {
+            xmid[j] = (xmax[j] + xmin[j]) * 0.5;
+            dx[j] = (xmax[j] - xmin[j]) * 0.5 + OVS_TOL;
+        }
+#define OVS_IBOX(q) (2 * ((int)floor((x[2 * (q)] - xmid[0]) / dx[0]) + 1) + ((int)floor((x[2 * (q) + 1] - xmid[1]) / dx[1]) + 1))
+        for (i = 0; i < nav; i++) npts[OVS_IBOX(avail[i])]++;
+        for (j = 0; j < 4; j++)
+            if (npts[j] == nav) icheck = 1;
+        if (!icheck) {
+            int* tmp = (int*)malloc(sizeof(int) * (size_t)nav);
+            cft[0] = 0;
+            for (j = 0; j < 4; j++) cft[j + 1] = cft[j] + npts[j];
+            for (i = 0; i < nav; i++) {
+                const int ib = OVS_IBOX(avail[i]);
+                npts[ib]--;
+                tmp[npts[ib] + cft[ib]] = avail[i];
+            }
+            memcpy(avail, tmp, sizeof(int) * (size_t)nav);
+            free(tmp);
+            for (j = 0; j < 4; j++)
+                if (cft[j + 1] > cft[j]) ovs_uniq_tree(x, itag, rtag, tag, avail + cft[j], cft[j + 1] - cft[j]);
+        }
+#undef OVS_IBOX
+    }
+    if (icheck)
+        for (i = 0; i < nav; i++) {
+            const int p1 = avail[i];
+            for (j = i + 1; j < nav; j++) {
+                const int p2 = avail[j];
+                if (fabs(x[2 * p1] - x[2 * p2]) + fabs(x[2 * p1 + 1] - x[2 * p2 + 1]) < OVS_TOL && tag[p1] == tag[p2]) {
+                    if (p1 > p2) {
+                        rtag[p2] = rtag[p1] > rtag[p2] ? rtag[p1] : rtag[p2];
+                        itag[p1] = itag[p2];
+                    } else {
+                        rtag[p1] = rtag[p1] > rtag[p2] ? rtag[p1] : rtag[p2];
+                        itag[p2] = itag[p1];
+                    }
+                }
+            }
+        }
+}
+
+/* MeshBlock::search of npts points (tags per point, resolutions rtag merged in
+ * place over coincident points) in a block whose cells are given in mesh
+ * order; unaccept[c] marks the cells whose cellRes is BIGVALUE.  donor[i] =
+ * the mesh cell (-1: none), xtag[i] = the point whose search it took. */
+void orc_adt_search(const double* xy, int ncell, const int* cverts, const int* nvert, const unsigned char* unaccept,
+                    long npts, const double* pts, const int* tags, double* rtag, int* donor, int* xtag) {
+    OvsBlk b;
+    OvsAdt t;
+    double xc[2], dxc[2], vec[2][2], *bbox;
+    int *order, *icell, *elist, *avail, iptr = -1, count = 0, p, k, l, nt = 0;
+    long i;
+    if (npts <= 0) return;
+    order = (int*)malloc(sizeof(int) * (size_t)(ncell > 0 ? ncell : 1));
+    for (k = 0; k < 2; k++)
+        for (p = 0; p < ncell; p++)
+            if ((nvert[p] == 3) == (k == 0)) order[nt++] = p;
+    ovs_find_obb(pts, npts, xc, dxc, vec);
+    icell = (int*)malloc(sizeof(int) * (size_t)(ncell > 0 ? ncell : 1));
+    for (p = 0; p < ncell; p++) {
+        const int c = order[p], nv = nvert[c];
+        double xmn[2] = {OVS_BIG, OVS_BIG}, xmx[2] = {-OVS_BIG, -OVS_BIG}, xd[2] = {0, 0}, dx[2] = {0, 0};
+        int m, j, q, cross = 1;
+        icell[p] = -1;
+        for (m = 0; m < nv; m++) {
+            const int id = cverts[4 * c + m];
+            for (j = 0; j < 2; j++) {
+                xd[j] = 0;
+                for (q = 0; q < 2; q++) xd[j] += (xy[2 * id + q] - xc[q]) * vec[j][q];
+                xmn[j] = xmn[j] < xd[j] ? xmn[j] : xd[j];
+                xmx[j] = xmx[j] > xd[j] ? xmx[j] : xd[j];
+            }
+            for (j = 0; j < 2; j++) {
+                xd[j] = (xmx[j] + xmn[j]) * 0.5;
+                dx[j] = (xmx[j] - xmn[j]) * 0.5;
+            }
+        }
+        for (j = 0; j < 2; j++) cross = cross && (fabs(xd[j]) <= dx[j] + dxc[j]);
+        if (cross) {
+            icell[p] = iptr;
+            iptr = p;
+            count++;
+        }
+    }
+    bbox = (double*)malloc(sizeof(double) * 4 * (size_t)(count > 0 ? count : 1));
+    elist = (int*)malloc(sizeof(int) * (size_t)(count > 0 ? count : 1));
+    for (k = iptr, l = 0; k != -1; k = icell[k], l++) {
+        const int c = order[k], nv = nvert[c];
+        double xmn[2] = {OVS_BIG, OVS_BIG}, xmx[2] = {-OVS_BIG, -OVS_BIG};
+        int m, j;
+        for (m = 0; m < nv; m++)
+            for (j = 0; j < 2; j++) {
+                const double v = xy[2 * cverts[4 * c + m] + j];
+                xmn[j] = xmn[j] < v ? xmn[j] : v;
+                xmx[j] = xmx[j] > v ? xmx[j] : v;
+            }
+        bbox[4 * l] = xmn[0];
+        bbox[4 * l + 1] = xmn[1];
+        bbox[4 * l + 2] = xmx[0];
+        bbox[4 * l + 3] = xmx[1];
+        elist[l] = k;
+    }
+    ovs_adt_build(&t, count, bbox);
+    b.xy = xy;
+    b.cverts = cverts;
+    b.nvert = nvert;
+    b.order = order;
+    b.unaccept = unaccept;
+    b.elist = elist;
+    avail = (int*)malloc(sizeof(int) * (size_t)npts);
+    for (i = 0; i < npts; i++) avail[i] = (int)i, xtag[i] = (int)i;
+    ovs_uniq_tree(pts, xtag, rtag, tags, avail, (int)npts);
+    for (i = 0; i < npts; i++) {
+        if (xtag[i] == i) {
+            int ci[2] = {-1, 0};
+            const double* q = pts + 2 * i;
+            if (q[0] >= t.ext[0] - OVS_TOL && q[1] >= t.ext[2] - OVS_TOL && q[0] <= t.ext[1] + OVS_TOL &&
+                q[1] <= t.ext[3] + OVS_TOL && count > 0)
+                ovs_adt_walk(&t, &b, ci, 0, q);
+            donor[i] = ci[0] < 0 ? -1 : order[ci[0]];
+        } else {
+            donor[i] = donor[xtag[i]];
+        }
+    }
+    free(avail);
+    free(t.ints);
+    free(t.reals);
+    free(bbox);
+    free(elist);
+    free(icell);
+    free(order);
+}
+
 /* getInterpolatedSolution + updateSolnData (UniTioga/dataUpdate.cpp:6-132):
  * receptor i gets sum_m q[inode[4i+m]] * w[4i+m] (m < nw[i], from 0, in list
  * order) and writes it to node recv[i] of qr, records in list order; layout 0

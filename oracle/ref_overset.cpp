@@ -10,6 +10,10 @@
 //     MESH: int32 nnode, ncell; double xy[2*nnode]; int32 nvert[ncell]; int32 verts[4*ncell] (0-based)
 //     PTS:  int32 n; double xy[2*n]
 //     OUT:  int32 donor[n] in the mesh's own cell numbering (-1: none)
+//   ref_overset search2 MESH PTS OUT   the same search with per-point mesh tags and
+//     resolutions and per-cell donor acceptance (cellRes = BIGVALUE where refused)
+//     PTS:  int32 n; double xy[2*n]; int32 tag[n]; double res[n]; int32 unaccept[ncell] (mesh order)
+//     OUT:  int32 donor[n] (mesh numbering, -1: none); int32 xtag[n]; double res[n] after the search
 //   ref_overset interp LIST OUT   MeshBlock::getInterpolatedSolution + updateSolnData
 //     (UniTioga/dataUpdate.cpp:6-132), ROW then COLUMN
 //     LIST: int32 nnodes, nvar, ninterp, nrecv_nodes; double q[nnodes*nvar] (ROW);
@@ -450,6 +454,45 @@ static int do_connect(const char* inf, const char* out) {
     return 0;  // the blocks are left allocated: the driver exits next
 }
 
+static int do_search2(const char* meshf, const char* ptsf, const char* out) {
+    static BlockData d;
+    if (!read_block(meshf, d)) return 3;
+    FILE* fp = fopen(ptsf, "rb");
+    if (!fp) return 3;
+    int n;
+    if (!rd(fp, &n, 1) || n < 0) return 3;
+    static std::vector<double> pts, res;
+    static std::vector<int> tags, unacc;
+    pts.resize(2 * (size_t)n);
+    tags.resize(n);
+    res.resize(n);
+    unacc.resize(d.ncell);
+    if (!rd(fp, pts.data(), pts.size()) || !rd(fp, tags.data(), n) || !rd(fp, res.data(), n) ||
+        !rd(fp, unacc.data(), d.ncell))
+        return 3;
+    fclose(fp);
+    MeshBlock* mb = make_block(d);
+    for (int k = 0; k < d.ncell; k++)
+        if (unacc[d.order[k]]) d.cellres[k] = BIGVALUE;
+    mb->nsearch = n;
+    mb->xsearch = pts.data();
+    mb->tagsearch = tags.data();
+    mb->res_search = res.data();
+    mb->search();
+    std::vector<int> donor(n, -1), xtag(n, 0);
+    for (int i = 0; i < n; i++) {
+        donor[i] = mb->donorId[i] < 0 ? -1 : d.order[mb->donorId[i]];
+        xtag[i] = mb->xtag[i];
+    }
+    FILE* fo = fopen(out, "wb");
+    if (!fo) return 4;
+    fwrite(donor.data(), 4, donor.size(), fo);
+    fwrite(xtag.data(), 4, xtag.size(), fo);
+    fwrite(res.data(), 8, res.size(), fo);
+    fclose(fo);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) {
         fprintf(stderr, "usage: %s weights|search|interp ...\n", argv[0]);
@@ -458,6 +501,7 @@ int main(int argc, char** argv) {
     const std::string mode = argv[1];
     if (mode == "weights" && argc == 4) return do_weights(argv[2], argv[3]);
     if (mode == "search" && argc == 5) return do_search(argv[2], argv[3], argv[4]);
+    if (mode == "search2" && argc == 5) return do_search2(argv[2], argv[3], argv[4]);
     if (mode == "interp" && argc == 4) return do_interp(argv[2], argv[3]);
     if (mode == "holemap" && argc == 6) return do_holemap(argv[2], argv[3], argv[4], argv[5]);
     if (mode == "celliblank" && argc == 5) return do_celliblank(argv[2], argv[3], argv[4]);

@@ -14,9 +14,15 @@ one rank of tioga::performConnectivity runs them) on seeded overset systems:
   three   a background and two overlapping cylinder O-grids (donor lists with
           several candidates)
 
-The component grids are rotated and shifted by irrational amounts so that no
-background node lies on a component edge (the two donor searches break ties
-between cells differently).  Each case stores every block's .grd arrays, wall
+  tcyl    the cylinder pair unrotated and centred on a background node: nodes
+          of each mesh lie on edges and radial lines of the other, so many
+          points lie in two or more cells (the donor is the first containing
+          cell of the reference's tree walk)
+  tthree  the three-mesh system with its O-grids unrotated and centred on
+          background nodes
+
+The other component grids are rotated and shifted by irrational amounts, so
+that every node lies inside one cell only.  Each case stores every block's .grd arrays, wall
 and overset-boundary nodes, and the reference's node iblank, cell iblank and
 surviving interpolations per donor block.
 
@@ -111,6 +117,11 @@ def cases():
     c2 = transform(meshgen.o_mesh(40, 12, r0=0.3, dr1=0.01, rout=1.0), 0.3141, (1.0371, 0.4129))
     c3 = transform(meshgen.o_mesh(40, 12, r0=0.3, dr1=0.01, rout=1.0), 1.2345, (-0.5213, -0.3377))
     yield "three", [bg, c2, c3], 1, 3
+    # background nodes lie on multiples of 6/64 = 0.09375, all exact binary fractions
+    yield "tcyl", [bg, meshgen.o_mesh(48, 16, r0=0.5, dr1=0.01, rout=1.5)], 1, 3
+    t2 = transform(meshgen.o_mesh(40, 12, r0=0.3, dr1=0.01, rout=1.0), 0.0, (0.9375, 0.375))
+    t3 = transform(meshgen.o_mesh(40, 12, r0=0.3, dr1=0.01, rout=1.0), 0.0, (-0.75, -0.5625))
+    yield "tthree", [bg, t2, t3], 1, 3
 
 
 def main():

@@ -19,6 +19,13 @@ mathTools sources by oracle/build_ref.sh) on seeded inputs:
   celliblank MeshBlock::getCellIblanks of random node blanking (holes,
             receptors, field nodes in clusters) on both golden meshes
 
+and tests/golden/overset_ties.npz, MeshBlock::search where several cells
+contain a point: every mesh node, every edge midpoint, cell centres and random
+points, coincident copies (within the 1e-10 L1 tolerance, same and other mesh
+tag), per-point resolutions and a random 30% of the cells refused as donors
+(cellRes = BIGVALUE), on both golden meshes and on a mesh whose edges carry
+the nodes of a second Cartesian mesh shifted by half a cell.
+
 usage: python tests/golden/make_golden_overset.py [REFERENCE_ROOT]
 """
 from __future__ import annotations
@@ -129,6 +136,73 @@ def cell_centres(m):
     return out
 
 
+def edge_midpoints(m):
+    cv = m.cell_verts.reshape(-1, 4)
+    xy = m.xy.reshape(-1, 2)
+    e = set()
+    for c in range(m.ncell):
+        n = m.cell_nvert[c]
+        for k in range(n):
+            a, b = int(cv[c, k]), int(cv[c, (k + 1) % n])
+            e.add((min(a, b), max(a, b)))
+    e = np.array(sorted(e))
+    return (xy[e[:, 0]] + xy[e[:, 1]]) * 0.5
+
+
+def ties_cases(rng: np.random.Generator):
+    from tmp_gb300 import meshgen
+
+    om = grd.read_grd(HERE / "omesh.grd", -1, -2)
+    mx = grd.read_grd(HERE / "mixed.grd", -1, -2)
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        g = meshgen.cart_mesh(24, 20, (-1.0, -1.0), (1.0, 1.0))
+        meshgen.write_grd(td / "ct.grd", g)
+        cart = grd.read_grd(td / "ct.grd", g.wall_tag, g.far_tag)
+        for name, m in (("mx", mx), ("om", om), ("ct", cart)):
+            xy = m.xy.reshape(-1, 2)
+            lo, hi = xy.min(0), xy.max(0)
+            base = [xy, edge_midpoints(m), cell_centres(m), lo + rng.uniform(-0.05, 1.05, (400, 2)) * (hi - lo)]
+            if name == "ct":  # the nodes of a Cartesian mesh shifted by half a cell lie on this one's edges
+                h = (hi - lo) / np.array([24, 20])
+                base.append(meshgen.cart_mesh(24, 20, tuple(lo + h / 2), tuple(hi + h / 2)).xy.reshape(-1, 2))
+            pts = np.concatenate(base)
+            # coincident copies: within the tolerance (L1 below 1e-10) or exact, same tag or another
+            pick = rng.choice(len(pts), 300, replace=False)
+            dup = pts[pick] + rng.choice([0.0, 2e-11, -3e-11], (300, 2))
+            pts = np.concatenate([pts, dup])
+            perm = rng.permutation(len(pts))
+            pts = pts[perm]
+            tags = np.where(rng.random(len(pts)) < 0.2, 2, 1).astype(np.int32)
+            res = rng.uniform(0.5, 2.0, len(pts))
+            unacc = (rng.random(m.ncell) < 0.3).astype(np.int32)
+            write_mesh(td / "m.bin", m)
+            with open(td / "p.bin", "wb") as f:
+                np.array([len(pts)], np.int32).tofile(f)
+                pts.astype(np.float64).tofile(f)
+                tags.tofile(f)
+                res.astype(np.float64).tofile(f)
+                unacc.tofile(f)
+            _run("search2", td / "m.bin", td / "p.bin", td / "s.out", cwd=td)
+            raw = (td / "s.out").read_bytes()
+            n = len(pts)
+            out[f"{name}_pts"] = pts
+            out[f"{name}_tags"] = tags
+            out[f"{name}_res"] = res
+            out[f"{name}_unaccept"] = unacc
+            out[f"{name}_donor"] = np.frombuffer(raw[:4 * n], np.int32)
+            out[f"{name}_xtag"] = np.frombuffer(raw[4 * n:8 * n], np.int32)
+            out[f"{name}_res_out"] = np.frombuffer(raw[8 * n:], np.float64)
+            if name == "ct":
+                out["ct_mesh_xy"] = m.xy
+                out["ct_mesh_verts"] = m.cell_verts
+                out["ct_mesh_nvert"] = m.cell_nvert
+    np.savez_compressed(HERE / "overset_ties.npz", **out)
+    print(f"wrote {HERE / 'overset_ties.npz'}: " + ", ".join(f"{k}: {len(out[k + '_pts'])} points"
+                                                           for k in ("mx", "om", "ct")))
+
+
 def main():
     if not DRV.exists():
         raise SystemExit(f"{DRV} missing: run oracle/build_ref.sh first")
@@ -228,6 +302,7 @@ def main():
     np.savez_compressed(HERE / "overset.npz", **out)
     print(f"wrote {HERE / 'overset.npz'}: {nv.size} weight cases, "
           f"{sum(v.size for k, v in out.items() if k.endswith('_donor'))} search points")
+    ties_cases(np.random.default_rng(20261204))
 
 
 if __name__ == "__main__":

@@ -1,0 +1,164 @@
+"""The donor search's tree order, host half (tmp_gb300/csrc/adt.cpp), on the CPU.
+
+The device search (k_donor_search) keeps, per point, the contained and
+acceptable cell of lowest preorder number in the reference's search tree, else
+the outcome of the highest-numbered cell it checks, and coincident points take
+the first one's donor.  Here the product's host code (compiled with g++ into
+tests/adt_check.cpp) gives the tree order and the coincident-point hash, the
+same selection is evaluated in numpy with the oracle's weights, and the donors
+must be the reference's own (tests/golden/overset.npz, overset_ties.npz, from
+MeshBlock::search compiled from its sources) on every point, ties included.
+"""
+from __future__ import annotations
+
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+import oracle
+from oracle import grd
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not present")
+    exe = tmp_path_factory.mktemp("adt") / "adt_check"
+    csrc = ROOT / "tmp_gb300" / "csrc"
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", f"-I{csrc}", str(ROOT / "tests" / "adt_check.cpp"),
+           str(csrc / "adt.cpp"), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+def run(exe, tmp, xy, cv, nv, pts, tags, res):
+    inp, out = tmp / "in.bin", tmp / "out.bin"
+    with open(inp, "wb") as f:
+        np.array([len(xy.reshape(-1)) // 2, len(nv)], np.int32).tofile(f)
+        np.asarray(xy, np.float64).tofile(f)
+        np.asarray(nv, np.int32).tofile(f)
+        np.asarray(cv, np.int32).reshape(-1).tofile(f)
+        np.array([len(pts)], np.int32).tofile(f)
+        np.asarray(pts, np.float64).tofile(f)
+        np.asarray(tags, np.int32).tofile(f)
+        np.asarray(res, np.float64).tofile(f)
+    subprocess.run([str(exe), str(inp), str(out)], check=True)
+    raw = out.read_bytes()
+    nc, n = len(nv), len(pts)
+    rank = np.frombuffer(raw[:4 * nc], np.int32)
+    xtag = np.frombuffer(raw[4 * nc:4 * (nc + n)], np.int32)
+    rout = np.frombuffer(raw[4 * (nc + n):], np.float64)
+    return rank, xtag, rout
+
+
+def select(xy, cv, nv, pts, rank, unacc, xtag, amb=None):
+    """k_donor_search's choice per point, then k_take_coincident's; amb (optional, filled): the points whose
+    choice depends on the order of the tree cells (several cells stop the walk, or none does and a refused one
+    contains the point)."""
+    xy = np.asarray(xy).reshape(-1, 2)
+    cv = np.asarray(cv).reshape(-1, 4)
+    lo = np.full((len(nv), 2), 1e15)
+    hi = np.full((len(nv), 2), -1e15)
+    for m in range(4):
+        has = nv > m
+        v = xy[cv[has, m]]
+        lo[has] = np.minimum(lo[has], v)
+        hi[has] = np.maximum(hi[has], v)
+    n = len(pts)
+    donor = np.full(n, -1, np.int32)
+    for i in range(n):
+        if xtag[i] != i:
+            continue
+        p = pts[i]
+        cand = np.flatnonzero((rank >= 0) & (p[0] >= lo[:, 0] - TOL) & (p[1] >= lo[:, 1] - TOL) &
+                              (p[0] <= hi[:, 0] + TOL) & (p[1] <= hi[:, 1] + TOL))
+        if cand.size == 0:
+            continue
+        xv = np.zeros((cand.size, 8))
+        for m in range(4):
+            idx = np.where(nv[cand] > m, cv[cand, m], cv[cand, 2])
+            xv[:, 2 * m:2 * m + 2] = xy[idx]
+        f, bad = oracle.nodal_weights(nv[cand], xv, np.repeat(p[None], cand.size, 0))
+        assert bad == 0
+        used = np.arange(4)[None, :] < nv[cand][:, None]
+        inside = np.all(~used | ((f + TOL) * (f - 1.0 - TOL) <= 0), axis=1)
+        refused = unacc[cand].astype(bool) & np.any(used & (np.abs(f) < TOL), axis=1)
+        good = inside & ~refused
+        if amb is not None:
+            amb[i] = good.sum() > 1 or (good.sum() == 0 and (inside & refused).any())
+        if good.any():
+            donor[i] = cand[good][np.argmin(rank[cand][good])]
+        else:
+            k = np.argmax(rank[cand])
+            donor[i] = cand[k] if inside[k] else -1
+    for i in range(n):  # xtag[i] <= i: the group's first point is already final
+        if xtag[i] != i:
+            donor[i] = donor[xtag[i]]
+    return donor
+
+
+def _golden_meshes():
+    return {"mx": grd.read_grd(GOLDEN / "mixed.grd", -1, -2), "om": grd.read_grd(GOLDEN / "omesh.grd", -1, -2)}
+
+
+@pytest.mark.parametrize("name", ["mx", "om"])
+def test_tree_order_gives_reference_donors(harness, tmp_path, name):
+    ov = np.load(GOLDEN / "overset.npz")
+    m = _golden_meshes()[name]
+    pts, ref = ov[f"s_{name}_pts"], ov[f"s_{name}_donor"]
+    n = len(pts)
+    rank, xtag, _ = run(harness, tmp_path, m.xy, m.cell_verts, m.cell_nvert, pts, np.ones(n), np.ones(n))
+    donor = select(m.xy, m.cell_verts, m.cell_nvert, pts, rank, np.zeros(m.ncell, np.uint8), xtag)
+    assert np.array_equal(donor, ref)
+    _, cnt, _ = oracle.donor_search(m.xy, m.cell_verts, m.cell_nvert, pts)
+    assert (cnt > 1).sum() >= 100  # ties: points in several cells
+
+
+@pytest.mark.parametrize("name", ["mx", "om", "ct"])
+def test_tree_order_ties_refusals_and_coincident_points(harness, tmp_path, name):
+    t = np.load(GOLDEN / "overset_ties.npz")
+    if name == "ct":
+        xy, cv, nv = t["ct_mesh_xy"], t["ct_mesh_verts"], t["ct_mesh_nvert"]
+    else:
+        m = _golden_meshes()[name]
+        xy, cv, nv = m.xy, m.cell_verts, m.cell_nvert
+    pts = t[f"{name}_pts"]
+    rank, xtag, rout = run(harness, tmp_path, xy, cv, nv, pts, t[f"{name}_tags"], t[f"{name}_res"])
+    assert np.array_equal(xtag, t[f"{name}_xtag"])
+    assert np.array_equal(rout.view(np.int64), t[f"{name}_res_out"].view(np.int64))
+    assert (xtag != np.arange(len(pts))).sum() > 100
+    donor = select(xy, cv, nv, pts, rank, t[f"{name}_unaccept"], xtag)
+    assert np.array_equal(donor, t[f"{name}_donor"])
+    # the device's first pass gives every tree cell one rank: it is exact wherever the choice does not depend on
+    # the order, and it flags the rest
+    amb = np.zeros(len(pts), bool)
+    first = select(xy, cv, nv, pts, np.where(rank >= 0, 0, -1), t[f"{name}_unaccept"], np.arange(len(pts)), amb)
+    assert amb.sum() > 50
+    assert np.array_equal(first[~amb], select(xy, cv, nv, pts, rank, t[f"{name}_unaccept"], np.arange(len(pts)))[~amb])
+
+
+@pytest.mark.parametrize("name", ["mx", "om", "ct"])
+def test_oracle_walk_matches_reference(name):
+    """The oracle's literal restatement of the tree walk (oracle/cfd_oracle.c, orc_adt_search)."""
+    t = np.load(GOLDEN / "overset_ties.npz")
+    if name == "ct":
+        xy, cv, nv = t["ct_mesh_xy"], t["ct_mesh_verts"], t["ct_mesh_nvert"]
+    else:
+        m = _golden_meshes()[name]
+        xy, cv, nv = m.xy, m.cell_verts, m.cell_nvert
+    d, xt, r = oracle.adt_search(xy, cv, nv, t[f"{name}_pts"], t[f"{name}_unaccept"], t[f"{name}_tags"],
+                                 t[f"{name}_res"])
+    assert np.array_equal(d, t[f"{name}_donor"])
+    assert np.array_equal(xt, t[f"{name}_xtag"])
+    assert np.array_equal(r.view(np.int64), t[f"{name}_res_out"].view(np.int64))
+    ov = np.load(GOLDEN / "overset.npz")
+    if name != "ct":
+        d, _, _ = oracle.adt_search(xy, cv, nv, ov[f"s_{name}_pts"])
+        assert np.array_equal(d, ov[f"s_{name}_donor"])

@@ -1,9 +1,11 @@
 """Overset kernels on the GPU against the oracle and the reference's fixtures.
 
-Weights and interpolated values are compared bit for bit.  Donor search is
-compared with the oracle's brute-force containment everywhere (both take the
-lowest-numbered containing cell) and with the reference's own search wherever
-exactly one cell contains the point.
+Weights and interpolated values are compared bit for bit.  Donors are
+compared with the reference's own MeshBlock::search on every fixture point,
+including points that lie in several cells (a shared edge or vertex, where the
+first cell of the reference's tree walk donates), coincident points and cells
+refused as donors (tests/golden/overset_ties.npz), and with the oracle's
+literal restatement of that walk (orc_adt_search) on larger random sets.
 """
 from __future__ import annotations
 
@@ -59,21 +61,70 @@ def test_weights_match_oracle_random(built_lib):
     assert _eq(abi.nodal_weights(nv[ok], xv[ok], xp[ok]), ref[ok])
 
 
+def _weights_in(topo, pts, donor):
+    """The oracle's weights of each point in its donor cell (0 where there is none)."""
+    xy = topo.xy.reshape(-1, 2)
+    cv = topo.cell_verts.reshape(-1, 4)
+    hit = donor >= 0
+    w = np.zeros((len(pts), 4))
+    c = donor[hit]
+    nv = topo.cell_nvert[c]
+    xv = np.zeros((c.size, 8))
+    for m in range(4):
+        xv[:, 2 * m:2 * m + 2] = xy[np.where(nv > m, cv[c, m], cv[c, 2])]
+    f, bad = oracle.nodal_weights(nv, xv, pts[hit])
+    assert bad == 0
+    w[hit] = f
+    return w
+
+
 def test_search_matches_reference_and_oracle(built_lib, ov):
     from tmp_gb300 import abi
 
     for name, (mesh, blk, topo) in _blocks(abi).items():
         pts, ref = ov[f"s_{name}_pts"], ov[f"s_{name}_donor"]
         d, nodes, w = blk.search(pts)
-        od, cnt, ow = oracle.donor_search(topo.xy, topo.cell_verts, topo.cell_nvert, pts)
+        assert np.array_equal(d, ref)  # every point, the ties included
+        od, _, _ = oracle.adt_search(topo.xy, topo.cell_verts, topo.cell_nvert, pts)
         assert np.array_equal(d, od)
-        assert _eq(w, ow)
-        uniq = cnt <= 1
-        assert np.array_equal(d[uniq], ref[uniq])
+        assert _eq(w, _weights_in(topo, pts, d))
+        low, cnt, _ = oracle.donor_search(topo.xy, topo.cell_verts, topo.cell_nvert, pts)
+        assert (cnt > 1).sum() >= 100 and (d != low).sum() > 50  # ties where the tree order matters
         cv = topo.cell_verts.reshape(-1, 4)
         hit = d >= 0
         assert np.array_equal(nodes[hit], cv[d[hit]])
         assert np.all(nodes[~hit] == -1)
+
+
+@pytest.mark.parametrize("name", ["mx", "om", "ct"])
+def test_search_ties_refusals_and_coincident_points(built_lib, name):
+    """overset_ties.npz: every node, every edge midpoint, coincident copies (same and other tag), per-point
+    resolutions and 30% of the cells refused as donors, against the reference's MeshBlock::search."""
+    from tmp_gb300 import abi
+
+    from tmp_gb300 import meshgen
+
+    t = np.load(GOLDEN / "overset_ties.npz")
+    if name == "ct":  # the fixture's Cartesian mesh, regenerated; its cells must be the ones the reference saw
+        g = meshgen.cart_mesh(24, 20, (-1.0, -1.0), (1.0, 1.0))
+        path = GOLDEN.parent / "_ct_tmp.grd"
+        meshgen.write_grd(path, g)
+        try:
+            mesh = abi.Mesh.load_grd(path, g.wall_tag, g.far_tag)
+            topo = grd.read_grd(path, g.wall_tag, g.far_tag)
+        finally:
+            path.unlink()
+        assert np.array_equal(topo.xy, t["ct_mesh_xy"]) and np.array_equal(topo.cell_verts, t["ct_mesh_verts"])
+        blk = abi.Block(mesh)
+    else:
+        mesh, blk, topo = _blocks(abi)[name]
+    pts = t[f"{name}_pts"]
+    d, nodes, w, xtag, res = blk.search_ex(pts, t[f"{name}_tags"], t[f"{name}_res"], t[f"{name}_unaccept"])
+    assert np.array_equal(d, t[f"{name}_donor"])
+    assert np.array_equal(xtag, t[f"{name}_xtag"])
+    assert _eq(res, t[f"{name}_res_out"])
+    assert _eq(w, _weights_in(topo, pts, d))  # merged points: their own weights in the first point's cell
+    assert (xtag != np.arange(len(pts))).sum() > 100
 
 
 def test_search_larger_mesh_random_points(built_lib):
@@ -96,8 +147,9 @@ def test_search_larger_mesh_random_points(built_lib):
                           xy[rng.choice(len(xy), 2000, replace=False)],
                           rng.normal(0.5, 0.3, (8000, 2))])
     d, _, w = blk.search(pts)
-    od, cnt, ow = oracle.donor_search(topo.xy, topo.cell_verts, topo.cell_nvert, pts)
-    assert np.array_equal(d, od) and _eq(w, ow)
+    od, _, _ = oracle.adt_search(topo.xy, topo.cell_verts, topo.cell_nvert, pts)
+    assert np.array_equal(d, od) and _eq(w, _weights_in(topo, pts, d))
+    _, cnt, _ = oracle.donor_search(topo.xy, topo.cell_verts, topo.cell_nvert, pts)
     assert (cnt > 1).sum() > 100 and (d >= 0).sum() > 20000
 
 

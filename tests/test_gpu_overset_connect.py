@@ -2,7 +2,9 @@
 own assembly code: node iblank, cell iblank and the surviving interpolation
 lists, bit for bit, on the systems of tests/golden/overset_connect.npz
 (background + cylinder O-grid with two fringe settings, background + mixed
-mesh around an airfoil, background + two overlapping O-grids).
+mesh around an airfoil, background + two overlapping O-grids, and the
+cylinder and three-mesh systems unrotated on background nodes, where many
+nodes lie in two or more donor cells).
 """
 from __future__ import annotations
 
@@ -19,7 +21,7 @@ def gc():
     return np.load(GOLDEN / "overset_connect.npz")
 
 
-@pytest.mark.parametrize("case", ["cyl", "cyl2", "naca", "three"])
+@pytest.mark.parametrize("case", ["cyl", "cyl2", "naca", "three", "tcyl", "tthree"])
 def test_connect_matches_reference(built_lib, gc, case):
     from tmp_gb300 import abi
 

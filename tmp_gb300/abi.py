@@ -104,6 +104,7 @@ def lib() -> C.CDLL:
         "cfd_block_create": (C.c_int, [vp, vp, C.POINTER(vp)]),
         "cfd_block_free": (None, [vp]),
         "cfd_block_search": (C.c_int, [vp, C.c_longlong, dp, ip, ip, dp]),
+        "cfd_block_search_ex": (C.c_int, [vp, C.c_longlong, dp, ip, dp, C.c_char_p, ip, ip, dp, ip]),
         "cfd_block_node_to_cell": (C.c_int, [vp, vp, C.c_int, vp, vp]),
         "cfd_interp_create": (C.c_int, [vp, C.c_longlong, dp, ip, C.POINTER(vp)]),
         "cfd_interp_create_list": (C.c_int, [C.c_longlong, ip, ip, ip, dp, vp, C.POINTER(vp)]),
@@ -426,6 +427,24 @@ class Block:
         w = np.zeros(4 * n)
         check(lib().cfd_block_search(self.h, n, _dptr(p), _iptr(d), _iptr(nodes), _dptr(w)))
         return d, nodes.reshape(n, 4), w.reshape(n, 4)
+
+    def search_ex(self, xy: np.ndarray, tags=None, res=None, unaccept=None):
+        """MeshBlock::search with per-point mesh tags and resolutions and per-cell refusals:
+        (donor_cell[n], donor_nodes[n, 4], weights[n, 4], xtag[n], merged resolutions[n] or None)."""
+        p = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
+        n = p.size // 2
+        d = np.empty(n, np.int32)
+        nodes = np.empty(4 * n, np.int32)
+        w = np.empty(4 * n)
+        xt = np.empty(n, np.int32)
+        tg = None if tags is None else np.ascontiguousarray(tags, np.int32)
+        rs = None if res is None else np.array(res, np.float64)
+        ua = None if unaccept is None else np.ascontiguousarray(unaccept, np.uint8)
+        check(lib().cfd_block_search_ex(self.h, n, _dptr(p), _iptr(tg) if tg is not None else None,
+                                        _dptr(rs) if rs is not None else None,
+                                        ua.ctypes.data_as(C.c_char_p) if ua is not None else None, _iptr(d),
+                                        _iptr(nodes), _dptr(w), _iptr(xt)))
+        return d, nodes.reshape(n, 4), w.reshape(n, 4), xt, rs
 
     def cell_iblank(self, node_iblank: np.ndarray) -> np.ndarray:
         """getCellIblanks: 0 if any node is a hole, -1 if all nodes are receptors, else 1."""

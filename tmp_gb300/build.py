@@ -38,6 +38,7 @@ UNITS = [
     ("k_sst.cu", ["-fmad=false"]),
     ("k_noalloc.cu", []),
     ("k_fringe.cu", ["-fmad=false"]),
+    ("adt.cpp", []),
 ]
 
 

@@ -8,18 +8,23 @@
 // the reference's compiled code, so the weights are bit-identical to
 // computeNodalWeight2D's.
 //
-// Donor search.  The reference builds an alternating digital tree over the
-// bounding boxes of the cells near the query points and walks it per point.
-// Here the donor block keeps a uniform grid of bins over its bounding box;
-// each cell is listed, in ascending cell order, in every bin its
-// TOL-widened bounding box touches (a radix sort of (bin, cell) keys makes the
-// lists).  A query thread walks the candidate list of its bin and takes the
-// first cell that passes the reference's two tests: the point lies in the
-// cell's box widened by TOL (recursiveADT.cpp:117-124) and every weight lies in
-// [-TOL, 1 + TOL] (checkContainment.cpp:41-46).  Where exactly one cell passes
-// both tests the donor is the reference's; where several do (a point on a
-// shared edge, within 1e-10) the lowest-numbered one is taken, whereas the
-// reference takes the first in its tree order.
+// Donor search.  The reference (MeshBlock::search, search.cpp:81-270) puts
+// the cells whose boxes cross the oriented box of the query points in an
+// alternating digital tree and walks it per point; the walk checks, in the
+// tree's preorder, every cell whose TOL-widened box holds the point
+// (recursiveADT.cpp:111-156) and stops at the first that contains it
+// (checkContainment.cpp:4-62: every weight in [-TOL, 1 + TOL]) unless that
+// cell may not donate (cellRes = BIGVALUE) and one of its weights vanishes;
+// without such a stop the last check of the walk decides.  So the donor is
+// fixed by each candidate cell's preorder number alone: the host builds the
+// tree's order (adt.cpp) and the device evaluates the choice per point.
+// The donor block keeps a uniform grid of bins over its bounding box; each
+// cell is listed in every bin its TOL-widened bounding box touches (a radix
+// sort of (bin, cell) keys makes the lists).  A query thread tests every cell
+// of its bin that is in the tree and keeps the contained, acceptable one of
+// lowest preorder number, else the outcome of the highest-numbered check.
+// Coincident query points (uniquenodes_octree) take the donor cell of the
+// first of them, with their own weights in it.
 #include <cuda_runtime.h>
 
 #include <cub/device/device_radix_sort.cuh>
@@ -32,9 +37,12 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "../../include/cfdgb.h"
+#include "adt.hpp"
 #include "mesh.hpp"
 
 namespace {
@@ -273,36 +281,77 @@ __global__ void k_bin_ptr(long long nbins, long long nent, const unsigned long l
     binptr[t] = (int)lo;
 }
 
+// Cells whose box in the frame of the query points' oriented box overlaps that
+// box: the cells the reference puts in its tree.
+__global__ void k_obb_cross(int ncell, const double* __restrict__ xy, const int4* __restrict__ cv, cfdgb::adt::Obb o,
+                            unsigned char* __restrict__ cross, int* __restrict__ rank0) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int4 v = cv[c];
+    const int nv = v.w < 0 ? 3 : 4;
+    const int id[4] = {v.x, v.y, v.z, v.w};
+    double x[8];
+    for (int m = 0; m < 4; m++)
+        if (m < nv) x[2 * m] = xy[2 * id[m]], x[2 * m + 1] = xy[2 * id[m] + 1];
+    const bool hit = cfdgb::adt::crosses(o, nv, x);
+    cross[c] = hit ? 1 : 0;
+    rank0[c] = hit ? 0 : -1;  // one rank for every tree cell until the tree's order is needed
+}
+
+__device__ __forceinline__ void cell_coords(const double* __restrict__ xy, int4 v, double x[8]) {
+    x[0] = xy[2 * v.x]; x[1] = xy[2 * v.x + 1];
+    x[2] = xy[2 * v.y]; x[3] = xy[2 * v.y + 1];
+    x[4] = xy[2 * v.z]; x[5] = xy[2 * v.z + 1];
+    if (v.w >= 0) {
+        x[6] = xy[2 * v.w]; x[7] = xy[2 * v.w + 1];
+    } else {
+        x[6] = x[4]; x[7] = x[5];
+    }
+}
+
+__device__ __forceinline__ void put_donor(long long i, int cell, int4 v, const double f[4], int* __restrict__ donor,
+                                          int* __restrict__ dnodes, double* __restrict__ w) {
+    donor[i] = cell;
+    if (dnodes) {
+        dnodes[4 * i] = cell >= 0 ? v.x : -1;
+        dnodes[4 * i + 1] = cell >= 0 ? v.y : -1;
+        dnodes[4 * i + 2] = cell >= 0 ? v.z : -1;
+        dnodes[4 * i + 3] = cell >= 0 ? v.w : -1;
+    }
+    if (w)
+        for (int m = 0; m < 4; m++) w[4 * i + m] = cell >= 0 ? f[m] : 0.0;
+}
+
+// rank[c]: the cell's preorder number in the search tree, -1 if not in it;
+// unacc[c] (may be null): the cell may not donate (cellRes = BIGVALUE).
 __global__ void k_donor_search(long long n, const double* __restrict__ pts, const double* __restrict__ xy,
                                const int4* __restrict__ cv, const float4* __restrict__ fbox,
                                const int* __restrict__ binptr, const int* __restrict__ cells, BinGrid g,
-                               int* __restrict__ donor, int* __restrict__ dnodes, double* __restrict__ w,
-                               int* err) {
+                               const int* __restrict__ rank, const unsigned char* __restrict__ unacc,
+                               int* __restrict__ donor, int* __restrict__ dnodes, double* __restrict__ w, int* err,
+                               int* ambiguous) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double px = pts[2 * i], py = pts[2 * i + 1];
     const float pxu = __double2float_ru(px), pxd = __double2float_rd(px);
     const float pyu = __double2float_ru(py), pyd = __double2float_rd(py);
     const int b = bin_coord(py, g.y0, g.inv_hy, g.nby) * g.nbx + bin_coord(px, g.x0, g.inv_hx, g.nbx);
-    int found = -1;
-    int4 fv = make_int4(-1, -1, -1, -1);
-    double fw[4] = {0.0, 0.0, 0.0, 0.0};
+    int good = -1, good_rank = INT_MAX;  // contained and acceptable, lowest preorder number
+    int last = -1, last_rank = -1;       // the highest-numbered check and its outcome
+    int ngood = 0, nrefused = 0;         // contained cells that stop the walk / that do not
+    int4 good_v = make_int4(-1, -1, -1, -1), last_v = good_v;
+    double good_w[4] = {0.0, 0.0, 0.0, 0.0}, last_w[4] = {0.0, 0.0, 0.0, 0.0};
     const int e1 = binptr[b + 1];
     for (int e = binptr[b]; e < e1; e++) {
         const int c = cells[e];
+        const int r = rank[c];
+        if (r < 0) continue;
         const float4 fb = fbox[c];
         if (pxu < fb.x || pyu < fb.y || pxd > fb.z || pyd > fb.w) continue;
         const int4 v = cv[c];
         const int nv = v.w < 0 ? 3 : 4;
         double x[8];
-        x[0] = xy[2 * v.x]; x[1] = xy[2 * v.x + 1];
-        x[2] = xy[2 * v.y]; x[3] = xy[2 * v.y + 1];
-        x[4] = xy[2 * v.z]; x[5] = xy[2 * v.z + 1];
-        if (nv == 4) {
-            x[6] = xy[2 * v.w]; x[7] = xy[2 * v.w + 1];
-        } else {
-            x[6] = x[4]; x[7] = x[5];
-        }
+        cell_coords(xy, v, x);
         double xmin = 1.0e15, ymin = 1.0e15, xmax = -1.0e15, ymax = -1.0e15;
         for (int m = 0; m < 4; m++) {
             if (m < nv) {
@@ -314,25 +363,51 @@ __global__ void k_donor_search(long long n, const double* __restrict__ pts, cons
         }
         if (!(px >= xmin - kTol && py >= ymin - kTol && px <= xmax + kTol && py <= ymax + kTol)) continue;
         double f[4];
-        if (!nodal_weights(nv, x, px, py, f)) {
-            atomicOr(err, 1);
-            continue;
+        bool in = nodal_weights(nv, x, px, py, f);
+        if (!in) atomicOr(err, 1);  // the reference throws here
+        in = in && inside_weights(nv, f);
+        bool refused = false;
+        if (in && unacc && unacc[c])
+            for (int m = 0; m < 4; m++) refused = refused || (m < nv && fabs(f[m]) < kTol);
+        ngood += in && !refused;
+        nrefused += in && refused;
+        if (in && !refused && r < good_rank) {
+            good = c, good_rank = r, good_v = v;
+            for (int m = 0; m < 4; m++) good_w[m] = f[m];
         }
-        if (!inside_weights(nv, f)) continue;
-        found = c;
-        fv = v;
-        for (int m = 0; m < 4; m++) fw[m] = f[m];
-        break;
+        if (r > last_rank) {
+            last_rank = r;
+            last = in ? c : -1;
+            last_v = v;
+            for (int m = 0; m < 4; m++) last_w[m] = f[m];
+        }
     }
-    donor[i] = found;
-    if (dnodes) {
-        dnodes[4 * i] = fv.x;
-        dnodes[4 * i + 1] = fv.y;
-        dnodes[4 * i + 2] = fv.z;
-        dnodes[4 * i + 3] = found >= 0 ? fv.w : -1;
+    if (good >= 0) put_donor(i, good, good_v, good_w, donor, dnodes, w);
+    else put_donor(i, last, last_v, last_w, donor, dnodes, w);
+    // the choice depends on the tree's order only where several cells stop the walk, or none does and a
+    // refused cell contains the point
+    if (ambiguous && (ngood > 1 || (ngood == 0 && nrefused > 0))) atomicOr(ambiguous, 1);
+}
+
+// A point whose search was merged into an earlier coincident one's takes that
+// point's donor cell (search.cpp:255-262) and its own weights in it.
+__global__ void k_take_coincident(long long n, const int* __restrict__ xtag, const double* __restrict__ pts,
+                                  const double* __restrict__ xy, const int4* __restrict__ cv, int* __restrict__ donor,
+                                  int* __restrict__ dnodes, double* __restrict__ w, int* err) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n || xtag[i] == i) return;
+    long long r = i;
+    while (xtag[r] != r) r = xtag[r];  // xtag[r] < r: ends at the first point of the group
+    const int c = donor[r];
+    double f[4] = {0.0, 0.0, 0.0, 0.0};
+    int4 v = make_int4(-1, -1, -1, -1);
+    if (c >= 0) {
+        v = cv[c];
+        double x[8];
+        cell_coords(xy, v, x);
+        if (!nodal_weights(v.w < 0 ? 3 : 4, x, pts[2 * i], pts[2 * i + 1], f)) atomicOr(err, 1);
     }
-    if (w)
-        for (int m = 0; m < 4; m++) w[4 * i + m] = fw[m];
+    put_donor(i, c, v, f, donor, dnodes, w);
 }
 
 // ---------------------------------------------------------------------------
@@ -661,6 +736,11 @@ struct cfd_block_s {
     int nwall = 0;
     int* wall_nodes = nullptr;           // ends of the wall faces, ascending
     unsigned char* wall_flag = nullptr;  // per node: 1 on a wall face
+    // host copies for the search tree: nodes, cells, and MeshBlock's cell
+    // numbering (triangles first, then quadrilaterals, each in mesh order)
+    std::vector<double> hxy;
+    std::vector<int4> hcv;
+    std::vector<int> order;
     ~cfd_block_s() {
         dfree(wall_nodes);
         dfree(wall_flag);
@@ -710,16 +790,97 @@ void read_err(int* d_err, cudaStream_t s, int* h) {
     ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
 }
 
-// Search points (device) in block b; outputs are device arrays.
-void search_device(cfd_block_t b, long long n, const double* d_pts, int* d_donor, int* d_nodes, double* d_w) {
+template <class T>
+struct DevBuf {  // a device temporary freed on scope exit
+    T* p = nullptr;
+    explicit DevBuf(size_t n) { dalloc(&p, n); }
+    ~DevBuf() { dfree(p); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+};
+
+// What MeshBlock::search is given besides the points: per point a mesh tag
+// and a resolution (merged in place over coincident points), per donor cell
+// whether it may donate.  Null tags / res: one tag and unit resolutions, as a
+// lone search of one point set.
+struct SearchQuery {
+    const double* h_pts = nullptr;           // host copy of the points
+    const int* tags = nullptr;
+    double* res = nullptr;                   // in / out
+    const unsigned char* d_unacc = nullptr;  // device, per cell (null: every cell may donate)
+    int* xtag = nullptr;                     // out (may be null): the point whose search each took
+};
+
+// Search n points (device d_pts, host copy in q) in block b, as
+// MeshBlock::search does; outputs are device arrays (d_nodes, d_w may be null).
+void search_device(cfd_block_t b, long long n, const double* d_pts, const SearchQuery& q, int* d_donor, int* d_nodes,
+                   double* d_w) {
     if (n == 0) return;
-    ck(cudaMemsetAsync(b->err, 0, sizeof(int), b->stream), "cudaMemsetAsync");
-    k_donor_search<<<blocks_for(n, 128), 128, 0, b->stream>>>(n, d_pts, b->xy, b->cv, b->fbox, b->binptr, b->cells,
-                                                               b->grid, d_donor, d_nodes, d_w, b->err);
+    if (n > INT_MAX) throw OversetError(CFD_ERR_ARG, "donor search: more than 2^31-1 points");
+    cudaStream_t s = b->stream;
+    // the coincident-point hash runs on a host thread while the tree is built
+    std::vector<int> xtag(n), ones;
+    std::vector<double> unit;
+    const int* tags = q.tags;
+    double* res = q.res;
+    if (!tags) {
+        ones.assign(n, 1);
+        tags = ones.data();
+    }
+    if (!res) {
+        unit.assign(n, 1.0);
+        res = unit.data();
+    }
+    struct Joiner {
+        std::thread t;
+        ~Joiner() {
+            if (t.joinable()) t.join();
+        }
+    } hash;
+    hash.t = std::thread([&] { cfdgb::adt::coincident(n, q.h_pts, tags, res, xtag.data()); });
+    const cfdgb::adt::Obb o = cfdgb::adt::find_obb(q.h_pts, n);
+    DevBuf<unsigned char> d_cross(b->ncell);
+    DevBuf<int> d_rank(b->ncell), d_err(2);  // d_err[1]: some point's donor depends on the tree's order
+    k_obb_cross<<<blocks_for(b->ncell, 256), 256, 0, s>>>(b->ncell, b->xy, b->cv, o, d_cross.p, d_rank.p);
+    ck(cudaGetLastError(), "k_obb_cross");
+    ck(cudaMemsetAsync(d_err.p, 0, 2 * sizeof(int), s), "cudaMemsetAsync");
+    // first pass with one rank for all tree cells: exact wherever at most one cell stops the walk
+    k_donor_search<<<blocks_for(n, 128), 128, 0, s>>>(n, d_pts, b->xy, b->cv, b->fbox, b->binptr, b->cells, b->grid,
+                                                       d_rank.p, q.d_unacc, d_donor, d_nodes, d_w, d_err.p,
+                                                       d_err.p + 1);
     ck(cudaGetLastError(), "k_donor_search");
+    int amb = 0;
+    ck(cudaMemcpyAsync(&amb, d_err.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    ck(cudaStreamSynchronize(s), "sync");
+    if (amb) {
+        // the tree's preorder numbers, then the search again with them
+        std::vector<unsigned char> cross(b->ncell);
+        ck(cudaMemcpyAsync(cross.data(), d_cross.p, b->ncell, cudaMemcpyDeviceToHost, s), "copy");
+        ck(cudaStreamSynchronize(s), "sync");
+        static_assert(sizeof(int4) == 4 * sizeof(int), "int4 holds four ints");
+        const std::vector<int> rank = cfdgb::adt::tree_ranks(
+            b->ncell, b->hxy.data(), reinterpret_cast<const int*>(b->hcv.data()), b->order.data(), cross.data());
+        ck(cudaMemcpyAsync(d_rank.p, rank.data(), b->ncell * sizeof(int), cudaMemcpyHostToDevice, s), "copy");
+        k_donor_search<<<blocks_for(n, 128), 128, 0, s>>>(n, d_pts, b->xy, b->cv, b->fbox, b->binptr, b->cells,
+                                                           b->grid, d_rank.p, q.d_unacc, d_donor, d_nodes, d_w,
+                                                           d_err.p, nullptr);
+        ck(cudaGetLastError(), "k_donor_search");
+    }
+    hash.t.join();
+    bool merged = false;
+    for (long long i = 0; i < n && !merged; i++) merged = xtag[i] != i;
+    if (merged) {
+        DevBuf<int> d_xtag(n);
+        ck(cudaMemcpyAsync(d_xtag.p, xtag.data(), n * sizeof(int), cudaMemcpyHostToDevice, s), "copy");
+        k_take_coincident<<<blocks_for(n, 128), 128, 0, s>>>(n, d_xtag.p, d_pts, b->xy, b->cv, d_donor, d_nodes, d_w,
+                                                              d_err.p);
+        ck(cudaGetLastError(), "k_take_coincident");
+        ck(cudaStreamSynchronize(s), "sync");
+    }
     int h = 0;
-    read_err(b->err, b->stream, &h);
+    read_err(d_err.p, s, &h);
     if (h & 1) throw OversetError(CFD_ERR_MESH, "donor search: a triangle's weight system is singular (matrix degenerate)");
+    if (q.xtag) std::copy(xtag.begin(), xtag.end(), q.xtag);
 }
 
 // Keep the last entry per receiving node (updateSolnData writes in list order,
@@ -832,6 +993,12 @@ int cfd_block_create(cfd_mesh_t mesh, void* stream, cfd_block_t* out) {
                 throw OversetError(CFD_ERR_MESH, "cfd_block_create: only triangles and quadrilaterals");
             hcv[c] = make_int4(v[0], v[1], v[2], m.cell_nvert[c] == 4 ? v[3] : -1);
         }
+        b->hxy = m.xy;
+        b->hcv = hcv;
+        b->order.reserve(m.ncell);
+        for (int pass = 0; pass < 2; pass++)
+            for (int c = 0; c < m.ncell; c++)
+                if ((hcv[c].w < 0) == (pass == 0)) b->order.push_back(c);
         // Bins: a uniform grid over the nodes' box with about four bins per cell.
         double x0 = 1e300, y0 = 1e300, x1 = -1e300, y1 = -1e300;
         for (int i = 0; i < m.nnode; i++) {
@@ -925,13 +1092,15 @@ int cfd_block_create(cfd_mesh_t mesh, void* stream, cfd_block_t* out) {
 
 void cfd_block_free(cfd_block_t b) { delete b; }
 
-int cfd_block_search(cfd_block_t b, long long npts, const double* xy, int* donor_cell, int* donor_nodes,
-                     double* weights) {
+int cfd_block_search_ex(cfd_block_t b, long long npts, const double* xy, const int* tags, double* res,
+                        const unsigned char* cell_unaccept, int* donor_cell, int* donor_nodes, double* weights,
+                        int* xtag) {
     if (!b || npts < 0 || (npts > 0 && (!xy || !donor_cell)))
         return cfdgb::set_last_error(CFD_ERR_ARG, "cfd_block_search: bad argument");
     if (npts == 0) return CFD_OK;
     double *d_pts = nullptr, *d_w = nullptr;
     int *d_donor = nullptr, *d_nodes = nullptr;
+    unsigned char* d_unacc = nullptr;
     int rc = CFD_OK;
     try {
         cudaStream_t s = b->stream;
@@ -939,8 +1108,18 @@ int cfd_block_search(cfd_block_t b, long long npts, const double* xy, int* donor
         dalloc(&d_donor, npts);
         if (donor_nodes) dalloc(&d_nodes, 4 * npts);
         if (weights) dalloc(&d_w, 4 * npts);
+        if (cell_unaccept) {
+            dalloc(&d_unacc, b->ncell);
+            ck(cudaMemcpyAsync(d_unacc, cell_unaccept, b->ncell, cudaMemcpyHostToDevice, s), "copy");
+        }
         ck(cudaMemcpyAsync(d_pts, xy, 2 * npts * sizeof(double), cudaMemcpyHostToDevice, s), "copy");
-        search_device(b, npts, d_pts, d_donor, d_nodes, d_w);
+        SearchQuery q;
+        q.h_pts = xy;
+        q.tags = tags;
+        q.res = res;
+        q.d_unacc = d_unacc;
+        q.xtag = xtag;
+        search_device(b, npts, d_pts, q, d_donor, d_nodes, d_w);
         ck(cudaMemcpyAsync(donor_cell, d_donor, npts * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
         if (donor_nodes)
             ck(cudaMemcpyAsync(donor_nodes, d_nodes, 4 * npts * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
@@ -948,12 +1127,22 @@ int cfd_block_search(cfd_block_t b, long long npts, const double* xy, int* donor
         ck(cudaStreamSynchronize(s), "sync");
     } catch (const OversetError& e) {
         rc = report(e);
+    } catch (const std::bad_alloc&) {
+        rc = cfdgb::set_last_error(CFD_ERR_CUDA, "cfd_block_search: host allocation failed");
+    } catch (const std::system_error&) {
+        rc = cfdgb::set_last_error(CFD_ERR_CUDA, "cfd_block_search: could not start a host thread");
     }
     dfree(d_pts);
     dfree(d_donor);
     dfree(d_nodes);
     dfree(d_w);
+    dfree(d_unacc);
     return rc;
+}
+
+int cfd_block_search(cfd_block_t b, long long npts, const double* xy, int* donor_cell, int* donor_nodes,
+                     double* weights) {
+    return cfd_block_search_ex(b, npts, xy, nullptr, nullptr, nullptr, donor_cell, donor_nodes, weights, nullptr);
 }
 
 int cfd_block_node_to_cell(cfd_block_t b, const double* d_q_node, int nvar, double* d_q_cell, void* stream) {
@@ -987,7 +1176,9 @@ int cfd_interp_create(cfd_block_t donor, long long n, const double* xy, const in
             dalloc(&d_nodes, 4 * n);
             dalloc(&d_w, 4 * n);
             ck(cudaMemcpyAsync(d_pts, xy, 2 * n * sizeof(double), cudaMemcpyHostToDevice, s), "copy");
-            search_device(donor, n, d_pts, d_donor, d_nodes, d_w);
+            SearchQuery q;
+            q.h_pts = xy;
+            search_device(donor, n, d_pts, q, d_donor, d_nodes, d_w);
             ck(cudaMemcpyAsync(hd.data(), d_donor, n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
             ck(cudaMemcpyAsync(hn.data(), d_nodes, 4 * n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
             ck(cudaMemcpyAsync(hw.data(), d_w, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
@@ -1058,6 +1249,9 @@ int cfd_interp_create_list(long long n, const int* recv_node, const int* nweight
     } catch (const OversetError& e) {
         delete it;
         return report(e);
+    } catch (const std::exception& e) {  // host allocation or thread start
+        delete it;
+        return cfdgb::set_last_error(CFD_ERR_CUDA, std::string("cfd_interp_create: ") + e.what());
     }
     *out = it;
     return CFD_OK;
@@ -1295,6 +1489,7 @@ struct ConnDonor {
     int d;          // donor block
     int cell;       // donor cell
     double res;     // donor cellRes
+    double rres;    // receptor resolution from the search (merged over coincident nodes)
 };
 }  // namespace
 
@@ -1320,8 +1515,10 @@ int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holema
     // donor[d][r]: donor cell in block d of every node of block r (-1: none), with its weights
     std::vector<std::vector<std::vector<int>>> dcell(nb, std::vector<std::vector<int>>(nb));
     std::vector<std::vector<std::vector<double>>> dw(nb, std::vector<std::vector<double>>(nb));
+    // rres[d][r][v]: the receptor resolution block d's search returns for node v of block r
+    std::vector<std::vector<std::vector<double>>> rres(nb, std::vector<std::vector<double>>(nb));
     std::vector<std::vector<std::vector<int>>> inside(nb, std::vector<std::vector<int>>(nb));
-    double *d_vol = nullptr, *d_w = nullptr;
+    double* d_vol = nullptr;
     int *d_donor = nullptr, *d_in = nullptr;
     int rc = CFD_OK;
     cfd_connect_s* res = new cfd_connect_s;
@@ -1331,7 +1528,6 @@ int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holema
         dalloc(&d_vol, nmax);
         dalloc(&d_donor, nmax);
         dalloc(&d_in, nmax);
-        dalloc(&d_w, 4 * nmax);
         for (int b = 0; b < nb; b++) {
             cfd_block_s* B = blocks[b];
             cudaStream_t s = B->stream;
@@ -1348,30 +1544,6 @@ int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holema
                 for (int c = 0; c < B->ncell; c++)
                     if ((hcv[b][c].w < 0) == (pass == 0)) tm[b].push_back(c);
         }
-        // searches and hole-map tests, all on the device
-        for (int d = 0; d < nb; d++)
-            for (int r = 0; r < nb; r++) {
-                if (r == d) continue;
-                const int n = blocks[r]->nnode;
-                ck(cudaStreamSynchronize(blocks[r]->stream), "sync");
-                search_device(blocks[d], n, blocks[r]->xy, d_donor, nullptr, d_w);
-                dcell[d][r].resize(n);
-                dw[d][r].resize(4 * (size_t)n);
-                ck(cudaMemcpyAsync(dcell[d][r].data(), d_donor, n * sizeof(int), cudaMemcpyDeviceToHost,
-                                   blocks[d]->stream), "copy");
-                ck(cudaMemcpyAsync(dw[d][r].data(), d_w, 4 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
-                                   blocks[d]->stream), "copy");
-                ck(cudaStreamSynchronize(blocks[d]->stream), "sync");
-                if (maps[d]) {
-                    k_hole_check<<<blocks_for(n, 256), 256, 0, maps[d]->stream>>>(n, blocks[r]->xy, maps[d]->g,
-                                                                                  maps[d]->sam, d_in);
-                    ck(cudaGetLastError(), "k_hole_check");
-                    inside[d][r].resize(n);
-                    ck(cudaMemcpyAsync(inside[d][r].data(), d_in, n * sizeof(int), cudaMemcpyDeviceToHost,
-                                       maps[d]->stream), "copy");
-                    ck(cudaStreamSynchronize(maps[d]->stream), "sync");
-                }
-            }
         // ---- profile: resolutions, mandatory overset-boundary receptors, mexclude
         auto verts = [&](int b, int c, int* v) {
             const int4 q = hcv[b][c];
@@ -1415,6 +1587,70 @@ int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holema
                 iex = iex1;
             }
         }
+        // searches and hole-map tests, all on the device: block d is searched
+        // once for the nodes of every other block, in block order, each node
+        // tagged with its block and carrying its resolution (exchangeSearchData)
+        for (int d = 0; d < nb; d++) {
+            long long ntot = 0;
+            for (int r = 0; r < nb; r++)
+                if (r != d) ntot += blocks[r]->nnode;
+            std::vector<double> pts;
+            std::vector<int> tags, xtag(ntot);
+            std::vector<double> rsearch;
+            pts.reserve(2 * ntot);
+            tags.reserve(ntot);
+            rsearch.reserve(ntot);
+            DevBuf<double> d_pts(2 * ntot), d_wd(4 * ntot);
+            DevBuf<int> d_dn(ntot);
+            DevBuf<unsigned char> d_unacc(blocks[d]->ncell);
+            long long off = 0;
+            for (int r = 0; r < nb; r++) {
+                if (r == d) continue;
+                const int n = blocks[r]->nnode;
+                ck(cudaStreamSynchronize(blocks[r]->stream), "sync");
+                ck(cudaMemcpyAsync(d_pts.p + 2 * off, blocks[r]->xy, 2 * (size_t)n * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, blocks[d]->stream), "copy");
+                pts.insert(pts.end(), hxy[r].begin(), hxy[r].end());
+                tags.insert(tags.end(), n, r + 1);
+                rsearch.insert(rsearch.end(), nodeRes[r].begin(), nodeRes[r].end());
+                off += n;
+            }
+            std::vector<unsigned char> unacc(blocks[d]->ncell);
+            for (int c = 0; c < blocks[d]->ncell; c++) unacc[c] = cellRes[d][c] == kBig;
+            ck(cudaMemcpyAsync(d_unacc.p, unacc.data(), unacc.size(), cudaMemcpyHostToDevice, blocks[d]->stream), "copy");
+            SearchQuery q;
+            q.h_pts = pts.data();
+            q.tags = tags.data();
+            q.res = rsearch.data();
+            q.d_unacc = d_unacc.p;
+            q.xtag = xtag.data();
+            search_device(blocks[d], ntot, d_pts.p, q, d_dn.p, nullptr, d_wd.p);
+            std::vector<int> dn(ntot);
+            std::vector<double> wd(4 * ntot);
+            ck(cudaMemcpyAsync(dn.data(), d_dn.p, ntot * sizeof(int), cudaMemcpyDeviceToHost, blocks[d]->stream), "copy");
+            ck(cudaMemcpyAsync(wd.data(), d_wd.p, 4 * ntot * sizeof(double), cudaMemcpyDeviceToHost, blocks[d]->stream),
+               "copy");
+            ck(cudaStreamSynchronize(blocks[d]->stream), "sync");
+            off = 0;
+            for (int r = 0; r < nb; r++) {
+                if (r == d) continue;
+                const int n = blocks[r]->nnode;
+                dcell[d][r].assign(dn.begin() + off, dn.begin() + off + n);
+                dw[d][r].assign(wd.begin() + 4 * off, wd.begin() + 4 * (off + n));
+                rres[d][r].resize(n);
+                for (int v = 0; v < n; v++) rres[d][r][v] = rsearch[xtag[off + v]];  // res_search[xtag[i]]
+                off += n;
+                if (maps[d]) {
+                    k_hole_check<<<blocks_for(n, 256), 256, 0, maps[d]->stream>>>(n, blocks[r]->xy, maps[d]->g,
+                                                                                  maps[d]->sam, d_in);
+                    ck(cudaGetLastError(), "k_hole_check");
+                    inside[d][r].resize(n);
+                    ck(cudaMemcpyAsync(inside[d][r].data(), d_in, n * sizeof(int), cudaMemcpyDeviceToHost,
+                                       maps[d]->stream), "copy");
+                    ck(cudaStreamSynchronize(maps[d]->stream), "sync");
+                }
+            }
+        }
         // ---- donor lists (ascending donor resolution, ties in block order)
         std::vector<std::vector<std::vector<ConnDonor>>> dl(nb);
         for (int r = 0; r < nb; r++) dl[r].resize(blocks[r]->nnode);
@@ -1425,7 +1661,7 @@ int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holema
                     const int c = dcell[d][r][v];
                     if (c < 0) continue;
                     auto& L = dl[r][v];
-                    ConnDonor e{d, c, cellRes[d][c]};
+                    ConnDonor e{d, c, cellRes[d][c], rres[d][r][v]};
                     size_t at = 0;
                     while (at < L.size() && !(std::fabs(L[at].res) > e.res)) at++;
                     L.insert(L.begin() + at, e);
@@ -1445,7 +1681,11 @@ int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holema
             ibl[r].assign(nn, 1);
             for (int i = 0; i < nn; i++) {
                 unsigned long long has = 0;  // blocks that gave node i a donor
-                for (const auto& e : dl[r][i]) has |= 1ull << e.d;
+                for (const auto& e : dl[r][i]) {
+                    has |= 1ull << e.d;
+                    // a coincident node of the same block may have brought a larger resolution
+                    nodeRes[r][i] = nodeRes[r][i] > e.rres ? nodeRes[r][i] : e.rres;
+                }
                 for (int j = 0; j < nb; j++) {
                     if (j == r || !maps[j] || ((has >> j) & 1)) continue;
                     if (inside[j][r][i]) {
@@ -1598,9 +1838,10 @@ int cfd_overset_connect(int nblocks, const cfd_block_t* blocks, const cfd_holema
         rc = report(e);
     } catch (const std::bad_alloc&) {
         rc = cfdgb::set_last_error(CFD_ERR_CUDA, "cfd_overset_connect: host allocation failed");
+    } catch (const std::system_error&) {
+        rc = cfdgb::set_last_error(CFD_ERR_CUDA, "cfd_overset_connect: could not start a host thread");
     }
     dfree(d_vol);
-    dfree(d_w);
     dfree(d_donor);
     dfree(d_in);
     if (rc != CFD_OK) {
@@ -1664,7 +1905,9 @@ int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, c
         for (int j = 0; j < nother; j++) {
             if (!maps[j]) continue;
             ck(cudaStreamSynchronize(s), "sync");
-            search_device(others[j], n, self->xy, d_donor, nullptr, nullptr);  // on the other block's stream
+            SearchQuery q;
+            q.h_pts = self->hxy.data();
+            search_device(others[j], n, self->xy, q, d_donor, nullptr, nullptr);  // on the other block's stream
             ck(cudaStreamSynchronize(others[j]->stream), "sync");
             k_blank_nodes<<<blocks_for(n, 256), 256, 0, s>>>(n, self->xy, d_donor, maps[j]->g, maps[j]->sam, d_ib);
             ck(cudaGetLastError(), "k_blank_nodes");
@@ -1687,6 +1930,8 @@ int cfd_overset_blank(cfd_block_t self, int nother, const cfd_block_t* others, c
         ck(cudaStreamSynchronize(s), "sync");
     } catch (const OversetError& e) {
         rc = report(e);
+    } catch (const std::exception& e) {  // host allocation or thread start
+        rc = cfdgb::set_last_error(CFD_ERR_CUDA, std::string("cfd_overset_blank: ") + e.what());
     }
     dfree(d_ib);
     dfree(d_donor);
