@@ -158,7 +158,13 @@ typedef struct {
                           SST turbulence sweeps): threads per block, 64, 128 or
                           256 (0 = 256); fewer warps per block put fewer cells
                           on one SM sub-partition's pipes at a time            */
-    int reserved[4];
+    int sst_sequential; /* CFD_FLOW_SST with the round-robin schedule (mode 0):
+                           0 = the turbulence sweep of each direction runs in
+                           the flow's sweep launch, on its own blocks, taking
+                           each slot's updated face velocity from the flow's
+                           sweep as it is formed; 1 = the turbulence sweeps run
+                           after the flow's.  Both give the same bits        */
+    int reserved[3];
 } cfd_params_t;
 
 /* ---- errors -------------------------------------------------------------- */
@@ -256,7 +262,9 @@ long long cfd_launch_count(cfd_case_t c);
  * (all levels), 5 backward sweep (all levels), 6 LU-SGS update, 7 whole step;
  * coupled SST cases: 8 the model's residual passes, 9 the turbulence sweeps
  * (constants, forward, backward), 10 the k, omega, mu_t update; connected
- * overset cases: 11 the fringe exchange. */
+ * overset cases: 11 the fringe exchange; SST cases that overlap their sweeps
+ * (cfd_params_t.sst_sequential 0, sweep mode 0): 12 both directions' flow and
+ * turbulence sweeps with their per-step constants, as a step runs them. */
 int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms);
 /* Autotuner of the dataflow sweeps' launch shape (no reference counterpart):
  * times `reps` whole LU-SGS steps for each co-resident block count per SM

@@ -6,7 +6,11 @@ SST functions are pinned bit for bit to the reference's own by
 tests/test_oracle_sst.py) and the device must follow it: mu + mu_t in the
 viscous flux and spectral radii, dt = CFL vol / (spec_c + 4 spec_v), the model's
 residual sum(Fc - Fv) - Q vol, the turbulence sweeps after the flow's, k and
-omega floored at 1e-4 of the freestream.  Tolerance: 1e-10 relative on the
+omega floored at 1e-4 of the freestream.  By default the turbulence sweep of
+each direction runs in the flow's sweep launch (its own blocks, each slot's
+updated face velocity taken from the flow's blocks as it is formed); the
+sequential form (turbulence sweeps after the flow's) must give the same bits
+in every form.  Tolerance: 1e-10 relative on the
 fields after the steps (pow() in the far-field state and Sutherland's law and
 tanh in F1 / F2 may differ in the last bit between CUDA and glibc).
 """
@@ -28,7 +32,7 @@ def rel(a, b) -> float:
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
-def setup(mesh_file, ma, aoa, re, cfl, tu, ratio, precision, seed):
+def setup(mesh_file, ma, aoa, re, cfl, tu, ratio, precision, seed, sequential=False):
     import oracle
     from oracle import grd
     from tmp_gb300 import abi, meshgen
@@ -46,7 +50,7 @@ def setup(mesh_file, ma, aoa, re, cfl, tu, ratio, precision, seed):
     o.sst_cons()
     mesh = abi.Mesh.load_grd(GOLDEN / mesh_file, -1, -2)
     case = abi.Case([mesh], [dict(mach=ma, aoa_deg=aoa, reynolds=re)], abi.FLOW_SST, abi.ADV_LUSGS, precision,
-                    cfl=cfl)
+                    cfl=cfl, sst_sequential=sequential)
     abi.sst_set_inflow(case, tu, ratio)
     case.init_freestream()
     assert np.array_equal(abi.sst_freestream(case), np.array([inf[0], inf[1], o.sst_field("SST_MUT")[0]]))
@@ -109,6 +113,64 @@ def test_coupled_sst_fast_forms_follow_plain(built_lib, form):
     assert rel(case.get("SST_T"), o.sst_field("SST_T")) <= 1e-2
     assert np.isfinite(case.norm("L2_R_RHO"))
     case.close()
+
+
+@pytest.mark.parametrize("form", ["FP64", "MIXED", "MIXFF"])
+@pytest.mark.parametrize("mesh_file", ["mixed.grd", "omesh.grd"])
+def test_overlapped_sweeps_equal_sequential(built_lib, form, mesh_file):
+    """The flow's and the turbulence sweeps in one launch per direction give the bits of the turbulence sweeps
+    run after the flow's, step after step (direct and graph-replayed)."""
+    from tmp_gb300 import abi
+
+    prec = {"FP64": abi.PREC_FP64, "MIXED": abi.PREC_MIXED, "MIXFF": abi.PREC_MIXFF}[form]
+    _, a = setup(mesh_file, 0.3, 2.0, 1e5, 5.0, 0.01, 0.035, prec, 9)
+    _, b = setup(mesh_file, 0.3, 2.0, 1e5, 5.0, 0.01, 0.035, prec, 9, sequential=True)
+    for k in range(3):
+        a.step(1)
+        b.step(1)
+        for name in ("U", "SST_T", "SST_MUT"):
+            assert np.array_equal(a.get(name), b.get(name)), (k, name)
+    a.step_graph(40)
+    b.step_graph(40)
+    a.sync()
+    b.sync()
+    for name in ("U", "SST_T", "SST_MUT"):
+        assert np.array_equal(a.get(name), b.get(name)), name
+    assert np.isfinite(a.norm("L2_R_RHO"))
+    a.close()
+    b.close()
+
+
+def test_overlapped_sweeps_larger_mesh(built_lib):
+    """A 49k-cell SST airfoil mesh (hundreds of levels, every block busy): overlapped == sequential, bit for bit."""
+    import tempfile
+    from pathlib import Path
+
+    from tmp_gb300 import abi, meshgen
+
+    g = meshgen.mixed_mesh(meshgen.naca_body(128), nlayer=24, dr1=1e-4, growth=1.2, rfar=10.0, seed=31, density=1.0,
+                           grade=0.9)
+    with tempfile.TemporaryDirectory() as td:
+        path = Path(td) / "m.grd"
+        meshgen.write_grd(path, g)
+        mesh = abi.Mesh.load_grd(path, g.wall_tag, g.far_tag)
+    cases = []
+    for prec in (abi.PREC_FP64, abi.PREC_MIXFF):
+        pair = []
+        for seq in (False, True):
+            c = abi.Case([mesh], [dict(mach=0.2, aoa_deg=3.0, reynolds=3e6)], abi.FLOW_SST, abi.ADV_LUSGS, prec,
+                         cfl=10.0, sst_sequential=seq)
+            abi.sst_set_inflow(c, 0.001, 10.0)
+            c.init_freestream()
+            c.step_graph(30)
+            c.sync()
+            pair.append(c)
+        for name in ("U", "SST_T", "SST_MUT"):
+            assert np.array_equal(pair[0].get(name), pair[1].get(name)), (prec, name)
+        cases += pair
+    assert cases[0].ncell > 15000
+    for c in cases:
+        c.close()
 
 
 def test_coupled_sst_rejects_other_forms(built_lib):

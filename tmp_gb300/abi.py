@@ -52,7 +52,8 @@ class Freestream(C.Structure):
 class Params(C.Structure):
     _fields_ = [("flow", C.c_int), ("advance", C.c_int), ("precision", C.c_int), ("first_order", C.c_int),
                 ("cfl", C.c_double), ("sweep_mode", C.c_int), ("sweep_blocks_per_sm", C.c_int),
-                ("sweep_poll_ns", C.c_int), ("sweep_threads", C.c_int), ("reserved", C.c_int * 4)]
+                ("sweep_poll_ns", C.c_int), ("sweep_threads", C.c_int), ("sst_sequential", C.c_int),
+                ("reserved", C.c_int * 3)]
 
 
 _lib = None
@@ -239,14 +240,15 @@ class Case:
 
     def __init__(self, meshes: Sequence[Mesh], freestreams: Sequence[dict], flow: int, advance: int,
                  precision: int = PREC_FP64, cfl: float = 1.0, first_order: bool = False, stream: int | None = None,
-                 sweep_mode: int = 0, sweep_blocks_per_sm: int = 0, sweep_poll_ns: int = 0, sweep_threads: int = 0):
+                 sweep_mode: int = 0, sweep_blocks_per_sm: int = 0, sweep_poll_ns: int = 0, sweep_threads: int = 0,
+                 sst_sequential: bool = False):
         self.meshes = list(meshes)
         arr = (C.c_void_p * len(meshes))(*[m.h.value for m in meshes])
         fs = (Freestream * len(meshes))(*[Freestream(f["mach"], f.get("aoa_deg", 0.0), f.get("reynolds", 1.0),
                                                      f.get("density", 1.225), f.get("pressure", 101325.0))
                                           for f in freestreams])
         p = Params(flow, advance, precision, int(first_order), float(cfl), int(sweep_mode), int(sweep_blocks_per_sm),
-                   int(sweep_poll_ns), int(sweep_threads))
+                   int(sweep_poll_ns), int(sweep_threads), int(bool(sst_sequential)))
         h = C.c_void_p()
         check(lib().cfd_case_create(arr, len(meshes), fs, C.byref(p), C.c_void_p(stream) if stream else None,
                                     C.byref(h)))
@@ -358,7 +360,8 @@ class Case:
         return int(lib().cfd_launch_count(self.h))
 
     PASSES = dict(face_state=0, cell_grad=1, face_flux=2, cell_update=3, sweep_fwd=4, sweep_bwd=5,
-                  lusgs_update=6, step=7, sst_residual=8, sst_sweeps=9, sst_update=10, fringe=11)
+                  lusgs_update=6, step=7, sst_residual=8, sst_sweeps=9, sst_update=10, fringe=11,
+                  sweeps_overlapped=12)
 
     def bench_pass(self, name: str, reps: int, flush_bytes: int = 0) -> float:
         """Mean device time (ms) of one pass, CUDA events on the case's stream."""

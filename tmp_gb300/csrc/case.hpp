@@ -77,7 +77,12 @@ struct DevArrays {
     double* sstDinv = nullptr;   // [2*nc] 1 / diagonal (the binary32 sweep)
     float2* sstDW1f = nullptr;   // [nc] binary32 copies published by the binary32 sweep
     float2* sstDWf = nullptr;    // [nc]
+    float4* sstSlotf = nullptr;  // [4*nc] binary32 sweep: per (cell, slot) (fc_k, fc_omega, r_A, face length)
+    float* sstVnpf = nullptr;    // [4*nc] binary32 sweep: per (cell, slot) Vn(W_j + dW_j)
+    float2* sstWf = nullptr;     // [nc] binary32 copy of sstW for that sweep
     int sst_grid = 0;            // co-resident blocks of the turbulence sweeps
+    int cpl_grid = 0;            // co-resident blocks of the flow + turbulence sweep launch
+    int cpl_nflow = 0;           // of which the flow's sweep takes [0, cpl_nflow)
     float* omega = nullptr;      // [nc] relaxation of the last learned update
     float* omega_mean = nullptr; // [nmesh] its mean per mesh
     int* mlp_samples = nullptr;  // cells the network is evaluated on, mesh by mesh
@@ -231,6 +236,13 @@ void launch_sst_stage(const DevArrays& d, const LaunchCfg& L, int stage);
 // the turbulence LU-SGS sweeps of a coupled step (after the flow's sweeps):
 // per-slot constants, forward and backward dataflow sweeps, binary64 or binary32
 cudaError_t launch_sst_sweeps(const DevArrays& d, const LaunchCfg& L, bool fp32);
+// the same sweeps overlapped with the flow's round-robin sweeps: the per-slot
+// constants before the flow's sweeps (coupled: Vn(W_j + dW_j) left to the
+// flow's sweep), then one cooperative launch per direction holding both, the
+// flow on blocks [0, nflow)
+void launch_sst_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool fp32, bool coupled);
+cudaError_t launch_sweep_coupled(const DevArrays& d, const LaunchCfg& L, bool forward, bool fp32, int grid, int nflow);
+int sweep_coupled_max_grid(bool fp32, int blocks_per_sm, int threads, bool pf);
 // W_t += dW_t, k and omega from the updated rho (floored), mu_t (after the flow's update)
 void launch_sst_update(const DevArrays& d, const LaunchCfg& L);
 // W_t = rho (k, omega) from the current U and k, omega

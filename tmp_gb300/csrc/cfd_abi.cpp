@@ -138,6 +138,10 @@ struct cfd_case_s {
     bool fast_sweep() const { return p.precision != CFD_PREC_FP64 && p.advance == CFD_ADV_LUSGS; }
     // the binary32 sweep over a chain schedule: mode 5 (lists spread over blocks) or 6 (block-local lists)
     bool chain_sweep() const { return fast_sweep() && (p.sweep_mode == 5 || p.sweep_mode == 6); }
+    // turbulence sweeps in the flow's sweep launches: SST, LU-SGS, the round-robin schedule
+    bool sst_overlap() const {
+        return turb() && p.advance == CFD_ADV_LUSGS && p.sweep_mode == 0 && !p.sst_sequential && d.cpl_grid >= 2;
+    }
     LaunchCfg L() { return LaunchCfg{stream, &launches}; }
     void drop_graph() {
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -157,7 +161,13 @@ static void set_sweep_shape(cfd_case_s* c, int bpsm, int threads, int pf = -1) {
     if (pf >= 0) c->d.flow_pf = pf ? 1 : 0;
     c->d.flow_threads = threads;
     c->d.flow_grid = sweep_flow_max_grid(c->p.precision != CFD_PREC_FP64, bpsm, threads, c->d.flow_pf != 0);
-    if (c->turb()) c->d.sst_grid = sst_sweep_max_grid(bpsm > 0 ? bpsm : 2, threads, c->d.flow_pf != 0);
+    if (c->turb()) {
+        c->d.sst_grid = sst_sweep_max_grid(bpsm > 0 ? bpsm : 2, threads, c->d.flow_pf != 0);
+        // the flow's and the turbulence sweep's blocks share one co-resident grid, half each
+        c->d.cpl_grid = sweep_coupled_max_grid(c->p.precision != CFD_PREC_FP64, bpsm > 0 ? bpsm : 2, threads,
+                                               c->d.flow_pf != 0);
+        c->d.cpl_nflow = c->d.cpl_grid / 2;
+    }
 }
 static void sst_freestream(cfd_case_s* c);
 static void sst_init_state(cfd_case_s* c);
@@ -177,7 +187,7 @@ void free_case(cfd_case_s* c) {
                     d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_jenc[0], d.chain_jenc[1], d.chain_stage[0],
                     d.chain_stage[1], d.chain_posb, d.chain_dF, d.Uq, d.gradq, d.phiq, d.speccq, d.specvq, d.gradTq,
                     d.muq, d.Ueq, d.fspecq, d.mueq, d.Fcq, d.Fvq, d.fg0q, d.fg1q, d.fvisq, d.cgeoq, d.sstW, d.sstDW1,
-                    d.sstDW, d.sstFcs, d.sstRA, d.sstVnp, d.sstDinv, d.sstDW1f, d.sstDWf, d.iblank_cell,
+                    d.sstDW, d.sstFcs, d.sstRA, d.sstVnp, d.sstDinv, d.sstDW1f, d.sstDWf, d.sstSlotf, d.sstWf, d.sstVnpf, d.iblank_cell,
                     c->fringe.src_nodes, c->fringe.src_ptr, c->fringe.src_cells, c->fringe.recv_node, c->fringe.nw,
                     c->fringe.inode, c->fringe.w, c->fringe.recv_cells, c->fringe.qn, c->fringe.vals};
     for (void* q : ptrs)
@@ -469,6 +479,26 @@ void sweeps(cfd_case_s* c, bool forward) {
     }
 }
 
+// The flow's round-robin sweeps with the turbulence equations' sweeps in the
+// same launches (CFD_FLOW_SST): the per-step constants of both first, then per
+// direction one cooperative grid whose turbulence blocks take each slot's
+// Vn(W_j + dW_j) from the flow's blocks as it is formed.  The turbulence
+// sweep's arithmetic is unchanged, so the bits equal the sequential form's.
+void overlapped_sweeps(cfd_case_s* c) {
+    auto L = c->L();
+    const DevArrays& d = c->d;
+    const bool f32 = c->fast_sweep();
+    if (f32) {
+        launch_inv_diag(d, L);
+        launch_sweep_prep32(d, L, c->viscous(), c->mu_kind());
+    } else {
+        launch_sweep_prep(d, L, c->viscous(), c->fp32(), true);
+    }
+    launch_sst_sweep_prep(d, L, f32, true);
+    ck(launch_sweep_coupled(d, L, true, f32, d.cpl_grid, d.cpl_nflow), "cooperative flow + turbulence sweep launch");
+    ck(launch_sweep_coupled(d, L, false, f32, d.cpl_grid, d.cpl_nflow), "cooperative flow + turbulence sweep launch");
+}
+
 // LUSGSIntegrator::UpdateSerial (LUSGS_Integrator.cpp:228-240).  With a
 // learned network attached the final update is the fused learned one.
 void learned_update(cfd_case_s* c);
@@ -480,10 +510,14 @@ void lusgs_step(cfd_case_s* c) {
     residual_pass(c);
     update_pass(c, 2 /*UPD_LUSGS*/, c->p.cfl, 0, 0.0);
     if (c->turb()) launch_sst_stage(d, L, 3);  // the model's residual and diagonal (needs dt and the radii)
-    sweeps(c, true);
-    sweeps(c, false);
-    // the turbulence sweeps read the flow's W before the update and its increments of this step
-    if (c->turb()) ck(launch_sst_sweeps(d, L, c->fast_sweep()), "cooperative turbulence sweep launch");
+    if (c->sst_overlap()) {
+        overlapped_sweeps(c);
+    } else {
+        sweeps(c, true);
+        sweeps(c, false);
+        // the turbulence sweeps read the flow's W before the update and its increments of this step
+        if (c->turb()) ck(launch_sst_sweeps(d, L, c->fast_sweep()), "cooperative turbulence sweep launch");
+    }
     if (c->mlp) learned_update(c);
     else launch_lusgs_update(d, L, c->fp32());
     if (c->turb()) launch_sst_update(d, L);  // with rho after the flow's update
@@ -885,6 +919,7 @@ static void sst_alloc(cfd_case_s* c) {
         dalloc(&d.sstW, 2 * nc); dalloc(&d.sstDW1, 2 * nc); dalloc(&d.sstDW, 2 * nc);
         dalloc(&d.sstFcs, 8 * nc); dalloc(&d.sstRA, 4 * nc); dalloc(&d.sstVnp, 4 * nc);
         dalloc(&d.sstDinv, 2 * nc); dalloc(&d.sstDW1f, nc); dalloc(&d.sstDWf, nc);
+        dalloc(&d.sstSlotf, 4 * nc); dalloc(&d.sstWf, nc); dalloc(&d.sstVnpf, 4 * nc);
         ck(cudaMemsetAsync(d.sstDW, 0, 2 * nc * sizeof(double), c->stream), "memset");
         ck(cudaMemsetAsync(d.sstDW1, 0, 2 * nc * sizeof(double), c->stream), "memset");
     }
@@ -1432,7 +1467,8 @@ int cfd_selftest_bounded_wait(cfd_case_t c, long long polls) {
 
 int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, double* avg_ms) {
     if (!c || !avg_ms || reps <= 0) return fail(CFD_ERR_ARG, "null argument or reps <= 0");
-    if (pass < 0 || pass > 11) return fail(CFD_ERR_ARG, "unknown pass");
+    if (pass < 0 || pass > 12) return fail(CFD_ERR_ARG, "unknown pass");
+    if (pass == 12 && !c->sst_overlap()) return fail(CFD_ERR_STATE, "the case does not overlap its sweeps");
     if (pass >= 8 && pass <= 10 && !c->turb()) return fail(CFD_ERR_STATE, "not a coupled SST case");
     if (pass == 11 && !c->connected) return fail(CFD_ERR_STATE, "not a connected overset case");
     ABI_TRY
@@ -1469,6 +1505,7 @@ int cfd_bench_pass(cfd_case_t c, int pass, int reps, long long flush_bytes, doub
             case 9: ck(launch_sst_sweeps(d, L, c->fast_sweep()), "turbulence sweeps"); break;
             case 10: launch_sst_update(d, L); break;
             case 11: launch_fringe(d, c->fringe, L); break;
+            case 12: overlapped_sweeps(c); break;
         }
         ck(cudaEventRecord(e1, c->stream), "cudaEventRecord");
         ck(cudaEventSynchronize(e1), "cudaEventSynchronize");

@@ -15,6 +15,7 @@
 #include <type_traits>
 
 #include "case.hpp"
+#include "sweep_flow.cuh"
 
 namespace cfdgb {
 namespace {
@@ -254,8 +255,10 @@ __device__ __forceinline__ bool sent_tf(float x) { return __float_as_uint(x) == 
 // Per (cell i, face slot s): the increment-free terms of the turbulence SolveDF
 // - W_t,j Vn(W_j), r_A, and Vn(W_j + dW_j) with the flow increment of the
 // direction that uses this slot (forward if j < i, backward if j > i) - then
-// the "not yet computed" sentinels and 1/D_t.  After the flow's sweeps.
-__global__ void __launch_bounds__(256) k_sst_sweep_prep(DevArrays d) {
+// the "not yet computed" sentinels and 1/D_t.  After the flow's sweeps; or,
+// `coupled`, before them: Vn(W_j + dW_j) then comes from the flow's sweep of
+// the same launch (its sentinel is set here).
+__global__ void __launch_bounds__(256) k_sst_sweep_prep(DevArrays d, int coupled) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 4 * d.nc) return;
     const int i = t >> 2, s = t & 3;
@@ -278,10 +281,15 @@ __global__ void __launch_bounds__(256) k_sst_sweep_prep(DevArrays d) {
         if (j >= 0) {
             const d4 g = d.fg0[f];
             const d4 w0 = ld4(d.W + j);
-            const d4 dw = ld4((j < i ? d.dW1 : d.dW) + j);
-            const d4 wp = d4{w0.x + dw.x, w0.y + dw.y, w0.z + dw.z, w0.w + dw.w};
             const double vn0 = dot2(w0.z / w0.x, w0.w / w0.x, g.x, g.y);
-            vnp = dot2(wp.z / wp.x, wp.w / wp.x, g.x, g.y);
+            if (coupled) {
+                vnp = __longlong_as_double((long long)kSentT);
+            } else {
+                // as the flow's binary64 sweep forms Vn on this face
+                const d4 dw = ld4((j < i ? d.dW1 : d.dW) + j);
+                const d4 wp = d4{w0.x + dw.x, w0.y + dw.y, w0.z + dw.z, w0.w + dw.w};
+                vnp = dot2(wp.z / wp.x, wp.w / wp.x, g.x, g.y);
+            }
             fc0 = d.sstW[2 * j] * vn0;
             fc1 = d.sstW[2 * j + 1] * vn0;
             const d4 uj = ld4(d.U + j);
@@ -298,6 +306,62 @@ __global__ void __launch_bounds__(256) k_sst_sweep_prep(DevArrays d) {
     d.sstVnp[t] = vnp;
 }
 
+// The fast forms' prep: the same per-slot terms formed in binary32 from the
+// binary32 copies of the flow's state and increments (Wf, dW1f / dWf, as the
+// flow's binary32 sweep polls them), packed per slot for the binary32 sweep,
+// with a binary32 copy of W_t; the sentinels and 1/D as above.  Only the
+// sweep operator is rounded differently: the update and the residual that
+// fix the converged state stay as they are.
+__global__ void __launch_bounds__(256) k_sst_sweep_prep32(DevArrays d, int coupled) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * d.nc) return;
+    const int i = t >> 2, s = t & 3;
+    if (s < 2) {
+        d.sstDW1[2 * i + s] = __longlong_as_double((long long)kSentT);
+        d.sstDW[2 * i + s] = __longlong_as_double((long long)kSentT);
+        d.sstDinv[2 * i + s] = 1.0 / d.sstD[2 * i + s];
+    }
+    if (s == 0) {
+        const float sf = __uint_as_float(kSentTf);
+        d.sstDW1f[i] = make_float2(sf, sf);
+        d.sstDWf[i] = make_float2(sf, sf);
+        d.sstWf[i] = make_float2((float)d.sstW[2 * i], (float)d.sstW[2 * i + 1]);
+    }
+    const int code = (&d.cface[i].x)[s];
+    float fc0 = 0.f, fc1 = 0.f, rA = 0.f, vnp = 0.f, A = 0.f;
+    if (code != 0) {
+        const int f = code > 0 ? code - 1 : -code - 1;
+        const int2 e = d.lr[f];
+        const int j = code > 0 ? e.y : e.x;
+        if (j >= 0) {
+            const float4 g = d.fg0f[f];
+            const float4 w0 = d.Wf[j];
+            A = g.z;
+            const float u = w0.z / w0.x, v = w0.w / w0.x;
+            const float vn0 = u * g.x + v * g.y;
+            if (coupled) {
+                vnp = __uint_as_float(kSentTf);
+            } else {
+                // Vn(W_j + dW_j) as the flow's binary32 sweep forms it (base velocity plus the exact difference)
+                const float4 dw = (j < i ? d.dW1f : d.dWf)[j];
+                const float rp = 1.f / (w0.x + dw.x);
+                const float du = (dw.z - u * dw.x) * rp, dv = (dw.w - v * dw.x) * rp;
+                vnp = vn0 + (du * g.x + dv * g.y);
+            }
+            fc0 = (float)d.sstW[2 * j] * vn0;
+            fc1 = (float)d.sstW[2 * j + 1] * vn0;
+            const d4 ud = ld4(d.U + j);
+            const float rho = (float)ud.x, p = (float)ud.y;
+            const float vn = (float)ud.z * g.x + (float)ud.w * g.y;
+            rA = 1.5f * (fabsf(vn) + sqrtf(1.4f * p / rho));
+            rA += fmaxf(4.f / (3.f * rho), 1.4f / rho) * ((float)d.mu[i] / 0.72f + (float)d.sstMut[i] / 0.9f) /
+                  sqrtf(d.fvisf[f].z);
+        }
+    }
+    d.sstSlotf[t] = make_float4(fc0, fc1, rA, A);
+    d.sstVnpf[t] = vnp;
+}
+
 // One dataflow launch per direction: one warp per cell, taken in level order
 // (positions p = block + B*q, as the flow's dataflow sweep), lanes 2s+m for
 // face slot s and equation m.  A neighbour's increment is final once its
@@ -305,15 +369,18 @@ __global__ void __launch_bounds__(256) k_sst_sweep_prep(DevArrays d) {
 // T = double: the plain form (every operation in binary64, as the C
 // restatement); T = float: the slot terms in binary32 and the published copy
 // polled in binary32, the increment itself formed in binary64 from them.
-template <bool FWD, class T, bool PF>
-__global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __restrict__ order) {
+// CPL: the flow's sweep runs in the same grid and writes Vn(W_j + dW_j) per
+// slot as it goes; the slot's value is then awaited like an increment.  bid, B:
+// this block's number among the B blocks that run the turbulence sweep.
+template <bool FWD, class T, bool PF, bool CPL>
+__device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __restrict__ order, int bid, int B) {
     const int lane = threadIdx.x & 31;
     const int s = (lane >> 1) & 3, m = lane & 1;
     const int warp = threadIdx.x >> 5;
-    const int B = gridDim.x, NW = blockDim.x >> 5;
+    const int NW = blockDim.x >> 5;
     double* dst = FWD ? d.sstDW1 : d.sstDW;
     float2* dstf = FWD ? d.sstDW1f : d.sstDWf;
-    const int q0 = ((warp - (int)(blockIdx.x % NW)) % NW + NW) % NW;
+    const int q0 = ((warp - (int)(bid % NW)) % NW + NW) % NW;
     // PF: the inputs of a position that do not depend on a neighbour's
     // increment (its cell, face slot, neighbour and the per-slot constants) are
     // loaded one position ahead, while the warp waits for the current
@@ -326,6 +393,7 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
         bool use, left;
         T wt, fc, rA, vnp, A;
         double own, dd;
+        float ownf, ddf;
     };
     auto load = [&](long long p, In& x) {
         x.i = order[p];
@@ -348,17 +416,29 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
             x.own = FWD ? d.sstR[2 * x.i + m] : d.sstDW1[2 * x.i + m];
             x.dd = std::is_same<T, double>::value ? d.sstD[2 * x.i + m] : d.sstDinv[2 * x.i + m];
         }
+        x.ownf = (float)x.own;
+        x.ddf = (float)x.dd;
         x.wt = x.fc = x.rA = x.vnp = x.A = T(0);
         if (x.use) {
             const size_t t = (size_t)x.i * 4 + s;
-            x.wt = (T)d.sstW[2 * x.j + m];
-            x.fc = (T)d.sstFcs[2 * t + m];
-            x.rA = (T)d.sstRA[t];
-            x.vnp = (T)d.sstVnp[t];
-            x.A = (T)d.fgeo[f].z;
+            if constexpr (std::is_same<T, double>::value) {
+                x.wt = d.sstW[2 * x.j + m];
+                x.fc = d.sstFcs[2 * t + m];
+                x.rA = d.sstRA[t];
+                if (!CPL) x.vnp = d.sstVnp[t];
+                x.A = d.fgeo[f].z;
+            } else {
+                const float4 sl = d.sstSlotf[t];
+                const float2 wt = d.sstWf[x.j];
+                x.wt = m ? wt.y : wt.x;
+                x.fc = m ? sl.y : sl.x;
+                x.rA = sl.z;
+                if (!CPL) x.vnp = d.sstVnpf[t];
+                x.A = sl.w;
+            }
         }
     };
-    long long p = (long long)blockIdx.x + (long long)B * q0;
+    long long p = (long long)bid + (long long)B * q0;
     if (p >= d.nc) return;
     In cur, nxt;
     load(p, cur);
@@ -370,6 +450,29 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
         if (cur.use) {
             long long it = 0;
             T dt;
+            if (CPL) {  // the flow's Vn(W_j + dW_j) of this slot, written once by the flow's sweep
+                const size_t t = (size_t)cur.i * 4 + s;
+                if constexpr (std::is_same<T, double>::value) {
+                    double v;
+                    while (true) {
+                        v = __ldcv(d.sstVnp + t);
+                        if (!sent_t(v)) break;
+                        if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
+                        if (d.poll_ns) __nanosleep(d.poll_ns);
+                    }
+                    cur.vnp = v;
+                } else {
+                    float v;
+                    while (true) {
+                        v = __ldcv(d.sstVnpf + t);
+                        if (!sent_tf(v)) break;
+                        if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
+                        if (d.poll_ns) __nanosleep(d.poll_ns);
+                    }
+                    cur.vnp = v;
+                }
+                it = 0;
+            }
             if (std::is_same<T, double>::value) {
                 const double2* qd = reinterpret_cast<const double2*>((FWD ? d.sstDW1 : d.sstDW) + 2 * (size_t)cur.j);
                 double2 a;
@@ -415,7 +518,7 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
             // the binary32 copy the next levels wait for first, then the binary64 increment
             float resf = 0.f;
             if (lane < 2)
-                resf = FWD ? (-(float)cur.own - (float)dF) * (float)cur.dd : (float)cur.own - (float)dF * (float)cur.dd;
+                resf = FWD ? (-cur.ownf - (float)dF) * cur.ddf : cur.ownf - (float)dF * cur.ddf;
             const float f1 = __shfl_sync(0xffffffffu, resf, 1);
             if (lane == 0) __stcg(dstf + cur.i, make_float2(resf, f1));
             double res = 0.0;
@@ -427,6 +530,34 @@ __global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __res
         if (!PF) load(pn, nxt);
         cur = nxt;
         p = pn;
+    }
+}
+
+template <bool FWD, class T, bool PF>
+__global__ void __launch_bounds__(256) k_sst_sweep(DevArrays d, const int* __restrict__ order) {
+    sst_sweep_body<FWD, T, PF, false>(d, order, blockIdx.x, gridDim.x);
+}
+
+// The flow's and the turbulence equations' sweeps of one direction in one
+// cooperative grid: blocks [0, nflow) run the flow's round-robin sweep (F32:
+// its binary32 form) and hand each slot's Vn(W_j + dW_j) to the turbulence
+// sweep on the other blocks, which no longer waits for the whole flow sweep.
+// Each part only depends on its own and the flow's earlier positions, and
+// every block is resident, so both always progress; every wait is bounded.
+template <bool FWD, bool F32, bool PF>
+__global__ void __launch_bounds__(256) k_sweep_coupled(DevArrays d, int nflow) {
+    if ((int)blockIdx.x < nflow) {
+        if constexpr (F32) {
+            sweep_flow32_body<FWD, false, PF>(blockIdx.x, nflow, FWD ? d.npos2_fwd : d.npos2_bwd,
+                                              FWD ? d.fwd_order2 : d.bwd_order2, d.cface, d.lr, d.fg0f, d.Wf, d.swraf,
+                                              d.R, d.invD, d.dW1, d.dW, d.dW1f, d.dWf, d.err, d.poll_ns, d.sstVnpf);
+        } else {
+            sweep_flow_body<FWD, PF>(blockIdx.x, nflow, d.nc, FWD ? d.fwd_order : d.bwd_order, d.cface, d.lr, d.fg0,
+                                     d.W, d.swfc, d.swra, d.R, d.diag, d.invD, d.dW1, d.dW, d.err, d.poll_ns, d.sstVnp);
+        }
+    } else {
+        sst_sweep_body<FWD, typename std::conditional<F32, float, double>::type, PF, true>(
+            d, FWD ? d.fwd_order : d.bwd_order, blockIdx.x - nflow, gridDim.x - nflow);
     }
 }
 
@@ -511,8 +642,50 @@ int sst_sweep_max_grid(int blocks_per_sm, int threads, bool pf) {
     return per * sms;
 }
 
+void launch_sst_sweep_prep(const DevArrays& d, const LaunchCfg& L, bool fp32, bool coupled) {
+    const int cp = coupled ? 1 : 0;
+    if (fp32)
+        k_sst_sweep_prep32<<<nb(4 * d.nc, 256), 256, 0, L.stream>>>(d, cp);
+    else
+        k_sst_sweep_prep<<<nb(4 * d.nc, 256), 256, 0, L.stream>>>(d, cp);
+    *L.counter += 1;
+}
+
+int sweep_coupled_max_grid(bool fp32, int blocks_per_sm, int threads, bool pf) {
+    int dev = 0, sms = 0, a = 0, b = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void* f1 = fp32 ? (pf ? (void*)k_sweep_coupled<true, true, true> : (void*)k_sweep_coupled<true, true, false>)
+                    : (pf ? (void*)k_sweep_coupled<true, false, true> : (void*)k_sweep_coupled<true, false, false>);
+    void* f2 = fp32 ? (pf ? (void*)k_sweep_coupled<false, true, true> : (void*)k_sweep_coupled<false, true, false>)
+                    : (pf ? (void*)k_sweep_coupled<false, false, true> : (void*)k_sweep_coupled<false, false, false>);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, f1, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f2, threads, 0);
+    int per = a < b ? a : b;
+    if (blocks_per_sm > 0 && blocks_per_sm < per) per = blocks_per_sm;
+    return per * sms;
+}
+
+cudaError_t launch_sweep_coupled(const DevArrays& d, const LaunchCfg& L, bool forward, bool fp32, int grid,
+                                 int nflow) {
+    void* args[] = {(void*)&d, (void*)&nflow};
+    void* fn;
+    if (fp32)
+        fn = d.flow_pf ? (forward ? (void*)k_sweep_coupled<true, true, true> : (void*)k_sweep_coupled<false, true, true>)
+                       : (forward ? (void*)k_sweep_coupled<true, true, false> : (void*)k_sweep_coupled<false, true, false>);
+    else
+        fn = d.flow_pf ? (forward ? (void*)k_sweep_coupled<true, false, true> : (void*)k_sweep_coupled<false, false, true>)
+                       : (forward ? (void*)k_sweep_coupled<true, false, false> : (void*)k_sweep_coupled<false, false, false>);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(d.flow_threads), args, 0, L.stream);
+    *L.counter += 1;
+    return e;
+}
+
 cudaError_t launch_sst_sweeps(const DevArrays& d, const LaunchCfg& L, bool fp32) {
-    k_sst_sweep_prep<<<nb(4 * d.nc, 256), 256, 0, L.stream>>>(d);
+    if (fp32)
+        k_sst_sweep_prep32<<<nb(4 * d.nc, 256), 256, 0, L.stream>>>(d, 0);
+    else
+        k_sst_sweep_prep<<<nb(4 * d.nc, 256), 256, 0, L.stream>>>(d, 0);
     *L.counter += 1;
     for (int dir = 0; dir < 2; dir++) {
         const int* order = dir == 0 ? d.fwd_order : d.bwd_order;
