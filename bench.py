@@ -191,6 +191,17 @@ def alg_bytes(pass_name: str, nc: int, nf: int, viscous: bool, precision: str) -
     raise KeyError(pass_name)
 
 
+def sweep_dict(case) -> dict:
+    """The LU-SGS schedule a case runs (after autotune), with, for SST, whether the turbulence sweeps share the
+    flow's sweep launches."""
+    from tmp_gb300 import abi
+
+    d = dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), case.sweep_config()))
+    if case.flow == abi.FLOW_SST:
+        d["turbulence_overlapped"] = case.sst_overlapped()
+    return d
+
+
 def traffic_table() -> dict:
     p = ROOT / "profiles" / "traffic.json"
     try:
@@ -352,7 +363,7 @@ def overset_leg(stream) -> dict:
                       "cell_iters_per_s": ncell / (step_ms * 1e-3), "fringe_ms": round(fringe_ms, 4),
                       "hole_cells": [int((i == 0).sum()) for i in ib],
                       "receptor_cells": [int((i == -1).sum()) for i in ib],
-                      "sweep": dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), case.sweep_config())),
+                      "sweep": sweep_dict(case),
                       "finite_after_200_steps": bool(np.isfinite(case.get("U", 0)).all() and
                                                      np.isfinite(case.get("U", 1)).all())}
     case.close()
@@ -410,7 +421,7 @@ def batch_leg(stream, precision: int, nmesh: int = 256, steps: int = 5, mode: in
     tuned = []
     for c in packed:
         c.autotune(2)
-        tuned.append(dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), c.sweep_config())))
+        tuned.append(sweep_dict(c))
     ms_packed = run(packed)
     net = learn.load()
     ms_learned = None
@@ -679,12 +690,12 @@ def run_ours(args):
         c2 = make_case(f)
         fm, _ = timed_steps(c2, args.steps)
         forms[f] = {"ms_per_step": sum(fm) / args.steps, "value": nc * args.steps / (sum(fm) / 1e3),
-                    "sweep": dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), c2.sweep_config()))}
+                    "sweep": sweep_dict(c2)}
         if f == "fp64" and not args.no_e2e:
             forms[f]["e2e"] = e2e_of(c2)
         c2.close()
     forms[args.precision] = {"ms_per_step": 1e3 * t_local / args.steps, "value": nc * args.steps / t_local,
-                             "sweep": dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), case.sweep_config())), "e2e": e2e}
+                             "sweep": sweep_dict(case), "e2e": e2e}
     # the plain binary64 form (results equal to the reference's) next to the headline form
     plain = forms.get("fp64")
 
@@ -767,7 +778,7 @@ def run_ours(args):
         passes += ["sweep_fwd", "sweep_bwd", "lusgs_update"]
     if w.flow == "sst":
         passes += ["sst_residual", "sst_sweeps", "sst_update"]
-        if case.sweep_config()[0] == 0:  # the step runs the flow's and the turbulence sweeps in one launch each
+        if case.sst_overlapped():  # the step runs the flow's and the turbulence sweeps in one launch each
             passes += ["sweeps_overlapped"]
     mode = sweep_mode_for(args.precision)
     per, launches_of = {}, {}
@@ -830,7 +841,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision], "data": "synthetic",
             "config": {"workload": w.name, "ncell": nc, "nedge": nf, "levels": list(nlev), "mach": w.mach,
                        "aoa": w.aoa, "re": w.re, "cfl": w.cfl, "flow": w.flow, **w.extra, "precision": args.precision,
-                       "sweep": dict(zip(("mode", "blocks_per_sm", "threads", "lookahead"), case.sweep_config())),
+                       "sweep": sweep_dict(case),
                        "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
             "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms_per_step"], "e2e": plain.get("e2e"),

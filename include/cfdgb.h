@@ -294,6 +294,10 @@ int cfd_chain_schedule(cfd_mesh_t mesh, int forward, int nlists, int local, int 
  * fewer resident warps; after cfd_autotune, the ones it chose); any pointer
  * may be NULL. No reference counterpart. */
 int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm, int* threads, int* lookahead);
+/* 1 if the case's LU-SGS step runs its turbulence sweeps in the flow's sweep
+ * launches (CFD_FLOW_SST, sweep mode 0, sst_sequential 0; cfd_autotune sets
+ * sst_sequential by timing both), else 0. */
+int cfd_case_sst_overlap(cfd_case_t c, int* overlapped);
 /* Failure-detection self-test (no reference counterpart): launch a kernel that
  * waits, at most `polls` polls, on a device flag nothing sets, exactly as the
  * dataflow LU-SGS sweep waits on its neighbours.  Returns CFD_ERR_TIMEOUT when

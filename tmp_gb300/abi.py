@@ -146,6 +146,7 @@ def lib() -> C.CDLL:
         "cfd_set_precision": (C.c_int, [vp, C.c_int]),
         "cfd_autotune": (C.c_int, [vp, C.c_int, ip, dp]),
         "cfd_case_sweep": (C.c_int, [vp, ip, ip, ip, ip]),
+        "cfd_case_sst_overlap": (C.c_int, [vp, ip]),
         "cfd_chain_schedule": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, ip, ip, ip, ip, ip]),
         "cfd_sst_enable": (C.c_int, [vp]),
         "cfd_sst_freestream": (C.c_int, [vp, C.c_int, dp]),
@@ -296,6 +297,12 @@ class Case:
         a, b, t, la = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         check(lib().cfd_case_sweep(self.h, C.byref(a), C.byref(b), C.byref(t), C.byref(la)))
         return a.value, b.value, t.value, la.value
+
+    def sst_overlapped(self) -> bool:
+        """Whether the LU-SGS step runs the turbulence sweeps in the flow's sweep launches."""
+        v = C.c_int()
+        check(lib().cfd_case_sst_overlap(self.h, C.byref(v)))
+        return bool(v.value)
 
     def connect(self, meshes, obc_nodes=None, nfringe: int = 1, mexclude: int = 3):
         """Overset connectivity of the case's meshes (the handles it was created from); afterwards every LU-SGS

@@ -70,8 +70,9 @@ def c3_mesh() -> meshgen.GrdMesh:
                               density=1.0, grade=1.25, hmax=4e-3)
 
 
-def c3(aoa: float = 4.0, cfl: float = 10.0) -> Workload:
-    """The SST airfoil case; extra: freestream turbulence (intensity, mu_t / mu)."""
+def c3(aoa: float = 4.0, cfl: float = 400.0) -> Workload:
+    """The SST airfoil case; extra: freestream turbulence (intensity, mu_t / mu).  CFL 400 is the reference's
+    LU-SGS default (LUSGS_Integrator.h:18); the case names none."""
     return Workload(f"C3 NACA 0012 ~1.07M SST k-omega AoA {aoa:g}", c3_mesh(), "sst", "lusgs", 0.15, aoa, 6e6, cfl,
                     extra=dict(tu=0.001, mut_ratio=10.0))
 

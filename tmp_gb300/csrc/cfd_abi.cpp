@@ -2120,6 +2120,12 @@ extern "C" int cfd_case_sweep(cfd_case_t c, int* sweep_mode, int* blocks_per_sm,
     return CFD_OK;
 }
 
+extern "C" int cfd_case_sst_overlap(cfd_case_t c, int* overlapped) {
+    if (!c || !overlapped) return fail(CFD_ERR_ARG, "null argument");
+    *overlapped = c->sst_overlap() ? 1 : 0;
+    return CFD_OK;
+}
+
 extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_ms) {
     if (!c || reps <= 0) return fail(CFD_ERR_ARG, "cfd_autotune: null case or reps <= 0");
     if (c->p.advance != CFD_ADV_LUSGS) return fail(CFD_ERR_STATE, "cfd_autotune: only the LU-SGS sweeps are tuned");
@@ -2155,12 +2161,17 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
     // mode 6 keeps neighbouring lists in one block with a shared-memory hand-off)
     std::vector<int> modes{c->p.sweep_mode};
     if (c->fast_sweep() && (c->p.sweep_mode == 0 || c->p.sweep_mode == 5 || c->p.sweep_mode == 6)) modes = {0, 5, 6};
-    const int mode0 = c->p.sweep_mode, threads0 = d.flow_threads, pf0 = d.flow_pf;
-    int best = 0, best_mode = mode0, best_threads = threads0, best_pf = pf0;
+    const int mode0 = c->p.sweep_mode, threads0 = d.flow_threads, pf0 = d.flow_pf, seq0 = c->p.sst_sequential;
+    int best = 0, best_mode = mode0, best_threads = threads0, best_pf = pf0, best_seq = seq0;
     double best_t = 1e300;
     int rc = CFD_OK;
-    for (int mode : modes) {
+    for (int mode : modes)
+    // a coupled SST case with the round-robin schedule also tries its turbulence sweeps in the flow's launches
+    // and after them: overlapping pays where the chains wait on hand-offs (the binary32 sweeps) and not where
+    // both are bound by the same binary64 pipe
+    for (int seq : (c->turb() && mode == 0) ? std::vector<int>{0, 1} : std::vector<int>{seq0}) {
         c->p.sweep_mode = mode;
+        c->p.sst_sequential = seq;
         // the chain schedules run 256-thread blocks; the round-robin sweeps also try
         // fewer warps per block (fewer cells sharing one sub-partition's pipes)
         const bool chain = c->fast_sweep() && (mode == 5 || mode == 6);
@@ -2190,11 +2201,13 @@ extern "C" int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, dou
                     best_mode = mode;
                     best_threads = threads;
                     best_pf = pf;
+                    best_seq = seq;
                 }
             }
         }
     }
     c->p.sweep_mode = rc == CFD_OK ? best_mode : mode0;
+    c->p.sst_sequential = rc == CFD_OK ? best_seq : seq0;
     if (rc == CFD_OK) {
         c->p.sweep_blocks_per_sm = best;
         set_sweep_shape(c, best, best_threads, best_pf);
