@@ -109,6 +109,10 @@ struct cfd_case_s {
     DevArrays d;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // SST cases: a second stream for the model's residual passes, which only read the flow's
+    // intermediates and so run beside the flow's later passes (forked and joined by events)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fs = nullptr, ev_cg = nullptr, ev_upd = nullptr, ev_done = nullptr;
     long long launches = 0;
     cudaGraphExec_t gexec = nullptr;
     cudaGraph_t graph = nullptr;
@@ -193,6 +197,9 @@ void free_case(cfd_case_s* c) {
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    for (cudaEvent_t e : {c->ev_fs, c->ev_cg, c->ev_upd, c->ev_done})
+        if (e) cudaEventDestroy(e);
+    if (c->side) cudaStreamDestroy(c->side);
     delete c;
 }
 
@@ -201,17 +208,50 @@ void free_case(cfd_case_s* c) {
 // the plain form's reproduces the reference's roundings (k_fp64.cu).
 void launch_pass(const DevArrays& d, const LaunchCfg& L, bool visc, bool f32, int which, int first_order,
                  bool mixed, bool ffq);
-void residual_pass(cfd_case_s* c) {
+// The model's stream and events (created with the first turbulent residual).
+static void ensure_side(cfd_case_s* c) {
+    if (c->side) return;
+    int lo = 0, hi = 0, pr = 0;
+    ck(cudaDeviceGetStreamPriorityRange(&lo, &hi), "cudaDeviceGetStreamPriorityRange");
+    ck(cudaStreamGetPriority(c->stream, &pr), "cudaStreamGetPriority");
+    ck(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, pr), "cudaStreamCreate");
+    for (cudaEvent_t* e : {&c->ev_fs, &c->ev_cg, &c->ev_upd, &c->ev_done})
+        ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
+}
+// `from` waits for what `to_wait` has issued so far
+static void after(cudaStream_t from, cudaStream_t to_wait, cudaEvent_t e) {
+    ck(cudaEventRecord(e, to_wait), "cudaEventRecord");
+    ck(cudaStreamWaitEvent(from, e, 0), "cudaStreamWaitEvent");
+}
+
+// join_model: the caller's stream waits for the model's passes before returning
+// (lusgs_step instead joins after the model's last pass, which needs the time step).
+void residual_pass(cfd_case_s* c, bool join_model = true) {
     auto L = c->L();
     if (c->turb()) {
         // ViscousFlow2D::preprocessAdvance with the model (ViscousFlow2D.h:163-190): the
         // face states (with each face's mu_t), the turbulence face values, the gradients
-        // (with mu and F1 / F2 of the model), then the flow's and the model's face fluxes
-        for (int which = 0; which < 3; which++) {
-            launch_pass(c->d, L, true, false, which, c->p.first_order, c->mixed(), c->ffres());
-            if (c->ffres()) launch_ff_to_fp64(c->d, L, which);  // the model reads binary64 arrays
-            launch_sst_stage(c->d, L, which);
-        }
+        // (with mu and F1 / F2 of the model), then the flow's and the model's face fluxes.
+        // The flow's passes never read the model's arrays of the same step (mu_t changes
+        // only in the step's last update), so the model's passes run on the side stream as
+        // soon as the flow's intermediates they read exist: face values after the face
+        // states, gradients and fluxes after the flow's gradients (beside the flow's fluxes
+        // and its residual sum); no array is written on one stream and read or written on
+        // the other while both run.
+        ensure_side(c);
+        LaunchCfg S{c->side, &c->launches};
+        const DevArrays& d = c->d;
+        launch_pass(d, L, true, false, 0, c->p.first_order, c->mixed(), c->ffres());
+        after(c->side, c->stream, c->ev_fs);
+        if (c->ffres()) launch_ff_to_fp64(d, S, 0);  // the model reads binary64 arrays
+        launch_sst_stage(d, S, 0);
+        launch_pass(d, L, true, false, 1, c->p.first_order, c->mixed(), c->ffres());
+        after(c->side, c->stream, c->ev_cg);
+        if (c->ffres()) launch_ff_to_fp64(d, S, 1);
+        launch_sst_stage(d, S, 1);
+        launch_sst_stage(d, S, 2);
+        launch_pass(d, L, true, false, 2, c->p.first_order, c->mixed(), c->ffres());
+        if (join_model) after(c->stream, c->side, c->ev_done);
         return;
     }
     if (c->fp32()) launch_residual_fp32(c->d, L, c->viscous(), c->p.first_order);
@@ -507,9 +547,13 @@ void lusgs_step(cfd_case_s* c) {
     const DevArrays& d = c->d;
     if (c->track || c->mlp)
         ck(cudaMemcpyAsync(d.dWprev, d.dW, sizeof(d4) * d.nc, cudaMemcpyDeviceToDevice, c->stream), "dWprev");
-    residual_pass(c);
+    residual_pass(c, false);
     update_pass(c, 2 /*UPD_LUSGS*/, c->p.cfl, 0, 0.0);
-    if (c->turb()) launch_sst_stage(d, L, 3);  // the model's residual and diagonal (needs dt and the radii)
+    if (c->turb()) {  // the model's residual and diagonal (needs dt and the radii), then the join
+        after(c->side, c->stream, c->ev_upd);
+        launch_sst_stage(d, LaunchCfg{c->side, &c->launches}, 3);
+        after(c->stream, c->side, c->ev_done);
+    }
     if (c->sst_overlap()) {
         overlapped_sweeps(c);
     } else {
@@ -851,6 +895,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             ck(cudaMemcpyAsync(d.wblocks, wb.data(), wb.size() * sizeof(int4), cudaMemcpyHostToDevice, s), "upload");
         if (c->turb()) {
             sst_alloc(c);
+            ensure_side(c);  // not inside a stream capture later
             d.turb = 1;
             set_sweep_shape(c, P.sweep_blocks_per_sm, P.sweep_threads);
             sst_freestream(c);
