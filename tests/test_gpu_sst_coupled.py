@@ -115,6 +115,31 @@ def test_coupled_sst_fast_forms_follow_plain(built_lib, form):
     case.close()
 
 
+@pytest.mark.parametrize("mesh_file", ["mixed.grd", "omesh.grd"])
+def test_mixff_model_passes_follow_binary64(built_lib, mesh_file):
+    """MIXFF runs the model's residual passes in float-float (pairs of binary32 numbers, about 48 significant
+    bits): at one state their face values, gradients, F1 / F2 and face fluxes agree with the binary64 passes of the
+    plain form within 1e-10 (normwise relative; tanh is binary64 in both)."""
+    _, a = setup(mesh_file, 0.3, 2.0, 1e5, 5.0, 0.01, 0.035, abi_prec("FP64"), 13)
+    _, b = setup(mesh_file, 0.3, 2.0, 1e5, 5.0, 0.01, 0.035, abi_prec("MIXFF"), 13)
+    for c in (a, b):
+        c.residual()
+        c.sync()
+    worst = {}
+    for name in ("SST_TFACE", "SST_TGRAD", "SST_F1", "SST_F2", "SST_FCONV", "SST_FVISC"):
+        worst[name] = rel(b.get(name), a.get(name))
+        assert worst[name] <= 1e-10, (name, worst[name])
+    print("mixff model passes vs binary64:", worst)
+    a.close()
+    b.close()
+
+
+def abi_prec(form):
+    from tmp_gb300 import abi
+
+    return {"FP64": abi.PREC_FP64, "MIXED": abi.PREC_MIXED, "MIXFF": abi.PREC_MIXFF}[form]
+
+
 @pytest.mark.parametrize("form", ["FP64", "MIXED", "MIXFF"])
 @pytest.mark.parametrize("mesh_file", ["mixed.grd", "omesh.grd"])
 def test_overlapped_sweeps_equal_sequential(built_lib, form, mesh_file):

@@ -80,6 +80,10 @@ struct DevArrays {
     float4* sstSlotf = nullptr;  // [4*nc] binary32 sweep: per (cell, slot) (fc_k, fc_omega, r_A, face length)
     float* sstVnpf = nullptr;    // [4*nc] binary32 sweep: per (cell, slot) Vn(W_j + dW_j)
     float2* sstWf = nullptr;     // [nc] binary32 copy of sstW for that sweep
+    ff* sstTq = nullptr;         // [2*nc] MIXFF: float-float copies of k, omega, mu_t and the wall distance
+    ff* sstMutq = nullptr;       // [nc]   that the model's float-float passes read
+    ff* walldq = nullptr;        // [nc]
+    int ffsst = 0;               // 1: the model's residual passes run in float-float (MIXFF)
     int sst_grid = 0;            // co-resident blocks of the turbulence sweeps
     int cpl_grid = 0;            // co-resident blocks of the flow + turbulence sweep launch
     int cpl_nflow = 0;           // of which the flow's sweep takes [0, cpl_nflow)
@@ -255,8 +259,6 @@ void launch_update_fp32(const DevArrays& d, const LaunchCfg& L, bool viscous, in
 void launch_residual_ff(const DevArrays& d, const LaunchCfg& L, bool viscous, int first_order, int which = -1);
 void launch_update_ff(const DevArrays& d, const LaunchCfg& L, bool viscous, int mode, double cfl, int stage, double alpha);
 void launch_to_ff(const DevArrays& d, const LaunchCfg& L, bool geometry);
-// binary64 copies of the float-float residual arrays the SST model reads (which: 0 after face_state, 1 after cell_grad)
-void launch_ff_to_fp64(const DevArrays& d, const LaunchCfg& L, int which);
 // ---- k_misc.cu ----
 void launch_to_fp32(const DevArrays& d, const LaunchCfg& L, bool geometry);
 void launch_norm(const DevArrays& d, const LaunchCfg& L, int which);

@@ -191,7 +191,7 @@ void free_case(cfd_case_s* c) {
                     d.chain_cells[0], d.chain_cells[1], d.chain_rec[0], d.chain_rec[1], d.chain_jenc[0], d.chain_jenc[1], d.chain_stage[0],
                     d.chain_stage[1], d.chain_posb, d.chain_dF, d.Uq, d.gradq, d.phiq, d.speccq, d.specvq, d.gradTq,
                     d.muq, d.Ueq, d.fspecq, d.mueq, d.Fcq, d.Fvq, d.fg0q, d.fg1q, d.fvisq, d.cgeoq, d.sstW, d.sstDW1,
-                    d.sstDW, d.sstFcs, d.sstRA, d.sstVnp, d.sstDinv, d.sstDW1f, d.sstDWf, d.sstSlotf, d.sstWf, d.sstVnpf, d.iblank_cell,
+                    d.sstDW, d.sstFcs, d.sstRA, d.sstVnp, d.sstDinv, d.sstDW1f, d.sstDWf, d.sstSlotf, d.sstWf, d.sstVnpf, d.sstTq, d.sstMutq, d.walldq, d.iblank_cell,
                     c->fringe.src_nodes, c->fringe.src_ptr, c->fringe.src_cells, c->fringe.recv_node, c->fringe.nw,
                     c->fringe.inode, c->fringe.w, c->fringe.recv_cells, c->fringe.qn, c->fringe.vals};
     for (void* q : ptrs)
@@ -243,11 +243,10 @@ void residual_pass(cfd_case_s* c, bool join_model = true) {
         const DevArrays& d = c->d;
         launch_pass(d, L, true, false, 0, c->p.first_order, c->mixed(), c->ffres());
         after(c->side, c->stream, c->ev_fs);
-        if (c->ffres()) launch_ff_to_fp64(d, S, 0);  // the model reads binary64 arrays
+        // (MIXFF: the model's passes read the float-float arrays themselves; d.ffsst)
         launch_sst_stage(d, S, 0);
         launch_pass(d, L, true, false, 1, c->p.first_order, c->mixed(), c->ffres());
         after(c->side, c->stream, c->ev_cg);
-        if (c->ffres()) launch_ff_to_fp64(d, S, 1);
         launch_sst_stage(d, S, 1);
         launch_sst_stage(d, S, 2);
         launch_pass(d, L, true, false, 2, c->p.first_order, c->mixed(), c->ffres());
@@ -897,6 +896,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
             sst_alloc(c);
             ensure_side(c);  // not inside a stream capture later
             d.turb = 1;
+            d.ffsst = c->ffres() ? 1 : 0;
             set_sweep_shape(c, P.sweep_blocks_per_sm, P.sweep_threads);
             sst_freestream(c);
         }
@@ -965,6 +965,7 @@ static void sst_alloc(cfd_case_s* c) {
         dalloc(&d.sstFcs, 8 * nc); dalloc(&d.sstRA, 4 * nc); dalloc(&d.sstVnp, 4 * nc);
         dalloc(&d.sstDinv, 2 * nc); dalloc(&d.sstDW1f, nc); dalloc(&d.sstDWf, nc);
         dalloc(&d.sstSlotf, 4 * nc); dalloc(&d.sstWf, nc); dalloc(&d.sstVnpf, 4 * nc);
+        dalloc(&d.sstTq, 2 * nc); dalloc(&d.sstMutq, nc); dalloc(&d.walldq, nc);
         ck(cudaMemsetAsync(d.sstDW, 0, 2 * nc * sizeof(double), c->stream), "memset");
         ck(cudaMemsetAsync(d.sstDW1, 0, 2 * nc * sizeof(double), c->stream), "memset");
     }
@@ -1592,6 +1593,15 @@ FieldRef field_ref(cfd_case_s* c, int which) {
             case CFD_FIELD_MUEDGE: return {nullptr, nullptr, 1, true, false, d.mueq};
             default: break;
         }
+        if (d.ffsst) switch (which) {  // the model's float-float intermediates, stored as pairs in their slots
+            case CFD_FIELD_SST_TFACE: return {nullptr, nullptr, 2, true, false, d.sstTf};
+            case CFD_FIELD_SST_TGRAD: return {nullptr, nullptr, 4, false, false, d.sstG};
+            case CFD_FIELD_SST_F1: return {nullptr, nullptr, 1, false, false, d.sstF1};
+            case CFD_FIELD_SST_F2: return {nullptr, nullptr, 1, false, false, d.sstF2};
+            case CFD_FIELD_SST_FCONV: return {nullptr, nullptr, 2, true, false, d.sstFc};
+            case CFD_FIELD_SST_FVISC: return {nullptr, nullptr, 2, true, false, d.sstFv};
+            default: break;
+        }
     }
     switch (which) {
         case CFD_FIELD_U: return {d.U, nullptr, 4, false, true};
@@ -2089,6 +2099,7 @@ extern "C" int cfd_set_precision(cfd_case_t c, int precision) {
     c->p.precision = precision;
     c->d.resid32 = precision == CFD_PREC_FP32 ? 1 : 0;
     c->d.residq = precision == CFD_PREC_MIXFF ? 1 : 0;
+    c->d.ffsst = (c->d.residq && c->d.turb) ? 1 : 0;
     if (c->p.advance == CFD_ADV_LUSGS)
         set_sweep_shape(c, c->p.sweep_blocks_per_sm, c->d.flow_threads);
     c->drop_graph();

@@ -23,34 +23,6 @@ __global__ void k_to_q4(int n, const d4* __restrict__ a, q4* __restrict__ b) {
     st4(b + i, q4{ff(v.x), ff(v.y), ff(v.z), ff(v.w)});
 }
 
-__global__ void k_from_q4(int n, const q4* __restrict__ a, d4* __restrict__ b) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const q4 v = ld4(a + i);
-    st4(b + i, d4{(double)v.x, (double)v.y, (double)v.z, (double)v.w});
-}
-__global__ void k_from_ff(int n, const ff* __restrict__ a, double* __restrict__ b) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (double)a[i];
-}
-
-// Binary64 copies of the float-float residual arrays the SST model reads (its
-// kernels run in binary64): after face_state the face states and viscosities,
-// after cell_grad the gradients, cell viscosities and spectral radii.
-void launch_ff_to_fp64(const DevArrays& d, const LaunchCfg& L, int which) {
-    if (which == 0) {
-        k_from_q4<<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.Ueq, d.Ue);
-        k_from_ff<<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.mueq, d.mue);
-        *L.counter += 2;
-    } else if (which == 1) {
-        k_from_q4<<<nblk(2 * d.nc, 256), 256, 0, L.stream>>>(2 * d.nc, d.gradq, d.grad);
-        k_from_ff<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.muq, d.mu);
-        k_from_ff<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.speccq, d.specc);
-        k_from_ff<<<nblk(d.nc, 256), 256, 0, L.stream>>>(d.nc, d.specvq, d.specv);
-        *L.counter += 4;
-    }
-}
-
 void launch_to_ff(const DevArrays& d, const LaunchCfg& L, bool geometry) {
     if (geometry) {
         k_to_q4<<<nblk(d.nf, 256), 256, 0, L.stream>>>(d.nf, d.fg0, d.fg0q);

@@ -16,6 +16,7 @@
 
 #include "case.hpp"
 #include "sweep_flow.cuh"
+#include "fv_ff.cuh"
 
 namespace cfdgb {
 namespace {
@@ -27,144 +28,226 @@ constexpr double beta1 = 0.075, beta2 = 0.0828, sigma_k1 = 0.85, sigma_k2 = 1.0,
 __device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }  // std::max
 __device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }  // std::min
 
+// Where the model's passes read the flow's intermediates and the model's own
+// state.  T = double: the binary64 arrays (the plain and MIXED forms; with
+// -fmad=false and the reference's operation order this reproduces its SST
+// functions).  T = ff (MIXFF): the float-float residual's own arrays and
+// float-float copies of k, omega, mu_t and the wall distance made at the start
+// of the model's passes, so the model runs on the FP32 pipe like the flow's
+// residual; its intermediates (face k and omega, gradients, F1 / F2, face
+// fluxes) are stored as pairs in the same 8-byte slots, and the residual and
+// diagonal are written back in binary64.  tanh (F1, F2) is evaluated in
+// binary64 in both.
+template <class T> struct SstIo;
+template <> struct SstIo<double> {
+    typedef d4 V;
+    static __device__ __forceinline__ double rho(const DevArrays& d, int c) { return d.U[c].x; }
+    static __device__ __forceinline__ d4 ue(const DevArrays& d, int f) { return d.Ue[f]; }
+    static __device__ __forceinline__ double mue(const DevArrays& d, int f) { return d.mue[f]; }
+    static __device__ __forceinline__ double mu(const DevArrays& d, int c) { return d.mu[c]; }
+    static __device__ __forceinline__ d4 fgeo(const DevArrays& d, int f) { return d.fgeo[f]; }
+    static __device__ __forceinline__ d4 cgeo(const DevArrays& d, int c) { return d.cgeo[c]; }
+    static __device__ __forceinline__ double kw(const DevArrays& d, int i) { return d.sstT[i]; }
+    static __device__ __forceinline__ double mut(const DevArrays& d, int c) { return d.sstMut[c]; }
+    static __device__ __forceinline__ double walld(const DevArrays& d, int c) { return d.walld[c]; }
+    static __device__ __forceinline__ d4 gradu(const DevArrays& d, int c) { return d.grad[2 * c + 1]; }
+    static __device__ __forceinline__ double specc(const DevArrays& d, int c) { return d.specc[c]; }
+    static __device__ __forceinline__ double specv(const DevArrays& d, int c) { return d.specv[c]; }
+    static __device__ __forceinline__ double mutf(const DevArrays& d, int f) { return d.sstMutf[f]; }
+    static __device__ __forceinline__ double dt(const DevArrays& d, int c) { return d.dt[c]; }
+    static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
+    static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+    static __device__ __forceinline__ double tanh_(double x) { return tanh(x); }
+};
+template <> struct SstIo<ff> {
+    typedef q4 V;
+    static __device__ __forceinline__ ff rho(const DevArrays& d, int c) { return reinterpret_cast<const ff*>(d.Uq)[4 * (size_t)c]; }
+    static __device__ __forceinline__ q4 ue(const DevArrays& d, int f) { return ld4(d.Ueq + f); }
+    static __device__ __forceinline__ ff mue(const DevArrays& d, int f) { return d.mueq[f]; }
+    static __device__ __forceinline__ ff mu(const DevArrays& d, int c) { return d.muq[c]; }
+    static __device__ __forceinline__ q4 fgeo(const DevArrays& d, int f) { return ld4(d.fg0q + f); }  // nx, ny, length
+    static __device__ __forceinline__ q4 cgeo(const DevArrays& d, int c) { return ld4(d.cgeoq + c); }
+    static __device__ __forceinline__ ff kw(const DevArrays& d, int i) { return d.sstTq[i]; }
+    static __device__ __forceinline__ ff mut(const DevArrays& d, int c) { return d.sstMutq[c]; }
+    static __device__ __forceinline__ ff walld(const DevArrays& d, int c) { return d.walldq[c]; }
+    static __device__ __forceinline__ q4 gradu(const DevArrays& d, int c) { return ld4(d.gradq + 2 * (size_t)c + 1); }
+    static __device__ __forceinline__ ff specc(const DevArrays& d, int c) { return d.speccq[c]; }
+    static __device__ __forceinline__ ff specv(const DevArrays& d, int c) { return d.specvq[c]; }
+    static __device__ __forceinline__ ff mutf(const DevArrays& d, int f) { return ff(d.sstMutf[f]); }
+    static __device__ __forceinline__ ff dt(const DevArrays& d, int c) { return ff(d.dt[c]); }
+    static __device__ __forceinline__ ff abs_(ff x) { return ff_abs(x); }
+    static __device__ __forceinline__ ff sqrt_(ff x) { return ff_sqrt(x); }
+    static __device__ __forceinline__ ff tanh_(ff x) { return ff(tanh((double)x)); }
+};
+template <class T> __device__ __forceinline__ T tmax(T a, T b) { return (a < b) ? b : a; }  // std::max
+template <class T> __device__ __forceinline__ T tmin(T a, T b) { return (b < a) ? b : a; }  // std::min
+template <class T> __device__ __forceinline__ T* as(double* p) { return reinterpret_cast<T*>(p); }
+template <class T> __device__ __forceinline__ const T* as(const double* p) { return reinterpret_cast<const T*>(p); }
+
+// The float-float copies of the model's state the MIXFF passes read.
+__global__ void k_sst_to_ff(DevArrays d) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nc) return;
+    d.sstTq[2 * c] = ff(d.sstT[2 * c]);
+    d.sstTq[2 * c + 1] = ff(d.sstT[2 * c + 1]);
+    d.sstMutq[c] = ff(d.sstMut[c]);
+    d.walldq[c] = ff(d.walld[c]);
+}
+
 // ComputeFaceTValue (:615-659) and the face loop of
 // ComputeTurbulenceViscousCoefficient (:749-777).
+template <class T>
 __global__ void k_sst_face(DevArrays d) {
+    typedef SstIo<T> IO;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= d.nf) return;
     const int2 lr = d.lr[f];
-    const d4 g = d.fgeo[f];
+    const auto g = IO::fgeo(d, f);
     const MeshPrm& P = d.prm[d.fmesh[f]];
     const int l = lr.x, r = lr.y;
-    double t0, t1, mf;
+    T t0, t1, mf;
     if (r >= 0) {
-        t0 = 0.5 * (d.sstT[2 * l] + d.sstT[2 * r]);
-        t1 = 0.5 * (d.sstT[2 * l + 1] + d.sstT[2 * r + 1]);
-        mf = 0.5 * (d.sstMut[l] + d.sstMut[r]);
+        t0 = T(0.5) * (IO::kw(d, 2 * l) + IO::kw(d, 2 * r));
+        t1 = T(0.5) * (IO::kw(d, 2 * l + 1) + IO::kw(d, 2 * r + 1));
+        mf = T(0.5) * (IO::mut(d, l) + IO::mut(d, r));
     } else if (r == BC_WALL) {
-        const double dis = d.walld[l];
-        t0 = 0.0;
-        t1 = 10.0 * 6.0 * d.mue[f] / (d.Ue[f].x * beta1 * dis * dis);
-        mf = 0.0;
+        const T dis = IO::walld(d, l);
+        t0 = T(0.0);
+        t1 = T(10.0) * T(6.0) * IO::mue(d, f) / (IO::ue(d, f).x * T(beta1) * dis * dis);
+        mf = T(0.0);
     } else {
-        const d4 ue = d.Ue[f];
-        double vn = 0;
+        const auto ue = IO::ue(d, f);
+        T vn = T(0);
         vn += ue.z * g.x;
         vn += ue.w * g.y;
-        if (vn > 0.0) {
-            t0 = d.sstT[2 * l];
-            t1 = d.sstT[2 * l + 1];
+        if (vn > T(0.0)) {
+            t0 = IO::kw(d, 2 * l);
+            t1 = IO::kw(d, 2 * l + 1);
         } else {
-            t0 = P.sst_k;
-            t1 = P.sst_w;
+            t0 = T(P.sst_k);
+            t1 = T(P.sst_w);
         }
-        mf = vn > 0.0 ? d.sstMut[l] : P.sst_mut;
+        mf = vn > T(0.0) ? IO::mut(d, l) : T(P.sst_mut);
     }
-    d.sstTf[2 * f] = t0;
-    d.sstTf[2 * f + 1] = t1;
-    if (!d.turb) d.sstMutf[f] = mf;  // coupled, the flow's face_state pass has formed it (for the viscous radius)
+    T* Tf = as<T>(d.sstTf);
+    Tf[2 * f] = t0;
+    Tf[2 * f + 1] = t1;
+    if (!d.turb) d.sstMutf[f] = (double)mf;  // coupled, the flow's face_state pass has formed it (for the viscous radius)
 }
 
 // ComputeCellTGradient (:662-692) and ComputeSSTf1f2 (:695-722).
+template <class T>
 __global__ void k_sst_cell(DevArrays d) {
+    typedef SstIo<T> IO;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d.nc) return;
     const int4 cf = d.cface[c];
     const int codes[4] = {cf.x, cf.y, cf.z, cf.w};
-    double gk0 = 0, gk1 = 0, gw0 = 0, gw1 = 0;
+    const T* Tf = as<T>(d.sstTf);
+    T gk0 = T(0), gk1 = T(0), gw0 = T(0), gw1 = T(0);
     for (int s = 0; s < 4; s++) {
         const int code = codes[s];
         if (code == 0) continue;
         const int f = code > 0 ? code - 1 : -code - 1;
-        const d4 g = d.fgeo[f];
-        const double ak = g.z * d.sstTf[2 * f], aw = g.z * d.sstTf[2 * f + 1];
-        const double vk0 = g.x * ak, vk1 = g.y * ak, vw0 = g.x * aw, vw1 = g.y * aw;
+        const auto g = IO::fgeo(d, f);
+        const T ak = g.z * Tf[2 * f], aw = g.z * Tf[2 * f + 1];
+        const T vk0 = g.x * ak, vk1 = g.y * ak, vw0 = g.x * aw, vw1 = g.y * aw;
         if (code > 0) {
             gk0 = gk0 + vk0; gk1 = gk1 + vk1; gw0 = gw0 + vw0; gw1 = gw1 + vw1;
         } else {
             gk0 = gk0 - vk0; gk1 = gk1 - vk1; gw0 = gw0 - vw0; gw1 = gw1 - vw1;
         }
     }
-    const double vol = d.cgeo[c].x;
+    const T vol = IO::cgeo(d, c).x;
     gk0 = gk0 / vol; gk1 = gk1 / vol; gw0 = gw0 / vol; gw1 = gw1 / vol;
-    d.sstG[4 * c] = gk0; d.sstG[4 * c + 1] = gk1; d.sstG[4 * c + 2] = gw0; d.sstG[4 * c + 3] = gw1;
-    double gradVal = 0;
+    T* G = as<T>(d.sstG);
+    G[4 * c] = gk0; G[4 * c + 1] = gk1; G[4 * c + 2] = gw0; G[4 * c + 3] = gw1;
+    T gradVal = T(0);
     gradVal += gk0 * gw0;
     gradVal += gk1 * gw1;
-    const double rho = d.U[c].x, dis = d.walld[c], K = d.sstT[2 * c], w = d.sstT[2 * c + 1], muL = d.mu[c];
-    const double CD_kw = dmax(2.0 * rho * sigma_w2 / w * gradVal, 1.0e-20);
-    double arg1 = dmax(sqrt(K) / (0.09 * w * dis), 500.0 * muL / (rho * w * dis * dis));
-    arg1 = dmin(arg1, 4.0 * rho * sigma_w2 * K / (CD_kw * dis * dis));
-    const double arg2 = dmax(2.0 * sqrt(K) / (0.09 * w * dis), 500.0 * muL / (rho * w * dis * dis));
-    d.sstF1[c] = tanh(arg1 * arg1 * arg1 * arg1);
-    d.sstF2[c] = tanh(arg2 * arg2);
+    const T rho = IO::rho(d, c), dis = IO::walld(d, c), K = IO::kw(d, 2 * c), w = IO::kw(d, 2 * c + 1),
+            muL = IO::mu(d, c);
+    const T CD_kw = tmax(T(2.0) * rho * T(sigma_w2) / w * gradVal, T(1.0e-20));
+    T arg1 = tmax(IO::sqrt_(K) / (T(0.09) * w * dis), T(500.0) * muL / (rho * w * dis * dis));
+    arg1 = tmin(arg1, T(4.0) * rho * T(sigma_w2) * K / (CD_kw * dis * dis));
+    const T arg2 = tmax(T(2.0) * IO::sqrt_(K) / (T(0.09) * w * dis), T(500.0) * muL / (rho * w * dis * dis));
+    as<T>(d.sstF1)[c] = IO::tanh_(arg1 * arg1 * arg1 * arg1);
+    as<T>(d.sstF2)[c] = IO::tanh_(arg2 * arg2);
 }
 
 // SolveConvectiveTFlux (:783-831) and SolveViscousTFlux (:834-920).  The
 // interior face gradient is corrected along the centre line one component
 // after the other, the y component using the already corrected x component,
 // as the reference does.
+template <class T>
 __global__ void k_sst_flux(DevArrays d) {
+    typedef SstIo<T> IO;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= d.nf) return;
     const int2 lr = d.lr[f];
     const int l = lr.x, r = lr.y;
-    const d4 g = d.fgeo[f];
-    const double nx = g.x, ny = g.y, A = g.z;
-    const d4 ue = d.Ue[f];
-    double vn = 0;
+    const auto g = IO::fgeo(d, f);
+    const T nx = g.x, ny = g.y, A = g.z;
+    const auto ue = IO::ue(d, f);
+    const T* Tf = as<T>(d.sstTf);
+    const T* F1 = as<T>(d.sstF1);
+    const T* G = as<T>(d.sstG);
+    T vn = T(0);
     vn += ue.z * nx;
     vn += ue.w * ny;
-    double fc0, fc1;
+    T fc0, fc1;
     if (r >= 0) {
-        const double vp = 0.5 * (vn + fabs(vn)), vs = 0.5 * (vn - fabs(vn));
-        const double rl = d.U[l].x, rr = d.U[r].x;
-        fc0 = d.sstT[2 * l] * rl * vp * A + d.sstT[2 * r] * rr * vs * A;
-        fc1 = d.sstT[2 * l + 1] * rl * vp * A + d.sstT[2 * r + 1] * rr * vs * A;
+        const T vp = T(0.5) * (vn + IO::abs_(vn)), vs = T(0.5) * (vn - IO::abs_(vn));
+        const T rl = IO::rho(d, l), rr = IO::rho(d, r);
+        fc0 = IO::kw(d, 2 * l) * rl * vp * A + IO::kw(d, 2 * r) * rr * vs * A;
+        fc1 = IO::kw(d, 2 * l + 1) * rl * vp * A + IO::kw(d, 2 * r + 1) * rr * vs * A;
     } else {
-        fc0 = vn * ue.x * d.sstTf[2 * f] * A;
-        fc1 = vn * ue.x * d.sstTf[2 * f + 1] * A;
+        fc0 = vn * ue.x * Tf[2 * f] * A;
+        fc1 = vn * ue.x * Tf[2 * f + 1] * A;
     }
-    double face_f1, g00, g01, g10, g11;
+    T face_f1, g00, g01, g10, g11;
     if (r >= 0) {
-        const double l0 = d.cgeo[r].y - d.cgeo[l].y, l1 = d.cgeo[r].z - d.cgeo[l].z;
-        double L2 = 0;
+        const auto cl = IO::cgeo(d, l), cr = IO::cgeo(d, r);
+        const T l0 = cr.y - cl.y, l1 = cr.z - cl.z;
+        T L2 = T(0);
         L2 += l0 * l0;
         L2 += l1 * l1;
-        face_f1 = 0.5 * (d.sstF1[l] + d.sstF1[r]);
-        const double* Gl = d.sstG + 4 * l;
-        const double* Gr = d.sstG + 4 * r;
-        g00 = (Gl[0] + Gr[0]) * 0.5;
-        g01 = (Gl[1] + Gr[1]) * 0.5;
-        g10 = (Gl[2] + Gr[2]) * 0.5;
-        g11 = (Gl[3] + Gr[3]) * 0.5;
-        const double dk = d.sstT[2 * r] - d.sstT[2 * l], dw = d.sstT[2 * r + 1] - d.sstT[2 * l + 1];
+        face_f1 = T(0.5) * (F1[l] + F1[r]);
+        const T* Gl = G + 4 * l;
+        const T* Gr = G + 4 * r;
+        g00 = (Gl[0] + Gr[0]) * T(0.5);
+        g01 = (Gl[1] + Gr[1]) * T(0.5);
+        g10 = (Gl[2] + Gr[2]) * T(0.5);
+        g11 = (Gl[3] + Gr[3]) * T(0.5);
+        const T dk = IO::kw(d, 2 * r) - IO::kw(d, 2 * l), dw = IO::kw(d, 2 * r + 1) - IO::kw(d, 2 * l + 1);
         g00 = g00 + ((dk) - (g00 * l0 + g01 * l1)) * l0 / L2;
         g01 = g01 + ((dk) - (g00 * l0 + g01 * l1)) * l1 / L2;
         g10 = g10 + ((dw) - (g10 * l0 + g11 * l1)) * l0 / L2;
         g11 = g11 + ((dw) - (g10 * l0 + g11 * l1)) * l1 / L2;
     } else {
-        face_f1 = d.sstF1[l];
-        g00 = d.sstG[4 * l];
-        g01 = d.sstG[4 * l + 1];
-        g10 = d.sstG[4 * l + 2];
-        g11 = d.sstG[4 * l + 3];
+        face_f1 = F1[l];
+        g00 = G[4 * l];
+        g01 = G[4 * l + 1];
+        g10 = G[4 * l + 2];
+        g11 = G[4 * l + 3];
     }
-    const double sigma_k = face_f1 * sigma_k1 + (1 - face_f1) * sigma_k2;
-    const double sigma_w = face_f1 * sigma_w1 + (1 - face_f1) * sigma_w2;
-    const double faceMul = d.mue[f], faceMut = d.sstMutf[f];
-    const double txx_k = (faceMul + sigma_k * faceMut) * g00;
-    const double tyy_k = (faceMul + sigma_k * faceMut) * g01;
-    const double txx_w = (faceMul + sigma_w * faceMut) * g10;
-    const double tyy_w = (faceMul + sigma_w * faceMut) * g11;
-    double fv0 = txx_k * nx + tyy_k * ny;
-    double fv1 = txx_w * nx + tyy_w * ny;
+    const T sigma_k = face_f1 * T(sigma_k1) + (T(1) - face_f1) * T(sigma_k2);
+    const T sigma_w = face_f1 * T(sigma_w1) + (T(1) - face_f1) * T(sigma_w2);
+    const T faceMul = IO::mue(d, f), faceMut = IO::mutf(d, f);
+    const T txx_k = (faceMul + sigma_k * faceMut) * g00;
+    const T tyy_k = (faceMul + sigma_k * faceMut) * g01;
+    const T txx_w = (faceMul + sigma_w * faceMut) * g10;
+    const T tyy_w = (faceMul + sigma_w * faceMut) * g11;
+    T fv0 = txx_k * nx + tyy_k * ny;
+    T fv1 = txx_w * nx + tyy_w * ny;
     fv0 *= A;
     fv1 *= A;
-    d.sstFc[2 * f] = fc0;
-    d.sstFc[2 * f + 1] = fc1;
-    d.sstFv[2 * f] = fv0;
-    d.sstFv[2 * f + 1] = fv1;
+    T* Fc = as<T>(d.sstFc);
+    T* Fv = as<T>(d.sstFv);
+    Fc[2 * f] = fc0;
+    Fc[2 * f + 1] = fc1;
+    Fv[2 * f] = fv0;
+    Fv[2 * f + 1] = fv1;
 }
 
 // rans_P_Solver (:923-966), SolveTotalTFlux (:969-1013) and SolveDiag (:170-192).
@@ -172,35 +255,39 @@ __global__ void k_sst_flux(DevArrays d) {
 // model inside every LU-SGS step): sum(Fc - Fv) - Q vol, the sign that
 // dW = -R / D needs for the sources (the written sign turns production into
 // destruction).
+template <class T>
 __global__ void k_sst_total(DevArrays d, int coupled) {
+    typedef SstIo<T> IO;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d.nc) return;
-    const double f1 = d.sstF1[c];
-    const double* G = d.sstG + 4 * c;
-    double rdiv = 0;
+    const T f1 = as<T>(d.sstF1)[c];
+    const T* G = as<T>(d.sstG) + 4 * c;
+    T rdiv = T(0);
     rdiv += G[0] * G[2];
     rdiv += G[1] * G[3];
-    const double Cw = f1 * Cw1 + (1.0 - f1) * Cw2;
-    const double beta = f1 * beta1 + (1.0 - f1) * beta2;
-    const double rho = d.U[c].x;
-    const double k = d.sstT[2 * c], w = d.sstT[2 * c + 1], mut = d.sstMut[c];
-    const d4 gu = d.grad[2 * c + 1];  // (du/dx, du/dy, dv/dx, dv/dy)
-    const double ux = gu.x, uy = gu.y, vx = gu.z, vy = gu.w;
-    const double ddls0 = 2.0 / 3.0 * ((ux - vy) * (ux - vy));
-    const double ddls1 = (uy + vx) * (uy + vx);
-    const double ddls2 = 2.0 / 3.0 * rho * k * (ux + vy);
-    const double P = (ddls0 + ddls1) * mut - ddls2;
-    const double q0 = P - beta_star * rho * k * w;
-    const double q1 = Cw * rho * P / mut - beta * rho * w * w + 2 * (1 - f1) * rho * sigma_w2 / w * rdiv;
-    const double vol = d.cgeo[c].x;
-    double r0 = coupled ? -(q0 * vol) : q0 * vol, r1 = coupled ? -(q1 * vol) : q1 * vol;
+    const T Cw = f1 * T(Cw1) + (T(1.0) - f1) * T(Cw2);
+    const T beta = f1 * T(beta1) + (T(1.0) - f1) * T(beta2);
+    const T rho = IO::rho(d, c);
+    const T k = IO::kw(d, 2 * c), w = IO::kw(d, 2 * c + 1), mut = IO::mut(d, c);
+    const auto gu = IO::gradu(d, c);  // (du/dx, du/dy, dv/dx, dv/dy)
+    const T ux = gu.x, uy = gu.y, vx = gu.z, vy = gu.w;
+    const T ddls0 = T(2.0 / 3.0) * ((ux - vy) * (ux - vy));
+    const T ddls1 = (uy + vx) * (uy + vx);
+    const T ddls2 = T(2.0 / 3.0) * rho * k * (ux + vy);
+    const T P = (ddls0 + ddls1) * mut - ddls2;
+    const T q0 = P - T(beta_star) * rho * k * w;
+    const T q1 = Cw * rho * P / mut - beta * rho * w * w + T(2) * (T(1) - f1) * rho * T(sigma_w2) / w * rdiv;
+    const T vol = IO::cgeo(d, c).x;
+    T r0 = coupled ? -(q0 * vol) : q0 * vol, r1 = coupled ? -(q1 * vol) : q1 * vol;
     const int4 cf = d.cface[c];
     const int codes[4] = {cf.x, cf.y, cf.z, cf.w};
+    const T* Fc = as<T>(d.sstFc);
+    const T* Fv = as<T>(d.sstFv);
     for (int s = 0; s < 4; s++) {
         const int code = codes[s];
         if (code == 0) continue;
         const int f = code > 0 ? code - 1 : -code - 1;
-        const double e0 = d.sstFc[2 * f] - d.sstFv[2 * f], e1 = d.sstFc[2 * f + 1] - d.sstFv[2 * f + 1];
+        const T e0 = Fc[2 * f] - Fv[2 * f], e1 = Fc[2 * f + 1] - Fv[2 * f + 1];
         if (code > 0) {
             r0 += e0;
             r1 += e1;
@@ -209,16 +296,30 @@ __global__ void k_sst_total(DevArrays d, int coupled) {
             r1 -= e1;
         }
     }
-    d.sstR[2 * c] = r0;
-    d.sstR[2 * c + 1] = r1;
-    const double OMEGAN = 1.5;
-    const double diag = vol / d.dt[c] + 0.5 * OMEGAN * d.specc[c] + d.specv[c];
-    d.sstD[2 * c] = diag + 2.0 * beta_star * w * vol;  // omega, as the reference (:183)
-    d.sstD[2 * c + 1] = diag + vol * fabs(2.0 * beta * w + 2.0 * sigma_w2 * (1 - f1) * rdiv / (w * w));
+    d.sstR[2 * c] = (double)r0;
+    d.sstR[2 * c + 1] = (double)r1;
+    const T OMEGAN = T(1.5);
+    const T diag = vol / IO::dt(d, c) + T(0.5) * OMEGAN * IO::specc(d, c) + IO::specv(d, c);
+    d.sstD[2 * c] = (double)(diag + T(2.0) * T(beta_star) * w * vol);  // omega, as the reference (:183)
+    d.sstD[2 * c + 1] = (double)(diag + vol * IO::abs_(T(2.0) * beta * w + T(2.0) * T(sigma_w2) * (T(1) - f1) * rdiv / (w * w)));
 }
 
 // initializeConsData then UpdatePrimitiveVariables: W = rho (k, omega),
 // (k, omega) = W / rho, mu_t = a1 W_k / max(a1 W_omega / rho, F2 |dv/dx - du/dy|).
+// |dv/dx - du/dy| and F2 of cell c for the eddy-viscosity update, from the
+// binary64 arrays or (MIXFF) the float-float ones the model's passes used.
+__device__ __forceinline__ void model_curl_f2(const DevArrays& d, int c, double& curl, double& f2) {
+    if (d.ffsst) {
+        const q4 gu = ld4(d.gradq + 2 * (size_t)c + 1);
+        curl = fabs((double)(gu.z - gu.y));
+        f2 = (double)as<ff>(d.sstF2)[c];
+    } else {
+        const d4 gu = d.grad[2 * c + 1];
+        curl = fabs(gu.z - gu.y);
+        f2 = d.sstF2[c];
+    }
+}
+
 __global__ void k_sst_mut(DevArrays d) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d.nc) return;
@@ -226,9 +327,9 @@ __global__ void k_sst_mut(DevArrays d) {
     const double W0 = d.sstT[2 * c] * rho, W1 = d.sstT[2 * c + 1] * rho;
     d.sstT[2 * c] = W0 / rho;
     d.sstT[2 * c + 1] = W1 / rho;
-    const d4 gu = d.grad[2 * c + 1];
-    const double curl = fabs(gu.z - gu.y);
-    const double h = dmax(a1 * W1 / rho, d.sstF2[c] * curl);
+    double curl, f2;
+    model_curl_f2(d, c, curl, f2);
+    const double h = dmax(a1 * W1 / rho, f2 * curl);
     d.sstMut[c] = a1 * W0 / h;
 }
 
@@ -354,7 +455,8 @@ __global__ void __launch_bounds__(256) k_sst_sweep_prep32(DevArrays d, int coupl
             const float rho = (float)ud.x, p = (float)ud.y;
             const float vn = (float)ud.z * g.x + (float)ud.w * g.y;
             rA = 1.5f * (fabsf(vn) + sqrtf(1.4f * p / rho));
-            rA += fmaxf(4.f / (3.f * rho), 1.4f / rho) * ((float)d.mu[i] / 0.72f + (float)d.sstMut[i] / 0.9f) /
+            const float mui = d.ffsst ? d.muq[i].hi : (float)d.mu[i];
+            rA += fmaxf(4.f / (3.f * rho), 1.4f / rho) * (mui / 0.72f + (float)d.sstMut[i] / 0.9f) /
                   sqrtf(d.fvisf[f].z);
         }
     }
@@ -579,9 +681,9 @@ __global__ void k_sst_update(DevArrays d) {
     d.sstW[2 * c + 1] = w1;
     d.sstT[2 * c] = k;
     d.sstT[2 * c + 1] = w;
-    const d4 gu = d.grad[2 * c + 1];
-    const double curl = fabs(gu.z - gu.y);
-    const double h = dmax(a1 * w1 / rho, d.sstF2[c] * curl);
+    double curl, f2;
+    model_curl_f2(d, c, curl, f2);
+    const double h = dmax(a1 * w1 / rho, f2 * curl);
     d.sstMut[c] = a1 * w0 / h;
 }
 
@@ -599,18 +701,29 @@ inline unsigned nb(int n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 }  // namespace
 
 void launch_sst_residual(const DevArrays& d, const LaunchCfg& L) {
-    k_sst_face<<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
-    k_sst_cell<<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
-    k_sst_flux<<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
-    k_sst_total<<<nb(d.nc, 256), 256, 0, L.stream>>>(d, 0);
+    k_sst_face<double><<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
+    k_sst_cell<double><<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
+    k_sst_flux<double><<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
+    k_sst_total<double><<<nb(d.nc, 256), 256, 0, L.stream>>>(d, 0);
     *L.counter += 4;
 }
 
 void launch_sst_stage(const DevArrays& d, const LaunchCfg& L, int stage) {
-    if (stage == 0) k_sst_face<<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
-    else if (stage == 1) k_sst_cell<<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
-    else if (stage == 2) k_sst_flux<<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
-    else k_sst_total<<<nb(d.nc, 256), 256, 0, L.stream>>>(d, 1);
+    if (d.ffsst) {  // MIXFF: the model in float-float on its copies of k, omega, mu_t and the wall distance
+        if (stage == 0) {
+            k_sst_to_ff<<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
+            *L.counter += 1;
+        }
+        if (stage == 0) k_sst_face<ff><<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
+        else if (stage == 1) k_sst_cell<ff><<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
+        else if (stage == 2) k_sst_flux<ff><<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
+        else k_sst_total<ff><<<nb(d.nc, 256), 256, 0, L.stream>>>(d, 1);
+    } else {
+        if (stage == 0) k_sst_face<double><<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
+        else if (stage == 1) k_sst_cell<double><<<nb(d.nc, 256), 256, 0, L.stream>>>(d);
+        else if (stage == 2) k_sst_flux<double><<<nb(d.nf, 256), 256, 0, L.stream>>>(d);
+        else k_sst_total<double><<<nb(d.nc, 256), 256, 0, L.stream>>>(d, 1);
+    }
     *L.counter += 1;
 }
 
