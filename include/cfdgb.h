@@ -164,7 +164,9 @@ typedef struct {
                            each slot's updated face velocity from the flow's
                            sweep as it is formed; 1 = the turbulence sweeps run
                            after the flow's.  Both give the same bits        */
-    int reserved[3];
+    int sst_sweep_share; /* overlapped sweeps: percent of the launch's blocks that
+                            run the turbulence sweep (0 = 50; 10..90)         */
+    int reserved[2];
 } cfd_params_t;
 
 /* ---- errors -------------------------------------------------------------- */

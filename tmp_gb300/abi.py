@@ -53,7 +53,7 @@ class Params(C.Structure):
     _fields_ = [("flow", C.c_int), ("advance", C.c_int), ("precision", C.c_int), ("first_order", C.c_int),
                 ("cfl", C.c_double), ("sweep_mode", C.c_int), ("sweep_blocks_per_sm", C.c_int),
                 ("sweep_poll_ns", C.c_int), ("sweep_threads", C.c_int), ("sst_sequential", C.c_int),
-                ("reserved", C.c_int * 3)]
+                ("sst_sweep_share", C.c_int), ("reserved", C.c_int * 2)]
 
 
 _lib = None
@@ -242,14 +242,14 @@ class Case:
     def __init__(self, meshes: Sequence[Mesh], freestreams: Sequence[dict], flow: int, advance: int,
                  precision: int = PREC_FP64, cfl: float = 1.0, first_order: bool = False, stream: int | None = None,
                  sweep_mode: int = 0, sweep_blocks_per_sm: int = 0, sweep_poll_ns: int = 0, sweep_threads: int = 0,
-                 sst_sequential: bool = False):
+                 sst_sequential: bool = False, sst_sweep_share: int = 0):
         self.meshes = list(meshes)
         arr = (C.c_void_p * len(meshes))(*[m.h.value for m in meshes])
         fs = (Freestream * len(meshes))(*[Freestream(f["mach"], f.get("aoa_deg", 0.0), f.get("reynolds", 1.0),
                                                      f.get("density", 1.225), f.get("pressure", 101325.0))
                                           for f in freestreams])
         p = Params(flow, advance, precision, int(first_order), float(cfl), int(sweep_mode), int(sweep_blocks_per_sm),
-                   int(sweep_poll_ns), int(sweep_threads), int(bool(sst_sequential)))
+                   int(sweep_poll_ns), int(sweep_threads), int(bool(sst_sequential)), int(sst_sweep_share))
         h = C.c_void_p()
         check(lib().cfd_case_create(arr, len(meshes), fs, C.byref(p), C.c_void_p(stream) if stream else None,
                                     C.byref(h)))

@@ -167,10 +167,12 @@ static void set_sweep_shape(cfd_case_s* c, int bpsm, int threads, int pf = -1) {
     c->d.flow_grid = sweep_flow_max_grid(c->p.precision != CFD_PREC_FP64, bpsm, threads, c->d.flow_pf != 0);
     if (c->turb()) {
         c->d.sst_grid = sst_sweep_max_grid(bpsm > 0 ? bpsm : 2, threads, c->d.flow_pf != 0);
-        // the flow's and the turbulence sweep's blocks share one co-resident grid, half each
+        // the flow's and the turbulence sweep's blocks share one co-resident grid (by default half each)
         c->d.cpl_grid = sweep_coupled_max_grid(c->p.precision != CFD_PREC_FP64, bpsm > 0 ? bpsm : 2, threads,
                                                c->d.flow_pf != 0);
-        c->d.cpl_nflow = c->d.cpl_grid / 2;
+        const int share = c->p.sst_sweep_share >= 10 && c->p.sst_sweep_share <= 90 ? c->p.sst_sweep_share : 50;
+        int nflow = (int)((long long)c->d.cpl_grid * (100 - share) / 100);
+        c->d.cpl_nflow = nflow < 1 ? 1 : (nflow > c->d.cpl_grid - 1 ? c->d.cpl_grid - 1 : nflow);
     }
 }
 static void sst_freestream(cfd_case_s* c);
