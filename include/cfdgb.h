@@ -43,8 +43,10 @@ extern "C" {
                                  reference never runs): mu + mu_t in the
                                  viscous flux and radii, dt = CFL vol /
                                  (spec_c + 4 spec_v), a two-equation
-                                 turbulence sweep after the flow's.  LU-SGS
-                                 with the FP64, MIXED or MIXFF form        */
+                                 turbulence sweep beside or after the
+                                 flow's.  LU-SGS with the FP64, MIXED or
+                                 MIXFF form (MIXFF: the model's residual
+                                 passes in float-float as well)            */
 #define CFD_ADV_RK5       0   /* RungeKuttaStrategy(5)                     */
 #define CFD_ADV_LUSGS     1   /* LUSGSIntegrator                           */
 #define CFD_PREC_FP64     0   /* plain: every kernel in binary64           */
@@ -63,7 +65,7 @@ extern "C" {
                                  the binary32 pipe) summed per cell into a
                                  binary64 residual; converges to the
                                  binary64 solution within ~1e-14 relative.
-                                 LU-SGS sweep modes 0, 3, 4, 5 only; no SST */
+                                 LU-SGS sweep modes 0, 3, 4, 5, 6 only    */
 
 /* Field selectors for cfd_get_field / cfd_put_field.  Cell fields use the
  * reference's interleaved layout [NEQU*cell + eq]; face fields [4*face + eq]. */
@@ -153,7 +155,9 @@ typedef struct {
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
                                 the occupancy limit)                             */
     int sweep_poll_ns; /* dataflow sweep: pause between polls of a neighbour's
-                          increment in ns (__nanosleep; 0 = spin)                */
+                          increment in ns (__nanosleep; 0 = spin); negative, in
+                          the binary32 round-robin and turbulence sweeps: keep
+                          two polls in flight, issued -n clock cycles apart   */
     int sweep_threads; /* round-robin dataflow sweeps (modes 0, 3, 4 and the
                           SST turbulence sweeps): threads per block, 64, 128 or
                           256 (0 = 256); fewer warps per block put fewer cells

@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(256) k_sweep_pair64(int npos, const int* __res
                     atomicOr(err, ERR_TIMEOUT);
                     break;
                 }
-                if (poll_ns) __nanosleep(poll_ns);
+                if (poll_ns > 0) __nanosleep(poll_ns);
             }
             dw[0] = a.x; dw[1] = a.y; dw[2] = b.x; dw[3] = b.y;
         }
@@ -895,7 +895,7 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
                         gave_up = true;
                         break;
                     }
-                    if (poll_ns) __nanosleep(poll_ns);
+                    if (poll_ns > 0) __nanosleep(poll_ns);
                 }
             }
         }

@@ -560,7 +560,7 @@ __device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __
                         v = __ldcv(d.sstVnp + t);
                         if (!sent_t(v)) break;
                         if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
-                        if (d.poll_ns) __nanosleep(d.poll_ns);
+                        if (d.poll_ns > 0) __nanosleep(d.poll_ns);
                     }
                     cur.vnp = v;
                 } else {
@@ -569,7 +569,7 @@ __device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __
                         v = __ldcv(d.sstVnpf + t);
                         if (!sent_tf(v)) break;
                         if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
-                        if (d.poll_ns) __nanosleep(d.poll_ns);
+                        if (d.poll_ns > 0) __nanosleep(d.poll_ns);
                     }
                     cur.vnp = v;
                 }
@@ -582,17 +582,32 @@ __device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __
                     a = __ldcv(qd);
                     if (!sent_t(a.x) && !sent_t(a.y)) break;
                     if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
-                    if (d.poll_ns) __nanosleep(d.poll_ns);
+                    if (d.poll_ns > 0) __nanosleep(d.poll_ns);
                 }
                 dt = (T)(m ? a.y : a.x);
             } else {
                 const float2* qf = (FWD ? d.sstDW1f : d.sstDWf) + cur.j;
                 float2 a;
-                while (true) {
+                if (d.poll_ns >= 0) {
+                    while (true) {
+                        a = __ldcv(qf);
+                        if (!sent_tf(a.x) && !sent_tf(a.y)) break;
+                        if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
+                        if (d.poll_ns > 0) __nanosleep(d.poll_ns);
+                    }
+                } else {  // two loads in flight, as the flow's binary32 sweep polls
                     a = __ldcv(qf);
-                    if (!sent_tf(a.x) && !sent_tf(a.y)) break;
-                    if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
-                    if (d.poll_ns) __nanosleep(d.poll_ns);
+                    spin_cycles(-d.poll_ns);
+                    float2 b = __ldcv(qf);
+                    for (;; it++) {
+                        if (!sent_tf(a.x) && !sent_tf(a.y)) break;
+                        if (it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
+                        spin_cycles(-d.poll_ns);
+                        a = __ldcv(qf);
+                        if (!sent_tf(b.x) && !sent_tf(b.y)) { a = b; break; }
+                        spin_cycles(-d.poll_ns);
+                        b = __ldcv(qf);
+                    }
                 }
                 dt = (T)(m ? a.y : a.x);
             }
