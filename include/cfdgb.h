@@ -155,9 +155,7 @@ typedef struct {
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
                                 the occupancy limit)                             */
     int sweep_poll_ns; /* dataflow sweep: pause between polls of a neighbour's
-                          increment in ns (__nanosleep; 0 = spin); negative, in
-                          the binary32 round-robin and turbulence sweeps: keep
-                          two polls in flight, issued -n clock cycles apart   */
+                          increment in ns (__nanosleep; 0 = spin)                */
     int sweep_threads; /* round-robin dataflow sweeps (modes 0, 3, 4 and the
                           SST turbulence sweeps): threads per block, 64, 128 or
                           256 (0 = 256); fewer warps per block put fewer cells

@@ -856,7 +856,7 @@ int cfd_case_create(const cfd_mesh_t* meshes, int nmesh, const cfd_freestream_t*
                 dalloc(&d.dW1f, nc); dalloc(&d.dWf, nc);
             }
             set_sweep_shape(c, P.sweep_blocks_per_sm, P.sweep_threads);
-            d.poll_ns = P.sweep_poll_ns < -10000 ? -10000 : (P.sweep_poll_ns > 10000 ? 10000 : P.sweep_poll_ns);
+            d.poll_ns = P.sweep_poll_ns < 0 ? 0 : (P.sweep_poll_ns > 10000 ? 10000 : P.sweep_poll_ns);
         }
         if (P.advance == CFD_ADV_LUSGS) {  // for the chain sweep schedule, built on first use
             c->h_cface = cface;

@@ -588,26 +588,11 @@ __device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __
             } else {
                 const float2* qf = (FWD ? d.sstDW1f : d.sstDWf) + cur.j;
                 float2 a;
-                if (d.poll_ns >= 0) {
-                    while (true) {
-                        a = __ldcv(qf);
-                        if (!sent_tf(a.x) && !sent_tf(a.y)) break;
-                        if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
-                        if (d.poll_ns > 0) __nanosleep(d.poll_ns);
-                    }
-                } else {  // two loads in flight, as the flow's binary32 sweep polls
+                while (true) {
                     a = __ldcv(qf);
-                    spin_cycles(-d.poll_ns);
-                    float2 b = __ldcv(qf);
-                    for (;; it++) {
-                        if (!sent_tf(a.x) && !sent_tf(a.y)) break;
-                        if (it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
-                        spin_cycles(-d.poll_ns);
-                        a = __ldcv(qf);
-                        if (!sent_tf(b.x) && !sent_tf(b.y)) { a = b; break; }
-                        spin_cycles(-d.poll_ns);
-                        b = __ldcv(qf);
-                    }
+                    if (!sent_tf(a.x) && !sent_tf(a.y)) break;
+                    if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
+                    if (d.poll_ns > 0) __nanosleep(d.poll_ns);
                 }
                 dt = (T)(m ? a.y : a.x);
             }

@@ -26,32 +26,6 @@ __device__ __forceinline__ bool is_sentinel_f(float x) { return __float_as_uint(
 __device__ __forceinline__ bool ready_f4(const float4& v) {
     return !is_sentinel_f(v.x) && !is_sentinel_f(v.y) && !is_sentinel_f(v.z) && !is_sentinel_f(v.w);
 }
-__device__ __forceinline__ void spin_cycles(long long n) {
-    const long long t0 = clock64();
-    while (clock64() - t0 < n) {
-    }
-}
-// Polling with two loads in flight, issued `gap` cycles apart: the wait ends
-// within about half a round trip of the value reaching L2 instead of a whole
-// one (each load's result is only used after the next load has been issued).
-// Bounded like the single poll.
-__device__ __forceinline__ float4 poll2_f4(const float4* q, int gap, unsigned* err) {
-    float4 a = __ldcv(q);
-    spin_cycles(gap);
-    float4 b = __ldcv(q);
-    for (long long it = 0;; it++) {
-        if (ready_f4(a)) return a;
-        if (it > kSpinLimit) {
-            atomicOr(err, ERR_TIMEOUT);
-            return a;
-        }
-        spin_cycles(gap);
-        a = __ldcv(q);
-        if (ready_f4(b)) return b;
-        spin_cycles(gap);
-        b = __ldcv(q);
-    }
-}
 
 template <bool FWD, bool PF>
 __device__ __forceinline__ void sweep_flow_body(int bid, int B, int nc, const int* __restrict__ order,
@@ -284,19 +258,15 @@ __device__ __forceinline__ void sweep_flow32_body(int bid, int B, int npos, cons
         float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
         if (cur.use) {
             const float4* qf = (FWD ? dW1f : dWf) + cur.j;
-            if (poll_ns >= 0) {
-                long long it = 0;
-                while (true) {
-                    dw = __ldcv(qf);
-                    if (ready_f4(dw)) break;
-                    if (++it > kSpinLimit) {
-                        atomicOr(err, ERR_TIMEOUT);
-                        break;
-                    }
-                    if (poll_ns > 0) __nanosleep(poll_ns);
+            long long it = 0;
+            while (true) {
+                dw = __ldcv(qf);
+                if (ready_f4(dw)) break;
+                if (++it > kSpinLimit) {
+                    atomicOr(err, ERR_TIMEOUT);
+                    break;
                 }
-            } else {
-                dw = poll2_f4(qf, -poll_ns, err);
+                if (poll_ns > 0) __nanosleep(poll_ns);
             }
         }
         __syncwarp(mask);
