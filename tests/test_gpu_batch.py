@@ -53,6 +53,29 @@ def test_uneven_batch_packed_matches_separate(precision, sweep_mode, flow):
     packed.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixff"])
+def test_uneven_batch_sst_packed_matches_separate(precision):
+    """The batch's SST half: packed SST meshes (the model's per-mesh freestream turbulence, wall distance per mesh,
+    the turbulence sweeps over the merged levels, overlapped with the flow's) give each mesh's separate bits."""
+    from tmp_gb300 import abi
+
+    prec = dict(fp64=abi.PREC_FP64, mixed=abi.PREC_MIXED, mixff=abi.PREC_MIXFF)[precision]
+    _, meshes, fs = _batch(n=6, seed=91)
+    packed = abi.Case(meshes, fs, abi.FLOW_SST, abi.ADV_LUSGS, prec, cfl=10.0)
+    packed.init_freestream()
+    packed.step_graph(4)
+    packed.sync()
+    for k, (m, f) in enumerate(zip(meshes, fs)):
+        single = abi.Case([m], [f], abi.FLOW_SST, abi.ADV_LUSGS, prec, cfl=10.0)
+        single.init_freestream()
+        single.step_graph(4)
+        single.sync()
+        for name in ("U", "SST_T", "SST_MUT"):
+            np.testing.assert_array_equal(packed.get(name, mesh=k), single.get(name), err_msg=f"mesh {k} {name}")
+        single.close()
+    packed.close()
+
+
 def test_uneven_batch_learned_packed_matches_separate():
     """With the learned relaxation attached, each mesh's pooled factor comes
     from its own sampled cells only.  The relaxation is attached after 30 plain

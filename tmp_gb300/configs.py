@@ -106,7 +106,8 @@ def c5_cases(n: int = 256, seed: int = 5005, lo: int = 5_000, hi: int = 200_000)
     resolution that gives a size follows the generator's own scaling (cells
     ~ 2.8 nbody^2 for the cylinder recipe, ~ 6.1 nbody^2 for the airfoil, with
     16 quad layers and the triangle fill to 30 body lengths).  The first half
-    of the cases (in index order) is Euler, the second half viscous."""
+    of the cases (in index order) is Euler, the second half viscous (the
+    batch leg runs it with the SST k-omega model)."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
