@@ -198,6 +198,23 @@ def ties_cases(rng: np.random.Generator):
                 out["ct_mesh_xy"] = m.xy
                 out["ct_mesh_verts"] = m.cell_verts
                 out["ct_mesh_nvert"] = m.cell_nvert
+            # tiny query sets: one point and two points take findOBB's special cases (an axis box of
+            # half-width 1e-3, or the reference's max(1e-3, d) * 0.5 that halves only the second operand)
+            for k, sel in enumerate(([0], [1, 2], [3, 4, 5])):
+                tp = np.asarray(xy[rng.choice(len(xy), len(sel), replace=False)], np.float64)
+                tg = np.ones(len(tp), np.int32)
+                tr = np.ones(len(tp))
+                tu = np.zeros(m.ncell, np.int32)
+                with open(td / "p.bin", "wb") as f:
+                    np.array([len(tp)], np.int32).tofile(f)
+                    tp.tofile(f)
+                    tg.tofile(f)
+                    tr.tofile(f)
+                    tu.tofile(f)
+                _run("search2", td / "m.bin", td / "p.bin", td / "s.out", cwd=td)
+                raw = (td / "s.out").read_bytes()
+                out[f"{name}_tiny{k}_pts"] = tp
+                out[f"{name}_tiny{k}_donor"] = np.frombuffer(raw[:4 * len(tp)], np.int32)
     np.savez_compressed(HERE / "overset_ties.npz", **out)
     print(f"wrote {HERE / 'overset_ties.npz'}: " + ", ".join(f"{k}: {len(out[k + '_pts'])} points"
                                                            for k in ("mx", "om", "ct")))

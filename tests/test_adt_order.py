@@ -145,6 +145,25 @@ def test_tree_order_ties_refusals_and_coincident_points(harness, tmp_path, name)
 
 
 @pytest.mark.parametrize("name", ["mx", "om", "ct"])
+def test_tree_order_tiny_query_sets(harness, tmp_path, name):
+    """One, two and three query points: findOBB's special cases for one and two points."""
+    t = np.load(GOLDEN / "overset_ties.npz")
+    if name == "ct":
+        xy, cv, nv = t["ct_mesh_xy"], t["ct_mesh_verts"], t["ct_mesh_nvert"]
+    else:
+        m = _golden_meshes()[name]
+        xy, cv, nv = m.xy, m.cell_verts, m.cell_nvert
+    for k in range(3):
+        pts = t[f"{name}_tiny{k}_pts"]
+        n = len(pts)
+        rank, xtag, _ = run(harness, tmp_path, xy, cv, nv, pts, np.ones(n), np.ones(n))
+        donor = select(xy, cv, nv, pts, rank, np.zeros(len(nv), np.uint8), xtag)
+        assert np.array_equal(donor, t[f"{name}_tiny{k}_donor"]), k
+        d, _, _ = oracle.adt_search(xy, cv, nv, pts)
+        assert np.array_equal(d, t[f"{name}_tiny{k}_donor"]), k
+
+
+@pytest.mark.parametrize("name", ["mx", "om", "ct"])
 def test_oracle_walk_matches_reference(name):
     """The oracle's literal restatement of the tree walk (oracle/cfd_oracle.c, orc_adt_search)."""
     t = np.load(GOLDEN / "overset_ties.npz")

@@ -125,6 +125,9 @@ def test_search_ties_refusals_and_coincident_points(built_lib, name):
     assert _eq(res, t[f"{name}_res_out"])
     assert _eq(w, _weights_in(topo, pts, d))  # merged points: their own weights in the first point's cell
     assert (xtag != np.arange(len(pts))).sum() > 100
+    for k in range(3):  # one, two and three query points (findOBB's special cases)
+        d, _, _ = blk.search(t[f"{name}_tiny{k}_pts"])
+        assert np.array_equal(d, t[f"{name}_tiny{k}_donor"]), k
 
 
 def test_search_larger_mesh_random_points(built_lib):
