@@ -210,6 +210,7 @@ __device__ __forceinline__ void sweep_flow32_body(int bid, int B, int npos, cons
         float4 w0, g;
         float rA, u, v, vv, p, vn;
         double own, dinv;
+        float ownf, dinvf;  // their binary32 roundings, formed here rather than on the dependence chain
     };
     auto load = [&](long long P, In& x) {
         x.i = order2[2 * P + h];
@@ -233,6 +234,8 @@ __device__ __forceinline__ void sweep_flow32_body(int bid, int B, int npos, cons
             x.own = FWD ? (&R[x.i].x)[m] : (&dW1[x.i].x)[m];
             x.dinv = invD[x.i];
         }
+        x.ownf = (float)x.own;
+        x.dinvf = (float)x.dinv;
         x.w0 = make_float4(1.f, 1.f, 0.f, 0.f);
         x.g = make_float4(0.f, 0.f, 0.f, 0.f);
         x.rA = x.u = x.v = x.vv = x.p = x.vn = 0.f;
@@ -307,8 +310,9 @@ __device__ __forceinline__ void sweep_flow32_body(int bid, int B, int npos, cons
         // published first, in binary32; the binary64 increment (used only by
         // the backward sweep and the update, after this launch) follows off
         // the critical path.
-        const float ownf = (float)cur.own, dinvf = (float)cur.dinv;
-        const float resf = FWD ? (-ownf - dF) * dinvf : ownf - dF * dinvf;
+        const float resf = FWD ? (-cur.ownf - dF) * cur.dinvf : cur.ownf - dF * cur.dinvf;
+        // one 16-byte store (measured faster than each lane storing its own word: readers then
+        // saw partly written records and polled again)
         float f1 = __shfl_sync(mask, resf, base + 1);
         float f2 = __shfl_sync(mask, resf, base + 2);
         float f3 = __shfl_sync(mask, resf, base + 3);
