@@ -166,6 +166,31 @@ def test_overlapped_sweeps_equal_sequential(built_lib, form, mesh_file):
     b.close()
 
 
+@pytest.mark.parametrize("form", ["MIXED", "MIXFF"])
+def test_sst_every_sweep_schedule_same_bits(built_lib, form):
+    """The binary32 flow sweeps give the same bits in every schedule (round-robin, overlapped with the turbulence
+    sweep or not, and the two chain schedules), so the coupled SST step does too."""
+    from tmp_gb300 import abi
+
+    prec = abi_prec(form)
+    ref = None
+    for mode, seq in ((0, False), (0, True), (5, True), (6, True)):
+        mesh = abi.Mesh.load_grd(GOLDEN / "mixed.grd", -1, -2)
+        c = abi.Case([mesh], [dict(mach=0.3, aoa_deg=2.0, reynolds=1e5)], abi.FLOW_SST, abi.ADV_LUSGS, prec,
+                     cfl=5.0, sweep_mode=mode, sst_sequential=seq)
+        abi.sst_set_inflow(c, 0.01, 0.035)
+        c.init_freestream()
+        c.step_graph(25)
+        c.sync()
+        got = [c.get(name) for name in ("U", "SST_T", "SST_MUT")]
+        if ref is None:
+            ref = got
+        else:
+            for a, b, name in zip(got, ref, ("U", "SST_T", "SST_MUT")):
+                np.testing.assert_array_equal(a, b, err_msg=f"mode {mode} sequential {seq} {name}")
+        c.close()
+
+
 def test_overlapped_sweeps_larger_mesh(built_lib):
     """A 49k-cell SST airfoil mesh (hundreds of levels, every block busy): overlapped == sequential, bit for bit."""
     import tempfile
