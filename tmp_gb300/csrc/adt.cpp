@@ -7,6 +7,9 @@
 #include "adt.hpp"
 
 #include <cmath>
+#include <exception>
+#include <mutex>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -18,6 +21,47 @@ constexpr double kBig = 1.0e15;   // BIGVALUE, UniTioga/codetypes.h:52
 constexpr double kTol = 1.0e-10;  // TOL, UniTioga/codetypes.h:54
 constexpr int kParallelSize = 1 << 16;
 constexpr int kParallelDepth = 4;
+
+// Subtree tasks: each runs on a thread of its own when one can be started,
+// else in the caller; an exception thrown in a thread (an allocation that
+// failed) is kept and rethrown by join(), and every thread is joined before
+// the object goes away.
+class Tasks {
+  public:
+    template <class F>
+    void run(bool parallel, F f) {
+        if (parallel) {
+            try {
+                ts_.emplace_back([this, f]() {
+                    try {
+                        f();
+                    } catch (...) {
+                        std::lock_guard<std::mutex> g(mu_);
+                        if (!err_) err_ = std::current_exception();
+                    }
+                });
+                return;
+            } catch (const std::system_error&) {
+                // no thread to be had: run it here
+            }
+        }
+        f();
+    }
+    void join() {
+        for (auto& t : ts_) t.join();
+        ts_.clear();
+        if (err_) std::rethrow_exception(err_);
+    }
+    ~Tasks() {
+        for (auto& t : ts_)
+            if (t.joinable()) t.join();
+    }
+
+  private:
+    std::vector<std::thread> ts_;
+    std::exception_ptr err_;
+    std::mutex mu_;
+};
 
 // One Jacobi sweep set of kaiser() on a symmetric 2x2 matrix held by columns,
 // then the columns scaled to unit length (zero columns stay zero).
@@ -179,9 +223,10 @@ void build(int* node, Elem* e, int nav, int level, int base, int depth) {
         node[e[nleft - 1].id] = base;
         if (nleft > 1) {
             if (nav >= kParallelSize && depth < kParallelDepth) {
-                std::thread left(build, node, e, nleft - 1, level + 1, base + 1, depth + 1);
+                Tasks tasks;
+                tasks.run(true, [=] { build(node, e, nleft - 1, level + 1, base + 1, depth + 1); });
                 build(node, e + nleft, nav - nleft, level + 1, base + nleft, depth + 1);
-                left.join();
+                tasks.join();
                 return;
             }
             build(node, e, nleft - 1, level + 1, base + 1, depth + 1);
@@ -235,16 +280,15 @@ void octree(const double* x, const int* tag, double* res, int* xtag, int* avail,
             std::vector<int> tmp(nav);
             for (int i = 0; i < nav; i++) tmp[start[q[i]] + --cnt[q[i]]] = avail[i];  // each quadrant filled from its end
             for (int i = 0; i < nav; i++) avail[i] = tmp[i];
-            std::vector<std::thread> pool;
+            Tasks tasks;
             for (int j = 0; j < 4; j++) {
                 const int len = start[j + 1] - start[j];
                 if (len <= 0) continue;
-                if (nav >= kParallelSize && depth < kParallelDepth)
-                    pool.emplace_back(octree, x, tag, res, xtag, avail + start[j], len, depth + 1);
-                else
-                    octree(x, tag, res, xtag, avail + start[j], len, depth + 1);
+                int* sub = avail + start[j];
+                tasks.run(nav >= kParallelSize && depth < kParallelDepth,
+                          [=] { octree(x, tag, res, xtag, sub, len, depth + 1); });
             }
-            for (auto& t : pool) t.join();
+            tasks.join();
         }
     }
     if (!leaf) return;

@@ -34,6 +34,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdint>
+#include <exception>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -831,13 +832,20 @@ void search_device(cfd_block_t b, long long n, const double* d_pts, const Search
         unit.assign(n, 1.0);
         res = unit.data();
     }
+    std::exception_ptr hash_err;  // declared before the thread's joiner: it outlives the thread
     struct Joiner {
         std::thread t;
         ~Joiner() {
             if (t.joinable()) t.join();
         }
     } hash;
-    hash.t = std::thread([&] { cfdgb::adt::coincident(n, q.h_pts, tags, res, xtag.data()); });
+    hash.t = std::thread([&] {
+        try {
+            cfdgb::adt::coincident(n, q.h_pts, tags, res, xtag.data());
+        } catch (...) {
+            hash_err = std::current_exception();  // rethrown after the join
+        }
+    });
     const cfdgb::adt::Obb o = cfdgb::adt::find_obb(q.h_pts, n);
     DevBuf<unsigned char> d_cross(b->ncell);
     DevBuf<int> d_rank(b->ncell), d_err(2);  // d_err[1]: some point's donor depends on the tree's order
@@ -867,6 +875,7 @@ void search_device(cfd_block_t b, long long n, const double* d_pts, const Search
         ck(cudaGetLastError(), "k_donor_search");
     }
     hash.t.join();
+    if (hash_err) std::rethrow_exception(hash_err);
     bool merged = false;
     for (long long i = 0; i < n && !merged; i++) merged = xtag[i] != i;
     if (merged) {
