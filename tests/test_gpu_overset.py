@@ -130,6 +130,35 @@ def test_search_ties_refusals_and_coincident_points(built_lib, name):
         assert np.array_equal(d, t[f"{name}_tiny{k}_donor"]), k
 
 
+def test_search_large_sets_coincident_screen(built_lib):
+    """Query sets of 2^16 points or more are screened for coincident pairs on the device before the reference's
+    hash runs: with coincident copies (within 1e-10 in L1, same and other tag) the merges, donors and merged
+    resolutions must be the oracle's; without any, every point keeps its own search."""
+    from tmp_gb300 import abi
+
+    mesh, blk, topo = _blocks(abi)["mx"]
+    xy = topo.xy.reshape(-1, 2)
+    lo, hi = xy.min(0), xy.max(0)
+    rng = np.random.default_rng(17)
+    base = np.concatenate([lo + rng.uniform(-0.02, 1.02, (70000, 2)) * (hi - lo), xy])
+    for with_copies in (True, False):
+        pts = base
+        if with_copies:
+            pick = rng.choice(len(base), 500, replace=False)
+            pts = np.concatenate([base, base[pick] + rng.choice([0.0, 2e-11, -3e-11, 4e-11], (500, 2))])
+        n = len(pts)
+        tags = np.where(rng.random(n) < 0.3, 2, 1).astype(np.int32)
+        res = rng.uniform(0.5, 2.0, n)
+        unacc = (rng.random(topo.ncell) < 0.2).astype(np.uint8)
+        d, _, w, xtag, r = blk.search_ex(pts, tags, res, unacc)
+        od, oxt, orr = oracle.adt_search(topo.xy, topo.cell_verts, topo.cell_nvert, pts, unacc, tags, res)
+        assert np.array_equal(xtag, oxt)
+        assert np.array_equal(d, od)
+        assert _eq(r, orr)
+        merged = int((xtag != np.arange(n)).sum())
+        assert (merged > 100) if with_copies else (merged == 0)
+
+
 def test_search_larger_mesh_random_points(built_lib):
     from tmp_gb300 import abi, meshgen
 

@@ -77,8 +77,8 @@ struct DevArrays {
     double* sstDinv = nullptr;   // [2*nc] 1 / diagonal (the binary32 sweep)
     float2* sstDW1f = nullptr;   // [nc] binary32 copies published by the binary32 sweep
     float2* sstDWf = nullptr;    // [nc]
-    float4* sstSlotf = nullptr;  // [4*nc] binary32 sweep: per (cell, slot) (fc_k, fc_omega, r_A, face length)
-    float* sstVnpf = nullptr;    // [4*nc] binary32 sweep: per (cell, slot) Vn(W_j + dW_j)
+    float4* sstSlotf = nullptr;  // [4*nc] binary32 sweep: per (cell, slot) (0, 0, r_A, face length)
+    float2* sstVnpf = nullptr;   // [4*nc] binary32 sweep: per (cell, slot) Vn(W_j + dW_j) and its change dVn
     float2* sstWf = nullptr;     // [nc] binary32 copy of sstW for that sweep
     ff* sstTq = nullptr;         // [2*nc] MIXFF: float-float copies of k, omega, mu_t and the wall distance
     ff* sstMutq = nullptr;       // [nc]   that the model's float-float passes read

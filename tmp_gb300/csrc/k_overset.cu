@@ -390,6 +390,82 @@ __global__ void k_donor_search(long long n, const double* __restrict__ pts, cons
     if (ambiguous && (ngood > 1 || (ngood == 0 && nrefused > 0))) atomicOr(ambiguous, 1);
 }
 
+// Coincident query points, screened on the device.  The reference's hash
+// (uniquenodes_octree) merges only points closer than TOL in L1 that carry the
+// same tag; where no such pair exists it merges nothing, and the host's octree
+// restatement can be skipped.  The points are sorted by (tag, x, y) - three
+// stable radix passes on order-preserving keys, -0.0 taken as +0.0 - and point
+// i is compared with the next point (the nearest larger y of its tag and x)
+// and with the nearest y of every following x within TOL (of its tag), found
+// by binary search: every pair closer than TOL in L1 is one of those.
+__device__ __forceinline__ unsigned long long order_key(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v == 0.0 ? 0.0 : v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__global__ void k_coinc_keys(long long n, const double* __restrict__ pts, const int* __restrict__ tags, int coord,
+                             const int* __restrict__ perm, unsigned long long* __restrict__ key) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int p = perm[i];
+    key[i] = coord < 2 ? order_key(pts[2 * (size_t)p + coord]) : (unsigned long long)(unsigned)(tags[p] ^ INT_MIN);
+}
+__global__ void k_coinc_iota(long long n, int* __restrict__ perm) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) perm[i] = (int)i;
+}
+__global__ void k_coinc_gather(long long n, const double* __restrict__ pts, const int* __restrict__ tags,
+                               const int* __restrict__ perm, double* __restrict__ sx, double* __restrict__ sy,
+                               int* __restrict__ st) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int p = perm[i];
+    sx[i] = pts[2 * (size_t)p];
+    sy[i] = pts[2 * (size_t)p + 1];
+    st[i] = tags[p];
+}
+__device__ __forceinline__ bool coinc_pair(double x0, double y0, double x1, double y1) {
+    return fabs(x0 - x1) + fabs(y0 - y1) < kTol;
+}
+__global__ void k_coinc_scan(long long n, const double* __restrict__ sx, const double* __restrict__ sy,
+                             const int* __restrict__ st, int* __restrict__ found) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xi = sx[i], yi = sy[i];
+    const int ti = st[i];
+    if (i + 1 < n && st[i + 1] == ti && coinc_pair(xi, yi, sx[i + 1], sy[i + 1])) {
+        atomicOr(found, 1);
+        return;
+    }
+    // end of this tag's run, then the following x groups within TOL
+    long long lo = i + 1, hi = n;  // first index with tag != ti or x > xi
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (st[mid] == ti && !(sx[mid] > xi)) lo = mid + 1;
+        else hi = mid;
+    }
+    long long g = lo;
+    while (g < n && st[g] == ti && sx[g] - xi < kTol) {
+        const double xg = sx[g];
+        long long e = g + 1, h2 = n;  // end of the group of x = xg
+        while (e < h2) {
+            const long long mid = (e + h2) >> 1;
+            if (st[mid] == ti && !(sx[mid] > xg)) e = mid + 1;
+            else h2 = mid;
+        }
+        long long a = g, b = e;  // first y >= yi in [g, e)
+        while (a < b) {
+            const long long mid = (a + b) >> 1;
+            if (sy[mid] < yi) a = mid + 1;
+            else b = mid;
+        }
+        if ((a < e && coinc_pair(xi, yi, xg, sy[a])) || (a > g && coinc_pair(xi, yi, xg, sy[a - 1]))) {
+            atomicOr(found, 1);
+            return;
+        }
+        g = e;
+    }
+}
+
 // A point whose search was merged into an earlier coincident one's takes that
 // point's donor cell (search.cpp:255-262) and its own weights in it.
 __global__ void k_take_coincident(long long n, const int* __restrict__ xtag, const double* __restrict__ pts,
@@ -791,6 +867,9 @@ void read_err(int* d_err, cudaStream_t s, int* h) {
     ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
 }
 
+// below this many query points the host hash is cheaper than the device screen
+constexpr long long kScreenMin = 1 << 16;
+
 template <class T>
 struct DevBuf {  // a device temporary freed on scope exit
     T* p = nullptr;
@@ -811,6 +890,39 @@ struct SearchQuery {
     const unsigned char* d_unacc = nullptr;  // device, per cell (null: every cell may donate)
     int* xtag = nullptr;                     // out (may be null): the point whose search each took
 };
+
+// Whether the coincident-point hash of n device points (tags on the host, null:
+// one tag) can merge anything (see k_coinc_scan).
+bool coincident_possible(long long n, const double* d_pts, const int* tags, cudaStream_t s) {
+    DevBuf<int> d_tags(n), p0(n), p1(n), d_found(1);
+    DevBuf<unsigned long long> k0(n), k1(n);
+    DevBuf<double> sx(n), sy(n);
+    DevBuf<int> st(n);
+    if (tags) ck(cudaMemcpyAsync(d_tags.p, tags, n * sizeof(int), cudaMemcpyHostToDevice, s), "copy");
+    else ck(cudaMemsetAsync(d_tags.p, 0, n * sizeof(int), s), "cudaMemsetAsync");
+    k_coinc_iota<<<blocks_for(n, 256), 256, 0, s>>>(n, p0.p);
+    ck(cudaGetLastError(), "k_coinc_iota");
+    size_t tb = 0;
+    ck(cub::DeviceRadixSort::SortPairs(nullptr, tb, k0.p, k1.p, p0.p, p1.p, (int)n, 0, 64, s), "sort size");
+    DevBuf<unsigned char> tmp(tb);
+    int* cur = p0.p;
+    int* nxt = p1.p;
+    for (int coord : {1, 0, 2}) {  // y, then x, then the tag: stable passes give (tag, x, y) order
+        k_coinc_keys<<<blocks_for(n, 256), 256, 0, s>>>(n, d_pts, d_tags.p, coord, cur, k0.p);
+        ck(cudaGetLastError(), "k_coinc_keys");
+        ck(cub::DeviceRadixSort::SortPairs(tmp.p, tb, k0.p, k1.p, cur, nxt, (int)n, 0, 64, s), "sort");
+        std::swap(cur, nxt);
+    }
+    k_coinc_gather<<<blocks_for(n, 256), 256, 0, s>>>(n, d_pts, d_tags.p, cur, sx.p, sy.p, st.p);
+    ck(cudaGetLastError(), "k_coinc_gather");
+    ck(cudaMemsetAsync(d_found.p, 0, sizeof(int), s), "cudaMemsetAsync");
+    k_coinc_scan<<<blocks_for(n, 256), 256, 0, s>>>(n, sx.p, sy.p, st.p, d_found.p);
+    ck(cudaGetLastError(), "k_coinc_scan");
+    int found = 0;
+    ck(cudaMemcpyAsync(&found, d_found.p, sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    ck(cudaStreamSynchronize(s), "sync");
+    return found != 0;
+}
 
 // Search n points (device d_pts, host copy in q) in block b, as
 // MeshBlock::search does; outputs are device arrays (d_nodes, d_w may be null).
@@ -839,13 +951,18 @@ void search_device(cfd_block_t b, long long n, const double* d_pts, const Search
             if (t.joinable()) t.join();
         }
     } hash;
-    hash.t = std::thread([&] {
-        try {
-            cfdgb::adt::coincident(n, q.h_pts, tags, res, xtag.data());
-        } catch (...) {
-            hash_err = std::current_exception();  // rethrown after the join
-        }
-    });
+    // the reference's hash only where some pair can merge (else xtag is the identity and res is unchanged)
+    if (n < kScreenMin || coincident_possible(n, d_pts, q.tags, s)) {
+        hash.t = std::thread([&] {
+            try {
+                cfdgb::adt::coincident(n, q.h_pts, tags, res, xtag.data());
+            } catch (...) {
+                hash_err = std::current_exception();  // rethrown after the join
+            }
+        });
+    } else {
+        for (long long i = 0; i < n; i++) xtag[i] = (int)i;
+    }
     const cfdgb::adt::Obb o = cfdgb::adt::find_obb(q.h_pts, n);
     DevBuf<unsigned char> d_cross(b->ncell);
     DevBuf<int> d_rank(b->ncell), d_err(2);  // d_err[1]: some point's donor depends on the tree's order
@@ -874,7 +991,7 @@ void search_device(cfd_block_t b, long long n, const double* d_pts, const Search
                                                            d_err.p, nullptr);
         ck(cudaGetLastError(), "k_donor_search");
     }
-    hash.t.join();
+    if (hash.t.joinable()) hash.t.join();
     if (hash_err) std::rethrow_exception(hash_err);
     bool merged = false;
     for (long long i = 0; i < n && !merged; i++) merged = xtag[i] != i;

@@ -429,28 +429,28 @@ __global__ void __launch_bounds__(256) k_sst_sweep_prep32(DevArrays d, int coupl
         d.sstWf[i] = make_float2((float)d.sstW[2 * i], (float)d.sstW[2 * i + 1]);
     }
     const int code = (&d.cface[i].x)[s];
-    float fc0 = 0.f, fc1 = 0.f, rA = 0.f, vnp = 0.f, A = 0.f;
+    float rA = 0.f, vnp = 0.f, dvn = 0.f, A = 0.f;
     if (code != 0) {
         const int f = code > 0 ? code - 1 : -code - 1;
         const int2 e = d.lr[f];
         const int j = code > 0 ? e.y : e.x;
         if (j >= 0) {
             const float4 g = d.fg0f[f];
-            const float4 w0 = d.Wf[j];
             A = g.z;
-            const float u = w0.z / w0.x, v = w0.w / w0.x;
-            const float vn0 = u * g.x + v * g.y;
             if (coupled) {
-                vnp = __uint_as_float(kSentTf);
+                vnp = dvn = __uint_as_float(kSentTf);
             } else {
-                // Vn(W_j + dW_j) as the flow's binary32 sweep forms it (base velocity plus the exact difference)
+                // Vn(W_j + dW_j) and its change as the flow's binary32 sweep forms them (base velocity
+                // plus the exact difference)
+                const float4 w0 = d.Wf[j];
+                const float u = w0.z / w0.x, v = w0.w / w0.x;
+                const float vn0 = u * g.x + v * g.y;
                 const float4 dw = (j < i ? d.dW1f : d.dWf)[j];
                 const float rp = 1.f / (w0.x + dw.x);
                 const float du = (dw.z - u * dw.x) * rp, dv = (dw.w - v * dw.x) * rp;
-                vnp = vn0 + (du * g.x + dv * g.y);
+                dvn = du * g.x + dv * g.y;
+                vnp = vn0 + dvn;
             }
-            fc0 = (float)d.sstW[2 * j] * vn0;
-            fc1 = (float)d.sstW[2 * j + 1] * vn0;
             const d4 ud = ld4(d.U + j);
             const float rho = (float)ud.x, p = (float)ud.y;
             const float vn = (float)ud.z * g.x + (float)ud.w * g.y;
@@ -460,8 +460,8 @@ __global__ void __launch_bounds__(256) k_sst_sweep_prep32(DevArrays d, int coupl
                   sqrtf(d.fvisf[f].z);
         }
     }
-    d.sstSlotf[t] = make_float4(fc0, fc1, rA, A);
-    d.sstVnpf[t] = vnp;
+    d.sstSlotf[t] = make_float4(0.f, 0.f, rA, A);
+    d.sstVnpf[t] = make_float2(vnp, dvn);
 }
 
 // One dataflow launch per direction: one warp per cell, taken in level order
@@ -494,6 +494,7 @@ __device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __
         int4 cf;
         bool use, left;
         T wt, fc, rA, vnp, A;
+        float dvn;  // binary32 form: the exact change of Vn, so the flux change needs no cancelling difference
         double own, dd;
         float ownf, ddf;
     };
@@ -521,6 +522,7 @@ __device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __
         x.ownf = (float)x.own;
         x.ddf = (float)x.dd;
         x.wt = x.fc = x.rA = x.vnp = x.A = T(0);
+        x.dvn = 0.f;
         if (x.use) {
             const size_t t = (size_t)x.i * 4 + s;
             if constexpr (std::is_same<T, double>::value) {
@@ -533,9 +535,12 @@ __device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __
                 const float4 sl = d.sstSlotf[t];
                 const float2 wt = d.sstWf[x.j];
                 x.wt = m ? wt.y : wt.x;
-                x.fc = m ? sl.y : sl.x;
                 x.rA = sl.z;
-                if (!CPL) x.vnp = d.sstVnpf[t];
+                if (!CPL) {
+                    const float2 vv = d.sstVnpf[t];
+                    x.vnp = vv.x;
+                    x.dvn = vv.y;
+                }
                 x.A = sl.w;
             }
         }
@@ -564,14 +569,15 @@ __device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __
                     }
                     cur.vnp = v;
                 } else {
-                    float v;
+                    float2 v;
                     while (true) {
                         v = __ldcv(d.sstVnpf + t);
-                        if (!sent_tf(v)) break;
+                        if (!sent_tf(v.x) && !sent_tf(v.y)) break;
                         if (++it > kSpinT) { atomicOr(d.err, ERR_TIMEOUT); break; }
                         if (d.poll_ns > 0) __nanosleep(d.poll_ns);
                     }
-                    cur.vnp = v;
+                    cur.vnp = v.x;
+                    cur.dvn = v.y;
                 }
                 it = 0;
             }
@@ -596,8 +602,15 @@ __device__ __forceinline__ void sst_sweep_body(const DevArrays& d, const int* __
                 }
                 dt = (T)(m ? a.y : a.x);
             }
-            const T fcp = (cur.wt + dt) * cur.vnp;
-            const T dfc = cur.left ? (fcp - cur.fc) : (cur.fc - fcp);
+            T dfc;
+            if constexpr (std::is_same<T, double>::value) {
+                const T fcp = (cur.wt + dt) * cur.vnp;
+                dfc = cur.left ? (fcp - cur.fc) : (cur.fc - fcp);
+            } else {
+                // (W_t + dW_t) Vn' - W_t Vn = W_t dVn + dW_t Vn': no difference of nearly equal products
+                const T ch = cur.wt * cur.dvn + dt * cur.vnp;
+                dfc = cur.left ? ch : -ch;
+            }
             DF = T(0.5) * (dfc - cur.rA * dt) * cur.A;
         }
         __syncwarp();

@@ -5,7 +5,8 @@
 // grid, the flow on blocks [0, B) and the turbulence on the rest, each block
 // numbered within its part (bid).  vnp_out (may be null) receives, per
 // (cell, face slot) with a contributing neighbour j, Vn(W_j + dW_j): the
-// updated normal velocity the turbulence sweep needs for the same slot.
+// updated normal velocity the turbulence sweep needs for the same slot (the
+// binary32 form also its exact change Vn(W_j + dW_j) - Vn(W_j)).
 #pragma once
 
 #include "case.hpp"
@@ -183,7 +184,7 @@ __device__ __forceinline__ void sweep_flow32_body(int bid, int B, int npos, cons
                                                       const float* __restrict__ swraf,
                                                       const d4* __restrict__ R, const double* __restrict__ invD,
                                                       d4* dW1, d4* dW, float4* dW1f, float4* dWf, unsigned* err,
-                                                      int poll_ns, float* vnp_out) {
+                                                      int poll_ns, float2* vnp_out) {
     const float GM1 = 1.4f - 1.0f;
     const int lane = threadIdx.x & 31;
     const int h = lane >> 4, base = lane & 16;
@@ -288,8 +289,9 @@ __device__ __forceinline__ void sweep_flow32_body(int bid, int B, int npos, cons
         const float dp = GM1 * (d1 - 0.5f * (d0 * (vv + dq) + rho * dq));
         const float dvn = du * g.x + dv * g.y;
         const float vnp = vn + dvn;
-        // Vn(W_j + dW_j) on this face is the turbulence sweep's input for the same (cell, slot)
-        if (vnp_out && cur.use && m == 0) __stcg(vnp_out + (size_t)cur.i * 4 + s, vnp);
+        // Vn(W_j + dW_j) on this face and its exact change are the turbulence sweep's input for the same
+        // (cell, slot)
+        if (vnp_out && cur.use && m == 0) __stcg(vnp_out + (size_t)cur.i * 4 + s, make_float2(vnp, dvn));
         const float dfm = m == 0 ? d2 * g.x + d3 * g.y
                         : m == 1 ? (d1 + dp) * vnp + (E + p) * dvn
                         : m == 2 ? d2 * vnp + mx * dvn + dp * g.x
