@@ -181,3 +181,68 @@ def test_oracle_walk_matches_reference(name):
     if name != "ct":
         d, _, _ = oracle.adt_search(xy, cv, nv, ov[f"s_{name}_pts"])
         assert np.array_equal(d, ov[f"s_{name}_donor"])
+
+
+def _screen(pts, tags, tol=TOL):
+    """The device screen's logic (k_coinc_scan) on the host: sort by (tag, x, y); each point against its
+    successor and against the nearest y of every following x within tol of its tag."""
+    x = pts[:, 0] + 0.0  # -0.0 as +0.0
+    y = pts[:, 1]
+    order = np.lexsort((y, x, tags))
+    sx, sy, st = x[order], y[order], tags[order]
+    n = len(sx)
+    for i in range(n):
+        if i + 1 < n and st[i + 1] == st[i] and abs(sx[i] - sx[i + 1]) + abs(sy[i] - sy[i + 1]) < tol:
+            return True
+        run = np.flatnonzero(st == st[i])
+        lo, hi = run[0], run[-1] + 1
+        g = lo + np.searchsorted(sx[lo:hi], sx[i], side="right")
+        while g < hi and sx[g] - sx[i] < tol:
+            e = lo + np.searchsorted(sx[lo:hi], sx[g], side="right")
+            a = g + np.searchsorted(sy[g:e], sy[i], side="left")
+            for k in (a, a - 1):
+                if g <= k < e and abs(sx[i] - sx[k]) + abs(sy[i] - sy[k]) < tol:
+                    return True
+            g = e
+    return False
+
+
+def _brute(pts, tags, tol=TOL):
+    n = len(pts)
+    for i in range(n):
+        d = np.abs(pts[i + 1:] - pts[i]).sum(1)
+        if np.any((d < tol) & (tags[i + 1:] == tags[i])):
+            return True
+    return False
+
+
+def test_coincident_screen_logic():
+    """The device screen for coincident query points (k_overset.cu, k_coinc_scan) finds a pair closer than TOL
+    in L1 with one tag exactly when one exists: its logic, restated in numpy, against all pairs on sets built to
+    defeat it (whole columns of equal x, x values within TOL of each other, signed zeros, pairs across tags)."""
+    rng = np.random.default_rng(5)
+    positives = 0
+    for trial in range(100):
+        kind = trial % 5
+        if kind == 0:  # a Cartesian lattice (columns of equal x) plus a few stray points
+            g = np.stack(np.meshgrid(np.arange(12) * 0.1, np.arange(9) * 0.1), -1).reshape(-1, 2)
+            pts = np.concatenate([g, rng.uniform(0, 1, (20, 2))])
+        elif kind in (1, 2):  # columns whose x differ by less than TOL, sharing (1) or shifting (2) their y values
+            cols = [0.5, 0.5 + 4e-11, 0.5 + 2e-10]
+            ys = np.arange(10) * 0.07
+            pts = np.concatenate([np.stack([np.full(10, c), ys + (7e-11 * k if kind == 2 else 0.0)], 1)
+                                  for k, c in enumerate(cols)])
+        elif kind == 3:  # signed zeros
+            pts = np.stack([np.where(rng.random(40) < 0.5, -0.0, 0.0), rng.uniform(-1, 1, 40)], 1)
+        else:
+            pts = rng.uniform(-1, 1, (60, 2))
+        tags = rng.integers(1, 3, len(pts)).astype(np.int32)
+        if trial % 3 == 0:  # plant one near-coincident pair, sometimes across tags only
+            i, j = rng.choice(len(pts), 2, replace=False)
+            pts[j] = pts[i] + rng.choice([0.0, 3e-11, -4e-11], 2)
+            if trial % 2:
+                tags[j] = 3 - tags[i]
+        want = _brute(pts, tags)
+        positives += want
+        assert _screen(pts, tags) == want, trial
+    assert 20 <= positives <= 80
