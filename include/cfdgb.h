@@ -149,8 +149,9 @@ typedef struct {
                           four consecutive lists in one block (one per SM
                           sub-partition), a slot whose producer runs in the
                           same block waiting on a shared-memory table instead
-                          of global memory (without the table when it would
-                          not leave the grid co-resident).
+                          of global memory (the table capped to the block's
+                          first positions when the whole range would not
+                          leave the grid co-resident).
                           All modes give the same bits */
     int sweep_blocks_per_sm; /* dataflow sweep residency (0 = default 2; capped at
                                 the occupancy limit)                             */
@@ -168,7 +169,11 @@ typedef struct {
                            after the flow's.  Both give the same bits        */
     int sst_sweep_share; /* overlapped sweeps: percent of the launch's blocks that
                             run the turbulence sweep (0 = 50; 10..90)         */
-    int reserved[2];
+    int chain_table_cap; /* sweep mode 6: at most this many shared-memory
+                            hand-off entries per block, covering the block's
+                            first positions (0 = the whole range, or the
+                            largest count that keeps the grid co-resident)   */
+    int reserved[1];
 } cfd_params_t;
 
 /* ---- errors -------------------------------------------------------------- */
@@ -283,13 +288,15 @@ int cfd_autotune(cfd_case_t c, int reps, int* best_blocks_per_sm, double* best_m
  * for one mesh, as a case holding that mesh builds it (no reference
  * counterpart; needs no GPU).  forward: 1 forward sweep, 0 backward; nlists:
  * warps of the launch (a multiple of 8); local: mode 6's block-local list
- * numbering; table: encode same-block dependencies as shared-memory table
- * entries.  Outputs: hptr[nlists+1] each list's range of positions;
- * cells[2*ncell] per position (cell, bits 2s..2s+1 = 1/2 when slot s waits
- * for the list's previous cell / the one before); rec[8*ncell] per position
- * and face slot (neighbour waited for or -1, signed face code); jenc[4*ncell]
- * the dependency as the sweep reads it (-1 none, -2/-3 registers, -4-t table
- * entry t, else the cell id); *table_entries the table's entries per block. */
+ * numbering; table: 0 no shared-memory table, else its cap in entries per
+ * block (INT_MAX: the block's whole range) -- a dependency on a producer of
+ * the same block at a position below the cap is encoded as a table entry.
+ * Outputs: hptr[nlists+1] each list's range of positions; cells[2*ncell]
+ * per position (cell, bits 2s..2s+1 = 1/2 when slot s waits for the list's
+ * previous cell / the one before); rec[8*ncell] per position and face slot
+ * (neighbour waited for or -1, signed face code); jenc[4*ncell] the
+ * dependency as the sweep reads it (-1 none, -2/-3 registers, -4-t table entry
+ * t, else the cell id); *table_entries the table's entries per block. */
 int cfd_chain_schedule(cfd_mesh_t mesh, int forward, int nlists, int local, int table, int* hptr,
                        int* cells, int* rec, int* jenc, int* table_entries);
 /* The case's current LU-SGS schedule: sweep_mode, blocks per SM, threads per

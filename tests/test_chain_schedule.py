@@ -11,7 +11,8 @@ from deadlock rest on.
 * a slot marked "registers" waits for the list's previous cell or the one
   before, and a slot encoded as a shared-memory table entry waits for a cell
   of the same block at exactly that entry (and every such same-block
-  dependency is encoded so when the table is on); the entries fit the table.
+  dependency whose producer sits below the table's cap is encoded so when the
+  table is on); the entries fit the table.
 """
 from __future__ import annotations
 
@@ -69,7 +70,8 @@ def _face_codes_and_deps(mesh, fwd):
 
 @pytest.mark.parametrize("fwd", [True, False])
 @pytest.mark.parametrize("nlists,local,table", [(8, False, False), (64, False, False), (64, True, False),
-                                               (64, True, True), (456 * 8, True, True)])
+                                               (64, True, True), (456 * 8, True, True), (64, True, 97),
+                                               (16, True, 300)])
 def test_chain_schedule_invariants(built_lib, fwd, nlists, local, table):
     for name, mesh in meshes():
         nc = mesh.ncell
@@ -104,15 +106,17 @@ def test_chain_schedule_invariants(built_lib, fwd, nlists, local, table):
             else:
                 pj = pos[jj]
                 same_block = lst[pj] // 8 == h // 8
-                if table and local and same_block:
+                rel = pj - hptr[8 * (h // 8)]
+                if table is not False and local and same_block and rel < tbl:
                     t = -4 - e
-                    assert e <= -4 and t == pj - hptr[8 * (h // 8)] and 0 <= t < tbl, (name, q, s)
+                    assert e <= -4 and t == rel and 0 <= t < tbl, (name, q, s)
                 else:
                     assert e == jj, (name, q, s)
         assert np.all(jenc[~has] == -1), name
-        if local and table:
+        if local and table is not False:
             blocks = hptr[8::8] - hptr[:-1:8]
-            assert tbl == blocks.max(), name
+            cap = blocks.max() if table is True else min(blocks.max(), table)
+            assert tbl == cap, name
         else:
             assert tbl == 0, name
 

@@ -333,7 +333,9 @@ def test_fast_sweep_chain_schedule_bitwise(prec, bpsm):
     lists consecutive and same-block dependencies handed over in shared
     memory) give the same bits as the default dataflow sweep, on the fixture mesh and on a cylinder mesh of ~25k cells
     whose quad rows form long chains, at two grid sizes (two schedules), both
-    through plain steps and through the graph-captured step."""
+    through plain steps and through the graph-captured step.  Mode 6 also runs
+    with its table capped to a block's first 5 and 24 positions (the later
+    producers hand off through global memory only)."""
     from tmp_gb300 import abi, learn
 
     c, g = manifest()["mixed_lam_lusgs"], golden("mixed_lam_lusgs")
@@ -344,9 +346,9 @@ def test_fast_sweep_chain_schedule_bitwise(prec, bpsm):
     fs_cyl = dict(mach=spec.mach, aoa_deg=spec.aoa, reynolds=spec.re)
     for mesh, fs, init in [(fixture, fs_fix, g["init_U"]), (cyl, fs_cyl, None)]:
         out = []
-        for sm in (0, 5, 6):
+        for sm, cap in ((0, 0), (5, 0), (6, 0), (6, 5), (6, 24)):
             case = abi.Case([mesh], [fs], abi.FLOW_LAMINAR, abi.ADV_LUSGS, getattr(abi, f"PREC_{prec}"),
-                            cfl=c["cfl"], sweep_mode=sm, sweep_blocks_per_sm=bpsm)
+                            cfl=c["cfl"], sweep_mode=sm, sweep_blocks_per_sm=bpsm, chain_table_cap=cap)
             if init is None:
                 case.init_freestream()
             else:

@@ -53,7 +53,7 @@ class Params(C.Structure):
     _fields_ = [("flow", C.c_int), ("advance", C.c_int), ("precision", C.c_int), ("first_order", C.c_int),
                 ("cfl", C.c_double), ("sweep_mode", C.c_int), ("sweep_blocks_per_sm", C.c_int),
                 ("sweep_poll_ns", C.c_int), ("sweep_threads", C.c_int), ("sst_sequential", C.c_int),
-                ("sst_sweep_share", C.c_int), ("reserved", C.c_int * 2)]
+                ("sst_sweep_share", C.c_int), ("chain_table_cap", C.c_int), ("reserved", C.c_int * 1)]
 
 
 _lib = None
@@ -215,17 +215,20 @@ class Mesh:
         check(lib().cfd_mesh_levels(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
-    def chain_schedule(self, forward: bool, nlists: int, local: bool = False, table: bool = False) -> dict:
+    def chain_schedule(self, forward: bool, nlists: int, local: bool = False, table: bool | int = False) -> dict:
         """The binary32 sweep's chain schedule of this mesh (host only): per-list
         position ranges, (cell, register bits) per position, (neighbour, face
-        code) per slot, each slot's dependency encoding and the table size."""
+        code) per slot, each slot's dependency encoding and the table size.
+        table: False none, True a table over each block's whole range, an int
+        a table capped at that many entries per block."""
+        cap = 0 if table is False else (2**31 - 1 if table is True else int(table))
         nc = self.ncell
         hptr = np.empty(nlists + 1, np.int32)
         cells = np.empty(2 * nc, np.int32)
         rec = np.empty(8 * nc, np.int32)
         jenc = np.empty(4 * nc, np.int32)
         tbl = C.c_int()
-        check(lib().cfd_chain_schedule(self.h, int(bool(forward)), int(nlists), int(bool(local)), int(bool(table)),
+        check(lib().cfd_chain_schedule(self.h, int(bool(forward)), int(nlists), int(bool(local)), cap,
                                        _iptr(hptr), _iptr(cells), _iptr(rec), _iptr(jenc), C.byref(tbl)))
         return dict(hptr=hptr, cells=cells.reshape(-1, 2), rec=rec.reshape(-1, 4, 2), jenc=jenc.reshape(-1, 4),
                     table_entries=tbl.value)
@@ -242,14 +245,15 @@ class Case:
     def __init__(self, meshes: Sequence[Mesh], freestreams: Sequence[dict], flow: int, advance: int,
                  precision: int = PREC_FP64, cfl: float = 1.0, first_order: bool = False, stream: int | None = None,
                  sweep_mode: int = 0, sweep_blocks_per_sm: int = 0, sweep_poll_ns: int = 0, sweep_threads: int = 0,
-                 sst_sequential: bool = False, sst_sweep_share: int = 0):
+                 sst_sequential: bool = False, sst_sweep_share: int = 0, chain_table_cap: int = 0):
         self.meshes = list(meshes)
         arr = (C.c_void_p * len(meshes))(*[m.h.value for m in meshes])
         fs = (Freestream * len(meshes))(*[Freestream(f["mach"], f.get("aoa_deg", 0.0), f.get("reynolds", 1.0),
                                                      f.get("density", 1.225), f.get("pressure", 101325.0))
                                           for f in freestreams])
         p = Params(flow, advance, precision, int(first_order), float(cfl), int(sweep_mode), int(sweep_blocks_per_sm),
-                   int(sweep_poll_ns), int(sweep_threads), int(bool(sst_sequential)), int(sst_sweep_share))
+                   int(sweep_poll_ns), int(sweep_threads), int(bool(sst_sequential)), int(sst_sweep_share),
+                   int(chain_table_cap))
         h = C.c_void_p()
         check(lib().cfd_case_create(arr, len(meshes), fs, C.byref(p), C.c_void_p(stream) if stream else None,
                                     C.byref(h)))

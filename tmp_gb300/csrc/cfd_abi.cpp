@@ -393,11 +393,15 @@ void build_chain(const std::vector<int>& order, const std::vector<int>& lptr, co
 // Each slot's dependency as the sweep reads it (k_chain_static stores it in the
 // stage record): -1 none, -2 / -3 the list's previous cell / the one before
 // (kept in registers), -4 - t the block-local hand-off table's entry t (the
-// producer runs in the same block, sweep mode 6 with a table), else the cell id
-// (waited for in global memory).  Table entries are positions relative to the
-// block's first position.
+// producer runs in the same block at a position below the table's cap, sweep
+// mode 6 with a table), else the cell id (waited for in global memory).  Table
+// entries are positions relative to the block's first position; table_cap is
+// the table's entries per block (0: no table).
+// Smallest capped table worth its shared memory (entries per block).
+constexpr int kChainMinTable = 64;
+
 std::vector<int> encode_chain(const std::vector<int>& hptr, const std::vector<int2>& cells,
-                              const std::vector<int2>& rec, bool table) {
+                              const std::vector<int2>& rec, int table_cap) {
     const int nc = (int)cells.size(), nh = (int)hptr.size() - 1;
     std::vector<int> pos(nc), list(nc), jenc(4 * (size_t)nc, -1);
     for (int h = 0; h < nh; h++)
@@ -412,7 +416,8 @@ std::vector<int> encode_chain(const std::vector<int>& hptr, const std::vector<in
             if (j < 0) e = -1;
             else if (lm == 1) e = -2;
             else if (lm == 2) e = -3;
-            else if (table && list[pos[j]] / 8 == h / 8) e = -4 - (pos[j] - hptr[8 * (h / 8)]);
+            else if (table_cap > 0 && list[pos[j]] / 8 == h / 8 && pos[j] - hptr[8 * (h / 8)] < table_cap)
+                e = -4 - (pos[j] - hptr[8 * (h / 8)]);
             jenc[4 * (size_t)at + s] = e;
         }
     }
@@ -455,10 +460,24 @@ void ensure_chain(cfd_case_s* c) {
         if (local)
             for (int b = 0; b < grid; b++) tbl = std::max(tbl, hptr[k][std::min(8 * b + 8, nh)] - hptr[k][8 * b]);
     }
-    // a table that would keep the grid's blocks from being co-resident is not used
-    if (tbl > 0 && !sweep_chain_fits(grid, tbl * (int)sizeof(float4))) tbl = 0;
+    if (local && c->p.chain_table_cap > 0) tbl = std::min(tbl, c->p.chain_table_cap);
+    // A table that would keep the grid's blocks from being co-resident is capped:
+    // it then covers the first positions of each block's range (the leading
+    // lists whole), the largest count that still fits; the producers of later
+    // positions hand off through global memory only.
+    if (tbl > 0 && !sweep_chain_fits(grid, tbl * (int)sizeof(float4))) {
+        int lo = 0, hi = tbl;  // lo fits (or is 0), hi does not
+        while (hi - lo > 1) {
+            const int mid = lo + (hi - lo) / 2;
+            if (sweep_chain_fits(grid, mid * (int)sizeof(float4))) lo = mid;
+            else hi = mid;
+        }
+        tbl = lo >= kChainMinTable ? lo : 0;
+        // leaves the kernels' dynamic shared-memory limit at the chosen size
+        if (tbl > 0 && !sweep_chain_fits(grid, tbl * (int)sizeof(float4))) tbl = 0;
+    }
     for (int k = 0; k < 2; k++) {
-        const std::vector<int> jenc = encode_chain(hptr[k], cells[k], rec[k], tbl > 0);
+        const std::vector<int> jenc = encode_chain(hptr[k], cells[k], rec[k], tbl);
         if (d.chain_ptr[k]) cudaFree(d.chain_ptr[k]);
         d.chain_ptr[k] = nullptr;
         dalloc(&d.chain_ptr[k], nh + 1);
@@ -2149,9 +2168,11 @@ extern "C" int cfd_chain_schedule(cfd_mesh_t mesh, int forward, int nlists, int 
         std::vector<int2> cl, rc;
         build_chain(order, lptr, cface, lr, fwd, nlists, local != 0, hp, cl, rc);
         int tbl = 0;
-        if (local && table)
+        if (local && table > 0) {
             for (int b = 0; b < nlists / 8; b++) tbl = std::max(tbl, hp[8 * b + 8] - hp[8 * b]);
-        const std::vector<int> je = encode_chain(hp, cl, rc, tbl > 0);
+            tbl = std::min(tbl, table);
+        }
+        const std::vector<int> je = encode_chain(hp, cl, rc, tbl);
         for (int h = 0; h <= nlists; h++) hptr[h] = hp[h];
         for (int q = 0; q < nc; q++) {
             cells[2 * q] = cl[q].x;

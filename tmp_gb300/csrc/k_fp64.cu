@@ -794,9 +794,10 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
                                                        int tbl_n) {
     __shared__ __align__(16) float4 ring[kChainWarps][kChainDepth][kStageW];
     __shared__ __align__(16) float4 spec[kChainWarps][kChainDepth][4];
-    // block-local hand-off table (sweep mode 6): the increment of every cell
-    // of this block's lists, by position within the block's range; a slot
-    // whose producer runs in this block waits here instead of in global memory
+    // block-local hand-off table (sweep mode 6): the increment of each cell
+    // of this block's lists at positions [0, tbl_n) of the block's range (all
+    // of them unless the table was capped to keep the grid co-resident); a
+    // slot whose producer has an entry waits here instead of in global memory
     extern __shared__ __align__(16) float4 tbl[];
     const float GM1 = 1.4f - 1.0f;
     const int lane = threadIdx.x & 31;
@@ -931,7 +932,7 @@ __global__ void __launch_bounds__(256) k_sweep_chain32(int nh, const int* __rest
         const float r3 = __shfl_sync(mask, resf, 3);
         if (lane == 0) {
             __stcg(pub + i, make_float4(r0, r1, r2, r3));
-            if (tbl_n) {
+            if (p0 + k - b0 < tbl_n) {  // the table may cover only the block's first positions
                 volatile float* q = reinterpret_cast<volatile float*>(tbl + (p0 + k - b0));
                 q[0] = r0; q[1] = r1; q[2] = r2; q[3] = r3;
             }
