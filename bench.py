@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c3", help="workload: c3 (SST airfoil, 1.07M cells), c2, c2big, c1")
+    ap.add_argument("--aoa", type=float, default=None,
+                    help="c3 only: angle of attack in degrees (the case is named at 0, 4 and 10; default 4)")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "fp32", "mixed", "mixff"],
                     help="headline form (auto: mixff, the float-float residual with the binary32 sweeps)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU baseline sample")
@@ -513,6 +515,17 @@ def _ref_worker(args):
     return t.ncell * steps, time.perf_counter() - t0
 
 
+def workload(args):
+    """The named workload; --aoa sets C3's angle of attack."""
+    from tmp_gb300 import configs
+
+    if args.aoa is None:
+        return configs.WORKLOADS[args.config]()
+    if args.config != "c3":
+        raise SystemExit("--aoa applies to the c3 workload only")
+    return configs.c3(aoa=args.aoa)
+
+
 def run_reference(args):
     """Reference arm: the reference's CPU algorithm (C restatement, bit-exact to
     the reference's compiled serial path) on all host cores as independent
@@ -529,7 +542,7 @@ def run_reference(args):
     from oracle import grd
 
     oracle.build()
-    w = configs.WORKLOADS[args.config]()
+    w = workload(args)
     ncores = os.cpu_count() or 1
     # the reader's topology once, shared by the copies through a file
     g = w.mesh
@@ -585,7 +598,7 @@ def run_ours(args):
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     build_library()
-    w = configs.WORKLOADS[args.config]()
+    w = workload(args)
     g = w.mesh
     mesh = abi.Mesh.from_arrays(g.xy, g.edge_nodes, g.edge_cells, g.ncell, g.wall_tag, g.far_tag)
     viscous = w.flow in ("laminar", "sst")
