@@ -57,3 +57,15 @@ def test_header_constants_match_bindings():
     assert not missing, missing
     wrong = {k: (d[k], v) for k, v in pairs.items() if d[k] != v}
     assert not wrong, wrong
+
+
+def test_header_compiles_as_c_and_cxx():
+    """include/cfdgb.h is a plain C header: it compiles as C99 and as C++17
+    with every warning on, so a C, cgo or ctypes caller can include it."""
+    import subprocess
+
+    h = str(ROOT / "include" / "cfdgb.h")
+    for cmd in (["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", "c", h],
+                ["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", "c++", h]):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, (cmd[0], r.stderr)
