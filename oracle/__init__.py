@@ -57,6 +57,8 @@ def _load():
         L.orc_lusgs_step.argtypes = [vp, C.c_double, C.c_int]
         L.orc_lusgs_step.restype = C.c_int
         L.orc_wall_force.argtypes = [vp, dp]
+        L.orc_hold_limiter.argtypes = [vp, C.c_int]
+        L.orc_hold_turbulence.argtypes = [vp, C.c_int]
         L.orc_field.argtypes = [vp, C.c_int]
         L.orc_field.restype = dp
         L.orc_nodal_weights.argtypes = [C.c_long, ip, dp, dp, dp]
@@ -140,6 +142,14 @@ class Oracle:
         n = (self.m.nedge if per_face else self.m.ncell) * width
         a = np.ctypeslib.as_array(_load().orc_sst_field(self.h, fid), shape=(n,))
         return a.reshape(-1, width) if width > 1 else a
+
+    def hold_limiter(self, on: bool = True):
+        """Freeze the limiter factors at their current values (analysis only)."""
+        _load().orc_hold_limiter(self.h, int(on))
+
+    def hold_turbulence(self, on: bool = True):
+        """Freeze k, omega and mu_t in the coupled step (analysis only)."""
+        _load().orc_hold_turbulence(self.h, int(on))
 
     def wall_force(self) -> np.ndarray:
         """(Fx, Fy) through the wall faces in the last residual evaluation."""

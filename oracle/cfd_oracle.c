@@ -51,6 +51,12 @@ typedef struct {
     double density, pressure;          /* dimensional freestream */
     double sst_k, sst_w, sst_mut;       /* nondimensional freestream k, omega, mu_t */
     double *T, *Tw, *Tf, *TG, *F1, *F2, *mut, *mutf, *Tfc, *Tfv, *TR, *TD, *TdW1, *TdW;
+    /* analysis switches (no reference counterpart; off by default): limiter
+     * factors held at the values they had when phi_hold was set, and the
+     * turbulence state (k, omega, mu_t) held by skipping the model's sweeps
+     * and update in the coupled step */
+    double* phi_hold;
+    int turb_hold;
 } orc_t;
 
 static const double Gamma = 1.4;
@@ -86,7 +92,7 @@ void orc_free(orc_t* o) {
     double* p[] = {o->vol, o->cen, o->nrm, o->area, o->ecen, o->walld, o->U, o->Ue, o->grad, o->gradT, o->specc,
                    o->specv, o->R, o->dt, o->mu, o->mue, o->phi, o->UL, o->UR, o->umax, o->umin, o->W, o->Wnow,
                    o->D, o->dW1, o->dW, o->T, o->Tw, o->Tf, o->TG, o->F1, o->F2, o->mut, o->mutf, o->Tfc, o->Tfv,
-                   o->TR, o->TD, o->TdW1, o->TdW};
+                   o->TR, o->TD, o->TdW1, o->TdW, o->phi_hold};
     for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++) free(p[i]);
     free(o);
 }
@@ -428,6 +434,7 @@ int orc_residual(orc_t* o, int first_order) {
     }
     if (first_order)
         for (int i = 0; i < 4 * nc; i++) o->phi[i] = 0.0;
+    if (o->phi_hold) memcpy(o->phi, o->phi_hold, 4 * 8 * (size_t)nc);
     /* updateLeftRight + flux loop (HLLCFluxStrategy.h:35-100, HLLCFluxStrategy.cpp:4-170) */
     for (int k = 0; k < ne; k++) {
         int l = o->lr[2 * k], r = o->lr[2 * k + 1];
@@ -600,12 +607,12 @@ int orc_lusgs_step(orc_t* o, double cfl, int first_order) {
         }
         for (int m = 0; m < 4; m++) o->dW[4 * c + m] = o->dW1[4 * c + m] - s[m] / o->D[c];
     }
-    if (turb(o)) sst_step_sweeps(o);
+    if (turb(o) && !o->turb_hold) sst_step_sweeps(o);
     for (int c = 0; c < o->ncell; c++) {
         for (int m = 0; m < 4; m++) o->W[4 * c + m] = o->W[4 * c + m] + o->dW[4 * c + m];
         prim_from_cons(o->W + 4 * c, o->U + 4 * c);
     }
-    if (turb(o)) sst_step_update(o);
+    if (turb(o) && !o->turb_hold) sst_step_update(o);
     return err;
 }
 
@@ -1738,3 +1745,20 @@ void orc_holemap_check(const int* nxy, const double* geo, const int* sam, long n
         inside[i] = out ? 0 : sam[ix[1] * nxy[0] + ix[0]];
     }
 }
+
+/* Analysis switches, for separating what keeps an iteration from converging:
+ * orc_hold_limiter(o, 1) freezes the Venkatakrishnan factors at their current
+ * values (every later residual uses them; 0 releases them), and
+ * orc_hold_turbulence(o, 1) freezes k, omega and mu_t (the coupled step skips
+ * the model's sweeps and update; the flow still sees the held mu_t). */
+void orc_hold_limiter(orc_t* o, int on) {
+    if (on) {
+        if (!o->phi_hold) o->phi_hold = malloc(4 * 8 * (size_t)o->ncell);
+        if (o->phi_hold) memcpy(o->phi_hold, o->phi, 4 * 8 * (size_t)o->ncell);
+    } else {
+        free(o->phi_hold);
+        o->phi_hold = NULL;
+    }
+}
+
+void orc_hold_turbulence(orc_t* o, int on) { o->turb_hold = on != 0; }

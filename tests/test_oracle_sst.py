@@ -92,3 +92,32 @@ def test_oracle_sst_coupled_converges(built_oracle, mesh_file, ma, aoa, re, cfl,
     assert got < 1e-10
     # gcc builds on x86-64 and AArch64 round the same way (no contraction, libm's pow and tanh may differ)
     assert abs(got - fall) <= 1e-3 * fall, got
+
+
+def test_oracle_hold_switches(built_oracle):
+    """The restatement's analysis switches: held limiter factors stay as they
+    were while the state moves; a held turbulence state (k, omega, mu_t)
+    stays while the flow steps; releasing either resumes the computation."""
+    import oracle
+    from oracle import grd
+
+    topo = grd.read_grd(GOLDEN / "mixed.grd", -1, -2)
+    o = oracle.Oracle(topo, 0.3, 2.0, 1e5, True)
+    o.sst_enable(True)
+    for _ in range(5):
+        assert o.lusgs_step(5.0) == 0
+    phi0 = o.field("PHI").copy()
+    o.hold_limiter(True)
+    T0, mut0, U0 = o.sst_field("SST_T").copy(), o.sst_field("SST_MUT").copy(), o.field("U").copy()
+    o.hold_turbulence(True)
+    for _ in range(3):
+        assert o.lusgs_step(5.0) == 0
+    assert not np.array_equal(o.field("U"), U0)
+    np.testing.assert_array_equal(o.field("PHI"), phi0)
+    np.testing.assert_array_equal(o.sst_field("SST_T"), T0)
+    np.testing.assert_array_equal(o.sst_field("SST_MUT"), mut0)
+    o.hold_limiter(False)
+    o.hold_turbulence(False)
+    assert o.lusgs_step(5.0) == 0
+    assert not np.array_equal(o.field("PHI"), phi0)
+    assert not np.array_equal(o.sst_field("SST_T"), T0)
