@@ -59,6 +59,7 @@ def _load():
         L.orc_wall_force.argtypes = [vp, dp]
         L.orc_hold_limiter.argtypes = [vp, C.c_int]
         L.orc_hold_turbulence.argtypes = [vp, C.c_int]
+        L.orc_sst_production_limit.argtypes = [vp, C.c_double]
         L.orc_field.argtypes = [vp, C.c_int]
         L.orc_field.restype = dp
         L.orc_nodal_weights.argtypes = [C.c_long, ip, dp, dp, dp]
@@ -150,6 +151,11 @@ class Oracle:
     def hold_turbulence(self, on: bool = True):
         """Freeze k, omega and mu_t in the coupled step (analysis only)."""
         _load().orc_hold_turbulence(self.h, int(on))
+
+    def sst_production_limit(self, factor: float):
+        """Limit the k equation's production to factor * beta* rho k omega (0: the reference's unlimited
+        production; analysis only)."""
+        _load().orc_sst_production_limit(self.h, float(factor))
 
     def wall_force(self) -> np.ndarray:
         """(Fx, Fy) through the wall faces in the last residual evaluation."""

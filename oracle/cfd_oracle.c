@@ -57,6 +57,10 @@ typedef struct {
      * and update in the coupled step */
     double* phi_hold;
     int turb_hold;
+    /* > 0: the k equation's production limited to plim * beta* rho k omega
+     * (Menter's SST guard, absent from the reference's rans_P_Solver); 0: as
+     * the reference computes it */
+    double plim;
 } orc_t;
 
 static const double Gamma = 1.4;
@@ -788,6 +792,7 @@ static void sst_equation(orc_t* o) {
         double d1 = (uy + vx) * (uy + vx);
         double d2 = 2.0 / 3.0 * rho * k * (ux + vy);
         double P = (d0 + d1) * mt - d2;
+        if (o->plim > 0) P = dmin(P, o->plim * sst_bstar * rho * k * w);
         double q0 = P - sst_bstar * rho * k * w;
         double q1 = cw * rho * P / mt - beta * rho * w * w + 2 * (1 - f1) * rho * sst_sw2 / w * rdiv;
         if (o->coupled) { /* sum(Fc - Fv) - Q vol: the source with the sign of dW = -R/D */
@@ -1762,3 +1767,8 @@ void orc_hold_limiter(orc_t* o, int on) {
 }
 
 void orc_hold_turbulence(orc_t* o, int on) { o->turb_hold = on != 0; }
+
+/* The k equation's production limited to factor * beta* rho k omega (Menter's
+ * SST guard at stagnation points; factor 0 restores the reference's unlimited
+ * production).  Analysis only: it departs from the reference's model. */
+void orc_sst_production_limit(orc_t* o, double factor) { o->plim = factor > 0 ? factor : 0; }

@@ -121,3 +121,25 @@ def test_oracle_hold_switches(built_oracle):
     assert o.lusgs_step(5.0) == 0
     assert not np.array_equal(o.field("PHI"), phi0)
     assert not np.array_equal(o.sst_field("SST_T"), T0)
+
+
+def test_oracle_production_limit_switch(built_oracle):
+    """The analysis switch that limits the k equation's production (Menter's
+    guard, absent from the reference's model): off by default, a huge factor
+    changes nothing, a small one (1e-3, which bites everywhere) changes the
+    turbulence state."""
+    import oracle
+    from oracle import grd
+
+    topo = grd.read_grd(GOLDEN / "mixed.grd", -1, -2)
+    runs = {}
+    for factor in (0.0, 1e30, 1e-3):
+        o = oracle.Oracle(topo, 0.3, 2.0, 1e5, True)
+        o.sst_enable(True)
+        o.sst_production_limit(factor)
+        for _ in range(20):
+            assert o.lusgs_step(5.0) == 0
+        runs[factor] = (o.field("U").copy(), o.sst_field("SST_T").copy())
+    np.testing.assert_array_equal(runs[1e30][0], runs[0.0][0])
+    np.testing.assert_array_equal(runs[1e30][1], runs[0.0][1])
+    assert not np.array_equal(runs[1e-3][1], runs[0.0][1])
